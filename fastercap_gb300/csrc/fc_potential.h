@@ -1,0 +1,310 @@
+// Panel-pair potential integrals shared by the host model builder (refinement
+// criteria) and the device coefficient-fill kernels.
+//
+// Restated from the reference's collocation formulas:
+//   potential_opt        CPotential::PotentialOpt        Solver/Potential.cpp:1561-1711
+//   potential_numerical  CPotential::PotentialNumerical  Solver/Potential.cpp:2077-2153
+//   enfield_numerical    CPotential::EnFieldNumerical    Solver/Potential.cpp:2172-2254
+//   quadrature rules 2, 3, 5 of CPotential::InitNumerical Solver/Potential.cpp:112-128,133-149,181-206
+//   pot_estimate         CAutoRefine::PotEstimateOpt (one-way, collocation)
+//                                                        Solver/Autorefine.cpp:3474-3733
+//   self_potential       CAutoRefine::SelfPotential      Solver/Autorefine.cpp:2358-2427
+//   diel_normal          CAutoPanel::GetDielNormal       Solver/AutoPanel.h:114-139
+//
+// Panel vertices, centroids and normals are single precision (as the
+// reference stores them); every formula works in double. A difference of two
+// float vectors is formed in float and then widened (the rule the model
+// builder uses everywhere), a float operand meeting a double one is widened
+// first. The order of every floating-point operation follows the reference so
+// that host results are bit-reproducible (host code is compiled with
+// -ffp-contract=off).
+#ifndef FCG_POTENTIAL_H
+#define FCG_POTENTIAL_H
+
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define FCG_HD __host__ __device__ __forceinline__
+#else
+#define FCG_HD inline
+#endif
+
+// physical constants as the reference defines them (Solver/Potential.h:41-45)
+#define FCG_FOUR_PI_TIMES_E0 1.1126500559756e-10
+#define FCG_TWO_TIMES_E0 1.7708375634e-11
+#define FCG_POTENTIAL_GEO_EPS 1E-6
+#define FCG_PANEL_EPS 1E-12
+
+// element type bits (Solver/AutoElement.h:44-48)
+#define FCG_IS_LEAF 1u
+#define FCG_IS_DIEL 2u
+#define FCG_OUTPERM_NORMAL_DIR 4u
+#define FCG_OUTPERM_ELEMENT_LEVEL 8u
+#define FCG_IS_SUPER_NODE 128u
+
+struct fcg_d3 {
+    double x, y, z;
+};
+
+FCG_HD fcg_d3 fcg_mk(double x, double y, double z) { fcg_d3 r; r.x = x; r.y = y; r.z = z; return r; }
+FCG_HD fcg_d3 fcg_widen(const float *v) { return fcg_mk((double)v[0], (double)v[1], (double)v[2]); }
+// float difference a-b formed in float, then widened
+FCG_HD fcg_d3 fcg_fsub(const float *a, const float *b) {
+    float x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+    return fcg_mk((double)x, (double)y, (double)z);
+}
+FCG_HD double fcg_mod(fcg_d3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+FCG_HD double fcg_dot(fcg_d3 a, fcg_d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+FCG_HD fcg_d3 fcg_cross(fcg_d3 a, fcg_d3 b) {
+    return fcg_mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Quadrature rules in homogeneous triangle coordinates (x, y, 1) with weights.
+// rule 2: 3 points, Strang-Fix #1; rule 3: 3 points, Strang-Fix #2;
+// rule 5: 6 points, Strang-Fix #4 (the only rules the collocation scheme uses).
+FCG_HD int fcg_rule_npts(int rule) { return rule == 5 ? 6 : 3; }
+FCG_HD void fcg_rule_point(int rule, int i, double *px, double *py, double *w) {
+    if (rule == 2) {
+        const double a = 1.0 / 6.0, c = 4.0 / 6.0;
+        *px = (i == 0) ? c : a;
+        *py = (i == 1) ? c : a;
+        *w = 1.0 / 3.0;
+    } else if (rule == 3) {
+        *px = (i == 0) ? 0.0 : 0.5;
+        *py = (i == 1) ? 0.0 : 0.5;
+        *w = 1.0 / 3.0;
+    } else {
+        const double a = 0.659027622374092, b = 0.231933368553031, c = 0.109039009072877;
+        const double xs[6] = {a, a, b, b, c, c};
+        const double ys[6] = {b, c, a, c, a, b};
+        *px = xs[i];
+        *py = ys[i];
+        *w = 1.0 / 6.0;
+    }
+}
+
+// Analytic potential at r of a uniform unit charge density on the triangle v
+// (9 floats), divided by the triangle area.
+FCG_HD double fcg_potential_opt(fcg_d3 r, const float *v) {
+    fcg_d3 side[3], rhomp, Pmp[3], Rmp[3], n, rho, l, u;
+    double Rmp_norm[3];
+    side[0] = fcg_fsub(v + 3, v + 0);
+    side[1] = fcg_fsub(v + 6, v + 3);
+    side[2] = fcg_fsub(v + 0, v + 6);
+    n = fcg_cross(side[0], side[1]);
+    double nmod = fcg_mod(n);
+    n.x = n.x / nmod;
+    n.y = n.y / nmod;
+    n.z = n.z / nmod;
+    double nr = fcg_dot(n, r);
+    rho.x = r.x - n.x * nr;
+    rho.y = r.y - n.y * nr;
+    rho.z = r.z - n.z * nr;
+    for (int i = 0; i < 3; i++) {
+        fcg_d3 vi = fcg_widen(v + 3 * i);
+        double nv = fcg_dot(n, vi);
+        rhomp.x = vi.x - n.x * nv;
+        rhomp.y = vi.y - n.y * nv;
+        rhomp.z = vi.z - n.z * nv;
+        Pmp[i].x = rhomp.x - rho.x;
+        Pmp[i].y = rhomp.y - rho.y;
+        Pmp[i].z = rhomp.z - rho.z;
+        Rmp[i].x = vi.x - r.x;
+        Rmp[i].y = vi.y - r.y;
+        Rmp[i].z = vi.z - r.z;
+        Rmp_norm[i] = fcg_mod(Rmp[i]);
+    }
+    double d = -fcg_dot(n, Rmp[0]);
+    double dnorm = fabs(d);
+    double result = 0.0;
+    for (int i = 0; i < 3; i++) {
+        int j = (i == 2) ? 0 : i + 1;
+        double ms = fcg_mod(side[i]);
+        l.x = side[i].x / ms;
+        l.y = side[i].y / ms;
+        l.z = side[i].z / ms;
+        u.x = l.y * n.z - l.z * n.y;
+        u.y = l.z * n.x - l.x * n.z;
+        u.z = l.x * n.y - l.y * n.x;
+        double P0signed = fcg_dot(Pmp[j], u);
+        double P0 = fabs(P0signed);
+        double lplus = fcg_dot(Pmp[j], l);
+        double lminus = fcg_dot(Pmp[i], l);
+        double R0 = sqrt(P0 * P0 + d * d);
+        double lplusabs = fabs(lplus), lminusabs = fabs(lminus);
+        // the reference compares the signed values here
+        double lmax = (lplus > lminus) ? lplusabs : lminusabs;
+        if (P0 / lmax > FCG_POTENTIAL_GEO_EPS && fabs((Rmp_norm[j] + lplus) / lmax) > FCG_POTENTIAL_GEO_EPS &&
+            fabs((Rmp_norm[i] + lminus) / lmax) > FCG_POTENTIAL_GEO_EPS) {
+            double R0square = R0 * R0;
+            double tan1 = atan(P0 * lplus / (R0square + dnorm * Rmp_norm[j]));
+            double tan2 = atan(P0 * lminus / (R0square + dnorm * Rmp_norm[i]));
+            double ln = log((Rmp_norm[j] + lplus) / (Rmp_norm[i] + lminus));
+            double P0sign = (double)((P0signed > 0) - (P0signed < 0));
+            result += P0sign * (P0 * ln - dnorm * (tan1 - tan2));
+        }
+    }
+    return (result * 2.0) / nmod;
+}
+
+// Local 2D frame of a source triangle for the quadrature formulas.
+struct fcg_quad_frame {
+    fcg_d3 x, y, v0;
+    double vert2d01, vert2d02, vert2d12, jacobian, area;
+};
+
+FCG_HD fcg_quad_frame fcg_frame(const float *v) {
+    fcg_quad_frame f;
+    fcg_d3 side1 = fcg_fsub(v + 3, v + 0);
+    fcg_d3 side2 = fcg_fsub(v + 6, v + 3);
+    fcg_d3 side3 = fcg_fsub(v + 0, v + 6);
+    fcg_d3 normal, z;
+    normal.x = side1.y * side2.z - side1.z * side2.y;
+    normal.y = -side1.x * side2.z + side1.z * side2.x;
+    normal.z = side1.x * side2.y - side1.y * side2.x;
+    double mn = fcg_mod(normal);
+    z.x = normal.x / mn;
+    z.y = normal.y / mn;
+    z.z = normal.z / mn;
+    double m1 = fcg_mod(side1);
+    f.x.x = side1.x / m1;
+    f.x.y = side1.y / m1;
+    f.x.z = side1.z / m1;
+    f.y.x = f.x.y * z.z - f.x.z * z.y;
+    f.y.y = f.x.z * z.x - f.x.x * z.z;
+    f.y.z = f.x.x * z.y - f.x.y * z.x;
+    f.vert2d01 = m1;
+    f.vert2d02 = -(side3.x * f.x.x + side3.y * f.x.y + side3.z * f.x.z);
+    f.vert2d12 = -(side3.x * f.y.x + side3.y * f.y.y + side3.z * f.y.z);
+    f.jacobian = (f.vert2d02 - f.vert2d01) * f.vert2d12 - f.vert2d12 * f.vert2d02;
+    f.area = mn / 2.0;
+    f.v0 = fcg_widen(v);
+    return f;
+}
+
+FCG_HD fcg_d3 fcg_frame_point(const fcg_quad_frame &f, double px, double py) {
+    // homogeneous third coordinate is 1
+    double point0 = (f.vert2d01 - f.vert2d02) * px + f.vert2d02 * (1.0 - py);
+    double point1 = f.vert2d12 * (1.0 - px - py);
+    fcg_d3 p;
+    p.x = f.v0.x + f.x.x * point0 + f.y.x * point1;
+    p.y = f.v0.y + f.x.y * point0 + f.y.y * point1;
+    p.z = f.v0.z + f.x.z * point0 + f.y.z * point1;
+    return p;
+}
+
+// Quadrature of 1/|p - r| over the triangle, divided by its area.
+FCG_HD double fcg_potential_numerical(fcg_d3 r, const float *v, int rule) {
+    fcg_quad_frame f = fcg_frame(v);
+    double result = 0.0;
+    int np = fcg_rule_npts(rule);
+    for (int i = 0; i < np; i++) {
+        double px, py, w;
+        fcg_rule_point(rule, i, &px, &py, &w);
+        fcg_d3 p = fcg_frame_point(f, px, py);
+        fcg_d3 dd = fcg_mk(p.x - r.x, p.y - r.y, p.z - r.z);
+        double pot = 1 / fcg_mod(dd);
+        result += w * pot;
+    }
+    result *= f.jacobian / 2.0;
+    result /= f.area;
+    return result;
+}
+
+// Quadrature of (r - p).n / |r - p|^3 over the triangle, divided by its area.
+FCG_HD double fcg_enfield_numerical(fcg_d3 r, const float *v, fcg_d3 tn, int rule) {
+    fcg_quad_frame f = fcg_frame(v);
+    double result = 0.0;
+    int np = fcg_rule_npts(rule);
+    for (int i = 0; i < np; i++) {
+        double px, py, w;
+        fcg_rule_point(rule, i, &px, &py, &w);
+        fcg_d3 p = fcg_frame_point(f, px, py);
+        fcg_d3 dist = fcg_mk(r.x - p.x, r.y - p.y, r.z - p.z);
+        double rd = fcg_mod(dist);
+        double pot = fcg_dot(dist, tn) / (rd * rd * rd);
+        result += w * pot;
+    }
+    result *= f.jacobian / 2.0;
+    result /= f.area;
+    return result;
+}
+
+// Unit normal pointing to the outer-permittivity side of a dielectric element.
+// Super nodes store an area-weighted, unnormalised normal.
+FCG_HD fcg_d3 fcg_diel_normal(unsigned type, const float *normal) {
+    fcg_d3 u;
+    if (type & FCG_IS_SUPER_NODE) {
+        fcg_d3 n = fcg_widen(normal);
+        double m = fcg_mod(n);
+        if (m < FCG_PANEL_EPS) u = fcg_mk(0.0, 0.0, 0.0);
+        else u = fcg_mk(n.x / m, n.y / m, n.z / m);
+    } else {
+        u = fcg_widen(normal);
+    }
+    if ((type & FCG_OUTPERM_NORMAL_DIR) != FCG_OUTPERM_NORMAL_DIR) {
+        u.x = -u.x;
+        u.y = -u.y;
+        u.z = -u.z;
+    }
+    return u;
+}
+
+// Distance band of a panel pair: 0 analytic (rho < 1), 1 rule 5 (rho < 2),
+// 2 rule 3 (rho < 4), 3 rule 2 (rho < 10), 4 point formula.
+FCG_HD int fcg_band(double rdist, double rmax) {
+    double rho = rdist / rmax;
+    if (rho < 1.0) return 0;
+    if (rho < 2.0) return 1;
+    if (rho < 4.0) return 2;
+    if (rho < 10.0) return 3;
+    return 4;
+}
+
+// Coefficient of potential (conductor evaluation element) or of normal
+// electric field (dielectric evaluation element) at element 1's centroid due
+// to a unit charge spread over element 2.
+FCG_HD double fcg_pot_estimate(unsigned type1, const float *c1, const float *n1, double maxside1,
+                               const float *c2, const float *v2, double maxside2) {
+    fcg_d3 dist = fcg_fsub(c1, c2);
+    double rdist = fcg_mod(dist);
+    double rmax = (maxside1 > maxside2) ? maxside1 : maxside2;
+    int band = fcg_band(rdist, rmax);
+    fcg_d3 r1 = fcg_widen(c1);
+    if ((type1 & FCG_IS_DIEL) != FCG_IS_DIEL) {
+        switch (band) {
+        case 0: return fcg_potential_opt(r1, v2) / FCG_FOUR_PI_TIMES_E0;
+        case 1: return fcg_potential_numerical(r1, v2, 5) / FCG_FOUR_PI_TIMES_E0;
+        case 2: return fcg_potential_numerical(r1, v2, 3) / FCG_FOUR_PI_TIMES_E0;
+        case 3: return fcg_potential_numerical(r1, v2, 2) / FCG_FOUR_PI_TIMES_E0;
+        default: return 1 / (FCG_FOUR_PI_TIMES_E0 * rdist);
+        }
+    }
+    fcg_d3 nrm = fcg_diel_normal(type1, n1);
+    switch (band) {
+    case 0: {
+        // central difference of the analytic potential across the panel
+        double h = rdist / 20;
+        fcg_d3 ep = fcg_mk(r1.x + nrm.x * h, r1.y + nrm.y * h, r1.z + nrm.z * h);
+        fcg_d3 em = fcg_mk(r1.x - nrm.x * h, r1.y - nrm.y * h, r1.z - nrm.z * h);
+        double pp = fcg_potential_opt(ep, v2);
+        double pn = fcg_potential_opt(em, v2);
+        return (pn - pp) / (2 * h * FCG_FOUR_PI_TIMES_E0);
+    }
+    case 1: return fcg_enfield_numerical(r1, v2, nrm, 5) / FCG_FOUR_PI_TIMES_E0;
+    case 2: return fcg_enfield_numerical(r1, v2, nrm, 3) / FCG_FOUR_PI_TIMES_E0;
+    case 3: return fcg_enfield_numerical(r1, v2, nrm, 2) / FCG_FOUR_PI_TIMES_E0;
+    default: return fcg_dot(dist, nrm) / (FCG_FOUR_PI_TIMES_E0 * rdist * rdist * rdist);
+    }
+}
+
+// Self coefficient of a leaf panel: collocated analytic potential for a
+// conductor panel, field-discontinuity term for a dielectric panel with
+// permittivities eb (outer side) and ea (inner side).
+FCG_HD double fcg_self_potential(unsigned type, const float *c, const float *v, double area, double eb, double ea) {
+    if (type & FCG_IS_DIEL) return (ea + eb) / (FCG_TWO_TIMES_E0 * (eb - ea) * area);
+    return fcg_potential_opt(fcg_widen(c), v) / FCG_FOUR_PI_TIMES_E0;
+}
+
+#endif

@@ -1,0 +1,959 @@
+// Host model builder: FastCap-format input -> panel hierarchy -> adaptive mesh
+// -> interaction links -> flattened SoA model.
+//
+// The steps restate the reference's model construction so that the panel,
+// node and link sets (and the order of links inside every node's row) are the
+// same as the reference's:
+//   parse_file          CAutoRefine::Parse3DInputFile   Solver/Autorefine.cpp:4746-5568
+//   create_panel        CAutoRefine::CreatePanel        Solver/Autorefine.cpp:5990-6083
+//                       CAutoPanel::CalcPanelGeomPar    Solver/AutoPanel.cpp:51-104
+//   get_conductor       CAutoRefine::GetConductor       Solver/Autorefine.cpp:6279-6365
+//   build_super         CAutoRefine::BuildSuperHierarchy / RecurBuild3DSuperHier
+//                                                       Solver/Autorefine.cpp:6410-6629
+//   make_super          CAutoPanel::MakeSuperPanel      Solver/AutoPanel.cpp:209-379
+//   subdivide           CAutoPanel::Subdivide           Solver/AutoPanel.cpp:382-523
+//   discretize_*        CAutoRefine::DiscretizeMutual/Self Solver/Autorefine.cpp:2638-2795
+//   refine_criteria     CAutoRefine::RefineCriteria     Solver/Autorefine.cpp:2928-3003
+//   refine_mutual/self  CAutoRefine::RefineMutual/RefineSelf Solver/Autorefine.cpp:3096-3235, 2115-2229
+//   flatten             CAutoRefine::RecurseIndex       Solver/Autorefine.cpp:1173-1220
+// Elements live in one index-addressed array instead of a pointer tree; the
+// links are emitted once as (node, node) pairs in traversal order and bucketed
+// by destination with a stable counting sort, which yields the reference's row
+// order without its separate counting pass.
+//
+// Floating-point rules (kept identical everywhere): panel geometry is float; a
+// difference or sum of two float vectors is formed in float; an operation that
+// meets a double operand, and every modulus / dot / cross product, is done in
+// double; a double result stored into panel geometry is rounded to float.
+#include "model.hpp"
+
+#include <deque>
+#include <map>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <unistd.h>
+
+#include "../csrc/fc_potential.h"
+
+namespace fcg {
+namespace {
+
+const double kCosMin = 0.99619469809174553229501040247389;  // 5 degrees
+const double kQuadSideTol = 0.2;
+const double kQuadAngleTol = 0.1;
+const double kRelDielTol = 0.001;
+const double k2DivFourthRoot27 = 0.87738267530166164054614593453133;
+const double k2DivFourthRoot3 = 1.5196713713031850946623755013091;
+const double kMinus05PlusSqr2Div4 = -0.14644660940672623779957781894758;
+const double k05PlusSqr2Div4 = 0.85355339059327376220042218105242;
+const double kSqr2 = 1.4142135623730950488016887242097;
+const int kMaxParseLevel = 128;
+const int kMaxDepth = 4096;
+const int kMaxLineLen = 512;
+
+struct D3 {
+    double x, y, z;
+    double &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    double operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+inline D3 d3(double x, double y, double z) { D3 r = {x, y, z}; return r; }
+inline D3 widen(const float *v) { return d3(v[0], v[1], v[2]); }
+inline D3 fsub(const float *a, const float *b) {
+    float x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+    return d3(x, y, z);
+}
+inline D3 sub(D3 a, D3 b) { return d3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline D3 add(D3 a, D3 b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline D3 scale(D3 a, double s) { return d3(a.x * s, a.y * s, a.z * s); }
+inline D3 divs(D3 a, double s) { return d3(a.x / s, a.y / s, a.z / s); }
+inline double mod(D3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 cross(D3 a, D3 b) { return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline void store(float *dst, D3 a) { dst[0] = (float)a.x; dst[1] = (float)a.y; dst[2] = (float)a.z; }
+inline void normalize(D3 &a) { double m = mod(a); a.x /= m; a.y /= m; a.z /= m; }
+
+// One physical input file, split the way fgets() with a 512-byte buffer splits
+// it; `eof` marks a final chunk without a newline (the reference's read loop
+// stops before processing such a chunk).
+struct InFile {
+    std::vector<std::string> lines;
+    std::vector<bool> eof;
+    std::map<std::string, size_t> sub;  // "File <name>" sections -> first line index
+};
+
+struct Builder {
+    BuildOptions opt;
+    std::vector<Element> el;
+    std::vector<Conductor> conds;
+    std::deque<int> order;  // solver order of conductors
+    std::deque<InFile> files;
+    int parse_level = -1;
+    int group_num[kMaxParseLevel + 2];
+    long group_diel_num = 0;
+    int64_t input_panels = 0, raw_cond = 0, raw_diel = 0;
+    double max_area = 0, max_side = 0, total_area = 0, max_mesh_eps = 0;
+    double eps = 0, mesh_eps = 0, mesh_curv = 3.0;
+    int level = 0, max_level = 0;
+    bool warned_thin = false, warned_skew = false, warned_tri = false;
+    std::string err;
+    std::vector<std::string> warnings;
+    std::vector<std::pair<int32_t, int32_t>> pairs;
+
+    void warn(const std::string &w) {
+        warnings.push_back(w);
+        if (opt.verbose) fprintf(stderr, "%s\n", w.c_str());
+    }
+
+    // ---------------------------------------------------------------- files
+    int load_file(const std::string &name, InFile *&out) {
+        FILE *f = fopen(name.c_str(), "rb");
+        if (!f) { err = "cannot open file '" + name + "'"; return FC_CANNOT_OPEN_FILE; }
+        files.push_back(InFile());
+        InFile &F = files.back();
+        char buf[kMaxLineLen];
+        while (fgets(buf, kMaxLineLen, f)) {
+            F.lines.push_back(buf);
+            size_t n = strlen(buf);
+            bool nl = n > 0 && buf[n - 1] == '\n';
+            F.eof.push_back(!nl && feof(f));
+        }
+        fclose(f);
+        for (size_t i = 0; i < F.lines.size(); i++) {
+            if (F.lines[i][0] == 'F') {
+                char t1[kMaxLineLen], t2[kMaxLineLen];
+                if (sscanf(F.lines[i].c_str(), "%s %s", t1, t2) == 2) F.sub.insert(std::make_pair(std::string(t2), i + 1));
+            }
+        }
+        out = &F;
+        return FC_NORMAL_END;
+    }
+
+    // ----------------------------------------------------------- conductors
+    int find_cond(const std::string &name) {
+        for (size_t i = 0; i < order.size(); i++)
+            if (conds[order[i]].name == name) return (int)i;
+        return -1;
+    }
+
+    int get_conductor(const std::string &name, bool isdiel, double outperm, double inperm, const double *ref, uint8_t *diel_index) {
+        int pos = find_cond(name);
+        int id;
+        if (pos < 0) {
+            Conductor c;
+            c.name = name;
+            c.is_diel = isdiel;
+            c.outperm = outperm;
+            if (isdiel) {
+                c.inperm = inperm;
+                c.ref[0] = ref[0]; c.ref[1] = ref[1]; c.ref[2] = ref[2];
+            }
+            conds.push_back(c);
+            id = (int)conds.size() - 1;
+            if (isdiel) order.push_front(id);
+            else order.push_back(id);
+        } else {
+            id = order[pos];
+        }
+        if (!isdiel) {
+            Conductor &c = conds[id];
+            size_t k;
+            for (k = 0; k < c.surf_outperm.size(); k++)
+                if (c.surf_outperm[k] == outperm) break;
+            if (k == c.surf_outperm.size()) {
+                if (c.surf_outperm.size() < 255) c.surf_outperm.push_back(outperm);
+                else { k--; warn("maximum number of permittivities around conductor " + c.name + " reached"); }
+            }
+            *diel_index = (uint8_t)k;
+        }
+        return id;
+    }
+
+    // -------------------------------------------------------------- panels
+    static uint8_t max_side3(Element &e, double l0, double l1, double l2) {
+        if (l0 >= l1 && l0 >= l2) { e.maxside_idx = 0; e.maxside = l0; }
+        else if (l1 >= l0 && l1 >= l2) { e.maxside_idx = 1; e.maxside = l1; }
+        else { e.maxside_idx = 2; e.maxside = l2; }
+        return e.maxside_idx;
+    }
+
+    // Newell normal of the triangle accumulated in float; returns its modulus
+    static double newell_normal(const float *v, float *n) {
+        n[0] = n[1] = n[2] = 0.0f;
+        for (int i = 0; i < 3; i++) {
+            int j = i + 1 > 2 ? 0 : i + 1;
+            const float *a = v + 3 * i, *b = v + 3 * j;
+            n[0] += (a[1] - b[1]) * (a[2] + b[2]);
+            n[1] += (a[2] - b[2]) * (a[0] + b[0]);
+            n[2] += (a[0] - b[0]) * (a[1] + b[1]);
+        }
+        double m = mod(widen(n));
+        if (m > FCG_PANEL_EPS) {
+            n[0] = (float)(n[0] / m); n[1] = (float)(n[1] / m); n[2] = (float)(n[2] / m);
+        }
+        return m;
+    }
+
+    static void centroid3(Element &e) {
+        float sx = e.v[0] + e.v[3], sy = e.v[1] + e.v[4], sz = e.v[2] + e.v[5];
+        sx = sx + e.v[6]; sy = sy + e.v[7]; sz = sz + e.v[8];
+        e.c[0] = (float)(sx / 3.0); e.c[1] = (float)(sy / 3.0); e.c[2] = (float)(sz / 3.0);
+    }
+
+    // returns the cosine of the smallest angle
+    static double geom_par(Element &e) {
+        double sl[3];
+        sl[0] = mod(fsub(e.v + 3, e.v + 0));
+        sl[1] = mod(fsub(e.v + 6, e.v + 3));
+        sl[2] = mod(fsub(e.v + 0, e.v + 6));
+        double nm = newell_normal(e.v, e.n);
+        e.area = nm / 2.0;
+        centroid3(e);
+        uint8_t b;
+        double l0 = sl[0], l1 = sl[1], l2 = sl[2];
+        uint8_t minside;
+        if (l0 >= l1 && l0 >= l2) { e.maxside_idx = 0; e.maxside = l0; minside = (l1 >= l2) ? 2 : 1; }
+        else if (l1 >= l0 && l1 >= l2) { e.maxside_idx = 1; e.maxside = l1; minside = (l0 >= l2) ? 2 : 0; }
+        else { e.maxside_idx = 2; e.maxside = l2; minside = (l0 >= l1) ? 1 : 0; }
+        b = minside;
+        int a, c;
+        if (b == 0) { a = 2; c = 1; }
+        else if (b == 1) { a = 0; c = 2; }
+        else { a = 1; c = 0; }
+        return (sl[a] * sl[a] + sl[c] * sl[c] - sl[b] * sl[b]) / (2.0 * sl[a] * sl[c]);
+    }
+
+    int create_panel(const float *vtx, int cond, uint8_t diel_index, bool uselocal, const double *localref, bool triangulated) {
+        Element e;
+        memcpy(e.v, vtx, sizeof(e.v));
+        double cosmin = geom_par(e);
+        Conductor &C = conds[cond];
+        if (C.is_diel) {
+            const double *ref = uselocal ? localref : C.ref;
+            D3 r = d3(ref[0] - (double)e.v[0], ref[1] - (double)e.v[1], ref[2] - (double)e.v[2]);
+            float tmpref = (float)dot(r, widen(e.n));
+            if (uselocal) e.type |= FCG_OUTPERM_ELEMENT_LEVEL;
+            if (tmpref > 0) e.type |= (FCG_IS_DIEL | FCG_OUTPERM_NORMAL_DIR);
+            else e.type |= FCG_IS_DIEL;
+        } else {
+            e.diel = diel_index;
+        }
+        if (cosmin >= kCosMin && !warned_thin) {
+            warned_thin = true;
+            warn(std::string("thin triangles (min angle less than 5 degrees) ") +
+                 (triangulated ? "created in the triangulation of a quadrilateral panel" : "found in the input file"));
+        }
+        el.push_back(e);
+        input_panels++;
+        C.panels.push_back((int32_t)el.size() - 1);
+        return FC_NORMAL_END;
+    }
+
+    int create_tri(const D3 &a, const D3 &b, const D3 &c, int cond, uint8_t di, bool ul, const double *lr) {
+        float v[9];
+        store(v, a); store(v + 3, b); store(v + 6, c);
+        return create_panel(v, cond, di, ul, lr, true);
+    }
+
+    // Quadrilateral handling: plane, planarity test, split into triangles.
+    int quad_panel(D3 q[4], int cond, uint8_t di, bool ul, const double *lr) {
+        D3 nrm = d3(0, 0, 0), avg = d3(0, 0, 0);
+        for (int i = 0; i < 4; i++) {
+            int j = (i + 1) % 4;
+            nrm.x += (q[i].y - q[j].y) * (q[i].z + q[j].z);
+            nrm.y += (q[i].z - q[j].z) * (q[i].x + q[j].x);
+            nrm.z += (q[i].x - q[j].x) * (q[i].y + q[j].y);
+            avg = add(avg, q[i]);
+        }
+        double m = mod(nrm);
+        nrm = divs(nrm, m);
+        avg = divs(avg, 4.0);
+        double pd = -dot(nrm, avg);
+        bool planar = true;
+        for (int i = 0; i < 4; i++) {
+            double dist = dot(nrm, q[i]) + pd;
+            if (fabs(dist) > FCG_PANEL_EPS) {
+                if (!warned_skew) {
+                    warned_skew = true;
+                    warn("non-planar quadrilateral panels found in the input file; splitting into two triangles along the smaller diagonal");
+                }
+                if (opt.verbose) { planar = false; break; }
+            }
+        }
+        if (!planar) return split_diag(q, cond, di, ul, lr);
+
+        D3 sides[4];
+        double ds[4];
+        for (int i = 0; i < 4; i++) { sides[i] = sub(q[(i + 1) % 4], q[i]); ds[i] = mod(sides[i]); }
+        double cosangle = dot(sides[0], sides[1]) / (ds[0] * ds[1]);
+        if (fabs(ds[2] - ds[0]) < ds[0] * kQuadSideTol && fabs(ds[3] - ds[1]) < ds[1] * kQuadSideTol && fabs(cosangle) < kQuadAngleTol) {
+            if (ds[0] < ds[1]) {
+                D3 t = q[0]; q[0] = q[1]; q[1] = q[2]; q[2] = q[3]; q[3] = t;
+                t = sides[0]; sides[0] = sides[1]; sides[1] = sides[2]; sides[2] = sides[3]; sides[3] = t;
+                double tm = ds[0]; ds[0] = ds[1]; ds[1] = ds[2]; ds[2] = ds[3]; ds[3] = tm;
+            }
+            long numsegs = (long)(ds[0] / (ds[1] * 5.0) + 0.5);
+            if (numsegs == 0) numsegs = 1;
+            D3 nodes[4];
+            nodes[0] = q[0];
+            nodes[3] = q[3];
+            D3 span01 = divs(sides[0], (double)numsegs);
+            D3 span32 = divs(d3(-sides[2].x, -sides[2].y, -sides[2].z), (double)numsegs);
+            int ret;
+            for (long i = 0; i < numsegs - 1; i++) {
+                nodes[1] = add(nodes[0], span01);
+                nodes[2] = add(nodes[3], span32);
+                if ((ret = create_tri(nodes[0], nodes[1], nodes[2], cond, di, ul, lr)) != FC_NORMAL_END) return ret;
+                if ((ret = create_tri(nodes[0], nodes[2], nodes[3], cond, di, ul, lr)) != FC_NORMAL_END) return ret;
+                nodes[0] = nodes[1];
+                nodes[3] = nodes[2];
+            }
+            nodes[1] = q[1];
+            nodes[2] = q[2];
+            if ((ret = create_tri(nodes[0], nodes[1], nodes[2], cond, di, ul, lr)) != FC_NORMAL_END) return ret;
+            return create_tri(nodes[0], nodes[2], nodes[3], cond, di, ul, lr);
+        }
+        // The reference runs a constrained quality Delaunay triangulation here;
+        // this builder splits the quadrilateral along its shorter diagonal.
+        if (!warned_tri) {
+            warned_tri = true;
+            warn("quadrilateral far from a rectangle: split along the shorter diagonal (no quality triangulation)");
+        }
+        return split_diag(q, cond, di, ul, lr);
+    }
+
+    int split_diag(D3 q[4], int cond, uint8_t di, bool ul, const double *lr) {
+        double diag1 = mod(sub(q[2], q[0])), diag2 = mod(sub(q[3], q[1]));
+        int ret;
+        if (diag1 <= diag2) {
+            if ((ret = create_tri(q[0], q[1], q[2], cond, di, ul, lr)) != FC_NORMAL_END) return ret;
+            return create_tri(q[2], q[3], q[0], cond, di, ul, lr);
+        }
+        if ((ret = create_tri(q[0], q[1], q[3], cond, di, ul, lr)) != FC_NORMAL_END) return ret;
+        return create_tri(q[1], q[2], q[3], cond, di, ul, lr);
+    }
+
+    // ---------------------------------------------------------------- parser
+    // reads a permittivity "re[-jim|+jim]"; complex values are rejected
+    bool read_perm(const char *&point, float &re) {
+        int skip = 0;
+        sscanf(point, "%f%n", &re, &skip);
+        point += skip;
+        float im;
+        if (sscanf(point, " - j %f%n", &im, &skip) == 1 || sscanf(point, " + j %f%n", &im, &skip) == 1) {
+            err = "complex permittivities are not supported by this solver";
+            return false;
+        }
+        return true;
+    }
+
+    int parse_file(const std::string &fname, InFile *parent, bool isdiel, D3 offset, double outperm,
+                   const std::string &groupname, double inperm, D3 dielref) {
+        parse_level++;
+        if (parse_level >= kMaxParseLevel) { err = "input file nesting too deep"; return FC_FILE_ERROR; }
+        InFile *F = NULL;
+        size_t li = 0;
+        if (parent && parent->sub.count(fname)) {
+            F = parent;
+            li = parent->sub[fname];
+        } else {
+            int r = load_file(fname, F);
+            if (r != FC_NORMAL_END) return r;
+        }
+        int ret = FC_NORMAL_END;
+        for (; li < F->lines.size(); li++) {
+            if (F->eof[li]) break;
+            const char *line = F->lines[li].c_str();
+            char c0 = line[0];
+            if (c0 == 'E' || c0 == 'e' || c0 == 'F' || c0 == 'f') break;
+            char name[kMaxLineLen], tmpname[kMaxLineLen];
+            int skip = 0;
+            if (c0 == 'C') {
+                const char *point = line + 1;
+                sscanf(point, "%s%n", name, &skip);
+                point += skip;
+                float perm;
+                if (!read_perm(point, perm)) { ret = FC_FILE_ERROR; break; }
+                float x = 0, y = 0, z = 0;
+                sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+                D3 loff = add(d3(x, y, z), offset);
+                point += skip;
+                std::string lgroup = (parse_level == 0) ? std::string("g") : groupname;
+                char num[32];
+                snprintf(num, sizeof num, "%d_", group_num[parse_level]);
+                lgroup += num;
+                tmpname[0] = '\0';
+                sscanf(point, "%s%n", tmpname, &skip);
+                if (tmpname[0] != '+') group_num[parse_level]++;
+                group_num[parse_level + 1] = 1;
+                InFile *mapsrc = F;
+                ret = parse_file(name, mapsrc, false, loff, (double)perm, lgroup, 0.0, d3(0, 0, 0));
+                if (ret != FC_NORMAL_END) break;
+            } else if (c0 == 'D') {
+                const char *point = line + 1;
+                sscanf(point, "%s%n", name, &skip);
+                point += skip;
+                float out, in;
+                if (!read_perm(point, out) || !read_perm(point, in)) { ret = FC_FILE_ERROR; break; }
+                float x = 0, y = 0, z = 0;
+                sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+                D3 loff = add(d3(x, y, z), offset);
+                point += skip;
+                sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+                D3 lref = add(d3(x, y, z), offset);
+                point += skip;
+                tmpname[0] = '\0';
+                sscanf(point, "%s%n", tmpname, &skip);
+                if (tmpname[0] == '-') { float t = out; out = in; in = t; }
+                bool dummy = (in <= 0.0 || out <= 0.0) || (fabs(in - out) / in < kRelDielTol);
+                if (dummy) {
+                    warn("dummy dielectric-dielectric interface found in the input file, skipping");
+                } else {
+                    char g[64];
+                    snprintf(g, sizeof g, "diel%ld", group_diel_num);
+                    group_diel_num++;
+                    ret = parse_file(name, F, true, loff, (double)out, g, (double)in, lref);
+                    if (ret != FC_NORMAL_END) break;
+                }
+            } else if (c0 == 'T' || c0 == 'Q') {
+                int nv = (c0 == 'T') ? 3 : 4;
+                const char *point = line + 1;
+                sscanf(point, "%s%n", tmpname, &skip);
+                point += skip;
+                float fv[12];
+                D3 qv[4];
+                for (int i = 0; i < nv; i++) {
+                    float x = 0, y = 0, z = 0;
+                    sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+                    if (nv == 3) {
+                        fv[3 * i] = (float)((double)x + offset.x);
+                        fv[3 * i + 1] = (float)((double)y + offset.y);
+                        fv[3 * i + 2] = (float)((double)z + offset.z);
+                    } else {
+                        qv[i] = add(d3(x, y, z), offset);
+                    }
+                    point += skip;
+                }
+                float x, y, z;
+                double lref[3] = {0, 0, 0};
+                bool uselocal = false;
+                if (sscanf(point, "%f%f%f%n", &x, &y, &z, &skip) == 3) {
+                    lref[0] = (double)x + offset.x; lref[1] = (double)y + offset.y; lref[2] = (double)z + offset.z;
+                    uselocal = true;
+                }
+                std::string cname = groupname;
+                if (!isdiel) cname += tmpname;
+                double refp[3] = {dielref.x, dielref.y, dielref.z};
+                if (nv == 4) {
+                    // degenerate (collinear) quadrilaterals are skipped before any conductor is created
+                    D3 nrm = d3(0, 0, 0);
+                    for (int i = 0; i < 4; i++) {
+                        int j = (i + 1) % 4;
+                        nrm.x += (qv[i].y - qv[j].y) * (qv[i].z + qv[j].z);
+                        nrm.y += (qv[i].z - qv[j].z) * (qv[i].x + qv[j].x);
+                        nrm.z += (qv[i].x - qv[j].x) * (qv[i].y + qv[j].y);
+                    }
+                    if (mod(nrm) < 1e-300) {
+                        warn("degenerate quadrilateral panel 'Q' found (co-linear vertexes), skipping");
+                        if (isdiel) raw_diel++; else raw_cond++;
+                        continue;
+                    }
+                }
+                uint8_t di = 0;
+                int cond = get_conductor(cname, isdiel, outperm, inperm, refp, &di);
+                if (nv == 3) ret = create_panel(fv, cond, di, uselocal, lref, false);
+                else ret = quad_panel(qv, cond, di, uselocal, lref);
+                if (ret != FC_NORMAL_END) break;
+                if (isdiel) raw_diel++; else raw_cond++;
+            } else if (c0 == 'N') {
+                if (!isdiel) {
+                    const char *point = line + 1;
+                    char condname[kMaxLineLen];
+                    sscanf(point, "%s%n", condname, &skip);
+                    point += skip;
+                    sscanf(point, "%s%n", tmpname, &skip);
+                    std::string oldn = groupname + condname, newn = groupname + tmpname;
+                    if (oldn != newn) {
+                        int po = find_cond(oldn);
+                        if (po >= 0) {
+                            int pn = find_cond(newn);
+                            if (pn >= 0) {
+                                // merge the old conductor's panels into the new one
+                                int ido = order[po], idn = order[pn];
+                                conds[idn].panels.insert(conds[idn].panels.end(), conds[ido].panels.begin(), conds[ido].panels.end());
+                                order.erase(order.begin() + po);
+                            } else {
+                                conds[order[po]].name = newn;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        parse_level--;
+        return ret;
+    }
+
+    // ------------------------------------------------------ super hierarchy
+    double geo_normal_calc(const Element &e, D3 &out) {
+        float n[3];
+        double m = newell_normal(e.v, n);
+        out = widen(n);
+        return m;
+    }
+    D3 geo_normal(int id) {
+        const Element &e = el[id];
+        if (e.type & FCG_IS_SUPER_NODE) { D3 n; geo_normal_calc(e, n); return n; }
+        return widen(e.n);
+    }
+
+    int make_super(int lid, int rid) {
+        Element e;
+        const Element &L = el[lid], &R = el[rid];
+        bool ld = L.type & FCG_IS_DIEL, rd = R.type & FCG_IS_DIEL;
+        if (ld != rd) warn("internal: dielectric sub-panels not coherent in type");
+        if (ld && rd) e.type |= (FCG_IS_SUPER_NODE | FCG_IS_DIEL | FCG_OUTPERM_NORMAL_DIR);
+        else e.type |= FCG_IS_SUPER_NODE;
+        e.type &= ~FCG_IS_LEAF;
+        e.left = lid;
+        e.right = rid;
+        e.area = L.area + R.area;
+        D3 cen = divs(add(scale(widen(L.c), L.area), scale(widen(R.c), R.area)), e.area);
+        store(e.c, cen);
+        D3 ln = widen(L.n), rn = widen(R.n);
+        if (!(L.type & FCG_OUTPERM_NORMAL_DIR)) ln = d3(-ln.x, -ln.y, -ln.z);
+        if (!(R.type & FCG_OUTPERM_NORMAL_DIR)) rn = d3(-rn.x, -rn.y, -rn.z);
+        D3 an = divs(add(scale(ln, L.area), scale(rn, R.area)), e.area);
+        store(e.n, an);
+        double modnormal = mod(widen(e.n));
+        D3 normal;
+        if (modnormal < FCG_PANEL_EPS) {
+            if (fabs(ln.x) > FCG_PANEL_EPS) { normal.x = (-ln.y - ln.z) / ln.x; normal.y = 1.0f; normal.z = 1.0f; }
+            else if (fabs(ln.y) > FCG_PANEL_EPS) { normal.y = (-ln.x - ln.z) / ln.y; normal.x = 1.0f; normal.z = 1.0f; }
+            else if (fabs(ln.z) > FCG_PANEL_EPS) { normal.z = (-ln.x - ln.y) / ln.z; normal.x = 1.0f; normal.y = 1.0f; }
+            else {
+                normal = add(scale(geo_normal(lid), el[lid].area), scale(geo_normal(rid), el[rid].area));
+                normalize(normal);
+                if (mod(normal) < FCG_PANEL_EPS) normal = d3(0, 0, 1);
+            }
+        } else {
+            normal = divs(widen(e.n), modnormal);
+        }
+        D3 cm;
+        if (L.area < R.area) cm = fsub(L.c, e.c);
+        else cm = fsub(R.c, e.c);
+        if (mod(cross(normal, cm)) < FCG_PANEL_EPS) {
+            cm.x = normal.x * 0.5 + normal.y * kMinus05PlusSqr2Div4 + normal.z * k05PlusSqr2Div4;
+            cm.y = normal.x * 0.5 + normal.y * k05PlusSqr2Div4 + normal.z * kMinus05PlusSqr2Div4;
+            cm.z = normal.x * (-kSqr2) + normal.y * 0.5 + normal.z * 0.5;
+        }
+        D3 xv = cross(cm, normal);
+        normalize(xv);
+        D3 yv = cross(normal, xv);
+        normalize(yv);
+        double Rr = k2DivFourthRoot27 * sqrt(e.area);
+        D3 c = widen(e.c);
+        store(e.v, add(c, scale(yv, Rr)));
+        double a = k2DivFourthRoot3 * sqrt(e.area);
+        store(e.v + 3, sub(sub(c, scale(yv, Rr / 2.0)), scale(xv, a / 2.0)));
+        store(e.v + 6, add(sub(c, scale(yv, Rr / 2.0)), scale(xv, a / 2.0)));
+        e.maxside_idx = 0;
+        e.maxside = a;
+        el.push_back(e);
+        return (int)el.size() - 1;
+    }
+
+    struct BBox {
+        D3 mn, mx;
+        bool empty = true;
+        void add(const float *p) {
+            D3 q = widen(p);
+            if (empty) { mn = q; mx = q; empty = false; return; }
+            for (int i = 0; i < 3; i++) {
+                if (q[i] < mn[i]) mn[i] = q[i];
+                if (q[i] > mx[i]) mx[i] = q[i];
+            }
+        }
+        int max_side() const {
+            double dx = mx.x - mn.x, dy = mx.y - mn.y, dz = mx.z - mn.z;
+            if (dx >= dy && dx >= dz) return 0;
+            if (dy >= dz) return 1;
+            return 2;
+        }
+    };
+
+    std::vector<int32_t> arr1, arr2;
+
+    int rec_super(size_t first, size_t n, const BBox &bb, int depth) {
+        if (n == 1) return arr1[first];
+        if (depth > kMaxDepth) { err = "super hierarchy too deep (coincident panel centroids?)"; return -1; }
+        int mc = bb.max_side();
+        double mid = (bb.mx[mc] + bb.mn[mc]) / 2.0;
+        size_t lo = first, hi = first + n - 1;
+        for (size_t i = first; i < first + n; i++) {
+            if ((double)el[arr1[i]].c[mc] <= mid) arr2[lo++] = arr1[i];
+            else arr2[hi--] = arr1[i];
+        }
+        if (lo == first || lo == first + n) {
+            err = "panels with coincident centroids cannot be split into a hierarchy";
+            return -1;
+        }
+        BBox lb, rb;
+        for (size_t i = first; i < lo; i++) { arr1[i] = arr2[i]; lb.add(el[arr1[i]].c); }
+        for (size_t i = lo; i < first + n; i++) { arr1[i] = arr2[i]; rb.add(el[arr1[i]].c); }
+        int l = rec_super(first, lo - first, lb, depth + 1);
+        if (l < 0) return -1;
+        int r = rec_super(lo, first + n - lo, rb, depth + 1);
+        if (r < 0) return -1;
+        return make_super(l, r);
+    }
+
+    int build_super() {
+        max_area = max_side = total_area = 0.0;
+        for (size_t k = 0; k < order.size(); k++) {
+            Conductor &C = conds[order[k]];
+            if (C.panels.empty()) { err = "conductor " + C.name + " has no panels"; return FC_FILE_ERROR; }
+            BBox bb;
+            arr1.assign(C.panels.begin(), C.panels.end());
+            arr2.assign(C.panels.size(), 0);
+            for (size_t i = 0; i < arr1.size(); i++) bb.add(el[arr1[i]].c);
+            int top = rec_super(0, arr1.size(), bb, 0);
+            if (top < 0) return FC_FILE_ERROR;
+            C.top = top;
+            if (el[top].maxside > max_side) max_side = el[top].maxside;
+            if (el[top].area > max_area) max_area = el[top].area;
+            total_area += el[top].area;
+        }
+        return FC_NORMAL_END;
+    }
+
+    // ------------------------------------------------------------ refinement
+    int subdivide(int id) {
+        if (!(el[id].type & FCG_IS_LEAF)) return FC_NORMAL_END;
+        Element P = el[id];
+        Element Lc, Rc;
+        int ms = P.maxside_idx;
+        const float *v0 = P.v, *v1 = P.v + 3, *v2 = P.v + 6;
+        // midpoint of the longest side (float sum, exact halving)
+        const float *a, *b, *o;  // side endpoints a-b, opposite vertex o
+        if (ms == 0) { a = v1; b = v0; o = v2; }
+        else if (ms == 1) { a = v2; b = v1; o = v0; }
+        else { a = v0; b = v2; o = v1; }
+        float sx = a[0] + b[0], sy = a[1] + b[1], sz = a[2] + b[2];
+        D3 mid = d3(sx / 2.0, sy / 2.0, sz / 2.0);
+        double newside = mod(d3((double)o[0] - mid.x, (double)o[1] - mid.y, (double)o[2] - mid.z));
+        double half = P.maxside / 2.0;
+        float m[3];
+        store(m, mid);
+        double lsl[3], rsl[3];
+        auto setv = [](Element &e, const float *p0, const float *p1, const float *p2) {
+            memcpy(e.v, p0, 12); memcpy(e.v + 3, p1, 12); memcpy(e.v + 6, p2, 12);
+        };
+        if (ms == 0) {
+            setv(Lc, v0, m, v2);
+            lsl[0] = half; lsl[1] = newside; lsl[2] = mod(fsub(v0, v2));
+            setv(Rc, m, v1, v2);
+            rsl[0] = half; rsl[1] = mod(fsub(v2, v1)); rsl[2] = newside;
+        } else if (ms == 1) {
+            setv(Lc, v1, m, v0);
+            lsl[0] = half; lsl[1] = newside; lsl[2] = mod(fsub(v1, v0));
+            setv(Rc, m, v2, v0);
+            rsl[0] = half; rsl[1] = mod(fsub(v0, v2)); rsl[2] = newside;
+        } else {
+            setv(Lc, v2, m, v1);
+            lsl[0] = half; lsl[1] = newside; lsl[2] = mod(fsub(v2, v1));
+            setv(Rc, m, v0, v1);
+            rsl[0] = half; rsl[1] = mod(fsub(v1, v0)); rsl[2] = newside;
+        }
+        Lc.type = Rc.type = P.type;
+        Lc.diel = Rc.diel = P.diel;
+        Lc.area = Rc.area = P.area / 2.0;
+        memcpy(Lc.n, P.n, 12);
+        memcpy(Rc.n, P.n, 12);
+        centroid3(Lc);
+        centroid3(Rc);
+        max_side3(Lc, lsl[0], lsl[1], lsl[2]);
+        max_side3(Rc, rsl[0], rsl[1], rsl[2]);
+        el.push_back(Lc);
+        el.push_back(Rc);
+        int l = (int)el.size() - 2, r = (int)el.size() - 1;
+        el[id].left = l;
+        el[id].right = r;
+        el[id].type &= ~FCG_IS_LEAF;
+        return FC_NORMAL_END;
+    }
+
+    bool refine_criteria(double *c1, double *c2, int p1, int p2, D3 dist, double rdist, double rmax, double e, double ccoeff) {
+        const Element &A = el[p1], &B = el[p2];
+        bool force = false;
+        fcg_d3 n1 = fcg_diel_normal(A.type, A.n), n2 = fcg_diel_normal(B.type, B.n);
+        double pe1, pe2;
+        bool d1 = (A.type & FCG_IS_DIEL), d2 = (B.type & FCG_IS_DIEL);
+        if (rdist / rmax < 2.0) {
+            fcg_d3 ca = fcg_widen(A.c), cb = fcg_widen(B.c);
+            pe1 = d1 ? fcg_enfield_numerical(ca, B.v, n1, 2) : fcg_potential_numerical(ca, B.v, 2);
+            pe2 = d2 ? fcg_enfield_numerical(cb, A.v, n2, 2) : fcg_potential_numerical(cb, A.v, 2);
+        } else {
+            if (d1) pe1 = (dist.x * n1.x + dist.y * n1.y + dist.z * n1.z) / (rdist * rdist * rdist);
+            else pe1 = 1.0f / rdist;
+            if (d2) pe2 = (-dist.x * n2.x + -dist.y * n2.y + -dist.z * n2.z) / (rdist * rdist * rdist);
+            else pe2 = 1.0f / rdist;
+        }
+        if (d1) *c1 = fabs(pe1 * B.area * B.maxside / (max_side * max_area * ccoeff));
+        else *c1 = fabs(pe1 * B.area / (max_area * ccoeff));
+        if (*c1 > e) force = true;
+        if (d2) *c2 = fabs(pe2 * A.area * A.maxside / (max_side * max_area * ccoeff));
+        else *c2 = fabs(pe2 * A.area / (max_area * ccoeff));
+        if (*c2 > e) force = true;
+        return force;
+    }
+
+    int discretize_mutual(int p1, int p2, bool selfc) {
+        level++;
+        if (level > max_level) max_level = level;
+        if (level > kMaxDepth) { err = "mesh refinement recursion too deep (touching or overlapping panels?)"; return FC_GENERIC_ERROR; }
+        D3 dist = fsub(el[p1].c, el[p2].c);
+        double rdist = mod(dist);
+        double r1 = el[p1].maxside, r2 = el[p2].maxside;
+        double rmax = r1 > r2 ? r1 : r2;
+        double ccoeff;
+        if (selfc) ccoeff = (mesh_curv - 1.0) * (dot(geo_normal(p1), geo_normal(p2)) + 1.0) + 1.0;
+        else ccoeff = 1.0f;
+        double c1, c2;
+        int ret = FC_NORMAL_END;
+        if (refine_criteria(&c1, &c2, p1, p2, dist, rdist, rmax, mesh_eps, ccoeff)) {
+            if (el[p1].area > el[p2].area) {
+                subdivide(p1);
+                if ((ret = discretize_mutual(el[p1].left, p2, selfc)) == FC_NORMAL_END)
+                    ret = discretize_mutual(el[p1].right, p2, selfc);
+            } else {
+                subdivide(p2);
+                if ((ret = discretize_mutual(p1, el[p2].left, selfc)) == FC_NORMAL_END)
+                    ret = discretize_mutual(p1, el[p2].right, selfc);
+            }
+        } else {
+            if (!(el[p1].type & FCG_IS_SUPER_NODE) && c1 > max_mesh_eps) max_mesh_eps = c1;
+            if (!(el[p2].type & FCG_IS_SUPER_NODE) && c2 > max_mesh_eps) max_mesh_eps = c2;
+        }
+        level--;
+        return ret;
+    }
+
+    int discretize_self(int id, int64_t &panels, int64_t &nodes) {
+        level++;
+        if (level > max_level) max_level = level;
+        int ret = FC_NORMAL_END;
+        if ((el[id].type & FCG_IS_LEAF) && level == 1) subdivide(id);
+        if (!(el[id].type & FCG_IS_LEAF)) {
+            int l = el[id].left, r = el[id].right;
+            if ((ret = discretize_mutual(l, r, true)) != FC_NORMAL_END) return ret;
+            if ((ret = discretize_self(l, panels, nodes)) != FC_NORMAL_END) return ret;
+            if ((ret = discretize_self(r, panels, nodes)) != FC_NORMAL_END) return ret;
+        } else {
+            panels++;
+        }
+        nodes++;
+        level--;
+        return ret;
+    }
+
+    void refine_mutual(int p1, int p2) {
+        level++;
+        if (level > max_level) max_level = level;
+        D3 dist = fsub(el[p1].c, el[p2].c);
+        double rdist = mod(dist);
+        double r1 = el[p1].maxside, r2 = el[p2].maxside;
+        double rmax = r1 > r2 ? r1 : r2;
+        bool leaf1 = el[p1].type & FCG_IS_LEAF, leaf2 = el[p2].type & FCG_IS_LEAF;
+        bool force = false;
+        if (!leaf1 || !leaf2) {
+            double c1, c2;
+            force = refine_criteria(&c1, &c2, p1, p2, dist, rdist, rmax, eps, 1.0f);
+        }
+        if (force) {
+            int which;
+            if (!leaf1 && leaf2) which = 1;
+            else if (leaf1 && !leaf2) which = 2;
+            else which = (el[p1].area > el[p2].area) ? 1 : 2;
+            if (which == 1) { refine_mutual(el[p1].left, p2); refine_mutual(el[p1].right, p2); }
+            else { refine_mutual(p1, el[p2].left); refine_mutual(p1, el[p2].right); }
+        } else {
+            pairs.push_back(std::make_pair(p1, p2));
+        }
+        level--;
+    }
+
+    void refine_self(int id) {
+        level++;
+        if (level > max_level) max_level = level;
+        if (!(el[id].type & FCG_IS_LEAF)) {
+            refine_mutual(el[id].left, el[id].right);
+            refine_self(el[id].left);
+            refine_self(el[id].right);
+        }
+        level--;
+    }
+
+    // ---------------------------------------------------------------- flatten
+    int flatten(Model &M) {
+        size_t ne = el.size();
+        std::vector<int32_t> node_of(ne, -1);
+        std::vector<int32_t> post;
+        post.reserve(ne);
+        int64_t leaf_counter = 0;
+        M.conductors.clear();
+        M.cond_leaf_first.clear();
+        std::vector<int64_t> leaf_first_of(ne, 0), leaf_count_of(ne, 0);
+        std::vector<int32_t> cond_of;
+        for (size_t k = 0; k < order.size(); k++) {
+            Conductor &C = conds[order[k]];
+            int64_t start = leaf_counter;
+            // iterative post-order traversal
+            std::vector<std::pair<int32_t, int>> st;
+            st.push_back(std::make_pair(C.top, 0));
+            while (!st.empty()) {
+                std::pair<int32_t, int> &t = st.back();
+                int32_t id = t.first;
+                if (el[id].type & FCG_IS_LEAF) {
+                    leaf_first_of[id] = leaf_counter;
+                    leaf_count_of[id] = 1;
+                    leaf_counter++;
+                    node_of[id] = (int32_t)post.size();
+                    post.push_back(id);
+                    st.pop_back();
+                } else if (t.second == 0) {
+                    t.second = 1;
+                    st.push_back(std::make_pair(el[id].left, 0));
+                } else if (t.second == 1) {
+                    t.second = 2;
+                    st.push_back(std::make_pair(el[id].right, 0));
+                } else {
+                    leaf_first_of[id] = leaf_first_of[el[id].left];
+                    leaf_count_of[id] = leaf_count_of[el[id].left] + leaf_count_of[el[id].right];
+                    node_of[id] = (int32_t)post.size();
+                    post.push_back(id);
+                    st.pop_back();
+                }
+            }
+            cond_of.resize(post.size(), (int32_t)k);
+            C.leaf_count = leaf_counter - start;
+            M.cond_leaf_first.push_back(start);
+            M.conductors.push_back(C);
+        }
+        int64_t Nn = (int64_t)post.size(), Np = leaf_counter, L = 2 * (int64_t)pairs.size();
+        if (L > 0x7fffffffLL || Nn > 0x7fffffffLL) { err = "model too large for 32-bit link indices"; return FC_OUT_OF_MEMORY; }
+        M.n_nodes = Nn; M.n_panels = Np; M.n_links = L;
+        M.type.resize(Nn); M.left.resize(Nn); M.right.resize(Nn); M.cond.resize(Nn);
+        M.leaf_first.resize(Nn); M.leaf_count.resize(Nn); M.link_ptr.assign(Nn + 1, 0);
+        M.vert.resize(Nn * 9); M.cent.resize(Nn * 3); M.norm.resize(Nn * 3);
+        M.area.resize(Nn); M.maxside.resize(Nn); M.maxside_idx.resize(Nn);
+        M.leaf_node.resize(Np); M.leaf_diel.resize(Np);
+        for (int64_t i = 0; i < Nn; i++) {
+            const Element &e = el[post[i]];
+            M.cond[i] = cond_of[i];
+            M.type[i] = e.type;
+            M.left[i] = e.left >= 0 ? node_of[e.left] : -1;
+            M.right[i] = e.right >= 0 ? node_of[e.right] : -1;
+            M.leaf_first[i] = leaf_first_of[post[i]];
+            M.leaf_count[i] = leaf_count_of[post[i]];
+            memcpy(&M.vert[i * 9], e.v, 36);
+            memcpy(&M.cent[i * 3], e.c, 12);
+            memcpy(&M.norm[i * 3], e.n, 12);
+            M.area[i] = e.area;
+            M.maxside[i] = e.maxside;
+            M.maxside_idx[i] = e.maxside_idx;
+            if (e.type & FCG_IS_LEAF) {
+                M.leaf_node[M.leaf_first[i]] = (int32_t)i;
+                M.leaf_diel[M.leaf_first[i]] = (e.type & FCG_IS_DIEL) ? 0 : e.diel;
+            }
+        }
+        // links: stable counting sort of the emitted pairs by destination node
+        std::vector<int64_t> cnt(Nn + 1, 0);
+        for (size_t k = 0; k < pairs.size(); k++) { cnt[node_of[pairs[k].first]]++; cnt[node_of[pairs[k].second]]++; }
+        for (int64_t i = 0; i < Nn; i++) M.link_ptr[i + 1] = M.link_ptr[i] + cnt[i];
+        std::vector<int64_t> fill(M.link_ptr.begin(), M.link_ptr.end() - 1);
+        M.link_src.resize(L);
+        for (size_t k = 0; k < pairs.size(); k++) {
+            int32_t a = node_of[pairs[k].first], b = node_of[pairs[k].second];
+            M.link_src[fill[a]++] = b;
+            M.link_src[fill[b]++] = a;
+        }
+        std::vector<std::pair<int32_t, int32_t>>().swap(pairs);
+        return FC_NORMAL_END;
+    }
+};
+
+}  // namespace
+
+int build_model(const std::string &path, const BuildOptions &opt, Model &M, std::string &err) {
+    Builder B;
+    B.opt = opt;
+    for (int i = 0; i < kMaxParseLevel + 2; i++) B.group_num[i] = 1;
+    B.mesh_eps = opt.mesh_eps;
+    B.eps = opt.eps_ratio * opt.mesh_eps;
+    if (B.eps == 0.0) B.eps = 0.01;
+    B.mesh_curv = opt.mesh_curv < 1.0 ? 1.0 : opt.mesh_curv;
+
+    // sub-file names and external files resolve relative to the input's directory
+    std::string dir, base = path;
+    size_t slash = path.rfind('/');
+    if (slash != std::string::npos) { dir = path.substr(0, slash + 1); base = path.substr(slash + 1); }
+    {
+        InFile *F = NULL;
+        int r = B.load_file(path, F);
+        if (r != FC_NORMAL_END) { err = B.err; return r; }
+        // the first line decides 2D versus 3D
+        if (!F->lines.empty() && (strstr(F->lines[0].c_str(), "2D") || strstr(F->lines[0].c_str(), "2d"))) {
+            err = "2D input files are not supported by this solver";
+            return FC_FILE_ERROR;
+        }
+        B.files.clear();
+    }
+    char cwd[4096];
+    bool have_cwd = getcwd(cwd, sizeof cwd) != NULL;
+    if (!dir.empty() && chdir(dir.c_str()) != 0) { err = "cannot enter directory " + dir; return FC_FILE_ERROR; }
+    int ret = B.parse_file(base, NULL, false, d3(0, 0, 0), 1.0, "", 0.0, d3(0, 0, 0));
+    if (!dir.empty() && have_cwd && chdir(cwd) != 0) { /* keep going: the model is in memory */ }
+    if (ret != FC_NORMAL_END) { err = B.err; return ret; }
+    if (B.order.empty()) { err = "no panels found in the input file"; return FC_FILE_ERROR; }
+
+    if ((ret = B.build_super()) != FC_NORMAL_END) { err = B.err; return ret; }
+
+    // adaptive mesh: mutual refinement of all conductor pairs, then self
+    B.level = 0;
+    B.max_level = 0;
+    B.max_mesh_eps = 0.0;
+    size_t nc = B.order.size();
+    for (size_t i = 0; i < nc; i++)
+        for (size_t j = i + 1; j < nc; j++) {
+            ret = B.discretize_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top, false);
+            if (ret != FC_NORMAL_END) { err = B.err; return ret; }
+        }
+    int64_t panels = 0, nodes = 0;
+    for (size_t i = 0; i < nc; i++) {
+        B.level = 0;
+        ret = B.discretize_self(B.conds[B.order[i]].top, panels, nodes);
+        if (ret != FC_NORMAL_END) { err = B.err; return ret; }
+    }
+    // links: mutual interactions of all conductor pairs, then self, conductor by conductor
+    for (size_t i = 0; i < nc; i++) {
+        for (size_t j = i + 1; j < nc; j++) B.refine_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top);
+        B.refine_self(B.conds[B.order[i]].top);
+    }
+    if ((ret = B.flatten(M)) != FC_NORMAL_END) { err = B.err; return ret; }
+    M.input_panels = B.input_panels;
+    M.raw_cond_panels = B.raw_cond;
+    M.raw_diel_panels = B.raw_diel;
+    M.max_mesh_eps = B.max_mesh_eps;
+    M.max_area = B.max_area;
+    M.max_side = B.max_side;
+    M.total_area = B.total_area;
+    M.eps = B.eps;
+    M.mesh_eps = B.mesh_eps;
+    M.max_level = B.max_level;
+    M.warnings = B.warnings;
+    return FC_NORMAL_END;
+}
+
+}  // namespace fcg
