@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 capacitance solve path.
+
+Metric: solves/s of one complete capacitance extraction (GPU coefficient fill
++ batched preconditioned GMRES + capacitance assembly) of a resident model,
+with p50/p99 step latency, for the mixed-precision path (headline) beside the
+plain FP64 path, and the end-to-end figure through the C ABI with the model
+uploaded from pinned host memory and the capacitance matrix read back.
+
+Workload (default): single conductor sphere, radius 1 m, icosahedron
+subdivided 7 times (327,680 triangles), mesh refinement off (-m1e30), link
+tolerance 3e-4 (-d3e-34), GMRES tolerance 1e-4, Jacobi preconditioner.
+Synthetic, generated deterministically by fastercap_gb300.geometry.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs replicas (one independent workload per GPU, launched by torchrun).
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port; the reference's own binary where it was built on this machine)
+on all host cores, on the same model.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FOUR_PI_E0 = 1.1126500559756e-10
+METRIC = "solves/s & p50/p99 latency, mixed vs FP64 on GB300 at <=0.1% C-matrix error"
+
+WORKLOADS = {
+    # name: (writer, mesh_eps, eps_ratio, gmres tol, analytic C or None)
+    "sphere_327680": (lambda p: __import__("fastercap_gb300.geometry", fromlist=["x"]).write_sphere(p, 7),
+                      1e30, 3e-34, 1e-4, FOUR_PI_E0),
+    "sphere_81920": (lambda p: __import__("fastercap_gb300.geometry", fromlist=["x"]).write_sphere(p, 6),
+                     1e30, 1e-33, 1e-4, FOUR_PI_E0),
+    "sphere_20480": (lambda p: __import__("fastercap_gb300.geometry", fromlist=["x"]).write_sphere(p, 5),
+                     1e30, 1e-33, 1e-4, FOUR_PI_E0),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_model(workload: str):
+    import fastercap_gb300 as fc
+    writer, meps, dratio, tol, analytic = WORKLOADS[workload]
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, workload + ".txt")
+        writer(path)
+        t0 = time.perf_counter()
+        model = fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio)
+        build_s = time.perf_counter() - t0
+    return model, build_s, tol, analytic, meps * dratio
+
+
+def model_bytes(model) -> int:
+    return int(sum(np.asarray(v).nbytes for v in model.arrays.values()))
+
+
+def pinned_model(model):
+    """Copy the model arrays into pinned host memory (the e2e upload source)."""
+    import torch
+    import fastercap_gb300 as fc
+    arrays, keep = {}, []
+    for k, v in model.arrays.items():
+        a = np.ascontiguousarray(v)
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        view = t.numpy().view(a.dtype).reshape(a.shape)
+        view[...] = a
+        arrays[k] = view
+        keep.append(t)
+    m = fc.Model.from_arrays(arrays, list(model.names))
+    m._pinned = keep
+    return m
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the oracle port on every host core, full solves of the same model."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    model, build_s, tol, analytic, eps = build_model(args.workload)
+    cores = os.cpu_count() or 1
+    o = Oracle(model.arrays, threads=cores)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        o.fill()
+        cap, it, _, _ = o.solve(tol, 1)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = len(times) / total
+    sample = "full solves (fill + GMRES + C) of the %d-panel, %d-link model" % (model.n_panels, model.n_links)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "p50_ms": 1000 * float(np.percentile(times, 50)), "p99_ms": 1000 * float(np.percentile(times, 99)),
+        "config": {"workload": args.workload, "panels": model.n_panels, "links": model.n_links, "link_eps": eps,
+                   "gmres_tol": tol, "precond": "jacobi", "rhs": len(model.conductor_names)},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "capacitance": float(cap[0, 0]), "iterations": [int(x) for x in it],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(prob, stream, n, tol, flush_buf, torch):
+    """Per-step device times (ms) of fill + solve, L2 flushed between steps."""
+    s = torch.cuda.ExternalStream(stream)
+    times, cap, it = [], None, None
+    for _ in range(n):
+        with torch.cuda.stream(s):
+            flush_buf.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        prob.fill()
+        cap, it = prob.solve(tol=tol)
+        e1.record(s)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return times, cap, it
+
+
+def run_gb300(args, rank, world, local_rank):
+    import torch
+    import fastercap_gb300 as fc
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    model, build_s, tol, analytic, eps = build_model(args.workload)
+    ctx = fc.Context(local_rank)
+    stream = ctx.stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # resident mixed-precision problem: the headline
+    prob = ctx.problem(model, fc.PREC_MIXED)
+    time_steps(prob, stream, args.warmup, tol, flush, torch)
+    prob.reset_stats()
+    prob.set_profiling(True)
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        times, cap_m, it_m = time_steps(prob, stream, args.steps, tol, flush, torch)
+    barrier()
+    st = prob.stats()
+    prob.set_profiling(False)
+    total_ms = sum(times)
+    # plain FP64 path on the same model
+    p64 = ctx.problem(model, fc.PREC_FP64)
+    time_steps(p64, stream, max(1, args.warmup), tol, flush, torch)
+    times64, cap_64, it_64 = time_steps(p64, stream, args.steps, tol, flush, torch)
+    p64.close()
+    # end to end through the C ABI: pinned host model -> upload -> fill -> solve -> C back
+    pm = pinned_model(model)
+    h2d = model_bytes(model)
+    s = torch.cuda.ExternalStream(stream)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(s):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        pe = ctx.problem(pm, fc.PREC_MIXED)
+        pe.fill()
+        cap_e, _ = pe.solve(tol=tol)
+        e1.record(s)
+        e1.synchronize()
+        pe.close()
+        if i >= args.warmup:
+            e2e_times.append(e0.elapsed_time(e1))
+    d2h = cap_e.nbytes + 4 * len(cap_e)
+
+    tmax = total_ms
+    if world > 1:
+        t = torch.tensor([total_ms, sum(e2e_times)], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tmax, e2e_max = float(t[0]), float(t[1])
+    else:
+        e2e_max = sum(e2e_times)
+    value = world * args.steps / (tmax / 1000.0)
+    e2e_value = world * args.steps / (e2e_max / 1000.0)
+    peak, peak_kind = peaks()
+    link_avg_ms = st["link_ms"] / max(1, st["link_launches"])
+    link_bytes = st["link_bytes"] / max(1, st["link_launches"])
+    achieved = link_bytes / (link_avg_ms / 1000.0) / 1e9 if link_avg_ms > 0 else None
+    rel_mixed_vs_64 = float(np.max(np.abs(cap_m - cap_64) / np.abs(cap_64)))
+    result = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
+        "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99)),
+        "config": {"workload": args.workload, "panels": model.n_panels, "links": model.n_links, "link_eps": eps,
+                   "gmres_tol": tol, "precond": "jacobi", "rhs": len(model.conductor_names),
+                   "l2": "flushed between steps (256 MiB write)", "host_build_s": round(build_s, 3),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": world * args.steps / (sum(times64) / 1000.0), "unit": "solves/s",
+                 "p50_ms": float(np.percentile(times64, 50)), "p99_ms": float(np.percentile(times64, 99)),
+                 "iterations": [int(x) for x in it_64]},
+        "mixed_vs_fp64": {"speedup": (sum(times64) / sum(times)), "max_rel_c_err": rel_mixed_vs_64},
+        "accuracy": {"c_mixed": float(cap_m[0, 0]), "c_fp64": float(cap_64[0, 0]),
+                     "rel_err_vs_analytic": (float(cap_m[0, 0]) - analytic) / analytic if analytic else None,
+                     "iterations": [int(x) for x in it_m]},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "p50_ms": float(np.percentile(e2e_times, 50))},
+        "gpu_launches": int(st["kernel_launches"]),
+        "roofline": {"kernel": "k_spmv32 (link product)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+                     "traffic": None, "launches": int(st["link_launches"]),
+                     "bytes_per_launch": link_bytes, "avg_launch_ms": link_avg_ms},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+        cores = os.cpu_count() or 1
+        o = Oracle(model.arrays, threads=cores)
+        t0 = time.perf_counter()
+        o.fill()
+        ocap, oit, _, _ = o.solve(tol, 1)
+        dt = time.perf_counter() - t0
+        result["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+                                  "sample": "one full solve (fill + GMRES + C) of the same model"}
+        result["accuracy"]["max_rel_c_err_vs_cpu_fp64"] = float(np.max(np.abs(cap_m - ocap) / np.abs(ocap)))
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    prob.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sphere_327680", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3")
+        args.warmup = 3
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

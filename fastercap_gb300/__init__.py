@@ -1,0 +1,362 @@
+"""fastercap_gb300: GB300-native solve path for FasterCap input files.
+
+Python binding over the C ABI of ``libfastercap_gb300.so``
+(``include/fastercap_gb300.h``). The library is built in-tree by
+``fastercap_gb300.build.build()``; importing this package never falls back to
+another implementation: if the library is missing, :func:`lib` raises.
+
+Typical use::
+
+    import fastercap_gb300 as fc
+    model = fc.Model.build("bus.txt", mesh_eps=0.01)
+    with fc.Context() as ctx:
+        prob = ctx.problem(model, precision=fc.PREC_MIXED)
+        prob.fill()
+        cap, iters = prob.solve(tol=1e-4)
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfastercap_gb300.so")
+
+NORMAL_END = 0
+GENERIC_ERROR = 1
+COMMAND_LINE_ERROR = 64
+CANNOT_OPEN_FILE = 66
+OUT_OF_MEMORY = 71
+FILE_ERROR = 74
+USER_BREAK = 125
+DEVICE_ERROR = 90
+NOT_CONVERGED = 91
+
+PRECOND_NONE = 0
+PRECOND_JACOBI = 1
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# element type bits
+IS_LEAF, IS_DIEL, OUTPERM_NORMAL_DIR, IS_SUPER_NODE = 1, 2, 4, 128
+
+
+class FCError(RuntimeError):
+    """A C ABI call returned a non-zero FC_* status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, code))
+        self.code = code
+
+
+class BuildOptions(C.Structure):
+    _fields_ = [("mesh_eps", C.c_double), ("eps_ratio", C.c_double), ("mesh_curv", C.c_double), ("verbose", C.c_int)]
+
+
+class ModelArrays(C.Structure):
+    _fields_ = [
+        ("n_nodes", C.c_int64), ("n_panels", C.c_int64), ("n_links", C.c_int64), ("n_conductors", C.c_int32),
+        ("node_type", C.c_void_p), ("node_left", C.c_void_p), ("node_right", C.c_void_p),
+        ("node_leaf_first", C.c_void_p), ("node_leaf_count", C.c_void_p),
+        ("node_vertices", C.c_void_p), ("node_centroid", C.c_void_p), ("node_normal", C.c_void_p),
+        ("node_area", C.c_void_p), ("node_maxside", C.c_void_p),
+        ("link_ptr", C.c_void_p), ("link_src", C.c_void_p), ("leaf_diel", C.c_void_p),
+        ("cond_is_diel", C.c_void_p), ("cond_leaf_first", C.c_void_p), ("cond_leaf_count", C.c_void_p),
+        ("cond_outperm", C.c_void_p), ("cond_inperm", C.c_void_p), ("cond_surf_ptr", C.c_void_p),
+        ("cond_surf_outperm", C.c_void_p),
+    ]
+
+
+class ModelInfo(C.Structure):
+    _fields_ = [("n_nodes", C.c_int64), ("n_panels", C.c_int64), ("n_links", C.c_int64), ("input_panels", C.c_int64),
+                ("n_conductors", C.c_int32), ("n_dielectrics", C.c_int32), ("max_level", C.c_int32),
+                ("max_mesh_eps", C.c_double), ("eps", C.c_double), ("mesh_eps", C.c_double)]
+
+
+class ProblemStats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_int64), ("link_launches", C.c_int64), ("link_ms", C.c_double),
+                ("link_bytes", C.c_int64), ("fill_ms", C.c_double), ("solve_ms", C.c_double)]
+
+
+class SolveOptions(C.Structure):
+    _fields_ = [("tol", C.c_double), ("precond", C.c_int), ("max_iter", C.c_int)]
+
+
+# (field, dtype, length key, columns)
+ARRAY_FIELDS = [
+    ("node_type", np.uint8, "n_nodes", 1), ("node_left", np.int32, "n_nodes", 1), ("node_right", np.int32, "n_nodes", 1),
+    ("node_leaf_first", np.int64, "n_nodes", 1), ("node_leaf_count", np.int64, "n_nodes", 1),
+    ("node_vertices", np.float32, "n_nodes", 9), ("node_centroid", np.float32, "n_nodes", 3),
+    ("node_normal", np.float32, "n_nodes", 3), ("node_area", np.float64, "n_nodes", 1),
+    ("node_maxside", np.float64, "n_nodes", 1), ("link_ptr", np.int64, "n_nodes+1", 1),
+    ("link_src", np.int32, "n_links", 1), ("leaf_diel", np.uint8, "n_panels", 1),
+    ("cond_is_diel", np.uint8, "n_conductors", 1), ("cond_leaf_first", np.int64, "n_conductors", 1),
+    ("cond_leaf_count", np.int64, "n_conductors", 1), ("cond_outperm", np.float64, "n_conductors", 1),
+    ("cond_inperm", np.float64, "n_conductors", 1), ("cond_surf_ptr", np.int32, "n_conductors+1", 1),
+]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("%s is missing: run fastercap_gb300.build.build() first" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, dp, ip = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    L.fcg_model_build.argtypes = [C.c_char_p, C.POINTER(BuildOptions), C.POINTER(vp), C.c_char_p, C.c_size_t]
+    L.fcg_model_info_get.argtypes = [vp, C.POINTER(ModelInfo)]
+    L.fcg_model_arrays_get.argtypes = [vp, C.POINTER(ModelArrays)]
+    L.fcg_model_conductor_name.argtypes = [vp, i32]
+    L.fcg_model_conductor_name.restype = C.c_char_p
+    L.fcg_model_free.argtypes = [vp]
+    L.fcg_model_free.restype = None
+    L.fcg_context_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.fcg_context_destroy.argtypes = [vp]
+    L.fcg_context_destroy.restype = None
+    L.fcg_last_error.restype = C.c_char_p
+    L.fcg_problem_create.argtypes = [vp, C.POINTER(ModelArrays), C.c_int, C.POINTER(vp)]
+    L.fcg_problem_create_on_stream.argtypes = [vp, C.POINTER(ModelArrays), C.c_int, vp, C.POINTER(vp)]
+    L.fcg_context_stream.argtypes = [vp]
+    L.fcg_context_stream.restype = vp
+    L.fcg_problem_set_profiling.argtypes = [vp, C.c_int]
+    L.fcg_problem_get_stats.argtypes = [vp, C.POINTER(ProblemStats)]
+    L.fcg_problem_reset_stats.argtypes = [vp]
+    L.fcg_problem_destroy.argtypes = [vp]
+    L.fcg_problem_destroy.restype = None
+    L.fcg_problem_device_bytes.argtypes = [vp]
+    L.fcg_problem_device_bytes.restype = i64
+    L.fcg_problem_fill.argtypes = [vp]
+    L.fcg_problem_get_coefficients.argtypes = [vp, vp, vp]
+    L.fcg_problem_matvec.argtypes = [vp, vp, vp, C.c_int]
+    L.fcg_problem_matvec_device.argtypes = [vp, vp, vp, C.c_int]
+    L.fcg_problem_solve.argtypes = [vp, C.POINTER(SolveOptions), vp, vp]
+    L.fcg_problem_get_charges.argtypes = [vp, vp]
+    L.fcg_run_command_line.argtypes = [C.c_char_p]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().fcg_last_error().decode(errors="replace")
+
+
+def _check(code: int, what: str):
+    if code != NORMAL_END:
+        raise FCError(code, "%s: %s" % (what, last_error()))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Model:
+    """A refined panel hierarchy with its links (host memory).
+
+    ``arrays`` holds numpy views (or owned copies for models made from
+    arrays) of the flattened layout described in ``include/fastercap_gb300.h``.
+    """
+
+    def __init__(self, handle, arrays: dict, names: list, info: dict):
+        self._h = handle
+        self.arrays = arrays
+        self.names = names
+        self.info = info
+        self._keep = None
+
+    @classmethod
+    def build(cls, path: str, mesh_eps: float = 0.1, eps_ratio: float = 1.0, mesh_curv: float = 3.0,
+              verbose: bool = False) -> "Model":
+        L = lib()
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        opt = BuildOptions(mesh_eps, eps_ratio, mesh_curv, 1 if verbose else 0)
+        code = L.fcg_model_build(os.fsencode(path), C.byref(opt), C.byref(h), err, 512)
+        if code != NORMAL_END:
+            raise FCError(code, "model build failed: " + err.value.decode(errors="replace"))
+        info_s = ModelInfo()
+        _check(L.fcg_model_info_get(h, C.byref(info_s)), "model info")
+        info = {f: getattr(info_s, f) for f, _ in ModelInfo._fields_}
+        a = ModelArrays()
+        _check(L.fcg_model_arrays_get(h, C.byref(a)), "model arrays")
+        counts = {"n_nodes": a.n_nodes, "n_nodes+1": a.n_nodes + 1, "n_links": a.n_links, "n_panels": a.n_panels,
+                  "n_conductors": a.n_conductors, "n_conductors+1": a.n_conductors + 1}
+        arrays = {}
+        for name, dt, key, cols in ARRAY_FIELDS:
+            n = counts[key] * cols
+            addr = getattr(a, name)
+            if n == 0 or not addr:
+                arrays[name] = np.zeros((0,) if cols == 1 else (0, cols), dtype=dt)
+                continue
+            buf = (C.c_char * (n * np.dtype(dt).itemsize)).from_address(addr)
+            arr = np.frombuffer(buf, dtype=dt, count=n)
+            arrays[name] = arr.reshape(-1, cols) if cols > 1 else arr
+        nsurf = int(arrays["cond_surf_ptr"][-1])
+        buf = (C.c_char * (max(nsurf, 1) * 8)).from_address(a.cond_surf_outperm)
+        arrays["cond_surf_outperm"] = np.frombuffer(buf, dtype=np.float64, count=max(nsurf, 1))
+        names = [L.fcg_model_conductor_name(h, i).decode() for i in range(a.n_conductors)]
+        m = cls(h, arrays, names, info)
+        return m
+
+    @classmethod
+    def from_arrays(cls, arrays: dict, names=None) -> "Model":
+        """Wrap externally produced arrays (e.g. a golden fixture) without a native handle."""
+        own = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        info = {"n_nodes": len(own["node_type"]), "n_panels": len(own["leaf_diel"]), "n_links": len(own["link_src"]),
+                "n_conductors": len(own["cond_is_diel"])}
+        return cls(None, own, names or ["c%d" % i for i in range(info["n_conductors"])], info)
+
+    @property
+    def n_panels(self) -> int:
+        return int(len(self.arrays["leaf_diel"]))
+
+    @property
+    def n_links(self) -> int:
+        return int(len(self.arrays["link_src"]))
+
+    @property
+    def n_nodes(self) -> int:
+        return int(len(self.arrays["node_type"]))
+
+    @property
+    def conductor_names(self):
+        return [n for n, d in zip(self.names, self.arrays["cond_is_diel"]) if not d]
+
+    def c_arrays(self) -> ModelArrays:
+        a = ModelArrays()
+        a.n_nodes, a.n_panels, a.n_links = self.n_nodes, self.n_panels, self.n_links
+        a.n_conductors = len(self.arrays["cond_is_diel"])
+        keep = []
+        for name, dt, _, _ in ARRAY_FIELDS + [("cond_surf_outperm", np.float64, None, 1)]:
+            arr = np.ascontiguousarray(self.arrays[name], dtype=dt)
+            keep.append(arr)
+            setattr(a, name, arr.ctypes.data)
+        self._keep = keep
+        return a
+
+    def close(self):
+        if self._h is not None:
+            lib().fcg_model_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Problem:
+    """A model resident on the GPU (links, coefficients, sweep plan, Krylov workspace)."""
+
+    def __init__(self, ctx: "Context", model: Model, precision: int, stream=None):
+        self.model = model
+        self.precision = precision
+        self.n_panels = model.n_panels
+        self.n_links = model.n_links
+        self.n_cond = len(model.conductor_names)
+        h = C.c_void_p()
+        arr = model.c_arrays()
+        st = C.c_void_p(stream) if stream is not None else C.c_void_p(lib().fcg_context_stream(ctx._h))
+        _check(lib().fcg_problem_create_on_stream(ctx._h, C.byref(arr), precision, st, C.byref(h)), "problem create")
+        self._h = h
+
+    def set_profiling(self, on: bool):
+        _check(lib().fcg_problem_set_profiling(self._h, 1 if on else 0), "profiling")
+
+    def stats(self) -> dict:
+        st = ProblemStats()
+        _check(lib().fcg_problem_get_stats(self._h, C.byref(st)), "stats")
+        return {f: getattr(st, f) for f, _ in ProblemStats._fields_}
+
+    def reset_stats(self):
+        _check(lib().fcg_problem_reset_stats(self._h), "reset stats")
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().fcg_problem_device_bytes(self._h))
+
+    def fill(self):
+        _check(lib().fcg_problem_fill(self._h), "coefficient fill")
+
+    def coefficients(self):
+        lc = np.empty(self.n_links, np.float64)
+        sc = np.empty(self.n_panels, np.float64)
+        _check(lib().fcg_problem_get_coefficients(self._h, _ptr(lc), _ptr(sc)), "get coefficients")
+        return lc, sc
+
+    def matvec(self, q: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        single = q.ndim == 1
+        q2 = q.reshape(1, -1) if single else q
+        v = np.empty_like(q2)
+        _check(lib().fcg_problem_matvec(self._h, _ptr(q2), _ptr(v), q2.shape[0]), "matvec")
+        return v[0] if single else v
+
+    def matvec_device(self, q_ptr: int, v_ptr: int, k: int):
+        _check(lib().fcg_problem_matvec_device(self._h, C.c_void_p(q_ptr), C.c_void_p(v_ptr), k), "matvec")
+
+    def solve(self, tol: float = 0.01, precond: int = PRECOND_JACOBI, max_iter: int = 0, allow_not_converged=False):
+        cap = np.empty((self.n_cond, self.n_cond), np.float64)
+        it = np.empty(self.n_cond, np.int32)
+        opt = SolveOptions(tol, precond, max_iter)
+        code = lib().fcg_problem_solve(self._h, C.byref(opt), _ptr(cap), _ptr(it))
+        if not (code == NORMAL_END or (allow_not_converged and code == NOT_CONVERGED)):
+            _check(code, "solve")
+        return cap, it
+
+    def charges(self) -> np.ndarray:
+        k = min(self.n_cond, 32)
+        x = np.empty((k, self.n_panels), np.float64)
+        _check(lib().fcg_problem_get_charges(self._h, _ptr(x)), "get charges")
+        return x
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            lib().fcg_problem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One GPU."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().fcg_context_create(device, C.byref(h)), "context create")
+        self._h = h
+
+    @property
+    def stream(self) -> int:
+        """The context's default cudaStream_t (as an integer handle)."""
+        return int(lib().fcg_context_stream(self._h) or 0)
+
+    def problem(self, model: Model, precision: int = PREC_MIXED, stream=None) -> Problem:
+        return Problem(self, model, precision, stream)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            lib().fcg_context_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def run_command_line(cmd: str) -> int:
+    """Run the headless console (reference command-line switches)."""
+    return int(lib().fcg_run_command_line(cmd.encode()))

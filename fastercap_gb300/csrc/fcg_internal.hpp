@@ -1,0 +1,57 @@
+// Internal interfaces between the C ABI layer (host/api.cpp) and the device
+// solver (csrc/problem.cu). Not installed; not part of the public header.
+#ifndef FCG_INTERNAL_HPP
+#define FCG_INTERNAL_HPP
+
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/fastercap_gb300.h"
+
+namespace fcg {
+
+// thread-local last error message
+void set_error(const std::string &msg);
+const char *get_error();
+
+struct DeviceProblem;
+
+// device context: one GPU
+struct DeviceContext {
+    int device = 0;
+    int sm_count = 0;
+    size_t free_bytes = 0, total_bytes = 0;
+    void *stream = nullptr;  // cudaStream_t owned by the context
+};
+void context_release(DeviceContext &ctx);
+
+int context_init(DeviceContext &ctx, int device);
+
+// problem lifetime
+int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out);
+void problem_destroy(DeviceProblem *p);
+int64_t problem_device_bytes(const DeviceProblem *p);
+int problem_fill(DeviceProblem *p);
+int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_coef);
+int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k);
+int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k);
+int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations);
+int problem_get_charges(DeviceProblem *p, double *charges);
+int problem_n_cond(const DeviceProblem *p);
+
+// timings of the last fill / solve in milliseconds (CUDA events on the problem's stream)
+struct SolveTimings {
+    float fill_ms = 0, solve_ms = 0, assemble_ms = 0;
+    int iterations_max = 0;
+    int64_t matvecs = 0;
+    int64_t launches = 0, link_launches = 0, link_bytes = 0;
+    double link_ms = 0;
+};
+SolveTimings problem_timings(const DeviceProblem *p);
+int problem_set_profiling(DeviceProblem *p, bool on);
+void problem_reset_stats(DeviceProblem *p);
+
+}  // namespace fcg
+
+#endif

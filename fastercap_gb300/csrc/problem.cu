@@ -1,0 +1,1271 @@
+// Device-resident capacitance problem for sm_103a: coefficient fill,
+// hierarchical matrix-vector product and batched preconditioned GMRES.
+//
+// Layout in HBM (uploaded once per model, see fcg_problem_create):
+//   geo[n_nodes]          80-byte NodeGeo records (vertices, centroid, normal,
+//                         type, max side, area): gathered by the fill kernels
+//   link_ptr[n_nodes+1]   int64 CSR offsets, links grouped by destination node
+//   link_src[n_links]     int32 source node of each link
+//   coef64 / coef32       link coefficients (FP64 path / mixed path)
+//   self[n_panels]        FP64 self coefficients (also the Jacobi diagonal)
+//   sweep plan            the node tree cut into subtrees of <= kBlockLeaves
+//                         leaves (one CTA each) plus the "top" nodes above them,
+//                         every group listed level by level
+// Matrix-vector product v = P q (CMultHier::MultiplyMatByVec_fast,
+// Solver/MultiplyHierarchical.cpp:285-304) for k right-hand sides at once:
+//   up_block/up_top     node charges Q(node) = Q(left) + Q(right)     (:72-127)
+//   spmv                P(node) = sum_l coef[l] * Q(src[l])           (:141-226)
+//   down_top/down_block A(node) = P(node) + A(parent); v = self*q + P + A(parent)
+//                                                                     (:231-283)
+// Node-indexed work arrays hold the k values of one node contiguously.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "fc_potential.h"
+#include "fcg_internal.hpp"
+
+namespace fcg {
+
+#define FCG_CK(call)                                                                         \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            set_error(std::string(#call) + " failed: " + cudaGetErrorString(e_));            \
+            return FCG_DEVICE_ERROR;                                                         \
+        }                                                                                    \
+    } while (0)
+
+static const int kBlockLeaves = 256;  // leaves per sweep subtree
+static const int kMaxK = 32;          // right-hand sides per matvec batch
+static const int kDotChunk = 1024;    // vector elements per CTA in the Krylov kernels
+
+struct __align__(16) NodeGeo {
+    float v[9];
+    float c[3];
+    float n[3];
+    uint32_t type;
+    double maxside;
+    double area;
+};
+
+// device allocation tracked against the problem's byte count
+template <class T> static int dalloc(T **p, size_t n, int64_t &bytes) {
+    *p = NULL;
+    if (n == 0) return FCG_NORMAL_END;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed: " + cudaGetErrorString(e));
+        *p = NULL;
+        return e == cudaErrorMemoryAllocation ? FCG_OUT_OF_MEMORY : FCG_DEVICE_ERROR;
+    }
+    bytes += (int64_t)(n * sizeof(T));
+    return FCG_NORMAL_END;
+}
+template <class T> static void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = NULL;
+}
+template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes, cudaStream_t s) {
+    int r = dalloc(p, n, bytes);
+    if (r != FCG_NORMAL_END) return r;
+    if (n) FCG_CK(cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    return FCG_NORMAL_END;
+}
+
+struct SweepPlan {
+    int n_blocks = 0, n_top_levels = 0, max_block_levels = 0;
+    int32_t *blk_leaf_first = NULL, *blk_nleaves = NULL, *blk_lvl_first = NULL, *blk_nlvls = NULL;
+    int32_t *lvl_ptr = NULL, *lvl_nodes = NULL;
+    int32_t *top_lvl_ptr = NULL, *top_nodes = NULL;
+};
+
+struct DeviceProblem {
+    DeviceContext *ctx = NULL;
+    int precision = FCG_PREC_FP64;
+    int64_t Nn = 0, Np = 0, L = 0;
+    int n_cond_all = 0;
+    std::vector<int> cond_cols;  // solver-order index of every non-dielectric conductor
+    std::vector<int64_t> cond_first, cond_count;
+    cudaStream_t stream = NULL;
+    bool owns_stream = false;
+    cudaEvent_t ev0 = NULL, ev1 = NULL;
+    int64_t bytes = 0;
+    bool filled = false;
+    SolveTimings timings;
+    // profiling of the link product: event pairs awaiting readout
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+
+    // model
+    NodeGeo *geo = NULL;
+    int64_t *link_ptr = NULL;
+    int32_t *link_src = NULL;
+    int32_t *leaf_node = NULL, *parent = NULL, *left = NULL, *right = NULL;
+    double *leaf_eb = NULL, *leaf_ea = NULL, *leaf_weight = NULL;
+    double *coef64 = NULL;
+    float *coef32 = NULL;
+    double *self = NULL;
+    unsigned *status = NULL;
+    SweepPlan plan;
+
+    // matvec workspace (kcap values per node)
+    int kcap = 0;
+    double *Qd = NULL, *Pd = NULL, *Ad = NULL;
+    float *Qf = NULL, *Pf = NULL;
+
+    // Krylov workspace
+    int gk = 0, gM = 0;  // right-hand sides, max iterations allocated
+    std::vector<double *> V;  // basis vectors, each [gk][Np]
+    double **Vptr = NULL;
+    int Vptr_cap = 0;
+    double *H = NULL, *cs = NULL, *sn = NULL, *g = NULL, *normb = NULL, *hnorm = NULL, *nrm2 = NULL, *z = NULL;
+    double *partial = NULL;
+    int partial_cap = 0;
+    int *active = NULL, *iters = NULL, *n_active = NULL;
+    int *h_n_active = NULL;
+    double *b = NULL, *x0 = NULL, *w = NULL, *vv = NULL, *x = NULL;
+    int x_k = 0;
+};
+
+// --------------------------------------------------------------- kernels
+
+__global__ void k_fill_links(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+                             const NodeGeo *__restrict__ geo, double *__restrict__ c64, float *__restrict__ c32,
+                             unsigned *status) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        const NodeGeo &g1 = geo[row];
+        unsigned t1 = g1.type;
+        float c1[3] = {g1.c[0], g1.c[1], g1.c[2]};
+        float n1[3] = {g1.n[0], g1.n[1], g1.n[2]};
+        double ms1 = g1.maxside;
+        int64_t s = ptr[row], e = ptr[row + 1];
+        for (int64_t l = s + lane; l < e; l += 32) {
+            const NodeGeo &g2 = geo[src[l]];
+            double val = fcg_pot_estimate(t1, c1, n1, ms1, g2.c, g2.v, g2.maxside);
+            if (!isfinite(val)) atomicOr(status, 1u);
+            if (c64) c64[l] = val;
+            if (c32) c32[l] = (float)val;
+        }
+    }
+}
+
+__global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
+                            const double *__restrict__ eb, const double *__restrict__ ea, double *__restrict__ self,
+                            unsigned *status) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
+        const NodeGeo &g = geo[leaf_node[j]];
+        double val = fcg_self_potential(g.type, g.c, g.v, g.area, eb[j], ea[j]);
+        if (!isfinite(val) || val == 0.0) atomicOr(status, 2u);
+        self[j] = val;
+    }
+}
+
+// Up-sweep over the sweep subtrees: leaves take the (optionally Jacobi
+// scaled) input, internal nodes add their children level by level.
+template <bool MIXED>
+__global__ void k_up_block(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
+                           const double *__restrict__ in, int64_t ld, int k, int kp, const double *__restrict__ diag,
+                           double *Qd, float *Qf, const int32_t *__restrict__ left_of, const int32_t *__restrict__ right_of) {
+    int b = blockIdx.x;
+    int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b];
+    for (int t = threadIdx.x; t < nl * k; t += blockDim.x) {
+        int i = t % nl, r = t / nl;
+        int j = lf + i;
+        double xv = in[(int64_t)r * ld + j];
+        if (diag) xv = xv / diag[j];
+        int64_t node = leaf_node[j];
+        Qd[node * kp + r] = xv;
+        if (MIXED) Qf[node * kp + r] = (float)xv;
+    }
+    __syncthreads();
+    int lv0 = plan.blk_lvl_first[b], nlv = plan.blk_nlvls[b];
+    for (int h = 0; h < nlv; h++) {
+        int a = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a;
+        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
+            int n = plan.lvl_nodes[a + t % cnt], r = t / cnt;
+            double s = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
+            Qd[(int64_t)n * kp + r] = s;
+            if (MIXED) Qf[(int64_t)n * kp + r] = (float)s;
+        }
+        __syncthreads();
+    }
+}
+
+template <bool MIXED>
+__global__ void k_up_top(const SweepPlan plan, int k, int kp, double *Qd, float *Qf, const int32_t *__restrict__ left_of,
+                         const int32_t *__restrict__ right_of) {
+    for (int h = 0; h < plan.n_top_levels; h++) {
+        int a = plan.top_lvl_ptr[h], e = plan.top_lvl_ptr[h + 1], cnt = e - a;
+        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
+            int n = plan.top_nodes[a + t % cnt], r = t / cnt;
+            double s = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
+            Qd[(int64_t)n * kp + r] = s;
+            if (MIXED) Qf[(int64_t)n * kp + r] = (float)s;
+        }
+        __syncthreads();
+    }
+}
+
+template <class TP>
+__global__ void k_down_top(const SweepPlan plan, int k, int kp, const TP *__restrict__ P, double *A,
+                           const int32_t *__restrict__ parent) {
+    for (int h = plan.n_top_levels - 1; h >= 0; h--) {
+        int a = plan.top_lvl_ptr[h], e = plan.top_lvl_ptr[h + 1], cnt = e - a;
+        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
+            int n = plan.top_nodes[a + t % cnt], r = t / cnt;
+            int p = parent[n];
+            double acc = (double)P[(int64_t)n * kp + r];
+            if (p >= 0) acc = acc + A[(int64_t)p * kp + r];
+            A[(int64_t)n * kp + r] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+template <class TP>
+__global__ void k_down_block(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const double *__restrict__ in,
+                             int64_t ld, int k, int kp, const double *__restrict__ diag, const double *__restrict__ self,
+                             const TP *__restrict__ P, double *A, const int32_t *__restrict__ parent,
+                             double *__restrict__ out) {
+    int b = blockIdx.x;
+    int lv0 = plan.blk_lvl_first[b], nlv = plan.blk_nlvls[b];
+    for (int h = nlv - 1; h >= 0; h--) {
+        int a = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a;
+        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
+            int n = plan.lvl_nodes[a + t % cnt], r = t / cnt;
+            int p = parent[n];
+            double acc = (double)P[(int64_t)n * kp + r];
+            if (p >= 0) acc = acc + A[(int64_t)p * kp + r];
+            A[(int64_t)n * kp + r] = acc;
+        }
+        __syncthreads();
+    }
+    int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b];
+    for (int t = threadIdx.x; t < nl * k; t += blockDim.x) {
+        int i = t % nl, r = t / nl;
+        int j = lf + i;
+        double xv = in[(int64_t)r * ld + j];
+        if (diag) xv = xv / diag[j];
+        int64_t node = leaf_node[j];
+        int p = parent[node];
+        double v = self[j] * xv + (double)P[node * kp + r];
+        if (p >= 0) v = v + A[(int64_t)p * kp + r];
+        out[(int64_t)r * ld + j] = v;
+    }
+}
+
+// Link product, FP64: one warp per destination node, lanes stride over the
+// node's links, K right-hand sides per link.
+template <int K>
+__global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+                         const double *__restrict__ coef, const double *__restrict__ Q, double *__restrict__ P) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        double acc[K];
+#pragma unroll
+        for (int r = 0; r < K; r++) acc[r] = 0.0;
+        int64_t s = ptr[row], e = ptr[row + 1];
+        for (int64_t l = s + lane; l < e; l += 32) {
+            double c = coef[l];
+            const double *q = Q + (int64_t)src[l] * K;
+#pragma unroll
+            for (int r = 0; r < K; r++) acc[r] += c * q[r];
+        }
+#pragma unroll
+        for (int r = 0; r < K; r++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+        }
+#pragma unroll
+        for (int r = 0; r < K; r++)
+            if (lane == (r & 31)) P[row * K + r] = acc[r];
+    }
+}
+
+// compensated FP32 accumulation (Kahan-Babuska / Neumaier)
+struct KSum {
+    float s, c;
+};
+__device__ __forceinline__ void kadd(KSum &a, float x) {
+    float t = a.s + x;
+    if (fabsf(a.s) >= fabsf(x)) a.c += (a.s - t) + x;
+    else a.c += (x - t) + a.s;
+    a.s = t;
+}
+
+// Link product, mixed: FP32 coefficients and charges, compensated FP32 sums.
+template <int K>
+__global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+                         const float *__restrict__ coef, const float *__restrict__ Q, float *__restrict__ P) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        KSum acc[K];
+#pragma unroll
+        for (int r = 0; r < K; r++) { acc[r].s = 0.f; acc[r].c = 0.f; }
+        int64_t s = ptr[row], e = ptr[row + 1];
+        for (int64_t l = s + lane; l < e; l += 32) {
+            float c = coef[l];
+            const float *q = Q + (int64_t)src[l] * K;
+#pragma unroll
+            for (int r = 0; r < K; r++) kadd(acc[r], c * q[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < K; r++) {
+            KSum a = acc[r];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                float os = __shfl_xor_sync(0xffffffffu, a.s, o);
+                float oc = __shfl_xor_sync(0xffffffffu, a.c, o);
+                a.c += oc;
+                kadd(a, os);
+            }
+            acc[r] = a;
+        }
+#pragma unroll
+        for (int r = 0; r < K; r++)
+            if (lane == (r & 31)) P[row * K + r] = acc[r].s + acc[r].c;
+    }
+}
+
+// ---- Krylov kernels: vectors are [k][ld] with ld = n_panels
+
+__global__ void k_set_rhs(int64_t Np, int k, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
+                          double *__restrict__ b) {
+    int64_t n = (int64_t)k * Np;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / Np);
+        int64_t j = t - (int64_t)r * Np;
+        b[t] = (j >= first[r] && j < first[r] + count[r]) ? 1.0 : 0.0;
+    }
+}
+
+// y = a / diag (Jacobi) or a copy
+__global__ void k_precond(int64_t Np, int k, const double *__restrict__ a, const double *__restrict__ diag, double *__restrict__ y) {
+    int64_t n = (int64_t)k * Np;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t j = t % Np;
+        y[t] = diag ? a[t] / diag[j] : a[t];
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+    if (w == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// partial[(r*nvec + j)*nch + chunk] = <Vj[r] chunk, w[r] chunk>
+__global__ void k_dots(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w,
+                       const int *__restrict__ active, double *__restrict__ partial) {
+    __shared__ double sh[32];
+    int r = blockIdx.y, ch = blockIdx.x, nch = gridDim.x;
+    if (active && !active[r]) return;
+    int64_t base = (int64_t)ch * kDotChunk;
+    double wv[kDotChunk / 256];
+#pragma unroll
+    for (int u = 0; u < kDotChunk / 256; u++) {
+        int64_t j = base + threadIdx.x + u * 256;
+        wv[u] = (j < Np) ? w[(int64_t)r * Np + j] : 0.0;
+    }
+    for (int jv = 0; jv < nvec; jv++) {
+        const double *v = Vp[jv] + (int64_t)r * Np;
+        double s = 0.0;
+#pragma unroll
+        for (int u = 0; u < kDotChunk / 256; u++) {
+            int64_t j = base + threadIdx.x + u * 256;
+            if (j < Np) s += v[j] * wv[u];
+        }
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) partial[((int64_t)r * nvec + jv) * nch + ch] = s;
+    }
+}
+
+// out[(r*nvec + j)*ostride + ooff] = sum over chunks
+__global__ void k_reduce_partials(int nvec, int nch, const double *__restrict__ partial, const int *__restrict__ active,
+                                  double *__restrict__ out, int64_t ostride_r, int64_t ostride_j) {
+    __shared__ double sh[32];
+    int j = blockIdx.x, r = blockIdx.y;
+    if (active && !active[r]) return;
+    double s = 0.0;
+    for (int c = threadIdx.x; c < nch; c += blockDim.x) s += partial[((int64_t)r * nvec + j) * nch + c];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[r * ostride_r + j * ostride_j] = s;
+}
+
+// v[r] = w[r] - sum_j h_j V_j[r]; partial sums of |v|^2
+__global__ void k_update(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w,
+                         const double *__restrict__ H, int64_t hstride_r, const int *__restrict__ active,
+                         double *__restrict__ v, double *__restrict__ partial) {
+    __shared__ double sh[32];
+    int r = blockIdx.y, ch = blockIdx.x, nch = gridDim.x;
+    if (active && !active[r]) return;
+    const double *h = H + r * hstride_r;
+    double s2 = 0.0;
+    for (int u = 0; u < kDotChunk / 256; u++) {
+        int64_t j = (int64_t)ch * kDotChunk + threadIdx.x + u * 256;
+        if (j >= Np) break;
+        double x = w[(int64_t)r * Np + j];
+        for (int jv = 0; jv < nvec; jv++) x = x - h[jv] * Vp[jv][(int64_t)r * Np + j];
+        v[(int64_t)r * Np + j] = x;
+        s2 += x * x;
+    }
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) partial[(int64_t)r * nch + ch] = s2;
+}
+
+// Givens update of column i of every active right-hand side (one thread each)
+__global__ void k_givens(int k, int i, int M, double *H, double *cs, double *sn, double *g, const double *normb,
+                         const double *nrm2, double *hnorm, double tol, int *active, int *iters, int *n_active) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) *n_active = 0;
+    __syncthreads();
+    if (r >= k) return;
+    if (!active[r]) return;
+    double *hc = H + ((int64_t)r * (M + 1) + i) * (M + 2);
+    double *c = cs + (int64_t)r * (M + 2), *s = sn + (int64_t)r * (M + 2), *gg = g + (int64_t)r * (M + 2);
+    double hn = sqrt(nrm2[r]);
+    hnorm[r] = hn;
+    hc[i + 1] = hn;
+    for (int j = 0; j < i; j++) {
+        double t1 = hc[j], t2 = hc[j + 1];
+        hc[j] = c[j] * t1 - s[j] * t2;
+        hc[j + 1] = c[j] * t2 + s[j] * t1;
+    }
+    double t1 = hc[i], t2 = hc[i + 1];
+    double len = sqrt(t1 * t1 + t2 * t2);
+    c[i] = t1 / len;
+    s[i] = -t2 / len;
+    hc[i] = c[i] * t1 - s[i] * t2;
+    hc[i + 1] = 0;
+    t1 = gg[i];
+    gg[i] = c[i] * t1;
+    gg[i + 1] = s[i] * t1;
+    double res = fabs(gg[i + 1]) / normb[r];
+    if (res < tol) {
+        active[r] = 0;
+        iters[r] = i;
+    } else {
+        atomicAdd(n_active, 1);
+    }
+}
+
+__global__ void k_scale(int64_t Np, int k, const double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
+                        double *__restrict__ out) {
+    int64_t n = (int64_t)k * Np;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / Np);
+        if (active && !active[r]) continue;
+        out[t] = v[t] / hn[r];
+    }
+}
+
+// back substitution R z = g for every right-hand side (one thread each)
+__global__ void k_backsub(int k, int M, const double *H, const double *g, const int *iters, double *z) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    int it = iters[r];
+    double *zz = z + (int64_t)r * (M + 2);
+    const double *gg = g + (int64_t)r * (M + 2);
+    for (int i = 0; i <= it; i++) zz[i] = gg[i];
+    for (int i = it; i >= 0; i--) {
+        const double *hc = H + ((int64_t)r * (M + 1) + i) * (M + 2);
+        zz[i] = zz[i] / hc[i];
+        for (int j = i - 1; j >= 0; j--) zz[j] = zz[j] - hc[j] * zz[i];
+    }
+}
+
+// y[r] = sum_{j <= iters[r]} z_j V_j[r]
+__global__ void k_combine(int64_t Np, int k, int M, double *const *__restrict__ Vp, const double *__restrict__ z,
+                          const int *__restrict__ iters, double *__restrict__ y) {
+    int64_t n = (int64_t)k * Np;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / Np);
+        int64_t j = t - (int64_t)r * Np;
+        int it = iters[r];
+        double s = 0.0;
+        for (int jv = 0; jv <= it; jv++) s += Vp[jv][(int64_t)r * Np + j] * z[(int64_t)r * (M + 2) + jv];
+        y[t] = s;
+    }
+}
+
+// x = x0 + P y (or x0 alone when the initial guess already met the tolerance)
+__global__ void k_finish(int64_t Np, int k, const double *__restrict__ x0, const double *__restrict__ y,
+                         const double *__restrict__ diag, const int *__restrict__ iters, double *__restrict__ x) {
+    int64_t n = (int64_t)k * Np;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / Np);
+        int64_t j = t - (int64_t)r * Np;
+        if (iters[r] < 0) { x[t] = x0[t]; continue; }
+        double py = diag ? y[t] / diag[j] : y[t];
+        x[t] = x0[t] + py;
+    }
+}
+
+// r = b - w, and partial norms of r and b
+__global__ void k_residual(int64_t Np, const double *__restrict__ b, const double *__restrict__ wv, double *__restrict__ r,
+                           double *__restrict__ pr, double *__restrict__ pb) {
+    __shared__ double sh[32];
+    int rr = blockIdx.y, ch = blockIdx.x, nch = gridDim.x;
+    double s1 = 0.0, s2 = 0.0;
+    for (int u = 0; u < kDotChunk / 256; u++) {
+        int64_t j = (int64_t)ch * kDotChunk + threadIdx.x + u * 256;
+        if (j >= Np) break;
+        int64_t t = (int64_t)rr * Np + j;
+        double bb = b[t];
+        double x = wv ? bb - wv[t] : bb;
+        r[t] = x;
+        s1 += x * x;
+        s2 += bb * bb;
+    }
+    s1 = block_sum(s1, sh);
+    if (threadIdx.x == 0) pr[(int64_t)rr * nch + ch] = s1;
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) pb[(int64_t)rr * nch + ch] = s2;
+}
+
+__global__ void k_init_state(int k, int M, double *nr2, double *nb2, double *normb, double *g, double *hn, double tol,
+                             int *active, int *iters) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    double nr = sqrt(nr2[r]), nb = sqrt(nb2[r]);
+    normb[r] = nb;
+    g[(int64_t)r * (M + 2)] = nr;
+    hn[r] = nr;
+    if (nr / nb < tol) { active[r] = 0; iters[r] = -1; }
+    else { active[r] = 1; iters[r] = 0; }
+}
+
+// cap[r][c] = sum over conductor c's leaves of weight * charge
+__global__ void k_assemble(int64_t Np, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
+                           const double *__restrict__ weight, const double *__restrict__ x, int ncol, double *__restrict__ cap) {
+    __shared__ double sh[32];
+    int c = blockIdx.x, r = blockIdx.y;
+    double s = 0.0;
+    for (int64_t j = first[c] + threadIdx.x; j < first[c] + count[c]; j += blockDim.x) s += weight[j] * x[(int64_t)r * Np + j];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) cap[(int64_t)r * ncol + c] = s;
+}
+
+// -------------------------------------------------------------- host side
+
+static int grid_for(int64_t n, int threads, int sms) {
+    int64_t g = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+int context_init(DeviceContext &ctx, int device) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error(std::string("no CUDA device available: ") + (e == cudaSuccess ? "zero devices" : cudaGetErrorString(e)));
+        return FCG_DEVICE_ERROR;
+    }
+    if (device < 0 || device >= n) { set_error("device index out of range"); return FCG_DEVICE_ERROR; }
+    FCG_CK(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    FCG_CK(cudaGetDeviceProperties(&prop, device));
+    ctx.device = device;
+    ctx.sm_count = prop.multiProcessorCount;
+    FCG_CK(cudaMemGetInfo(&ctx.free_bytes, &ctx.total_bytes));
+    cudaStream_t st;
+    FCG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    ctx.stream = (void *)st;
+    return FCG_NORMAL_END;
+}
+
+void context_release(DeviceContext &ctx) {
+    if (ctx.stream) {
+        cudaSetDevice(ctx.device);
+        cudaStreamSynchronize((cudaStream_t)ctx.stream);
+        cudaStreamDestroy((cudaStream_t)ctx.stream);
+        ctx.stream = nullptr;
+    }
+}
+
+static std::string validate(const fcg_model_arrays &a) {
+    if (a.n_nodes <= 0 || a.n_panels <= 0 || a.n_links < 0 || a.n_conductors <= 0) return "empty model";
+    if (a.n_nodes > 0x7fffffffLL || a.n_links > 0x7fffffffLL) return "model too large for 32-bit indices";
+    if (!a.node_type || !a.node_left || !a.node_right || !a.node_leaf_first || !a.node_leaf_count || !a.node_vertices ||
+        !a.node_centroid || !a.node_normal || !a.node_area || !a.node_maxside || !a.link_ptr || (a.n_links && !a.link_src) ||
+        !a.leaf_diel || !a.cond_is_diel || !a.cond_leaf_first || !a.cond_leaf_count || !a.cond_outperm || !a.cond_inperm ||
+        !a.cond_surf_ptr || !a.cond_surf_outperm)
+        return "null model array";
+    if (a.link_ptr[0] != 0 || a.link_ptr[a.n_nodes] != a.n_links) return "link_ptr does not span the links";
+    int64_t leaves = 0;
+    for (int64_t i = 0; i < a.n_nodes; i++) {
+        if (a.link_ptr[i + 1] < a.link_ptr[i]) return "link_ptr not monotone";
+        bool leaf = a.node_type[i] & FCG_IS_LEAF;
+        if (leaf) {
+            if (a.node_left[i] != -1 || a.node_right[i] != -1 || a.node_leaf_count[i] != 1) return "bad leaf node";
+            leaves++;
+        } else {
+            int32_t l = a.node_left[i], r = a.node_right[i];
+            if (l < 0 || r < 0 || l >= i || r >= i) return "children must precede their parent (post-order)";
+            if (a.node_leaf_count[i] != a.node_leaf_count[l] + a.node_leaf_count[r]) return "inconsistent leaf counts";
+            if (a.node_leaf_first[i] != a.node_leaf_first[l] || a.node_leaf_first[r] != a.node_leaf_first[l] + a.node_leaf_count[l])
+                return "leaf ranges are not contiguous";
+        }
+        if (a.node_leaf_first[i] < 0 || a.node_leaf_first[i] + a.node_leaf_count[i] > a.n_panels) return "leaf range out of bounds";
+    }
+    if (leaves != a.n_panels) return "leaf count does not match n_panels";
+    for (int64_t l = 0; l < a.n_links; l++)
+        if (a.link_src[l] < 0 || a.link_src[l] >= a.n_nodes) return "link source out of range";
+    int64_t next = 0;
+    for (int32_t c = 0; c < a.n_conductors; c++) {
+        if (a.cond_leaf_first[c] != next || a.cond_leaf_count[c] <= 0) return "conductor leaf ranges must tile the leaves";
+        next += a.cond_leaf_count[c];
+        if (a.cond_surf_ptr[c + 1] < a.cond_surf_ptr[c]) return "cond_surf_ptr not monotone";
+        if (!a.cond_is_diel[c]) {
+            int32_t ns = a.cond_surf_ptr[c + 1] - a.cond_surf_ptr[c];
+            for (int64_t j = a.cond_leaf_first[c]; j < a.cond_leaf_first[c] + a.cond_leaf_count[c]; j++)
+                if (a.leaf_diel[j] >= ns) return "leaf permittivity index out of range";
+        } else if (a.cond_outperm[c] == a.cond_inperm[c]) {
+            return "dielectric interface with equal permittivities";
+        }
+    }
+    if (next != a.n_panels) return "conductor leaf ranges must tile the leaves";
+    return "";
+}
+
+// Cut the node forest into subtrees of at most kBlockLeaves leaves (one CTA
+// each in the sweep kernels) and the top nodes above them, each listed by
+// height so that children are processed before parents.
+static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::vector<int32_t> &parent, cudaStream_t s) {
+    int64_t Nn = a.n_nodes;
+    std::vector<int32_t> height(Nn, 0);
+    for (int64_t i = 0; i < Nn; i++)
+        if (!(a.node_type[i] & FCG_IS_LEAF)) height[i] = 1 + std::max(height[a.node_left[i]], height[a.node_right[i]]);
+    std::vector<int32_t> blk_leaf_first, blk_nleaves, blk_lvl_first, blk_nlvls, lvl_ptr, lvl_nodes;
+    std::vector<int32_t> top_cnt;
+    std::vector<std::vector<int32_t>> top_by_h;
+    int max_lv = 0;
+    for (int64_t i = 0; i < Nn; i++) {
+        int64_t lc = a.node_leaf_count[i];
+        int32_t par = parent[i];
+        if (lc > kBlockLeaves) {
+            if ((int)top_by_h.size() <= height[i]) top_by_h.resize(height[i] + 1);
+            top_by_h[height[i]].push_back((int32_t)i);
+            continue;
+        }
+        if (par >= 0 && a.node_leaf_count[par] <= kBlockLeaves) continue;  // not a subtree root
+        // subtree root: nodes [i - (2*lc - 1) + 1, i] in post-order
+        int64_t first = i - (2 * lc - 1) + 1;
+        int H = height[i];
+        blk_leaf_first.push_back((int32_t)a.node_leaf_first[i]);
+        blk_nleaves.push_back((int32_t)lc);
+        blk_lvl_first.push_back((int32_t)lvl_ptr.size());
+        blk_nlvls.push_back(H);
+        std::vector<std::vector<int32_t>> byh(H + 1);
+        for (int64_t n = first; n <= i; n++)
+            if (!(a.node_type[n] & FCG_IS_LEAF)) byh[height[n]].push_back((int32_t)n);
+        for (int h = 1; h <= H; h++) {
+            lvl_ptr.push_back((int32_t)lvl_nodes.size());
+            lvl_nodes.insert(lvl_nodes.end(), byh[h].begin(), byh[h].end());
+        }
+        lvl_ptr.push_back((int32_t)lvl_nodes.size());
+        max_lv = std::max(max_lv, H);
+    }
+    // lvl_ptr holds, per block, H+1 offsets; blk_lvl_first indexes into it
+    std::vector<int32_t> top_lvl_ptr(1, 0), top_nodes;
+    for (size_t h = 0; h < top_by_h.size(); h++) {
+        if (top_by_h[h].empty()) continue;
+        top_nodes.insert(top_nodes.end(), top_by_h[h].begin(), top_by_h[h].end());
+        top_lvl_ptr.push_back((int32_t)top_nodes.size());
+    }
+    SweepPlan &pl = p->plan;
+    pl.n_blocks = (int)blk_leaf_first.size();
+    pl.n_top_levels = (int)top_lvl_ptr.size() - 1;
+    pl.max_block_levels = max_lv;
+    int r;
+    if ((r = upload(&pl.blk_leaf_first, blk_leaf_first.data(), blk_leaf_first.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.blk_nleaves, blk_nleaves.data(), blk_nleaves.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.blk_lvl_first, blk_lvl_first.data(), blk_lvl_first.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.blk_nlvls, blk_nlvls.data(), blk_nlvls.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.lvl_ptr, lvl_ptr.data(), lvl_ptr.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.lvl_nodes, lvl_nodes.data(), lvl_nodes.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.top_lvl_ptr, top_lvl_ptr.data(), top_lvl_ptr.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.top_nodes, top_nodes.data(), top_nodes.size(), p->bytes, s))) return r;
+    return FCG_NORMAL_END;
+}
+
+int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out) {
+    *out = NULL;
+    std::string bad = validate(a);
+    if (!bad.empty()) { set_error("invalid model: " + bad); return FCG_GENERIC_ERROR; }
+    if (precision != FCG_PREC_FP64 && precision != FCG_PREC_MIXED) { set_error("unknown precision"); return FCG_GENERIC_ERROR; }
+    FCG_CK(cudaSetDevice(ctx.device));
+    DeviceProblem *p = new DeviceProblem();
+    p->ctx = &ctx;
+    p->precision = precision;
+    p->Nn = a.n_nodes;
+    p->Np = a.n_panels;
+    p->L = a.n_links;
+    p->n_cond_all = a.n_conductors;
+    for (int32_t c = 0; c < a.n_conductors; c++) {
+        if (!a.cond_is_diel[c]) p->cond_cols.push_back(c);
+        p->cond_first.push_back(a.cond_leaf_first[c]);
+        p->cond_count.push_back(a.cond_leaf_count[c]);
+    }
+    int r = FCG_NORMAL_END;
+#define FCG_TRY(x) do { if ((r = (x)) != FCG_NORMAL_END) { problem_destroy(p); return r; } } while (0)
+    if (stream) {
+        p->stream = (cudaStream_t)stream;
+    } else {
+        p->owns_stream = true;
+        if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) p->stream = NULL;
+    }
+    if (!p->stream || cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess) {
+        set_error("cannot create stream/events");
+        problem_destroy(p);
+        return FCG_DEVICE_ERROR;
+    }
+    cudaStream_t s = p->stream;
+    int64_t Nn = a.n_nodes, Np = a.n_panels;
+    std::vector<NodeGeo> geo(Nn);
+    for (int64_t i = 0; i < Nn; i++) {
+        NodeGeo &g = geo[i];
+        memcpy(g.v, a.node_vertices + 9 * i, 36);
+        memcpy(g.c, a.node_centroid + 3 * i, 12);
+        memcpy(g.n, a.node_normal + 3 * i, 12);
+        g.type = a.node_type[i];
+        g.maxside = a.node_maxside[i];
+        g.area = a.node_area[i];
+    }
+    std::vector<int32_t> parent(Nn, -1), leaf_node(Np, -1);
+    for (int64_t i = 0; i < Nn; i++) {
+        if (a.node_type[i] & FCG_IS_LEAF) leaf_node[a.node_leaf_first[i]] = (int32_t)i;
+        else { parent[a.node_left[i]] = (int32_t)i; parent[a.node_right[i]] = (int32_t)i; }
+    }
+    std::vector<double> eb(Np, 0.0), ea(Np, 0.0), weight(Np, 0.0);
+    for (int32_t c = 0; c < a.n_conductors; c++) {
+        for (int64_t j = a.cond_leaf_first[c]; j < a.cond_leaf_first[c] + a.cond_leaf_count[c]; j++) {
+            if (a.cond_is_diel[c]) { eb[j] = a.cond_outperm[c]; ea[j] = a.cond_inperm[c]; }
+            else weight[j] = a.cond_surf_outperm[a.cond_surf_ptr[c] + a.leaf_diel[j]];
+        }
+    }
+    FCG_TRY(upload(&p->geo, geo.data(), Nn, p->bytes, s));
+    FCG_TRY(upload(&p->link_ptr, a.link_ptr, Nn + 1, p->bytes, s));
+    FCG_TRY(upload(&p->link_src, a.link_src, a.n_links, p->bytes, s));
+    FCG_TRY(upload(&p->leaf_node, leaf_node.data(), Np, p->bytes, s));
+    FCG_TRY(upload(&p->parent, parent.data(), Nn, p->bytes, s));
+    FCG_TRY(upload(&p->leaf_eb, eb.data(), Np, p->bytes, s));
+    FCG_TRY(upload(&p->leaf_ea, ea.data(), Np, p->bytes, s));
+    FCG_TRY(upload(&p->leaf_weight, weight.data(), Np, p->bytes, s));
+    FCG_TRY(dalloc(&p->self, Np, p->bytes));
+    if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
+    else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
+    FCG_TRY(dalloc(&p->status, 1, p->bytes));
+    FCG_TRY(build_plan(p, a, parent, s));
+    FCG_TRY(upload(&p->left, a.node_left, Nn, p->bytes, s));
+    FCG_TRY(upload(&p->right, a.node_right, Nn, p->bytes, s));
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+        set_error(std::string("upload failed: ") + cudaGetErrorString(cudaGetLastError()));
+        problem_destroy(p);
+        return FCG_DEVICE_ERROR;
+    }
+    *out = p;
+    return FCG_NORMAL_END;
+#undef FCG_TRY
+}
+
+void problem_destroy(DeviceProblem *p) {
+    if (!p) return;
+    cudaSetDevice(p->ctx->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
+    dfree(p->left); dfree(p->right); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
+    dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
+    SweepPlan &pl = p->plan;
+    dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls);
+    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
+    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf);
+    for (size_t i = 0; i < p->V.size(); i++) dfree(p->V[i]);
+    dfree(p->Vptr); dfree(p->H); dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->normb); dfree(p->hnorm);
+    dfree(p->nrm2); dfree(p->z); dfree(p->partial); dfree(p->active); dfree(p->iters); dfree(p->n_active);
+    dfree(p->b); dfree(p->x0); dfree(p->w); dfree(p->vv); dfree(p->x);
+    if (p->h_n_active) cudaFreeHost(p->h_n_active);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    for (size_t i = 0; i < p->ev_pool.size(); i++) cudaEventDestroy(p->ev_pool[i]);
+    if (p->stream && p->owns_stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+int64_t problem_device_bytes(const DeviceProblem *p) { return p ? p->bytes : 0; }
+int problem_n_cond(const DeviceProblem *p) { return p ? (int)p->cond_cols.size() : 0; }
+SolveTimings problem_timings(const DeviceProblem *p) { return p ? p->timings : SolveTimings(); }
+
+int problem_set_profiling(DeviceProblem *p, bool on) {
+    p->profiling = on;
+    return FCG_NORMAL_END;
+}
+
+void problem_reset_stats(DeviceProblem *p) {
+    p->timings.launches = p->timings.link_launches = p->timings.link_bytes = 0;
+    p->timings.link_ms = 0;
+    p->timings.matvecs = 0;
+}
+
+// event pair around one link-product launch (profiling mode)
+static void prof_begin(DeviceProblem *p) {
+    if (!p->profiling) return;
+    if (p->ev_used + 2 > p->ev_pool.size()) {
+        for (int i = 0; i < 64; i++) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            p->ev_pool.push_back(e);
+        }
+    }
+    cudaEventRecord(p->ev_pool[p->ev_used], p->stream);
+}
+static void prof_end(DeviceProblem *p) {
+    if (!p->profiling || p->ev_used + 2 > p->ev_pool.size()) return;
+    cudaEventRecord(p->ev_pool[p->ev_used + 1], p->stream);
+    p->ev_used += 2;
+}
+// read the recorded pairs (the stream must be synchronised)
+static void prof_collect(DeviceProblem *p) {
+    for (size_t i = 0; i + 1 < p->ev_used; i += 2) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p->ev_pool[i], p->ev_pool[i + 1]) == cudaSuccess) p->timings.link_ms += ms;
+    }
+    p->ev_used = 0;
+}
+
+static int check_status(DeviceProblem *p, const char *what) {
+    unsigned st = 0;
+    FCG_CK(cudaMemcpyAsync(&st, p->status, sizeof(unsigned), cudaMemcpyDeviceToHost, p->stream));
+    FCG_CK(cudaStreamSynchronize(p->stream));
+    if (st) {
+        set_error(std::string(what) + ": non-finite or zero coefficient (status " + std::to_string(st) + ")");
+        return FCG_GENERIC_ERROR;
+    }
+    return FCG_NORMAL_END;
+}
+
+int problem_fill(DeviceProblem *p) {
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    cudaStream_t s = p->stream;
+    FCG_CK(cudaMemsetAsync(p->status, 0, sizeof(unsigned), s));
+    FCG_CK(cudaEventRecord(p->ev0, s));
+    int sms = p->ctx->sm_count;
+    if (p->L > 0) {
+        int64_t warps = p->Nn;
+        int grid = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)sms * 32);
+        k_fill_links<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->coef32, p->status);
+        FCG_CK(cudaGetLastError());
+        p->timings.launches++;
+    }
+    k_fill_self<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->leaf_eb, p->leaf_ea, p->self, p->status);
+    FCG_CK(cudaGetLastError());
+    p->timings.launches++;
+    FCG_CK(cudaEventRecord(p->ev1, s));
+    int r = check_status(p, "coefficient fill");
+    cudaEventElapsedTime(&p->timings.fill_ms, p->ev0, p->ev1);
+    if (r != FCG_NORMAL_END) return r;
+    p->filled = true;
+    return FCG_NORMAL_END;
+}
+
+int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_coef) {
+    if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    if (link_coef && p->L) {
+        if (p->coef64) {
+            FCG_CK(cudaMemcpyAsync(link_coef, p->coef64, p->L * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+            FCG_CK(cudaStreamSynchronize(p->stream));
+        } else {
+            std::vector<float> tmp(p->L);
+            FCG_CK(cudaMemcpyAsync(tmp.data(), p->coef32, p->L * sizeof(float), cudaMemcpyDeviceToHost, p->stream));
+            FCG_CK(cudaStreamSynchronize(p->stream));
+            for (int64_t l = 0; l < p->L; l++) link_coef[l] = tmp[l];
+        }
+    }
+    if (self_coef) {
+        FCG_CK(cudaMemcpyAsync(self_coef, p->self, p->Np * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+        FCG_CK(cudaStreamSynchronize(p->stream));
+    }
+    return FCG_NORMAL_END;
+}
+
+static int kpad(int k) {
+    int kp = 1;
+    while (kp < k) kp <<= 1;
+    return kp;
+}
+
+static int ensure_matvec_ws(DeviceProblem *p, int kp) {
+    if (p->kcap >= kp) return FCG_NORMAL_END;
+    int64_t before = p->bytes;
+    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf);
+    p->bytes = before - (int64_t)p->kcap * p->Nn * (p->precision == FCG_PREC_FP64 ? 24 : 24);
+    p->kcap = 0;
+    int r;
+    size_t n = (size_t)p->Nn * kp;
+    if ((r = dalloc(&p->Qd, n, p->bytes))) return r;
+    if ((r = dalloc(&p->Ad, n, p->bytes))) return r;
+    if (p->precision == FCG_PREC_FP64) {
+        if ((r = dalloc(&p->Pd, n, p->bytes))) return r;
+    } else {
+        if ((r = dalloc(&p->Qf, n, p->bytes))) return r;
+        if ((r = dalloc(&p->Pf, n, p->bytes))) return r;
+    }
+    p->kcap = kp;
+    return FCG_NORMAL_END;
+}
+
+// v = P * (in / diag) for k right-hand sides ([k][Np] device arrays)
+static int matvec(DeviceProblem *p, const double *in, double *out, int k, const double *diag) {
+    if (k < 1 || k > kMaxK) { set_error("right-hand sides per matvec must be in [1, 32]"); return FCG_GENERIC_ERROR; }
+    int kp = kpad(k);
+    int r = ensure_matvec_ws(p, kp);
+    if (r != FCG_NORMAL_END) return r;
+    cudaStream_t s = p->stream;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    const SweepPlan &pl = p->plan;
+    int64_t Np = p->Np;
+    if (kp != k) {
+        // padded right-hand sides carry zeros
+        FCG_CK(cudaMemsetAsync(p->Qd, 0, (size_t)p->Nn * kp * sizeof(double), s));
+        if (mixed) FCG_CK(cudaMemsetAsync(p->Qf, 0, (size_t)p->Nn * kp * sizeof(float), s));
+    }
+    if (mixed) k_up_block<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, in, Np, k, kp, diag, p->Qd, p->Qf, p->left, p->right);
+    else k_up_block<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, in, Np, k, kp, diag, p->Qd, p->Qf, p->left, p->right);
+    FCG_CK(cudaGetLastError());
+    if (pl.n_top_levels > 0) {
+        if (mixed) k_up_top<true><<<1, 1024, 0, s>>>(pl, k, kp, p->Qd, p->Qf, p->left, p->right);
+        else k_up_top<false><<<1, 1024, 0, s>>>(pl, k, kp, p->Qd, p->Qf, p->left, p->right);
+        FCG_CK(cudaGetLastError());
+    }
+    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
+    int64_t launches = 2 + (pl.n_top_levels > 0 ? 2 : 0);
+    if (p->L > 0) {
+        int64_t cb = mixed ? 4 : 8;
+        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + 2 * cb * (int64_t)k * p->Nn;
+        p->timings.link_launches++;
+        launches++;
+        prof_begin(p);
+        if (!mixed) {
+            switch (kp) {
+            case 1: k_spmv64<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
+            case 2: k_spmv64<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
+            case 4: k_spmv64<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
+            case 8: k_spmv64<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
+            case 16: k_spmv64<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
+            default: k_spmv64<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
+            }
+        } else {
+            switch (kp) {
+            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            }
+        }
+        prof_end(p);
+        FCG_CK(cudaGetLastError());
+    } else {
+        if (mixed) FCG_CK(cudaMemsetAsync(p->Pf, 0, (size_t)p->Nn * kp * sizeof(float), s));
+        else FCG_CK(cudaMemsetAsync(p->Pd, 0, (size_t)p->Nn * kp * sizeof(double), s));
+    }
+    if (pl.n_top_levels > 0) {
+        if (mixed) k_down_top<float><<<1, 1024, 0, s>>>(pl, k, kp, p->Pf, p->Ad, p->parent);
+        else k_down_top<double><<<1, 1024, 0, s>>>(pl, k, kp, p->Pd, p->Ad, p->parent);
+        FCG_CK(cudaGetLastError());
+    }
+    if (mixed) k_down_block<float><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, p->Pf, p->Ad, p->parent, out);
+    else k_down_block<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, p->Pd, p->Ad, p->parent, out);
+    FCG_CK(cudaGetLastError());
+    p->timings.matvecs++;
+    p->timings.launches += launches;
+    return FCG_NORMAL_END;
+}
+
+int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k) {
+    if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    int r = matvec(p, d_q, d_v, k, NULL);
+    if (r != FCG_NORMAL_END) return r;
+    FCG_CK(cudaStreamSynchronize(p->stream));
+    prof_collect(p);
+    return FCG_NORMAL_END;
+}
+
+int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k) {
+    if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    double *dq = NULL, *dv = NULL;
+    int64_t tmp = 0;
+    size_t n = (size_t)k * p->Np;
+    int r = dalloc(&dq, n, tmp);
+    if (r == FCG_NORMAL_END) r = dalloc(&dv, n, tmp);
+    if (r == FCG_NORMAL_END && cudaMemcpyAsync(dq, q, n * sizeof(double), cudaMemcpyHostToDevice, p->stream) != cudaSuccess) {
+        set_error("copy of q failed");
+        r = FCG_DEVICE_ERROR;
+    }
+    for (int r0 = 0; r == FCG_NORMAL_END && r0 < k; r0 += kMaxK) {
+        int kk = std::min(kMaxK, k - r0);
+        r = matvec(p, dq + (size_t)r0 * p->Np, dv + (size_t)r0 * p->Np, kk, NULL);
+    }
+    if (r == FCG_NORMAL_END && (cudaMemcpyAsync(v, dv, n * sizeof(double), cudaMemcpyDeviceToHost, p->stream) != cudaSuccess ||
+                                cudaStreamSynchronize(p->stream) != cudaSuccess)) {
+        set_error(std::string("matvec failed: ") + cudaGetErrorString(cudaGetLastError()));
+        r = FCG_DEVICE_ERROR;
+    }
+    dfree(dq);
+    dfree(dv);
+    return r;
+}
+
+// ------------------------------------------------------------------ GMRES
+
+static int ensure_solve_ws(DeviceProblem *p, int k, int M) {
+    int64_t Np = p->Np;
+    int nch = (int)((Np + kDotChunk - 1) / kDotChunk);
+    int r;
+    if (p->gk != k || p->gM < M) {
+        dfree(p->H); dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->z);
+        dfree(p->normb); dfree(p->hnorm); dfree(p->nrm2); dfree(p->active); dfree(p->iters); dfree(p->n_active);
+        dfree(p->b); dfree(p->x0); dfree(p->w); dfree(p->vv); dfree(p->x);
+        for (size_t i = 0; i < p->V.size(); i++) dfree(p->V[i]);
+        p->V.clear();
+        dfree(p->Vptr);
+        p->Vptr_cap = 0;
+        int64_t &B = p->bytes;
+        size_t hs = (size_t)k * (M + 1) * (M + 2);
+        if ((r = dalloc(&p->H, hs, B))) return r;
+        if ((r = dalloc(&p->cs, (size_t)k * (M + 2), B))) return r;
+        if ((r = dalloc(&p->sn, (size_t)k * (M + 2), B))) return r;
+        if ((r = dalloc(&p->g, (size_t)k * (M + 2), B))) return r;
+        if ((r = dalloc(&p->z, (size_t)k * (M + 2), B))) return r;
+        if ((r = dalloc(&p->normb, k, B))) return r;
+        if ((r = dalloc(&p->hnorm, k, B))) return r;
+        if ((r = dalloc(&p->nrm2, 2 * k, B))) return r;
+        if ((r = dalloc(&p->active, k, B))) return r;
+        if ((r = dalloc(&p->iters, k, B))) return r;
+        if ((r = dalloc(&p->n_active, 1, B))) return r;
+        size_t n = (size_t)k * Np;
+        if ((r = dalloc(&p->b, n, B))) return r;
+        if ((r = dalloc(&p->x0, n, B))) return r;
+        if ((r = dalloc(&p->w, n, B))) return r;
+        if ((r = dalloc(&p->vv, n, B))) return r;
+        if ((r = dalloc(&p->x, n, B))) return r;
+        if ((r = dalloc(&p->Vptr, (size_t)M + 2, B))) return r;
+        p->Vptr_cap = M + 2;
+        p->gk = k;
+        p->gM = M;
+        p->x_k = k;
+        if (!p->h_n_active && cudaHostAlloc((void **)&p->h_n_active, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+            set_error("cannot allocate pinned host memory");
+            return FCG_OUT_OF_MEMORY;
+        }
+    }
+    size_t need = (size_t)2 * k * (M + 1) * nch;
+    if ((size_t)p->partial_cap < need) {
+        dfree(p->partial);
+        if ((r = dalloc(&p->partial, need, p->bytes))) return r;
+        p->partial_cap = (int)need;
+    }
+    return FCG_NORMAL_END;
+}
+
+// make sure basis vector j exists (allocated in groups of 16 vectors)
+static int ensure_basis(DeviceProblem *p, int j) {
+    if ((int)p->V.size() > j) return FCG_NORMAL_END;
+    const int group = 16;
+    size_t n = (size_t)p->gk * p->Np;
+    int r;
+    while ((int)p->V.size() <= j) {
+        int start = (int)p->V.size();
+        int cnt = std::min(group, p->Vptr_cap - start);
+        if (cnt <= 0) { set_error("Krylov basis exhausted"); return FCG_GENERIC_ERROR; }
+        double *blk = NULL;
+        if ((r = dalloc(&blk, n * cnt, p->bytes))) return r;
+        for (int i = 0; i < cnt; i++) p->V.push_back(i == 0 ? blk : NULL);
+        std::vector<double *> ptrs(cnt);
+        for (int i = 0; i < cnt; i++) ptrs[i] = blk + n * i;
+        FCG_CK(cudaMemcpyAsync(p->Vptr + start, ptrs.data(), cnt * sizeof(double *), cudaMemcpyHostToDevice, p->stream));
+        // the pinned copy source must outlive the transfer
+        FCG_CK(cudaStreamSynchronize(p->stream));
+    }
+    return FCG_NORMAL_END;
+}
+
+// host-side address of basis vector j (V holds group heads; others are offsets)
+static double *basis_addr(DeviceProblem *p, int j) {
+    int head = j;
+    while (p->V[head] == NULL) head--;
+    return p->V[head] + (size_t)(j - head) * p->gk * p->Np;
+}
+
+int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations) {
+    if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    int ncol = (int)p->cond_cols.size();
+    if (ncol == 0) { set_error("no conductors to solve for"); return FCG_GENERIC_ERROR; }
+    int64_t Np = p->Np;
+    int cap_it = opt.max_iter > 0 ? opt.max_iter : 1000;
+    if (cap_it > Np) cap_it = (int)Np;
+    if (cap_it > 1000 && opt.max_iter <= 0) cap_it = 1000;
+    const double *diag = (opt.precond == FCG_PRECOND_JACOBI) ? p->self : NULL;
+    cudaStream_t s = p->stream;
+    int sms = p->ctx->sm_count;
+    std::vector<int64_t> cf(ncol), cc(ncol);
+    for (int c = 0; c < ncol; c++) { cf[c] = p->cond_first[p->cond_cols[c]]; cc[c] = p->cond_count[p->cond_cols[c]]; }
+    int64_t *d_cf = NULL, *d_cc = NULL;
+    double *d_cap = NULL;
+    int64_t tmpb = 0;
+    int r;
+    if ((r = upload(&d_cf, cf.data(), ncol, tmpb, s)) || (r = upload(&d_cc, cc.data(), ncol, tmpb, s)) ||
+        (r = dalloc(&d_cap, (size_t)ncol * ncol, tmpb))) {
+        dfree(d_cf); dfree(d_cc); dfree(d_cap);
+        return r;
+    }
+    std::vector<double> h_cap((size_t)ncol * ncol, 0.0);
+    std::vector<int> h_iters(ncol, 0);
+    p->timings.iterations_max = 0;
+    int status = FCG_NORMAL_END;
+    float solve_ms_total = 0, asm_ms_total = 0;
+    // right-hand sides in batches of at most kMaxK conductors
+    for (int c0 = 0; c0 < ncol && status == FCG_NORMAL_END; c0 += kMaxK) {
+        int k = std::min(kMaxK, ncol - c0);
+        int M = cap_it;
+        if ((r = ensure_solve_ws(p, k, M))) { status = r; break; }
+        int nch = (int)((Np + kDotChunk - 1) / kDotChunk);
+        int64_t n = (int64_t)k * Np;
+        int g1 = grid_for(n, 256, sms);
+        cudaEventRecord(p->ev0, s);
+        k_set_rhs<<<g1, 256, 0, s>>>(Np, k, d_cf + c0, d_cc + c0, p->b);
+        if ((r = ensure_basis(p, 0))) { status = r; break; }
+        double *V0 = basis_addr(p, 0);
+        double *pr = p->partial, *pb = p->partial + (size_t)k * nch;
+        if (diag) {
+            k_precond<<<g1, 256, 0, s>>>(Np, k, p->b, diag, p->x0);
+            if ((r = matvec(p, p->x0, p->w, k, NULL))) { status = r; break; }
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, p->vv, pr, pb);
+        } else {
+            FCG_CK(cudaMemsetAsync(p->x0, 0, n * sizeof(double), s));
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, NULL, p->vv, pr, pb);
+        }
+        k_reduce_partials<<<dim3(1, k), 256, 0, s>>>(1, nch, pr, NULL, p->nrm2, 1, 0);
+        k_reduce_partials<<<dim3(1, k), 256, 0, s>>>(1, nch, pb, NULL, p->nrm2 + k, 1, 0);
+        FCG_CK(cudaMemsetAsync(p->g, 0, (size_t)k * (M + 2) * sizeof(double), s));
+        k_init_state<<<1, 32 * ((k + 31) / 32), 0, s>>>(k, M, p->nrm2, p->nrm2 + k, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters);
+        k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, V0);
+        FCG_CK(cudaGetLastError());
+        p->timings.launches += diag ? 7 : 6;
+        int64_t hstride_r = (int64_t)(M + 1) * (M + 2);
+        int last_i = -1;
+        bool any = true;
+        // check whether the initial guess already satisfies the tolerance
+        {
+            std::vector<int> act(k);
+            FCG_CK(cudaMemcpyAsync(act.data(), p->active, k * sizeof(int), cudaMemcpyDeviceToHost, s));
+            FCG_CK(cudaStreamSynchronize(s));
+            any = false;
+            for (int i = 0; i < k; i++) any |= act[i] != 0;
+        }
+        for (int i = 0; any && i < cap_it; i++) {
+            if ((r = ensure_basis(p, i + 1))) { status = r; break; }
+            double *Vi = basis_addr(p, i), *Vn = basis_addr(p, i + 1);
+            // w = A P q_i
+            if ((r = matvec(p, Vi, p->w, k, diag))) { status = r; break; }
+            // classical Gram-Schmidt against q_0..q_i
+            k_dots<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, p->active, p->partial);
+            double *hcol = p->H + (int64_t)i * (M + 2);
+            k_reduce_partials<<<dim3(i + 1, k), 256, 0, s>>>(i + 1, nch, p->partial, p->active, hcol, hstride_r, 1);
+            k_update<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, hcol, hstride_r, p->active, p->vv, p->partial);
+            k_reduce_partials<<<dim3(1, k), 256, 0, s>>>(1, nch, p->partial, p->active, p->nrm2, 1, 0);
+            k_givens<<<1, 32 * ((k + 31) / 32), 0, s>>>(k, i, M, p->H, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, opt.tol,
+                                                        p->active, p->iters, p->n_active);
+            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, p->active, Vn);
+            FCG_CK(cudaGetLastError());
+            p->timings.launches += 6;
+            FCG_CK(cudaMemcpyAsync(p->h_n_active, p->n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FCG_CK(cudaStreamSynchronize(s));
+            prof_collect(p);
+            last_i = i;
+            any = *p->h_n_active > 0;
+            (void)Vn;
+        }
+        if (status != FCG_NORMAL_END) break;
+        // right-hand sides still active hit the cap: use the last Arnoldi step
+        std::vector<int> it(k), act(k);
+        FCG_CK(cudaMemcpyAsync(it.data(), p->iters, k * sizeof(int), cudaMemcpyDeviceToHost, s));
+        FCG_CK(cudaMemcpyAsync(act.data(), p->active, k * sizeof(int), cudaMemcpyDeviceToHost, s));
+        FCG_CK(cudaStreamSynchronize(s));
+        bool notconv = false;
+        for (int i = 0; i < k; i++)
+            if (act[i]) { it[i] = last_i; notconv = true; }
+        FCG_CK(cudaMemcpyAsync(p->iters, it.data(), k * sizeof(int), cudaMemcpyHostToDevice, s));
+        k_backsub<<<1, 32 * ((k + 31) / 32), 0, s>>>(k, M, p->H, p->g, p->iters, p->z);
+        k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->w);
+        k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->x);
+        FCG_CK(cudaGetLastError());
+        cudaEventRecord(p->ev1, s);
+        k_assemble<<<dim3(ncol, k), 256, 0, s>>>(Np, d_cf, d_cc, p->leaf_weight, p->x, ncol, d_cap + (size_t)c0 * ncol);
+        FCG_CK(cudaGetLastError());
+        p->timings.launches += 4;
+        FCG_CK(cudaStreamSynchronize(s));
+        prof_collect(p);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        solve_ms_total += ms;
+        for (int i = 0; i < k; i++) {
+            h_iters[c0 + i] = it[i] + 1;
+            p->timings.iterations_max = std::max(p->timings.iterations_max, it[i] + 1);
+        }
+        if (notconv) status = FCG_NOT_CONVERGED;
+        if (ncol > kMaxK) {
+            // keep the charges of this batch in the x buffer of the last batch only
+        }
+    }
+    if (status == FCG_NORMAL_END || status == FCG_NOT_CONVERGED) {
+        if (cudaMemcpy(h_cap.data(), d_cap, h_cap.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            set_error("copy of the capacitance matrix failed");
+            status = FCG_DEVICE_ERROR;
+        } else {
+            if (cap) memcpy(cap, h_cap.data(), h_cap.size() * sizeof(double));
+            if (iterations) memcpy(iterations, h_iters.data(), ncol * sizeof(int));
+        }
+    }
+    p->timings.solve_ms = solve_ms_total;
+    p->timings.assemble_ms = asm_ms_total;
+    dfree(d_cf);
+    dfree(d_cc);
+    dfree(d_cap);
+    return status;
+}
+
+int problem_get_charges(DeviceProblem *p, double *charges) {
+    if (!p->x) { set_error("no solve has run"); return FCG_GENERIC_ERROR; }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    FCG_CK(cudaMemcpy(charges, p->x, (size_t)p->x_k * p->Np * sizeof(double), cudaMemcpyDeviceToHost));
+    return FCG_NORMAL_END;
+}
+
+}  // namespace fcg

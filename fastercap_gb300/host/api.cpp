@@ -1,0 +1,415 @@
+// C ABI of fastercap_gb300 (include/fastercap_gb300.h): model construction,
+// device problems and the reference-compatible command-line driver.
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "../../include/fastercap_gb300.h"
+#include "../csrc/fcg_internal.hpp"
+#include "model.hpp"
+
+namespace fcg {
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+const char *get_error() { return g_err.c_str(); }
+}  // namespace fcg
+
+struct fcg_model {
+    fcg::Model m;
+    // flattened conductor arrays for the C view
+    std::vector<uint8_t> cond_is_diel;
+    std::vector<int64_t> cond_first, cond_count;
+    std::vector<double> cond_out, cond_in, surf;
+    std::vector<int32_t> surf_ptr;
+};
+
+struct fcg_context {
+    fcg::DeviceContext dev;
+};
+
+struct fcg_problem {
+    fcg::DeviceProblem *p;
+};
+
+static void finish_model(fcg_model *fm) {
+    fcg::Model &m = fm->m;
+    fm->surf_ptr.assign(1, 0);
+    for (size_t c = 0; c < m.conductors.size(); c++) {
+        const fcg::Conductor &C = m.conductors[c];
+        fm->cond_is_diel.push_back(C.is_diel ? 1 : 0);
+        fm->cond_first.push_back(m.cond_leaf_first[c]);
+        fm->cond_count.push_back(C.leaf_count);
+        fm->cond_out.push_back(C.outperm);
+        fm->cond_in.push_back(C.inperm);
+        fm->surf.insert(fm->surf.end(), C.surf_outperm.begin(), C.surf_outperm.end());
+        fm->surf_ptr.push_back((int32_t)fm->surf.size());
+    }
+    if (fm->surf.empty()) fm->surf.push_back(0.0);
+}
+
+extern "C" {
+
+int fcg_model_build(const char *path, const fcg_build_options *opt, fcg_model **out, char *err, size_t err_len) {
+    if (!path || !out) return FCG_GENERIC_ERROR;
+    *out = NULL;
+    fcg::BuildOptions o;
+    if (opt) {
+        o.mesh_eps = opt->mesh_eps;
+        o.eps_ratio = opt->eps_ratio;
+        o.mesh_curv = opt->mesh_curv;
+        o.verbose = opt->verbose != 0;
+    }
+    fcg_model *fm = new (std::nothrow) fcg_model();
+    if (!fm) return FCG_OUT_OF_MEMORY;
+    std::string e;
+    int r;
+    try {
+        r = fcg::build_model(path, o, fm->m, e);
+    } catch (std::bad_alloc &) {
+        r = FCG_OUT_OF_MEMORY;
+        e = "out of host memory while building the model";
+    }
+    if (r != FCG_NORMAL_END) {
+        fcg::set_error(e);
+        if (err && err_len) snprintf(err, err_len, "%s", e.c_str());
+        delete fm;
+        return r;
+    }
+    finish_model(fm);
+    *out = fm;
+    return FCG_NORMAL_END;
+}
+
+int fcg_model_info_get(const fcg_model *fm, fcg_model_info *info) {
+    if (!fm || !info) return FCG_GENERIC_ERROR;
+    const fcg::Model &m = fm->m;
+    info->n_nodes = m.n_nodes;
+    info->n_panels = m.n_panels;
+    info->n_links = m.n_links;
+    info->input_panels = m.input_panels;
+    info->n_conductors = (int32_t)m.conductors.size();
+    int nd = 0;
+    for (size_t c = 0; c < m.conductors.size(); c++) nd += m.conductors[c].is_diel ? 1 : 0;
+    info->n_dielectrics = nd;
+    info->max_level = m.max_level;
+    info->max_mesh_eps = m.max_mesh_eps;
+    info->eps = m.eps;
+    info->mesh_eps = m.mesh_eps;
+    return FCG_NORMAL_END;
+}
+
+int fcg_model_arrays_get(const fcg_model *fm, fcg_model_arrays *a) {
+    if (!fm || !a) return FCG_GENERIC_ERROR;
+    const fcg::Model &m = fm->m;
+    a->n_nodes = m.n_nodes;
+    a->n_panels = m.n_panels;
+    a->n_links = m.n_links;
+    a->n_conductors = (int32_t)m.conductors.size();
+    a->node_type = m.type.data();
+    a->node_left = m.left.data();
+    a->node_right = m.right.data();
+    a->node_leaf_first = m.leaf_first.data();
+    a->node_leaf_count = m.leaf_count.data();
+    a->node_vertices = m.vert.data();
+    a->node_centroid = m.cent.data();
+    a->node_normal = m.norm.data();
+    a->node_area = m.area.data();
+    a->node_maxside = m.maxside.data();
+    a->link_ptr = m.link_ptr.data();
+    a->link_src = m.link_src.data();
+    a->leaf_diel = m.leaf_diel.data();
+    a->cond_is_diel = fm->cond_is_diel.data();
+    a->cond_leaf_first = fm->cond_first.data();
+    a->cond_leaf_count = fm->cond_count.data();
+    a->cond_outperm = fm->cond_out.data();
+    a->cond_inperm = fm->cond_in.data();
+    a->cond_surf_ptr = fm->surf_ptr.data();
+    a->cond_surf_outperm = fm->surf.data();
+    return FCG_NORMAL_END;
+}
+
+const char *fcg_model_conductor_name(const fcg_model *fm, int32_t i) {
+    if (!fm || i < 0 || i >= (int32_t)fm->m.conductors.size()) return NULL;
+    return fm->m.conductors[i].name.c_str();
+}
+
+void fcg_model_free(fcg_model *fm) { delete fm; }
+
+const char *fcg_last_error(void) { return fcg::get_error(); }
+
+int fcg_context_create(int device, fcg_context **out) {
+    if (!out) return FCG_GENERIC_ERROR;
+    *out = NULL;
+    fcg_context *c = new fcg_context();
+    int r = fcg::context_init(c->dev, device);
+    if (r != FCG_NORMAL_END) { delete c; return r; }
+    *out = c;
+    return FCG_NORMAL_END;
+}
+
+void fcg_context_destroy(fcg_context *ctx) {
+    if (!ctx) return;
+    fcg::context_release(ctx->dev);
+    delete ctx;
+}
+
+void *fcg_context_stream(fcg_context *ctx) { return ctx ? ctx->dev.stream : NULL; }
+
+int fcg_problem_create(fcg_context *ctx, const fcg_model_arrays *a, int precision, fcg_problem **out) {
+    return fcg_problem_create_on_stream(ctx, a, precision, ctx ? ctx->dev.stream : NULL, out);
+}
+
+int fcg_problem_create_on_stream(fcg_context *ctx, const fcg_model_arrays *a, int precision, void *stream, fcg_problem **out) {
+    if (!ctx || !a || !out) return FCG_GENERIC_ERROR;
+    *out = NULL;
+    fcg::DeviceProblem *p = NULL;
+    int r = fcg::problem_create(ctx->dev, *a, precision, stream, &p);
+    if (r != FCG_NORMAL_END) return r;
+    *out = new fcg_problem();
+    (*out)->p = p;
+    return FCG_NORMAL_END;
+}
+
+void fcg_problem_destroy(fcg_problem *p) {
+    if (!p) return;
+    fcg::problem_destroy(p->p);
+    delete p;
+}
+
+int64_t fcg_problem_device_bytes(const fcg_problem *p) { return p ? fcg::problem_device_bytes(p->p) : 0; }
+int fcg_problem_fill(fcg_problem *p) { return p ? fcg::problem_fill(p->p) : FCG_GENERIC_ERROR; }
+int fcg_problem_get_coefficients(fcg_problem *p, double *lc, double *sc) {
+    return p ? fcg::problem_get_coefficients(p->p, lc, sc) : FCG_GENERIC_ERROR;
+}
+int fcg_problem_matvec(fcg_problem *p, const double *q, double *v, int k) {
+    return (p && q && v && k > 0) ? fcg::problem_matvec_host(p->p, q, v, k) : FCG_GENERIC_ERROR;
+}
+int fcg_problem_matvec_device(fcg_problem *p, const double *q, double *v, int k) {
+    return (p && q && v && k > 0) ? fcg::problem_matvec_device(p->p, q, v, k) : FCG_GENERIC_ERROR;
+}
+int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap, int *iterations) {
+    if (!p) return FCG_GENERIC_ERROR;
+    fcg_solve_options o;
+    o.tol = 0.01;
+    o.precond = FCG_PRECOND_JACOBI;
+    o.max_iter = 0;
+    if (opt) o = *opt;
+    return fcg::problem_solve(p->p, o, cap, iterations);
+}
+int fcg_problem_get_charges(fcg_problem *p, double *charges) {
+    return (p && charges) ? fcg::problem_get_charges(p->p, charges) : FCG_GENERIC_ERROR;
+}
+
+int fcg_problem_set_profiling(fcg_problem *p, int enable) {
+    return p ? fcg::problem_set_profiling(p->p, enable != 0) : FCG_GENERIC_ERROR;
+}
+
+int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *st) {
+    if (!p || !st) return FCG_GENERIC_ERROR;
+    fcg::SolveTimings t = fcg::problem_timings(p->p);
+    st->kernel_launches = t.launches;
+    st->link_launches = t.link_launches;
+    st->link_ms = t.link_ms;
+    st->link_bytes = t.link_bytes;
+    st->fill_ms = t.fill_ms;
+    st->solve_ms = t.solve_ms;
+    return FCG_NORMAL_END;
+}
+
+int fcg_problem_reset_stats(fcg_problem *p) {
+    if (!p) return FCG_GENERIC_ERROR;
+    fcg::problem_reset_stats(p->p);
+    return FCG_NORMAL_END;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ driver
+
+namespace {
+
+struct CmdOptions {
+    std::string file;
+    double mesh_eps = 0.1, eps_ratio = 1.0, mesh_curv = 3.0, gmres_tol = 0.01, out_of_core = 5.0, max_disc_side = 0.1;
+    double auto_err = 0.01;
+    int precond = FCG_PRECOND_JACOBI;
+    unsigned super_dim = 128, block_size = 32;
+    bool automatic = false, auto_precond = false, galerkin = false, dump_residual = false, dump_time = false, verbose = false;
+    bool out_geo = false, dump_input = false, out_cap = false, out_charge = false, keep_charge = false;
+    int precision = FCG_PREC_MIXED;
+};
+
+// Same grammar as FasterCapConsole::ParseCmdLine (FasterCapConsole.cpp:136-357):
+// options are matched on their first letters; returns true on error.
+bool parse_cmd(const char *cmd, CmdOptions &o, std::string &err) {
+    std::vector<std::string> args;
+    const char *p = cmd;
+    while (*p) {
+        while (*p == ' ' || *p == '\t' || *p == '\n') p++;
+        if (!*p) break;
+        std::string tok;
+        if (*p == '"') {
+            p++;
+            while (*p && *p != '"') tok += *p++;
+            if (*p == '"') p++;
+        } else {
+            while (*p && *p != ' ' && *p != '\t' && *p != '\n') {
+                if (*p == '"') { p++; continue; }
+                tok += *p++;
+            }
+        }
+        args.push_back(tok);
+    }
+    if (args.empty()) { err = "FasterCap launched without enough arguments! You must specify at least the input file name"; return true; }
+    for (size_t i = 0; i < args.size(); i++) {
+        const std::string &a = args[i];
+        if (a.size() && a[0] == '-') {
+            char c1 = a.size() > 1 ? a[1] : 0, c2 = a.size() > 2 ? a[2] : 0;
+            const char *rest2 = a.c_str() + (a.size() > 2 ? 2 : a.size());
+            const char *rest3 = a.c_str() + (a.size() > 3 ? 3 : a.size());
+            if (c1 == 's') {
+                if (sscanf(rest2, "%lf", &o.max_disc_side) != 1) { err = "unsupported parameter '" + a + "'"; return true; }
+            } else if (c1 == 'm') {
+                if (c2 == 'c') {
+                    if (sscanf(rest3, "%lf", &o.mesh_curv) != 1) { err = "bad mesh curvature coefficient '" + a + "'"; return true; }
+                } else if (sscanf(rest2, "%lf", &o.mesh_eps) != 1) { err = "bad mesh relative refinement value '" + a + "'"; return true; }
+            } else if (c1 == 'd') {
+                if (sscanf(rest2, "%lf", &o.eps_ratio) != 1) { err = "bad direct potential interaction coefficient '" + a + "'"; return true; }
+            } else if (c1 == 'f') {
+                if (sscanf(rest2, "%lf", &o.out_of_core) != 1) { err = "bad out-of-core ratio '" + a + "'"; return true; }
+            } else if (c1 == 'p') {
+                if (c2 == 'N' || c2 == 'n') o.precond = FCG_PRECOND_NONE;
+                else if (c2 == 'J' || c2 == 'j') o.precond |= FCG_PRECOND_JACOBI;
+                else if (c2 == 'S' || c2 == 's') {
+                    if (sscanf(rest3, "%u", &o.super_dim) != 1) { err = "bad preconditioner dimension '" + a + "'"; return true; }
+                    o.precond |= 4;
+                } else if (c2 == 'B' || c2 == 'b') {
+                    if (sscanf(rest3, "%u", &o.block_size) != 1) { err = "bad preconditioner dimension '" + a + "'"; return true; }
+                    o.precond |= 2;
+                } else if (c2 == 'H' || c2 == 'h') {
+                    o.precond |= 8;
+                } else { err = "bad preconditioner type '" + a + "'"; return true; }
+            } else if (c1 == 'c') o.out_charge = true;
+            else if (c1 == 'k') { if (c2 == 'c') o.keep_charge = true; }
+            else if (c1 == 'r') o.dump_residual = true;
+            else if (c1 == 'i') o.dump_time = true;
+            else if (c1 == 'v') o.verbose = true;
+            else if (c1 == 't') {
+                if (sscanf(rest2, "%lf", &o.gmres_tol) != 1) { err = "bad GMRES iteration tolerance '" + a + "'"; return true; }
+            } else if (c1 == 'o') { if (c2 == 'i') o.dump_input = true; else o.out_geo = true; }
+            else if (c1 == 'e') o.out_cap = true;
+            else if (c1 == 'g') o.galerkin = true;
+            else if (c1 == 'a') {
+                if (c2 == 'p' || c2 == 'P') o.auto_precond = true;
+                else {
+                    o.automatic = true;
+                    if (sscanf(rest2, "%lf", &o.auto_err) != 1) { err = "bad max error value for auto option '" + a + "'"; return true; }
+                }
+            } else if (c1 == 'x') {
+                // -x64 / -xm: arithmetic of the GPU link product (this library only)
+                if (a == "-x64") o.precision = FCG_PREC_FP64;
+                else if (a == "-xm") o.precision = FCG_PREC_MIXED;
+                else { err = "illegal option -- '" + a.substr(1) + "'"; return true; }
+            } else if (c1 != 'b') { err = "illegal option -- '" + a.substr(1) + "'"; return true; }
+        } else {
+            o.file = a;
+        }
+    }
+    return false;
+}
+
+}  // namespace
+
+extern "C" int fcg_run_command_line(const char *command_line) {
+    CmdOptions o;
+    std::string err;
+    if (!command_line || parse_cmd(command_line, o, err)) {
+        printf("%s\n", err.c_str());
+        printf("Usage: fastercap_gb300 <input file> [-m<mesh>] [-mc<mesh curvature>] [-t<tolerance>] [-d<interaction coeff>]\n");
+        printf("                       [-pj|-pn] [-i] [-v] [-x64|-xm]\n");
+        return FCG_COMMAND_LINE_ERROR;
+    }
+    if (o.galerkin) { printf("Error: the Galerkin scheme (-g) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
+    if (o.automatic) { printf("Error: automatic mode (-a) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
+    if (o.precond & ~FCG_PRECOND_JACOBI) {
+        printf("Error: only the Jacobi preconditioner (-pj) or none (-pn) is supported by the GPU solver\n");
+        return FCG_COMMAND_LINE_ERROR;
+    }
+    printf("Running fastercap_gb300 (GB300 solve path for FasterCap input files)\n");
+    printf("Input file: %s\n", o.file.c_str());
+    auto t0 = std::chrono::steady_clock::now();
+    fcg_build_options bo = {o.mesh_eps, o.eps_ratio, o.mesh_curv, o.verbose ? 1 : 0};
+    fcg_model *m = NULL;
+    char ebuf[512];
+    int r = fcg_model_build(o.file.c_str(), &bo, &m, ebuf, sizeof ebuf);
+    if (r != FCG_NORMAL_END) { printf("Error: %s\n", ebuf); return r; }
+    auto t1 = std::chrono::steady_clock::now();
+    fcg_model_info info;
+    fcg_model_info_get(m, &info);
+    printf("Mesh refinement (-m): %g\nGMRES tolerance (-t): %g\n", o.mesh_eps, o.gmres_tol);
+    printf("Precond Type(s) (-p): %s\n", o.precond == FCG_PRECOND_JACOBI ? "Jacobi" : "None");
+    printf("Number of input panels to solver engine: %lld\n", (long long)info.input_panels);
+    printf("Number of panels after refinement: %lld\n", (long long)info.n_panels);
+    printf("Number of links to be computed: %lld\n", (long long)info.n_links);
+    fcg_context *ctx = NULL;
+    fcg_problem *p = NULL;
+    fcg_model_arrays arr;
+    fcg_model_arrays_get(m, &arr);
+    r = fcg_context_create(0, &ctx);
+    if (r == FCG_NORMAL_END) r = fcg_problem_create(ctx, &arr, o.precision, &p);
+    if (r == FCG_NORMAL_END) r = fcg_problem_fill(p);
+    int nc = 0;
+    std::vector<double> cap;
+    std::vector<int> iters;
+    if (r == FCG_NORMAL_END) {
+        nc = info.n_conductors - info.n_dielectrics;
+        cap.resize((size_t)nc * nc);
+        iters.resize(nc);
+        fcg_solve_options so = {o.gmres_tol, o.precond, 0};
+        r = fcg_problem_solve(p, &so, cap.data(), iters.data());
+    }
+    auto t2 = std::chrono::steady_clock::now();
+    if (r != FCG_NORMAL_END && r != FCG_NOT_CONVERGED) {
+        printf("Error: %s\n", fcg_last_error());
+    } else {
+        if (r == FCG_NOT_CONVERGED) printf("Error: GMRES not converging within the iteration cap\n");
+        printf("GMRES iterations per conductor:");
+        for (int i = 0; i < nc; i++) printf(" %d", iters[i]);
+        printf("\nCapacitance matrix is:\nDimension %d x %d\n", nc, nc);
+        int row = 0;
+        for (int32_t c = 0; c < info.n_conductors; c++) {
+            if (arr.cond_is_diel[c]) continue;
+            printf("%s  ", fcg_model_conductor_name(m, c));
+            for (int j = 0; j < nc; j++) printf("%g ", cap[(size_t)row * nc + j]);
+            printf("\n");
+            row++;
+        }
+        for (int i = 0; i < nc; i++)
+            for (int j = 0; j < nc; j++)
+                if (i != j && cap[(size_t)i * nc + j] >= 0.0)
+                    printf("Warning: capacitance matrix has a non-negative off-diagonal element at row %d col %d\n", i + 1, j + 1);
+        printf("\nSolve statistics:\n");
+        printf("Number of panels after refinement: %lld\n", (long long)info.n_panels);
+        printf("Number of links: %lld\n", (long long)(info.n_links + info.n_panels));
+        printf("Max recursion level: %d\n", info.max_level);
+        printf("Max Mesh relative refinement value: %g\n", info.max_mesh_eps);
+        if (o.dump_time) {
+            fcg::SolveTimings t = fcg::problem_timings(p->p);
+            printf("Time for building the model (host): %fs\n", std::chrono::duration<double>(t1 - t0).count());
+            printf("Time for building potential matrix (GPU): %fs\n", t.fill_ms / 1000.0);
+            printf("Time for gmres solving (GPU): %fs\n", t.solve_ms / 1000.0);
+            printf("Device memory for the problem: %lld bytes\n", (long long)fcg_problem_device_bytes(p));
+        }
+        printf("Total time: %fs\n", std::chrono::duration<double>(t2 - t0).count());
+        if (r == FCG_NOT_CONVERGED) r = FCG_NORMAL_END;
+    }
+    fcg_problem_destroy(p);
+    fcg_context_destroy(ctx);
+    fcg_model_free(m);
+    return r;
+}

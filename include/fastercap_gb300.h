@@ -1,0 +1,190 @@
+/*
+ * fastercap_gb300: C ABI of the GB300 capacitance-solve hot path.
+ *
+ * The entry points below replace, one for one, the in-process C++ calls the
+ * reference FasterCap solver makes on its solve path. All sizes are element
+ * counts, all buffers are caller-owned host memory unless stated otherwise,
+ * and every function returns an FC_* status with the reference's values
+ * (Solver/SolverGlobal.h:39-49). No function aborts the process.
+ *
+ * Data layout of a model (post-order node array, CSR links by destination):
+ *   node i in [0, n_nodes): type bits, children, contiguous leaf range,
+ *   links link_ptr[i] .. link_ptr[i+1]-1 with source node link_src[l];
+ *   leaf j in [0, n_panels): permittivity index leaf_diel[j];
+ *   conductors in solver order (dielectric interfaces first), each owning a
+ *   contiguous leaf range.
+ */
+#ifndef FASTERCAP_GB300_H
+#define FASTERCAP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (Solver/SolverGlobal.h:39-49) */
+#define FCG_NORMAL_END 0
+#define FCG_GENERIC_ERROR 1
+#define FCG_COMMAND_LINE_ERROR 64
+#define FCG_CANNOT_OPEN_FILE 66
+#define FCG_OUT_OF_MEMORY 71
+#define FCG_FILE_ERROR 74
+#define FCG_USER_BREAK 125
+/* a CUDA call failed or no usable GPU; the message says which */
+#define FCG_DEVICE_ERROR 90
+/* a GMRES solve stopped at the iteration cap without converging */
+#define FCG_NOT_CONVERGED 91
+
+/* preconditioners (Solver/SolverGlobal.h:62-68) */
+#define FCG_PRECOND_NONE 0
+#define FCG_PRECOND_JACOBI 1
+
+/* arithmetic of the link coefficients and the link product */
+#define FCG_PREC_FP64 0  /* FP64 coefficients, FP64 sums */
+#define FCG_PREC_MIXED 1 /* FP32 coefficients and link sums (compensated), FP64 near field and Krylov */
+
+typedef struct fcg_context fcg_context;
+typedef struct fcg_model fcg_model;
+typedef struct fcg_problem fcg_problem;
+
+/* ---------------------------------------------------------------- model */
+
+/* Mesh and link options: -m, -d, -mc of the reference command line
+ * (FasterCapConsole.cpp:136-357, CAutoRefGlobalVars Solver/SolverGlobal.h:162-183). */
+typedef struct {
+    double mesh_eps;  /* -m  mesh relative refinement value (default 0.1) */
+    double eps_ratio; /* -d  link tolerance = eps_ratio * mesh_eps (default 1.0) */
+    double mesh_curv; /* -mc mesh curvature coefficient (default 3.0) */
+    int verbose;      /* -v */
+} fcg_build_options;
+
+/* Flattened model arrays. Pointers are read-only views; lengths follow the counts. */
+typedef struct {
+    int64_t n_nodes, n_panels, n_links;
+    int32_t n_conductors;
+    const uint8_t *node_type;          /* [n_nodes] bits: 1 leaf, 2 dielectric, 4 outperm on normal side, 128 super node */
+    const int32_t *node_left;          /* [n_nodes] child node or -1 */
+    const int32_t *node_right;         /* [n_nodes] */
+    const int64_t *node_leaf_first;    /* [n_nodes] first leaf of the node's subtree */
+    const int64_t *node_leaf_count;    /* [n_nodes] leaves under the node */
+    const float *node_vertices;        /* [n_nodes*9] triangle corners */
+    const float *node_centroid;        /* [n_nodes*3] */
+    const float *node_normal;          /* [n_nodes*3] (unnormalised for super nodes) */
+    const double *node_area;           /* [n_nodes] */
+    const double *node_maxside;        /* [n_nodes] */
+    const int64_t *link_ptr;           /* [n_nodes+1] */
+    const int32_t *link_src;           /* [n_links] */
+    const uint8_t *leaf_diel;          /* [n_panels] index into the conductor's outer permittivities */
+    const uint8_t *cond_is_diel;       /* [n_conductors] */
+    const int64_t *cond_leaf_first;    /* [n_conductors] */
+    const int64_t *cond_leaf_count;    /* [n_conductors] */
+    const double *cond_outperm;        /* [n_conductors] outer permittivity (dielectric: outperm side) */
+    const double *cond_inperm;         /* [n_conductors] inner permittivity (dielectrics only) */
+    const int32_t *cond_surf_ptr;      /* [n_conductors+1] offsets into cond_surf_outperm */
+    const double *cond_surf_outperm;   /* distinct outer permittivities around each conductor */
+} fcg_model_arrays;
+
+typedef struct {
+    int64_t n_nodes, n_panels, n_links, input_panels;
+    int32_t n_conductors, n_dielectrics, max_level;
+    double max_mesh_eps, eps, mesh_eps;
+} fcg_model_info;
+
+/* Parse a FastCap-format file and build the refined panel hierarchy and the
+ * links. Replaces CAutoRefine::ReadFastCapFile + BuildSuperHierarchy
+ * (Solver/Autorefine.cpp:4568, 6410), CAutoRefine::AutoRefinePanels
+ * (Solver/Autorefine.cpp:293) and the link-store pass and indexing of
+ * CAutoRefine::AutoRefineLinks (Solver/Autorefine.cpp:481-728). */
+int fcg_model_build(const char *path, const fcg_build_options *opt, fcg_model **out, char *err, size_t err_len);
+int fcg_model_info_get(const fcg_model *m, fcg_model_info *info);
+/* views into the model's arrays (valid until fcg_model_free) */
+int fcg_model_arrays_get(const fcg_model *m, fcg_model_arrays *arrays);
+/* conductor name in solver order */
+const char *fcg_model_conductor_name(const fcg_model *m, int32_t index);
+void fcg_model_free(fcg_model *m);
+
+/* ---------------------------------------------------------------- device */
+
+/* One GPU, its streams and the tuned launch shapes. */
+int fcg_context_create(int device, fcg_context **out);
+void fcg_context_destroy(fcg_context *ctx);
+/* last error message of the calling thread */
+const char *fcg_last_error(void);
+/* the context's default CUDA stream (a cudaStream_t), used by problems
+ * created with fcg_problem_create */
+void *fcg_context_stream(fcg_context *ctx);
+
+/* Upload a model once (copies the arrays to HBM). Replaces the reference's
+ * in-memory link chunks m_dPotCoeffLinks / m_pdPanelPtrLinks
+ * (Solver/Autorefine.h:271-272) and node array m_pNodes (Solver/Autorefine.h:283). */
+int fcg_problem_create(fcg_context *ctx, const fcg_model_arrays *arrays, int precision, fcg_problem **out);
+/* same, with all of the problem's work on a caller-owned CUDA stream (a
+ * cudaStream_t; NULL gives the problem a stream of its own) */
+int fcg_problem_create_on_stream(fcg_context *ctx, const fcg_model_arrays *arrays, int precision, void *stream,
+                                 fcg_problem **out);
+void fcg_problem_destroy(fcg_problem *p);
+/* device bytes held by the problem */
+int64_t fcg_problem_device_bytes(const fcg_problem *p);
+
+/* Coefficient fill on the GPU: every link coefficient and the self
+ * coefficients. Replaces the parallel PotEstimateOpt loop of
+ * CAutoRefine::AutoRefineLinks (Solver/Autorefine.cpp:766-840) and the self
+ * terms of CAutoRefine::RefineSelf / SelfPotential (Solver/Autorefine.cpp:2115-2229, 2358-2427). */
+int fcg_problem_fill(fcg_problem *p);
+/* copy coefficients back (FP64 values; mixed precision returns the stored FP32 values widened) */
+int fcg_problem_get_coefficients(fcg_problem *p, double *link_coef, double *self_coef);
+
+/* v = P q for k right-hand sides stored [k][n_panels] on the host.
+ * Replaces CMultHier::MultiplyMatByVec_fast (Solver/MultiplyHierarchical.cpp:285-304). */
+int fcg_problem_matvec(fcg_problem *p, const double *q, double *v, int k);
+/* same, with q and v already in device memory */
+int fcg_problem_matvec_device(fcg_problem *p, const double *d_q, double *d_v, int k);
+
+/* GMRES options: -t and -p of the reference command line. */
+typedef struct {
+    double tol;       /* -t GMRES relative residual tolerance (default 0.01) */
+    int precond;      /* FCG_PRECOND_NONE or FCG_PRECOND_JACOBI */
+    int max_iter;     /* 0: the reference's cap min(1000, n_panels) */
+} fcg_solve_options;
+
+/* Solve for the capacitance matrix: one right-hand side per conductor, all
+ * conductors in one batched right-preconditioned GMRES, C assembled on the
+ * device. cap is [n_cond x n_cond] row-major over the non-dielectric
+ * conductors in solver order; iterations receives the Arnoldi step count of
+ * every right-hand side (may be NULL). Replaces CSolveCap::Solve
+ * (Solver/SolveCapacitance.cpp:1138-1425) with gmresPrecondSFastAll
+ * (Solver/SolveCapacitance.cpp:2288-2574) and the Jacobi branch of
+ * ComputePrecondVectFast (Solver/SolveCapacitance.cpp:3489-3526). */
+int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap, int *iterations);
+/* the charge vectors of the last solve, [n_cond][n_panels] */
+int fcg_problem_get_charges(fcg_problem *p, double *charges);
+
+/* Launch and timing statistics of a problem. With profiling enabled, every
+ * link-product launch is bracketed by CUDA events on the problem's stream. */
+typedef struct {
+    int64_t kernel_launches;  /* kernels launched by the library for this problem */
+    int64_t link_launches;    /* link-product (SpMV) launches */
+    double link_ms;           /* summed device time of the link-product launches (profiling only) */
+    int64_t link_bytes;       /* algorithmic bytes of those launches */
+    double fill_ms;           /* device time of the last coefficient fill */
+    double solve_ms;          /* device time of the last solve */
+} fcg_problem_stats;
+int fcg_problem_set_profiling(fcg_problem *p, int enable);
+int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *stats);
+int fcg_problem_reset_stats(fcg_problem *p);
+
+/* ------------------------------------------------------------- driver */
+
+/* Full headless run with the reference's command line (input file and
+ * switches), printing the reference's report and "Capacitance matrix is:"
+ * block to stdout. Replaces FasterCapConsole::main / CSolveCap::Run
+ * (FasterCapConsole.cpp:44-132, Solver/SolveCapacitance.cpp:86-256). */
+int fcg_run_command_line(const char *command_line);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

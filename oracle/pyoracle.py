@@ -1,0 +1,105 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Used by tests/ (as the checker), by __graft_entry__.smoke() and by the
+CPU-baseline leg of bench.py. The product library never imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liboracle.so")
+
+FIELDS = [
+    ("n_nodes", C.c_int64), ("n_panels", C.c_int64), ("n_links", C.c_int64), ("n_conductors", C.c_int32),
+    ("node_type", C.c_void_p), ("node_left", C.c_void_p), ("node_right", C.c_void_p),
+    ("node_leaf_first", C.c_void_p), ("node_leaf_count", C.c_void_p),
+    ("node_vertices", C.c_void_p), ("node_centroid", C.c_void_p), ("node_normal", C.c_void_p),
+    ("node_area", C.c_void_p), ("node_maxside", C.c_void_p),
+    ("link_ptr", C.c_void_p), ("link_src", C.c_void_p), ("leaf_diel", C.c_void_p),
+    ("cond_is_diel", C.c_void_p), ("cond_leaf_first", C.c_void_p), ("cond_leaf_count", C.c_void_p),
+    ("cond_outperm", C.c_void_p), ("cond_inperm", C.c_void_p), ("cond_surf_ptr", C.c_void_p),
+    ("cond_surf_outperm", C.c_void_p),
+]
+
+DTYPES = {
+    "node_type": np.uint8, "node_left": np.int32, "node_right": np.int32, "node_leaf_first": np.int64,
+    "node_leaf_count": np.int64, "node_vertices": np.float32, "node_centroid": np.float32, "node_normal": np.float32,
+    "node_area": np.float64, "node_maxside": np.float64, "link_ptr": np.int64, "link_src": np.int32,
+    "leaf_diel": np.uint8, "cond_is_diel": np.uint8, "cond_leaf_first": np.int64, "cond_leaf_count": np.int64,
+    "cond_outperm": np.float64, "cond_inperm": np.float64, "cond_surf_ptr": np.int32, "cond_surf_outperm": np.float64,
+}
+
+
+class OrcModel(C.Structure):
+    _fields_ = FIELDS
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("%s is missing: run fastercap_gb300.build.build() first" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.orc_fill.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_int]
+        L.orc_fill.restype = None
+        L.orc_matvec.argtypes = [C.POINTER(OrcModel), vp, vp, vp, vp, C.c_int]
+        L.orc_matvec.restype = None
+        L.orc_solve.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_double, C.c_int, vp, vp, vp, C.c_int]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """CPU oracle over one model's arrays (a dict of numpy arrays)."""
+
+    def __init__(self, arrays: dict, threads: int = 0):
+        self.a = {k: np.ascontiguousarray(arrays[k], dtype=v) for k, v in DTYPES.items()}
+        s = OrcModel()
+        s.n_nodes = len(self.a["node_type"])
+        s.n_panels = len(self.a["leaf_diel"])
+        s.n_links = len(self.a["link_src"])
+        s.n_conductors = len(self.a["cond_is_diel"])
+        for k in DTYPES:
+            setattr(s, k, self.a[k].ctypes.data)
+        self.s = s
+        self.threads = threads
+        self.coef = None
+        self.self_coef = None
+
+    @property
+    def n_panels(self):
+        return int(self.s.n_panels)
+
+    def fill(self):
+        self.coef = np.empty(self.s.n_links, np.float64)
+        self.self_coef = np.empty(self.s.n_panels, np.float64)
+        lib().orc_fill(C.byref(self.s), self.coef.ctypes.data, self.self_coef.ctypes.data, self.threads)
+        return self.coef, self.self_coef
+
+    def matvec(self, q, coef=None, self_coef=None):
+        coef = self.coef if coef is None else np.ascontiguousarray(coef, np.float64)
+        sc = self.self_coef if self_coef is None else np.ascontiguousarray(self_coef, np.float64)
+        q = np.ascontiguousarray(q, np.float64)
+        v = np.empty_like(q)
+        lib().orc_matvec(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, q.ctypes.data, v.ctypes.data, self.threads)
+        return v
+
+    def solve(self, tol=0.01, precond=1, coef=None, self_coef=None):
+        coef = self.coef if coef is None else np.ascontiguousarray(coef, np.float64)
+        sc = self.self_coef if self_coef is None else np.ascontiguousarray(self_coef, np.float64)
+        nc = int((self.a["cond_is_diel"] == 0).sum())
+        cap = np.empty((nc, nc), np.float64)
+        it = np.empty(nc, np.int32)
+        ch = np.empty((nc, self.s.n_panels), np.float64)
+        capped = lib().orc_solve(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, tol, precond, cap.ctypes.data,
+                                 it.ctypes.data, ch.ctypes.data, self.threads)
+        return cap, it, ch, bool(capped)

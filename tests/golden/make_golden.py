@@ -1,0 +1,140 @@
+"""Generate the golden fixtures in tests/golden from the reference solver.
+
+Runs where the reference source tree is present: builds oracle/_ref (the
+reference's own Solver/*.cpp compiled against oracle/shim, see
+oracle/Makefile), writes each input with fastercap_gb300.geometry, runs
+oracle/_ref/fcref_dump on it and packs the dump into <case>.npz:
+
+  input_text            the exact input file (bytes)
+  switches              the reference command-line switches used
+  model arrays          the reference's post-order node array, links and
+                        conductor data converted to the C-ABI layout
+  ref_link_coef, ref_self_coef   the reference's FP64 coefficients
+  ref_mv_q, ref_mv_v    seeded matrix-vector products through the reference
+  ref_cap               the reference's capacitance matrix
+  ref_iterations        GMRES Arnoldi steps per conductor
+  ref_counts            panels, nodes, links; ref_max_mesh_eps
+
+Usage: python tests/golden/make_golden.py [reference dir]
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from fastercap_gb300 import geometry as geo  # noqa: E402
+
+TWO_CUBES_MERGED = """* two unit cubes short-circuited with '+', then renamed with N
+C cube.txt  1.0  0.0 0.0 0.0 +
+C cube.txt  1.0  2.5 0.0 0.0
+C bar.txt  1.0  0.0 3.0 0.0
+End
+File cube.txt
+* unit cube
+%s
+End
+File bar.txt
+* a bar whose panels use two names, merged by N
+%s
+N barA barB
+End
+"""
+
+
+def _cube_text():
+    from fastercap_gb300.geometry import box_faces, _q_line
+    return "\n".join(_q_line("cube", f) for f in box_faces(0, 0, 0, 1, 1, 1))
+
+
+def _bar_text():
+    from fastercap_gb300.geometry import box_faces, _q_line
+    faces = box_faces(0, 0, 0, 4, 1, 1)
+    return "\n".join(_q_line("barA" if i < 3 else "barB", f) for i, f in enumerate(faces))
+
+
+CASES = {
+    # name: (input text factory, switches)
+    "crossing2x2_m05": (lambda: geo.crossing_2x2().text(), ["-m0.05", "-t1e-4", "-pj", "-f0"]),
+    "crossing2x2_m02": (lambda: geo.crossing_2x2().text(), ["-m0.02", "-t1e-4", "-pj", "-f0"]),
+    "crossing2x2_m02_nopc": (lambda: geo.crossing_2x2().text(), ["-m0.02", "-t1e-3", "-pn", "-f0"]),
+    "sphere_d2": (lambda: geo.sphere_text(2), ["-m1e30", "-d1e-32", "-t1e-4", "-pj", "-f0"]),
+    "crossing2x2_slab": (lambda: geo.Crossing(k=2, length=10.0, pitch=3.0, gap=1.0, eps_r=3.9,
+                                              slab=(3.5, 1.0, 3.9, 15.0), name="c2slab").text(),
+                         ["-m0.02", "-t1e-4", "-pj", "-f0"]),
+    "random3": (lambda: geo.random_crossing(3).text(), ["-m0.05", "-t1e-4", "-pj", "-f0"]),
+    "merged_cubes": (lambda: TWO_CUBES_MERGED % (_cube_text(), _bar_text()), ["-m0.05", "-t1e-4", "-pj", "-f0"]),
+}
+
+
+def convert(dump: str) -> dict:
+    L = lambda n: np.load(os.path.join(dump, n + ".npy"))
+    meta = json.load(open(os.path.join(dump, "meta.json")))
+    t = L("node_type")
+    left, right, leaf, nch = L("node_left"), L("node_right"), L("node_leaf"), L("node_nchildren")
+    Nn = len(t)
+    lf = np.zeros(Nn, np.int64)
+    for i in range(Nn):
+        lf[i] = leaf[i] if (t[i] & 1) else lf[left[i]]
+    ls, le = L("node_link_start"), L("node_link_end")
+    assert np.all(ls[1:] == le[:-1]) and ls[0] == 0
+    link_ptr = np.concatenate([ls.astype(np.int64), le[-1:].astype(np.int64)])
+    conds = meta["conductors"]
+    cleaf = np.array([c["leaf_panels"] for c in conds], np.int64)
+    surf, sptr = [], [0]
+    for c in conds:
+        surf += c["surf_outperm"]
+        sptr.append(len(surf))
+    out = {
+        "node_type": t, "node_left": left, "node_right": right, "node_leaf_first": lf, "node_leaf_count": nch,
+        "node_vertices": L("node_vertices"), "node_centroid": L("node_centroid"), "node_normal": L("node_normal"),
+        "node_area": L("node_area"), "node_maxside": L("node_maxside"), "link_ptr": link_ptr,
+        "link_src": L("link_src"), "leaf_diel": L("leaf_diel"),
+        "cond_is_diel": np.array([1 if c["is_diel"] else 0 for c in conds], np.uint8),
+        "cond_leaf_first": np.concatenate([[0], np.cumsum(cleaf)[:-1]]).astype(np.int64),
+        "cond_leaf_count": cleaf,
+        "cond_outperm": np.array([c["outperm"] for c in conds], np.float64),
+        "cond_inperm": np.array([c["inperm"] for c in conds], np.float64),
+        "cond_surf_ptr": np.array(sptr, np.int32),
+        "cond_surf_outperm": np.array(surf if surf else [0.0], np.float64),
+        "cond_names": np.array([c["name"] for c in conds]),
+        "ref_link_coef": L("link_coef"), "ref_self_coef": L("self_coef"),
+        "ref_mv_q": L("mv_q"), "ref_mv_v": L("mv_v"), "ref_cap": L("cap"),
+        "ref_iterations": np.array(meta["gmres_iterations"], np.int32),
+        "ref_counts": np.array([meta["panels"], meta["nodes"], meta["links"]], np.int64),
+        "ref_max_mesh_eps": np.array(meta["max_mesh_eps"]),
+        "ref_max_level": np.array(meta["max_level"]),
+    }
+    return out
+
+
+def main(ref_dir: str = "/root/reference"):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + ref_dir], check=True)
+    dump_bin = os.path.join(ROOT, "oracle", "_ref", "fcref_dump")
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (text_fn, switches) in CASES.items():
+            text = text_fn()
+            inp = os.path.join(tmp, name + ".txt")
+            with open(inp, "w") as f:
+                f.write(text)
+            dump = os.path.join(tmp, name + "_dump")
+            subprocess.run([dump_bin, dump, inp] + switches + ["--mv", "2"], check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            out = convert(dump)
+            out["input_text"] = np.frombuffer(text.encode(), np.uint8)
+            out["switches"] = np.array(switches)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+            print("%-22s panels %6d nodes %6d links %8d" % ((name,) + tuple(out["ref_counts"])))
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

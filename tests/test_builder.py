@@ -1,0 +1,59 @@
+"""The host model builder against the reference: identical panels, nodes,
+links (and their order inside every row) and geometry, bit for bit."""
+
+import numpy as np
+import pytest
+
+import fastercap_gb300 as fc
+from conftest import MODEL_KEYS, build_from_golden, load_golden
+
+
+def test_builder_bit_exact(golden, tmp_path):
+    name, g = golden
+    m = build_from_golden(g, tmp_path)
+    assert (m.n_panels, m.n_nodes, m.n_links) == tuple(int(x) for x in g["ref_counts"])
+    for k in MODEL_KEYS:
+        a, b = m.arrays[k], g[k]
+        if k == "cond_surf_outperm":
+            a = a[: len(b)]
+        np.testing.assert_array_equal(np.asarray(a).reshape(b.shape), b, err_msg=k)
+    assert list(m.names) == [str(s) for s in g["cond_names"]]
+    assert m.info["max_mesh_eps"] == float(g["ref_max_mesh_eps"])
+
+
+def test_missing_file_status(tmp_path):
+    with pytest.raises(fc.FCError) as e:
+        fc.Model.build(str(tmp_path / "nope.txt"))
+    assert e.value.code == fc.CANNOT_OPEN_FILE
+
+
+def test_empty_file_status(tmp_path):
+    p = tmp_path / "empty.txt"
+    p.write_text("* nothing here\n")
+    with pytest.raises(fc.FCError) as e:
+        fc.Model.build(str(p))
+    assert e.value.code == fc.FILE_ERROR
+
+
+def test_complex_permittivity_rejected(tmp_path):
+    p = tmp_path / "cplx.txt"
+    p.write_text("* lossy\nC c.txt 3.0-j0.02 0 0 0\nEnd\nFile c.txt\nT a 0 0 0 1 0 0 0 1 0\nEnd\n")
+    with pytest.raises(fc.FCError) as e:
+        fc.Model.build(str(p))
+    assert e.value.code == fc.FILE_ERROR
+
+
+def test_coincident_panels_rejected(tmp_path):
+    p = tmp_path / "dup.txt"
+    p.write_text("* duplicate panel\nT a 0 0 0 1 0 0 0 1 0\nT a 0 0 0 1 0 0 0 1 0\nT b 0 0 3 1 0 3 0 1 3\n")
+    with pytest.raises(fc.FCError):
+        fc.Model.build(str(p))
+
+
+def test_external_subfile(tmp_path):
+    """C statements may name files on disk next to the input."""
+    (tmp_path / "sq.txt").write_text("* square\nQ s 0 0 0 1 0 0 1 1 0 0 1 0\n")
+    (tmp_path / "main.txt").write_text("* two squares\nC sq.txt 1.0 0 0 0\nC sq.txt 1.0 0 0 1\n")
+    m = fc.Model.build(str(tmp_path / "main.txt"), mesh_eps=0.05)
+    assert m.names == ["g1_s", "g2_s"]
+    assert m.n_panels > 4

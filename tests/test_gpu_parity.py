@@ -1,0 +1,109 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle and
+the reference's golden outputs.
+
+Tolerances: FP64 path - coefficients 1e-12 relative, matvec 1e-13 relative
+norm, capacitance 1e-6 relative per entry with the reference's GMRES
+iteration counts; mixed path - matvec 2e-6 relative norm, every capacitance
+entry within 1e-3 (0.1 %) of the reference FP64 result."""
+
+import numpy as np
+import pytest
+
+import fastercap_gb300 as fc
+from conftest import build_from_golden, load_golden, model_arrays, solve_params
+from pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = fc.Context(0)
+    yield c
+    c.close()
+
+
+def rel_norm(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_fill_fp64(ctx, golden):
+    name, g = golden
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_FP64)
+    p.fill()
+    lc, sc = p.coefficients()
+    np.testing.assert_allclose(lc, g["ref_link_coef"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(sc, g["ref_self_coef"], rtol=1e-12, atol=0)
+
+
+def test_fill_mixed_rounds_fp64(ctx, golden):
+    name, g = golden
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_MIXED)
+    p.fill()
+    lc, _ = p.coefficients()
+    np.testing.assert_allclose(lc, g["ref_link_coef"].astype(np.float32).astype(np.float64), rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("precision,tol", [(fc.PREC_FP64, 1e-13), (fc.PREC_MIXED, 2e-6)])
+def test_matvec(ctx, golden, precision, tol):
+    name, g = golden
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), precision)
+    p.fill()
+    for q, v in zip(g["ref_mv_q"], g["ref_mv_v"]):
+        assert rel_norm(p.matvec(q), v) < tol
+    # batched right-hand sides give the same columns as single ones
+    qs = np.random.default_rng(7).uniform(-1, 1, (5, p.n_panels))
+    vb = p.matvec(qs)
+    for i in range(5):
+        assert rel_norm(vb[i], p.matvec(qs[i])) < (1e-15 if precision == fc.PREC_FP64 else 1e-6)
+
+
+def test_solve_fp64_matches_reference(ctx, golden):
+    name, g = golden
+    tol, precond = solve_params(g)
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_FP64)
+    p.fill()
+    cap, it = p.solve(tol=tol, precond=precond)
+    np.testing.assert_allclose(cap, g["ref_cap"], rtol=1e-6, atol=0)
+    np.testing.assert_array_equal(it, g["ref_iterations"])
+
+
+def test_solve_mixed_within_tenth_percent(ctx, golden):
+    name, g = golden
+    tol, precond = solve_params(g)
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_MIXED)
+    p.fill()
+    cap, it = p.solve(tol=tol, precond=precond)
+    err = np.abs(cap - g["ref_cap"]) / np.abs(g["ref_cap"])
+    assert err.max() < 1e-3, err.max()
+
+
+def test_builder_to_gpu_end_to_end(ctx, golden, tmp_path):
+    """Input file -> host builder -> GPU fill and solve, against the reference."""
+    name, g = golden
+    tol, precond = solve_params(g)
+    m = build_from_golden(g, tmp_path)
+    p = ctx.problem(m, fc.PREC_FP64)
+    p.fill()
+    cap, it = p.solve(tol=tol, precond=precond)
+    np.testing.assert_allclose(cap, g["ref_cap"], rtol=1e-6, atol=0)
+
+
+def test_oracle_fill_vs_gpu_larger(ctx, tmp_path):
+    """A larger mesh than the fixtures: GPU against the oracle."""
+    from fastercap_gb300 import geometry as geo
+    path = tmp_path / "c2.txt"
+    geo.crossing_2x2().write(str(path))
+    m = fc.Model.build(str(path), mesh_eps=0.005)
+    o = Oracle(m.arrays)
+    oc, osc = o.fill()
+    p = ctx.problem(m, fc.PREC_FP64)
+    p.fill()
+    lc, sc = p.coefficients()
+    np.testing.assert_allclose(lc, oc, rtol=1e-12, atol=0)
+    q = np.random.default_rng(1).uniform(-1, 1, m.n_panels)
+    assert rel_norm(p.matvec(q), o.matvec(q)) < 1e-13
+    cap, it = p.solve(tol=1e-4)
+    ocap, oit, _, _ = o.solve(1e-4, 1)
+    np.testing.assert_allclose(cap, ocap, rtol=1e-6)
+    np.testing.assert_array_equal(it, oit)
