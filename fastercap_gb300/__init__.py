@@ -257,6 +257,7 @@ class Problem:
 
     def __init__(self, ctx: "Context", model: Model, precision: int, stream=None):
         self.model = model
+        self._ctx = ctx  # the context outlives its problems
         self.precision = precision
         self.n_panels = model.n_panels
         self.n_links = model.n_links

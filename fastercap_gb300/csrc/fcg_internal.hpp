@@ -4,6 +4,7 @@
 #define FCG_INTERNAL_HPP
 
 #include <stdint.h>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -23,8 +24,12 @@ struct DeviceContext {
     int sm_count = 0;
     size_t free_bytes = 0, total_bytes = 0;
     void *stream = nullptr;  // cudaStream_t owned by the context
+    // the handle and every problem created on the context hold a reference;
+    // the GPU resources go when the last one is dropped
+    std::atomic<int> refs{1};
 };
 void context_release(DeviceContext &ctx);
+void context_unref(DeviceContext *ctx);
 
 int context_init(DeviceContext &ctx, int device);
 

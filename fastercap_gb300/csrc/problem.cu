@@ -595,6 +595,13 @@ int context_init(DeviceContext &ctx, int device) {
     return FCG_NORMAL_END;
 }
 
+void context_unref(DeviceContext *ctx) {
+    if (ctx && ctx->refs.fetch_sub(1) == 1) {
+        context_release(*ctx);
+        delete ctx;
+    }
+}
+
 void context_release(DeviceContext &ctx) {
     if (ctx.stream) {
         cudaSetDevice(ctx.device);
@@ -718,6 +725,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     FCG_CK(cudaSetDevice(ctx.device));
     DeviceProblem *p = new DeviceProblem();
     p->ctx = &ctx;
+    ctx.refs.fetch_add(1);
     p->precision = precision;
     p->Nn = a.n_nodes;
     p->Np = a.n_panels;
@@ -810,7 +818,9 @@ void problem_destroy(DeviceProblem *p) {
     if (p->ev1) cudaEventDestroy(p->ev1);
     for (size_t i = 0; i < p->ev_pool.size(); i++) cudaEventDestroy(p->ev_pool[i]);
     if (p->stream && p->owns_stream) cudaStreamDestroy(p->stream);
+    DeviceContext *ctx = p->ctx;
     delete p;
+    context_unref(ctx);
 }
 
 int64_t problem_device_bytes(const DeviceProblem *p) { return p ? p->bytes : 0; }

@@ -29,7 +29,7 @@ struct fcg_model {
 };
 
 struct fcg_context {
-    fcg::DeviceContext dev;
+    fcg::DeviceContext *dev;
 };
 
 struct fcg_problem {
@@ -146,29 +146,30 @@ int fcg_context_create(int device, fcg_context **out) {
     if (!out) return FCG_GENERIC_ERROR;
     *out = NULL;
     fcg_context *c = new fcg_context();
-    int r = fcg::context_init(c->dev, device);
-    if (r != FCG_NORMAL_END) { delete c; return r; }
+    c->dev = new fcg::DeviceContext();
+    int r = fcg::context_init(*c->dev, device);
+    if (r != FCG_NORMAL_END) { fcg::context_unref(c->dev); delete c; return r; }
     *out = c;
     return FCG_NORMAL_END;
 }
 
 void fcg_context_destroy(fcg_context *ctx) {
     if (!ctx) return;
-    fcg::context_release(ctx->dev);
+    fcg::context_unref(ctx->dev);
     delete ctx;
 }
 
-void *fcg_context_stream(fcg_context *ctx) { return ctx ? ctx->dev.stream : NULL; }
+void *fcg_context_stream(fcg_context *ctx) { return ctx ? ctx->dev->stream : NULL; }
 
 int fcg_problem_create(fcg_context *ctx, const fcg_model_arrays *a, int precision, fcg_problem **out) {
-    return fcg_problem_create_on_stream(ctx, a, precision, ctx ? ctx->dev.stream : NULL, out);
+    return fcg_problem_create_on_stream(ctx, a, precision, ctx ? ctx->dev->stream : NULL, out);
 }
 
 int fcg_problem_create_on_stream(fcg_context *ctx, const fcg_model_arrays *a, int precision, void *stream, fcg_problem **out) {
     if (!ctx || !a || !out) return FCG_GENERIC_ERROR;
     *out = NULL;
     fcg::DeviceProblem *p = NULL;
-    int r = fcg::problem_create(ctx->dev, *a, precision, stream, &p);
+    int r = fcg::problem_create(*ctx->dev, *a, precision, stream, &p);
     if (r != FCG_NORMAL_END) return r;
     *out = new fcg_problem();
     (*out)->p = p;
