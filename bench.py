@@ -233,6 +233,7 @@ def run_gb300(args, rank, world, local_rank):
     barrier()
     st = prob.stats()
     prob.set_profiling(False)
+    phase = {"fill_ms_last": st["fill_ms"], "solve_ms_last": st["solve_ms"]}
     total_ms = sum(times)
     # plain FP64 path on the same model
     p64 = ctx.problem(model, fc.PREC_FP64)
@@ -292,6 +293,7 @@ def run_gb300(args, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "p50_ms": float(np.percentile(e2e_times, 50))},
         "gpu_launches": int(st["kernel_launches"]),
+        "phases": phase,
         "roofline": {"kernel": "k_spmv32 (link product)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
