@@ -299,6 +299,92 @@ FCG_HD double fcg_pot_estimate(unsigned type1, const float *c1, const float *n1,
     }
 }
 
+// Near-field (band 0) coefficient: analytic potential, or for a dielectric
+// evaluation element the central difference of the analytic potential.
+FCG_HD double fcg_pot_near(unsigned type1, const float *c1, const float *n1, const float *c2, const float *v2) {
+    fcg_d3 dist = fcg_fsub(c1, c2);
+    double rdist = fcg_mod(dist);
+    fcg_d3 r1 = fcg_widen(c1);
+    if ((type1 & FCG_IS_DIEL) != FCG_IS_DIEL) return fcg_potential_opt(r1, v2) / FCG_FOUR_PI_TIMES_E0;
+    fcg_d3 nrm = fcg_diel_normal(type1, n1);
+    double h = rdist / 20;
+    fcg_d3 ep = fcg_mk(r1.x + nrm.x * h, r1.y + nrm.y * h, r1.z + nrm.z * h);
+    fcg_d3 em = fcg_mk(r1.x - nrm.x * h, r1.y - nrm.y * h, r1.z - nrm.z * h);
+    double pp = fcg_potential_opt(ep, v2);
+    double pn = fcg_potential_opt(em, v2);
+    return (pn - pp) / (2 * h * FCG_FOUR_PI_TIMES_E0);
+}
+
+// ---- single-precision mid/far field (mixed-precision fill)
+
+FCG_HD float fcg_rsqrtf(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
+//
+// Distance bands from squared float distances (no square root): the same
+// thresholds rho = |c1 - c2| / rmax < 1, 2, 4, 10.
+FCG_HD int fcg_band32(float dx, float dy, float dz, float rmax) {
+    float d2 = dx * dx + dy * dy + dz * dz, r2 = rmax * rmax;
+    if (d2 < r2) return 0;
+    if (d2 < 4.0f * r2) return 1;
+    if (d2 < 16.0f * r2) return 2;
+    if (d2 < 100.0f * r2) return 3;
+    return 4;
+}
+
+// Quadrature of the source triangle v (centroid c2) seen from the evaluation
+// point at offset (dx,dy,dz) = c1 - c2. Quadrature points are formed relative
+// to c2, so the single-precision differences carry no cancellation from the
+// absolute coordinates. efield selects (r - p).n / |r - p|^3 over 1/|r - p|.
+// Result divided by the area, not by 4 pi eps0.
+FCG_HD float fcg_quad32(float dx, float dy, float dz, const float *v, const float *c2, int rule, bool efield, float nx,
+                        float ny, float nz) {
+    float s1x = v[3] - v[0], s1y = v[4] - v[1], s1z = v[5] - v[2];
+    float s2x = v[6] - v[3], s2y = v[7] - v[4], s2z = v[8] - v[5];
+    float s3x = v[0] - v[6], s3y = v[1] - v[7], s3z = v[2] - v[8];
+    float nX = s1y * s2z - s1z * s2y, nY = -s1x * s2z + s1z * s2x, nZ = s1x * s2y - s1y * s2x;
+    float mn = sqrtf(nX * nX + nY * nY + nZ * nZ);
+    float zx = nX / mn, zy = nY / mn, zz = nZ / mn;
+    float m1 = sqrtf(s1x * s1x + s1y * s1y + s1z * s1z);
+    float xx = s1x / m1, xy = s1y / m1, xz = s1z / m1;
+    float yx = xy * zz - xz * zy, yy = xz * zx - xx * zz, yz = xx * zy - xy * zx;
+    float v01 = m1, v02 = -(s3x * xx + s3y * xy + s3z * xz), v12 = -(s3x * yx + s3y * yy + s3z * yz);
+    float jac = (v02 - v01) * v12 - v12 * v02;
+    float ox = v[0] - c2[0], oy = v[1] - c2[1], oz = v[2] - c2[2];
+    float res = 0.0f;
+    int np = fcg_rule_npts(rule);
+    for (int i = 0; i < np; i++) {
+        double pxd, pyd, wd;
+        fcg_rule_point(rule, i, &pxd, &pyd, &wd);
+        float px = (float)pxd, py = (float)pyd, w = (float)wd;
+        float p0 = (v01 - v02) * px + v02 * (1.0f - py);
+        float p1 = v12 * (1.0f - px - py);
+        float ex = dx - (ox + xx * p0 + yx * p1);
+        float ey = dy - (oy + xy * p0 + yy * p1);
+        float ez = dz - (oz + xz * p0 + yz * p1);
+        float ir = fcg_rsqrtf(ex * ex + ey * ey + ez * ez);
+        float val = efield ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
+        res += w * val;
+    }
+    return res * (jac / mn);
+}
+
+// Mixed-precision coefficient for bands 1..4 (band 0 goes to fcg_pot_near).
+FCG_HD float fcg_pot_mid32(int band, bool diel, float dx, float dy, float dz, float nx, float ny, float nz, const float *c2,
+                           const float *v2) {
+    const float k = (float)(1.0 / FCG_FOUR_PI_TIMES_E0);
+    if (band == 4) {
+        float ir = fcg_rsqrtf(dx * dx + dy * dy + dz * dz);
+        return diel ? k * (dx * nx + dy * ny + dz * nz) * ir * ir * ir : k * ir;
+    }
+    int rule = band == 1 ? 5 : (band == 2 ? 3 : 2);
+    return k * fcg_quad32(dx, dy, dz, v2, c2, rule, diel, nx, ny, nz);
+}
+
 // Self coefficient of a leaf panel: collocated analytic potential for a
 // conductor panel, field-discontinuity term for a dielectric panel with
 // permittivities eb (outer side) and ea (inner side).

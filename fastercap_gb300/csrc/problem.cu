@@ -96,6 +96,9 @@ struct DeviceProblem {
     cudaEvent_t ev0 = NULL, ev1 = NULL;
     int64_t bytes = 0;
     bool filled = false;
+    // near-field (band 0) link list, built on the first fill
+    int64_t n_near = -1;
+    int32_t *near_link = NULL, *near_row = NULL;
     SolveTimings timings;
     // profiling of the link product: event pairs awaiting readout
     bool profiling = false;
@@ -135,26 +138,109 @@ struct DeviceProblem {
 
 // --------------------------------------------------------------- kernels
 
-__global__ void k_fill_links(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
-                             const NodeGeo *__restrict__ geo, double *__restrict__ c64, float *__restrict__ c32,
-                             unsigned *status) {
+// Distance band of link (row, src): FP64 exactly as the reference in the FP64
+// path, squared single-precision distances in the mixed path.
+template <bool MIXED>
+__device__ __forceinline__ int link_band(const NodeGeo &g1, const NodeGeo &g2) {
+    if (MIXED) {
+        float dx = g1.c[0] - g2.c[0], dy = g1.c[1] - g2.c[1], dz = g1.c[2] - g2.c[2];
+        float rmax = (float)(g1.maxside > g2.maxside ? g1.maxside : g2.maxside);
+        return fcg_band32(dx, dy, dz, rmax);
+    }
+    double rdist = fcg_mod(fcg_fsub(g1.c, g2.c));
+    return fcg_band(rdist, g1.maxside > g2.maxside ? g1.maxside : g2.maxside);
+}
+
+// count the near-field (band 0) links of every row
+template <bool MIXED>
+__global__ void k_near_count(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+                             const NodeGeo *__restrict__ geo, int32_t *__restrict__ cnt) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = warp; row < Nn; row += nwarps) {
-        const NodeGeo &g1 = geo[row];
-        unsigned t1 = g1.type;
-        float c1[3] = {g1.c[0], g1.c[1], g1.c[2]};
-        float n1[3] = {g1.n[0], g1.n[1], g1.n[2]};
-        double ms1 = g1.maxside;
+        const NodeGeo g1 = geo[row];
+        int64_t s = ptr[row], e = ptr[row + 1];
+        int c = 0;
+        for (int64_t l = s + lane; l < e; l += 32) c += link_band<MIXED>(g1, geo[src[l]]) == 0;
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) cnt[row] = c;
+    }
+}
+
+// list the near-field links of every row at its offset, in link order
+template <bool MIXED>
+__global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+                            const NodeGeo *__restrict__ geo, const int64_t *__restrict__ off, int32_t *__restrict__ near_link,
+                            int32_t *__restrict__ near_row) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        const NodeGeo g1 = geo[row];
+        int64_t s = ptr[row], e = ptr[row + 1];
+        int64_t o = off[row];
+        for (int64_t base = s; base < e; base += 32) {
+            int64_t l = base + lane;
+            bool nr = l < e && link_band<MIXED>(g1, geo[src[l]]) == 0;
+            unsigned m = __ballot_sync(0xffffffffu, nr);
+            if (nr) {
+                int64_t at = o + __popc(m & ((1u << lane) - 1u));
+                near_link[at] = (int32_t)l;
+                near_row[at] = (int32_t)row;
+            }
+            o += __popc(m);
+        }
+    }
+}
+
+// Links of bands 1..4 (quadrature and point formulas): one warp per row.
+template <bool MIXED>
+__global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+                           const NodeGeo *__restrict__ geo, double *__restrict__ c64, float *__restrict__ c32,
+                           unsigned *status) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        const NodeGeo g1 = geo[row];
+        bool diel = g1.type & FCG_IS_DIEL;
+        float nx = 0.f, ny = 0.f, nz = 0.f;
+        if (MIXED && diel) {
+            fcg_d3 n = fcg_diel_normal(g1.type, g1.n);
+            nx = (float)n.x; ny = (float)n.y; nz = (float)n.z;
+        }
         int64_t s = ptr[row], e = ptr[row + 1];
         for (int64_t l = s + lane; l < e; l += 32) {
             const NodeGeo &g2 = geo[src[l]];
-            double val = fcg_pot_estimate(t1, c1, n1, ms1, g2.c, g2.v, g2.maxside);
-            if (!isfinite(val)) atomicOr(status, 1u);
-            if (c64) c64[l] = val;
-            if (c32) c32[l] = (float)val;
+            int band = link_band<MIXED>(g1, g2);
+            if (band == 0) continue;
+            if (MIXED) {
+                float dx = g1.c[0] - g2.c[0], dy = g1.c[1] - g2.c[1], dz = g1.c[2] - g2.c[2];
+                float val = fcg_pot_mid32(band, diel, dx, dy, dz, nx, ny, nz, g2.c, g2.v);
+                if (!isfinite(val)) atomicOr(status, 1u);
+                c32[l] = val;
+            } else {
+                double val = fcg_pot_estimate(g1.type, g1.c, g1.n, g1.maxside, g2.c, g2.v, g2.maxside);
+                if (!isfinite(val)) atomicOr(status, 1u);
+                c64[l] = val;
+            }
         }
+    }
+}
+
+// Near-field links (band 0), FP64 analytic, one thread per listed link.
+__global__ void k_fill_near(int64_t n, const int32_t *__restrict__ near_link, const int32_t *__restrict__ near_row,
+                            const int32_t *__restrict__ src, const NodeGeo *__restrict__ geo, double *__restrict__ c64,
+                            float *__restrict__ c32, unsigned *status) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t l = near_link[t];
+        const NodeGeo &g1 = geo[near_row[t]];
+        const NodeGeo &g2 = geo[src[l]];
+        double val = fcg_pot_near(g1.type, g1.c, g1.n, g2.c, g2.v);
+        if (!isfinite(val)) atomicOr(status, 1u);
+        if (c64) c64[l] = val;
+        else c32[l] = (float)val;
     }
 }
 
@@ -805,6 +891,7 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
     dfree(p->left); dfree(p->right); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
     dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
+    dfree(p->near_link); dfree(p->near_row);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls);
     dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
@@ -875,18 +962,72 @@ static int check_status(DeviceProblem *p, const char *what) {
     return FCG_NORMAL_END;
 }
 
+// Build the near-field link list once per problem: per-row counts, an
+// exclusive scan on the host, then an ordered per-row compaction.
+static int build_near_list(DeviceProblem *p) {
+    cudaStream_t s = p->stream;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
+    int32_t *cnt = NULL;
+    int64_t *off = NULL;
+    int64_t tmp = 0;
+    int r;
+    if ((r = dalloc(&cnt, p->Nn, tmp))) return r;
+    if (mixed) k_near_count<true><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, cnt);
+    else k_near_count<false><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, cnt);
+    p->timings.launches++;
+    std::vector<int32_t> hc(p->Nn);
+    std::vector<int64_t> ho(p->Nn + 1, 0);
+    if (cudaMemcpyAsync(hc.data(), cnt, p->Nn * sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        set_error(std::string("near-field count failed: ") + cudaGetErrorString(cudaGetLastError()));
+        dfree(cnt);
+        return FCG_DEVICE_ERROR;
+    }
+    for (int64_t i = 0; i < p->Nn; i++) ho[i + 1] = ho[i] + hc[i];
+    int64_t n = ho[p->Nn];
+    dfree(cnt);
+    if ((r = upload(&off, ho.data(), p->Nn + 1, tmp, s))) return r;
+    if ((r = dalloc(&p->near_link, (size_t)std::max<int64_t>(n, 1), p->bytes)) ||
+        (r = dalloc(&p->near_row, (size_t)std::max<int64_t>(n, 1), p->bytes))) {
+        dfree(off);
+        return r;
+    }
+    if (n > 0) {
+        if (mixed) k_near_list<true><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, off, p->near_link, p->near_row);
+        else k_near_list<false><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, off, p->near_link, p->near_row);
+        p->timings.launches++;
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    dfree(off);
+    if (e != cudaSuccess) { set_error(std::string("near-field list failed: ") + cudaGetErrorString(e)); return FCG_DEVICE_ERROR; }
+    p->n_near = n;
+    return FCG_NORMAL_END;
+}
+
 int problem_fill(DeviceProblem *p) {
     FCG_CK(cudaSetDevice(p->ctx->device));
     cudaStream_t s = p->stream;
+    if (p->n_near < 0) {
+        int r = build_near_list(p);
+        if (r != FCG_NORMAL_END) return r;
+    }
     FCG_CK(cudaMemsetAsync(p->status, 0, sizeof(unsigned), s));
     FCG_CK(cudaEventRecord(p->ev0, s));
     int sms = p->ctx->sm_count;
+    bool mixed = p->precision == FCG_PREC_MIXED;
     if (p->L > 0) {
-        int64_t warps = p->Nn;
-        int grid = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)sms * 32);
-        k_fill_links<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->coef32, p->status);
+        int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)sms * 32);
+        if (mixed) k_fill_far<true><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->coef32, p->status);
+        else k_fill_far<false><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->coef32, p->status);
         FCG_CK(cudaGetLastError());
         p->timings.launches++;
+        if (p->n_near > 0) {
+            k_fill_near<<<grid_for(p->n_near, 128, sms), 128, 0, s>>>(p->n_near, p->near_link, p->near_row, p->link_src, p->geo,
+                                                                     p->coef64, p->coef32, p->status);
+            FCG_CK(cudaGetLastError());
+            p->timings.launches++;
+        }
     }
     k_fill_self<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->leaf_eb, p->leaf_ea, p->self, p->status);
     FCG_CK(cudaGetLastError());
