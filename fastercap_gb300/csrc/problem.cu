@@ -379,7 +379,10 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const int3
     }
 }
 
-// compensated FP32 accumulation (Kahan-Babuska / Neumaier)
+// Compensated FP32 accumulation (Kahan-Babuska / Neumaier). Each product is
+// split exactly into p + e with one FMA (e = c*q - p), e goes to the
+// compensation, and the row sum leaves the kernel as FP64 (s + c): the
+// stored potentials keep the precision the FP32 stream carries.
 struct KSum {
     float s, c;
 };
@@ -389,11 +392,18 @@ __device__ __forceinline__ void kadd(KSum &a, float x) {
     else a.c += (x - t) + a.s;
     a.s = t;
 }
+__device__ __forceinline__ void kmul_add(KSum &a, float c, float q) {
+    float p = c * q;
+    float e = fmaf(c, q, -p);
+    kadd(a, p);
+    a.c += e;
+}
 
-// Link product, mixed: FP32 coefficients and charges, compensated FP32 sums.
+// Link product, mixed: FP32 coefficients and charges, compensated FP32 sums,
+// FP64 node potentials.
 template <int K>
 __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
-                         const float *__restrict__ coef, const float *__restrict__ Q, float *__restrict__ P) {
+                         const float *__restrict__ coef, const float *__restrict__ Q, double *__restrict__ P) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -406,7 +416,7 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const int3
             float c = coef[l];
             const float *q = Q + (int64_t)src[l] * K;
 #pragma unroll
-            for (int r = 0; r < K; r++) kadd(acc[r], c * q[r]);
+            for (int r = 0; r < K; r++) kmul_add(acc[r], c, q[r]);
         }
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -422,7 +432,7 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const int3
         }
 #pragma unroll
         for (int r = 0; r < K; r++)
-            if (lane == (r & 31)) P[row * K + r] = acc[r].s + acc[r].c;
+            if (lane == (r & 31)) P[row * K + r] = (double)acc[r].s + (double)acc[r].c;
     }
 }
 
@@ -1077,11 +1087,9 @@ static int ensure_matvec_ws(DeviceProblem *p, int kp) {
     size_t n = (size_t)p->Nn * kp;
     if ((r = dalloc(&p->Qd, n, p->bytes))) return r;
     if ((r = dalloc(&p->Ad, n, p->bytes))) return r;
-    if (p->precision == FCG_PREC_FP64) {
-        if ((r = dalloc(&p->Pd, n, p->bytes))) return r;
-    } else {
+    if ((r = dalloc(&p->Pd, n, p->bytes))) return r;
+    if (p->precision == FCG_PREC_MIXED) {
         if ((r = dalloc(&p->Qf, n, p->bytes))) return r;
-        if ((r = dalloc(&p->Pf, n, p->bytes))) return r;
     }
     p->kcap = kp;
     return FCG_NORMAL_END;
@@ -1113,8 +1121,10 @@ static int matvec(DeviceProblem *p, const double *in, double *out, int k, const 
     int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
     int64_t launches = 2 + (pl.n_top_levels > 0 ? 2 : 0);
     if (p->L > 0) {
+        // coefficient + source index per link, row offsets, one charge read and
+        // one potential write per node and right-hand side
         int64_t cb = mixed ? 4 : 8;
-        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + 2 * cb * (int64_t)k * p->Nn;
+        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + (cb + 8) * (int64_t)k * p->Nn;
         p->timings.link_launches++;
         launches++;
         prof_begin(p);
@@ -1129,27 +1139,24 @@ static int matvec(DeviceProblem *p, const double *in, double *out, int k, const 
             }
         } else {
             switch (kp) {
-            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
-            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
-            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
-            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
-            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
-            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pf); break;
+            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
+            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
+            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
+            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
+            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
+            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
             }
         }
         prof_end(p);
         FCG_CK(cudaGetLastError());
     } else {
-        if (mixed) FCG_CK(cudaMemsetAsync(p->Pf, 0, (size_t)p->Nn * kp * sizeof(float), s));
-        else FCG_CK(cudaMemsetAsync(p->Pd, 0, (size_t)p->Nn * kp * sizeof(double), s));
+        FCG_CK(cudaMemsetAsync(p->Pd, 0, (size_t)p->Nn * kp * sizeof(double), s));
     }
     if (pl.n_top_levels > 0) {
-        if (mixed) k_down_top<float><<<1, 1024, 0, s>>>(pl, k, kp, p->Pf, p->Ad, p->parent);
-        else k_down_top<double><<<1, 1024, 0, s>>>(pl, k, kp, p->Pd, p->Ad, p->parent);
+        k_down_top<double><<<1, 1024, 0, s>>>(pl, k, kp, p->Pd, p->Ad, p->parent);
         FCG_CK(cudaGetLastError());
     }
-    if (mixed) k_down_block<float><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, p->Pf, p->Ad, p->parent, out);
-    else k_down_block<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, p->Pd, p->Ad, p->parent, out);
+    k_down_block<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, p->Pd, p->Ad, p->parent, out);
     FCG_CK(cudaGetLastError());
     p->timings.matvecs++;
     p->timings.launches += launches;
