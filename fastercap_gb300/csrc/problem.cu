@@ -43,6 +43,9 @@ namespace fcg {
 static const int kBlockLeaves = 256;  // leaves per sweep subtree
 static const int kMaxK = 32;          // right-hand sides per matvec batch
 static const int kDotChunk = 1024;    // vector elements per CTA in the Krylov kernels
+// link words: source node in the low 29 bits, distance band (0..4) in the top 3
+static const uint32_t kSrcMask = 0x1FFFFFFFu;
+static const int kBandShift = 29;
 
 struct __align__(16) NodeGeo {
     float v[9];
@@ -108,7 +111,7 @@ struct DeviceProblem {
     // model
     NodeGeo *geo = NULL;
     int64_t *link_ptr = NULL;
-    int32_t *link_src = NULL;
+    uint32_t *link_src = NULL;  // source node | band << kBandShift
     int32_t *leaf_node = NULL, *parent = NULL, *left = NULL, *right = NULL;
     double *leaf_eb = NULL, *leaf_ea = NULL, *leaf_weight = NULL;
     double *coef64 = NULL;
@@ -138,51 +141,55 @@ struct DeviceProblem {
 
 // --------------------------------------------------------------- kernels
 
-// Distance band of link (row, src): FP64 exactly as the reference in the FP64
-// path, squared single-precision distances in the mixed path.
-template <bool MIXED>
-__device__ __forceinline__ int link_band(const NodeGeo &g1, const NodeGeo &g2) {
-    if (MIXED) {
-        float dx = g1.c[0] - g2.c[0], dy = g1.c[1] - g2.c[1], dz = g1.c[2] - g2.c[2];
-        float rmax = (float)(g1.maxside > g2.maxside ? g1.maxside : g2.maxside);
-        return fcg_band32(dx, dy, dz, rmax);
-    }
-    double rdist = fcg_mod(fcg_fsub(g1.c, g2.c));
-    return fcg_band(rdist, g1.maxside > g2.maxside ? g1.maxside : g2.maxside);
-}
-
-// count the near-field (band 0) links of every row
-template <bool MIXED>
-__global__ void k_near_count(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
-                             const NodeGeo *__restrict__ geo, int32_t *__restrict__ cnt) {
+// Distance band of every link, in FP64 exactly as the reference decides it
+// (CAutoRefine::PotEstimateOpt, Solver/Autorefine.cpp:3495-3505, 3561-3598),
+// stored in the top bits of the link's source word. Runs once per problem.
+__global__ void k_classify(int64_t Nn, const int64_t *__restrict__ ptr, uint32_t *__restrict__ src,
+                           const NodeGeo *__restrict__ geo) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = warp; row < Nn; row += nwarps) {
-        const NodeGeo g1 = geo[row];
+        const float c1[3] = {geo[row].c[0], geo[row].c[1], geo[row].c[2]};
+        double ms1 = geo[row].maxside;
+        int64_t s = ptr[row], e = ptr[row + 1];
+        for (int64_t l = s + lane; l < e; l += 32) {
+            uint32_t j = src[l] & kSrcMask;
+            const NodeGeo &g2 = geo[j];
+            double rdist = fcg_mod(fcg_fsub(c1, g2.c));
+            int band = fcg_band(rdist, ms1 > g2.maxside ? ms1 : g2.maxside);
+            src[l] = j | ((uint32_t)band << kBandShift);
+        }
+    }
+}
+
+// count the near-field (band 0) links of every row
+__global__ void k_near_count(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
+                             int32_t *__restrict__ cnt) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
         int64_t s = ptr[row], e = ptr[row + 1];
         int c = 0;
-        for (int64_t l = s + lane; l < e; l += 32) c += link_band<MIXED>(g1, geo[src[l]]) == 0;
+        for (int64_t l = s + lane; l < e; l += 32) c += (src[l] >> kBandShift) == 0;
         for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
         if (lane == 0) cnt[row] = c;
     }
 }
 
 // list the near-field links of every row at its offset, in link order
-template <bool MIXED>
-__global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
-                            const NodeGeo *__restrict__ geo, const int64_t *__restrict__ off, int32_t *__restrict__ near_link,
-                            int32_t *__restrict__ near_row) {
+__global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
+                            const int64_t *__restrict__ off, int32_t *__restrict__ near_link, int32_t *__restrict__ near_row) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = warp; row < Nn; row += nwarps) {
-        const NodeGeo g1 = geo[row];
         int64_t s = ptr[row], e = ptr[row + 1];
         int64_t o = off[row];
         for (int64_t base = s; base < e; base += 32) {
             int64_t l = base + lane;
-            bool nr = l < e && link_band<MIXED>(g1, geo[src[l]]) == 0;
+            bool nr = l < e && (src[l] >> kBandShift) == 0;
             unsigned m = __ballot_sync(0xffffffffu, nr);
             if (nr) {
                 int64_t at = o + __popc(m & ((1u << lane) - 1u));
@@ -194,9 +201,10 @@ __global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const i
     }
 }
 
-// Links of bands 1..4 (quadrature and point formulas): one warp per row.
+// Links of bands 1..4 (quadrature and point formulas): one warp per row;
+// FP32 in the mixed path, the reference's FP64 formulas otherwise.
 template <bool MIXED>
-__global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+__global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                            const NodeGeo *__restrict__ geo, double *__restrict__ c64, float *__restrict__ c32,
                            unsigned *status) {
     int lane = threadIdx.x & 31;
@@ -205,23 +213,32 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const in
     for (int64_t row = warp; row < Nn; row += nwarps) {
         const NodeGeo g1 = geo[row];
         bool diel = g1.type & FCG_IS_DIEL;
-        float nx = 0.f, ny = 0.f, nz = 0.f;
-        if (MIXED && diel) {
-            fcg_d3 n = fcg_diel_normal(g1.type, g1.n);
-            nx = (float)n.x; ny = (float)n.y; nz = (float)n.z;
-        }
+        fcg_d3 n64 = fcg_mk(0, 0, 0);
+        if (diel) n64 = fcg_diel_normal(g1.type, g1.n);
+        float nx = (float)n64.x, ny = (float)n64.y, nz = (float)n64.z;
+        fcg_d3 r1 = fcg_widen(g1.c);
         int64_t s = ptr[row], e = ptr[row + 1];
         for (int64_t l = s + lane; l < e; l += 32) {
-            const NodeGeo &g2 = geo[src[l]];
-            int band = link_band<MIXED>(g1, g2);
+            uint32_t w = src[l];
+            int band = (int)(w >> kBandShift);
             if (band == 0) continue;
+            const NodeGeo &g2 = geo[w & kSrcMask];
             if (MIXED) {
                 float dx = g1.c[0] - g2.c[0], dy = g1.c[1] - g2.c[1], dz = g1.c[2] - g2.c[2];
                 float val = fcg_pot_mid32(band, diel, dx, dy, dz, nx, ny, nz, g2.c, g2.v);
                 if (!isfinite(val)) atomicOr(status, 1u);
                 c32[l] = val;
             } else {
-                double val = fcg_pot_estimate(g1.type, g1.c, g1.n, g1.maxside, g2.c, g2.v, g2.maxside);
+                double val;
+                if (band == 4) {
+                    fcg_d3 dist = fcg_fsub(g1.c, g2.c);
+                    double rd = fcg_mod(dist);
+                    val = diel ? fcg_dot(dist, n64) / (FCG_FOUR_PI_TIMES_E0 * rd * rd * rd) : 1 / (FCG_FOUR_PI_TIMES_E0 * rd);
+                } else {
+                    int rule = band == 1 ? 5 : (band == 2 ? 3 : 2);
+                    val = (diel ? fcg_enfield_numerical(r1, g2.v, n64, rule) : fcg_potential_numerical(r1, g2.v, rule)) /
+                          FCG_FOUR_PI_TIMES_E0;
+                }
                 if (!isfinite(val)) atomicOr(status, 1u);
                 c64[l] = val;
             }
@@ -231,12 +248,12 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const in
 
 // Near-field links (band 0), FP64 analytic, one thread per listed link.
 __global__ void k_fill_near(int64_t n, const int32_t *__restrict__ near_link, const int32_t *__restrict__ near_row,
-                            const int32_t *__restrict__ src, const NodeGeo *__restrict__ geo, double *__restrict__ c64,
+                            const uint32_t *__restrict__ src, const NodeGeo *__restrict__ geo, double *__restrict__ c64,
                             float *__restrict__ c32, unsigned *status) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t l = near_link[t];
         const NodeGeo &g1 = geo[near_row[t]];
-        const NodeGeo &g2 = geo[src[l]];
+        const NodeGeo &g2 = geo[src[l] & kSrcMask];
         double val = fcg_pot_near(g1.type, g1.c, g1.n, g2.c, g2.v);
         if (!isfinite(val)) atomicOr(status, 1u);
         if (c64) c64[l] = val;
@@ -352,7 +369,7 @@ __global__ void k_down_block(const SweepPlan plan, const int32_t *__restrict__ l
 // Link product, FP64: one warp per destination node, lanes stride over the
 // node's links, K right-hand sides per link.
 template <int K>
-__global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+__global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                          const double *__restrict__ coef, const double *__restrict__ Q, double *__restrict__ P) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -364,7 +381,7 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const int3
         int64_t s = ptr[row], e = ptr[row + 1];
         for (int64_t l = s + lane; l < e; l += 32) {
             double c = coef[l];
-            const double *q = Q + (int64_t)src[l] * K;
+            const double *q = Q + (int64_t)(src[l] & kSrcMask) * K;
 #pragma unroll
             for (int r = 0; r < K; r++) acc[r] += c * q[r];
         }
@@ -402,7 +419,7 @@ __device__ __forceinline__ void kmul_add(KSum &a, float c, float q) {
 // Link product, mixed: FP32 coefficients and charges, compensated FP32 sums,
 // FP64 node potentials.
 template <int K>
-__global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const int32_t *__restrict__ src,
+__global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                          const float *__restrict__ coef, const float *__restrict__ Q, double *__restrict__ P) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -414,7 +431,7 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const int3
         int64_t s = ptr[row], e = ptr[row + 1];
         for (int64_t l = s + lane; l < e; l += 32) {
             float c = coef[l];
-            const float *q = Q + (int64_t)src[l] * K;
+            const float *q = Q + (int64_t)(src[l] & kSrcMask) * K;
 #pragma unroll
             for (int r = 0; r < K; r++) kmul_add(acc[r], c, q[r]);
         }
@@ -709,7 +726,7 @@ void context_release(DeviceContext &ctx) {
 
 static std::string validate(const fcg_model_arrays &a) {
     if (a.n_nodes <= 0 || a.n_panels <= 0 || a.n_links < 0 || a.n_conductors <= 0) return "empty model";
-    if (a.n_nodes > 0x7fffffffLL || a.n_links > 0x7fffffffLL) return "model too large for 32-bit indices";
+    if (a.n_nodes > (int64_t)kSrcMask || a.n_links > 0x7fffffffLL) return "model too large (nodes must fit 29 bits, links 31 bits)";
     if (!a.node_type || !a.node_left || !a.node_right || !a.node_leaf_first || !a.node_leaf_count || !a.node_vertices ||
         !a.node_centroid || !a.node_normal || !a.node_area || !a.node_maxside || !a.link_ptr || (a.n_links && !a.link_src) ||
         !a.leaf_diel || !a.cond_is_diel || !a.cond_leaf_first || !a.cond_leaf_count || !a.cond_outperm || !a.cond_inperm ||
@@ -871,7 +888,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     }
     FCG_TRY(upload(&p->geo, geo.data(), Nn, p->bytes, s));
     FCG_TRY(upload(&p->link_ptr, a.link_ptr, Nn + 1, p->bytes, s));
-    FCG_TRY(upload(&p->link_src, a.link_src, a.n_links, p->bytes, s));
+    FCG_TRY(upload(&p->link_src, (const uint32_t *)a.link_src, a.n_links, p->bytes, s));
     FCG_TRY(upload(&p->leaf_node, leaf_node.data(), Np, p->bytes, s));
     FCG_TRY(upload(&p->parent, parent.data(), Nn, p->bytes, s));
     FCG_TRY(upload(&p->leaf_eb, eb.data(), Np, p->bytes, s));
@@ -972,20 +989,20 @@ static int check_status(DeviceProblem *p, const char *what) {
     return FCG_NORMAL_END;
 }
 
-// Build the near-field link list once per problem: per-row counts, an
+// Classify every link's distance band (stored with the source index) and
+// build the near-field link list once per problem: per-row counts, an
 // exclusive scan on the host, then an ordered per-row compaction.
 static int build_near_list(DeviceProblem *p) {
     cudaStream_t s = p->stream;
-    bool mixed = p->precision == FCG_PREC_MIXED;
     int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
     int32_t *cnt = NULL;
     int64_t *off = NULL;
     int64_t tmp = 0;
     int r;
     if ((r = dalloc(&cnt, p->Nn, tmp))) return r;
-    if (mixed) k_near_count<true><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, cnt);
-    else k_near_count<false><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, cnt);
-    p->timings.launches++;
+    k_classify<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo);
+    k_near_count<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, cnt);
+    p->timings.launches += 2;
     std::vector<int32_t> hc(p->Nn);
     std::vector<int64_t> ho(p->Nn + 1, 0);
     if (cudaMemcpyAsync(hc.data(), cnt, p->Nn * sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -1004,8 +1021,7 @@ static int build_near_list(DeviceProblem *p) {
         return r;
     }
     if (n > 0) {
-        if (mixed) k_near_list<true><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, off, p->near_link, p->near_row);
-        else k_near_list<false><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, off, p->near_link, p->near_row);
+        k_near_list<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, off, p->near_link, p->near_row);
         p->timings.launches++;
     }
     cudaError_t e = cudaStreamSynchronize(s);
