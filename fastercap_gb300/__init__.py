@@ -136,6 +136,7 @@ def lib() -> C.CDLL:
     L.fcg_problem_get_coefficients.argtypes = [vp, vp, vp]
     L.fcg_problem_matvec.argtypes = [vp, vp, vp, C.c_int]
     L.fcg_problem_matvec_device.argtypes = [vp, vp, vp, C.c_int]
+    L.fcg_problem_matvec_device_noalloc.argtypes = [vp, vp, vp, C.c_int]
     L.fcg_problem_solve.argtypes = [vp, C.POINTER(SolveOptions), vp, vp]
     L.fcg_problem_get_charges.argtypes = [vp, vp]
     L.fcg_run_command_line.argtypes = [C.c_char_p]
@@ -302,6 +303,11 @@ class Problem:
 
     def matvec_device(self, q_ptr: int, v_ptr: int, k: int):
         _check(lib().fcg_problem_matvec_device(self._h, C.c_void_p(q_ptr), C.c_void_p(v_ptr), k), "matvec")
+
+    def matvec_device_noalloc(self, q_ptr: int, v_ptr: int, k: int) -> int:
+        """The product without any device allocation (fixed per-GPU scratch);
+        returns the FC_* status instead of raising."""
+        return int(lib().fcg_problem_matvec_device_noalloc(self._h, C.c_void_p(q_ptr), C.c_void_p(v_ptr), k))
 
     def solve(self, tol: float = 0.01, precond: int = PRECOND_JACOBI, max_iter: int = 0, allow_not_converged=False):
         cap = np.empty((self.n_cond, self.n_cond), np.float64)

@@ -41,6 +41,7 @@ int problem_fill(DeviceProblem *p);
 int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_coef);
 int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k);
 int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k);
+int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int k);
 int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations);
 int problem_get_charges(DeviceProblem *p, double *charges);
 int problem_n_cond(const DeviceProblem *p);

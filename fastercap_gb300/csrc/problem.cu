@@ -23,6 +23,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1439,6 +1440,127 @@ int problem_get_charges(DeviceProblem *p, double *charges) {
     if (!p->x) { set_error("no solve has run"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
     FCG_CK(cudaMemcpy(charges, p->x, (size_t)p->x_k * p->Np * sizeof(double), cudaMemcpyDeviceToHost));
+    return FCG_NORMAL_END;
+}
+
+// ------------------------------------------------------ no-allocation matvec
+//
+// Some callers cannot allocate device memory at the point where they need a
+// product: code recording a CUDA graph (an allocation would break the
+// capture), hosts that reserve all device memory at start-up and forbid
+// allocation afterwards, or hosts whose device memory belongs to another
+// allocator. For them, problem_matvec_noalloc runs the same kernels as
+// problem_matvec_device with the node work arrays (charges, potentials,
+// ancestor sums) placed in this fixed, file-scope device array instead of the
+// problem's lazily allocated workspace. Every GPU that loads the library holds
+// the array until the process exits. All calls share it, and it keeps the
+// previous call's contents: calls that overlap on the GPU (different streams,
+// different problems) race on it and must be serialised by the caller.
+static const size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static const int kMaxDevices = 64;
+static void *g_noalloc_addr[kMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+// Resolve the device address of the scratch array for the current device
+// (once per device; the first call on a device should come before any stream
+// capture).
+static int noalloc_scratch(int device, unsigned char **out) {
+    if (device < 0 || device >= kMaxDevices) { set_error("device index out of range"); return FCG_DEVICE_ERROR; }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[device]) {
+        void *ptr = NULL;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            set_error(std::string("cudaGetSymbolAddress of the no-allocation scratch failed: ") + cudaGetErrorString(e));
+            return FCG_DEVICE_ERROR;
+        }
+        g_noalloc_addr[device] = ptr;
+    }
+    *out = (unsigned char *)g_noalloc_addr[device];
+    return FCG_NORMAL_END;
+}
+
+static size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// bytes of scratch a product with kp padded right-hand sides needs
+static size_t noalloc_need(const DeviceProblem *p, int kp) {
+    size_t n = (size_t)p->Nn * kp;
+    size_t need = 3 * align256(n * sizeof(double));
+    if (p->precision == FCG_PREC_MIXED) need += align256(n * sizeof(float));
+    return need;
+}
+
+int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int k) {
+    if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
+    if (k < 1 || k > kMaxK) { set_error("right-hand sides per matvec must be in [1, 32]"); return FCG_GENERIC_ERROR; }
+    int kp = kpad(k);
+    size_t need = noalloc_need(p, kp);
+    if (need > kNoAllocScratchBytes) {
+        set_error("no-allocation matvec: the model needs " + std::to_string(need) + " bytes of node scratch for " +
+                  std::to_string(k) + " right-hand side(s), more than the fixed " + std::to_string(kNoAllocScratchBytes) +
+                  "-byte array; use fcg_problem_matvec_device or fewer right-hand sides");
+        return FCG_OUT_OF_MEMORY;
+    }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    unsigned char *base = NULL;
+    int r = noalloc_scratch(p->ctx->device, &base);
+    if (r != FCG_NORMAL_END) return r;
+    size_t n = (size_t)p->Nn * kp;
+    double *Qd = (double *)base;
+    double *Pd = (double *)(base + align256(n * sizeof(double)));
+    double *Ad = (double *)(base + 2 * align256(n * sizeof(double)));
+    float *Qf = (float *)(base + 3 * align256(n * sizeof(double)));
+    cudaStream_t s = p->stream;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    const SweepPlan &pl = p->plan;
+    int64_t Np = p->Np;
+    if (kp != k) {
+        // padded right-hand sides must read as zero charges
+        FCG_CK(cudaMemsetAsync(Qd, 0, n * sizeof(double), s));
+        if (mixed) FCG_CK(cudaMemsetAsync(Qf, 0, n * sizeof(float), s));
+    }
+    if (mixed) k_up_block<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, d_q, Np, k, kp, NULL, Qd, Qf, p->left, p->right);
+    else k_up_block<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, d_q, Np, k, kp, NULL, Qd, Qf, p->left, p->right);
+    FCG_CK(cudaGetLastError());
+    if (pl.n_top_levels > 0) {
+        if (mixed) k_up_top<true><<<1, 1024, 0, s>>>(pl, k, kp, Qd, Qf, p->left, p->right);
+        else k_up_top<false><<<1, 1024, 0, s>>>(pl, k, kp, Qd, Qf, p->left, p->right);
+        FCG_CK(cudaGetLastError());
+    }
+    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
+    if (p->L > 0) {
+        if (!mixed) {
+            switch (kp) {
+            case 1: k_spmv64<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
+            case 2: k_spmv64<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
+            case 4: k_spmv64<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
+            case 8: k_spmv64<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
+            case 16: k_spmv64<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
+            default: k_spmv64<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
+            }
+        } else {
+            switch (kp) {
+            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
+            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
+            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
+            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
+            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
+            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
+            }
+        }
+        FCG_CK(cudaGetLastError());
+    } else {
+        FCG_CK(cudaMemsetAsync(Pd, 0, n * sizeof(double), s));
+    }
+    if (pl.n_top_levels > 0) {
+        k_down_top<double><<<1, 1024, 0, s>>>(pl, k, kp, Pd, Ad, p->parent);
+        FCG_CK(cudaGetLastError());
+    }
+    k_down_block<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, d_q, Np, k, kp, NULL, p->self, Pd, Ad, p->parent, d_v);
+    FCG_CK(cudaGetLastError());
+    FCG_CK(cudaStreamSynchronize(s));
     return FCG_NORMAL_END;
 }
 

@@ -193,6 +193,9 @@ int fcg_problem_matvec(fcg_problem *p, const double *q, double *v, int k) {
 int fcg_problem_matvec_device(fcg_problem *p, const double *q, double *v, int k) {
     return (p && q && v && k > 0) ? fcg::problem_matvec_device(p->p, q, v, k) : FCG_GENERIC_ERROR;
 }
+int fcg_problem_matvec_device_noalloc(fcg_problem *p, const double *q, double *v, int k) {
+    return (p && q && v && k > 0) ? fcg::problem_matvec_noalloc(p->p, q, v, k) : FCG_GENERIC_ERROR;
+}
 int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap, int *iterations) {
     if (!p) return FCG_GENERIC_ERROR;
     fcg_solve_options o;
