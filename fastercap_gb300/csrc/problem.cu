@@ -83,7 +83,7 @@ template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes
 
 struct SweepPlan {
     int n_blocks = 0, n_top_levels = 0, max_block_levels = 0;
-    int32_t *blk_leaf_first = NULL, *blk_nleaves = NULL, *blk_lvl_first = NULL, *blk_nlvls = NULL;
+    int32_t *blk_leaf_first = NULL, *blk_nleaves = NULL, *blk_lvl_first = NULL, *blk_nlvls = NULL, *blk_root = NULL;
     int32_t *lvl_ptr = NULL, *lvl_nodes = NULL;
     int32_t *top_lvl_ptr = NULL, *top_nodes = NULL;
 };
@@ -124,7 +124,9 @@ struct DeviceProblem {
     // matvec workspace (kcap values per node)
     int kcap = 0;
     double *Qd = NULL, *Pd = NULL, *Ad = NULL;
-    float *Qf = NULL, *Pf = NULL;
+    float *Qf = NULL;
+    float2 *Pf2 = NULL;
+    int *arrive = NULL;  // per-node arrival counters of the up-sweep (zero between products)
 
     // Krylov workspace
     int gk = 0, gM = 0;  // right-hand sides, max iterations allocated
@@ -273,12 +275,17 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
     }
 }
 
-// Up-sweep over the sweep subtrees: leaves take the (optionally Jacobi
-// scaled) input, internal nodes add their children level by level.
+// Up-sweep (CMultHier::ComputePanelCharges_fast, Solver/MultiplyHierarchical.cpp:72-127):
+// each CTA takes one subtree of at most kBlockLeaves leaves - leaves read the
+// (optionally Jacobi-scaled) input, internal nodes add their children level by
+// level - and then climbs the top of the tree: a CTA that completes a top
+// node's child increments that node's arrival counter, and the CTA that
+// arrives second (both children done) computes the node and goes on to its
+// parent. Nothing ever waits; the second arriver resets the counter.
 template <bool MIXED>
-__global__ void k_up_block(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
-                           const double *__restrict__ in, int64_t ld, int k, int kp, const double *__restrict__ diag,
-                           double *Qd, float *Qf, const int32_t *__restrict__ left_of, const int32_t *__restrict__ right_of) {
+__global__ void k_up(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const double *__restrict__ in, int64_t ld,
+                     int k, int kp, const double *__restrict__ diag, double *Qd, float *Qf, const int32_t *__restrict__ left_of,
+                     const int32_t *__restrict__ right_of, const int32_t *__restrict__ parent, int *arrive) {
     int b = blockIdx.x;
     int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b];
     for (int t = threadIdx.x; t < nl * k; t += blockDim.x) {
@@ -293,62 +300,87 @@ __global__ void k_up_block(const SweepPlan plan, const int32_t *__restrict__ lea
     __syncthreads();
     int lv0 = plan.blk_lvl_first[b], nlv = plan.blk_nlvls[b];
     for (int h = 0; h < nlv; h++) {
-        int a = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a;
+        int a0 = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a0;
         for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int n = plan.lvl_nodes[a + t % cnt], r = t / cnt;
-            double s = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
-            Qd[(int64_t)n * kp + r] = s;
-            if (MIXED) Qf[(int64_t)n * kp + r] = (float)s;
+            int n = plan.lvl_nodes[a0 + t % cnt], r = t / cnt;
+            double sum = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
+            Qd[(int64_t)n * kp + r] = sum;
+            if (MIXED) Qf[(int64_t)n * kp + r] = (float)sum;
         }
         __syncthreads();
     }
-}
-
-template <bool MIXED>
-__global__ void k_up_top(const SweepPlan plan, int k, int kp, double *Qd, float *Qf, const int32_t *__restrict__ left_of,
-                         const int32_t *__restrict__ right_of) {
-    for (int h = 0; h < plan.n_top_levels; h++) {
-        int a = plan.top_lvl_ptr[h], e = plan.top_lvl_ptr[h + 1], cnt = e - a;
-        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int n = plan.top_nodes[a + t % cnt], r = t / cnt;
-            double s = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
-            Qd[(int64_t)n * kp + r] = s;
-            if (MIXED) Qf[(int64_t)n * kp + r] = (float)s;
+    // every thread publishes its node values GPU-wide before the root is signalled
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    int lane = threadIdx.x;
+    int p = parent[plan.blk_root[b]];
+    while (p >= 0) {
+        __threadfence();  // this CTA's node values are visible GPU-wide before it signals
+        int old = 0;
+        if (lane == 0) old = atomicAdd(&arrive[p], 1);
+        old = __shfl_sync(0xffffffffu, old, 0);
+        if (old == 0) break;  // the sibling's CTA finishes this node
+        if (lane == 0) arrive[p] = 0;
+        int l = left_of[p], r = right_of[p];
+        for (int rr = lane; rr < k; rr += 32) {
+            double sum = __ldcg(&Qd[(int64_t)l * kp + rr]) + __ldcg(&Qd[(int64_t)r * kp + rr]);
+            Qd[(int64_t)p * kp + rr] = sum;
+            if (MIXED) Qf[(int64_t)p * kp + rr] = (float)sum;
         }
-        __syncthreads();
+        p = parent[p];
     }
 }
 
+__device__ __forceinline__ double pval(const double *P, int64_t i) { return P[i]; }
+__device__ __forceinline__ double pval(const float2 *P, int64_t i) {
+    float2 v = P[i];
+    return (double)v.x + (double)v.y;
+}
+
+// Down-sweep (CMultHier::ComputeLeafPotentials_fast, Solver/MultiplyHierarchical.cpp:231-283):
+// A(n) = P(n) + A(parent(n)) from the top; each CTA first sums the link
+// potentials of its subtree root's ancestors (top down, the reference's
+// order), then descends its subtree level by level and writes
+// v = (self * x + P(leaf)) + A(parent(leaf)).
 template <class TP>
-__global__ void k_down_top(const SweepPlan plan, int k, int kp, const TP *__restrict__ P, double *A,
-                           const int32_t *__restrict__ parent) {
-    for (int h = plan.n_top_levels - 1; h >= 0; h--) {
-        int a = plan.top_lvl_ptr[h], e = plan.top_lvl_ptr[h + 1], cnt = e - a;
-        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int n = plan.top_nodes[a + t % cnt], r = t / cnt;
-            int p = parent[n];
-            double acc = (double)P[(int64_t)n * kp + r];
-            if (p >= 0) acc = acc + A[(int64_t)p * kp + r];
-            A[(int64_t)n * kp + r] = acc;
-        }
-        __syncthreads();
-    }
-}
-
-template <class TP>
-__global__ void k_down_block(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const double *__restrict__ in,
-                             int64_t ld, int k, int kp, const double *__restrict__ diag, const double *__restrict__ self,
-                             const TP *__restrict__ P, double *A, const int32_t *__restrict__ parent,
-                             double *__restrict__ out) {
+__global__ void k_down(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const double *__restrict__ in, int64_t ld,
+                       int k, int kp, const double *__restrict__ diag, const double *__restrict__ self, const TP *__restrict__ P,
+                       double *A, const int32_t *__restrict__ parent, double *__restrict__ out, unsigned *status) {
+    __shared__ double s_anc[32];
+    __shared__ int s_hasp;
+    const int kMaxChain = 96;
     int b = blockIdx.x;
+    int root = plan.blk_root[b];
+    if (threadIdx.x < 32) {
+        int chain[kMaxChain];
+        int n = 0;
+        int pp = parent[root];
+        while (pp >= 0 && n < kMaxChain) { chain[n++] = pp; pp = parent[pp]; }
+        if (pp >= 0 && threadIdx.x == 0) atomicOr(status, 4u);  // deeper than supported: flagged, result invalid
+        for (int rr = threadIdx.x; rr < k; rr += 32) {
+            double acc = 0.0;
+            if (n > 0) {
+                acc = pval(P, (int64_t)chain[n - 1] * kp + rr);
+                for (int i = n - 2; i >= 0; i--) acc = pval(P, (int64_t)chain[i] * kp + rr) + acc;
+            }
+            s_anc[rr] = acc;
+        }
+        if (threadIdx.x == 0) s_hasp = n > 0;
+    }
+    __syncthreads();
+    bool hasp = s_hasp != 0;
     int lv0 = plan.blk_lvl_first[b], nlv = plan.blk_nlvls[b];
     for (int h = nlv - 1; h >= 0; h--) {
-        int a = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a;
+        int a0 = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a0;
         for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int n = plan.lvl_nodes[a + t % cnt], r = t / cnt;
-            int p = parent[n];
-            double acc = (double)P[(int64_t)n * kp + r];
-            if (p >= 0) acc = acc + A[(int64_t)p * kp + r];
+            int n = plan.lvl_nodes[a0 + t % cnt], r = t / cnt;
+            double acc = pval(P, (int64_t)n * kp + r);
+            if (n == root) {
+                if (hasp) acc = acc + s_anc[r];
+            } else {
+                acc = acc + A[(int64_t)parent[n] * kp + r];
+            }
             A[(int64_t)n * kp + r] = acc;
         }
         __syncthreads();
@@ -359,16 +391,21 @@ __global__ void k_down_block(const SweepPlan plan, const int32_t *__restrict__ l
         int j = lf + i;
         double xv = in[(int64_t)r * ld + j];
         if (diag) xv = xv / diag[j];
-        int64_t node = leaf_node[j];
-        int p = parent[node];
-        double v = self[j] * xv + (double)P[node * kp + r];
-        if (p >= 0) v = v + A[(int64_t)p * kp + r];
+        int node = leaf_node[j];
+        double v = self[j] * xv + pval(P, (int64_t)node * kp + r);
+        if (node == root) {
+            if (hasp) v = v + s_anc[r];
+        } else {
+            v = v + A[(int64_t)parent[node] * kp + r];
+        }
         out[(int64_t)r * ld + j] = v;
     }
 }
 
-// Link product, FP64: one warp per destination node, lanes stride over the
-// node's links, K right-hand sides per link.
+// Link product, FP64 (CMultHier::ComputePanelPotentials_2fast,
+// Solver/MultiplyHierarchical.cpp:141-226): one warp per destination node,
+// lanes stride over the node's links four at a time with independent loads,
+// K right-hand sides per link.
 template <int K>
 __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                          const double *__restrict__ coef, const double *__restrict__ Q, double *__restrict__ P) {
@@ -379,10 +416,23 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint
         double acc[K];
 #pragma unroll
         for (int r = 0; r < K; r++) acc[r] = 0.0;
-        int64_t s = ptr[row], e = ptr[row + 1];
-        for (int64_t l = s + lane; l < e; l += 32) {
-            double c = coef[l];
-            const double *q = Q + (int64_t)(src[l] & kSrcMask) * K;
+        int s = (int)ptr[row], e = (int)ptr[row + 1];
+        int l = s + lane;
+        for (; l + 96 < e; l += 128) {
+            double c[4];
+            uint32_t j[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + 32 * u]); j[u] = __ldcs(&src[l + 32 * u]) & kSrcMask; }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const double *q = Q + (int64_t)j[u] * K;
+#pragma unroll
+                for (int r = 0; r < K; r++) acc[r] += c[u] * q[r];
+            }
+        }
+        for (; l < e; l += 32) {
+            double c = __ldcs(&coef[l]);
+            const double *q = Q + (int64_t)(__ldcs(&src[l]) & kSrcMask) * K;
 #pragma unroll
             for (int r = 0; r < K; r++) acc[r] += c * q[r];
         }
@@ -398,9 +448,10 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint
 }
 
 // Compensated FP32 accumulation (Kahan-Babuska / Neumaier). Each product is
-// split exactly into p + e with one FMA (e = c*q - p), e goes to the
-// compensation, and the row sum leaves the kernel as FP64 (s + c): the
-// stored potentials keep the precision the FP32 stream carries.
+// split exactly into p + e with one FMA (e = c*q - p) and e joins the
+// compensation. The row sum leaves the kernel as the unevaluated pair
+// (sum, compensation), combined in FP64 by the down-sweep, so that no FP64
+// instruction runs in this kernel.
 struct KSum {
     float s, c;
 };
@@ -417,11 +468,26 @@ __device__ __forceinline__ void kmul_add(KSum &a, float c, float q) {
     a.c += e;
 }
 
-// Link product, mixed: FP32 coefficients and charges, compensated FP32 sums,
-// FP64 node potentials.
+template <int K> __device__ __forceinline__ void load_q(const float *__restrict__ Q, uint32_t j, float *q) {
+    if (K % 4 == 0) {
+        const float4 *q4 = reinterpret_cast<const float4 *>(Q + (int64_t)j * K);
+#pragma unroll
+        for (int r = 0; r < K / 4; r++) {
+            float4 v = q4[r];
+            q[4 * r] = v.x; q[4 * r + 1] = v.y; q[4 * r + 2] = v.z; q[4 * r + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < K; r++) q[r] = Q[(int64_t)j * K + r];
+    }
+}
+
+// Link product, mixed: FP32 coefficients and charges streamed, exact products
+// and compensated FP32 sums, one warp per destination node, four independent
+// links per lane in flight.
 template <int K>
 __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                         const float *__restrict__ coef, const float *__restrict__ Q, double *__restrict__ P) {
+                         const float *__restrict__ coef, const float *__restrict__ Q, float2 *__restrict__ P) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -429,10 +495,25 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
         KSum acc[K];
 #pragma unroll
         for (int r = 0; r < K; r++) { acc[r].s = 0.f; acc[r].c = 0.f; }
-        int64_t s = ptr[row], e = ptr[row + 1];
-        for (int64_t l = s + lane; l < e; l += 32) {
-            float c = coef[l];
-            const float *q = Q + (int64_t)(src[l] & kSrcMask) * K;
+        int s = (int)ptr[row], e = (int)ptr[row + 1];
+        int l = s + lane;
+        for (; l + 96 < e; l += 128) {
+            float c[4];
+            uint32_t j[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + 32 * u]); j[u] = __ldcs(&src[l + 32 * u]) & kSrcMask; }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                float q[K];
+                load_q<K>(Q, j[u], q);
+#pragma unroll
+                for (int r = 0; r < K; r++) kmul_add(acc[r], c[u], q[r]);
+            }
+        }
+        for (; l < e; l += 32) {
+            float c = __ldcs(&coef[l]);
+            float q[K];
+            load_q<K>(Q, __ldcs(&src[l]) & kSrcMask, q);
 #pragma unroll
             for (int r = 0; r < K; r++) kmul_add(acc[r], c, q[r]);
         }
@@ -450,7 +531,7 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
         }
 #pragma unroll
         for (int r = 0; r < K; r++)
-            if (lane == (r & 31)) P[row * K + r] = (double)acc[r].s + (double)acc[r].c;
+            if (lane == (r & 31)) P[row * K + r] = make_float2(acc[r].s, acc[r].c);
     }
 }
 
@@ -668,15 +749,28 @@ __global__ void k_init_state(int k, int M, double *nr2, double *nb2, double *nor
     else { active[r] = 1; iters[r] = 0; }
 }
 
-// cap[r][c] = sum over conductor c's leaves of weight * charge
-__global__ void k_assemble(int64_t Np, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
-                           const double *__restrict__ weight, const double *__restrict__ x, int ncol, double *__restrict__ cap) {
+// C assembly (CSolveCap::Solve, Solver/SolveCapacitance.cpp:1305-1366):
+// cap[r][c] = sum over conductor c's leaves of outer permittivity * charge.
+// Stage 1: every CTA sums one slice of kAsmChunk leaves of one conductor for
+// one right-hand side; stage 2 adds the slices in order (deterministic).
+static const int kAsmChunk = 4096;
+__global__ void k_assemble_part(int64_t Np, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
+                                const double *__restrict__ weight, const double *__restrict__ x, int ncol, double *__restrict__ part) {
     __shared__ double sh[32];
-    int c = blockIdx.x, r = blockIdx.y;
+    int sl = blockIdx.x, c = blockIdx.y, r = blockIdx.z;
+    int64_t lo = first[c] + (int64_t)sl * kAsmChunk, hi = min(first[c] + count[c], lo + kAsmChunk);
     double s = 0.0;
-    for (int64_t j = first[c] + threadIdx.x; j < first[c] + count[c]; j += blockDim.x) s += weight[j] * x[(int64_t)r * Np + j];
+    for (int64_t j = lo + threadIdx.x; j < hi; j += blockDim.x) s += weight[j] * x[(int64_t)r * Np + j];
     s = block_sum(s, sh);
-    if (threadIdx.x == 0) cap[(int64_t)r * ncol + c] = s;
+    if (threadIdx.x == 0) part[((int64_t)r * ncol + c) * gridDim.x + sl] = s;
+}
+
+__global__ void k_assemble_sum(int nslice, const double *__restrict__ part, int ncol, double *__restrict__ cap) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (c >= ncol) return;
+    double s = 0.0;
+    for (int i = 0; i < nslice; i++) s += part[((int64_t)r * ncol + c) * nslice + i];
+    cap[(int64_t)r * ncol + c] = s;
 }
 
 // -------------------------------------------------------------- host side
@@ -778,7 +872,7 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
     std::vector<int32_t> height(Nn, 0);
     for (int64_t i = 0; i < Nn; i++)
         if (!(a.node_type[i] & FCG_IS_LEAF)) height[i] = 1 + std::max(height[a.node_left[i]], height[a.node_right[i]]);
-    std::vector<int32_t> blk_leaf_first, blk_nleaves, blk_lvl_first, blk_nlvls, lvl_ptr, lvl_nodes;
+    std::vector<int32_t> blk_leaf_first, blk_nleaves, blk_lvl_first, blk_nlvls, blk_root, lvl_ptr, lvl_nodes;
     std::vector<int32_t> top_cnt;
     std::vector<std::vector<int32_t>> top_by_h;
     int max_lv = 0;
@@ -798,6 +892,7 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
         blk_nleaves.push_back((int32_t)lc);
         blk_lvl_first.push_back((int32_t)lvl_ptr.size());
         blk_nlvls.push_back(H);
+        blk_root.push_back((int32_t)i);
         std::vector<std::vector<int32_t>> byh(H + 1);
         for (int64_t n = first; n <= i; n++)
             if (!(a.node_type[n] & FCG_IS_LEAF)) byh[height[n]].push_back((int32_t)n);
@@ -807,6 +902,15 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
         }
         lvl_ptr.push_back((int32_t)lvl_nodes.size());
         max_lv = std::max(max_lv, H);
+    }
+    // the down-sweep sums a subtree root's ancestors from a bounded chain
+    for (size_t b = 0; b < blk_root.size(); b++) {
+        int depth = 0;
+        for (int32_t q = parent[blk_root[b]]; q >= 0; q = parent[q]) depth++;
+        if (depth > 96) {
+            set_error("node tree too deep above its 256-leaf subtrees (" + std::to_string(depth) + " levels, at most 96)");
+            return FCG_GENERIC_ERROR;
+        }
     }
     // lvl_ptr holds, per block, H+1 offsets; blk_lvl_first indexes into it
     std::vector<int32_t> top_lvl_ptr(1, 0), top_nodes;
@@ -824,6 +928,7 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
     if ((r = upload(&pl.blk_nleaves, blk_nleaves.data(), blk_nleaves.size(), p->bytes, s))) return r;
     if ((r = upload(&pl.blk_lvl_first, blk_lvl_first.data(), blk_lvl_first.size(), p->bytes, s))) return r;
     if ((r = upload(&pl.blk_nlvls, blk_nlvls.data(), blk_nlvls.size(), p->bytes, s))) return r;
+    if ((r = upload(&pl.blk_root, blk_root.data(), blk_root.size(), p->bytes, s))) return r;
     if ((r = upload(&pl.lvl_ptr, lvl_ptr.data(), lvl_ptr.size(), p->bytes, s))) return r;
     if ((r = upload(&pl.lvl_nodes, lvl_nodes.data(), lvl_nodes.size(), p->bytes, s))) return r;
     if ((r = upload(&pl.top_lvl_ptr, top_lvl_ptr.data(), top_lvl_ptr.size(), p->bytes, s))) return r;
@@ -900,6 +1005,12 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
     FCG_TRY(build_plan(p, a, parent, s));
+    FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
+    if (cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s) != cudaSuccess) {
+        set_error("cannot clear the arrival counters");
+        problem_destroy(p);
+        return FCG_DEVICE_ERROR;
+    }
     FCG_TRY(upload(&p->left, a.node_left, Nn, p->bytes, s));
     FCG_TRY(upload(&p->right, a.node_right, Nn, p->bytes, s));
     if (cudaStreamSynchronize(s) != cudaSuccess) {
@@ -921,9 +1032,9 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
     dfree(p->near_link); dfree(p->near_row);
     SweepPlan &pl = p->plan;
-    dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls);
+    dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
     dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
-    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf);
+    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->arrive);
     for (size_t i = 0; i < p->V.size(); i++) dfree(p->V[i]);
     dfree(p->Vptr); dfree(p->H); dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->normb); dfree(p->hnorm);
     dfree(p->nrm2); dfree(p->z); dfree(p->partial); dfree(p->active); dfree(p->iters); dfree(p->n_active);
@@ -1096,19 +1207,87 @@ static int kpad(int k) {
 
 static int ensure_matvec_ws(DeviceProblem *p, int kp) {
     if (p->kcap >= kp) return FCG_NORMAL_END;
-    int64_t before = p->bytes;
-    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf);
-    p->bytes = before - (int64_t)p->kcap * p->Nn * (p->precision == FCG_PREC_FP64 ? 24 : 24);
+    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2);
     p->kcap = 0;
     int r;
     size_t n = (size_t)p->Nn * kp;
     if ((r = dalloc(&p->Qd, n, p->bytes))) return r;
     if ((r = dalloc(&p->Ad, n, p->bytes))) return r;
-    if ((r = dalloc(&p->Pd, n, p->bytes))) return r;
     if (p->precision == FCG_PREC_MIXED) {
         if ((r = dalloc(&p->Qf, n, p->bytes))) return r;
+        if ((r = dalloc(&p->Pf2, n, p->bytes))) return r;
+    } else {
+        if ((r = dalloc(&p->Pd, n, p->bytes))) return r;
     }
     p->kcap = kp;
+    return FCG_NORMAL_END;
+}
+
+// node work arrays of one product (kp values per node)
+struct NodeWork {
+    double *Qd;
+    float *Qf;
+    double *Pd;
+    float2 *Pf2;
+    double *Ad;
+};
+
+// The three launches of one product v = P * (in / diag): up-sweep, link
+// product, down-sweep. Arrays in/out are [k][Np] on the device.
+static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag) {
+    cudaStream_t s = p->stream;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    const SweepPlan &pl = p->plan;
+    int64_t Np = p->Np;
+    size_t n = (size_t)p->Nn * kp;
+    if (kp != k) {
+        // padded right-hand sides carry zero charges
+        FCG_CK(cudaMemsetAsync(w.Qd, 0, n * sizeof(double), s));
+        if (mixed) FCG_CK(cudaMemsetAsync(w.Qf, 0, n * sizeof(float), s));
+    }
+    if (mixed) k_up<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
+    else k_up<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
+    FCG_CK(cudaGetLastError());
+    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
+    int64_t launches = 2;
+    if (p->L > 0) {
+        // coefficient + source word per link, row offsets, one charge read and
+        // one potential write per node and right-hand side
+        int64_t cb = mixed ? 4 : 8;
+        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + (cb + 8) * (int64_t)k * p->Nn;
+        p->timings.link_launches++;
+        launches++;
+        prof_begin(p);
+        if (!mixed) {
+            switch (kp) {
+            case 1: k_spmv64<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 2: k_spmv64<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 4: k_spmv64<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 8: k_spmv64<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 16: k_spmv64<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            default: k_spmv64<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            }
+        } else {
+            switch (kp) {
+            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            }
+        }
+        prof_end(p);
+        FCG_CK(cudaGetLastError());
+    } else {
+        if (mixed) FCG_CK(cudaMemsetAsync(w.Pf2, 0, n * sizeof(float2), s));
+        else FCG_CK(cudaMemsetAsync(w.Pd, 0, n * sizeof(double), s));
+    }
+    if (mixed) k_down<float2><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, w.Pf2, w.Ad, p->parent, out, p->status);
+    else k_down<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, w.Pd, w.Ad, p->parent, out, p->status);
+    FCG_CK(cudaGetLastError());
+    p->timings.matvecs++;
+    p->timings.launches += launches;
     return FCG_NORMAL_END;
 }
 
@@ -1118,66 +1297,8 @@ static int matvec(DeviceProblem *p, const double *in, double *out, int k, const 
     int kp = kpad(k);
     int r = ensure_matvec_ws(p, kp);
     if (r != FCG_NORMAL_END) return r;
-    cudaStream_t s = p->stream;
-    bool mixed = p->precision == FCG_PREC_MIXED;
-    const SweepPlan &pl = p->plan;
-    int64_t Np = p->Np;
-    if (kp != k) {
-        // padded right-hand sides carry zeros
-        FCG_CK(cudaMemsetAsync(p->Qd, 0, (size_t)p->Nn * kp * sizeof(double), s));
-        if (mixed) FCG_CK(cudaMemsetAsync(p->Qf, 0, (size_t)p->Nn * kp * sizeof(float), s));
-    }
-    if (mixed) k_up_block<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, in, Np, k, kp, diag, p->Qd, p->Qf, p->left, p->right);
-    else k_up_block<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, in, Np, k, kp, diag, p->Qd, p->Qf, p->left, p->right);
-    FCG_CK(cudaGetLastError());
-    if (pl.n_top_levels > 0) {
-        if (mixed) k_up_top<true><<<1, 1024, 0, s>>>(pl, k, kp, p->Qd, p->Qf, p->left, p->right);
-        else k_up_top<false><<<1, 1024, 0, s>>>(pl, k, kp, p->Qd, p->Qf, p->left, p->right);
-        FCG_CK(cudaGetLastError());
-    }
-    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
-    int64_t launches = 2 + (pl.n_top_levels > 0 ? 2 : 0);
-    if (p->L > 0) {
-        // coefficient + source index per link, row offsets, one charge read and
-        // one potential write per node and right-hand side
-        int64_t cb = mixed ? 4 : 8;
-        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + (cb + 8) * (int64_t)k * p->Nn;
-        p->timings.link_launches++;
-        launches++;
-        prof_begin(p);
-        if (!mixed) {
-            switch (kp) {
-            case 1: k_spmv64<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
-            case 2: k_spmv64<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
-            case 4: k_spmv64<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
-            case 8: k_spmv64<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
-            case 16: k_spmv64<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
-            default: k_spmv64<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, p->Qd, p->Pd); break;
-            }
-        } else {
-            switch (kp) {
-            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
-            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
-            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
-            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
-            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
-            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, p->Qf, p->Pd); break;
-            }
-        }
-        prof_end(p);
-        FCG_CK(cudaGetLastError());
-    } else {
-        FCG_CK(cudaMemsetAsync(p->Pd, 0, (size_t)p->Nn * kp * sizeof(double), s));
-    }
-    if (pl.n_top_levels > 0) {
-        k_down_top<double><<<1, 1024, 0, s>>>(pl, k, kp, p->Pd, p->Ad, p->parent);
-        FCG_CK(cudaGetLastError());
-    }
-    k_down_block<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, p->Pd, p->Ad, p->parent, out);
-    FCG_CK(cudaGetLastError());
-    p->timings.matvecs++;
-    p->timings.launches += launches;
-    return FCG_NORMAL_END;
+    NodeWork w = {p->Qd, p->Qf, p->Pd, p->Pf2, p->Ad};
+    return launch_matvec(p, w, in, out, k, kp, diag);
 }
 
 int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k) {
@@ -1312,12 +1433,15 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     std::vector<int64_t> cf(ncol), cc(ncol);
     for (int c = 0; c < ncol; c++) { cf[c] = p->cond_first[p->cond_cols[c]]; cc[c] = p->cond_count[p->cond_cols[c]]; }
     int64_t *d_cf = NULL, *d_cc = NULL;
-    double *d_cap = NULL;
-    int64_t tmpb = 0;
+    double *d_cap = NULL, *d_part = NULL;
+    int64_t tmpb = 0, maxcount = 1;
+    for (int c = 0; c < ncol; c++) maxcount = std::max(maxcount, cc[c]);
+    int nslice = (int)((maxcount + kAsmChunk - 1) / kAsmChunk);
     int r;
     if ((r = upload(&d_cf, cf.data(), ncol, tmpb, s)) || (r = upload(&d_cc, cc.data(), ncol, tmpb, s)) ||
-        (r = dalloc(&d_cap, (size_t)ncol * ncol, tmpb))) {
-        dfree(d_cf); dfree(d_cc); dfree(d_cap);
+        (r = dalloc(&d_cap, (size_t)ncol * ncol, tmpb)) ||
+        (r = dalloc(&d_part, (size_t)nslice * ncol * std::min(ncol, kMaxK), tmpb))) {
+        dfree(d_cf); dfree(d_cc); dfree(d_cap); dfree(d_part);
         return r;
     }
     std::vector<double> h_cap((size_t)ncol * ncol, 0.0);
@@ -1402,9 +1526,10 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->x);
         FCG_CK(cudaGetLastError());
         cudaEventRecord(p->ev1, s);
-        k_assemble<<<dim3(ncol, k), 256, 0, s>>>(Np, d_cf, d_cc, p->leaf_weight, p->x, ncol, d_cap + (size_t)c0 * ncol);
+        k_assemble_part<<<dim3(nslice, ncol, k), 256, 0, s>>>(Np, d_cf, d_cc, p->leaf_weight, p->x, ncol, d_part);
+        k_assemble_sum<<<dim3((ncol + 31) / 32, k), 32, 0, s>>>(nslice, d_part, ncol, d_cap + (size_t)c0 * ncol);
         FCG_CK(cudaGetLastError());
-        p->timings.launches += 4;
+        p->timings.launches += 5;
         FCG_CK(cudaStreamSynchronize(s));
         prof_collect(p);
         float ms = 0;
@@ -1433,6 +1558,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     dfree(d_cf);
     dfree(d_cc);
     dfree(d_cap);
+    dfree(d_part);
     return status;
 }
 
@@ -1508,58 +1634,15 @@ int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int
     int r = noalloc_scratch(p->ctx->device, &base);
     if (r != FCG_NORMAL_END) return r;
     size_t n = (size_t)p->Nn * kp;
-    double *Qd = (double *)base;
-    double *Pd = (double *)(base + align256(n * sizeof(double)));
-    double *Ad = (double *)(base + 2 * align256(n * sizeof(double)));
-    float *Qf = (float *)(base + 3 * align256(n * sizeof(double)));
+    NodeWork w;
+    w.Qd = (double *)base;
+    w.Pd = (double *)(base + align256(n * sizeof(double)));
+    w.Pf2 = (float2 *)w.Pd;  // the FP64 and mixed potential arrays share the slot (8 bytes per value)
+    w.Ad = (double *)(base + 2 * align256(n * sizeof(double)));
+    w.Qf = (float *)(base + 3 * align256(n * sizeof(double)));
     cudaStream_t s = p->stream;
-    bool mixed = p->precision == FCG_PREC_MIXED;
-    const SweepPlan &pl = p->plan;
-    int64_t Np = p->Np;
-    if (kp != k) {
-        // padded right-hand sides must read as zero charges
-        FCG_CK(cudaMemsetAsync(Qd, 0, n * sizeof(double), s));
-        if (mixed) FCG_CK(cudaMemsetAsync(Qf, 0, n * sizeof(float), s));
-    }
-    if (mixed) k_up_block<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, d_q, Np, k, kp, NULL, Qd, Qf, p->left, p->right);
-    else k_up_block<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, p->geo, d_q, Np, k, kp, NULL, Qd, Qf, p->left, p->right);
-    FCG_CK(cudaGetLastError());
-    if (pl.n_top_levels > 0) {
-        if (mixed) k_up_top<true><<<1, 1024, 0, s>>>(pl, k, kp, Qd, Qf, p->left, p->right);
-        else k_up_top<false><<<1, 1024, 0, s>>>(pl, k, kp, Qd, Qf, p->left, p->right);
-        FCG_CK(cudaGetLastError());
-    }
-    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
-    if (p->L > 0) {
-        if (!mixed) {
-            switch (kp) {
-            case 1: k_spmv64<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
-            case 2: k_spmv64<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
-            case 4: k_spmv64<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
-            case 8: k_spmv64<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
-            case 16: k_spmv64<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
-            default: k_spmv64<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, Qd, Pd); break;
-            }
-        } else {
-            switch (kp) {
-            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
-            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
-            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
-            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
-            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
-            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, Qf, Pd); break;
-            }
-        }
-        FCG_CK(cudaGetLastError());
-    } else {
-        FCG_CK(cudaMemsetAsync(Pd, 0, n * sizeof(double), s));
-    }
-    if (pl.n_top_levels > 0) {
-        k_down_top<double><<<1, 1024, 0, s>>>(pl, k, kp, Pd, Ad, p->parent);
-        FCG_CK(cudaGetLastError());
-    }
-    k_down_block<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, d_q, Np, k, kp, NULL, p->self, Pd, Ad, p->parent, d_v);
-    FCG_CK(cudaGetLastError());
+    r = launch_matvec(p, w, d_q, d_v, k, kp, NULL);
+    if (r != FCG_NORMAL_END) return r;
     FCG_CK(cudaStreamSynchronize(s));
     return FCG_NORMAL_END;
 }
