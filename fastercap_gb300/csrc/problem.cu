@@ -103,6 +103,7 @@ struct DeviceProblem {
     // near-field (band 0) link list, built on the first fill
     int64_t n_near = -1;
     int32_t *near_link = NULL, *near_row = NULL;
+    fcg_tri64 *tri = NULL;  // source-triangle tables for the near field
     SolveTimings timings;
     // profiling of the link product: event pairs awaiting readout
     bool profiling = false;
@@ -127,6 +128,7 @@ struct DeviceProblem {
     float *Qf = NULL;
     float2 *Pf2 = NULL;
     int *arrive = NULL;  // per-node arrival counters of the up-sweep (zero between products)
+    int spmv_lanes = 32;  // lanes per destination node in the link product (8, 16 or 32)
 
     // Krylov workspace
     int gk = 0, gM = 0;  // right-hand sides, max iterations allocated
@@ -249,15 +251,22 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const ui
     }
 }
 
+// source-triangle tables of the near-field kernel, one per node
+__global__ void k_make_tri(int64_t Nn, const NodeGeo *__restrict__ geo, fcg_tri64 *__restrict__ tri) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x)
+        fcg_tri64_make(geo[i].v, tri[i]);
+}
+
 // Near-field links (band 0), FP64 analytic, one thread per listed link.
 __global__ void k_fill_near(int64_t n, const int32_t *__restrict__ near_link, const int32_t *__restrict__ near_row,
-                            const uint32_t *__restrict__ src, const NodeGeo *__restrict__ geo, double *__restrict__ c64,
-                            float *__restrict__ c32, unsigned *status) {
+                            const uint32_t *__restrict__ src, const NodeGeo *__restrict__ geo, const fcg_tri64 *__restrict__ tri,
+                            double *__restrict__ c64, float *__restrict__ c32, unsigned *status) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t l = near_link[t];
         const NodeGeo &g1 = geo[near_row[t]];
-        const NodeGeo &g2 = geo[src[l] & kSrcMask];
-        double val = fcg_pot_near(g1.type, g1.c, g1.n, g2.c, g2.v);
+        uint32_t j = src[l] & kSrcMask;
+        const NodeGeo &g2 = geo[j];
+        double val = fcg_pot_near_tri(g1.type, g1.c, g1.n, g2.c, g2.v, tri[j]);
         if (!isfinite(val)) atomicOr(status, 1u);
         if (c64) c64[l] = val;
         else c32[l] = (float)val;
@@ -403,26 +412,29 @@ __global__ void k_down(const SweepPlan plan, const int32_t *__restrict__ leaf_no
 }
 
 // Link product, FP64 (CMultHier::ComputePanelPotentials_2fast,
-// Solver/MultiplyHierarchical.cpp:141-226): one warp per destination node,
-// lanes stride over the node's links four at a time with independent loads,
-// K right-hand sides per link.
-template <int K>
+// Solver/MultiplyHierarchical.cpp:141-226): SW lanes per destination node
+// (32/SW nodes per warp in flight), lanes stride over the node's links four
+// at a time with independent loads, K right-hand sides per link.
+template <int K, int SW>
 __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                          const double *__restrict__ coef, const double *__restrict__ Q, double *__restrict__ P) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t row = warp; row < Nn; row += nwarps) {
+    const int G = 32 / SW;
+    int lane = threadIdx.x & 31, gl = lane % SW;
+    int64_t grp = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * G + lane / SW;
+    int64_t ngrp = (((int64_t)gridDim.x * blockDim.x) >> 5) * G;
+    for (int64_t base = grp - lane / SW; base < Nn; base += ngrp) {
+        int64_t row = base + lane / SW;
+        bool valid = row < Nn;
         double acc[K];
 #pragma unroll
         for (int r = 0; r < K; r++) acc[r] = 0.0;
-        int s = (int)ptr[row], e = (int)ptr[row + 1];
-        int l = s + lane;
-        for (; l + 96 < e; l += 128) {
+        int s = valid ? (int)ptr[row] : 0, e = valid ? (int)ptr[row + 1] : 0;
+        int l = s + gl;
+        for (; l + 3 * SW < e; l += 4 * SW) {
             double c[4];
             uint32_t j[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + 32 * u]); j[u] = __ldcs(&src[l + 32 * u]) & kSrcMask; }
+            for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + SW * u]); j[u] = __ldcs(&src[l + SW * u]) & kSrcMask; }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const double *q = Q + (int64_t)j[u] * K;
@@ -430,7 +442,7 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint
                 for (int r = 0; r < K; r++) acc[r] += c[u] * q[r];
             }
         }
-        for (; l < e; l += 32) {
+        for (; l < e; l += SW) {
             double c = __ldcs(&coef[l]);
             const double *q = Q + (int64_t)(__ldcs(&src[l]) & kSrcMask) * K;
 #pragma unroll
@@ -439,11 +451,13 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint
 #pragma unroll
         for (int r = 0; r < K; r++) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+            for (int o = SW / 2; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
         }
+        if (valid) {
 #pragma unroll
-        for (int r = 0; r < K; r++)
-            if (lane == (r & 31)) P[row * K + r] = acc[r];
+            for (int r = 0; r < K; r++)
+                if (gl == (r % SW)) P[row * K + r] = acc[r];
+        }
     }
 }
 
@@ -483,25 +497,28 @@ template <int K> __device__ __forceinline__ void load_q(const float *__restrict_
 }
 
 // Link product, mixed: FP32 coefficients and charges streamed, exact products
-// and compensated FP32 sums, one warp per destination node, four independent
-// links per lane in flight.
-template <int K>
+// and compensated FP32 sums; SW lanes per destination node (32/SW nodes per
+// warp in flight), four independent links per lane.
+template <int K, int SW>
 __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                          const float *__restrict__ coef, const float *__restrict__ Q, float2 *__restrict__ P) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t row = warp; row < Nn; row += nwarps) {
+    const int G = 32 / SW;
+    int lane = threadIdx.x & 31, gl = lane % SW;
+    int64_t grp = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * G + lane / SW;
+    int64_t ngrp = (((int64_t)gridDim.x * blockDim.x) >> 5) * G;
+    for (int64_t base = grp - lane / SW; base < Nn; base += ngrp) {
+        int64_t row = base + lane / SW;
+        bool valid = row < Nn;
         KSum acc[K];
 #pragma unroll
         for (int r = 0; r < K; r++) { acc[r].s = 0.f; acc[r].c = 0.f; }
-        int s = (int)ptr[row], e = (int)ptr[row + 1];
-        int l = s + lane;
-        for (; l + 96 < e; l += 128) {
+        int s = valid ? (int)ptr[row] : 0, e = valid ? (int)ptr[row + 1] : 0;
+        int l = s + gl;
+        for (; l + 3 * SW < e; l += 4 * SW) {
             float c[4];
             uint32_t j[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + 32 * u]); j[u] = __ldcs(&src[l + 32 * u]) & kSrcMask; }
+            for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + SW * u]); j[u] = __ldcs(&src[l + SW * u]) & kSrcMask; }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 float q[K];
@@ -510,7 +527,7 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
                 for (int r = 0; r < K; r++) kmul_add(acc[r], c[u], q[r]);
             }
         }
-        for (; l < e; l += 32) {
+        for (; l < e; l += SW) {
             float c = __ldcs(&coef[l]);
             float q[K];
             load_q<K>(Q, __ldcs(&src[l]) & kSrcMask, q);
@@ -521,7 +538,7 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
         for (int r = 0; r < K; r++) {
             KSum a = acc[r];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
+            for (int o = SW / 2; o > 0; o >>= 1) {
                 float os = __shfl_xor_sync(0xffffffffu, a.s, o);
                 float oc = __shfl_xor_sync(0xffffffffu, a.c, o);
                 a.c += oc;
@@ -529,9 +546,11 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
             }
             acc[r] = a;
         }
+        if (valid) {
 #pragma unroll
-        for (int r = 0; r < K; r++)
-            if (lane == (r & 31)) P[row * K + r] = make_float2(acc[r].s, acc[r].c);
+            for (int r = 0; r < K; r++)
+                if (gl == (r % SW)) P[row * K + r] = make_float2(acc[r].s, acc[r].c);
+        }
     }
 }
 
@@ -1006,6 +1025,13 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
     FCG_TRY(build_plan(p, a, parent, s));
     FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
+    // lanes per node in the link product: about four links per lane per pass
+    {
+        double avg = (double)a.n_links / (double)Nn;
+        p->spmv_lanes = avg < 48.0 ? 8 : (avg < 96.0 ? 16 : 32);
+        const char *env = getenv("FCG_SPMV_LANES");
+        if (env && (atoi(env) == 8 || atoi(env) == 16 || atoi(env) == 32)) p->spmv_lanes = atoi(env);
+    }
     if (cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s) != cudaSuccess) {
         set_error("cannot clear the arrival counters");
         problem_destroy(p);
@@ -1030,7 +1056,7 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
     dfree(p->left); dfree(p->right); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
     dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
-    dfree(p->near_link); dfree(p->near_row);
+    dfree(p->near_link); dfree(p->near_row); dfree(p->tri);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
     dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
@@ -1136,6 +1162,11 @@ static int build_near_list(DeviceProblem *p) {
         k_near_list<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, off, p->near_link, p->near_row);
         p->timings.launches++;
     }
+    if (n > 0) {
+        if ((r = dalloc(&p->tri, p->Nn, p->bytes))) { dfree(off); return r; }
+        k_make_tri<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri);
+        p->timings.launches++;
+    }
     cudaError_t e = cudaStreamSynchronize(s);
     dfree(off);
     if (e != cudaSuccess) { set_error(std::string("near-field list failed: ") + cudaGetErrorString(e)); return FCG_DEVICE_ERROR; }
@@ -1162,7 +1193,7 @@ int problem_fill(DeviceProblem *p) {
         p->timings.launches++;
         if (p->n_near > 0) {
             k_fill_near<<<grid_for(p->n_near, 128, sms), 128, 0, s>>>(p->n_near, p->near_link, p->near_row, p->link_src, p->geo,
-                                                                     p->coef64, p->coef32, p->status);
+                                                                     p->tri, p->coef64, p->coef32, p->status);
             FCG_CK(cudaGetLastError());
             p->timings.launches++;
         }
@@ -1248,7 +1279,8 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     if (mixed) k_up<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
     else k_up<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
     FCG_CK(cudaGetLastError());
-    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
+    int64_t rows_per_cta = 8 * (32 / p->spmv_lanes);
+    int grid = (int)std::min<int64_t>((p->Nn + rows_per_cta - 1) / rows_per_cta, (int64_t)p->ctx->sm_count * 32);
     int64_t launches = 2;
     if (p->L > 0) {
         // coefficient + source word per link, row offsets, one charge read and
@@ -1258,25 +1290,28 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
         p->timings.link_launches++;
         launches++;
         prof_begin(p);
-        if (!mixed) {
-            switch (kp) {
-            case 1: k_spmv64<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 2: k_spmv64<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 4: k_spmv64<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 8: k_spmv64<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 16: k_spmv64<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            default: k_spmv64<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            }
-        } else {
-            switch (kp) {
-            case 1: k_spmv32<1><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            case 2: k_spmv32<2><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            case 4: k_spmv32<4><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            case 8: k_spmv32<8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            case 16: k_spmv32<16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            default: k_spmv32<32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            }
+        int sw = p->spmv_lanes;
+#define FCG_SPMV(KK)                                                                                                  \
+    do {                                                                                                              \
+        if (mixed) {                                                                                                  \
+            if (sw == 8) k_spmv32<KK, 8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); \
+            else if (sw == 16) k_spmv32<KK, 16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); \
+            else k_spmv32<KK, 32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2);     \
+        } else {                                                                                                      \
+            if (sw == 8) k_spmv64<KK, 8><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); \
+            else if (sw == 16) k_spmv64<KK, 16><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); \
+            else k_spmv64<KK, 32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd);     \
+        }                                                                                                             \
+    } while (0)
+        switch (kp) {
+        case 1: FCG_SPMV(1); break;
+        case 2: FCG_SPMV(2); break;
+        case 4: FCG_SPMV(4); break;
+        case 8: FCG_SPMV(8); break;
+        case 16: FCG_SPMV(16); break;
+        default: FCG_SPMV(32); break;
         }
+#undef FCG_SPMV
         prof_end(p);
         FCG_CK(cudaGetLastError());
     } else {
