@@ -48,6 +48,10 @@ WORKLOADS = {
                      1e30, 1e-33, 1e-4, FOUR_PI_E0),
     "sphere_20480": (lambda p: __import__("fastercap_gb300.geometry", fromlist=["x"]).write_sphere(p, 5),
                      1e30, 1e-33, 1e-4, FOUR_PI_E0),
+    # 8x8 bus crossing (16 conductors) in an eps_r=3.9 slab under a planar
+    # interface to eps_r=1: 130,942 panels, 81.4M links, 16 right-hand sides
+    "crossing8x8_slab": (lambda p: __import__("fastercap_gb300.geometry", fromlist=["x"]).crossing_8x8_slab().write(p),
+                         5e-6, 1.0, 1e-4, None),
 }
 
 
@@ -289,6 +293,7 @@ def run_gb300(args, rank, world, local_rank):
         "mixed_vs_fp64": {"speedup": (sum(times64) / sum(times)), "max_rel_c_err": rel_mixed_vs_64},
         "accuracy": {"c_mixed": float(cap_m[0, 0]), "c_fp64": float(cap_64[0, 0]),
                      "rel_err_vs_analytic": (float(cap_m[0, 0]) - analytic) / analytic if analytic else None,
+                     "min_abs_c_over_diag": float(np.min(np.abs(cap_64) / np.abs(np.diag(cap_64))[:, None])),
                      "iterations": [int(x) for x in it_m]},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "p50_ms": float(np.percentile(e2e_times, 50))},

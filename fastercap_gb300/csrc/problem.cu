@@ -171,6 +171,19 @@ __global__ void k_classify(int64_t Nn, const int64_t *__restrict__ ptr, uint32_t
     }
 }
 
+// Move every model row to its device position (height-major label) and
+// relabel its sources; rows keep their links in order.
+__global__ void k_relabel_links(int64_t Nn, const int64_t *__restrict__ ptr_model, const uint32_t *__restrict__ src_model,
+                                const int32_t *__restrict__ lab, const int64_t *__restrict__ ptr_dev, uint32_t *__restrict__ src_dev) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < Nn; i += nwarps) {
+        int64_t b0 = ptr_model[i], e0 = ptr_model[i + 1], o = ptr_dev[lab[i]] - b0;
+        for (int64_t l = b0 + lane; l < e0; l += 32) src_dev[o + l] = (uint32_t)lab[src_model[l]];
+    }
+}
+
 // count the near-field (band 0) links of every row
 __global__ void k_near_count(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                              int32_t *__restrict__ cnt) {
@@ -1042,11 +1055,9 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     p->h_ptr_model.assign(a.link_ptr, a.link_ptr + Nn + 1);
     p->h_ptr_dev.assign(Nn + 1, 0);
     p->h_inv = inv;
-    std::vector<uint32_t> dsrc(L);
     for (int64_t q = 0; q < Nn; q++) {
-        int64_t i = inv[q], b0 = a.link_ptr[i], cnt = a.link_ptr[i + 1] - b0, o = p->h_ptr_dev[q];
-        for (int64_t l = 0; l < cnt; l++) dsrc[o + l] = (uint32_t)lab[a.link_src[b0 + l]];
-        p->h_ptr_dev[q + 1] = o + cnt;
+        int64_t i = inv[q];
+        p->h_ptr_dev[q + 1] = p->h_ptr_dev[q] + (a.link_ptr[i + 1] - a.link_ptr[i]);
     }
     std::vector<double> eb(Np, 0.0), ea(Np, 0.0), weight(Np, 0.0);
     for (int32_t c = 0; c < a.n_conductors; c++) {
@@ -1057,7 +1068,29 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     }
     FCG_TRY(upload(&p->geo, geo.data(), Nn, p->bytes, s));
     FCG_TRY(upload(&p->link_ptr, p->h_ptr_dev.data(), Nn + 1, p->bytes, s));
-    FCG_TRY(upload(&p->link_src, dsrc.data(), L, p->bytes, s));
+    {
+        // relabel the links on the device from the caller's arrays
+        int64_t tb = 0;
+        uint32_t *src_model = NULL;
+        int64_t *ptr_model = NULL;
+        int32_t *dlab = NULL;
+        int rr = upload(&src_model, (const uint32_t *)a.link_src, L, tb, s);
+        if (rr == FCG_NORMAL_END) rr = upload(&ptr_model, a.link_ptr, Nn + 1, tb, s);
+        if (rr == FCG_NORMAL_END) rr = upload(&dlab, lab.data(), Nn, tb, s);
+        if (rr == FCG_NORMAL_END) rr = dalloc(&p->link_src, L, p->bytes);
+        if (rr == FCG_NORMAL_END && L > 0) {
+            int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)ctx.sm_count * 32);
+            k_relabel_links<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, dlab, p->link_ptr, p->link_src);
+            if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+                set_error("link relabelling failed");
+                rr = FCG_DEVICE_ERROR;
+            }
+        }
+        dfree(src_model);
+        dfree(ptr_model);
+        dfree(dlab);
+        if (rr != FCG_NORMAL_END) { problem_destroy(p); return rr; }
+    }
     FCG_TRY(upload(&p->leaf_node, dleaf.data(), Np, p->bytes, s));
     FCG_TRY(upload(&p->parent, dparent.data(), Nn, p->bytes, s));
     FCG_TRY(upload(&p->leaf_eb, eb.data(), Np, p->bytes, s));
