@@ -54,6 +54,14 @@ WORKLOADS = {
                          5e-6, 1.0, 1e-4, None),
 }
 
+# many independent geometries in one problem: name -> (seeds, mesh_eps,
+# eps_ratio, gmres tol). crossings32: 32 random k x k crossings in vacuum
+# (k in 2..10, length 10-60 um, pitch 2-4 um, gap 1-3 um; seeds 0..31):
+# 5,312 to 39,040 panels each, 748,928 panels and 257M links in all.
+MULTI = {
+    "crossings32": (list(range(32)), 1e-3, 1.0, 1e-4),
+}
+
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
@@ -118,6 +126,22 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def build_multi(workload: str):
+    """(concatenated model, geometry_of_conductor, [per-geometry models], build s, tol, link eps)"""
+    import fastercap_gb300 as fc
+    from fastercap_gb300 import geometry as geo
+    seeds, meps, dratio, tol = MULTI[workload]
+    models = []
+    t0 = time.perf_counter()
+    with tempfile.TemporaryDirectory() as tmp:
+        for sd in seeds:
+            path = os.path.join(tmp, "r%d.txt" % sd)
+            geo.random_crossing(sd).write(path)
+            models.append(fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio))
+    model, geom = fc.Model.concat(models)
+    return model, geom, models, time.perf_counter() - t0, tol, meps * dratio
 
 
 def build_model(workload: str):
@@ -187,6 +211,214 @@ def run_reference(args, rank, world):
         "capacitance": float(cap[0, 0]), "iterations": [int(x) for x in it],
     }
     print(json.dumps(line), flush=True)
+
+
+def run_reference_multi(args, rank, world):
+    """CPU arm for a multi-geometry workload: the oracle port on every host
+    core; each step solves one geometry (cycling through them in order)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    model, geom, models, build_s, tol, eps = build_multi(args.workload)
+    cores = os.cpu_count() or 1
+    times, panels = [], []
+    for i in range(args.warmup + args.steps):
+        m = models[i % len(models)]
+        o = Oracle(m.arrays, threads=cores)
+        t0 = time.perf_counter()
+        o.fill()
+        o.solve(tol, 1)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            panels.append(m.n_panels)
+    total = sum(times)
+    value = len(times) / total
+    sample = ("one geometry per step, cycling through the %d in seed order (steps %d..%d: %d panels in all)"
+              % (len(models), args.warmup, args.warmup + args.steps - 1, sum(panels)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "p50_ms": 1000 * float(np.percentile(times, 50)), "p99_ms": 1000 * float(np.percentile(times, 99)),
+        "config": {"workload": args.workload, "geometries": len(models), "panels": model.n_panels,
+                   "links": model.n_links, "link_eps": eps, "gmres_tol": tol, "precond": "jacobi",
+                   "solve": "one geometry's full capacitance matrix (fill + GMRES per conductor + C)"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_steps_multi(prob, stream, n, tol, flush_buf, torch, geom=None, rhs_width=0):
+    s = torch.cuda.ExternalStream(stream)
+    times, caps, its = [], None, None
+    for _ in range(n):
+        with torch.cuda.stream(s):
+            flush_buf.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        prob.fill()
+        caps, its = prob.solve(tol=tol, rhs_width=rhs_width)
+        e1.record(s)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return times, caps, its
+
+
+def run_gb300_multi(args, rank, world, local_rank):
+    """All geometries in one problem: every kernel launch covers all of them,
+    each geometry keeps its own GMRES solves."""
+    import torch
+    import fastercap_gb300 as fc
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    model, geom, models, build_s, tol, eps = build_multi(args.workload)
+    G = len(models)
+    ctx = fc.Context(local_rank)
+    stream = ctx.stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    prob = ctx.problem(model, fc.PREC_MIXED)
+    prob.set_geometries(geom)
+    time_steps_multi(prob, stream, args.warmup, tol, flush, torch)
+    prob.reset_stats()
+    prob.set_profiling(True)
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        times, caps_m, its_m = time_steps_multi(prob, stream, args.steps, tol, flush, torch)
+    barrier()
+    st = prob.stats()
+    prob.set_profiling(False)
+    total_ms = sum(times)
+    # FP64, same batching
+    p64 = ctx.problem(model, fc.PREC_FP64)
+    p64.set_geometries(geom)
+    time_steps_multi(p64, stream, 1, tol, flush, torch)
+    times64, caps_64, its_64 = time_steps_multi(p64, stream, max(1, min(args.steps, 3)), tol, flush, torch)
+    p64.close()
+    # plain FP64 single right-hand side: one problem per geometry, one
+    # conductor at a time
+    singles = []
+    for m in models:
+        q = ctx.problem(m, fc.PREC_FP64)
+        singles.append(q)
+    for q in singles:
+        q.fill()
+        q.solve(tol=tol, rhs_width=1)
+    torch.cuda.synchronize()
+    s = torch.cuda.ExternalStream(stream)
+    with torch.cuda.stream(s):
+        flush.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for q in singles:
+        q.fill()
+        q.solve(tol=tol, rhs_width=1)
+    e1.record(s)
+    e1.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    for q in singles:
+        q.close()
+    # end to end through the C ABI: pinned host model -> upload -> fill -> solve -> C back
+    pm = pinned_model(model)
+    h2d = model_bytes(model)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(s):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        pe = ctx.problem(pm, fc.PREC_MIXED)
+        pe.set_geometries(geom)
+        pe.fill()
+        caps_e, its_e = pe.solve(tol=tol)
+        e1.record(s)
+        e1.synchronize()
+        pe.close()
+        if i >= args.warmup:
+            e2e_times.append(e0.elapsed_time(e1))
+    d2h = sum(c.nbytes for c in caps_e) + 4 * sum(len(i) for i in its_e)
+    tmax, e2e_max = total_ms, sum(e2e_times)
+    if world > 1:
+        t = torch.tensor([total_ms, e2e_max], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tmax, e2e_max = float(t[0]), float(t[1])
+    value = world * args.steps * G / (tmax / 1000.0)
+    e2e_value = world * args.steps * G / (e2e_max / 1000.0)
+    peak, peak_kind = peaks()
+    link_avg_ms = st["link_ms"] / max(1, st["link_launches"])
+    link_bytes = st["link_bytes"] / max(1, st["link_launches"])
+    achieved = link_bytes / (link_avg_ms / 1000.0) / 1e9 if link_avg_ms > 0 else None
+    err_m64 = max(float(np.max(np.abs(a - b) / np.abs(b))) for a, b in zip(caps_m, caps_64))
+    it_all = np.concatenate([np.asarray(i) for i in its_m])
+    result = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
+        "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99)),
+        "config": {"workload": args.workload, "geometries": G, "panels": model.n_panels, "links": model.n_links,
+                   "panels_min_max": [min(m.n_panels for m in models), max(m.n_panels for m in models)],
+                   "link_eps": eps, "gmres_tol": tol, "precond": "jacobi",
+                   "rhs": int(sum(len(m.conductor_names) for m in models)),
+                   "solve": "one geometry's full capacitance matrix; a step solves all geometries in one problem",
+                   "l2": "flushed between steps (256 MiB write); links exceed L2", "host_build_s": round(build_s, 3),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": world * len(times64) * G / (sum(times64) / 1000.0), "unit": "solves/s",
+                 "p50_ms": float(np.percentile(times64, 50))},
+        "fp64_single_rhs": {"value": G / (single_ms / 1000.0), "unit": "solves/s", "ms_all_geometries": single_ms,
+                            "note": "one FP64 problem per geometry, one right-hand side at a time"},
+        "mixed_vs_fp64": {"speedup": (sum(times64) / len(times64)) / (total_ms / args.steps),
+                          "speedup_vs_single_rhs": single_ms / (total_ms / args.steps), "max_rel_c_err": err_m64},
+        "accuracy": {"iterations_min_max": [int(it_all.min()), int(it_all.max())]},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "p50_ms": float(np.percentile(e2e_times, 50))},
+        "gpu_launches": int(st["kernel_launches"]),
+        "phases": {"fill_ms_last": st["fill_ms"], "solve_ms_last": st["solve_ms"]},
+        "roofline": {"kernel": "link product (k_spmv32_multi)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+                     "traffic": None, "launches": int(st["link_launches"]),
+                     "bytes_per_launch": link_bytes, "avg_launch_ms": link_avg_ms},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        n_done, errs = 0, []
+        for m, cm in zip(models, caps_m):
+            o = Oracle(m.arrays, threads=cores)
+            o.fill()
+            ocap, _, _, _ = o.solve(tol, 1)
+            errs.append(float(np.max(np.abs(cm - ocap) / np.abs(ocap))))
+            n_done += 1
+            if time.perf_counter() - t0 > 20.0:
+                break
+        dt = time.perf_counter() - t0
+        result["cpu_baseline"] = {"value": n_done / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+                                  "sample": "the first %d geometries in seed order, one full solve each" % n_done}
+        result["accuracy"]["max_rel_c_err_vs_cpu_fp64"] = max(errs)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    prob.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def time_steps(prob, stream, n, tol, flush_buf, torch):
@@ -332,17 +564,18 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sphere_327680", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="sphere_327680", choices=sorted(WORKLOADS) + sorted(MULTI))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3
     rank, world, local_rank = dist_env()
+    multi = args.workload in MULTI
     if args.impl == "reference":
-        run_reference(args, rank, world)
+        (run_reference_multi if multi else run_reference)(args, rank, world)
     else:
-        run_gb300(args, rank, world, local_rank)
+        (run_gb300_multi if multi else run_gb300)(args, rank, world, local_rank)
 
 
 if __name__ == "__main__":

@@ -82,7 +82,7 @@ class ProblemStats(C.Structure):
 
 
 class SolveOptions(C.Structure):
-    _fields_ = [("tol", C.c_double), ("precond", C.c_int), ("max_iter", C.c_int)]
+    _fields_ = [("tol", C.c_double), ("precond", C.c_int), ("max_iter", C.c_int), ("rhs_width", C.c_int)]
 
 
 # (field, dtype, length key, columns)
@@ -140,6 +140,8 @@ def lib() -> C.CDLL:
     L.fcg_problem_solve.argtypes = [vp, C.POINTER(SolveOptions), vp, vp]
     L.fcg_problem_get_charges.argtypes = [vp, vp]
     L.fcg_run_command_line.argtypes = [C.c_char_p]
+    L.fcg_model_concat.argtypes = [C.POINTER(vp), i32, C.POINTER(vp), vp]
+    L.fcg_problem_set_geometries.argtypes = [vp, i32, vp]
     _lib = L
     return L
 
@@ -181,6 +183,39 @@ class Model:
         code = L.fcg_model_build(os.fsencode(path), C.byref(opt), C.byref(h), err, 512)
         if code != NORMAL_END:
             raise FCError(code, "model build failed: " + err.value.decode(errors="replace"))
+        return cls._from_handle(h)
+
+    @classmethod
+    def from_arrays(cls, arrays: dict, names=None) -> "Model":
+        """Wrap externally produced arrays (e.g. a golden fixture) without a native handle."""
+        own = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        info = {"n_nodes": len(own["node_type"]), "n_panels": len(own["leaf_diel"]), "n_links": len(own["link_src"]),
+                "n_conductors": len(own["cond_is_diel"])}
+        return cls(None, own, names or ["c%d" % i for i in range(info["n_conductors"])], info)
+
+    @classmethod
+    def concat(cls, models) -> tuple:
+        """Concatenate independent geometries into one model (a forest with no
+        link between geometries). Returns (model, geometry_of_conductor).
+        Models built from files go through fcg_model_concat; models made from
+        arrays are concatenated here with the same layout."""
+        models = list(models)
+        if not models:
+            raise ValueError("no models to concatenate")
+        ncond = sum(len(m.arrays["cond_is_diel"]) for m in models)
+        if all(m._h is not None for m in models):
+            L = lib()
+            hs = (C.c_void_p * len(models))(*[m._h for m in models])
+            h = C.c_void_p()
+            geom = np.empty(ncond, np.int32)
+            _check(L.fcg_model_concat(hs, len(models), C.byref(h), _ptr(geom)), "model concat")
+            tmp = cls._from_handle(h)
+            return tmp, geom
+        return cls._concat_arrays(models)
+
+    @classmethod
+    def _from_handle(cls, h) -> "Model":
+        L = lib()
         info_s = ModelInfo()
         _check(L.fcg_model_info_get(h, C.byref(info_s)), "model info")
         info = {f: getattr(info_s, f) for f, _ in ModelInfo._fields_}
@@ -202,16 +237,43 @@ class Model:
         buf = (C.c_char * (max(nsurf, 1) * 8)).from_address(a.cond_surf_outperm)
         arrays["cond_surf_outperm"] = np.frombuffer(buf, dtype=np.float64, count=max(nsurf, 1))
         names = [L.fcg_model_conductor_name(h, i).decode() for i in range(a.n_conductors)]
-        m = cls(h, arrays, names, info)
-        return m
+        return cls(h, arrays, names, info)
 
     @classmethod
-    def from_arrays(cls, arrays: dict, names=None) -> "Model":
-        """Wrap externally produced arrays (e.g. a golden fixture) without a native handle."""
-        own = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
-        info = {"n_nodes": len(own["node_type"]), "n_panels": len(own["leaf_diel"]), "n_links": len(own["link_src"]),
-                "n_conductors": len(own["cond_is_diel"])}
-        return cls(None, own, names or ["c%d" % i for i in range(info["n_conductors"])], info)
+    def _concat_arrays(cls, models) -> tuple:
+        out = {}
+        node_off = leaf_off = link_off = surf_off = 0
+        parts = {k: [] for k, _, _, _ in ARRAY_FIELDS}
+        parts["cond_surf_outperm"] = []
+        geom, names = [], []
+        for g, m in enumerate(models):
+            a = m.arrays
+            nn, npan, nl = m.n_nodes, m.n_panels, m.n_links
+            nc = len(a["cond_is_diel"])
+            for k in ("node_type", "node_leaf_count", "node_vertices", "node_centroid", "node_normal", "node_area",
+                      "node_maxside", "leaf_diel", "cond_is_diel", "cond_leaf_count", "cond_outperm", "cond_inperm"):
+                parts[k].append(np.asarray(a[k]))
+            for k in ("node_left", "node_right"):
+                v = np.asarray(a[k]).astype(np.int32)
+                parts[k].append(np.where(v >= 0, v + node_off, -1).astype(np.int32))
+            parts["node_leaf_first"].append(np.asarray(a["node_leaf_first"]) + leaf_off)
+            lp = np.asarray(a["link_ptr"])
+            parts["link_ptr"].append((lp[:-1] if g < len(models) - 1 else lp) + link_off)
+            parts["link_src"].append((np.asarray(a["link_src"]) + node_off).astype(np.int32))
+            parts["cond_leaf_first"].append(np.asarray(a["cond_leaf_first"]) + leaf_off)
+            sp = np.asarray(a["cond_surf_ptr"])
+            parts["cond_surf_ptr"].append((sp[:-1] if g < len(models) - 1 else sp) + surf_off)
+            parts["cond_surf_outperm"].append(np.asarray(a["cond_surf_outperm"])[: int(sp[-1])])
+            geom += [g] * nc
+            names += list(m.names)
+            node_off += nn
+            leaf_off += npan
+            link_off += nl
+            surf_off += int(sp[-1])
+        for k, dt, _, _ in ARRAY_FIELDS:
+            out[k] = np.ascontiguousarray(np.concatenate(parts[k]).astype(dt, copy=False))
+        out["cond_surf_outperm"] = np.concatenate(parts["cond_surf_outperm"]).astype(np.float64)
+        return cls.from_arrays(out, names), np.asarray(geom, np.int32)
 
     @property
     def n_panels(self) -> int:
@@ -268,6 +330,16 @@ class Problem:
         st = C.c_void_p(stream) if stream is not None else C.c_void_p(lib().fcg_context_stream(ctx._h))
         _check(lib().fcg_problem_create_on_stream(ctx._h, C.byref(arr), precision, st, C.byref(h)), "problem create")
         self._h = h
+        self.geometries = None  # per-geometry column counts once set_geometries ran
+
+    def set_geometries(self, geometry_of_conductor):
+        """Declare independent geometries (conductor -> geometry index, as
+        Model.concat returns it): every geometry gets its own GMRES solves."""
+        geom = np.ascontiguousarray(geometry_of_conductor, dtype=np.int32)
+        ng = int(geom.max()) + 1 if len(geom) else 0
+        _check(lib().fcg_problem_set_geometries(self._h, ng, _ptr(geom)), "set geometries")
+        diel = np.asarray(self.model.arrays["cond_is_diel"]) != 0
+        self.geometries = [int(np.sum((geom == g) & ~diel)) for g in range(ng)]
 
     def set_profiling(self, on: bool):
         _check(lib().fcg_problem_set_profiling(self._h, 1 if on else 0), "profiling")
@@ -309,17 +381,32 @@ class Problem:
         returns the FC_* status instead of raising."""
         return int(lib().fcg_problem_matvec_device_noalloc(self._h, C.c_void_p(q_ptr), C.c_void_p(v_ptr), k))
 
-    def solve(self, tol: float = 0.01, precond: int = PRECOND_JACOBI, max_iter: int = 0, allow_not_converged=False):
-        cap = np.empty((self.n_cond, self.n_cond), np.float64)
-        it = np.empty(self.n_cond, np.int32)
-        opt = SolveOptions(tol, precond, max_iter)
+    def solve(self, tol: float = 0.01, precond: int = PRECOND_JACOBI, max_iter: int = 0, allow_not_converged=False,
+              rhs_width: int = 0):
+        """(C, iterations); with geometries set, lists of per-geometry C and iterations."""
+        sizes = self.geometries or [self.n_cond]
+        cap = np.empty(sum(n * n for n in sizes), np.float64)
+        it = np.empty(sum(sizes), np.int32)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width)
+        self._last_width = min(rhs_width, 32) if rhs_width > 0 else 32
         code = lib().fcg_problem_solve(self._h, C.byref(opt), _ptr(cap), _ptr(it))
         if not (code == NORMAL_END or (allow_not_converged and code == NOT_CONVERGED)):
             _check(code, "solve")
-        return cap, it
+        caps, its, oc, oi = [], [], 0, 0
+        for n in sizes:
+            caps.append(cap[oc:oc + n * n].reshape(n, n))
+            its.append(it[oi:oi + n])
+            oc += n * n
+            oi += n
+        if self.geometries is None:
+            return caps[0], its[0]
+        return caps, its
 
     def charges(self) -> np.ndarray:
-        k = min(self.n_cond, 32)
+        """Charges of the last batch of right-hand-side columns, [k][n_panels]."""
+        ks = max(self.geometries or [self.n_cond])
+        w = getattr(self, "_last_width", 32)
+        k = ks - w * ((ks - 1) // w)
         x = np.empty((k, self.n_panels), np.float64)
         _check(lib().fcg_problem_get_charges(self._h, _ptr(x)), "get charges")
         return x

@@ -44,6 +44,7 @@ int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int 
 int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int k);
 int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations);
 int problem_get_charges(DeviceProblem *p, double *charges);
+int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond);
 int problem_n_cond(const DeviceProblem *p);
 
 // timings of the last fill / solve in milliseconds (CUDA events on the problem's stream)

@@ -133,16 +133,29 @@ struct DeviceProblem {
     int *arrive = NULL;  // per-node arrival counters of the up-sweep (zero between products)
     int spmv_lanes = 32;  // lanes per destination node in the link product (8, 16 or 32)
 
+    // solve geometries (independent models concatenated into one problem)
+    int n_geom = 0;
+    std::vector<int> geom_cols_ptr;  // cond_cols of geometry g: [geom_cols_ptr[g], geom_cols_ptr[g+1])
+    std::vector<int64_t> geom_leaf_first, geom_leaf_count;
+    std::vector<int64_t> h_node_leaf_first;  // per device node label
+    int nch = 0;  // Krylov chunks (never crossing a geometry)
+    int32_t *leaf_geom = NULL, *ch_len = NULL, *ch_geom = NULL, *g_ch_first = NULL, *g_ch_count = NULL;
+    int64_t *ch_start = NULL;
+
     // Krylov workspace
-    int gk = 0, gM = 0;  // right-hand sides, max iterations allocated
+    int gk = 0, gS = 0, gM = 0;  // right-hand-side columns, solves, max iterations allocated
     std::vector<double *> V;  // basis vectors, each [gk][Np]
     double **Vptr = NULL;
     int Vptr_cap = 0;
-    double *H = NULL, *cs = NULL, *sn = NULL, *g = NULL, *normb = NULL, *hnorm = NULL, *nrm2 = NULL, *z = NULL;
+    std::vector<double *> Hc;  // Hessenberg column i: [gS][i + 2]
+    std::vector<double *> Hblk;
+    double **Hptr = NULL;
+    double *cs = NULL, *sn = NULL, *g = NULL, *normb = NULL, *hnorm = NULL, *nrm2 = NULL, *z = NULL;
     double *partial = NULL;
-    int partial_cap = 0;
-    int *active = NULL, *iters = NULL, *n_active = NULL;
-    int *h_n_active = NULL;
+    size_t partial_cap = 0;
+    int *active = NULL, *iters = NULL, *capped = NULL, *scap = NULL, *n_active = NULL;
+    int *h_pin = NULL;  // pinned host ints for the per-iteration readback
+    size_t h_pin_cap = 0;
     double *b = NULL, *x0 = NULL, *w = NULL, *vv = NULL, *x = NULL;
     int x_k = 0;
 };
@@ -182,6 +195,21 @@ __global__ void k_relabel_links(int64_t Nn, const int64_t *__restrict__ ptr_mode
         int64_t b0 = ptr_model[i], e0 = ptr_model[i + 1], o = ptr_dev[lab[i]] - b0;
         for (int64_t l = b0 + lane; l < e0; l += 32) src_dev[o + l] = (uint32_t)lab[src_model[l]];
     }
+}
+
+// counts tree edges and links whose two nodes lie in different geometries
+__global__ void k_check_geometries(int64_t Nn, const int64_t *__restrict__ link_ptr, const uint32_t *__restrict__ link_src,
+                                   const int32_t *__restrict__ parent, const int32_t *__restrict__ node_geom, unsigned *bad) {
+    unsigned cnt = 0;
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = warp; v < Nn; v += nw) {
+        int gv = node_geom[v];
+        if (lane == 0 && parent[v] >= 0 && node_geom[parent[v]] != gv) cnt++;
+        for (int64_t l = link_ptr[v] + lane; l < link_ptr[v + 1]; l += 32)
+            if (node_geom[link_src[l] & kSrcMask] != gv) cnt++;
+    }
+    if (cnt) atomicAdd(bad, cnt);
 }
 
 // count the near-field (band 0) links of every row
@@ -570,15 +598,114 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
     }
 }
 
-// ---- Krylov kernels: vectors are [k][ld] with ld = n_panels
+// Link product for K >= 4 right-hand sides, mixed: K/4 lanes share a link,
+// each lane owns four right-hand sides (one 16-byte charge load per link), a
+// warp advances 128/K links per step; the link slots are reduced at the end.
+template <int K>
+__global__ void k_spmv32_multi(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
+                               const float *__restrict__ coef, const float *__restrict__ Q, float2 *__restrict__ P) {
+    const int LPL = K / 4, LPW = 32 / LPL;
+    int lane = threadIdx.x & 31, li = lane / LPL, ri = lane % LPL;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float4 *Q4 = reinterpret_cast<const float4 *>(Q);
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        KSum acc[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) { acc[r].s = 0.f; acc[r].c = 0.f; }
+        int s = (int)ptr[row], e = (int)ptr[row + 1];
+        int l = s + li;
+        for (; l + LPW < e; l += 2 * LPW) {
+            float c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
+            uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
+            float4 q0 = Q4[(int64_t)j0 * LPL + ri], q1 = Q4[(int64_t)j1 * LPL + ri];
+            kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
+            kmul_add(acc[0], c1, q1.x); kmul_add(acc[1], c1, q1.y); kmul_add(acc[2], c1, q1.z); kmul_add(acc[3], c1, q1.w);
+        }
+        if (l < e) {
+            float c0 = __ldcs(&coef[l]);
+            uint32_t j0 = __ldcs(&src[l]) & kSrcMask;
+            float4 q0 = Q4[(int64_t)j0 * LPL + ri];
+            kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            KSum a = acc[r];
+#pragma unroll
+            for (int o = 16; o >= LPL; o >>= 1) {
+                float os = __shfl_xor_sync(0xffffffffu, a.s, o);
+                float oc = __shfl_xor_sync(0xffffffffu, a.c, o);
+                a.c += oc;
+                kadd(a, os);
+            }
+            acc[r] = a;
+        }
+        if (li == 0) {
+            float4 *out = reinterpret_cast<float4 *>(P + row * K + 4 * ri);
+            out[0] = make_float4(acc[0].s, acc[0].c, acc[1].s, acc[1].c);
+            out[1] = make_float4(acc[2].s, acc[2].c, acc[3].s, acc[3].c);
+        }
+    }
+}
 
-__global__ void k_set_rhs(int64_t Np, int k, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
-                          double *__restrict__ b) {
-    int64_t n = (int64_t)k * Np;
+// FP64 counterpart: K/2 lanes share a link, each lane owns two right-hand sides.
+template <int K>
+__global__ void k_spmv64_multi(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
+                               const double *__restrict__ coef, const double *__restrict__ Q, double *__restrict__ P) {
+    const int LPL = K / 2, LPW = 32 / LPL;
+    int lane = threadIdx.x & 31, li = lane / LPL, ri = lane % LPL;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const double2 *Q2 = reinterpret_cast<const double2 *>(Q);
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        double a0 = 0.0, a1 = 0.0;
+        int s = (int)ptr[row], e = (int)ptr[row + 1];
+        int l = s + li;
+        for (; l + LPW < e; l += 2 * LPW) {
+            double c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
+            uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
+            double2 q0 = Q2[(int64_t)j0 * LPL + ri], q1 = Q2[(int64_t)j1 * LPL + ri];
+            a0 += c0 * q0.x; a1 += c0 * q0.y;
+            a0 += c1 * q1.x; a1 += c1 * q1.y;
+        }
+        if (l < e) {
+            double c0 = __ldcs(&coef[l]);
+            double2 q0 = Q2[(int64_t)(__ldcs(&src[l]) & kSrcMask) * LPL + ri];
+            a0 += c0 * q0.x; a1 += c0 * q0.y;
+        }
+#pragma unroll
+        for (int o = 16; o >= LPL; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        }
+        if (li == 0) reinterpret_cast<double2 *>(P + row * K)[ri] = make_double2(a0, a1);
+    }
+}
+
+// ---- Krylov kernels (CSolveCap::gmresPrecondSFastAll, Solver/SolveCapacitance.cpp:2288-2574)
+//
+// Vectors are [ks][Np]: column r of every vector carries one independent
+// solve per geometry g, solve s = g * ks + r, on g's leaf range. Reductions
+// run over chunks that never cross a geometry, so every solve has its own dot
+// products, norms, Givens rotations, iteration count and convergence test.
+// Hessenberg column i of all solves is one array Hc[i] of S * (i + 2) values.
+
+struct SegChunks {
+    const int64_t *start;  // first leaf of each chunk
+    const int32_t *len;    // leaves in each chunk (<= kDotChunk)
+    const int32_t *geom;   // geometry of each chunk
+    int n;
+};
+
+// b[r][j] = 1 on the leaves of solve (geometry of j, r)'s conductor
+__global__ void k_set_rhs(int64_t Np, int ks, const int32_t *__restrict__ leaf_geom, const int64_t *__restrict__ sf,
+                          const int64_t *__restrict__ sc, double *__restrict__ b) {
+    int64_t n = (int64_t)ks * Np;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int r = (int)(t / Np);
         int64_t j = t - (int64_t)r * Np;
-        b[t] = (j >= first[r] && j < first[r] + count[r]) ? 1.0 : 0.0;
+        int s = leaf_geom[j] * ks + r;
+        b[t] = (j >= sf[s] && j < sf[s] + sc[s]) ? 1.0 : 0.0;
     }
 }
 
@@ -603,209 +730,265 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return v;
 }
 
-// partial[(r*nvec + j)*nch + chunk] = <Vj[r] chunk, w[r] chunk>
-__global__ void k_dots(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w,
+// partial[(r*nvec + j)*nch + c] = <Vj[r], w[r]> over chunk c; the chunk of w
+// stays in registers, basis vectors are taken eight at a time with one block
+// reduction per group of eight.
+__global__ void k_dots(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w, SegChunks ch, int ks,
                        const int *__restrict__ active, double *__restrict__ partial) {
-    __shared__ double sh[32];
-    int r = blockIdx.y, ch = blockIdx.x, nch = gridDim.x;
-    if (active && !active[r]) return;
-    int64_t base = (int64_t)ch * kDotChunk;
+    __shared__ double sh[8][8];
+    const int T = 8;
+    int r = blockIdx.y, c = blockIdx.x;
+    if (!active[ch.geom[c] * ks + r]) return;
+    int64_t base = ch.start[c];
+    int len = ch.len[c];
     double wv[kDotChunk / 256];
 #pragma unroll
     for (int u = 0; u < kDotChunk / 256; u++) {
-        int64_t j = base + threadIdx.x + u * 256;
-        wv[u] = (j < Np) ? w[(int64_t)r * Np + j] : 0.0;
+        int o = threadIdx.x + u * 256;
+        wv[u] = (o < len) ? w[(int64_t)r * Np + base + o] : 0.0;
     }
-    for (int jv = 0; jv < nvec; jv++) {
-        const double *v = Vp[jv] + (int64_t)r * Np;
-        double s = 0.0;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j0 = 0; j0 < nvec; j0 += T) {
+        double acc[T];
 #pragma unroll
-        for (int u = 0; u < kDotChunk / 256; u++) {
-            int64_t j = base + threadIdx.x + u * 256;
-            if (j < Np) s += v[j] * wv[u];
+        for (int t = 0; t < T; t++) {
+            acc[t] = 0.0;
+            if (j0 + t < nvec) {
+                const double *v = Vp[j0 + t] + (int64_t)r * Np + base;
+#pragma unroll
+                for (int u = 0; u < kDotChunk / 256; u++) {
+                    int o = threadIdx.x + u * 256;
+                    if (o < len) acc[t] += v[o] * wv[u];
+                }
+            }
         }
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) partial[((int64_t)r * nvec + jv) * nch + ch] = s;
+#pragma unroll
+        for (int t = 0; t < T; t++)
+            for (int o = 16; o > 0; o >>= 1) acc[t] += __shfl_xor_sync(0xffffffffu, acc[t], o);
+        if (lane == 0)
+            for (int t = 0; t < T; t++) sh[warp][t] = acc[t];
+        __syncthreads();
+        if (threadIdx.x < T && j0 + threadIdx.x < nvec) {
+            double sum = 0.0;
+            for (int ww = 0; ww < 8; ww++) sum += sh[ww][threadIdx.x];
+            partial[((int64_t)r * nvec + j0 + threadIdx.x) * ch.n + c] = sum;
+        }
+        __syncthreads();
     }
 }
 
-// out[(r*nvec + j)*ostride + ooff] = sum over chunks
-__global__ void k_reduce_partials(int nvec, int nch, const double *__restrict__ partial, const int *__restrict__ active,
-                                  double *__restrict__ out, int64_t ostride_r, int64_t ostride_j) {
-    __shared__ double sh[32];
-    int j = blockIdx.x, r = blockIdx.y;
-    if (active && !active[r]) return;
-    double s = 0.0;
-    for (int c = threadIdx.x; c < nch; c += blockDim.x) s += partial[((int64_t)r * nvec + j) * nch + c];
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) out[r * ostride_r + j * ostride_j] = s;
+// out[sidx*ostride_s + j*ostride_j] = sum of partial[(r*nvec + j)*nch + c]
+// over geometry g's chunks, in chunk order; one warp per (j, r, g)
+__global__ void k_reduce_seg(int nvec, int ks, int G, int nch, const double *__restrict__ partial,
+                             const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
+                             const int *__restrict__ active, double *__restrict__ out, int64_t ostride_s, int64_t ostride_j) {
+    int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (wid >= (int64_t)nvec * ks * G) return;
+    int j = (int)(wid % nvec);
+    int64_t rg = wid / nvec;
+    int r = (int)(rg % ks), g = (int)(rg / ks);
+    int sidx = g * ks + r;
+    if (active && !active[sidx]) return;
+    double sum = 0.0;
+    int c0 = g_ch_first[g], cn = g_ch_count[g];
+    const double *pp = partial + ((int64_t)r * nvec + j) * nch + c0;
+    for (int c = lane; c < cn; c += 32) sum += pp[c];
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) out[sidx * ostride_s + j * ostride_j] = sum;
 }
 
-// v[r] = w[r] - sum_j h_j V_j[r]; partial sums of |v|^2
+// v[r] = w[r] - sum_j h_j V_j[r] with the solve's own h; partial |v|^2 per chunk
 __global__ void k_update(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w,
-                         const double *__restrict__ H, int64_t hstride_r, const int *__restrict__ active,
+                         const double *__restrict__ Hcol, SegChunks ch, int ks, const int *__restrict__ active,
                          double *__restrict__ v, double *__restrict__ partial) {
     __shared__ double sh[32];
-    int r = blockIdx.y, ch = blockIdx.x, nch = gridDim.x;
-    if (active && !active[r]) return;
-    const double *h = H + r * hstride_r;
+    int r = blockIdx.y, c = blockIdx.x;
+    int sidx = ch.geom[c] * ks + r;
+    if (!active[sidx]) return;
+    const double *h = Hcol + (int64_t)sidx * (nvec + 1);
+    int64_t base = ch.start[c];
+    int len = ch.len[c];
     double s2 = 0.0;
     for (int u = 0; u < kDotChunk / 256; u++) {
-        int64_t j = (int64_t)ch * kDotChunk + threadIdx.x + u * 256;
-        if (j >= Np) break;
-        double x = w[(int64_t)r * Np + j];
-        for (int jv = 0; jv < nvec; jv++) x = x - h[jv] * Vp[jv][(int64_t)r * Np + j];
-        v[(int64_t)r * Np + j] = x;
+        int o = threadIdx.x + u * 256;
+        if (o >= len) break;
+        int64_t t = (int64_t)r * Np + base + o;
+        double x = w[t];
+        for (int jv = 0; jv < nvec; jv++) x = x - h[jv] * Vp[jv][t];
+        v[t] = x;
         s2 += x * x;
     }
     s2 = block_sum(s2, sh);
-    if (threadIdx.x == 0) partial[(int64_t)r * nch + ch] = s2;
+    if (threadIdx.x == 0) partial[(int64_t)r * ch.n + c] = s2;
 }
 
-// Givens update of column i of every active right-hand side (one thread each)
-__global__ void k_givens(int k, int i, int M, double *H, double *cs, double *sn, double *g, const double *normb,
-                         const double *nrm2, double *hnorm, double tol, int *active, int *iters, int *n_active) {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r == 0) *n_active = 0;
-    __syncthreads();
-    if (r >= k) return;
-    if (!active[r]) return;
-    double *hc = H + ((int64_t)r * (M + 1) + i) * (M + 2);
-    double *c = cs + (int64_t)r * (M + 2), *s = sn + (int64_t)r * (M + 2), *gg = g + (int64_t)r * (M + 2);
-    double hn = sqrt(nrm2[r]);
-    hnorm[r] = hn;
+// Givens update of Hessenberg column i of every active solve (one thread each)
+__global__ void k_givens(int S, int i, int M, double *__restrict__ Hc, double *cs, double *sn, double *g, const double *normb,
+                         const double *nrm2, double *hnorm, double tol, const int *scap, int *active, int *iters, int *capped,
+                         int *n_active) {
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= S || !active[sidx]) return;
+    double *hc = Hc + (int64_t)sidx * (i + 2);
+    double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2), *gg = g + (int64_t)sidx * (M + 2);
+    double hn = sqrt(nrm2[sidx]);
+    hnorm[sidx] = hn;
     hc[i + 1] = hn;
     for (int j = 0; j < i; j++) {
         double t1 = hc[j], t2 = hc[j + 1];
-        hc[j] = c[j] * t1 - s[j] * t2;
-        hc[j + 1] = c[j] * t2 + s[j] * t1;
+        hc[j] = c[j] * t1 - sv[j] * t2;
+        hc[j + 1] = c[j] * t2 + sv[j] * t1;
     }
     double t1 = hc[i], t2 = hc[i + 1];
     double len = sqrt(t1 * t1 + t2 * t2);
     c[i] = t1 / len;
-    s[i] = -t2 / len;
-    hc[i] = c[i] * t1 - s[i] * t2;
+    sv[i] = -t2 / len;
+    hc[i] = c[i] * t1 - sv[i] * t2;
     hc[i + 1] = 0;
     t1 = gg[i];
     gg[i] = c[i] * t1;
-    gg[i + 1] = s[i] * t1;
-    double res = fabs(gg[i + 1]) / normb[r];
+    gg[i + 1] = sv[i] * t1;
+    double res = fabs(gg[i + 1]) / normb[sidx];
     if (res < tol) {
-        active[r] = 0;
-        iters[r] = i;
+        active[sidx] = 0;
+        iters[sidx] = i;
+    } else if (i + 1 >= scap[sidx]) {
+        // the solve's iteration cap: keep the last Arnoldi step
+        active[sidx] = 0;
+        iters[sidx] = i;
+        capped[sidx] = 1;
     } else {
         atomicAdd(n_active, 1);
     }
 }
 
-__global__ void k_scale(int64_t Np, int k, const double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
-                        double *__restrict__ out) {
-    int64_t n = (int64_t)k * Np;
+// out[r][j] = v[r][j] / hn[solve of (j, r)] for active solves
+__global__ void k_scale(int64_t Np, int ks, const double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
+                        const int32_t *__restrict__ leaf_geom, double *__restrict__ out) {
+    int64_t n = (int64_t)ks * Np;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int r = (int)(t / Np);
-        if (active && !active[r]) continue;
-        out[t] = v[t] / hn[r];
+        int64_t j = t - (int64_t)r * Np;
+        int sidx = leaf_geom[j] * ks + r;
+        if (active && !active[sidx]) continue;
+        out[t] = v[t] / hn[sidx];
     }
 }
 
-// back substitution R z = g for every right-hand side (one thread each)
-__global__ void k_backsub(int k, int M, const double *H, const double *g, const int *iters, double *z) {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= k) return;
-    int it = iters[r];
-    double *zz = z + (int64_t)r * (M + 2);
-    const double *gg = g + (int64_t)r * (M + 2);
+// back substitution R z = g for every solve (one thread each)
+__global__ void k_backsub(int S, int M, double *const *__restrict__ Hc, const double *g, const int *iters, double *z) {
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= S) return;
+    int it = iters[sidx];
+    double *zz = z + (int64_t)sidx * (M + 2);
+    const double *gg = g + (int64_t)sidx * (M + 2);
     for (int i = 0; i <= it; i++) zz[i] = gg[i];
     for (int i = it; i >= 0; i--) {
-        const double *hc = H + ((int64_t)r * (M + 1) + i) * (M + 2);
+        const double *hc = Hc[i] + (int64_t)sidx * (i + 2);
         zz[i] = zz[i] / hc[i];
         for (int j = i - 1; j >= 0; j--) zz[j] = zz[j] - hc[j] * zz[i];
     }
 }
 
-// y[r] = sum_{j <= iters[r]} z_j V_j[r]
-__global__ void k_combine(int64_t Np, int k, int M, double *const *__restrict__ Vp, const double *__restrict__ z,
-                          const int *__restrict__ iters, double *__restrict__ y) {
-    int64_t n = (int64_t)k * Np;
+// y[r][j] = sum_{jv <= iters(s)} z_s[jv] V_jv[r][j]
+__global__ void k_combine(int64_t Np, int ks, int M, double *const *__restrict__ Vp, const double *__restrict__ z,
+                          const int *__restrict__ iters, const int32_t *__restrict__ leaf_geom, double *__restrict__ y) {
+    int64_t n = (int64_t)ks * Np;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int r = (int)(t / Np);
         int64_t j = t - (int64_t)r * Np;
-        int it = iters[r];
-        double s = 0.0;
-        for (int jv = 0; jv <= it; jv++) s += Vp[jv][(int64_t)r * Np + j] * z[(int64_t)r * (M + 2) + jv];
-        y[t] = s;
+        int sidx = leaf_geom[j] * ks + r;
+        int it = iters[sidx];
+        double sum = 0.0;
+        for (int jv = 0; jv <= it; jv++) sum += Vp[jv][t] * z[(int64_t)sidx * (M + 2) + jv];
+        y[t] = sum;
     }
 }
 
 // x = x0 + P y (or x0 alone when the initial guess already met the tolerance)
-__global__ void k_finish(int64_t Np, int k, const double *__restrict__ x0, const double *__restrict__ y,
-                         const double *__restrict__ diag, const int *__restrict__ iters, double *__restrict__ x) {
-    int64_t n = (int64_t)k * Np;
+__global__ void k_finish(int64_t Np, int ks, const double *__restrict__ x0, const double *__restrict__ y,
+                         const double *__restrict__ diag, const int *__restrict__ iters, const int32_t *__restrict__ leaf_geom,
+                         double *__restrict__ x) {
+    int64_t n = (int64_t)ks * Np;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int r = (int)(t / Np);
         int64_t j = t - (int64_t)r * Np;
-        if (iters[r] < 0) { x[t] = x0[t]; continue; }
+        if (iters[leaf_geom[j] * ks + r] < 0) { x[t] = x0[t]; continue; }
         double py = diag ? y[t] / diag[j] : y[t];
         x[t] = x0[t] + py;
     }
 }
 
-// r = b - w, and partial norms of r and b
-__global__ void k_residual(int64_t Np, const double *__restrict__ b, const double *__restrict__ wv, double *__restrict__ r,
-                           double *__restrict__ pr, double *__restrict__ pb) {
+// r = b - w over one chunk, with partial norms of r and b
+__global__ void k_residual(int64_t Np, const double *__restrict__ b, const double *__restrict__ wv, SegChunks ch,
+                           double *__restrict__ rv, double *__restrict__ pr, double *__restrict__ pb) {
     __shared__ double sh[32];
-    int rr = blockIdx.y, ch = blockIdx.x, nch = gridDim.x;
+    int r = blockIdx.y, c = blockIdx.x;
+    int64_t base = ch.start[c];
+    int len = ch.len[c];
     double s1 = 0.0, s2 = 0.0;
     for (int u = 0; u < kDotChunk / 256; u++) {
-        int64_t j = (int64_t)ch * kDotChunk + threadIdx.x + u * 256;
-        if (j >= Np) break;
-        int64_t t = (int64_t)rr * Np + j;
+        int o = threadIdx.x + u * 256;
+        if (o >= len) break;
+        int64_t t = (int64_t)r * Np + base + o;
         double bb = b[t];
         double x = wv ? bb - wv[t] : bb;
-        r[t] = x;
+        rv[t] = x;
         s1 += x * x;
         s2 += bb * bb;
     }
     s1 = block_sum(s1, sh);
-    if (threadIdx.x == 0) pr[(int64_t)rr * nch + ch] = s1;
+    if (threadIdx.x == 0) pr[(int64_t)r * ch.n + c] = s1;
     s2 = block_sum(s2, sh);
-    if (threadIdx.x == 0) pb[(int64_t)rr * nch + ch] = s2;
+    if (threadIdx.x == 0) pb[(int64_t)r * ch.n + c] = s2;
 }
 
-__global__ void k_init_state(int k, int M, double *nr2, double *nb2, double *normb, double *g, double *hn, double tol,
-                             int *active, int *iters) {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= k) return;
-    double nr = sqrt(nr2[r]), nb = sqrt(nb2[r]);
-    normb[r] = nb;
-    g[(int64_t)r * (M + 2)] = nr;
-    hn[r] = nr;
-    if (nr / nb < tol) { active[r] = 0; iters[r] = -1; }
-    else { active[r] = 1; iters[r] = 0; }
+__global__ void k_init_state(int S, int M, const double *nr2, const double *nb2, double *normb, double *g, double *hn, double tol,
+                             int *active, int *iters, int *capped) {
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= S) return;
+    capped[sidx] = 0;
+    double nr = sqrt(nr2[sidx]), nb = sqrt(nb2[sidx]);
+    normb[sidx] = nb;
+    g[(int64_t)sidx * (M + 2)] = nr;
+    if (nb == 0.0 || nr / nb < tol) {
+        // unused slot, or the initial guess already meets the tolerance
+        active[sidx] = 0;
+        iters[sidx] = -1;
+        hn[sidx] = 1.0;
+    } else {
+        active[sidx] = 1;
+        iters[sidx] = 0;
+        hn[sidx] = nr;
+    }
 }
 
 // C assembly (CSolveCap::Solve, Solver/SolveCapacitance.cpp:1305-1366):
-// cap[r][c] = sum over conductor c's leaves of outer permittivity * charge.
-// Stage 1: every CTA sums one slice of kAsmChunk leaves of one conductor for
-// one right-hand side; stage 2 adds the slices in order (deterministic).
+// entry e = (solve column slot, conductor column) of some geometry,
+// C_e = sum over the conductor's leaves of outer permittivity * charge.
+// Stage 1: every CTA sums one slice of kAsmChunk leaves of one entry; stage 2
+// adds the slices in order (deterministic).
 static const int kAsmChunk = 4096;
-__global__ void k_assemble_part(int64_t Np, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
-                                const double *__restrict__ weight, const double *__restrict__ x, int ncol, double *__restrict__ part) {
+__global__ void k_assemble_part(int64_t Np, const int32_t *__restrict__ e_slot, const int64_t *__restrict__ e_first,
+                                const int64_t *__restrict__ e_count, const double *__restrict__ weight, const double *__restrict__ x,
+                                double *__restrict__ part) {
     __shared__ double sh[32];
-    int sl = blockIdx.x, c = blockIdx.y, r = blockIdx.z;
-    int64_t lo = first[c] + (int64_t)sl * kAsmChunk, hi = min(first[c] + count[c], lo + kAsmChunk);
+    int e = blockIdx.x, sl = blockIdx.y;
+    int64_t lo = e_first[e] + (int64_t)sl * kAsmChunk, hi = min(e_first[e] + e_count[e], lo + kAsmChunk);
+    const double *xr = x + (int64_t)e_slot[e] * Np;
     double s = 0.0;
-    for (int64_t j = lo + threadIdx.x; j < hi; j += blockDim.x) s += weight[j] * x[(int64_t)r * Np + j];
+    for (int64_t j = lo + threadIdx.x; j < hi; j += blockDim.x) s += weight[j] * xr[j];
     s = block_sum(s, sh);
-    if (threadIdx.x == 0) part[((int64_t)r * ncol + c) * gridDim.x + sl] = s;
+    if (threadIdx.x == 0) part[(int64_t)e * gridDim.y + sl] = s;
 }
 
-__global__ void k_assemble_sum(int nslice, const double *__restrict__ part, int ncol, double *__restrict__ cap) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
-    if (c >= ncol) return;
+__global__ void k_assemble_sum(int nentry, int nslice, const double *__restrict__ part, const int64_t *__restrict__ e_out,
+                               double *__restrict__ cap) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nentry) return;
     double s = 0.0;
-    for (int i = 0; i < nslice; i++) s += part[((int64_t)r * ncol + c) * nslice + i];
-    cap[(int64_t)r * ncol + c] = s;
+    for (int i = 0; i < nslice; i++) s += part[(int64_t)e * nslice + i];
+    cap[e_out[e]] = s;
 }
 
 // -------------------------------------------------------------- host side
@@ -1052,6 +1235,8 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         dright[lab[i]] = a.node_right[i] >= 0 ? lab[a.node_right[i]] : -1;
     }
     for (int64_t j = 0; j < Np; j++) dleaf[j] = lab[leaf_node[j]];
+    p->h_node_leaf_first.assign(Nn, 0);
+    for (int64_t i = 0; i < Nn; i++) p->h_node_leaf_first[lab[i]] = a.node_leaf_first[i];
     p->h_ptr_model.assign(a.link_ptr, a.link_ptr + Nn + 1);
     p->h_ptr_dev.assign(Nn + 1, 0);
     p->h_inv = inv;
@@ -1127,6 +1312,8 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
 #undef FCG_TRY
 }
 
+static void free_solve_ws(DeviceProblem *p);
+
 void problem_destroy(DeviceProblem *p) {
     if (!p) return;
     cudaSetDevice(p->ctx->device);
@@ -1139,11 +1326,9 @@ void problem_destroy(DeviceProblem *p) {
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
     dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
     dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->arrive);
-    for (size_t i = 0; i < p->V.size(); i++) dfree(p->V[i]);
-    dfree(p->Vptr); dfree(p->H); dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->normb); dfree(p->hnorm);
-    dfree(p->nrm2); dfree(p->z); dfree(p->partial); dfree(p->active); dfree(p->iters); dfree(p->n_active);
-    dfree(p->b); dfree(p->x0); dfree(p->w); dfree(p->vv); dfree(p->x);
-    if (p->h_n_active) cudaFreeHost(p->h_n_active);
+    free_solve_ws(p);
+    dfree(p->partial);
+    dfree(p->leaf_geom); dfree(p->ch_start); dfree(p->ch_len); dfree(p->ch_geom); dfree(p->g_ch_first); dfree(p->g_ch_count);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     for (size_t i = 0; i < p->ev_pool.size(); i++) cudaEventDestroy(p->ev_pool[i]);
@@ -1387,13 +1572,26 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
             else k_spmv64<KK, 32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd);     \
         }                                                                                                             \
     } while (0)
-        switch (kp) {
-        case 1: FCG_SPMV(1); break;
-        case 2: FCG_SPMV(2); break;
-        case 4: FCG_SPMV(4); break;
-        case 8: FCG_SPMV(8); break;
-        case 16: FCG_SPMV(16); break;
-        default: FCG_SPMV(32); break;
+        int mgrid = (int)std::min<int64_t>((p->Nn + 7) / 8, (int64_t)p->ctx->sm_count * 32);
+        if (kp == 1) {
+            FCG_SPMV(1);
+        } else if (mixed && kp == 2) {
+            FCG_SPMV(2);
+        } else if (mixed) {
+            switch (kp) {
+            case 4: k_spmv32_multi<4><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 8: k_spmv32_multi<8><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 16: k_spmv32_multi<16><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            default: k_spmv32_multi<32><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            }
+        } else {
+            switch (kp) {
+            case 2: k_spmv64_multi<2><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 4: k_spmv64_multi<4><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 8: k_spmv64_multi<8><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 16: k_spmv64_multi<16><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            default: k_spmv64_multi<32><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            }
         }
 #undef FCG_SPMV
         prof_end(p);
@@ -1458,62 +1656,169 @@ int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k) {
 
 // ------------------------------------------------------------------ GMRES
 
-static int ensure_solve_ws(DeviceProblem *p, int k, int M) {
-    int64_t Np = p->Np;
-    int nch = (int)((Np + kDotChunk - 1) / kDotChunk);
+int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond) {
+    if (n < 1 || !geom_of_cond) { set_error("need at least one geometry"); return FCG_GENERIC_ERROR; }
+    int nc = p->n_cond_all;
+    if (nc < 1) { set_error("model has no conductors"); return FCG_GENERIC_ERROR; }
+    // conductors of a geometry are contiguous, geometries numbered in order,
+    // conductor leaf ranges back to back
+    if (geom_of_cond[0] != 0) { set_error("the first conductor must belong to geometry 0"); return FCG_GENERIC_ERROR; }
+    for (int c = 1; c < nc; c++) {
+        int d = geom_of_cond[c] - geom_of_cond[c - 1];
+        if (d != 0 && d != 1) { set_error("geometries must be numbered in conductor order without gaps"); return FCG_GENERIC_ERROR; }
+        if (p->cond_first[c] != p->cond_first[c - 1] + p->cond_count[c - 1]) {
+            set_error("conductor leaf ranges are not contiguous");
+            return FCG_GENERIC_ERROR;
+        }
+    }
+    if (geom_of_cond[nc - 1] != n - 1) { set_error("geometry count does not match the conductor map"); return FCG_GENERIC_ERROR; }
+    if (p->cond_first[0] != 0 || p->cond_first[nc - 1] + p->cond_count[nc - 1] != p->Np) {
+        set_error("conductor leaf ranges do not cover the panels");
+        return FCG_GENERIC_ERROR;
+    }
+    FCG_CK(cudaSetDevice(p->ctx->device));
+    int64_t Np = p->Np, Nn = p->Nn;
+    std::vector<int64_t> gfirst(n, -1), gcount(n, 0);
+    std::vector<int32_t> leaf_geom(Np);
+    for (int c = 0; c < nc; c++) {
+        int g = geom_of_cond[c];
+        if (gfirst[g] < 0) gfirst[g] = p->cond_first[c];
+        gcount[g] += p->cond_count[c];
+        for (int64_t j = p->cond_first[c]; j < p->cond_first[c] + p->cond_count[c]; j++) leaf_geom[j] = g;
+    }
+    for (int g = 0; g < n; g++)
+        if (gcount[g] == 0) { set_error("geometry " + std::to_string(g) + " has no panels"); return FCG_GENERIC_ERROR; }
+    std::vector<int> cols_ptr(n + 1, 0);
+    for (size_t i = 0; i < p->cond_cols.size(); i++) cols_ptr[geom_of_cond[p->cond_cols[i]] + 1]++;
+    for (int g = 0; g < n; g++) cols_ptr[g + 1] += cols_ptr[g];
+    // chunks of at most kDotChunk leaves inside each geometry
+    std::vector<int64_t> ch_start;
+    std::vector<int32_t> ch_len, ch_geom, gch_first(n), gch_count(n);
+    for (int g = 0; g < n; g++) {
+        gch_first[g] = (int32_t)ch_start.size();
+        for (int64_t j = gfirst[g]; j < gfirst[g] + gcount[g]; j += kDotChunk) {
+            ch_start.push_back(j);
+            ch_len.push_back((int32_t)std::min<int64_t>(kDotChunk, gfirst[g] + gcount[g] - j));
+            ch_geom.push_back(g);
+        }
+        gch_count[g] = (int32_t)ch_start.size() - gch_first[g];
+    }
+    // every node and link must stay inside one geometry: a product that
+    // couples geometries would make the separate solves wrong
+    std::vector<int32_t> node_geom(Nn);
+    for (int64_t v = 0; v < Nn; v++) node_geom[v] = leaf_geom[p->h_node_leaf_first[v]];
+    cudaStream_t s = p->stream;
+    int64_t tb = 0;
+    int32_t *d_ng = NULL;
+    unsigned *d_bad = NULL;
+    int r = upload(&d_ng, node_geom.data(), Nn, tb, s);
+    if (r == FCG_NORMAL_END) r = dalloc(&d_bad, 1, tb);
+    unsigned bad = 0;
+    if (r == FCG_NORMAL_END) {
+        cudaMemsetAsync(d_bad, 0, sizeof(unsigned), s);
+        int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
+        k_check_geometries<<<grid, 256, 0, s>>>(Nn, p->link_ptr, p->link_src, p->parent, d_ng, d_bad);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("geometry check failed");
+            r = FCG_DEVICE_ERROR;
+        }
+    }
+    dfree(d_ng);
+    dfree(d_bad);
+    if (r != FCG_NORMAL_END) return r;
+    if (bad) {
+        set_error(std::to_string(bad) + " tree edges or links connect different geometries");
+        return FCG_GENERIC_ERROR;
+    }
+    dfree(p->leaf_geom); dfree(p->ch_start); dfree(p->ch_len); dfree(p->ch_geom); dfree(p->g_ch_first); dfree(p->g_ch_count);
+    p->n_geom = 0;
+    if ((r = upload(&p->leaf_geom, leaf_geom.data(), Np, p->bytes, s)) ||
+        (r = upload(&p->ch_start, ch_start.data(), ch_start.size(), p->bytes, s)) ||
+        (r = upload(&p->ch_len, ch_len.data(), ch_len.size(), p->bytes, s)) ||
+        (r = upload(&p->ch_geom, ch_geom.data(), ch_geom.size(), p->bytes, s)) ||
+        (r = upload(&p->g_ch_first, gch_first.data(), n, p->bytes, s)) ||
+        (r = upload(&p->g_ch_count, gch_count.data(), n, p->bytes, s)))
+        return r;
+    FCG_CK(cudaStreamSynchronize(s));
+    p->n_geom = n;
+    p->nch = (int)ch_start.size();
+    p->geom_cols_ptr = cols_ptr;
+    p->geom_leaf_first = gfirst;
+    p->geom_leaf_count = gcount;
+    return FCG_NORMAL_END;
+}
+
+static void free_solve_ws(DeviceProblem *p) {
+    dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->z);
+    dfree(p->normb); dfree(p->hnorm); dfree(p->nrm2);
+    dfree(p->active); dfree(p->iters); dfree(p->capped); dfree(p->scap); dfree(p->n_active);
+    dfree(p->b); dfree(p->x0); dfree(p->w); dfree(p->vv); dfree(p->x);
+    for (size_t i = 0; i < p->V.size(); i++) dfree(p->V[i]);
+    p->V.clear();
+    for (size_t i = 0; i < p->Hblk.size(); i++) dfree(p->Hblk[i]);
+    p->Hblk.clear();
+    p->Hc.clear();
+    dfree(p->Vptr);
+    dfree(p->Hptr);
+    p->Vptr_cap = 0;
+    if (p->h_pin) cudaFreeHost(p->h_pin);
+    p->h_pin = NULL;
+    p->h_pin_cap = 0;
+    p->gk = p->gS = p->gM = 0;
+}
+
+static int ensure_solve_ws(DeviceProblem *p, int k, int S, int M) {
     int r;
-    if (p->gk != k || p->gM < M) {
-        dfree(p->H); dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->z);
-        dfree(p->normb); dfree(p->hnorm); dfree(p->nrm2); dfree(p->active); dfree(p->iters); dfree(p->n_active);
-        dfree(p->b); dfree(p->x0); dfree(p->w); dfree(p->vv); dfree(p->x);
-        for (size_t i = 0; i < p->V.size(); i++) dfree(p->V[i]);
-        p->V.clear();
-        dfree(p->Vptr);
-        p->Vptr_cap = 0;
+    if (p->gk != k || p->gS != S || p->gM < M) {
+        free_solve_ws(p);
         int64_t &B = p->bytes;
-        size_t hs = (size_t)k * (M + 1) * (M + 2);
-        if ((r = dalloc(&p->H, hs, B))) return r;
-        if ((r = dalloc(&p->cs, (size_t)k * (M + 2), B))) return r;
-        if ((r = dalloc(&p->sn, (size_t)k * (M + 2), B))) return r;
-        if ((r = dalloc(&p->g, (size_t)k * (M + 2), B))) return r;
-        if ((r = dalloc(&p->z, (size_t)k * (M + 2), B))) return r;
-        if ((r = dalloc(&p->normb, k, B))) return r;
-        if ((r = dalloc(&p->hnorm, k, B))) return r;
-        if ((r = dalloc(&p->nrm2, 2 * k, B))) return r;
-        if ((r = dalloc(&p->active, k, B))) return r;
-        if ((r = dalloc(&p->iters, k, B))) return r;
-        if ((r = dalloc(&p->n_active, 1, B))) return r;
-        size_t n = (size_t)k * Np;
-        if ((r = dalloc(&p->b, n, B))) return r;
-        if ((r = dalloc(&p->x0, n, B))) return r;
-        if ((r = dalloc(&p->w, n, B))) return r;
-        if ((r = dalloc(&p->vv, n, B))) return r;
-        if ((r = dalloc(&p->x, n, B))) return r;
-        if ((r = dalloc(&p->Vptr, (size_t)M + 2, B))) return r;
+        size_t sm = (size_t)S * (M + 2);
+        if ((r = dalloc(&p->cs, sm, B)) || (r = dalloc(&p->sn, sm, B)) || (r = dalloc(&p->g, sm, B)) || (r = dalloc(&p->z, sm, B)))
+            return r;
+        if ((r = dalloc(&p->normb, S, B)) || (r = dalloc(&p->hnorm, S, B)) || (r = dalloc(&p->nrm2, 2 * (size_t)S, B))) return r;
+        if ((r = dalloc(&p->active, S, B)) || (r = dalloc(&p->iters, S, B)) || (r = dalloc(&p->capped, S, B)) ||
+            (r = dalloc(&p->scap, S, B)) || (r = dalloc(&p->n_active, (size_t)M + 2, B)))
+            return r;
+        size_t n = (size_t)k * p->Np;
+        if ((r = dalloc(&p->b, n, B)) || (r = dalloc(&p->x0, n, B)) || (r = dalloc(&p->w, n, B)) || (r = dalloc(&p->vv, n, B)) ||
+            (r = dalloc(&p->x, n, B)))
+            return r;
+        if ((r = dalloc(&p->Vptr, (size_t)M + 2, B)) || (r = dalloc(&p->Hptr, (size_t)M + 2, B))) return r;
         p->Vptr_cap = M + 2;
         p->gk = k;
+        p->gS = S;
         p->gM = M;
         p->x_k = k;
-        if (!p->h_n_active && cudaHostAlloc((void **)&p->h_n_active, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+        p->h_pin_cap = 3 * (size_t)S + 4;
+        if (cudaHostAlloc((void **)&p->h_pin, p->h_pin_cap * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+            p->h_pin = NULL;
             set_error("cannot allocate pinned host memory");
             return FCG_OUT_OF_MEMORY;
         }
     }
-    size_t need = (size_t)2 * k * (M + 1) * nch;
-    if ((size_t)p->partial_cap < need) {
-        dfree(p->partial);
-        if ((r = dalloc(&p->partial, need, p->bytes))) return r;
-        p->partial_cap = (int)need;
-    }
     return FCG_NORMAL_END;
 }
 
-// make sure basis vector j exists (allocated in groups of 16 vectors)
+// partial sums: grows with the number of basis vectors
+static int ensure_partial(DeviceProblem *p, size_t need) {
+    if (p->partial_cap >= need) return FCG_NORMAL_END;
+    size_t cap = std::max(need, 2 * p->partial_cap);
+    FCG_CK(cudaStreamSynchronize(p->stream));
+    dfree(p->partial);
+    p->partial_cap = 0;
+    int r = dalloc(&p->partial, cap, p->bytes);
+    if (r == FCG_NORMAL_END) p->partial_cap = cap;
+    return r;
+}
+
+// make sure basis vector j and Hessenberg column j - 1 exist (allocated in
+// groups of 16)
 static int ensure_basis(DeviceProblem *p, int j) {
-    if ((int)p->V.size() > j) return FCG_NORMAL_END;
     const int group = 16;
-    size_t n = (size_t)p->gk * p->Np;
     int r;
+    size_t n = (size_t)p->gk * p->Np;
     while ((int)p->V.size() <= j) {
         int start = (int)p->V.size();
         int cnt = std::min(group, p->Vptr_cap - start);
@@ -1524,7 +1829,26 @@ static int ensure_basis(DeviceProblem *p, int j) {
         std::vector<double *> ptrs(cnt);
         for (int i = 0; i < cnt; i++) ptrs[i] = blk + n * i;
         FCG_CK(cudaMemcpyAsync(p->Vptr + start, ptrs.data(), cnt * sizeof(double *), cudaMemcpyHostToDevice, p->stream));
-        // the pinned copy source must outlive the transfer
+        // the copy source must outlive the transfer
+        FCG_CK(cudaStreamSynchronize(p->stream));
+    }
+    while ((int)p->Hc.size() < j) {
+        int start = (int)p->Hc.size();
+        int cnt = std::min(group, p->Vptr_cap - start);
+        if (cnt <= 0) { set_error("Hessenberg storage exhausted"); return FCG_GENERIC_ERROR; }
+        size_t tot = 0;
+        for (int i = 0; i < cnt; i++) tot += (size_t)p->gS * (start + i + 2);
+        double *blk = NULL;
+        if ((r = dalloc(&blk, tot, p->bytes))) return r;
+        p->Hblk.push_back(blk);
+        std::vector<double *> ptrs(cnt);
+        size_t off = 0;
+        for (int i = 0; i < cnt; i++) {
+            ptrs[i] = blk + off;
+            p->Hc.push_back(blk + off);
+            off += (size_t)p->gS * (start + i + 2);
+        }
+        FCG_CK(cudaMemcpyAsync(p->Hptr + start, ptrs.data(), cnt * sizeof(double *), cudaMemcpyHostToDevice, p->stream));
         FCG_CK(cudaStreamSynchronize(p->stream));
     }
     return FCG_NORMAL_END;
@@ -1540,144 +1864,187 @@ static double *basis_addr(DeviceProblem *p, int j) {
 int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations) {
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
-    int ncol = (int)p->cond_cols.size();
-    if (ncol == 0) { set_error("no conductors to solve for"); return FCG_GENERIC_ERROR; }
-    int64_t Np = p->Np;
-    int cap_it = opt.max_iter > 0 ? opt.max_iter : 1000;
-    if (cap_it > Np) cap_it = (int)Np;
-    if (cap_it > 1000 && opt.max_iter <= 0) cap_it = 1000;
+    int r;
+    if (p->cond_cols.empty()) { set_error("no conductors to solve for"); return FCG_GENERIC_ERROR; }
+    if (p->n_geom == 0) {
+        std::vector<int32_t> one(p->n_cond_all, 0);
+        if ((r = problem_set_geometries(p, 1, one.data()))) return r;
+    }
+    const int G = p->n_geom;
+    const int64_t Np = p->Np;
+    const int nch = p->nch;
+    // per geometry: columns, output offsets, iteration cap (the reference's
+    // min(1000, panels) for the geometry alone)
+    std::vector<int> ncol(G);
+    std::vector<int64_t> cap_off(G + 1, 0), it_off(G + 1, 0);
+    std::vector<int> gcap(G);
+    int ks = 0, M = 1;
+    for (int g = 0; g < G; g++) {
+        ncol[g] = p->geom_cols_ptr[g + 1] - p->geom_cols_ptr[g];
+        ks = std::max(ks, ncol[g]);
+        cap_off[g + 1] = cap_off[g] + (int64_t)ncol[g] * ncol[g];
+        it_off[g + 1] = it_off[g] + ncol[g];
+        int64_t c = opt.max_iter > 0 ? opt.max_iter : 1000;
+        c = std::min<int64_t>(c, p->geom_leaf_count[g]);
+        gcap[g] = (int)std::max<int64_t>(c, 1);
+        M = std::max(M, gcap[g]);
+    }
     const double *diag = (opt.precond == FCG_PRECOND_JACOBI) ? p->self : NULL;
     cudaStream_t s = p->stream;
     int sms = p->ctx->sm_count;
-    std::vector<int64_t> cf(ncol), cc(ncol);
-    for (int c = 0; c < ncol; c++) { cf[c] = p->cond_first[p->cond_cols[c]]; cc[c] = p->cond_count[p->cond_cols[c]]; }
-    int64_t *d_cf = NULL, *d_cc = NULL;
-    double *d_cap = NULL, *d_part = NULL;
-    int64_t tmpb = 0, maxcount = 1;
-    for (int c = 0; c < ncol; c++) maxcount = std::max(maxcount, cc[c]);
-    int nslice = (int)((maxcount + kAsmChunk - 1) / kAsmChunk);
-    int r;
-    if ((r = upload(&d_cf, cf.data(), ncol, tmpb, s)) || (r = upload(&d_cc, cc.data(), ncol, tmpb, s)) ||
-        (r = dalloc(&d_cap, (size_t)ncol * ncol, tmpb)) ||
-        (r = dalloc(&d_part, (size_t)nslice * ncol * std::min(ncol, kMaxK), tmpb))) {
-        dfree(d_cf); dfree(d_cc); dfree(d_cap); dfree(d_part);
-        return r;
-    }
-    std::vector<double> h_cap((size_t)ncol * ncol, 0.0);
-    std::vector<int> h_iters(ncol, 0);
+    SegChunks chunks = {p->ch_start, p->ch_len, p->ch_geom, nch};
+    double *d_cap = NULL;
+    int64_t tmpb = 0;
+    if ((r = dalloc(&d_cap, (size_t)std::max<int64_t>(cap_off[G], 1), tmpb))) return r;
+    std::vector<int> h_iters(it_off[G], 0);
     p->timings.iterations_max = 0;
     int status = FCG_NORMAL_END;
-    float solve_ms_total = 0, asm_ms_total = 0;
-    // right-hand sides in batches of at most kMaxK conductors
-    for (int c0 = 0; c0 < ncol && status == FCG_NORMAL_END; c0 += kMaxK) {
-        int k = std::min(kMaxK, ncol - c0);
-        int M = cap_it;
-        if ((r = ensure_solve_ws(p, k, M))) { status = r; break; }
-        int nch = (int)((Np + kDotChunk - 1) / kDotChunk);
-        int64_t n = (int64_t)k * Np;
-        int g1 = grid_for(n, 256, sms);
+    bool any_capped = false;
+    float solve_ms_total = 0;
+    // columns in batches of at most `width`: batch column r of geometry g is the
+    // solve for the geometry's conductor r0 + r
+    const int width = opt.rhs_width > 0 ? std::min(opt.rhs_width, kMaxK) : kMaxK;
+    for (int r0 = 0; r0 < ks && status == FCG_NORMAL_END; r0 += width) {
+        const int k = std::min(width, ks - r0);
+        const int S = G * k;
+        std::vector<int64_t> sf(S, 0), sc(S, 0);
+        std::vector<int> scap(S);
+        std::vector<int32_t> e_slot;
+        std::vector<int64_t> e_first, e_count, e_out;
+        int64_t maxcount = 1;
+        for (int g = 0; g < G; g++) {
+            const int *cols = p->cond_cols.data() + p->geom_cols_ptr[g];
+            for (int rr = 0; rr < k; rr++) {
+                int sidx = g * k + rr;
+                scap[sidx] = gcap[g];
+                if (r0 + rr >= ncol[g]) continue;
+                sf[sidx] = p->cond_first[cols[r0 + rr]];
+                sc[sidx] = p->cond_count[cols[r0 + rr]];
+                for (int c = 0; c < ncol[g]; c++) {
+                    e_slot.push_back(rr);
+                    e_first.push_back(p->cond_first[cols[c]]);
+                    e_count.push_back(p->cond_count[cols[c]]);
+                    e_out.push_back(cap_off[g] + (int64_t)(r0 + rr) * ncol[g] + c);
+                    maxcount = std::max(maxcount, p->cond_count[cols[c]]);
+                }
+            }
+        }
+        const int nentry = (int)e_slot.size();
+        const int nslice = (int)((maxcount + kAsmChunk - 1) / kAsmChunk);
+        int64_t *d_sf = NULL, *d_sc = NULL, *d_ef = NULL, *d_ec = NULL, *d_eo = NULL;
+        int32_t *d_es = NULL;
+        double *d_part = NULL;
+        int64_t bb = 0;
+        auto free_batch = [&]() {
+            cudaStreamSynchronize(s);
+            dfree(d_sf); dfree(d_sc); dfree(d_ef); dfree(d_ec); dfree(d_eo); dfree(d_es); dfree(d_part);
+        };
+        if ((r = ensure_solve_ws(p, k, S, M)) || (r = ensure_partial(p, (size_t)2 * k * nch)) ||
+            (r = upload(&d_sf, sf.data(), S, bb, s)) || (r = upload(&d_sc, sc.data(), S, bb, s)) ||
+            (r = upload(&d_es, e_slot.data(), nentry, bb, s)) || (r = upload(&d_ef, e_first.data(), nentry, bb, s)) ||
+            (r = upload(&d_ec, e_count.data(), nentry, bb, s)) || (r = upload(&d_eo, e_out.data(), nentry, bb, s)) ||
+            (r = dalloc(&d_part, (size_t)nentry * nslice, bb))) {
+            free_batch();
+            status = r;
+            break;
+        }
+        FCG_CK(cudaMemcpyAsync(p->scap, scap.data(), S * sizeof(int), cudaMemcpyHostToDevice, s));
+        const int64_t n = (int64_t)k * Np;
+        const int g1 = grid_for(n, 256, sms);
+        const int gs = (S + 127) / 128;
+        auto seg_grid = [&](int nvec) { return (int)(((int64_t)nvec * k * G * 32 + 255) / 256); };
+        if ((r = ensure_basis(p, 0))) { free_batch(); status = r; break; }
         cudaEventRecord(p->ev0, s);
-        k_set_rhs<<<g1, 256, 0, s>>>(Np, k, d_cf + c0, d_cc + c0, p->b);
-        if ((r = ensure_basis(p, 0))) { status = r; break; }
+        k_set_rhs<<<g1, 256, 0, s>>>(Np, k, p->leaf_geom, d_sf, d_sc, p->b);
         double *V0 = basis_addr(p, 0);
         double *pr = p->partial, *pb = p->partial + (size_t)k * nch;
         if (diag) {
             k_precond<<<g1, 256, 0, s>>>(Np, k, p->b, diag, p->x0);
-            if ((r = matvec(p, p->x0, p->w, k, NULL))) { status = r; break; }
-            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, p->vv, pr, pb);
+            if ((r = matvec(p, p->x0, p->w, k, NULL))) { free_batch(); status = r; break; }
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, chunks, p->vv, pr, pb);
         } else {
             FCG_CK(cudaMemsetAsync(p->x0, 0, n * sizeof(double), s));
-            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, NULL, p->vv, pr, pb);
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, NULL, chunks, p->vv, pr, pb);
         }
-        k_reduce_partials<<<dim3(1, k), 256, 0, s>>>(1, nch, pr, NULL, p->nrm2, 1, 0);
-        k_reduce_partials<<<dim3(1, k), 256, 0, s>>>(1, nch, pb, NULL, p->nrm2 + k, 1, 0);
-        FCG_CK(cudaMemsetAsync(p->g, 0, (size_t)k * (M + 2) * sizeof(double), s));
-        k_init_state<<<1, 32 * ((k + 31) / 32), 0, s>>>(k, M, p->nrm2, p->nrm2 + k, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters);
-        k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, V0);
+        k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pr, p->g_ch_first, p->g_ch_count, NULL, p->nrm2, 1, 0);
+        k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pb, p->g_ch_first, p->g_ch_count, NULL, p->nrm2 + S, 1, 0);
+        FCG_CK(cudaMemsetAsync(p->g, 0, (size_t)S * (M + 2) * sizeof(double), s));
+        FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
+        k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
+                                        p->capped);
+        k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0);
         FCG_CK(cudaGetLastError());
-        p->timings.launches += diag ? 7 : 6;
-        int64_t hstride_r = (int64_t)(M + 1) * (M + 2);
-        int last_i = -1;
-        bool any = true;
-        // check whether the initial guess already satisfies the tolerance
-        {
-            std::vector<int> act(k);
-            FCG_CK(cudaMemcpyAsync(act.data(), p->active, k * sizeof(int), cudaMemcpyDeviceToHost, s));
-            FCG_CK(cudaStreamSynchronize(s));
-            any = false;
-            for (int i = 0; i < k; i++) any |= act[i] != 0;
-        }
-        for (int i = 0; any && i < cap_it; i++) {
-            if ((r = ensure_basis(p, i + 1))) { status = r; break; }
+        p->timings.launches += diag ? 8 : 7;
+        // does any solve need an Arnoldi step?
+        bool any = false;
+        FCG_CK(cudaMemcpyAsync(p->h_pin, p->active, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+        FCG_CK(cudaStreamSynchronize(s));
+        for (int i = 0; i < S; i++) any |= p->h_pin[i] != 0;
+        for (int i = 0; any && i < M; i++) {
+            if ((r = ensure_basis(p, i + 1)) || (r = ensure_partial(p, (size_t)k * (i + 1) * nch))) { status = r; break; }
             double *Vi = basis_addr(p, i), *Vn = basis_addr(p, i + 1);
+            double *hcol = p->Hc[i];
             // w = A P q_i
             if ((r = matvec(p, Vi, p->w, k, diag))) { status = r; break; }
-            // classical Gram-Schmidt against q_0..q_i
-            k_dots<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, p->active, p->partial);
-            double *hcol = p->H + (int64_t)i * (M + 2);
-            k_reduce_partials<<<dim3(i + 1, k), 256, 0, s>>>(i + 1, nch, p->partial, p->active, hcol, hstride_r, 1);
-            k_update<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, hcol, hstride_r, p->active, p->vv, p->partial);
-            k_reduce_partials<<<dim3(1, k), 256, 0, s>>>(1, nch, p->partial, p->active, p->nrm2, 1, 0);
-            k_givens<<<1, 32 * ((k + 31) / 32), 0, s>>>(k, i, M, p->H, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, opt.tol,
-                                                        p->active, p->iters, p->n_active);
-            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, p->active, Vn);
+            // classical Gram-Schmidt against q_0..q_i, per solve
+            k_dots<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, chunks, k, p->active, p->partial);
+            k_reduce_seg<<<seg_grid(i + 1), 256, 0, s>>>(i + 1, k, G, nch, p->partial, p->g_ch_first, p->g_ch_count, p->active,
+                                                          hcol, i + 2, 1);
+            k_update<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, hcol, chunks, k, p->active, p->vv, p->partial);
+            k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1,
+                                                      0);
+            k_givens<<<gs, 128, 0, s>>>(S, i, M, hcol, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, opt.tol, p->scap, p->active,
+                                        p->iters, p->capped, p->n_active + i);
+            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, p->active, p->leaf_geom, Vn);
             FCG_CK(cudaGetLastError());
             p->timings.launches += 6;
-            FCG_CK(cudaMemcpyAsync(p->h_n_active, p->n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FCG_CK(cudaMemcpyAsync(p->h_pin, p->n_active + i, sizeof(int), cudaMemcpyDeviceToHost, s));
             FCG_CK(cudaStreamSynchronize(s));
             prof_collect(p);
-            last_i = i;
-            any = *p->h_n_active > 0;
-            (void)Vn;
+            any = p->h_pin[0] > 0;
         }
-        if (status != FCG_NORMAL_END) break;
-        // right-hand sides still active hit the cap: use the last Arnoldi step
-        std::vector<int> it(k), act(k);
-        FCG_CK(cudaMemcpyAsync(it.data(), p->iters, k * sizeof(int), cudaMemcpyDeviceToHost, s));
-        FCG_CK(cudaMemcpyAsync(act.data(), p->active, k * sizeof(int), cudaMemcpyDeviceToHost, s));
-        FCG_CK(cudaStreamSynchronize(s));
-        bool notconv = false;
-        for (int i = 0; i < k; i++)
-            if (act[i]) { it[i] = last_i; notconv = true; }
-        FCG_CK(cudaMemcpyAsync(p->iters, it.data(), k * sizeof(int), cudaMemcpyHostToDevice, s));
-        k_backsub<<<1, 32 * ((k + 31) / 32), 0, s>>>(k, M, p->H, p->g, p->iters, p->z);
-        k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->w);
-        k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->x);
-        FCG_CK(cudaGetLastError());
+        if (status != FCG_NORMAL_END) { free_batch(); break; }
+        k_backsub<<<gs, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
+        k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
+        k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->leaf_geom, p->x);
         cudaEventRecord(p->ev1, s);
-        k_assemble_part<<<dim3(nslice, ncol, k), 256, 0, s>>>(Np, d_cf, d_cc, p->leaf_weight, p->x, ncol, d_part);
-        k_assemble_sum<<<dim3((ncol + 31) / 32, k), 32, 0, s>>>(nslice, d_part, ncol, d_cap + (size_t)c0 * ncol);
+        if (nentry > 0) {
+            k_assemble_part<<<dim3(nentry, nslice), 256, 0, s>>>(Np, d_es, d_ef, d_ec, p->leaf_weight, p->x, d_part);
+            k_assemble_sum<<<(nentry + 127) / 128, 128, 0, s>>>(nentry, nslice, d_part, d_eo, d_cap);
+        }
         FCG_CK(cudaGetLastError());
-        p->timings.launches += 5;
+        p->timings.launches += nentry > 0 ? 5 : 3;
+        FCG_CK(cudaMemcpyAsync(p->h_pin, p->iters, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+        FCG_CK(cudaMemcpyAsync(p->h_pin + S, p->capped, S * sizeof(int), cudaMemcpyDeviceToHost, s));
         FCG_CK(cudaStreamSynchronize(s));
         prof_collect(p);
         float ms = 0;
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         solve_ms_total += ms;
-        for (int i = 0; i < k; i++) {
-            h_iters[c0 + i] = it[i] + 1;
-            p->timings.iterations_max = std::max(p->timings.iterations_max, it[i] + 1);
-        }
-        if (notconv) status = FCG_NOT_CONVERGED;
-        if (ncol > kMaxK) {
-            // keep the charges of this batch in the x buffer of the last batch only
-        }
+        bool notconv = false;
+        for (int g = 0; g < G; g++)
+            for (int rr = 0; rr < k && r0 + rr < ncol[g]; rr++) {
+                int sidx = g * k + rr, it = p->h_pin[sidx] + 1;
+                h_iters[it_off[g] + r0 + rr] = it;
+                p->timings.iterations_max = std::max(p->timings.iterations_max, it);
+                notconv |= p->h_pin[S + sidx] != 0;
+            }
+        free_batch();
+        any_capped |= notconv;
     }
+    if (status == FCG_NORMAL_END && any_capped) status = FCG_NOT_CONVERGED;
     if (status == FCG_NORMAL_END || status == FCG_NOT_CONVERGED) {
-        if (cudaMemcpy(h_cap.data(), d_cap, h_cap.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        if (cap && cap_off[G] > 0 &&
+            cudaMemcpy(cap, d_cap, (size_t)cap_off[G] * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
             set_error("copy of the capacitance matrix failed");
             status = FCG_DEVICE_ERROR;
-        } else {
-            if (cap) memcpy(cap, h_cap.data(), h_cap.size() * sizeof(double));
-            if (iterations) memcpy(iterations, h_iters.data(), ncol * sizeof(int));
+        } else if (iterations) {
+            memcpy(iterations, h_iters.data(), h_iters.size() * sizeof(int));
         }
     }
     p->timings.solve_ms = solve_ms_total;
-    p->timings.assemble_ms = asm_ms_total;
-    dfree(d_cf);
-    dfree(d_cc);
+    p->timings.assemble_ms = 0;
     dfree(d_cap);
-    dfree(d_part);
     return status;
 }
 

@@ -8,6 +8,8 @@
 #include <chrono>
 #include <string>
 #include <vector>
+#include <algorithm>
+#include <new>
 
 #include "../../include/fastercap_gb300.h"
 #include "../csrc/fcg_internal.hpp"
@@ -140,6 +142,69 @@ const char *fcg_model_conductor_name(const fcg_model *fm, int32_t i) {
 
 void fcg_model_free(fcg_model *fm) { delete fm; }
 
+int fcg_model_concat(const fcg_model *const *models, int32_t n, fcg_model **out, int32_t *geom_of_cond) {
+    if (!models || n <= 0 || !out) return FCG_GENERIC_ERROR;
+    *out = NULL;
+    fcg_model *fm = new (std::nothrow) fcg_model();
+    if (!fm) return FCG_OUT_OF_MEMORY;
+    fcg::Model &M = fm->m;
+    try {
+        int64_t node_off = 0, leaf_off = 0, link_off = 0;
+        int32_t ci = 0;
+        M.link_ptr.push_back(0);
+        for (int32_t g = 0; g < n; g++) {
+            if (!models[g]) { delete fm; return FCG_GENERIC_ERROR; }
+            const fcg::Model &A = models[g]->m;
+            for (int64_t i = 0; i < A.n_nodes; i++) {
+                M.type.push_back(A.type[i]);
+                M.left.push_back(A.left[i] >= 0 ? (int32_t)(A.left[i] + node_off) : -1);
+                M.right.push_back(A.right[i] >= 0 ? (int32_t)(A.right[i] + node_off) : -1);
+                M.cond.push_back(A.cond[i] + ci);
+                M.leaf_first.push_back(A.leaf_first[i] + leaf_off);
+                M.leaf_count.push_back(A.leaf_count[i]);
+                M.link_ptr.push_back(A.link_ptr[i + 1] + link_off);
+                M.area.push_back(A.area[i]);
+                M.maxside.push_back(A.maxside[i]);
+                M.maxside_idx.push_back(A.maxside_idx[i]);
+            }
+            M.vert.insert(M.vert.end(), A.vert.begin(), A.vert.end());
+            M.cent.insert(M.cent.end(), A.cent.begin(), A.cent.end());
+            M.norm.insert(M.norm.end(), A.norm.begin(), A.norm.end());
+            for (int64_t l = 0; l < A.n_links; l++) M.link_src.push_back((int32_t)(A.link_src[l] + node_off));
+            for (int64_t j = 0; j < A.n_panels; j++) {
+                M.leaf_node.push_back((int32_t)(A.leaf_node[j] + node_off));
+                M.leaf_diel.push_back(A.leaf_diel[j]);
+            }
+            for (size_t c = 0; c < A.conductors.size(); c++) {
+                M.conductors.push_back(A.conductors[c]);
+                M.cond_leaf_first.push_back(A.cond_leaf_first[c] + leaf_off);
+                if (geom_of_cond) geom_of_cond[ci] = g;
+                ci++;
+            }
+            node_off += A.n_nodes;
+            leaf_off += A.n_panels;
+            link_off += A.n_links;
+            M.input_panels += A.input_panels;
+            M.max_level = std::max(M.max_level, A.max_level);
+            M.max_mesh_eps = std::max(M.max_mesh_eps, A.max_mesh_eps);
+        }
+        if (node_off > 0x1FFFFFFF || link_off > 0x7fffffff) {
+            delete fm;
+            fcg::set_error("concatenated model too large");
+            return FCG_OUT_OF_MEMORY;
+        }
+        M.n_nodes = node_off;
+        M.n_panels = leaf_off;
+        M.n_links = link_off;
+    } catch (std::bad_alloc &) {
+        delete fm;
+        return FCG_OUT_OF_MEMORY;
+    }
+    finish_model(fm);
+    *out = fm;
+    return FCG_NORMAL_END;
+}
+
 const char *fcg_last_error(void) { return fcg::get_error(); }
 
 int fcg_context_create(int device, fcg_context **out) {
@@ -202,11 +267,16 @@ int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap,
     o.tol = 0.01;
     o.precond = FCG_PRECOND_JACOBI;
     o.max_iter = 0;
+    o.rhs_width = 0;
     if (opt) o = *opt;
     return fcg::problem_solve(p->p, o, cap, iterations);
 }
 int fcg_problem_get_charges(fcg_problem *p, double *charges) {
     return (p && charges) ? fcg::problem_get_charges(p->p, charges) : FCG_GENERIC_ERROR;
+}
+
+int fcg_problem_set_geometries(fcg_problem *p, int32_t n, const int32_t *geom) {
+    return p ? fcg::problem_set_geometries(p->p, n, geom) : FCG_GENERIC_ERROR;
 }
 
 int fcg_problem_set_profiling(fcg_problem *p, int enable) {
@@ -374,7 +444,7 @@ extern "C" int fcg_run_command_line(const char *command_line) {
         nc = info.n_conductors - info.n_dielectrics;
         cap.resize((size_t)nc * nc);
         iters.resize(nc);
-        fcg_solve_options so = {o.gmres_tol, o.precond, 0};
+        fcg_solve_options so = {o.gmres_tol, o.precond, 0, 0};
         r = fcg_problem_solve(p, &so, cap.data(), iters.data());
     }
     auto t2 = std::chrono::steady_clock::now();

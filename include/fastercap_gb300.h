@@ -105,6 +105,14 @@ int fcg_model_arrays_get(const fcg_model *m, fcg_model_arrays *arrays);
 const char *fcg_model_conductor_name(const fcg_model *m, int32_t index);
 void fcg_model_free(fcg_model *m);
 
+/* Concatenate independent models (geometries) into one model: a forest with
+ * no link between geometries, conductors and leaves in model order.
+ * geometry_of_conductor (may be NULL) receives, per conductor of the result,
+ * the index of the model it came from. Used to solve many geometries with one
+ * launch per kernel (fcg_problem_set_geometries). No counterpart in the
+ * reference, which solves one geometry per run. */
+int fcg_model_concat(const fcg_model *const *models, int32_t n_models, fcg_model **out, int32_t *geometry_of_conductor);
+
 /* ---------------------------------------------------------------- device */
 
 /* One GPU, its streams and the tuned launch shapes. */
@@ -161,7 +169,18 @@ typedef struct {
     double tol;       /* -t GMRES relative residual tolerance (default 0.01) */
     int precond;      /* FCG_PRECOND_NONE or FCG_PRECOND_JACOBI */
     int max_iter;     /* 0: the reference's cap min(1000, n_panels) */
+    int rhs_width;    /* right-hand sides per batched solve: 0 = up to 32, 1 = one at a time */
 } fcg_solve_options;
+
+/* Declare that the problem holds several independent geometries: conductor c
+ * belongs to geometry geometry_of_conductor[c]; every geometry's conductors
+ * and leaves must be contiguous (as fcg_model_concat produces them). Each
+ * geometry then gets its own GMRES solves (own residuals, Krylov bases,
+ * iteration counts) while every product runs once over all geometries.
+ * fcg_problem_solve then writes the geometries' capacitance matrices one
+ * after another (geometry g: n_g x n_g over its non-dielectric conductors)
+ * and iterations per geometry and conductor in the same order. */
+int fcg_problem_set_geometries(fcg_problem *p, int32_t n_geometries, const int32_t *geometry_of_conductor);
 
 /* Solve for the capacitance matrix: one right-hand side per conductor, all
  * conductors in one batched right-preconditioned GMRES, C assembled on the
