@@ -54,12 +54,14 @@ WORKLOADS = {
                          5e-6, 1.0, 1e-4, None),
 }
 
-# many independent geometries in one problem: name -> (seeds, mesh_eps,
-# eps_ratio, gmres tol). crossings32: 32 random k x k crossings in vacuum
-# (k in 2..10, length 10-60 um, pitch 2-4 um, gap 1-3 um; seeds 0..31):
-# 5,312 to 39,040 panels each, 748,928 panels and 257M links in all.
+# many independent geometries in one problem: name -> (crossing list,
+# mesh_eps, eps_ratio, gmres tol). crossings32: 32 random k x k crossings in
+# vacuum drawn in order from default_rng(0) (k in 2..10, length 10-60 um,
+# pitch 2-4 um, gap 1-3 um): 4,736 to 48,128 panels each, 765,504 panels,
+# 428 conductors and 255.2M links in all.
 MULTI = {
-    "crossings32": (list(range(32)), 1e-3, 1.0, 1e-4),
+    "crossings32": (lambda: __import__("fastercap_gb300.geometry", fromlist=["x"]).crossing_batch(0, 32, 2, 10),
+                    1e-3, 1.0, 1e-4),
 }
 
 
@@ -131,14 +133,13 @@ def peaks():
 def build_multi(workload: str):
     """(concatenated model, geometry_of_conductor, [per-geometry models], build s, tol, link eps)"""
     import fastercap_gb300 as fc
-    from fastercap_gb300 import geometry as geo
-    seeds, meps, dratio, tol = MULTI[workload]
+    make, meps, dratio, tol = MULTI[workload]
     models = []
     t0 = time.perf_counter()
     with tempfile.TemporaryDirectory() as tmp:
-        for sd in seeds:
-            path = os.path.join(tmp, "r%d.txt" % sd)
-            geo.random_crossing(sd).write(path)
+        for g, cr in enumerate(make()):
+            path = os.path.join(tmp, "g%d.txt" % g)
+            cr.write(path)
             models.append(fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio))
     model, geom = fc.Model.concat(models)
     return model, geom, models, time.perf_counter() - t0, tol, meps * dratio
@@ -237,7 +238,7 @@ def run_reference_multi(args, rank, world):
             panels.append(m.n_panels)
     total = sum(times)
     value = len(times) / total
-    sample = ("one geometry per step, cycling through the %d in seed order (steps %d..%d: %d panels in all)"
+    sample = ("one geometry per step, cycling through the %d in order (steps %d..%d: %d panels in all)"
               % (len(models), args.warmup, args.warmup + args.steps - 1, sum(panels)))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
@@ -411,7 +412,7 @@ def run_gb300_multi(args, rank, world, local_rank):
                 break
         dt = time.perf_counter() - t0
         result["cpu_baseline"] = {"value": n_done / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-                                  "sample": "the first %d geometries in seed order, one full solve each" % n_done}
+                                  "sample": "the first %d geometries in order, one full solve each" % n_done}
         result["accuracy"]["max_rel_c_err_vs_cpu_fp64"] = max(errs)
     if rank == 0:
         print(json.dumps(result), flush=True)

@@ -85,6 +85,25 @@ class SolveOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("precond", C.c_int), ("max_iter", C.c_int), ("rhs_width", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("memory_budget", C.c_int64), ("iterations_hint", C.c_int)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("status", C.c_int), ("n_cond", C.c_int), ("iterations_max", C.c_int),
+                ("slot", C.c_int), ("footprint_bytes", C.c_int64), ("device_bytes", C.c_int64),
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("fill_ms", C.c_double), ("solve_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("slots", C.c_int), ("running", C.c_int), ("queued", C.c_int), ("max_running", C.c_int),
+                ("budget", C.c_int64), ("in_use", C.c_int64), ("peak_in_use", C.c_int64),
+                ("submitted", C.c_int64), ("completed", C.c_int64)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_CANCELLED = 0, 1, 2, 3
+
+
 # (field, dtype, length key, columns)
 ARRAY_FIELDS = [
     ("node_type", np.uint8, "n_nodes", 1), ("node_left", np.int32, "n_nodes", 1), ("node_right", np.int32, "n_nodes", 1),
@@ -141,6 +160,17 @@ def lib() -> C.CDLL:
     L.fcg_problem_get_charges.argtypes = [vp, vp]
     L.fcg_run_command_line.argtypes = [C.c_char_p]
     L.fcg_model_concat.argtypes = [C.POINTER(vp), i32, C.POINTER(vp), vp]
+    L.fcg_problem_cancel.argtypes = [vp]
+    L.fcg_problem_estimate_bytes.argtypes = [C.POINTER(ModelArrays), C.c_int, C.c_int, C.c_int]
+    L.fcg_problem_estimate_bytes.restype = i64
+    L.fcg_server_create.argtypes = [vp, C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.fcg_server_destroy.argtypes = [vp]
+    L.fcg_server_destroy.restype = None
+    L.fcg_server_submit.argtypes = [vp, C.POINTER(ModelArrays), C.c_int, C.POINTER(SolveOptions), C.POINTER(i64)]
+    L.fcg_server_poll.argtypes = [vp, i64, C.POINTER(JobInfo)]
+    L.fcg_server_result.argtypes = [vp, i64, vp, vp, C.POINTER(JobInfo)]
+    L.fcg_server_cancel.argtypes = [vp, i64]
+    L.fcg_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
     L.fcg_problem_set_geometries.argtypes = [vp, i32, vp]
     _lib = L
     return L
@@ -402,6 +432,10 @@ class Problem:
             return caps[0], its[0]
         return caps, its
 
+    def cancel(self):
+        """Stop a running (or the next) solve at its next Arnoldi step (FCError USER_BREAK)."""
+        _check(lib().fcg_problem_cancel(self._h), "cancel")
+
     def charges(self) -> np.ndarray:
         """Charges of the last batch of right-hand-side columns, [k][n_panels]."""
         ks = max(self.geometries or [self.n_cond])
@@ -439,6 +473,9 @@ class Context:
     def problem(self, model: Model, precision: int = PREC_MIXED, stream=None) -> Problem:
         return Problem(self, model, precision, stream)
 
+    def server(self, slots: int = 4, memory_budget: int = 0, iterations_hint: int = 0) -> "Server":
+        return Server(self, slots, memory_budget, iterations_hint)
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             lib().fcg_context_destroy(self._h)
@@ -449,6 +486,87 @@ class Context:
 
     def __exit__(self, *a):
         self.close()
+
+
+def estimate_bytes(model: Model, precision: int = PREC_MIXED, rhs: int = 0, iterations: int = 64) -> int:
+    """Device bytes of a problem of this model after a solve (the server's admission footprint)."""
+    arr = model.c_arrays()
+    return int(lib().fcg_problem_estimate_bytes(C.byref(arr), precision, rhs or len(model.conductor_names), iterations))
+
+
+class Job:
+    """A submitted extraction; result() waits for it."""
+
+    def __init__(self, server: "Server", jid: int, model: Model, arrays: ModelArrays):
+        self.server, self.id, self.model = server, jid, model
+        self._arrays = arrays  # the C view must outlive the job
+        self.n_cond = len(model.conductor_names)
+        self.info = None
+        self.status = None
+
+    def poll(self) -> dict:
+        info = JobInfo()
+        _check(lib().fcg_server_poll(self.server._h, self.id, C.byref(info)), "poll")
+        return {f: getattr(info, f) for f, _ in JobInfo._fields_}
+
+    def cancel(self):
+        _check(lib().fcg_server_cancel(self.server._h, self.id), "cancel")
+
+    def result(self, allow_not_converged=False):
+        """(C, iterations); raises FCError if the job failed or was cancelled."""
+        cap = np.empty((self.n_cond, self.n_cond), np.float64)
+        it = np.empty(self.n_cond, np.int32)
+        info = JobInfo()
+        code = lib().fcg_server_result(self.server._h, self.id, _ptr(cap), _ptr(it), C.byref(info))
+        self.info = {f: getattr(info, f) for f, _ in JobInfo._fields_}
+        self.status = code
+        self._arrays = None
+        if not (code == NORMAL_END or (allow_not_converged and code == NOT_CONVERGED)):
+            _check(code, "job %d" % self.id)
+        return cap, it
+
+
+class Server:
+    """Continuous-admission extraction server on one GPU (fcg_server_*)."""
+
+    def __init__(self, ctx: "Context", slots: int = 4, memory_budget: int = 0, iterations_hint: int = 0):
+        self._ctx = ctx
+        h = C.c_void_p()
+        cfg = ServerConfig(slots, memory_budget, iterations_hint)
+        _check(lib().fcg_server_create(ctx._h, C.byref(cfg), C.byref(h)), "server create")
+        self._h = h
+
+    def submit(self, model: Model, precision: int = PREC_MIXED, tol: float = 0.01, precond: int = PRECOND_JACOBI,
+               max_iter: int = 0, rhs_width: int = 0) -> Job:
+        arr = model.c_arrays()
+        keep = model._keep
+        opt = SolveOptions(tol, precond, max_iter, rhs_width)
+        jid = C.c_int64()
+        _check(lib().fcg_server_submit(self._h, C.byref(arr), precision, C.byref(opt), C.byref(jid)), "submit")
+        job = Job(self, jid.value, model, (arr, keep))
+        return job
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().fcg_server_get_stats(self._h, C.byref(st)), "server stats")
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            lib().fcg_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_command_line(cmd: str) -> int:

@@ -62,7 +62,7 @@ def build(verbose: bool = False, reference: bool = True) -> None:
     headers += [os.path.join(host, f) for f in os.listdir(host) if f.endswith((".h", ".hpp"))]
     headers.append(os.path.join(ROOT, "include", "fastercap_gb300.h"))
     cu = [os.path.join(csrc, f) for f in sorted(os.listdir(csrc)) if f.endswith(".cu")]
-    cpp = [os.path.join(host, f) for f in ("model_builder.cpp", "api.cpp")]
+    cpp = [os.path.join(host, f) for f in ("model_builder.cpp", "api.cpp", "server.cpp")]
     objs, cmds = [], []
     for src in cu:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

@@ -5,6 +5,8 @@
 
 #include <stdint.h>
 #include <atomic>
+#include <mutex>
+#include <vector>
 #include <string>
 #include <vector>
 
@@ -27,6 +29,11 @@ struct DeviceContext {
     // the handle and every problem created on the context hold a reference;
     // the GPU resources go when the last one is dropped
     std::atomic<int> refs{1};
+    // pinned host words for per-iteration readbacks, one 64-byte slot per
+    // problem (allocated once: page-locked allocation synchronises the device)
+    int *pin = nullptr;
+    std::mutex pin_mu;
+    std::vector<int> pin_free;
 };
 void context_release(DeviceContext &ctx);
 void context_unref(DeviceContext *ctx);
@@ -46,6 +53,15 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
 int problem_get_charges(DeviceProblem *p, double *charges);
 int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond);
 int problem_n_cond(const DeviceProblem *p);
+// request cancellation: the solve returns FCG_USER_BREAK at its next Arnoldi step
+void problem_cancel(DeviceProblem *p);
+// device bytes a problem of this model will hold after a solve of `rhs`
+// right-hand sides in at most `iterations` Arnoldi steps
+int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs, int iterations);
+
+// CUDA streams for host code compiled without the CUDA headers
+void *stream_create(int device);
+void stream_destroy(int device, void *stream);
 
 // timings of the last fill / solve in milliseconds (CUDA events on the problem's stream)
 struct SolveTimings {

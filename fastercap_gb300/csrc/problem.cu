@@ -44,6 +44,8 @@ namespace fcg {
 static const int kBlockLeaves = 256;  // leaves per sweep subtree
 static const int kMaxK = 32;          // right-hand sides per matvec batch
 static const int kDotChunk = 1024;    // vector elements per CTA in the Krylov kernels
+static const int kPinSlots = 1024;    // pinned readback slots per context
+static const int kPinSlotInts = 16;
 // link words: source node in the low 29 bits, distance band (0..4) in the top 3
 static const uint32_t kSrcMask = 0x1FFFFFFFu;
 static const int kBandShift = 29;
@@ -57,13 +59,35 @@ struct __align__(16) NodeGeo {
     double area;
 };
 
+// Device allocations are stream-ordered (cudaMallocAsync / cudaFreeAsync on
+// the problem's stream, from the device's memory pool) inside an AllocScope:
+// no allocation or free synchronises the device, so problems on different
+// streams (the serving slots) never stall one another. Outside a scope the
+// plain calls are used.
+static thread_local cudaStream_t t_alloc_stream = NULL;
+static thread_local bool t_alloc_async = false;
+struct AllocScope {
+    cudaStream_t prev;
+    bool prev_async;
+    explicit AllocScope(cudaStream_t s) : prev(t_alloc_stream), prev_async(t_alloc_async) {
+        t_alloc_stream = s;
+        t_alloc_async = true;
+    }
+    ~AllocScope() {
+        t_alloc_stream = prev;
+        t_alloc_async = prev_async;
+    }
+};
+
 // device allocation tracked against the problem's byte count
 template <class T> static int dalloc(T **p, size_t n, int64_t &bytes) {
     *p = NULL;
     if (n == 0) return FCG_NORMAL_END;
-    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    cudaError_t e = t_alloc_async ? cudaMallocAsync((void **)p, n * sizeof(T), t_alloc_stream)
+                                  : cudaMalloc((void **)p, n * sizeof(T));
     if (e != cudaSuccess) {
-        set_error(std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed: " + cudaGetErrorString(e));
+        cudaGetLastError();
+        set_error(std::string("device allocation of ") + std::to_string(n * sizeof(T)) + " bytes failed: " + cudaGetErrorString(e));
         *p = NULL;
         return e == cudaErrorMemoryAllocation ? FCG_OUT_OF_MEMORY : FCG_DEVICE_ERROR;
     }
@@ -71,7 +95,10 @@ template <class T> static int dalloc(T **p, size_t n, int64_t &bytes) {
     return FCG_NORMAL_END;
 }
 template <class T> static void dfree(T *&p) {
-    if (p) cudaFree(p);
+    if (p) {
+        if (t_alloc_async) cudaFreeAsync(p, t_alloc_stream);
+        else cudaFree(p);
+    }
     p = NULL;
 }
 template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes, cudaStream_t s) {
@@ -154,8 +181,9 @@ struct DeviceProblem {
     double *partial = NULL;
     size_t partial_cap = 0;
     int *active = NULL, *iters = NULL, *capped = NULL, *scap = NULL, *n_active = NULL;
-    int *h_pin = NULL;  // pinned host ints for the per-iteration readback
-    size_t h_pin_cap = 0;
+    int *pin = NULL;  // pinned readback slot from the context (NULL: pageable fallback)
+    int pin_local[kPinSlotInts];
+    std::atomic<int> cancel{0};  // set by fcg_problem_cancel; checked between Arnoldi steps
     double *b = NULL, *x0 = NULL, *w = NULL, *vv = NULL, *x = NULL;
     int x_k = 0;
 };
@@ -944,7 +972,7 @@ __global__ void k_residual(int64_t Np, const double *__restrict__ b, const doubl
 }
 
 __global__ void k_init_state(int S, int M, const double *nr2, const double *nb2, double *normb, double *g, double *hn, double tol,
-                             int *active, int *iters, int *capped) {
+                             int *active, int *iters, int *capped, int *n_start) {
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (sidx >= S) return;
     capped[sidx] = 0;
@@ -960,6 +988,7 @@ __global__ void k_init_state(int S, int M, const double *nr2, const double *nb2,
         active[sidx] = 1;
         iters[sidx] = 0;
         hn[sidx] = nr;
+        atomicAdd(n_start, 1);
     }
 }
 
@@ -1018,7 +1047,34 @@ int context_init(DeviceContext &ctx, int device) {
     cudaStream_t st;
     FCG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     ctx.stream = (void *)st;
+    // the device's memory pool keeps freed blocks for reuse by later problems
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (cudaHostAlloc((void **)&ctx.pin, (size_t)kPinSlots * kPinSlotInts * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+        ctx.pin = nullptr;
+        set_error("cannot allocate pinned host memory");
+        return FCG_OUT_OF_MEMORY;
+    }
+    ctx.pin_free.clear();
+    for (int i = kPinSlots - 1; i >= 0; i--) ctx.pin_free.push_back(i);
     return FCG_NORMAL_END;
+}
+
+// a pinned slot of kPinSlotInts ints for one problem (NULL when all are taken)
+static int *pin_acquire(DeviceContext &ctx) {
+    std::lock_guard<std::mutex> lk(ctx.pin_mu);
+    if (!ctx.pin || ctx.pin_free.empty()) return NULL;
+    int i = ctx.pin_free.back();
+    ctx.pin_free.pop_back();
+    return ctx.pin + (size_t)i * kPinSlotInts;
+}
+static void pin_release(DeviceContext &ctx, int *slot) {
+    if (!slot || !ctx.pin) return;
+    std::lock_guard<std::mutex> lk(ctx.pin_mu);
+    ctx.pin_free.push_back((int)((slot - ctx.pin) / kPinSlotInts));
 }
 
 void context_unref(DeviceContext *ctx) {
@@ -1029,11 +1085,21 @@ void context_unref(DeviceContext *ctx) {
 }
 
 void context_release(DeviceContext &ctx) {
+    cudaSetDevice(ctx.device);
     if (ctx.stream) {
-        cudaSetDevice(ctx.device);
         cudaStreamSynchronize((cudaStream_t)ctx.stream);
         cudaStreamDestroy((cudaStream_t)ctx.stream);
         ctx.stream = nullptr;
+    }
+    if (ctx.pin) {
+        cudaFreeHost(ctx.pin);
+        ctx.pin = nullptr;
+    }
+    // hand the pool's unused blocks back
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx.device) == cudaSuccess) {
+        cudaDeviceSynchronize();
+        cudaMemPoolTrimTo(pool, 0);
     }
 }
 
@@ -1169,6 +1235,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     p->ctx = &ctx;
     ctx.refs.fetch_add(1);
     p->precision = precision;
+    p->pin = pin_acquire(ctx);
     p->Nn = a.n_nodes;
     p->Np = a.n_panels;
     p->L = a.n_links;
@@ -1193,6 +1260,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     }
     cudaStream_t s = p->stream;
     int64_t Nn = a.n_nodes, Np = a.n_panels, L = a.n_links;
+    AllocScope alloc_scope(s);
     // Device node labels: height-major (all leaves in leaf order, then every
     // height in tree order). Interaction partners have similar heights and are
     // spatially close, so the link product's charge gathers cluster (2.3x
@@ -1318,6 +1386,7 @@ void problem_destroy(DeviceProblem *p) {
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
+    AllocScope alloc_scope(p->stream);
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
     dfree(p->left); dfree(p->right); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
     dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
@@ -1334,11 +1403,51 @@ void problem_destroy(DeviceProblem *p) {
     for (size_t i = 0; i < p->ev_pool.size(); i++) cudaEventDestroy(p->ev_pool[i]);
     if (p->stream && p->owns_stream) cudaStreamDestroy(p->stream);
     DeviceContext *ctx = p->ctx;
+    pin_release(*ctx, p->pin);
     delete p;
     context_unref(ctx);
 }
 
 int64_t problem_device_bytes(const DeviceProblem *p) { return p ? p->bytes : 0; }
+
+void problem_cancel(DeviceProblem *p) {
+    if (p) p->cancel.store(1);
+}
+
+int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs, int iterations) {
+    int64_t Nn = a.n_nodes, Np = a.n_panels, L = a.n_links;
+    int64_t c = precision == FCG_PREC_FP64 ? 8 : 4;
+    int k = std::max(1, std::min(rhs, kMaxK));
+    int kp = 1;
+    while (kp < k) kp <<= 1;
+    int64_t nch = (Np + kDotChunk - 1) / kDotChunk + 1;
+    int64_t vecs = ((iterations + 1 + 15) / 16) * 16;
+    int64_t b = 0;
+    b += Nn * (int64_t)(sizeof(NodeGeo) + 8 + 4 * 3 + 4 + 4 * 4);  // geometry, row pointers, tree, arrivals, sweep plan
+    b += L * (4 + c);                                                  // links
+    b += Np * (4 + 8 * 4 + 4);                                         // leaf maps, permittivities, self terms, geometry map
+    b += L * 8 + Nn * (int64_t)sizeof(fcg_tri64);                      // near-field list (bound: every link near) and tables
+    b += (int64_t)kp * Nn * (8 * 3 + 4 + 8);                           // matvec node work
+    b += (int64_t)k * Np * 8 * (5 + vecs);                             // Krylov vectors and basis
+    b += (int64_t)k * (iterations + 1) * nch * 8;                      // partial sums
+    return b + b / 10;
+}
+
+void *stream_create(int device) {
+    cudaStream_t s = NULL;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return NULL;
+    }
+    return (void *)s;
+}
+
+void stream_destroy(int device, void *stream) {
+    if (!stream) return;
+    cudaSetDevice(device);
+    cudaStreamSynchronize((cudaStream_t)stream);
+    cudaStreamDestroy((cudaStream_t)stream);
+}
 int problem_n_cond(const DeviceProblem *p) { return p ? (int)p->cond_cols.size() : 0; }
 SolveTimings problem_timings(const DeviceProblem *p) { return p ? p->timings : SolveTimings(); }
 
@@ -1438,6 +1547,7 @@ static int build_near_list(DeviceProblem *p) {
 }
 
 int problem_fill(DeviceProblem *p) {
+    AllocScope alloc_scope(p->stream);
     FCG_CK(cudaSetDevice(p->ctx->device));
     cudaStream_t s = p->stream;
     if (p->n_near < 0) {
@@ -1473,6 +1583,7 @@ int problem_fill(DeviceProblem *p) {
 }
 
 int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_coef) {
+    AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
     if (link_coef && p->L) {
@@ -1619,6 +1730,7 @@ static int matvec(DeviceProblem *p, const double *in, double *out, int k, const 
 }
 
 int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k) {
+    AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
     int r = matvec(p, d_q, d_v, k, NULL);
@@ -1629,6 +1741,7 @@ int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int 
 }
 
 int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k) {
+    AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
     double *dq = NULL, *dv = NULL;
@@ -1657,6 +1770,7 @@ int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k) {
 // ------------------------------------------------------------------ GMRES
 
 int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond) {
+    AllocScope alloc_scope(p->stream);
     if (n < 1 || !geom_of_cond) { set_error("need at least one geometry"); return FCG_GENERIC_ERROR; }
     int nc = p->n_cond_all;
     if (nc < 1) { set_error("model has no conductors"); return FCG_GENERIC_ERROR; }
@@ -1763,9 +1877,6 @@ static void free_solve_ws(DeviceProblem *p) {
     dfree(p->Vptr);
     dfree(p->Hptr);
     p->Vptr_cap = 0;
-    if (p->h_pin) cudaFreeHost(p->h_pin);
-    p->h_pin = NULL;
-    p->h_pin_cap = 0;
     p->gk = p->gS = p->gM = 0;
 }
 
@@ -1791,12 +1902,6 @@ static int ensure_solve_ws(DeviceProblem *p, int k, int S, int M) {
         p->gS = S;
         p->gM = M;
         p->x_k = k;
-        p->h_pin_cap = 3 * (size_t)S + 4;
-        if (cudaHostAlloc((void **)&p->h_pin, p->h_pin_cap * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
-            p->h_pin = NULL;
-            set_error("cannot allocate pinned host memory");
-            return FCG_OUT_OF_MEMORY;
-        }
     }
     return FCG_NORMAL_END;
 }
@@ -1862,6 +1967,7 @@ static double *basis_addr(DeviceProblem *p, int j) {
 }
 
 int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations) {
+    AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
     int r;
@@ -1905,6 +2011,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     // solve for the geometry's conductor r0 + r
     const int width = opt.rhs_width > 0 ? std::min(opt.rhs_width, kMaxK) : kMaxK;
     for (int r0 = 0; r0 < ks && status == FCG_NORMAL_END; r0 += width) {
+        if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
         const int k = std::min(width, ks - r0);
         const int S = G * k;
         std::vector<int64_t> sf(S, 0), sc(S, 0);
@@ -1971,15 +2078,15 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         FCG_CK(cudaMemsetAsync(p->g, 0, (size_t)S * (M + 2) * sizeof(double), s));
         FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
         k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
-                                        p->capped);
+                                        p->capped, p->n_active + M + 1);
         k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0);
         FCG_CK(cudaGetLastError());
         p->timings.launches += diag ? 8 : 7;
         // does any solve need an Arnoldi step?
-        bool any = false;
-        FCG_CK(cudaMemcpyAsync(p->h_pin, p->active, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+        int *pin = p->pin ? p->pin : p->pin_local;
+        FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         FCG_CK(cudaStreamSynchronize(s));
-        for (int i = 0; i < S; i++) any |= p->h_pin[i] != 0;
+        bool any = pin[0] > 0;
         for (int i = 0; any && i < M; i++) {
             if ((r = ensure_basis(p, i + 1)) || (r = ensure_partial(p, (size_t)k * (i + 1) * nch))) { status = r; break; }
             double *Vi = basis_addr(p, i), *Vn = basis_addr(p, i + 1);
@@ -1998,10 +2105,11 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, p->active, p->leaf_geom, Vn);
             FCG_CK(cudaGetLastError());
             p->timings.launches += 6;
-            FCG_CK(cudaMemcpyAsync(p->h_pin, p->n_active + i, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FCG_CK(cudaMemcpyAsync(pin, p->n_active + i, sizeof(int), cudaMemcpyDeviceToHost, s));
             FCG_CK(cudaStreamSynchronize(s));
             prof_collect(p);
-            any = p->h_pin[0] > 0;
+            any = pin[0] > 0;
+            if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
         }
         if (status != FCG_NORMAL_END) { free_batch(); break; }
         k_backsub<<<gs, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
@@ -2014,8 +2122,9 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         }
         FCG_CK(cudaGetLastError());
         p->timings.launches += nentry > 0 ? 5 : 3;
-        FCG_CK(cudaMemcpyAsync(p->h_pin, p->iters, S * sizeof(int), cudaMemcpyDeviceToHost, s));
-        FCG_CK(cudaMemcpyAsync(p->h_pin + S, p->capped, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+        std::vector<int> hb(2 * (size_t)S);
+        FCG_CK(cudaMemcpyAsync(hb.data(), p->iters, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+        FCG_CK(cudaMemcpyAsync(hb.data() + S, p->capped, S * sizeof(int), cudaMemcpyDeviceToHost, s));
         FCG_CK(cudaStreamSynchronize(s));
         prof_collect(p);
         float ms = 0;
@@ -2024,10 +2133,10 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         bool notconv = false;
         for (int g = 0; g < G; g++)
             for (int rr = 0; rr < k && r0 + rr < ncol[g]; rr++) {
-                int sidx = g * k + rr, it = p->h_pin[sidx] + 1;
+                int sidx = g * k + rr, it = hb[sidx] + 1;
                 h_iters[it_off[g] + r0 + rr] = it;
                 p->timings.iterations_max = std::max(p->timings.iterations_max, it);
-                notconv |= p->h_pin[S + sidx] != 0;
+                notconv |= hb[S + sidx] != 0;
             }
         free_batch();
         any_capped |= notconv;
@@ -2035,7 +2144,8 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     if (status == FCG_NORMAL_END && any_capped) status = FCG_NOT_CONVERGED;
     if (status == FCG_NORMAL_END || status == FCG_NOT_CONVERGED) {
         if (cap && cap_off[G] > 0 &&
-            cudaMemcpy(cap, d_cap, (size_t)cap_off[G] * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            (cudaMemcpyAsync(cap, d_cap, (size_t)cap_off[G] * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+             cudaStreamSynchronize(s) != cudaSuccess)) {
             set_error("copy of the capacitance matrix failed");
             status = FCG_DEVICE_ERROR;
         } else if (iterations) {
@@ -2051,7 +2161,8 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
 int problem_get_charges(DeviceProblem *p, double *charges) {
     if (!p->x) { set_error("no solve has run"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
-    FCG_CK(cudaMemcpy(charges, p->x, (size_t)p->x_k * p->Np * sizeof(double), cudaMemcpyDeviceToHost));
+    FCG_CK(cudaMemcpyAsync(charges, p->x, (size_t)p->x_k * p->Np * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+    FCG_CK(cudaStreamSynchronize(p->stream));
     return FCG_NORMAL_END;
 }
 

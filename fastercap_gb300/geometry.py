@@ -138,6 +138,23 @@ def crossing_8x8_slab() -> Crossing:
                     slab=(4.0, 1.0, 3.9, 60.0), name="crossing8x8_slab")
 
 
+def crossing_batch(seed: int = 0, n: int = 32, kmin: int = 2, kmax: int = 10) -> list:
+    """n random crossings drawn in order from one numpy default_rng(seed):
+    per geometry k ~ U{kmin..kmax}, length ~ U[10, 60], pitch ~ U[2, 4],
+    gap ~ U[1, 3] (um), vacuum (the uneven-batch workload: 32 crossings from
+    seed 0)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for g in range(n):
+        k = int(rng.integers(kmin, kmax + 1))
+        length = float(rng.uniform(10.0, 60.0))
+        pitch = float(rng.uniform(2.0, 4.0))
+        gap = float(rng.uniform(1.0, 3.0))
+        out.append(Crossing(k=k, length=round(length, 6), pitch=round(pitch, 6), gap=round(gap, 6),
+                            name="batch%d_%d" % (seed, g), meta={"seed": seed, "index": g}))
+    return out
+
+
 def random_crossing(seed: int, kmin: int = 2, kmax: int = 10) -> Crossing:
     """Random crossing drawn from numpy default_rng(seed), in this order:
     k ~ U{kmin..kmax}, length ~ U[10, 60], pitch ~ U[2, 4], gap ~ U[1, 3] (um),

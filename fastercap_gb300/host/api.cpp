@@ -13,6 +13,7 @@
 
 #include "../../include/fastercap_gb300.h"
 #include "../csrc/fcg_internal.hpp"
+#include "handles.hpp"
 #include "model.hpp"
 
 namespace fcg {
@@ -30,13 +31,6 @@ struct fcg_model {
     std::vector<int32_t> surf_ptr;
 };
 
-struct fcg_context {
-    fcg::DeviceContext *dev;
-};
-
-struct fcg_problem {
-    fcg::DeviceProblem *p;
-};
 
 static void finish_model(fcg_model *fm) {
     fcg::Model &m = fm->m;
@@ -273,6 +267,16 @@ int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap,
 }
 int fcg_problem_get_charges(fcg_problem *p, double *charges) {
     return (p && charges) ? fcg::problem_get_charges(p->p, charges) : FCG_GENERIC_ERROR;
+}
+
+int fcg_problem_cancel(fcg_problem *p) {
+    if (!p) return FCG_GENERIC_ERROR;
+    fcg::problem_cancel(p->p);
+    return FCG_NORMAL_END;
+}
+
+int64_t fcg_problem_estimate_bytes(const fcg_model_arrays *a, int precision, int rhs, int iterations) {
+    return a ? fcg::problem_estimate_bytes(*a, precision, rhs, iterations) : -1;
 }
 
 int fcg_problem_set_geometries(fcg_problem *p, int32_t n, const int32_t *geom) {

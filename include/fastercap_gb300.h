@@ -191,8 +191,21 @@ int fcg_problem_set_geometries(fcg_problem *p, int32_t n_geometries, const int32
  * (Solver/SolveCapacitance.cpp:2288-2574) and the Jacobi branch of
  * ComputePrecondVectFast (Solver/SolveCapacitance.cpp:3489-3526). */
 int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap, int *iterations);
-/* the charge vectors of the last solve, [n_cond][n_panels] */
+/* the charge vectors of the last batch of right-hand sides, [k][n_panels]
+ * (k = the conductors of that batch, all of them up to 32) */
 int fcg_problem_get_charges(fcg_problem *p, double *charges);
+
+/* Ask a running or later solve of p to stop: it returns FCG_USER_BREAK at its
+ * next Arnoldi step. Safe to call from any thread while the solve runs; the
+ * flag stays set for the problem. Replaces the reference's cancellation flag
+ * g_bFCContinue polled in the GMRES loop (Solver/SolveCapacitance.cpp:2365). */
+int fcg_problem_cancel(fcg_problem *p);
+
+/* Device bytes a problem of this model holds after a solve with `rhs`
+ * right-hand sides (min with 32) in at most `iterations` Arnoldi steps: the
+ * admission footprint used by the server below. No counterpart in the
+ * reference. */
+int64_t fcg_problem_estimate_bytes(const fcg_model_arrays *arrays, int precision, int rhs, int iterations);
 
 /* Launch and timing statistics of a problem. With profiling enabled, every
  * link-product launch is bracketed by CUDA events on the problem's stream. */
@@ -207,6 +220,63 @@ typedef struct {
 int fcg_problem_set_profiling(fcg_problem *p, int enable);
 int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *stats);
 int fcg_problem_reset_stats(fcg_problem *p);
+
+/* ------------------------------------------------------------ serving */
+
+/* Extraction server on one GPU: jobs (one model each, caller-owned arrays
+ * that must stay valid until the job's result is taken) are queued in
+ * arrival order and admitted while a slot is free and the sum of admitted
+ * footprints (fcg_problem_estimate_bytes) stays within the memory budget;
+ * a job larger than the budget runs alone. Every slot is a host thread with
+ * its own CUDA stream, so admitted jobs overlap on the device. A job's
+ * result does not depend on what else runs (no state is shared between
+ * jobs). No counterpart in the reference (one solve per process). */
+typedef struct {
+    int slots;              /* concurrent jobs (0: 4) */
+    int64_t memory_budget;  /* bytes of admitted footprints (0: 80% of free device memory) */
+    int iterations_hint;    /* Arnoldi steps assumed by the footprint (0: 64) */
+} fcg_server_config;
+
+#define FCG_JOB_QUEUED 0
+#define FCG_JOB_RUNNING 1
+#define FCG_JOB_DONE 2      /* finished; status in fcg_job_info */
+#define FCG_JOB_CANCELLED 3
+
+typedef struct {
+    int state;              /* FCG_JOB_* */
+    int status;             /* FC_* status of the solve (FCG_USER_BREAK when cancelled) */
+    int n_cond;             /* capacitance matrix is n_cond x n_cond */
+    int iterations_max;
+    int slot;               /* slot that ran the job (-1 if it never ran) */
+    int64_t footprint_bytes;
+    int64_t device_bytes;   /* bytes the problem actually held */
+    double queue_ms;        /* submit -> admission (host clock) */
+    double run_ms;          /* admission -> result (host clock) */
+    double fill_ms, solve_ms;  /* device time of fill and solve (CUDA events) */
+} fcg_job_info;
+
+typedef struct {
+    int slots, running, queued;
+    int max_running;        /* most jobs seen running at once */
+    int64_t budget, in_use, peak_in_use;
+    int64_t submitted, completed;
+} fcg_server_stats;
+
+typedef struct fcg_server fcg_server;
+int fcg_server_create(fcg_context *ctx, const fcg_server_config *cfg, fcg_server **out);
+/* waits for running jobs; queued jobs are cancelled */
+void fcg_server_destroy(fcg_server *s);
+int fcg_server_submit(fcg_server *s, const fcg_model_arrays *arrays, int precision, const fcg_solve_options *opt,
+                      int64_t *job);
+/* state and timings without waiting */
+int fcg_server_poll(fcg_server *s, int64_t job, fcg_job_info *info);
+/* wait until the job is done or cancelled, copy its matrix (n_cond^2 values)
+ * and iterations (n_cond) if not NULL, and release the job; returns the job's
+ * status */
+int fcg_server_result(fcg_server *s, int64_t job, double *cap, int *iterations, fcg_job_info *info);
+/* a queued job is dropped; a running one stops at its next Arnoldi step */
+int fcg_server_cancel(fcg_server *s, int64_t job);
+int fcg_server_get_stats(fcg_server *s, fcg_server_stats *stats);
 
 /* ------------------------------------------------------------- driver */
 

@@ -1,0 +1,116 @@
+"""Serving (fcg_server_*): continuous admission of extraction jobs on one GPU.
+
+Every job's capacitance matrix is the same alone and in a mix of concurrent
+jobs (bit for bit: jobs share no state and every kernel sums in a fixed
+order), and within the stated tolerance of the oracle's FP64 result (FP64
+path 1e-6, mixed path 1e-3 per entry). Admission respects the memory budget
+(a budget below every footprint runs one job at a time), queued jobs can be
+cancelled, and a cancelled solve returns FCG_USER_BREAK.
+"""
+
+import numpy as np
+import pytest
+
+import fastercap_gb300 as fc
+from fastercap_gb300 import geometry as geo
+from pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = fc.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def models(tmp_path_factory):
+    d = tmp_path_factory.mktemp("srv")
+    ms = []
+    for r in range(6):
+        path = d / ("req%d.txt" % r)
+        geo.random_crossing(r, kmin=2, kmax=4).write(str(path))
+        ms.append(fc.Model.build(str(path), mesh_eps=0.02))
+    return ms
+
+
+def oracle_cap(m, tol):
+    o = Oracle(m.arrays)
+    o.fill()
+    return o.solve(tol, 1)[0]
+
+
+@pytest.mark.parametrize("precision", [fc.PREC_FP64, fc.PREC_MIXED])
+def test_same_alone_and_in_mix(ctx, models, precision):
+    with ctx.server(slots=4) as srv:
+        alone = []
+        for m in models:
+            alone.append(srv.submit(m, precision, tol=1e-4).result())
+        jobs = [srv.submit(m, precision, tol=1e-4) for m in models + models]
+        mixed = [j.result() for j in jobs]
+        st = srv.stats()
+    assert st["completed"] == 3 * len(models)
+    for i, (cap, it) in enumerate(mixed):
+        ca, ia = alone[i % len(models)]
+        np.testing.assert_array_equal(cap, ca)
+        np.testing.assert_array_equal(it, ia)
+    tol = 1e-6 if precision == fc.PREC_FP64 else 1e-3
+    for m, (cap, _) in zip(models, alone):
+        oc = oracle_cap(m, 1e-4)
+        assert np.max(np.abs(cap - oc) / np.abs(oc)) < tol
+
+
+def test_jobs_overlap_with_room(ctx, models):
+    with ctx.server(slots=4) as srv:
+        jobs = [srv.submit(m, fc.PREC_MIXED, tol=1e-4) for m in models * 3]
+        for j in jobs:
+            j.result()
+        st = srv.stats()
+    assert st["max_running"] >= 2
+    assert st["in_use"] == 0 and st["running"] == 0
+
+
+def test_budget_below_footprint_runs_one_at_a_time(ctx, models):
+    with ctx.server(slots=4, memory_budget=1) as srv:
+        jobs = [srv.submit(m, fc.PREC_MIXED, tol=1e-4) for m in models]
+        infos = []
+        for j in jobs:
+            j.result()
+            infos.append(j.info)
+        st = srv.stats()
+    assert st["max_running"] == 1
+    assert all(i["status"] == fc.NORMAL_END for i in infos)
+    # footprints cover what the problems held
+    assert all(i["device_bytes"] <= i["footprint_bytes"] for i in infos)
+
+
+def test_cancel_queued_job(ctx, models):
+    with ctx.server(slots=1, memory_budget=1) as srv:
+        jobs = [srv.submit(m, fc.PREC_FP64, tol=1e-6) for m in models]
+        last = jobs[-1]
+        last.cancel()
+        for j in jobs[:-1]:
+            j.result()
+        with pytest.raises(fc.FCError) as e:
+            last.result()
+        assert e.value.code == fc.USER_BREAK
+        assert last.info["state"] == fc.JOB_CANCELLED
+
+
+def test_problem_cancel(ctx, models):
+    p = ctx.problem(models[0], fc.PREC_FP64)
+    p.fill()
+    p.cancel()
+    with pytest.raises(fc.FCError) as e:
+        p.solve(tol=1e-6)
+    assert e.value.code == fc.USER_BREAK
+
+
+def test_estimate_covers_solve(ctx, models):
+    for m in models[:3]:
+        p = ctx.problem(m, fc.PREC_MIXED)
+        p.fill()
+        _, it = p.solve(tol=1e-4)
+        assert p.device_bytes <= fc.estimate_bytes(m, fc.PREC_MIXED, iterations=int(it.max()))
