@@ -422,6 +422,174 @@ def run_gb300_multi(args, rank, world, local_rank):
         torch.distributed.destroy_process_group()
 
 
+# Serving: request r is random_crossing(r) with k in 2..12 (numpy
+# default_rng(r)); arrivals are Poisson at rate lam with inter-arrival times
+# from default_rng(10000 + lam). Host models are built before the clock
+# starts (the solve is measured from an uploaded host model).
+SERVING = {"mesh_eps": 1e-3, "tol": 1e-4, "kmin": 2, "kmax": 12}
+
+
+def build_requests(n: int):
+    import fastercap_gb300 as fc
+    from fastercap_gb300 import geometry as geo
+    from concurrent.futures import ThreadPoolExecutor
+    tmp = tempfile.mkdtemp()
+
+    def one(r):
+        path = os.path.join(tmp, "req%d.txt" % r)
+        geo.random_crossing(r, SERVING["kmin"], SERVING["kmax"]).write(path)
+        m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"])
+        os.unlink(path)
+        return m
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:  # the native builder releases the GIL
+        models = list(ex.map(one, range(n)))
+    os.rmdir(tmp)
+    return models, time.perf_counter() - t0
+
+
+def serve_pass(srv, models, precision, lam, tol):
+    """Submit every request at its arrival time; returns per-request
+    (latency ms, completion s, C, iterations, info)."""
+    arr = np.cumsum(np.random.default_rng(10000 + int(lam)).exponential(1.0 / lam, len(models)))
+    t0 = time.perf_counter()
+    sub = []
+    for r, m in enumerate(models):
+        dt = t0 + arr[r] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        ts = time.perf_counter()
+        sub.append((ts, srv.submit(m, precision, tol=tol)))
+    out = []
+    for ts, j in sub:
+        cap, it = j.result()
+        lat = j.info["queue_ms"] + j.info["run_ms"]
+        out.append((lat, ts - t0 + lat / 1000.0, cap, it, j.info))
+    return out
+
+
+def run_serving(args, rank, world, local_rank):
+    import torch
+    import fastercap_gb300 as fc
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    torch.cuda.set_device(local_rank)
+    rates = [float(x) for x in args.rates.split(",")]
+    models, build_s = build_requests(args.requests)
+    ctx = fc.Context(local_rank)
+    tol = SERVING["tol"]
+    res = {}
+    caps = {}
+    launches = 0
+    clk_summary = None
+    with ctx.server(slots=args.slots) as srv:
+        # warm the pool and the kernels
+        for j in [srv.submit(m, fc.PREC_MIXED, tol=tol) for m in models[:4]]:
+            j.result()
+        for prec, name in ((fc.PREC_MIXED, "mixed"), (fc.PREC_FP64, "fp64")):
+            res[name] = {}
+            for lam in rates:
+                if name == "mixed" and lam == rates[-1]:
+                    with ClockSampler(local_rank) as clk:
+                        out = serve_pass(srv, models, prec, lam, tol)
+                    clk_summary = clk.summary()
+                else:
+                    out = serve_pass(srv, models, prec, lam, tol)
+                lat = np.array([o[0] for o in out])
+                span = max(o[1] for o in out)
+                res[name][str(int(lam))] = {"solves_s": len(out) / span, "p50_ms": float(np.percentile(lat, 50)),
+                                            "p99_ms": float(np.percentile(lat, 99)),
+                                            "mean_queue_ms": float(np.mean([o[4]["queue_ms"] for o in out]))}
+                caps[(name, lam)] = [o[2] for o in out]
+                if name == "mixed" and lam == rates[-1]:
+                    launches = int(sum(o[4]["kernel_launches"] for o in out))
+        st = srv.stats()
+    top = str(int(rates[-1]))
+    err = max(float(np.max(np.abs(a - b) / np.abs(b))) for a, b in zip(caps[("mixed", rates[-1])], caps[("fp64", rates[-1])]))
+    # the same request gives the same matrix at every rate (alone or in any mix)
+    same = all(np.array_equal(a, b) for lam in rates for a, b in zip(caps[("mixed", lam)], caps[("mixed", rates[0])]))
+    h2d = int(np.mean([model_bytes(m) for m in models]))
+    mixed_top = res["mixed"][top]
+    result = {
+        "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(models),
+        "warmup": 4, "ms_per_step": 1000.0 / mixed_top["solves_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
+        "p50_ms": mixed_top["p50_ms"], "p99_ms": mixed_top["p99_ms"],
+        "config": {"workload": "serving", "requests": len(models), "rates_req_s": rates, "slots": args.slots,
+                   "request": "random k x k crossing, k in 2..12, seed = request id", "link_eps": SERVING["mesh_eps"],
+                   "gmres_tol": tol, "precond": "jacobi",
+                   "panels_min_max_mean": [min(m.n_panels for m in models), max(m.n_panels for m in models),
+                                           int(np.mean([m.n_panels for m in models]))],
+                   "links_mean": int(np.mean([m.n_links for m in models])), "host_build_s": round(build_s, 2),
+                   "step": "one request (upload + fill + GMRES + C), value at the highest rate",
+                   "l2": "each request's links exceed L2 on average; no flush"},
+        "serving": res,
+        "mixed_vs_fp64": {"speedup_at_top_rate": mixed_top["solves_s"] / res["fp64"][top]["solves_s"],
+                          "max_rel_c_err": err},
+        "same_result_every_rate": bool(same),
+        "server": {"max_running": st["max_running"], "peak_in_use_bytes": st["peak_in_use"], "budget_bytes": st["budget"]},
+        "e2e": {"value": mixed_top["solves_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(np.mean([c.nbytes for c in caps[("mixed", rates[-1])]]))},
+        "gpu_launches": launches,
+        "clocks": clk_summary,
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        n = 0
+        for m in models:
+            o = Oracle(m.arrays, threads=cores)
+            o.fill()
+            o.solve(tol, 1)
+            n += 1
+            if time.perf_counter() - t0 > 20.0:
+                break
+        dt = time.perf_counter() - t0
+        result["cpu_baseline"] = {"value": n / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+                                  "sample": "the first %d requests, solved one after another" % n}
+    print(json.dumps(result), flush=True)
+    ctx.close()
+
+
+def run_reference_serving(args, rank, world):
+    """CPU arm for serving: the oracle port on every host core solves the
+    requests one after another (the first steps + warmup requests)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    models, build_s = build_requests(args.warmup + args.steps)
+    cores = os.cpu_count() or 1
+    times = []
+    for i, m in enumerate(models):
+        o = Oracle(m.arrays, threads=cores)
+        t0 = time.perf_counter()
+        o.fill()
+        o.solve(SERVING["tol"], 1)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "p50_ms": 1000 * float(np.percentile(times, 50)), "p99_ms": 1000 * float(np.percentile(times, 99)),
+        "config": {"workload": "serving", "requests": args.steps, "link_eps": SERVING["mesh_eps"],
+                   "gmres_tol": SERVING["tol"], "precond": "jacobi"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": "requests %d..%d solved one after another (no arrival process)"
+                                   % (args.warmup, args.warmup + args.steps - 1)},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def time_steps(prob, stream, n, tol, flush_buf, torch):
     """Per-step device times (ms) of fill + solve, L2 flushed between steps."""
     s = torch.cuda.ExternalStream(stream)
@@ -565,7 +733,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sphere_327680", choices=sorted(WORKLOADS) + sorted(MULTI))
+    ap.add_argument("--workload", default="sphere_327680", choices=sorted(WORKLOADS) + sorted(MULTI) + ["serving"])
+    ap.add_argument("--requests", type=int, default=200, help="serving: number of requests")
+    ap.add_argument("--rates", default="50,200,500", help="serving: arrival rates (req/s), comma separated")
+    ap.add_argument("--slots", type=int, default=4, help="serving: concurrent jobs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -573,6 +744,12 @@ def main():
         args.warmup = 3
     rank, world, local_rank = dist_env()
     multi = args.workload in MULTI
+    if args.workload == "serving":
+        if args.impl == "reference":
+            run_reference_serving(args, rank, world)
+        elif rank == 0:
+            run_serving(args, rank, world, local_rank)
+        return
     if args.impl == "reference":
         (run_reference_multi if multi else run_reference)(args, rank, world)
     else:

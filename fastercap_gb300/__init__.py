@@ -92,7 +92,8 @@ class ServerConfig(C.Structure):
 class JobInfo(C.Structure):
     _fields_ = [("state", C.c_int), ("status", C.c_int), ("n_cond", C.c_int), ("iterations_max", C.c_int),
                 ("slot", C.c_int), ("footprint_bytes", C.c_int64), ("device_bytes", C.c_int64),
-                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("fill_ms", C.c_double), ("solve_ms", C.c_double)]
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("fill_ms", C.c_double), ("solve_ms", C.c_double),
+                ("kernel_launches", C.c_int64)]
 
 
 class ServerStats(C.Structure):

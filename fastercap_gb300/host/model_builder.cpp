@@ -107,8 +107,14 @@ struct Builder {
     }
 
     // ---------------------------------------------------------------- files
+    // directory relative names resolve against (the input file's); the
+    // process working directory is never changed, so builds may run on
+    // several threads at once
+    std::string base_dir;
+
     int load_file(const std::string &name, InFile *&out) {
-        FILE *f = fopen(name.c_str(), "rb");
+        std::string full = (!name.empty() && name[0] != '/') ? base_dir + name : name;
+        FILE *f = fopen(full.c_str(), "rb");
         if (!f) { err = "cannot open file '" + name + "'"; return FC_CANNOT_OPEN_FILE; }
         files.push_back(InFile());
         InFile &F = files.back();
@@ -910,11 +916,8 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
         }
         B.files.clear();
     }
-    char cwd[4096];
-    bool have_cwd = getcwd(cwd, sizeof cwd) != NULL;
-    if (!dir.empty() && chdir(dir.c_str()) != 0) { err = "cannot enter directory " + dir; return FC_FILE_ERROR; }
+    B.base_dir = dir;
     int ret = B.parse_file(base, NULL, false, d3(0, 0, 0), 1.0, "", 0.0, d3(0, 0, 0));
-    if (!dir.empty() && have_cwd && chdir(cwd) != 0) { /* keep going: the model is in memory */ }
     if (ret != FC_NORMAL_END) { err = B.err; return ret; }
     if (B.order.empty()) { err = "no panels found in the input file"; return FC_FILE_ERROR; }
 

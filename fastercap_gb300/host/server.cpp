@@ -45,6 +45,7 @@ struct Job {
     double t_submit = 0, t_start = 0, t_end = 0;
     double fill_ms = 0, solve_ms = 0;
     int iterations_max = 0;
+    int64_t launches = 0;
     bool cancel = false;
     fcg::DeviceProblem *prob = nullptr;  // while running (guarded by the server mutex)
 };
@@ -92,6 +93,7 @@ static void run_job(fcg_server *s, Job *j, void *stream) {
         j->fill_ms = t.fill_ms;
         j->solve_ms = t.solve_ms;
         j->iterations_max = t.iterations_max;
+        j->launches = t.launches;
         j->device_bytes = fcg::problem_device_bytes(p);
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -150,6 +152,7 @@ static void fill_info(const Job *j, fcg_job_info *info) {
     info->run_ms = j->t_start > 0 ? end - j->t_start : 0.0;
     info->fill_ms = j->fill_ms;
     info->solve_ms = j->solve_ms;
+    info->kernel_launches = j->launches;
 }
 
 extern "C" {

@@ -253,6 +253,7 @@ typedef struct {
     double queue_ms;        /* submit -> admission (host clock) */
     double run_ms;          /* admission -> result (host clock) */
     double fill_ms, solve_ms;  /* device time of fill and solve (CUDA events) */
+    int64_t kernel_launches;   /* kernels the library launched for the job */
 } fcg_job_info;
 
 typedef struct {
