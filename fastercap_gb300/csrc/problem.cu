@@ -159,6 +159,8 @@ struct DeviceProblem {
     float2 *Pf2 = NULL;
     int *arrive = NULL;  // per-node arrival counters of the up-sweep (zero between products)
     int spmv_lanes = 32;  // lanes per destination node in the link product (8, 16 or 32)
+    int32_t *row_split = NULL;  // multi-right-hand-side link product: CTA b owns rows [row_split[b], row_split[b+1])
+    int n_row_split = 0;
 
     // solve geometries (independent models concatenated into one problem)
     int n_geom = 0;
@@ -538,20 +540,26 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint
 // compensation. The row sum leaves the kernel as the unevaluated pair
 // (sum, compensation), combined in FP64 by the down-sweep, so that no FP64
 // instruction runs in this kernel.
+// Compensated FP32 sum: the value is s + c.
 struct KSum {
     float s, c;
 };
+// Neumaier's update, used where two partial sums meet (lane reductions)
 __device__ __forceinline__ void kadd(KSum &a, float x) {
     float t = a.s + x;
     if (fabsf(a.s) >= fabsf(x)) a.c += (a.s - t) + x;
     else a.c += (x - t) + a.s;
     a.s = t;
 }
+// Kahan's update with the product folded in: y = c*q + correction is one
+// fused multiply-add (the product's rounding is of the order of the FP32
+// coefficient's own), then t = s + y and the new correction is the part of y
+// that t lost. Four instructions per link and right-hand side.
 __device__ __forceinline__ void kmul_add(KSum &a, float c, float q) {
-    float p = c * q;
-    float e = fmaf(c, q, -p);
-    kadd(a, p);
-    a.c += e;
+    float y = fmaf(c, q, a.c);
+    float t = a.s + y;
+    a.c = y - (t - a.s);
+    a.s = t;
 }
 
 template <int K> __device__ __forceinline__ void load_q(const float *__restrict__ Q, uint32_t j, float *q) {
@@ -568,8 +576,8 @@ template <int K> __device__ __forceinline__ void load_q(const float *__restrict_
     }
 }
 
-// Link product, mixed: FP32 coefficients and charges streamed, exact products
-// and compensated FP32 sums; SW lanes per destination node (32/SW nodes per
+// Link product, mixed: FP32 coefficients and charges streamed, compensated
+// FP32 sums; SW lanes per destination node (32/SW nodes per
 // warp in flight), four independent links per lane.
 template <int K, int SW>
 __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
@@ -626,50 +634,71 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
     }
 }
 
-// Link product for K >= 4 right-hand sides, mixed: K/4 lanes share a link,
-// each lane owns four right-hand sides (one 16-byte charge load per link), a
-// warp advances 128/K links per step; the link slots are reduced at the end.
+// Reduction of the link slots of a multi-right-hand-side warp: lane
+// li * LPL + ri holds slot li (of LPW) for right-hand-side group ri; after
+// the tree, slot 0 holds the sum of all slots (fixed order).
+template <int LPL, int LPW> __device__ __forceinline__ void slot_reduce(KSum &a, int lane, int li) {
+#pragma unroll
+    for (int o = 1; o < LPW; o <<= 1) {
+        int from = lane + o * LPL;
+        float os = __shfl_sync(0xffffffffu, a.s, from < 32 ? from : lane);
+        float oc = __shfl_sync(0xffffffffu, a.c, from < 32 ? from : lane);
+        if ((li & (2 * o - 1)) == 0 && li + o < LPW) {
+            a.c += oc;
+            kadd(a, os);
+        }
+    }
+}
+template <int LPL, int LPW> __device__ __forceinline__ double slot_reduce64(double a, int lane, int li) {
+#pragma unroll
+    for (int o = 1; o < LPW; o <<= 1) {
+        int from = lane + o * LPL;
+        double oa = __shfl_sync(0xffffffffu, a, from < 32 ? from : lane);
+        if ((li & (2 * o - 1)) == 0 && li + o < LPW) a += oa;
+    }
+    return a;
+}
+
+// Link product for K = 4, 8, ..., 32 right-hand sides, mixed: K/4 lanes
+// share a link and each owns four right-hand sides (one 16-byte charge
+// gather per link); a warp has 32/(K/4) link slots (lanes beyond them idle).
+// CTA b owns the contiguous rows [row_split[b], row_split[b+1]) (split for
+// equal link counts), its warps take every eighth row: consecutive rows
+// share most of their sources, so the gathers hit L1.
 template <int K>
-__global__ void k_spmv32_multi(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                               const float *__restrict__ coef, const float *__restrict__ Q, float2 *__restrict__ P) {
-    const int LPL = K / 4, LPW = 32 / LPL;
+__global__ void __launch_bounds__(256) k_spmv32_multi(const int32_t *__restrict__ row_split, const int64_t *__restrict__ ptr,
+                                                      const uint32_t *__restrict__ src, const float *__restrict__ coef,
+                                                      const float *__restrict__ Q, float2 *__restrict__ P) {
+    constexpr int LPL = K / 4, LPW = 32 / LPL;
     int lane = threadIdx.x & 31, li = lane / LPL, ri = lane % LPL;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    bool slot_ok = li < LPW;
     const float4 *Q4 = reinterpret_cast<const float4 *>(Q);
-    for (int64_t row = warp; row < Nn; row += nwarps) {
+    int r0 = row_split[blockIdx.x], r1 = row_split[blockIdx.x + 1];
+    for (int row = r0 + (threadIdx.x >> 5); row < r1; row += 8) {
         KSum acc[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) { acc[r].s = 0.f; acc[r].c = 0.f; }
         int s = (int)ptr[row], e = (int)ptr[row + 1];
         int l = s + li;
-        for (; l + LPW < e; l += 2 * LPW) {
-            float c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
-            uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
-            float4 q0 = Q4[(int64_t)j0 * LPL + ri], q1 = Q4[(int64_t)j1 * LPL + ri];
-            kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
-            kmul_add(acc[0], c1, q1.x); kmul_add(acc[1], c1, q1.y); kmul_add(acc[2], c1, q1.z); kmul_add(acc[3], c1, q1.w);
-        }
-        if (l < e) {
-            float c0 = __ldcs(&coef[l]);
-            uint32_t j0 = __ldcs(&src[l]) & kSrcMask;
-            float4 q0 = Q4[(int64_t)j0 * LPL + ri];
-            kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
-        }
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            KSum a = acc[r];
-#pragma unroll
-            for (int o = 16; o >= LPL; o >>= 1) {
-                float os = __shfl_xor_sync(0xffffffffu, a.s, o);
-                float oc = __shfl_xor_sync(0xffffffffu, a.c, o);
-                a.c += oc;
-                kadd(a, os);
+        if (slot_ok) {
+            for (; l + LPW < e; l += 2 * LPW) {
+                float c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
+                uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
+                float4 q0 = Q4[(int64_t)j0 * LPL + ri], q1 = Q4[(int64_t)j1 * LPL + ri];
+                kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
+                kmul_add(acc[0], c1, q1.x); kmul_add(acc[1], c1, q1.y); kmul_add(acc[2], c1, q1.z); kmul_add(acc[3], c1, q1.w);
             }
-            acc[r] = a;
+            if (l < e) {
+                float c0 = __ldcs(&coef[l]);
+                uint32_t j0 = __ldcs(&src[l]) & kSrcMask;
+                float4 q0 = Q4[(int64_t)j0 * LPL + ri];
+                kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
+            }
         }
+#pragma unroll
+        for (int r = 0; r < 4; r++) slot_reduce<LPL, LPW>(acc[r], lane, li);
         if (li == 0) {
-            float4 *out = reinterpret_cast<float4 *>(P + row * K + 4 * ri);
+            float4 *out = reinterpret_cast<float4 *>(P + (int64_t)row * K + 4 * ri);
             out[0] = make_float4(acc[0].s, acc[0].c, acc[1].s, acc[1].c);
             out[1] = make_float4(acc[2].s, acc[2].c, acc[3].s, acc[3].c);
         }
@@ -678,35 +707,35 @@ __global__ void k_spmv32_multi(int64_t Nn, const int64_t *__restrict__ ptr, cons
 
 // FP64 counterpart: K/2 lanes share a link, each lane owns two right-hand sides.
 template <int K>
-__global__ void k_spmv64_multi(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                               const double *__restrict__ coef, const double *__restrict__ Q, double *__restrict__ P) {
-    const int LPL = K / 2, LPW = 32 / LPL;
+__global__ void __launch_bounds__(256) k_spmv64_multi(const int32_t *__restrict__ row_split, const int64_t *__restrict__ ptr,
+                                                      const uint32_t *__restrict__ src, const double *__restrict__ coef,
+                                                      const double *__restrict__ Q, double *__restrict__ P) {
+    constexpr int LPL = K / 2, LPW = 32 / LPL;
     int lane = threadIdx.x & 31, li = lane / LPL, ri = lane % LPL;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    bool slot_ok = li < LPW;
     const double2 *Q2 = reinterpret_cast<const double2 *>(Q);
-    for (int64_t row = warp; row < Nn; row += nwarps) {
+    int r0 = row_split[blockIdx.x], r1 = row_split[blockIdx.x + 1];
+    for (int row = r0 + (threadIdx.x >> 5); row < r1; row += 8) {
         double a0 = 0.0, a1 = 0.0;
         int s = (int)ptr[row], e = (int)ptr[row + 1];
         int l = s + li;
-        for (; l + LPW < e; l += 2 * LPW) {
-            double c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
-            uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
-            double2 q0 = Q2[(int64_t)j0 * LPL + ri], q1 = Q2[(int64_t)j1 * LPL + ri];
-            a0 += c0 * q0.x; a1 += c0 * q0.y;
-            a0 += c1 * q1.x; a1 += c1 * q1.y;
+        if (slot_ok) {
+            for (; l + LPW < e; l += 2 * LPW) {
+                double c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
+                uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
+                double2 q0 = Q2[(int64_t)j0 * LPL + ri], q1 = Q2[(int64_t)j1 * LPL + ri];
+                a0 += c0 * q0.x; a1 += c0 * q0.y;
+                a0 += c1 * q1.x; a1 += c1 * q1.y;
+            }
+            if (l < e) {
+                double c0 = __ldcs(&coef[l]);
+                double2 q0 = Q2[(int64_t)(__ldcs(&src[l]) & kSrcMask) * LPL + ri];
+                a0 += c0 * q0.x; a1 += c0 * q0.y;
+            }
         }
-        if (l < e) {
-            double c0 = __ldcs(&coef[l]);
-            double2 q0 = Q2[(int64_t)(__ldcs(&src[l]) & kSrcMask) * LPL + ri];
-            a0 += c0 * q0.x; a1 += c0 * q0.y;
-        }
-#pragma unroll
-        for (int o = 16; o >= LPL; o >>= 1) {
-            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-        }
-        if (li == 0) reinterpret_cast<double2 *>(P + row * K)[ri] = make_double2(a0, a1);
+        a0 = slot_reduce64<LPL, LPW>(a0, lane, li);
+        a1 = slot_reduce64<LPL, LPW>(a1, lane, li);
+        if (li == 0) reinterpret_cast<double2 *>(P + (int64_t)row * K)[ri] = make_double2(a0, a1);
     }
 }
 
@@ -1355,6 +1384,22 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
     FCG_TRY(build_plan(p, a, parent, lab, s));
     FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
+    {
+        // contiguous row ranges of about equal work (links + 8 per row) for
+        // the multi-right-hand-side link product, at least 64 rows each
+        int64_t nb = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx.sm_count * 32, (Nn + 63) / 64));
+        std::vector<int32_t> split(nb + 1, 0);
+        double total = (double)L + 8.0 * (double)Nn;
+        int64_t row = 0;
+        for (int64_t b = 1; b < nb; b++) {
+            double target = total * (double)b / (double)nb;
+            while (row < Nn && (double)p->h_ptr_dev[row] + 8.0 * (double)row < target) row++;
+            split[b] = (int32_t)row;
+        }
+        split[nb] = (int32_t)Nn;
+        p->n_row_split = (int)nb;
+        FCG_TRY(upload(&p->row_split, split.data(), split.size(), p->bytes, s));
+    }
     // lanes per node in the link product: about four links per lane per pass
     {
         double avg = (double)a.n_links / (double)Nn;
@@ -1394,7 +1439,7 @@ void problem_destroy(DeviceProblem *p) {
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
     dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
-    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->arrive);
+    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->arrive); dfree(p->row_split);
     free_solve_ws(p);
     dfree(p->partial);
     dfree(p->leaf_geom); dfree(p->ch_start); dfree(p->ch_len); dfree(p->ch_geom); dfree(p->g_ch_first); dfree(p->g_ch_count);
@@ -1610,11 +1655,9 @@ int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_c
     return FCG_NORMAL_END;
 }
 
-static int kpad(int k) {
-    int kp = 1;
-    while (kp < k) kp <<= 1;
-    return kp;
-}
+// node-work columns for k right-hand sides: 1, 2, else a multiple of four
+// (the multi-right-hand-side link product moves four per 16-byte gather)
+static int kpad(int k) { return k <= 2 ? k : (k + 3) / 4 * 4; }
 
 static int ensure_matvec_ws(DeviceProblem *p, int kp) {
     if (p->kcap >= kp) return FCG_NORMAL_END;
@@ -1630,6 +1673,11 @@ static int ensure_matvec_ws(DeviceProblem *p, int kp) {
     } else {
         if ((r = dalloc(&p->Pd, n, p->bytes))) return r;
     }
+    // padding columns (right-hand sides k..kp-1) are read by the link product
+    // but never written by the up-sweep: start them at zero; afterwards they
+    // only ever hold finite charges, and columns never mix
+    FCG_CK(cudaMemsetAsync(p->Qd, 0, n * sizeof(double), p->stream));
+    if (p->Qf) FCG_CK(cudaMemsetAsync(p->Qf, 0, n * sizeof(float), p->stream));
     p->kcap = kp;
     return FCG_NORMAL_END;
 }
@@ -1651,11 +1699,6 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     const SweepPlan &pl = p->plan;
     int64_t Np = p->Np;
     size_t n = (size_t)p->Nn * kp;
-    if (kp != k) {
-        // padded right-hand sides carry zero charges
-        FCG_CK(cudaMemsetAsync(w.Qd, 0, n * sizeof(double), s));
-        if (mixed) FCG_CK(cudaMemsetAsync(w.Qf, 0, n * sizeof(float), s));
-    }
     if (mixed) k_up<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
     else k_up<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
     FCG_CK(cudaGetLastError());
@@ -1683,27 +1726,40 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
             else k_spmv64<KK, 32><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd);     \
         }                                                                                                             \
     } while (0)
-        int mgrid = (int)std::min<int64_t>((p->Nn + 7) / 8, (int64_t)p->ctx->sm_count * 32);
+        const int mgrid = p->n_row_split;
+        const int32_t *rs = p->row_split;
+#define FCG_MULTI32(KK) k_spmv32_multi<KK><<<mgrid, 256, 0, s>>>(rs, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2)
+#define FCG_MULTI64(KK) k_spmv64_multi<KK><<<mgrid, 256, 0, s>>>(rs, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd)
         if (kp == 1) {
             FCG_SPMV(1);
         } else if (mixed && kp == 2) {
             FCG_SPMV(2);
         } else if (mixed) {
             switch (kp) {
-            case 4: k_spmv32_multi<4><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            case 8: k_spmv32_multi<8><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            case 16: k_spmv32_multi<16><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
-            default: k_spmv32_multi<32><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef32, w.Qf, w.Pf2); break;
+            case 4: FCG_MULTI32(4); break;
+            case 8: FCG_MULTI32(8); break;
+            case 12: FCG_MULTI32(12); break;
+            case 16: FCG_MULTI32(16); break;
+            case 20: FCG_MULTI32(20); break;
+            case 24: FCG_MULTI32(24); break;
+            case 28: FCG_MULTI32(28); break;
+            default: FCG_MULTI32(32); break;
             }
         } else {
             switch (kp) {
-            case 2: k_spmv64_multi<2><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 4: k_spmv64_multi<4><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 8: k_spmv64_multi<8><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            case 16: k_spmv64_multi<16><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
-            default: k_spmv64_multi<32><<<mgrid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->coef64, w.Qd, w.Pd); break;
+            case 2: FCG_MULTI64(2); break;
+            case 4: FCG_MULTI64(4); break;
+            case 8: FCG_MULTI64(8); break;
+            case 12: FCG_MULTI64(12); break;
+            case 16: FCG_MULTI64(16); break;
+            case 20: FCG_MULTI64(20); break;
+            case 24: FCG_MULTI64(24); break;
+            case 28: FCG_MULTI64(28); break;
+            default: FCG_MULTI64(32); break;
             }
         }
+#undef FCG_MULTI32
+#undef FCG_MULTI64
 #undef FCG_SPMV
         prof_end(p);
         FCG_CK(cudaGetLastError());
