@@ -352,7 +352,15 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
                             unsigned *status) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
         const NodeGeo &g = geo[leaf_node[j]];
-        double val = fcg_self_potential(g.type, g.c, g.v, g.area, eb[j], ea[j]);
+        double val;
+        if (g.type & FCG_IS_DIEL) {
+            val = fcg_self_potential(g.type, g.c, g.v, g.area, eb[j], ea[j]);
+        } else {
+            // collocation at the own centroid, in the reduced-cost form
+            fcg_tri64 t;
+            fcg_tri64_make(g.v, t);
+            val = fcg_potential_opt_fast(fcg_widen(g.c), g.v, t) / FCG_FOUR_PI_TIMES_E0;
+        }
         if (!isfinite(val) || val == 0.0) atomicOr(status, 2u);
         self[j] = val;
     }
