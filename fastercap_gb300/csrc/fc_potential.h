@@ -481,6 +481,23 @@ FCG_HD float fcg_rsqrtf(float x) {
 //
 // Distance bands from squared float distances (no square root): the same
 // thresholds rho = |c1 - c2| / rmax < 1, 2, 4, 10.
+// fcg_band of the float offset (dx, dy, dz) and rmax, decided in single
+// precision where that is certain: the FP32 ratio carries a relative error
+// below 1e-6, so outside a 1e-5 relative margin around each threshold its
+// band is the FP64 band; inside the margin (or for a non-finite ratio) the
+// FP64 ratio decides. Returns exactly what fcg_band(fcg_mod(offset), rmax)
+// returns.
+FCG_HD int fcg_band_exact(float dx, float dy, float dz, double rmax) {
+    float d2 = dx * dx + dy * dy + dz * dz;
+    float rho = sqrtf(d2) / (float)rmax;
+    const float m = 1e-5f;
+    bool sure = rho == rho && rho < 3.0e38f && fabsf(rho - 1.0f) > m && fabsf(rho - 2.0f) > 2.0f * m &&
+                fabsf(rho - 4.0f) > 4.0f * m && fabsf(rho - 10.0f) > 10.0f * m;
+    if (sure) return rho < 1.0f ? 0 : rho < 2.0f ? 1 : rho < 4.0f ? 2 : rho < 10.0f ? 3 : 4;
+    double rd = sqrt((double)dx * (double)dx + (double)dy * (double)dy + (double)dz * (double)dz);
+    return fcg_band(rd, rmax);
+}
+
 FCG_HD int fcg_band32(float dx, float dy, float dz, float rmax) {
     float d2 = dx * dx + dy * dy + dz * dz, r2 = rmax * rmax;
     if (d2 < r2) return 0;

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
+#include <chrono>
 #include <string.h>
 #include <algorithm>
 #include <mutex>
@@ -145,6 +146,7 @@ struct DeviceProblem {
     int64_t *link_ptr = NULL;
     uint32_t *link_src = NULL;  // source node | band << kBandShift
     int32_t *leaf_node = NULL, *parent = NULL, *left = NULL, *right = NULL;
+    int64_t *node_lfirst = NULL;  // first leaf of every node
     double *leaf_eb = NULL, *leaf_ea = NULL, *leaf_weight = NULL;
     double *coef64 = NULL;
     float *coef32 = NULL;
@@ -166,7 +168,6 @@ struct DeviceProblem {
     int n_geom = 0;
     std::vector<int> geom_cols_ptr;  // cond_cols of geometry g: [geom_cols_ptr[g], geom_cols_ptr[g+1])
     std::vector<int64_t> geom_leaf_first, geom_leaf_count;
-    std::vector<int64_t> h_node_leaf_first;  // per device node label
     int nch = 0;  // Krylov chunks (never crossing a geometry)
     int32_t *leaf_geom = NULL, *ch_len = NULL, *ch_geom = NULL, *g_ch_first = NULL, *g_ch_count = NULL;
     int64_t *ch_start = NULL;
@@ -195,11 +196,14 @@ struct DeviceProblem {
 // Distance band of every link, in FP64 exactly as the reference decides it
 // (CAutoRefine::PotEstimateOpt, Solver/Autorefine.cpp:3495-3505, 3561-3598),
 // stored in the top bits of the link's source word. Runs once per problem.
+// band of every link, packed into the source word; counts the near-field
+// (band 0) links into *n_near
 __global__ void k_classify(int64_t Nn, const int64_t *__restrict__ ptr, uint32_t *__restrict__ src,
-                           const NodeGeo *__restrict__ geo) {
+                           const NodeGeo *__restrict__ geo, unsigned long long *n_near) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned cnt = 0;
     for (int64_t row = warp; row < Nn; row += nwarps) {
         const float c1[3] = {geo[row].c[0], geo[row].c[1], geo[row].c[2]};
         double ms1 = geo[row].maxside;
@@ -207,24 +211,96 @@ __global__ void k_classify(int64_t Nn, const int64_t *__restrict__ ptr, uint32_t
         for (int64_t l = s + lane; l < e; l += 32) {
             uint32_t j = src[l] & kSrcMask;
             const NodeGeo &g2 = geo[j];
-            double rdist = fcg_mod(fcg_fsub(c1, g2.c));
-            int band = fcg_band(rdist, ms1 > g2.maxside ? ms1 : g2.maxside);
+            double ms2 = g2.maxside;
+            int band = fcg_band_exact(c1[0] - g2.c[0], c1[1] - g2.c[1], c1[2] - g2.c[2], ms1 > ms2 ? ms1 : ms2);
             src[l] = j | ((uint32_t)band << kBandShift);
+            cnt += band == 0;
         }
     }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0 && cnt) atomicAdd(n_near, (unsigned long long)cnt);
 }
 
 // Move every model row to its device position (height-major label) and
 // relabel its sources; rows keep their links in order.
+// Device node arrays in height-major labels from the caller's post-order
+// arrays: geometry, children, parent, leaf map, first leaf of every node.
+__global__ void k_build_nodes(int64_t Nn, const int32_t *__restrict__ lab, const uint8_t *__restrict__ type,
+                              const float *__restrict__ vert, const float *__restrict__ cent, const float *__restrict__ norm,
+                              const double *__restrict__ area, const double *__restrict__ maxside, const int32_t *__restrict__ left,
+                              const int32_t *__restrict__ right, const int64_t *__restrict__ leaf_first, NodeGeo *__restrict__ geo,
+                              int32_t *__restrict__ dleft, int32_t *__restrict__ dright, int32_t *__restrict__ dparent,
+                              int32_t *__restrict__ leaf_node, int64_t *__restrict__ node_lfirst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t q = lab[i];
+        NodeGeo g;
+#pragma unroll
+        for (int k = 0; k < 9; k++) g.v[k] = vert[9 * i + k];
+#pragma unroll
+        for (int k = 0; k < 3; k++) { g.c[k] = cent[3 * i + k]; g.n[k] = norm[3 * i + k]; }
+        g.type = type[i];
+        g.maxside = maxside[i];
+        g.area = area[i];
+        geo[q] = g;
+        int32_t l = left[i], r = right[i];
+        dleft[q] = l >= 0 ? lab[l] : -1;
+        dright[q] = r >= 0 ? lab[r] : -1;
+        if (l >= 0) dparent[lab[l]] = q;
+        if (r >= 0) dparent[lab[r]] = q;
+        if (type[i] & FCG_IS_LEAF) leaf_node[leaf_first[i]] = q;
+        node_lfirst[q] = leaf_first[i];
+    }
+}
+
+// leaf permittivities: dielectric leaves get (outer, inner), conductor
+// leaves the outer permittivity of their surface as the C-assembly weight
+__global__ void k_build_leaves(int64_t Np, int n_cond, const int64_t *__restrict__ cfirst, const uint8_t *__restrict__ is_diel,
+                               const double *__restrict__ outp, const double *__restrict__ inp, const int32_t *__restrict__ sptr,
+                               const double *__restrict__ surf, const uint8_t *__restrict__ leaf_diel, double *__restrict__ eb,
+                               double *__restrict__ ea, double *__restrict__ weight) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_cond - 1;  // last conductor whose first leaf is <= j
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (cfirst[mid] <= j) lo = mid;
+            else hi = mid - 1;
+        }
+        if (is_diel[lo]) {
+            eb[j] = outp[lo];
+            ea[j] = inp[lo];
+            weight[j] = 0.0;
+        } else {
+            eb[j] = 0.0;
+            ea[j] = 0.0;
+            weight[j] = surf[sptr[lo] + leaf_diel[j]];
+        }
+    }
+}
+
+__global__ void k_node_geom(int64_t Nn, const int64_t *__restrict__ node_lfirst, const int32_t *__restrict__ leaf_geom,
+                            int32_t *__restrict__ node_geom) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nn; v += (int64_t)gridDim.x * blockDim.x)
+        node_geom[v] = leaf_geom[node_lfirst[v]];
+}
+
+// also validates the caller's sources: an index outside [0, Nn) is counted
+// in *bad and stored as node 0
 __global__ void k_relabel_links(int64_t Nn, const int64_t *__restrict__ ptr_model, const uint32_t *__restrict__ src_model,
-                                const int32_t *__restrict__ lab, const int64_t *__restrict__ ptr_dev, uint32_t *__restrict__ src_dev) {
+                                const int32_t *__restrict__ lab, const int64_t *__restrict__ ptr_dev, uint32_t *__restrict__ src_dev,
+                                unsigned *bad) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned nbad = 0;
     for (int64_t i = warp; i < Nn; i += nwarps) {
         int64_t b0 = ptr_model[i], e0 = ptr_model[i + 1], o = ptr_dev[lab[i]] - b0;
-        for (int64_t l = b0 + lane; l < e0; l += 32) src_dev[o + l] = (uint32_t)lab[src_model[l]];
+        for (int64_t l = b0 + lane; l < e0; l += 32) {
+            uint32_t j = src_model[l];  // a negative int32 reads as >= Nn
+            if (j >= (uint64_t)Nn) { nbad++; j = 0; }
+            src_dev[o + l] = (uint32_t)lab[j];
+        }
     }
+    if (nbad) atomicAdd(bad, nbad);
 }
 
 // counts tree edges and links whose two nodes lie in different geometries
@@ -243,39 +319,33 @@ __global__ void k_check_geometries(int64_t Nn, const int64_t *__restrict__ link_
 }
 
 // count the near-field (band 0) links of every row
-__global__ void k_near_count(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                             int32_t *__restrict__ cnt) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t row = warp; row < Nn; row += nwarps) {
-        int64_t s = ptr[row], e = ptr[row + 1];
-        int c = 0;
-        for (int64_t l = s + lane; l < e; l += 32) c += (src[l] >> kBandShift) == 0;
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        if (lane == 0) cnt[row] = c;
-    }
-}
 
 // list the near-field links of every row at its offset, in link order
+// (link, row) of every near-field link; slots are reserved with a cursor, so
+// the list order varies between runs (each entry is computed on its own)
 __global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                            const int64_t *__restrict__ off, int32_t *__restrict__ near_link, int32_t *__restrict__ near_row) {
+                            unsigned long long *cursor, int64_t cap, int32_t *__restrict__ near_link,
+                            int32_t *__restrict__ near_row) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = warp; row < Nn; row += nwarps) {
         int64_t s = ptr[row], e = ptr[row + 1];
-        int64_t o = off[row];
         for (int64_t base = s; base < e; base += 32) {
             int64_t l = base + lane;
             bool nr = l < e && (src[l] >> kBandShift) == 0;
             unsigned m = __ballot_sync(0xffffffffu, nr);
+            if (!m) continue;
+            unsigned long long at0 = 0;
+            if (lane == 0) at0 = atomicAdd(cursor, (unsigned long long)__popc(m));
+            at0 = __shfl_sync(0xffffffffu, at0, 0);
             if (nr) {
-                int64_t at = o + __popc(m & ((1u << lane) - 1u));
-                near_link[at] = (int32_t)l;
-                near_row[at] = (int32_t)row;
+                int64_t at = (int64_t)at0 + __popc(m & ((1u << lane) - 1u));
+                if (at < cap) {
+                    near_link[at] = (int32_t)l;
+                    near_row[at] = (int32_t)row;
+                }
             }
-            o += __popc(m);
         }
     }
 }
@@ -1166,8 +1236,7 @@ static std::string validate(const fcg_model_arrays &a) {
         if (a.node_leaf_first[i] < 0 || a.node_leaf_first[i] + a.node_leaf_count[i] > a.n_panels) return "leaf range out of bounds";
     }
     if (leaves != a.n_panels) return "leaf count does not match n_panels";
-    for (int64_t l = 0; l < a.n_links; l++)
-        if (a.link_src[l] < 0 || a.link_src[l] >= a.n_nodes) return "link source out of range";
+    // link sources are range-checked on the device while they are relabelled
     int64_t next = 0;
     for (int32_t c = 0; c < a.n_conductors; c++) {
         if (a.cond_leaf_first[c] != next || a.cond_leaf_count[c] <= 0) return "conductor leaf ranges must tile the leaves";
@@ -1188,14 +1257,25 @@ static std::string validate(const fcg_model_arrays &a) {
 // Cut the node forest into subtrees of at most kBlockLeaves leaves (one CTA
 // each in the sweep kernels) and the top nodes above them, each listed by
 // height so that children are processed before parents.
-static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::vector<int32_t> &parent, const std::vector<int32_t> &lab,
-                      cudaStream_t s) {
+// FCG_TRACE=1 prints the host phases of problem creation to stderr
+struct HostTrace {
+    bool on;
+    std::chrono::steady_clock::time_point t0, t;
+    HostTrace() : on(getenv("FCG_TRACE") != NULL), t0(std::chrono::steady_clock::now()), t(t0) {}
+    void mark(const char *what) {
+        if (!on) return;
+        auto n = std::chrono::steady_clock::now();
+        fprintf(stderr, "[fcg] %-24s %8.3f ms (total %8.3f)\n", what, std::chrono::duration<double, std::milli>(n - t).count(),
+                std::chrono::duration<double, std::milli>(n - t0).count());
+        t = n;
+    }
+};
+
+static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::vector<int32_t> &parent,
+                      const std::vector<int32_t> &height, const std::vector<int32_t> &lab, cudaStream_t s) {
     int64_t Nn = a.n_nodes;
-    std::vector<int32_t> height(Nn, 0);
-    for (int64_t i = 0; i < Nn; i++)
-        if (!(a.node_type[i] & FCG_IS_LEAF)) height[i] = 1 + std::max(height[a.node_left[i]], height[a.node_right[i]]);
     std::vector<int32_t> blk_leaf_first, blk_nleaves, blk_lvl_first, blk_nlvls, blk_root, lvl_ptr, lvl_nodes;
-    std::vector<int32_t> top_cnt;
+    std::vector<int32_t> top_cnt, hcount;
     std::vector<std::vector<int32_t>> top_by_h;
     int max_lv = 0;
     for (int64_t i = 0; i < Nn; i++) {
@@ -1215,14 +1295,17 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
         blk_lvl_first.push_back((int32_t)lvl_ptr.size());
         blk_nlvls.push_back(H);
         blk_root.push_back((int32_t)i);
-        std::vector<std::vector<int32_t>> byh(H + 1);
+        // internal nodes of the subtree grouped by height (counting sort)
+        hcount.assign(H + 2, 0);
         for (int64_t n = first; n <= i; n++)
-            if (!(a.node_type[n] & FCG_IS_LEAF)) byh[height[n]].push_back((int32_t)n);
-        for (int h = 1; h <= H; h++) {
-            lvl_ptr.push_back((int32_t)lvl_nodes.size());
-            lvl_nodes.insert(lvl_nodes.end(), byh[h].begin(), byh[h].end());
-        }
-        lvl_ptr.push_back((int32_t)lvl_nodes.size());
+            if (!(a.node_type[n] & FCG_IS_LEAF)) hcount[height[n] + 1]++;
+        for (int h = 1; h <= H; h++) hcount[h + 1] += hcount[h];
+        size_t base = lvl_nodes.size();
+        lvl_nodes.resize(base + hcount[H + 1]);
+        for (int h = 1; h <= H; h++) lvl_ptr.push_back((int32_t)(base + hcount[h]));
+        lvl_ptr.push_back((int32_t)(base + hcount[H + 1]));
+        for (int64_t n = first; n <= i; n++)
+            if (!(a.node_type[n] & FCG_IS_LEAF)) lvl_nodes[base + hcount[height[n]]++] = (int32_t)n;
         max_lv = std::max(max_lv, H);
     }
     // the down-sweep sums a subtree root's ancestors from a bounded chain
@@ -1264,7 +1347,9 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
 
 int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out) {
     *out = NULL;
+    HostTrace tr;
     std::string bad = validate(a);
+    tr.mark("validate");
     if (!bad.empty()) { set_error("invalid model: " + bad); return FCG_GENERIC_ERROR; }
     if (precision != FCG_PREC_FP64 && precision != FCG_PREC_MIXED) { set_error("unknown precision"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(ctx.device));
@@ -1318,30 +1403,10 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             inv[q] = (int32_t)i;
         }
     }
-    std::vector<NodeGeo> geo(Nn);
-    for (int64_t i = 0; i < Nn; i++) {
-        NodeGeo &g = geo[lab[i]];
-        memcpy(g.v, a.node_vertices + 9 * i, 36);
-        memcpy(g.c, a.node_centroid + 3 * i, 12);
-        memcpy(g.n, a.node_normal + 3 * i, 12);
-        g.type = a.node_type[i];
-        g.maxside = a.node_maxside[i];
-        g.area = a.node_area[i];
-    }
-    std::vector<int32_t> parent(Nn, -1), leaf_node(Np, -1);
-    for (int64_t i = 0; i < Nn; i++) {
-        if (a.node_type[i] & FCG_IS_LEAF) leaf_node[a.node_leaf_first[i]] = (int32_t)i;
-        else { parent[a.node_left[i]] = (int32_t)i; parent[a.node_right[i]] = (int32_t)i; }
-    }
-    std::vector<int32_t> dparent(Nn), dleft(Nn), dright(Nn), dleaf(Np);
-    for (int64_t i = 0; i < Nn; i++) {
-        dparent[lab[i]] = parent[i] >= 0 ? lab[parent[i]] : -1;
-        dleft[lab[i]] = a.node_left[i] >= 0 ? lab[a.node_left[i]] : -1;
-        dright[lab[i]] = a.node_right[i] >= 0 ? lab[a.node_right[i]] : -1;
-    }
-    for (int64_t j = 0; j < Np; j++) dleaf[j] = lab[leaf_node[j]];
-    p->h_node_leaf_first.assign(Nn, 0);
-    for (int64_t i = 0; i < Nn; i++) p->h_node_leaf_first[lab[i]] = a.node_leaf_first[i];
+    tr.mark("labels");
+    std::vector<int32_t> parent(Nn, -1);
+    for (int64_t i = 0; i < Nn; i++)
+        if (!(a.node_type[i] & FCG_IS_LEAF)) { parent[a.node_left[i]] = (int32_t)i; parent[a.node_right[i]] = (int32_t)i; }
     p->h_ptr_model.assign(a.link_ptr, a.link_ptr + Nn + 1);
     p->h_ptr_dev.assign(Nn + 1, 0);
     p->h_inv = inv;
@@ -1349,48 +1414,89 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         int64_t i = inv[q];
         p->h_ptr_dev[q + 1] = p->h_ptr_dev[q] + (a.link_ptr[i + 1] - a.link_ptr[i]);
     }
-    std::vector<double> eb(Np, 0.0), ea(Np, 0.0), weight(Np, 0.0);
-    for (int32_t c = 0; c < a.n_conductors; c++) {
-        for (int64_t j = a.cond_leaf_first[c]; j < a.cond_leaf_first[c] + a.cond_leaf_count[c]; j++) {
-            if (a.cond_is_diel[c]) { eb[j] = a.cond_outperm[c]; ea[j] = a.cond_inperm[c]; }
-            else weight[j] = a.cond_surf_outperm[a.cond_surf_ptr[c] + a.leaf_diel[j]];
-        }
-    }
-    FCG_TRY(upload(&p->geo, geo.data(), Nn, p->bytes, s));
+    tr.mark("parents, row offsets");
+    FCG_TRY(dalloc(&p->geo, Nn, p->bytes));
+    FCG_TRY(dalloc(&p->parent, Nn, p->bytes));
+    FCG_TRY(dalloc(&p->left, Nn, p->bytes));
+    FCG_TRY(dalloc(&p->right, Nn, p->bytes));
+    FCG_TRY(dalloc(&p->leaf_node, Np, p->bytes));
+    FCG_TRY(dalloc(&p->node_lfirst, Nn, p->bytes));
+    FCG_TRY(dalloc(&p->leaf_eb, Np, p->bytes));
+    FCG_TRY(dalloc(&p->leaf_ea, Np, p->bytes));
+    FCG_TRY(dalloc(&p->leaf_weight, Np, p->bytes));
     FCG_TRY(upload(&p->link_ptr, p->h_ptr_dev.data(), Nn + 1, p->bytes, s));
     {
-        // relabel the links on the device from the caller's arrays
+        // the caller's node, leaf and link arrays go to the device as they
+        // are; kernels scatter them into the device layout
         int64_t tb = 0;
+        int32_t *d_lab = NULL, *d_left = NULL, *d_right = NULL, *d_sptr = NULL;
+        uint8_t *d_type = NULL, *d_cdiel = NULL, *d_ldiel = NULL;
+        float *d_vert = NULL, *d_cent = NULL, *d_norm = NULL;
+        double *d_area = NULL, *d_maxs = NULL, *d_out = NULL, *d_in = NULL, *d_surf = NULL;
+        int64_t *d_lf = NULL, *d_cf = NULL, *ptr_model = NULL;
         uint32_t *src_model = NULL;
-        int64_t *ptr_model = NULL;
-        int32_t *dlab = NULL;
-        int rr = upload(&src_model, (const uint32_t *)a.link_src, L, tb, s);
-        if (rr == FCG_NORMAL_END) rr = upload(&ptr_model, a.link_ptr, Nn + 1, tb, s);
-        if (rr == FCG_NORMAL_END) rr = upload(&dlab, lab.data(), Nn, tb, s);
+        unsigned *dbad = NULL, hbad = 0;
+        int nsurf = a.cond_surf_ptr[a.n_conductors];
+        int rr = FCG_NORMAL_END;
+#define FCG_UP(ptr, host, n) if (rr == FCG_NORMAL_END) rr = upload(&ptr, host, n, tb, s)
+        FCG_UP(d_lab, lab.data(), Nn);
+        FCG_UP(d_type, a.node_type, Nn);
+        FCG_UP(d_vert, a.node_vertices, 9 * Nn);
+        FCG_UP(d_cent, a.node_centroid, 3 * Nn);
+        FCG_UP(d_norm, a.node_normal, 3 * Nn);
+        FCG_UP(d_area, a.node_area, Nn);
+        FCG_UP(d_maxs, a.node_maxside, Nn);
+        FCG_UP(d_left, a.node_left, Nn);
+        FCG_UP(d_right, a.node_right, Nn);
+        FCG_UP(d_lf, a.node_leaf_first, Nn);
+        FCG_UP(d_cf, a.cond_leaf_first, a.n_conductors);
+        FCG_UP(d_cdiel, a.cond_is_diel, a.n_conductors);
+        FCG_UP(d_out, a.cond_outperm, a.n_conductors);
+        FCG_UP(d_in, a.cond_inperm, a.n_conductors);
+        FCG_UP(d_sptr, a.cond_surf_ptr, a.n_conductors + 1);
+        FCG_UP(d_surf, a.cond_surf_outperm, std::max(nsurf, 1));
+        FCG_UP(d_ldiel, a.leaf_diel, Np);
+        FCG_UP(src_model, (const uint32_t *)a.link_src, L);
+        FCG_UP(ptr_model, a.link_ptr, Nn + 1);
+#undef FCG_UP
+        if (rr == FCG_NORMAL_END) rr = dalloc(&dbad, 1, tb);
         if (rr == FCG_NORMAL_END) rr = dalloc(&p->link_src, L, p->bytes);
-        if (rr == FCG_NORMAL_END && L > 0) {
-            int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)ctx.sm_count * 32);
-            k_relabel_links<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, dlab, p->link_ptr, p->link_src);
-            if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
-                set_error("link relabelling failed");
+        if (rr == FCG_NORMAL_END) {
+            int sms = ctx.sm_count;
+            cudaMemsetAsync(p->parent, 0xff, Nn * sizeof(int32_t), s);  // roots: -1
+            cudaMemsetAsync(dbad, 0, sizeof(unsigned), s);
+            k_build_nodes<<<grid_for(Nn, 256, sms), 256, 0, s>>>(Nn, d_lab, d_type, d_vert, d_cent, d_norm, d_area, d_maxs, d_left,
+                                                                  d_right, d_lf, p->geo, p->left, p->right, p->parent, p->leaf_node,
+                                                                  p->node_lfirst);
+            k_build_leaves<<<grid_for(Np, 256, sms), 256, 0, s>>>(Np, a.n_conductors, d_cf, d_cdiel, d_out, d_in, d_sptr, d_surf,
+                                                                   d_ldiel, p->leaf_eb, p->leaf_ea, p->leaf_weight);
+            if (L > 0) {
+                int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
+                k_relabel_links<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, d_lab, p->link_ptr, p->link_src, dbad);
+            }
+            p->timings.launches += L > 0 ? 3 : 2;
+            if (cudaGetLastError() != cudaSuccess ||
+                cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) {
+                set_error("building the device model failed");
                 rr = FCG_DEVICE_ERROR;
+            } else if (hbad) {
+                set_error("invalid model: " + std::to_string(hbad) + " link sources out of range");
+                rr = FCG_GENERIC_ERROR;
             }
         }
-        dfree(src_model);
-        dfree(ptr_model);
-        dfree(dlab);
+        dfree(d_lab); dfree(d_type); dfree(d_vert); dfree(d_cent); dfree(d_norm); dfree(d_area); dfree(d_maxs);
+        dfree(d_left); dfree(d_right); dfree(d_lf); dfree(d_cf); dfree(d_cdiel); dfree(d_out); dfree(d_in);
+        dfree(d_sptr); dfree(d_surf); dfree(d_ldiel); dfree(src_model); dfree(ptr_model); dfree(dbad);
         if (rr != FCG_NORMAL_END) { problem_destroy(p); return rr; }
     }
-    FCG_TRY(upload(&p->leaf_node, dleaf.data(), Np, p->bytes, s));
-    FCG_TRY(upload(&p->parent, dparent.data(), Nn, p->bytes, s));
-    FCG_TRY(upload(&p->leaf_eb, eb.data(), Np, p->bytes, s));
-    FCG_TRY(upload(&p->leaf_ea, ea.data(), Np, p->bytes, s));
-    FCG_TRY(upload(&p->leaf_weight, weight.data(), Np, p->bytes, s));
+    tr.mark("device model");
     FCG_TRY(dalloc(&p->self, Np, p->bytes));
     if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
-    FCG_TRY(build_plan(p, a, parent, lab, s));
+    FCG_TRY(build_plan(p, a, parent, height, lab, s));
+    tr.mark("sweep plan");
     FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
     {
         // contiguous row ranges of about equal work (links + 8 per row) for
@@ -1420,14 +1526,13 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         problem_destroy(p);
         return FCG_DEVICE_ERROR;
     }
-    FCG_TRY(upload(&p->left, dleft.data(), Nn, p->bytes, s));
-    FCG_TRY(upload(&p->right, dright.data(), Nn, p->bytes, s));
     // the uploads read host vectors that go out of scope: finish them here
     if (cudaStreamSynchronize(s) != cudaSuccess) {
         set_error(std::string("upload failed: ") + cudaGetErrorString(cudaGetLastError()));
         problem_destroy(p);
         return FCG_DEVICE_ERROR;
     }
+    tr.mark("rest + sync");
     *out = p;
     return FCG_NORMAL_END;
 #undef FCG_TRY
@@ -1441,7 +1546,7 @@ void problem_destroy(DeviceProblem *p) {
     if (p->stream) cudaStreamSynchronize(p->stream);
     AllocScope alloc_scope(p->stream);
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
-    dfree(p->left); dfree(p->right); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
+    dfree(p->left); dfree(p->right); dfree(p->node_lfirst); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
     dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
     dfree(p->near_link); dfree(p->near_row); dfree(p->tri);
     SweepPlan &pl = p->plan;
@@ -1558,42 +1663,34 @@ static int check_status(DeviceProblem *p, const char *what) {
 static int build_near_list(DeviceProblem *p) {
     cudaStream_t s = p->stream;
     int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
-    int32_t *cnt = NULL;
-    int64_t *off = NULL;
+    unsigned long long *ctr = NULL, hn[2] = {0, 0};
     int64_t tmp = 0;
     int r;
-    if ((r = dalloc(&cnt, p->Nn, tmp))) return r;
-    k_classify<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo);
-    k_near_count<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, cnt);
-    p->timings.launches += 2;
-    std::vector<int32_t> hc(p->Nn);
-    std::vector<int64_t> ho(p->Nn + 1, 0);
-    if (cudaMemcpyAsync(hc.data(), cnt, p->Nn * sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    if ((r = dalloc(&ctr, 2, tmp))) return r;
+    cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), s);
+    k_classify<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, ctr);
+    p->timings.launches++;
+    if (cudaMemcpyAsync(hn, ctr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {
-        set_error(std::string("near-field count failed: ") + cudaGetErrorString(cudaGetLastError()));
-        dfree(cnt);
+        set_error(std::string("link classification failed: ") + cudaGetErrorString(cudaGetLastError()));
+        dfree(ctr);
         return FCG_DEVICE_ERROR;
     }
-    for (int64_t i = 0; i < p->Nn; i++) ho[i + 1] = ho[i] + hc[i];
-    int64_t n = ho[p->Nn];
-    dfree(cnt);
-    if ((r = upload(&off, ho.data(), p->Nn + 1, tmp, s))) return r;
+    int64_t n = (int64_t)hn[0];
     if ((r = dalloc(&p->near_link, (size_t)std::max<int64_t>(n, 1), p->bytes)) ||
         (r = dalloc(&p->near_row, (size_t)std::max<int64_t>(n, 1), p->bytes))) {
-        dfree(off);
+        dfree(ctr);
         return r;
     }
     if (n > 0) {
-        k_near_list<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, off, p->near_link, p->near_row);
+        k_near_list<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, ctr + 1, n, p->near_link, p->near_row);
         p->timings.launches++;
-    }
-    if (n > 0) {
-        if ((r = dalloc(&p->tri, p->Nn, p->bytes))) { dfree(off); return r; }
+        if ((r = dalloc(&p->tri, p->Nn, p->bytes))) { dfree(ctr); return r; }
         k_make_tri<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri);
         p->timings.launches++;
     }
-    cudaError_t e = cudaStreamSynchronize(s);
-    dfree(off);
+    cudaError_t e = cudaGetLastError();
+    dfree(ctr);
     if (e != cudaSuccess) { set_error(std::string("near-field list failed: ") + cudaGetErrorString(e)); return FCG_DEVICE_ERROR; }
     p->n_near = n;
     return FCG_NORMAL_END;
@@ -1883,17 +1980,17 @@ int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond)
     }
     // every node and link must stay inside one geometry: a product that
     // couples geometries would make the separate solves wrong
-    std::vector<int32_t> node_geom(Nn);
-    for (int64_t v = 0; v < Nn; v++) node_geom[v] = leaf_geom[p->h_node_leaf_first[v]];
     cudaStream_t s = p->stream;
     int64_t tb = 0;
-    int32_t *d_ng = NULL;
+    int32_t *d_ng = NULL, *d_lg = NULL;
     unsigned *d_bad = NULL;
-    int r = upload(&d_ng, node_geom.data(), Nn, tb, s);
+    int r = upload(&d_lg, leaf_geom.data(), Np, tb, s);
+    if (r == FCG_NORMAL_END) r = dalloc(&d_ng, Nn, tb);
     if (r == FCG_NORMAL_END) r = dalloc(&d_bad, 1, tb);
     unsigned bad = 0;
     if (r == FCG_NORMAL_END) {
         cudaMemsetAsync(d_bad, 0, sizeof(unsigned), s);
+        k_node_geom<<<grid_for(Nn, 256, p->ctx->sm_count), 256, 0, s>>>(Nn, p->node_lfirst, d_lg, d_ng);
         int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
         k_check_geometries<<<grid, 256, 0, s>>>(Nn, p->link_ptr, p->link_src, p->parent, d_ng, d_bad);
         if (cudaGetLastError() != cudaSuccess ||
@@ -1904,6 +2001,7 @@ int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond)
         }
     }
     dfree(d_ng);
+    dfree(d_lg);
     dfree(d_bad);
     if (r != FCG_NORMAL_END) return r;
     if (bad) {

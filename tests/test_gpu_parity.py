@@ -125,3 +125,19 @@ def test_oracle_fill_vs_gpu_larger(ctx, tmp_path):
     np.testing.assert_allclose(lm, oc, rtol=1e-6, atol=1e-13 * np.abs(oc).max())
     capm, _ = pm.solve(tol=1e-4)
     assert np.max(np.abs(capm - ocap) / np.abs(ocap)) < 1e-3
+
+
+def test_invalid_link_source_rejected(ctx):
+    """Out-of-range link sources are found on the device and refused."""
+    g = load_golden("crossing2x2_m02")
+    a = model_arrays(g)
+    bad = dict(a)
+    src = np.array(a["link_src"], copy=True)
+    src[len(src) // 2] = len(a["node_type"]) + 5
+    src[0] = -3
+    bad["link_src"] = src
+    with pytest.raises(fc.FCError) as e:
+        ctx.problem(fc.Model.from_arrays(bad), fc.PREC_FP64)
+    assert "out of range" in str(e.value)
+    p = ctx.problem(fc.Model.from_arrays(a), fc.PREC_FP64)  # the context still works
+    p.fill()
