@@ -70,7 +70,8 @@ def log(*a):
 
 
 def dist_env():
-    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+    from fastercap_gb300 import replicas
+    return replicas.dist_env()
 
 
 class ClockSampler:
@@ -353,13 +354,10 @@ def run_gb300_multi(args, rank, world, local_rank):
         if i >= args.warmup:
             e2e_times.append(e0.elapsed_time(e1))
     d2h = sum(c.nbytes for c in caps_e) + 4 * sum(len(i) for i in its_e)
-    tmax, e2e_max = total_ms, sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([total_ms, e2e_max], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tmax, e2e_max = float(t[0]), float(t[1])
-    value = world * args.steps * G / (tmax / 1000.0)
-    e2e_value = world * args.steps * G / (e2e_max / 1000.0)
+    from fastercap_gb300 import replicas
+    tmax, e2e_max = replicas.max_over_ranks([total_ms, sum(e2e_times)], world)
+    value = replicas.throughput(args.steps * G, world, tmax / 1000.0)
+    e2e_value = replicas.throughput(args.steps * G, world, e2e_max / 1000.0)
     peak, peak_kind = peaks()
     link_avg_ms = st["link_ms"] / max(1, st["link_launches"])
     link_bytes = st["link_bytes"] / max(1, st["link_launches"])
@@ -429,7 +427,7 @@ def run_gb300_multi(args, rank, world, local_rank):
 SERVING = {"mesh_eps": 1e-3, "tol": 1e-4, "kmin": 2, "kmax": 12}
 
 
-def build_requests(n: int):
+def build_requests(n: int, rank: int = 0, world: int = 1):
     import fastercap_gb300 as fc
     from fastercap_gb300 import geometry as geo
     from concurrent.futures import ThreadPoolExecutor
@@ -442,20 +440,25 @@ def build_requests(n: int):
         os.unlink(path)
         return m
 
+    from fastercap_gb300 import replicas
+    ids = replicas.shard(n, rank, world)  # request r is served by GPU r mod world
     t0 = time.perf_counter()
     with ThreadPoolExecutor(os.cpu_count() or 1) as ex:  # the native builder releases the GIL
-        models = list(ex.map(one, range(n)))
+        models = list(ex.map(one, ids))
     os.rmdir(tmp)
-    return models, time.perf_counter() - t0
+    return models, ids, time.perf_counter() - t0
 
 
-def serve_pass(srv, models, precision, lam, tol):
-    """Submit every request at its arrival time; returns per-request
+def serve_pass(srv, models, ids, n_total, precision, lam, tol, world=1):
+    """Submit every request of this GPU's shard at its arrival time (one
+    Poisson schedule over all n_total requests); returns per-request
     (latency ms, completion s, C, iterations, info)."""
-    arr = np.cumsum(np.random.default_rng(10000 + int(lam)).exponential(1.0 / lam, len(models)))
+    arr = np.cumsum(np.random.default_rng(10000 + int(lam)).exponential(1.0 / lam, n_total))
+    from fastercap_gb300 import replicas
+    replicas.barrier(world)
     t0 = time.perf_counter()
     sub = []
-    for r, m in enumerate(models):
+    for r, m in zip(ids, models):
         dt = t0 + arr[r] - time.perf_counter()
         if dt > 0:
             time.sleep(dt)
@@ -475,8 +478,12 @@ def run_serving(args, rank, world, local_rank):
     from fastercap_gb300 import build as fbuild
     fbuild.build(reference=False)
     torch.cuda.set_device(local_rank)
+    from fastercap_gb300 import replicas
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     rates = [float(x) for x in args.rates.split(",")]
-    models, build_s = build_requests(args.requests)
+    models, ids, build_s = build_requests(args.requests, rank, world)
     ctx = fc.Context(local_rank)
     tol = SERVING["tol"]
     res = {}
@@ -492,13 +499,15 @@ def run_serving(args, rank, world, local_rank):
             for lam in rates:
                 if name == "mixed" and lam == rates[-1]:
                     with ClockSampler(local_rank) as clk:
-                        out = serve_pass(srv, models, prec, lam, tol)
+                        out = serve_pass(srv, models, ids, args.requests, prec, lam, tol, world)
                     clk_summary = clk.summary()
                 else:
-                    out = serve_pass(srv, models, prec, lam, tol)
-                lat = np.array([o[0] for o in out])
-                span = max(o[1] for o in out)
-                res[name][str(int(lam))] = {"solves_s": len(out) / span, "p50_ms": float(np.percentile(lat, 50)),
+                    out = serve_pass(srv, models, ids, args.requests, prec, lam, tol, world)
+                # latencies of every GPU's shard; the job ends with the slowest GPU
+                parts = replicas.gather_to_all(([o[0] for o in out], max(o[1] for o in out)), world)
+                lat = np.array([x for p_ in parts for x in p_[0]])
+                span = max(p_[1] for p_ in parts)
+                res[name][str(int(lam))] = {"solves_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
                                             "p99_ms": float(np.percentile(lat, 99)),
                                             "mean_queue_ms": float(np.mean([o[4]["queue_ms"] for o in out]))}
                 caps[(name, lam)] = [o[2] for o in out]
@@ -512,11 +521,12 @@ def run_serving(args, rank, world, local_rank):
     h2d = int(np.mean([model_bytes(m) for m in models]))
     mixed_top = res["mixed"][top]
     result = {
-        "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(models),
+        "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": world, "steps": args.requests,
         "warmup": 4, "ms_per_step": 1000.0 / mixed_top["solves_s"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
         "p50_ms": mixed_top["p50_ms"], "p99_ms": mixed_top["p99_ms"],
-        "config": {"workload": "serving", "requests": len(models), "rates_req_s": rates, "slots": args.slots,
+        "config": {"workload": "serving", "requests": args.requests, "rates_req_s": rates, "slots": args.slots,
+                   "parallelism": "request r on GPU r mod N" if world > 1 else "single GPU",
                    "request": "random k x k crossing, k in 2..12, seed = request id", "link_eps": SERVING["mesh_eps"],
                    "gmres_tol": tol, "precond": "jacobi",
                    "panels_min_max_mean": [min(m.n_panels for m in models), max(m.n_panels for m in models),
@@ -534,7 +544,7 @@ def run_serving(args, rank, world, local_rank):
         "gpu_launches": launches,
         "clocks": clk_summary,
     }
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         from pyoracle import Oracle
         cores = os.cpu_count() or 1
@@ -550,8 +560,11 @@ def run_serving(args, rank, world, local_rank):
         dt = time.perf_counter() - t0
         result["cpu_baseline"] = {"value": n / dt, "unit": "solves/s", "cores": cores, "kind": "port",
                                   "sample": "the first %d requests, solved one after another" % n}
-    print(json.dumps(result), flush=True)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
     ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def run_reference_serving(args, rank, world):
@@ -563,7 +576,7 @@ def run_reference_serving(args, rank, world):
     from pyoracle import Oracle
     from fastercap_gb300 import build as fbuild
     fbuild.build(reference=False)
-    models, build_s = build_requests(args.warmup + args.steps)
+    models, _, build_s = build_requests(args.warmup + args.steps)
     cores = os.cpu_count() or 1
     times = []
     for i, m in enumerate(models):
@@ -665,15 +678,10 @@ def run_gb300(args, rank, world, local_rank):
             e2e_times.append(e0.elapsed_time(e1))
     d2h = cap_e.nbytes + 4 * len(cap_e)
 
-    tmax = total_ms
-    if world > 1:
-        t = torch.tensor([total_ms, sum(e2e_times)], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tmax, e2e_max = float(t[0]), float(t[1])
-    else:
-        e2e_max = sum(e2e_times)
-    value = world * args.steps / (tmax / 1000.0)
-    e2e_value = world * args.steps / (e2e_max / 1000.0)
+    from fastercap_gb300 import replicas
+    tmax, e2e_max = replicas.max_over_ranks([total_ms, sum(e2e_times)], world)
+    value = replicas.throughput(args.steps, world, tmax / 1000.0)
+    e2e_value = replicas.throughput(args.steps, world, e2e_max / 1000.0)
     peak, peak_kind = peaks()
     link_avg_ms = st["link_ms"] / max(1, st["link_launches"])
     link_bytes = st["link_bytes"] / max(1, st["link_launches"])
@@ -747,7 +755,7 @@ def main():
     if args.workload == "serving":
         if args.impl == "reference":
             run_reference_serving(args, rank, world)
-        elif rank == 0:
+        else:
             run_serving(args, rank, world, local_rank)
         return
     if args.impl == "reference":
