@@ -65,6 +65,14 @@ MULTI = {
 }
 
 
+# DRAM bytes per link-product launch (dram__bytes_read.sum +
+# dram__bytes_write.sum) from one ncu capture of the same kernel and workload
+LINK_TRAFFIC = {
+    "sphere_327680": 531.318272e6 + 4.354048e6,    # k_spmv32<1, 32>
+    "crossing8x8_slab": 679.950848e6 + 7.460608e6,  # k_spmv32_multi<16>
+}
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -708,10 +716,11 @@ def run_gb300(args, rank, world, local_rank):
                 "p50_ms": float(np.percentile(e2e_times, 50))},
         "gpu_launches": int(st["kernel_launches"]),
         "phases": phase,
-        "roofline": {"kernel": "k_spmv32 (link product)", "bound": "hbm",
+        "roofline": {"kernel": "k_spmv32<1, 32> (link product)" if len(model.conductor_names) == 1
+                     else "k_spmv32_multi (link product)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-                     "traffic": None, "launches": int(st["link_launches"]),
+                     "traffic": LINK_TRAFFIC.get(args.workload), "launches": int(st["link_launches"]),
                      "bytes_per_launch": link_bytes, "avg_launch_ms": link_avg_ms},
         "clocks": clk.summary(),
     }
