@@ -9,8 +9,11 @@
  *   orc_matvec     CMultHier::MultiplyMatByVec_fast and its three passes
  *                                                  Solver/MultiplyHierarchical.cpp:72-304
  *   gmres          CSolveCap::gmresPrecondSFastAll Solver/SolveCapacitance.cpp:2288-2574
- *   precond        CSolveCap::ComputePrecondVectFast (none / Jacobi)
- *                                                  Solver/SolveCapacitance.cpp:3458-3526
+ *   precond        CSolveCap::ComputePrecondVectFast (none / Jacobi / two-level)
+ *                                                  Solver/SolveCapacitance.cpp:3458-3598
+ *   orc_super_build  two-level preconditioner setup: CSolveCap::MakePreconditioner,
+ *                  RecurseComputePrecond, ComputeSuperPrecond, InvertMatrix
+ *                                                  Solver/SolveCapacitance.cpp:1061-1133,1876-2066,2116-2258
  *   orc_solve      CSolveCap::Solve                Solver/SolveCapacitance.cpp:1138-1425
  * Vector arithmetic follows the conventions used to compile the reference
  * here: a difference of two single-precision vertices is formed in single
@@ -277,14 +280,162 @@ static double norm2(const double *a, int64_t n) {
     return sqrt(s);
 }
 
-static void precond(int pc, const double *self, const double *q, double *out, int64_t n) {
+/* ---- two-level preconditioner setup */
+
+static void super_visit(const orc_model *m, int64_t v, int d, int lev, orc_super *s) {
+    int leaf = (m->node_type[v] & T_LEAF) != 0;
+    if ((leaf && d <= lev) || (!leaf && d == lev)) {
+        s->elem_node[s->m++] = v;
+        return;
+    }
+    super_visit(m, m->node_left[v], d + 1, lev, s);
+    super_visit(m, m->node_right[v], d + 1, lev, s);
+}
+
+static void lu_inverse(double *a, double *inv, int32_t n) {
+    /* LU factorisation with partial pivoting, in place (right-looking, one
+     * rank-1 update per column), then the inverse column by column by forward
+     * and backward substitution (InvertMatrix, Solver/SolveCapacitance.cpp:2116-2258) */
+    int32_t *piv = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    double *col = (double *)malloc(sizeof(double) * (size_t)n);
+    int32_t j, i, k;
+    for (j = 0; j < n; j++) {
+        int32_t p = j;
+        double best = fabs(a[(size_t)j * n + j]);
+        for (i = j + 1; i < n; i++)
+            if (fabs(a[(size_t)i * n + j]) > best) { p = i; best = fabs(a[(size_t)i * n + j]); }
+        piv[j] = p;
+        if (p != j)
+            for (k = 0; k < n; k++) {
+                double t = a[(size_t)j * n + k];
+                a[(size_t)j * n + k] = a[(size_t)p * n + k];
+                a[(size_t)p * n + k] = t;
+            }
+        if (j < n - 1) {
+            double r = 1.0 / a[(size_t)j * n + j];
+            for (i = j + 1; i < n; i++) a[(size_t)i * n + j] *= r;
+            for (i = j + 1; i < n; i++)
+                for (k = j + 1; k < n; k++) a[(size_t)i * n + k] -= a[(size_t)i * n + j] * a[(size_t)j * n + k];
+        }
+    }
+    for (k = 0; k < n; k++) {
+        for (i = 0; i < n; i++) col[i] = 0.0;
+        col[k] = 1.0;
+        for (i = 0; i < n; i++) { /* the row swaps, in factorisation order */
+            double t = col[i];
+            col[i] = col[piv[i]];
+            col[piv[i]] = t;
+        }
+        for (i = 0; i < n; i++) { /* unit lower triangle */
+            double sum = col[i];
+            for (j = 0; j < i; j++) sum -= a[(size_t)i * n + j] * col[j];
+            col[i] = sum;
+        }
+        for (i = n - 1; i >= 0; i--) { /* upper triangle */
+            double sum = col[i];
+            for (j = i + 1; j < n; j++) sum -= a[(size_t)i * n + j] * col[j];
+            col[i] = sum / a[(size_t)i * n + i];
+        }
+        for (i = 0; i < n; i++) inv[(size_t)i * n + k] = col[i];
+    }
+    free(piv);
+    free(col);
+}
+
+int orc_super_build(const orc_model *m, unsigned dim, orc_super *s) {
+    int64_t i, j;
+    int32_t c, *parent;
+    memset(s, 0, sizeof *s);
+    if (dim > 4096) dim = 4096;
+    if (dim < 16) dim = 16;
+    if ((unsigned)m->n_conductors >= dim) return 0;
+    int lev = (int)(unsigned)(log((double)(dim / (unsigned)m->n_conductors)) / log(2.0));
+    s->elem_node = (int64_t *)malloc(sizeof(int64_t) * 4096);
+    parent = (int32_t *)malloc(sizeof(int32_t) * (size_t)m->n_nodes);
+    for (i = 0; i < m->n_nodes; i++) parent[i] = -1;
+    for (i = 0; i < m->n_nodes; i++)
+        if (!(m->node_type[i] & T_LEAF)) { parent[m->node_left[i]] = (int32_t)i; parent[m->node_right[i]] = (int32_t)i; }
+    /* each conductor's tree, in conductor order (roots in leaf order) */
+    for (c = 0; c < m->n_conductors; c++)
+        for (i = 0; i < m->n_nodes; i++)
+            if (parent[i] < 0 && m->node_leaf_first[i] == m->cond_leaf_first[c]) { super_visit(m, i, 0, lev, s); break; }
+    free(parent);
+    int32_t mm = s->m;
+    s->sup_index = (int32_t *)malloc(sizeof(int32_t) * (size_t)m->n_panels);
+    s->area = (float *)malloc(sizeof(float) * (size_t)m->n_panels);
+    s->dim = (double *)malloc(sizeof(double) * (size_t)mm);
+    int32_t *ln = leaf_nodes(m);
+    for (i = 0; i < mm; i++) {
+        int64_t v = s->elem_node[i];
+        s->dim[i] = m->node_area[v];
+        for (j = m->node_leaf_first[v]; j < m->node_leaf_first[v] + m->node_leaf_count[v]; j++) s->sup_index[j] = (int32_t)i;
+    }
+    for (j = 0; j < m->n_panels; j++) s->area[j] = (float)m->node_area[ln[j]];
+    free(ln);
+    /* super potential matrix: self terms on the diagonal, the one-way
+     * estimate both ways off it (ComputeSuperPrecond) */
+    double *pm = (double *)malloc(sizeof(double) * (size_t)mm * mm);
+    s->minv = (double *)malloc(sizeof(double) * (size_t)mm * mm);
+    for (i = 0; i < mm; i++) {
+        int64_t v = s->elem_node[i];
+        for (c = 0; c < m->n_conductors; c++)
+            if (m->node_leaf_first[v] >= m->cond_leaf_first[c] &&
+                m->node_leaf_first[v] < m->cond_leaf_first[c] + m->cond_leaf_count[c]) break;
+        if (m->node_type[v] & T_DIEL) {
+            double eb = m->cond_outperm[c], ea = m->cond_inperm[c];
+            pm[(size_t)i * mm + i] = (ea + eb) / (TWO_E0 * (eb - ea) * m->node_area[v]);
+        } else {
+            pm[(size_t)i * mm + i] = pot_opt(wid(m->node_centroid + 3 * v), m->node_vertices + 9 * v) / FOUR_PI_E0;
+        }
+        for (j = i + 1; j < mm; j++) {
+            pm[(size_t)i * mm + j] = pot_estimate(m, v, s->elem_node[j]);
+            pm[(size_t)j * mm + i] = pot_estimate(m, s->elem_node[j], v);
+        }
+    }
+    lu_inverse(pm, s->minv, mm);
+    free(pm);
+    return mm;
+}
+
+void orc_super_free(orc_super *s) {
+    free(s->elem_node); free(s->sup_index); free(s->area); free(s->dim); free(s->minv);
+    memset(s, 0, sizeof *s);
+}
+
+/* two-level preconditioner product (ComputePrecondVectFast, super branch,
+ * Solver/SolveCapacitance.cpp:3547-3598): leaf values are averaged into their
+ * super element by area, multiplied by the inverse super potential matrix
+ * without its diagonal, spread back by area, plus the diagonal term per leaf */
+static void super_apply(const orc_super *sp, const double *q, double *out, int64_t n) {
+    int32_t mm = sp->m, i, k;
+    int64_t j;
+    double *pot = (double *)calloc((size_t)mm, sizeof(double)), *chg = (double *)calloc((size_t)mm, sizeof(double));
+    for (j = 0; j < n; j++) {
+        int32_t e = sp->sup_index[j];
+        pot[e] += q[j] * (double)sp->area[j] / sp->dim[e];
+    }
+    for (i = 0; i < mm; i++)
+        for (k = 0; k < mm; k++)
+            if (i != k) chg[i] += sp->minv[(size_t)i * mm + k] * pot[k];
+    for (j = 0; j < n; j++) {
+        int32_t e = sp->sup_index[j];
+        out[j] = chg[e] * (double)sp->area[j] / sp->dim[e];
+        out[j] += sp->minv[(size_t)e * mm + e] * q[j] * (double)sp->area[j] / sp->dim[e];
+    }
+    free(pot);
+    free(chg);
+}
+
+/* pc: 0 none, 1 Jacobi, 2 two-level (sp) */
+static void precond(int pc, const double *self, const orc_super *sp, const double *q, double *out, int64_t n) {
     int64_t i;
+    if (pc == 2) { super_apply(sp, q, out, n); return; }
     for (i = 0; i < n; i++) out[i] = pc ? q[i] / self[i] : q[i];
 }
 
 /* returns the index of the last Arnoldi step (-1 if x0 was accepted); *capped set on non-convergence */
-static int gmres(const orc_model *m, const double *coef, const double *self, const double *b, double *x, double tol, int pc,
-                 int *capped, double *chg, double *pot) {
+static int gmres(const orc_model *m, const double *coef, const double *self, const orc_super *sp, const double *b, double *x,
+                 double tol, int pc, int *capped, double *chg, double *pot) {
     int64_t n = m->n_panels, k;
     int maxit = GMRES_ITER_MAX < n ? GMRES_ITER_MAX : (int)n;
     double *x0 = (double *)calloc((size_t)n, sizeof(double));
@@ -298,7 +449,7 @@ static int gmres(const orc_model *m, const double *coef, const double *self, con
     int i, j, iteration;
     *capped = 0;
     if (pc) {
-        precond(pc, self, b, x0, n);
+        precond(pc, self, sp, b, x0, n);
         matvec_ws(m, coef, self, x0, vv, chg, pot);
         for (k = 0; k < n; k++) rr[k] = b[k] - vv[k];
         normr = norm2(rr, n);
@@ -320,7 +471,7 @@ static int gmres(const orc_model *m, const double *coef, const double *self, con
         H[i] = (double *)calloc((size_t)i + 2, sizeof(double));
         Q[i + 1] = (double *)malloc(sizeof(double) * (size_t)n);
         if (pc) {
-            precond(pc, self, Q[i], Pq, n);
+            precond(pc, self, sp, Q[i], Pq, n);
             matvec_ws(m, coef, self, Pq, vv, chg, pot);
         } else {
             matvec_ws(m, coef, self, Q[i], vv, chg, pot);
@@ -369,7 +520,7 @@ static int gmres(const orc_model *m, const double *coef, const double *self, con
         vv[k] = t;
     }
     if (pc) {
-        precond(pc, self, vv, x, n);
+        precond(pc, self, sp, vv, x, n);
         for (k = 0; k < n; k++) x[k] = x0[k] + x[k];
     } else {
         memcpy(x, vv, sizeof(double) * (size_t)n);
@@ -381,8 +532,8 @@ done:
     return iteration;
 }
 
-int orc_solve(const orc_model *m, const double *coef, const double *self, double tol, int pc, double *cap, int *iterations,
-              double *charges, int threads) {
+int orc_solve_ex(const orc_model *m, const double *coef, const double *self, double tol, int pc, unsigned super_dim,
+                 double *cap, int *iterations, double *charges, int threads) {
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
 #else
@@ -392,6 +543,9 @@ int orc_solve(const orc_model *m, const double *coef, const double *self, double
     double *b = (double *)calloc((size_t)n, sizeof(double)), *x = (double *)malloc(sizeof(double) * (size_t)n);
     double *chg = (double *)malloc(sizeof(double) * (size_t)m->n_nodes), *pot = (double *)malloc(sizeof(double) * (size_t)m->n_nodes);
     int ncol = 0, row = 0, any_capped = 0;
+    orc_super sp;
+    memset(&sp, 0, sizeof sp);
+    if (pc == 2 && orc_super_build(m, super_dim, &sp) == 0) pc = 0;  /* too many roots: no preconditioner */
     int32_t c, c2;
     for (c = 0; c < m->n_conductors; c++) ncol += m->cond_is_diel[c] ? 0 : 1;
     for (c = 0; c < m->n_conductors; c++) {
@@ -399,7 +553,7 @@ int orc_solve(const orc_model *m, const double *coef, const double *self, double
         int capped, col = 0;
         if (m->cond_is_diel[c]) continue;
         for (j = m->cond_leaf_first[c]; j < m->cond_leaf_first[c] + m->cond_leaf_count[c]; j++) b[j] = 1.0;
-        int it = gmres(m, coef, self, b, x, tol, pc, &capped, chg, pot);
+        int it = gmres(m, coef, self, &sp, b, x, tol, pc, &capped, chg, pot);
         any_capped |= capped;
         if (iterations) iterations[row] = it + 1;
         if (charges) memcpy(charges + (size_t)row * n, x, sizeof(double) * (size_t)n);
@@ -415,5 +569,11 @@ int orc_solve(const orc_model *m, const double *coef, const double *self, double
         row++;
     }
     free(b); free(x); free(chg); free(pot);
+    orc_super_free(&sp);
     return any_capped;
+}
+
+int orc_solve(const orc_model *m, const double *coef, const double *self, double tol, int pc, double *cap, int *iterations,
+              double *charges, int threads) {
+    return orc_solve_ex(m, coef, self, tol, pc, 0, cap, iterations, charges, threads);
 }

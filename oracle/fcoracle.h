@@ -47,6 +47,26 @@ void orc_matvec(const orc_model *m, const double *link_coef, const double *self_
 int orc_solve(const orc_model *m, const double *link_coef, const double *self_coef, double tol, int precond, double *cap,
               int *iterations, double *charges, int threads);
 
+/* two-level preconditioner (-ps<dim>): m super elements (nodes at depth
+ * log2(dim / conductors) of every conductor's tree, or leaves above it, in
+ * depth-first order), the leaf -> element map, leaf areas as float, element
+ * areas and the inverse of the m x m super potential matrix (row-major) */
+typedef struct {
+    int32_t m;
+    int64_t *elem_node;
+    int32_t *sup_index;
+    float *area;
+    double *dim;
+    double *minv;
+} orc_super;
+/* returns m; 0 when there are at least `dim` conductors (no two-level preconditioner) */
+int orc_super_build(const orc_model *m, unsigned dim, orc_super *s);
+void orc_super_free(orc_super *s);
+/* orc_solve with precond 2 = two-level of dimension super_dim (falls back to
+ * no preconditioner when orc_super_build returns 0) */
+int orc_solve_ex(const orc_model *m, const double *link_coef, const double *self_coef, double tol, int precond,
+                 unsigned super_dim, double *cap, int *iterations, double *charges, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,11 @@ class OrcModel(C.Structure):
     _fields_ = FIELDS
 
 
+class OrcSuper(C.Structure):
+    _fields_ = [("m", C.c_int32), ("elem_node", C.POINTER(C.c_int64)), ("sup_index", C.POINTER(C.c_int32)),
+                ("area", C.POINTER(C.c_float)), ("dim", C.POINTER(C.c_double)), ("minv", C.POINTER(C.c_double))]
+
+
 _lib = None
 
 
@@ -54,6 +59,10 @@ def lib():
         L.orc_matvec.argtypes = [C.POINTER(OrcModel), vp, vp, vp, vp, C.c_int]
         L.orc_matvec.restype = None
         L.orc_solve.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_double, C.c_int, vp, vp, vp, C.c_int]
+        L.orc_solve_ex.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_double, C.c_int, C.c_uint, vp, vp, vp, C.c_int]
+        L.orc_super_build.argtypes = [C.POINTER(OrcModel), C.c_uint, C.POINTER(OrcSuper)]
+        L.orc_super_free.argtypes = [C.POINTER(OrcSuper)]
+        L.orc_super_free.restype = None
         _lib = L
     return _lib
 
@@ -93,13 +102,26 @@ class Oracle:
         lib().orc_matvec(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, q.ctypes.data, v.ctypes.data, self.threads)
         return v
 
-    def solve(self, tol=0.01, precond=1, coef=None, self_coef=None):
+    def super_build(self, dim):
+        """The two-level preconditioner of dimension dim: (elements, leaf map, leaf areas, inverse matrix)."""
+        sp = OrcSuper()
+        m = lib().orc_super_build(C.byref(self.s), dim, C.byref(sp))
+        out = None
+        if m > 0:
+            n = self.s.n_panels
+            out = (np.ctypeslib.as_array(sp.elem_node, (m,)).copy(), np.ctypeslib.as_array(sp.sup_index, (n,)).copy(),
+                   np.ctypeslib.as_array(sp.area, (n,)).copy(), np.ctypeslib.as_array(sp.minv, (m, m)).copy())
+        lib().orc_super_free(C.byref(sp))
+        return out
+
+    def solve(self, tol=0.01, precond=1, coef=None, self_coef=None, super_dim=0):
+        """precond: 0 none, 1 Jacobi, 2 two-level of dimension super_dim."""
         coef = self.coef if coef is None else np.ascontiguousarray(coef, np.float64)
         sc = self.self_coef if self_coef is None else np.ascontiguousarray(self_coef, np.float64)
         nc = int((self.a["cond_is_diel"] == 0).sum())
         cap = np.empty((nc, nc), np.float64)
         it = np.empty(nc, np.int32)
         ch = np.empty((nc, self.s.n_panels), np.float64)
-        capped = lib().orc_solve(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, tol, precond, cap.ctypes.data,
-                                 it.ctypes.data, ch.ctypes.data, self.threads)
+        capped = lib().orc_solve_ex(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, tol, precond, super_dim,
+                                    cap.ctypes.data, it.ctypes.data, ch.ctypes.data, self.threads)
         return cap, it, ch, bool(capped)

@@ -110,6 +110,15 @@ int main(int argc, char **argv) {
     if (console.ParseCmdLine(cmd.c_str(), gv, err)) { fprintf(stderr, "%s\n", (const char *)err); return 64; }
     gv.m_dEps = gv.m_dEpsRatio * gv.m_dMeshEps;
     if (gv.m_dEps == 0.0) gv.m_dEps = 0.01;
+    // the option checks CSolveCap::Run applies before solving
+    // (Solver/SolveCapacitance.cpp:122-147): two-level wins over Jacobi, and
+    // its dimension is clamped
+    if ((gv.m_ucPrecondType & AUTOREFINE_PRECOND_SUPER) && (gv.m_ucPrecondType & AUTOREFINE_PRECOND_JACOBI))
+        gv.m_ucPrecondType = AUTOREFINE_PRECOND_SUPER;
+    if (gv.m_ucPrecondType & AUTOREFINE_PRECOND_SUPER) {
+        if (gv.m_uiSuperPreDim > SOLVE_MAX_SUPER_PRECOND_NUM) gv.m_uiSuperPreDim = SOLVE_MAX_SUPER_PRECOND_NUM;
+        else if (gv.m_uiSuperPreDim < SOLVE_MIN_SUPER_PRECOND_NUM) gv.m_uiSuperPreDim = SOLVE_MIN_SUPER_PRECOND_NUM;
+    }
 
     CSolveCap *solve = new CSolveCap();
     CMultHier &mh = solve->m_clsMulthier;
@@ -200,6 +209,19 @@ int main(int argc, char **argv) {
     if (ret != FC_NORMAL_END) { fprintf(stderr, "solve failed %d\n", ret); return ret; }
     std::vector<double> cap(cRe.m_a.begin(), cRe.m_a.end());
     npy("cap", "<f8", cap, cRe.num_cols());
+    // two-level preconditioner as the reference built it
+    if ((solve->m_clsGlobalVars.m_ucPrecondType & AUTOREFINE_PRECOND_SUPER) && solve->m_uiSupPreNum > 0) {
+        unsigned int msup = solve->m_uiSupPreNum;
+        std::vector<int> sn(msup), si(Np);
+        std::vector<float> sa(Np);
+        std::vector<double> minv((size_t)msup * msup);
+        for (unsigned int i = 0; i < msup; i++) sn[i] = idx[solve->m_clsSupPrecondElements[i].m_pclsHiLevLeaf];
+        for (unsigned long i = 0; i < Np; i++) { si[i] = (int)solve->m_puiSupPrecondIndex[i]; sa[i] = solve->m_pfSupPrecondAreae[i]; }
+        for (unsigned int i = 0; i < msup; i++)
+            for (unsigned int j = 0; j < msup; j++) minv[(size_t)i * msup + j] = solve->m_pclsSupPrecondMtx[i][j];
+        npy("sup_nodes", "<i4", sn); npy("sup_index", "<i4", si); npy("sup_area", "<f4", sa);
+        npy("sup_minv", "<f8", minv, (long)msup);
+    }
 
     // GMRES iteration lists "GMRES Iteration: 0 1 2 ... k" -> k+1 Arnoldi steps
     std::vector<int> iters;

@@ -54,10 +54,20 @@ def build_from_golden(g, tmp_path):
 
 
 def solve_params(g):
+    """(GMRES tolerance, preconditioner: 0 none, 1 Jacobi, 2 two-level)"""
     sw = [str(s) for s in g["switches"]]
     tol = switch_value(sw, "-t", 0.01)
-    precond = 0 if "-pn" in sw else 1
+    precond = 0 if "-pn" in sw else (2 if any(s.startswith("-ps") for s in sw) else 1)
     return tol, precond
+
+
+def super_dim(g):
+    """the two-level preconditioner dimension of -ps<dim> (0 if absent)"""
+    for s in g["switches"]:
+        s = str(s)
+        if s.startswith("-ps"):
+            return int(s[3:])
+    return 0
 
 
 @pytest.fixture(params=golden_names())

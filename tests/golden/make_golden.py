@@ -15,7 +15,10 @@ oracle/_ref/fcref_dump on it and packs the dump into <case>.npz:
   ref_iterations        GMRES Arnoldi steps per conductor
   ref_counts            panels, nodes, links; ref_max_mesh_eps
 
-Usage: python tests/golden/make_golden.py [reference dir]
+  ref_sup_*             (two-level cases) the reference's super elements,
+                        leaf map, leaf areas and inverse super matrix
+
+Usage: python tests/golden/make_golden.py [reference dir [case ...]]
 """
 
 from __future__ import annotations
@@ -73,6 +76,12 @@ CASES = {
                          ["-m0.02", "-t1e-4", "-pj", "-f0"]),
     "random3": (lambda: geo.random_crossing(3).text(), ["-m0.05", "-t1e-4", "-pj", "-f0"]),
     "merged_cubes": (lambda: TWO_CUBES_MERGED % (_cube_text(), _bar_text()), ["-m0.05", "-t1e-4", "-pj", "-f0"]),
+    # two-level preconditioner (-ps<dim>): conductors only, and with a dielectric interface
+    "crossing2x2_m02_ps64": (lambda: geo.crossing_2x2().text(), ["-m0.02", "-t1e-4", "-ps64", "-f0"]),
+    "crossing2x2_slab_ps32": (lambda: geo.Crossing(k=2, length=10.0, pitch=3.0, gap=1.0, eps_r=3.9,
+                                                   slab=(3.5, 1.0, 3.9, 15.0), name="c2slab").text(),
+                              ["-m0.02", "-t1e-4", "-ps32", "-f0"]),
+    "sphere_d2_ps256": (lambda: geo.sphere_text(2), ["-m1e30", "-d1e-32", "-t1e-4", "-ps256", "-f0"]),
 }
 
 
@@ -114,14 +123,19 @@ def convert(dump: str) -> dict:
         "ref_max_mesh_eps": np.array(meta["max_mesh_eps"]),
         "ref_max_level": np.array(meta["max_level"]),
     }
+    if os.path.exists(os.path.join(dump, "sup_nodes.npy")):
+        out.update({"ref_sup_nodes": L("sup_nodes"), "ref_sup_index": L("sup_index"), "ref_sup_area": L("sup_area"),
+                    "ref_sup_minv": L("sup_minv")})
     return out
 
 
-def main(ref_dir: str = "/root/reference"):
+def main(ref_dir: str = "/root/reference", *only):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + ref_dir], check=True)
     dump_bin = os.path.join(ROOT, "oracle", "_ref", "fcref_dump")
     with tempfile.TemporaryDirectory() as tmp:
         for name, (text_fn, switches) in CASES.items():
+            if only and name not in only:
+                continue
             text = text_fn()
             inp = os.path.join(tmp, name + ".txt")
             with open(inp, "w") as f:
