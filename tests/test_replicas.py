@@ -37,7 +37,7 @@ def _rank_main(rank, world, port, out_dir):
     times = [1.0 + rank, 5.0 - rank]
     mx = replicas.max_over_ranks(times, w)
     # each rank solves its shard of the golden geometries with the oracle
-    from conftest import golden_names, load_golden, model_arrays, solve_params
+    from conftest import golden_names, load_golden, model_arrays, solve_params, super_dim
     from pyoracle import Oracle
     names = golden_names()
     mine = replicas.shard(len(names), r, w)
@@ -47,7 +47,7 @@ def _rank_main(rank, world, port, out_dir):
         o = Oracle(model_arrays(g))
         o.fill()
         tol, pc = solve_params(g)
-        cap, _, _, _ = o.solve(tol, pc)
+        cap, _, _, _ = o.solve(tol, pc, super_dim=super_dim(g))
         caps[names[j]] = cap.tolist()
     total = replicas.sum_over_ranks([len(mine)], w)[0]
     gathered = replicas.gather_to_all({"rank": r, "jobs": mine}, w)
