@@ -164,6 +164,15 @@ struct DeviceProblem {
     int32_t *row_split = NULL;  // multi-right-hand-side link product: CTA b owns rows [row_split[b], row_split[b+1])
     int n_row_split = 0;
 
+    // two-level preconditioner (built for one dimension, kept until another is asked for)
+    int sup_dim = -1;  // dimension it was built for (-1: never built)
+    int sup_m = 0;     // super elements (0: disabled, at least as many conductors as the dimension)
+    int sup_kcap = 0;
+    int32_t *sup_index = NULL;
+    float *sup_area = NULL;
+    int64_t *sup_first = NULL, *sup_count = NULL;
+    double *sup_dimv = NULL, *sup_T = NULL, *sup_diag = NULL, *sup_pot = NULL, *sup_chg = NULL;
+
     // solve geometries (independent models concatenated into one problem)
     int n_geom = 0;
     std::vector<int> geom_cols_ptr;  // cond_cols of geometry g: [geom_cols_ptr[g], geom_cols_ptr[g+1])
@@ -814,6 +823,204 @@ __global__ void __launch_bounds__(256) k_spmv64_multi(const int32_t *__restrict_
         a0 = slot_reduce64<LPL, LPW>(a0, lane, li);
         a1 = slot_reduce64<LPL, LPW>(a1, lane, li);
         if (li == 0) reinterpret_cast<double2 *>(P + (int64_t)row * K)[ri] = make_double2(a0, a1);
+    }
+}
+
+// ---- two-level preconditioner (CSolveCap::MakePreconditioner,
+// ComputeSuperPrecond, InvertMatrix, ComputePrecondVectFast super branch;
+// Solver/SolveCapacitance.cpp:1061-1133, 2007-2066, 2116-2258, 3547-3598)
+
+__global__ void k_node_leafflag(int64_t Nn, const NodeGeo *__restrict__ geo, uint8_t *__restrict__ leaf) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nn; v += (int64_t)gridDim.x * blockDim.x)
+        leaf[v] = (geo[v].type & FCG_IS_LEAF) ? 1 : 0;
+}
+
+// leaf -> element map, leaf areas (single precision, as the reference keeps
+// them), element areas
+__global__ void k_sup_maps(int m, const int32_t *__restrict__ elem, const int64_t *__restrict__ first,
+                           const int64_t *__restrict__ count, const NodeGeo *__restrict__ geo, const int32_t *__restrict__ leaf_node,
+                           int32_t *__restrict__ index, float *__restrict__ area, double *__restrict__ dimv) {
+    int s = blockIdx.x;
+    if (s >= m) return;
+    if (threadIdx.x == 0) dimv[s] = geo[elem[s]].area;
+    for (int64_t j = first[s] + threadIdx.x; j < first[s] + count[s]; j += blockDim.x) {
+        index[j] = s;
+        area[j] = (float)geo[leaf_node[j]].area;
+    }
+}
+
+// super potential matrix A (row-major): self terms on the diagonal, the
+// one-way coefficient of element i's evaluation point due to element j off it
+__global__ void k_sup_matrix(int m, const int32_t *__restrict__ elem, const int64_t *__restrict__ first,
+                             const NodeGeo *__restrict__ geo, const double *__restrict__ leaf_eb, const double *__restrict__ leaf_ea,
+                             double *__restrict__ A) {
+    int64_t n = (int64_t)m * m;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int i = (int)(t / m), j = (int)(t - (int64_t)i * m);
+        const NodeGeo &gi = geo[elem[i]];
+        double v;
+        if (i == j) {
+            if (gi.type & FCG_IS_DIEL) {
+                double eb = leaf_eb[first[i]], ea = leaf_ea[first[i]];
+                v = (ea + eb) / (FCG_TWO_TIMES_E0 * (eb - ea) * gi.area);
+            } else {
+                v = fcg_potential_opt(fcg_widen(gi.c), gi.v) / FCG_FOUR_PI_TIMES_E0;
+            }
+        } else {
+            const NodeGeo &gj = geo[elem[j]];
+            v = fcg_pot_estimate(gi.type, gi.c, gi.n, gi.maxside, gj.c, gj.v, gj.maxside);
+        }
+        A[t] = v;
+    }
+}
+
+// LU step j, part 1 (one CTA): pivot = first row of largest |A[i][j]|, i >= j;
+// swap rows j and pivot; scale the column below the diagonal
+__global__ void k_lu_pivot(int m, int j, double *__restrict__ A, int32_t *__restrict__ piv) {
+    __shared__ double bv[32];
+    __shared__ int bi[32];
+    __shared__ int pv;
+    double best = -1.0;
+    int bidx = m;
+    for (int i = j + threadIdx.x; i < m; i += blockDim.x) {
+        double a = fabs(A[(int64_t)i * m + j]);
+        if (a > best) { best = a; bidx = i; }  // ascending i per thread: first on ties
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (ob > best || (ob == best && oi < bidx)) { best = ob; bidx = oi; }
+    }
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { bv[w] = best; bi[w] = bidx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = bv[0];
+        int bx = bi[0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); q++)
+            if (bv[q] > b || (bv[q] == b && bi[q] < bx)) { b = bv[q]; bx = bi[q]; }
+        if (bx >= m) bx = j;
+        pv = bx;
+        piv[j] = bx;
+    }
+    __syncthreads();
+    int pr = pv;
+    if (pr != j)
+        for (int k = threadIdx.x; k < m; k += blockDim.x) {
+            double t = A[(int64_t)j * m + k];
+            A[(int64_t)j * m + k] = A[(int64_t)pr * m + k];
+            A[(int64_t)pr * m + k] = t;
+        }
+    __syncthreads();
+    if (j < m - 1) {
+        double r = 1.0 / A[(int64_t)j * m + j];
+        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) A[(int64_t)i * m + j] *= r;
+    }
+}
+
+// LU step j, part 2: rank-1 update of the trailing block
+__global__ void k_lu_update(int m, int j, double *__restrict__ A) {
+    int64_t w = m - j - 1, n = w * w;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = j + 1 + t / w, k = j + 1 + t % w;
+        A[i * m + k] -= A[i * m + j] * A[(int64_t)j * m + k];
+    }
+}
+
+// X = the identity with the factorisation's row swaps applied (one CTA)
+__global__ void k_perm_identity(int m, const int32_t *__restrict__ piv, int32_t *__restrict__ idx, double *__restrict__ X) {
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < m; i++) idx[i] = i;
+        for (int i = 0; i < m; i++) {
+            int t = idx[i];
+            idx[i] = idx[piv[i]];
+            idx[piv[i]] = t;
+        }
+    }
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t < (int64_t)m * m; t += blockDim.x) {
+        int i = (int)(t / m), k = (int)(t % m);
+        X[t] = idx[i] == k ? 1.0 : 0.0;
+    }
+}
+
+// forward substitution step i (unit lower factor): rows below i lose L[r][i] * row i
+__global__ void k_inv_forward(int m, int i, const double *__restrict__ A, double *__restrict__ X) {
+    int64_t n = (int64_t)(m - i - 1) * m;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = i + 1 + t / m, k = t % m;
+        X[r * m + k] -= A[r * m + i] * X[(int64_t)i * m + k];
+    }
+}
+
+// backward substitution step i: row i is divided by U[i][i], rows above lose U[r][i] * row i
+__global__ void k_inv_scale(int m, int i, const double *__restrict__ A, double *__restrict__ X) {
+    double d = A[(int64_t)i * m + i];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) X[(int64_t)i * m + k] /= d;
+}
+__global__ void k_inv_backward(int m, int i, const double *__restrict__ A, double *__restrict__ X) {
+    int64_t n = (int64_t)i * m;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = t / m, k = t % m;
+        X[r * m + k] -= A[r * m + i] * X[(int64_t)i * m + k];
+    }
+}
+
+// T = X transposed (column-major inverse, coalesced in the product), its
+// diagonal, and a count of non-finite entries
+__global__ void k_inv_finish(int m, const double *__restrict__ X, double *__restrict__ T, double *__restrict__ diag, unsigned *bad) {
+    int64_t n = (int64_t)m * m;
+    unsigned nb = 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = t / m, k = t % m;
+        double v = X[t];
+        if (!isfinite(v)) nb++;
+        T[k * m + r] = v;
+        if (r == k) diag[r] = v;
+    }
+    if (nb) atomicAdd(bad, nb);
+}
+
+// apply, step 1: pot[r][s] = sum over element s's leaves (leaf order) of q * area / dim
+__global__ void k_sup_collect(int m, int k, int64_t Np, const int64_t *__restrict__ first, const int64_t *__restrict__ count,
+                              const float *__restrict__ area, const double *__restrict__ dimv, const double *__restrict__ in,
+                              double *__restrict__ pot) {
+    int64_t n = (int64_t)m * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int s = (int)(t % m), r = (int)(t / m);
+        const double *q = in + (int64_t)r * Np;
+        double acc = 0.0, d = dimv[s];
+        for (int64_t j = first[s]; j < first[s] + count[s]; j++) acc += q[j] * (double)area[j] / d;
+        pot[t] = acc;
+    }
+}
+
+// step 2: chg[r][s] = sum over k != s (ascending) of Minv[s][k] * pot[r][k]
+__global__ void k_sup_mult(int m, int k, const double *__restrict__ T, const double *__restrict__ pot, double *__restrict__ chg) {
+    int64_t n = (int64_t)m * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int s = (int)(t % m), r = (int)(t / m);
+        const double *pr = pot + (int64_t)r * m;
+        double acc = 0.0;
+        for (int q = 0; q < m; q++)
+            if (q != s) acc += T[(int64_t)q * m + s] * pr[q];
+        chg[t] = acc;
+    }
+}
+
+// step 3: out = chg * area / dim + Minv[s][s] * q * area / dim per leaf
+__global__ void k_sup_spread(int m, int k, int64_t Np, const int32_t *__restrict__ index, const float *__restrict__ area,
+                             const double *__restrict__ dimv, const double *__restrict__ diag, const double *__restrict__ chg,
+                             const double *__restrict__ in, double *__restrict__ out) {
+    int64_t n = (int64_t)k * Np;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / Np);
+        int64_t j = t - (int64_t)r * Np;
+        int s = index[j];
+        double a = (double)area[j], d = dimv[s];
+        double v = chg[(int64_t)r * m + s] * a / d;
+        v += diag[s] * in[t] * a / d;
+        out[t] = v;
     }
 }
 
@@ -1539,6 +1746,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
 }
 
 static void free_solve_ws(DeviceProblem *p);
+static void free_two_level(DeviceProblem *p);
 
 void problem_destroy(DeviceProblem *p) {
     if (!p) return;
@@ -1556,6 +1764,7 @@ void problem_destroy(DeviceProblem *p) {
     free_solve_ws(p);
     dfree(p->partial);
     dfree(p->leaf_geom); dfree(p->ch_start); dfree(p->ch_len); dfree(p->ch_geom); dfree(p->g_ch_first); dfree(p->g_ch_count);
+    free_two_level(p);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     for (size_t i = 0; i < p->ev_pool.size(); i++) cudaEventDestroy(p->ev_pool[i]);
@@ -2128,6 +2337,150 @@ static double *basis_addr(DeviceProblem *p, int j) {
     return p->V[head] + (size_t)(j - head) * p->gk * p->Np;
 }
 
+static void free_two_level(DeviceProblem *p) {
+    dfree(p->sup_index); dfree(p->sup_area); dfree(p->sup_first); dfree(p->sup_count);
+    dfree(p->sup_dimv); dfree(p->sup_T); dfree(p->sup_diag); dfree(p->sup_pot); dfree(p->sup_chg);
+    p->sup_m = 0;
+    p->sup_kcap = 0;
+    p->sup_dim = -1;
+}
+
+// Build the two-level preconditioner of dimension dim (clamped to
+// [16, 4096]). Super elements: in every conductor's tree, the nodes at depth
+// log2(dim / conductors) and the leaves above that depth, in leaf order. With
+// at least dim conductors it is disabled (sup_m = 0) and the solve runs
+// without preconditioner, as the reference does.
+static int build_two_level(DeviceProblem *p, int dim) {
+    if (dim <= 0) dim = 128;  // the reference's default dimension
+    if (dim > 4096) dim = 4096;
+    if (dim < 16) dim = 16;
+    if (p->sup_dim == dim) return FCG_NORMAL_END;
+    free_two_level(p);
+    unsigned roots = (unsigned)p->n_cond_all;
+    if (roots >= (unsigned)dim) {
+        p->sup_dim = dim;
+        return FCG_NORMAL_END;
+    }
+    int lev = (int)(unsigned)(log((double)((unsigned)dim / roots)) / log(2.0));
+    cudaStream_t s = p->stream;
+    int64_t Nn = p->Nn, Np = p->Np, tb = 0;
+    int sms = p->ctx->sm_count;
+    int r;
+    // tree shape on the host: parents (device labels; a parent's label is
+    // larger than its children's), first leaves, leaf flags
+    std::vector<int32_t> par(Nn);
+    std::vector<int64_t> lf(Nn);
+    std::vector<uint8_t> leaf(Nn);
+    uint8_t *d_leaf = NULL;
+    if ((r = dalloc(&d_leaf, Nn, tb))) return r;
+    k_node_leafflag<<<grid_for(Nn, 256, sms), 256, 0, s>>>(Nn, p->geo, d_leaf);
+    if (cudaMemcpyAsync(par.data(), p->parent, Nn * sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(lf.data(), p->node_lfirst, Nn * sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(leaf.data(), d_leaf, Nn, cudaMemcpyDeviceToHost, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+        dfree(d_leaf);
+        set_error("reading the tree for the two-level preconditioner failed");
+        return FCG_DEVICE_ERROR;
+    }
+    dfree(d_leaf);
+    std::vector<int32_t> depth(Nn, 0);
+    int64_t nroots = 0;
+    for (int64_t v = Nn - 1; v >= 0; v--) {
+        if (par[v] < 0) { nroots++; continue; }
+        depth[v] = depth[par[v]] + 1;
+    }
+    if (nroots != (int64_t)roots) {
+        set_error("two-level preconditioner: every conductor must have one tree");
+        return FCG_GENERIC_ERROR;
+    }
+    std::vector<std::pair<int64_t, int32_t>> sel;
+    for (int64_t v = 0; v < Nn; v++)
+        if ((leaf[v] && depth[v] <= lev) || (!leaf[v] && depth[v] == lev)) sel.push_back(std::make_pair(lf[v], (int32_t)v));
+    std::sort(sel.begin(), sel.end());
+    int m = (int)sel.size();
+    std::vector<int32_t> elem(m);
+    std::vector<int64_t> first(m), count(m);
+    for (int i = 0; i < m; i++) {
+        elem[i] = sel[i].second;
+        first[i] = sel[i].first;
+        count[i] = (i + 1 < m ? sel[i + 1].first : Np) - sel[i].first;
+    }
+    int32_t *d_elem = NULL, *d_piv = NULL, *d_idx = NULL;
+    double *A = NULL, *X = NULL;
+    unsigned *d_bad = NULL, bad = 0;
+    int64_t &B = p->bytes;
+    if ((r = upload(&d_elem, elem.data(), m, tb, s)) || (r = upload(&p->sup_first, first.data(), m, B, s)) ||
+        (r = upload(&p->sup_count, count.data(), m, B, s)) || (r = dalloc(&p->sup_index, Np, B)) ||
+        (r = dalloc(&p->sup_area, Np, B)) || (r = dalloc(&p->sup_dimv, m, B)) || (r = dalloc(&p->sup_T, (size_t)m * m, B)) ||
+        (r = dalloc(&p->sup_diag, m, B)) || (r = dalloc(&A, (size_t)m * m, tb)) || (r = dalloc(&X, (size_t)m * m, tb)) ||
+        (r = dalloc(&d_piv, m, tb)) || (r = dalloc(&d_idx, m, tb)) || (r = dalloc(&d_bad, 1, tb))) {
+        dfree(d_elem); dfree(A); dfree(X); dfree(d_piv); dfree(d_idx); dfree(d_bad);
+        free_two_level(p);
+        return r;
+    }
+    int64_t mm = (int64_t)m * m;
+    k_sup_maps<<<m, 128, 0, s>>>(m, d_elem, p->sup_first, p->sup_count, p->geo, p->leaf_node, p->sup_index, p->sup_area,
+                                 p->sup_dimv);
+    k_sup_matrix<<<grid_for(mm, 128, sms), 128, 0, s>>>(m, d_elem, p->sup_first, p->geo, p->leaf_eb, p->leaf_ea, A);
+    for (int j = 0; j < m; j++) {
+        k_lu_pivot<<<1, 1024, 0, s>>>(m, j, A, d_piv);
+        if (j < m - 1) k_lu_update<<<grid_for((int64_t)(m - j - 1) * (m - j - 1), 256, sms), 256, 0, s>>>(m, j, A);
+    }
+    k_perm_identity<<<1, 1024, 0, s>>>(m, d_piv, d_idx, X);
+    for (int i = 0; i < m - 1; i++) k_inv_forward<<<grid_for((int64_t)(m - i - 1) * m, 256, sms), 256, 0, s>>>(m, i, A, X);
+    for (int i = m - 1; i >= 0; i--) {
+        k_inv_scale<<<(m + 255) / 256, 256, 0, s>>>(m, i, A, X);
+        if (i > 0) k_inv_backward<<<grid_for((int64_t)i * m, 256, sms), 256, 0, s>>>(m, i, A, X);
+    }
+    cudaMemsetAsync(d_bad, 0, sizeof(unsigned), s);
+    k_inv_finish<<<grid_for(mm, 256, sms), 256, 0, s>>>(m, X, p->sup_T, p->sup_diag, d_bad);
+    p->timings.launches += 4 + 2 * (int64_t)m + (m - 1) + 2 * (int64_t)m;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dfree(d_elem); dfree(A); dfree(X); dfree(d_piv); dfree(d_idx); dfree(d_bad);
+    if (e != cudaSuccess) {
+        free_two_level(p);
+        set_error(std::string("two-level preconditioner setup failed: ") + cudaGetErrorString(e));
+        return FCG_DEVICE_ERROR;
+    }
+    if (bad) {
+        free_two_level(p);
+        set_error("two-level preconditioner: the super potential matrix is singular");
+        return FCG_GENERIC_ERROR;
+    }
+    p->sup_m = m;
+    p->sup_dim = dim;
+    return FCG_NORMAL_END;
+}
+
+// out = P in for k columns ([k][Np]): Jacobi (diag), two-level, or a copy
+static int precond_apply(DeviceProblem *p, int kind, const double *in, double *out, int k) {
+    cudaStream_t s = p->stream;
+    int64_t Np = p->Np;
+    int sms = p->ctx->sm_count;
+    int g1 = grid_for((int64_t)k * Np, 256, sms);
+    if (kind == FCG_PRECOND_TWO_LEVEL) {
+        int m = p->sup_m, r;
+        if (p->sup_kcap < k) {
+            dfree(p->sup_pot);
+            dfree(p->sup_chg);
+            p->sup_kcap = 0;
+            if ((r = dalloc(&p->sup_pot, (size_t)m * k, p->bytes)) || (r = dalloc(&p->sup_chg, (size_t)m * k, p->bytes))) return r;
+            p->sup_kcap = k;
+        }
+        int gm = grid_for((int64_t)m * k, 128, sms);
+        k_sup_collect<<<gm, 128, 0, s>>>(m, k, Np, p->sup_first, p->sup_count, p->sup_area, p->sup_dimv, in, p->sup_pot);
+        k_sup_mult<<<gm, 128, 0, s>>>(m, k, p->sup_T, p->sup_pot, p->sup_chg);
+        k_sup_spread<<<g1, 256, 0, s>>>(m, k, Np, p->sup_index, p->sup_area, p->sup_dimv, p->sup_diag, p->sup_chg, in, out);
+        p->timings.launches += 3;
+    } else {
+        k_precond<<<g1, 256, 0, s>>>(Np, k, in, kind == FCG_PRECOND_JACOBI ? p->self : NULL, out);
+        p->timings.launches++;
+    }
+    FCG_CK(cudaGetLastError());
+    return FCG_NORMAL_END;
+}
+
 int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations) {
     AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
@@ -2157,7 +2510,20 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         gcap[g] = (int)std::max<int64_t>(c, 1);
         M = std::max(M, gcap[g]);
     }
-    const double *diag = (opt.precond == FCG_PRECOND_JACOBI) ? p->self : NULL;
+    // preconditioner: Jacobi is fused into the product's up-sweep; the
+    // two-level one is applied before it (and falls back to none when there
+    // are at least as many conductors as its dimension, as in the reference)
+    int pk = opt.precond;
+    if (pk != FCG_PRECOND_NONE && pk != FCG_PRECOND_JACOBI && pk != FCG_PRECOND_TWO_LEVEL) {
+        set_error("unknown preconditioner");
+        return FCG_GENERIC_ERROR;
+    }
+    if (pk == FCG_PRECOND_TWO_LEVEL) {
+        if ((r = build_two_level(p, opt.precond_dim))) return r;
+        if (p->sup_m == 0) pk = FCG_PRECOND_NONE;
+    }
+    const double *diag = (pk == FCG_PRECOND_JACOBI) ? p->self : NULL;
+    const bool pre = pk != FCG_PRECOND_NONE;
     cudaStream_t s = p->stream;
     int sms = p->ctx->sm_count;
     SegChunks chunks = {p->ch_start, p->ch_len, p->ch_geom, nch};
@@ -2227,9 +2593,12 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         k_set_rhs<<<g1, 256, 0, s>>>(Np, k, p->leaf_geom, d_sf, d_sc, p->b);
         double *V0 = basis_addr(p, 0);
         double *pr = p->partial, *pb = p->partial + (size_t)k * nch;
-        if (diag) {
-            k_precond<<<g1, 256, 0, s>>>(Np, k, p->b, diag, p->x0);
-            if ((r = matvec(p, p->x0, p->w, k, NULL))) { free_batch(); status = r; break; }
+        if (pre) {
+            if ((r = precond_apply(p, pk, p->b, p->x0, k)) || (r = matvec(p, p->x0, p->w, k, NULL))) {
+                free_batch();
+                status = r;
+                break;
+            }
             k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, chunks, p->vv, pr, pb);
         } else {
             FCG_CK(cudaMemsetAsync(p->x0, 0, n * sizeof(double), s));
@@ -2243,7 +2612,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
                                         p->capped, p->n_active + M + 1);
         k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0);
         FCG_CK(cudaGetLastError());
-        p->timings.launches += diag ? 8 : 7;
+        p->timings.launches += pre ? 7 : 7;
         // does any solve need an Arnoldi step?
         int *pin = p->pin ? p->pin : p->pin_local;
         FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -2254,7 +2623,12 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             double *Vi = basis_addr(p, i), *Vn = basis_addr(p, i + 1);
             double *hcol = p->Hc[i];
             // w = A P q_i
-            if ((r = matvec(p, Vi, p->w, k, diag))) { status = r; break; }
+            if (pk == FCG_PRECOND_TWO_LEVEL) {
+                if ((r = precond_apply(p, pk, Vi, p->vv, k)) || (r = matvec(p, p->vv, p->w, k, NULL))) { status = r; break; }
+            } else if ((r = matvec(p, Vi, p->w, k, diag))) {
+                status = r;
+                break;
+            }
             // classical Gram-Schmidt against q_0..q_i, per solve
             k_dots<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, chunks, k, p->active, p->partial);
             k_reduce_seg<<<seg_grid(i + 1), 256, 0, s>>>(i + 1, k, G, nch, p->partial, p->g_ch_first, p->g_ch_count, p->active,
@@ -2276,7 +2650,12 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         if (status != FCG_NORMAL_END) { free_batch(); break; }
         k_backsub<<<gs, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
         k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
-        k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->leaf_geom, p->x);
+        if (pk == FCG_PRECOND_TWO_LEVEL) {
+            if ((r = precond_apply(p, pk, p->w, p->vv, k))) { free_batch(); status = r; break; }
+            k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->vv, NULL, p->iters, p->leaf_geom, p->x);
+        } else {
+            k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->leaf_geom, p->x);
+        }
         cudaEventRecord(p->ev1, s);
         if (nentry > 0) {
             k_assemble_part<<<dim3(nentry, nslice), 256, 0, s>>>(Np, d_es, d_ef, d_ec, p->leaf_weight, p->x, d_part);

@@ -262,6 +262,7 @@ int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap,
     o.precond = FCG_PRECOND_JACOBI;
     o.max_iter = 0;
     o.rhs_width = 0;
+    o.precond_dim = 0;
     if (opt) o = *opt;
     return fcg::problem_solve(p->p, o, cap, iterations);
 }
@@ -409,15 +410,31 @@ extern "C" int fcg_run_command_line(const char *command_line) {
     if (!command_line || parse_cmd(command_line, o, err)) {
         printf("%s\n", err.c_str());
         printf("Usage: fastercap_gb300 <input file> [-m<mesh>] [-mc<mesh curvature>] [-t<tolerance>] [-d<interaction coeff>]\n");
-        printf("                       [-pj|-pn] [-i] [-v] [-x64|-xm]\n");
+        printf("                       [-pj|-pn|-ps<dim>] [-i] [-v] [-x64|-xm]\n");
         return FCG_COMMAND_LINE_ERROR;
     }
     if (o.galerkin) { printf("Error: the Galerkin scheme (-g) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
     if (o.automatic) { printf("Error: automatic mode (-a) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
-    if (o.precond & ~FCG_PRECOND_JACOBI) {
-        printf("Error: only the Jacobi preconditioner (-pj) or none (-pn) is supported by the GPU solver\n");
+    if (o.precond & (2 | 8)) {
+        printf("Error: the block (-pb) and hierarchical (-ph) preconditioners are not supported by the GPU solver\n");
         return FCG_COMMAND_LINE_ERROR;
     }
+    // CSolveCap::Run's option checks (Solver/SolveCapacitance.cpp:122-147)
+    if ((o.precond & 4) && (o.precond & FCG_PRECOND_JACOBI)) {
+        o.precond = 4;
+        printf("Warning: both two-levels preconditioner and Jacobi preconditioner specified, keeping only the two-levels preconditioner\n");
+    }
+    if (o.precond & 4) {
+        if (o.super_dim > 4096) {
+            o.super_dim = 4096;
+            printf("Warning: maximum two-levels preconditioner dimension is 4096, using 4096\n");
+        } else if (o.super_dim < 16) {
+            o.super_dim = 16;
+            printf("Warning: minimum two-levels preconditioner dimension is 16, using 16\n");
+        }
+    }
+    const int precond_kind = (o.precond & 4) ? FCG_PRECOND_TWO_LEVEL : (o.precond & FCG_PRECOND_JACOBI) ? FCG_PRECOND_JACOBI
+                                                                                                       : FCG_PRECOND_NONE;
     printf("Running fastercap_gb300 (GB300 solve path for FasterCap input files)\n");
     printf("Input file: %s\n", o.file.c_str());
     auto t0 = std::chrono::steady_clock::now();
@@ -430,7 +447,8 @@ extern "C" int fcg_run_command_line(const char *command_line) {
     fcg_model_info info;
     fcg_model_info_get(m, &info);
     printf("Mesh refinement (-m): %g\nGMRES tolerance (-t): %g\n", o.mesh_eps, o.gmres_tol);
-    printf("Precond Type(s) (-p): %s\n", o.precond == FCG_PRECOND_JACOBI ? "Jacobi" : "None");
+    if (precond_kind == FCG_PRECOND_TWO_LEVEL) printf("Precond Type(s) (-p): Two-levels, dimension %u\n", o.super_dim);
+    else printf("Precond Type(s) (-p): %s\n", precond_kind == FCG_PRECOND_JACOBI ? "Jacobi" : "None");
     printf("Number of input panels to solver engine: %lld\n", (long long)info.input_panels);
     printf("Number of panels after refinement: %lld\n", (long long)info.n_panels);
     printf("Number of links to be computed: %lld\n", (long long)info.n_links);
@@ -448,7 +466,7 @@ extern "C" int fcg_run_command_line(const char *command_line) {
         nc = info.n_conductors - info.n_dielectrics;
         cap.resize((size_t)nc * nc);
         iters.resize(nc);
-        fcg_solve_options so = {o.gmres_tol, o.precond, 0, 0};
+        fcg_solve_options so = {o.gmres_tol, precond_kind, 0, 0, (int)o.super_dim};
         r = fcg_problem_solve(p, &so, cap.data(), iters.data());
     }
     auto t2 = std::chrono::steady_clock::now();

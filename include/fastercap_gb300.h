@@ -40,6 +40,7 @@ extern "C" {
 /* preconditioners (Solver/SolverGlobal.h:62-68) */
 #define FCG_PRECOND_NONE 0
 #define FCG_PRECOND_JACOBI 1
+#define FCG_PRECOND_TWO_LEVEL 2 /* -ps<dim>: the reference's two-level (super) preconditioner */
 
 /* arithmetic of the link coefficients and the link product */
 #define FCG_PREC_FP64 0  /* FP64 coefficients, FP64 sums */
@@ -167,9 +168,10 @@ int fcg_problem_matvec_device_noalloc(fcg_problem *p, const double *d_q, double 
 /* GMRES options: -t and -p of the reference command line. */
 typedef struct {
     double tol;       /* -t GMRES relative residual tolerance (default 0.01) */
-    int precond;      /* FCG_PRECOND_NONE or FCG_PRECOND_JACOBI */
+    int precond;      /* FCG_PRECOND_NONE, FCG_PRECOND_JACOBI or FCG_PRECOND_TWO_LEVEL */
     int max_iter;     /* 0: the reference's cap min(1000, n_panels) */
     int rhs_width;    /* right-hand sides per batched solve: 0 = up to 32, 1 = one at a time */
+    int precond_dim;  /* two-level dimension (the number of -ps<dim>), clamped to [16, 4096]; 0 = 128 */
 } fcg_solve_options;
 
 /* Declare that the problem holds several independent geometries: conductor c
@@ -188,8 +190,11 @@ int fcg_problem_set_geometries(fcg_problem *p, int32_t n_geometries, const int32
  * conductors in solver order; iterations receives the Arnoldi step count of
  * every right-hand side (may be NULL). Replaces CSolveCap::Solve
  * (Solver/SolveCapacitance.cpp:1138-1425) with gmresPrecondSFastAll
- * (Solver/SolveCapacitance.cpp:2288-2574) and the Jacobi branch of
- * ComputePrecondVectFast (Solver/SolveCapacitance.cpp:3489-3526). */
+ * (Solver/SolveCapacitance.cpp:2288-2574), the Jacobi and two-level branches
+ * of ComputePrecondVectFast (Solver/SolveCapacitance.cpp:3489-3526, 3547-3598)
+ * and, for the two-level preconditioner, MakePreconditioner /
+ * ComputeSuperPrecond / InvertMatrix (Solver/SolveCapacitance.cpp:1061-1133,
+ * 2007-2066, 2116-2258), built on the first solve that asks for it. */
 int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap, int *iterations);
 /* the charge vectors of the last batch of right-hand sides, [k][n_panels]
  * (k = the conductors of that batch, all of them up to 32) */

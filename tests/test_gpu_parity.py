@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import fastercap_gb300 as fc
-from conftest import build_from_golden, load_golden, model_arrays, solve_params
+from conftest import build_from_golden, load_golden, model_arrays, solve_params, super_dim
 from pyoracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -75,7 +75,7 @@ def test_solve_fp64_matches_reference(ctx, golden):
     tol, precond = solve_params(g)
     p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_FP64)
     p.fill()
-    cap, it = p.solve(tol=tol, precond=precond)
+    cap, it = p.solve(tol=tol, precond=precond, precond_dim=super_dim(g))
     np.testing.assert_allclose(cap, g["ref_cap"], rtol=1e-6, atol=0)
     np.testing.assert_array_equal(it, g["ref_iterations"])
 
@@ -85,7 +85,7 @@ def test_solve_mixed_within_tenth_percent(ctx, golden):
     tol, precond = solve_params(g)
     p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_MIXED)
     p.fill()
-    cap, it = p.solve(tol=tol, precond=precond)
+    cap, it = p.solve(tol=tol, precond=precond, precond_dim=super_dim(g))
     err = np.abs(cap - g["ref_cap"]) / np.abs(g["ref_cap"])
     assert err.max() < 1e-3, err.max()
 
@@ -97,7 +97,7 @@ def test_builder_to_gpu_end_to_end(ctx, golden, tmp_path):
     m = build_from_golden(g, tmp_path)
     p = ctx.problem(m, fc.PREC_FP64)
     p.fill()
-    cap, it = p.solve(tol=tol, precond=precond)
+    cap, it = p.solve(tol=tol, precond=precond, precond_dim=super_dim(g))
     np.testing.assert_allclose(cap, g["ref_cap"], rtol=1e-6, atol=0)
 
 
@@ -141,3 +141,24 @@ def test_invalid_link_source_rejected(ctx):
     assert "out of range" in str(e.value)
     p = ctx.problem(fc.Model.from_arrays(a), fc.PREC_FP64)  # the context still works
     p.fill()
+
+
+def test_two_level_disabled_with_many_conductors(ctx, tmp_path):
+    """With at least as many conductors as the dimension the two-level
+    preconditioner is dropped (no preconditioner), as in the reference."""
+    from fastercap_gb300 import geometry as geo
+    path = tmp_path / "c8.txt"
+    geo.Crossing(k=8, length=20.0, pitch=2.0, gap=1.0, name="c8").write(str(path))
+    m = fc.Model.build(str(path), mesh_eps=0.5)
+    p = ctx.problem(m, fc.PREC_FP64)
+    p.fill()
+    c2, i2 = p.solve(tol=1e-3, precond=fc.PRECOND_TWO_LEVEL, precond_dim=16)
+    c0, i0 = p.solve(tol=1e-3, precond=fc.PRECOND_NONE)
+    np.testing.assert_array_equal(c2, c0)
+    np.testing.assert_array_equal(i2, i0)
+    o = Oracle(m.arrays)
+    o.fill()
+    c3, i3, _, _ = o.solve(1e-3, 2, super_dim=64)
+    c4, i4 = p.solve(tol=1e-3, precond=fc.PRECOND_TWO_LEVEL, precond_dim=64)
+    np.testing.assert_allclose(c4, c3, rtol=1e-6)
+    np.testing.assert_array_equal(i4, i3)
