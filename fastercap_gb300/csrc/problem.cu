@@ -603,11 +603,23 @@ __global__ void k_spmv64(int64_t Nn, const int64_t *__restrict__ ptr, const uint
                 for (int r = 0; r < K; r++) acc[r] += c[u] * q[r];
             }
         }
-        for (; l < e; l += SW) {
-            double c = __ldcs(&coef[l]);
-            const double *q = Q + (int64_t)(__ldcs(&src[l]) & kSrcMask) * K;
+        if (l < e) {
+            double c[4];
+            uint32_t j[4];
 #pragma unroll
-            for (int r = 0; r < K; r++) acc[r] += c * q[r];
+            for (int u = 0; u < 4; u++) {
+                bool ok = l + SW * u < e;
+                c[u] = ok ? __ldcs(&coef[l + SW * u]) : 0.0;
+                j[u] = ok ? (__ldcs(&src[l + SW * u]) & kSrcMask) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (l + SW * u < e) {
+                    const double *q = Q + (int64_t)j[u] * K;
+#pragma unroll
+                    for (int r = 0; r < K; r++) acc[r] += c[u] * q[r];
+                }
+            }
         }
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -694,12 +706,26 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
                 for (int r = 0; r < K; r++) kmul_add(acc[r], c[u], q[r]);
             }
         }
-        for (; l < e; l += SW) {
-            float c = __ldcs(&coef[l]);
-            float q[K];
-            load_q<K>(Q, __ldcs(&src[l]) & kSrcMask, q);
+        if (l < e) {
+            // the rest of the row (fewer than 4 links per lane): every load
+            // is issued before the first charge is used, as in the loop
+            float c[4];
+            uint32_t j[4];
 #pragma unroll
-            for (int r = 0; r < K; r++) kmul_add(acc[r], c, q[r]);
+            for (int u = 0; u < 4; u++) {
+                bool ok = l + SW * u < e;
+                c[u] = ok ? __ldcs(&coef[l + SW * u]) : 0.f;
+                j[u] = ok ? (__ldcs(&src[l + SW * u]) & kSrcMask) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (l + SW * u < e) {
+                    float q[K];
+                    load_q<K>(Q, j[u], q);
+#pragma unroll
+                    for (int r = 0; r < K; r++) kmul_add(acc[r], c[u], q[r]);
+                }
+            }
         }
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -1724,7 +1750,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     // lanes per node in the link product: about four links per lane per pass
     {
         double avg = (double)a.n_links / (double)Nn;
-        p->spmv_lanes = avg < 48.0 ? 8 : (avg < 96.0 ? 16 : 32);
+        p->spmv_lanes = avg < 40.0 ? 8 : (avg < 160.0 ? 16 : 32);
         const char *env = getenv("FCG_SPMV_LANES");
         if (env && (atoi(env) == 8 || atoi(env) == 16 || atoi(env) == 32)) p->spmv_lanes = atoi(env);
     }
