@@ -68,7 +68,7 @@ MULTI = {
 # DRAM bytes per link-product launch (dram__bytes_read.sum +
 # dram__bytes_write.sum) from one ncu capture of the same kernel and workload
 LINK_TRAFFIC = {
-    "sphere_327680": 531.318272e6 + 4.354048e6,    # k_spmv32<1, 32>
+    "sphere_327680": 531.318272e6 + 4.354048e6,    # k_spmv32<1, 32> (16 lanes move the same bytes)
     "crossing8x8_slab": 679.950848e6 + 7.460608e6,  # k_spmv32_multi<16>
 }
 
@@ -306,11 +306,17 @@ def run_gb300_multi(args, rank, world, local_rank):
     prob.set_geometries(geom)
     time_steps_multi(prob, stream, args.warmup, tol, flush, torch)
     prob.reset_stats()
-    prob.set_profiling(True)
     barrier()
     with ClockSampler(local_rank) as clk:
         times, caps_m, its_m = time_steps_multi(prob, stream, args.steps, tol, flush, torch)
     barrier()
+    st_timed = prob.stats()
+    # link-product roofline: the same steps again with CUDA events around
+    # every link-product launch (the timed steps run each Arnoldi loop as one
+    # CUDA graph, which cannot bracket single kernels)
+    prob.reset_stats()
+    prob.set_profiling(True)
+    time_steps_multi(prob, stream, max(1, min(args.steps, 3)), tol, flush, torch)
     st = prob.stats()
     prob.set_profiling(False)
     total_ms = sum(times)
@@ -393,9 +399,10 @@ def run_gb300_multi(args, rank, world, local_rank):
         "accuracy": {"iterations_min_max": [int(it_all.min()), int(it_all.max())]},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "p50_ms": float(np.percentile(e2e_times, 50))},
-        "gpu_launches": int(st["kernel_launches"]),
-        "phases": {"fill_ms_last": st["fill_ms"], "solve_ms_last": st["solve_ms"]},
+        "gpu_launches": int(st_timed["kernel_launches"]),
+        "phases": {"fill_ms_last": st_timed["fill_ms"], "solve_ms_last": st_timed["solve_ms"]},
         "roofline": {"kernel": "link product (k_spmv32_multi)", "bound": "hbm",
+                     "timing": "CUDA events around every link-product launch, steps re-run after the timed region",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
                      "traffic": None, "launches": int(st["link_launches"]),
@@ -652,14 +659,20 @@ def run_gb300(args, rank, world, local_rank):
     prob = ctx.problem(model, fc.PREC_MIXED)
     time_steps(prob, stream, args.warmup, tol, flush, torch)
     prob.reset_stats()
-    prob.set_profiling(True)
     barrier()
     with ClockSampler(local_rank) as clk:
         times, cap_m, it_m = time_steps(prob, stream, args.steps, tol, flush, torch)
     barrier()
+    st_timed = prob.stats()
+    phase = {"fill_ms_last": st_timed["fill_ms"], "solve_ms_last": st_timed["solve_ms"]}
+    # link-product roofline: the same steps again with CUDA events around
+    # every link-product launch (the timed steps run each Arnoldi loop as one
+    # CUDA graph, which cannot bracket single kernels)
+    prob.reset_stats()
+    prob.set_profiling(True)
+    time_steps(prob, stream, args.steps, tol, flush, torch)
     st = prob.stats()
     prob.set_profiling(False)
-    phase = {"fill_ms_last": st["fill_ms"], "solve_ms_last": st["solve_ms"]}
     total_ms = sum(times)
     # plain FP64 path on the same model
     p64 = ctx.problem(model, fc.PREC_FP64)
@@ -714,10 +727,11 @@ def run_gb300(args, rank, world, local_rank):
                      "iterations": [int(x) for x in it_m]},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "p50_ms": float(np.percentile(e2e_times, 50))},
-        "gpu_launches": int(st["kernel_launches"]),
+        "gpu_launches": int(st_timed["kernel_launches"]),
         "phases": phase,
-        "roofline": {"kernel": "k_spmv32<1, 32> (link product)" if len(model.conductor_names) == 1
+        "roofline": {"kernel": "k_spmv32<1, lanes> (link product)" if len(model.conductor_names) == 1
                      else "k_spmv32_multi (link product)", "bound": "hbm",
+                     "timing": "CUDA events around every link-product launch, same steps re-run after the timed region",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
                      "traffic": LINK_TRAFFIC.get(args.workload), "launches": int(st["link_launches"]),

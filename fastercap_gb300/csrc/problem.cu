@@ -194,6 +194,15 @@ struct DeviceProblem {
     size_t partial_cap = 0;
     int *active = NULL, *iters = NULL, *capped = NULL, *scap = NULL, *n_active = NULL;
     int *pin = NULL;  // pinned readback slot from the context (NULL: pageable fallback)
+    int *pin_dev = NULL;  // the same slot as the device sees it (NULL: no device access)
+    int *d_it = NULL;     // device step state: [0] step index, [1] go on, [2] active solves after the step
+    double *ptmp = NULL;  // two-level preconditioner output ([k][Np])
+    // the Arnoldi loop as one CUDA graph (a while node whose body is one step)
+    cudaGraph_t graph = NULL;
+    cudaGraphExec_t gexec = NULL;
+    std::vector<unsigned char> gkey;
+    int g_launches = 0, g_link_launches = 0;
+    int64_t g_link_bytes = 0;
     int pin_local[kPinSlotInts];
     std::atomic<int> cancel{0};  // set by fcg_problem_cancel; checked between Arnoldi steps
     double *b = NULL, *x0 = NULL, *w = NULL, *vv = NULL, *x = NULL;
@@ -1101,10 +1110,11 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // partial[(r*nvec + j)*nch + c] = <Vj[r], w[r]> over chunk c; the chunk of w
 // stays in registers, basis vectors are taken eight at a time with one block
 // reduction per group of eight.
-__global__ void k_dots(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w, SegChunks ch, int ks,
-                       const int *__restrict__ active, double *__restrict__ partial) {
+__global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
+                       SegChunks ch, int ks, const int *__restrict__ active, double *__restrict__ partial) {
     __shared__ double sh[8][8];
     const int T = 8;
+    const int nvec = *iter + 1;
     int r = blockIdx.y, c = blockIdx.x;
     if (!active[ch.geom[c] * ks + r]) return;
     int64_t base = ch.start[c];
@@ -1167,14 +1177,15 @@ __global__ void k_reduce_seg(int nvec, int ks, int G, int nch, const double *__r
 }
 
 // v[r] = w[r] - sum_j h_j V_j[r] with the solve's own h; partial |v|^2 per chunk
-__global__ void k_update(int64_t Np, int nvec, double *const *__restrict__ Vp, const double *__restrict__ w,
-                         const double *__restrict__ Hcol, SegChunks ch, int ks, const int *__restrict__ active,
+__global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
+                         double *const *__restrict__ Hp, SegChunks ch, int ks, const int *__restrict__ active,
                          double *__restrict__ v, double *__restrict__ partial) {
     __shared__ double sh[32];
+    const int nvec = *iter + 1;
     int r = blockIdx.y, c = blockIdx.x;
     int sidx = ch.geom[c] * ks + r;
     if (!active[sidx]) return;
-    const double *h = Hcol + (int64_t)sidx * (nvec + 1);
+    const double *h = Hp[nvec - 1] + (int64_t)sidx * (nvec + 1);
     int64_t base = ch.start[c];
     int len = ch.len[c];
     double s2 = 0.0;
@@ -1192,12 +1203,14 @@ __global__ void k_update(int64_t Np, int nvec, double *const *__restrict__ Vp, c
 }
 
 // Givens update of Hessenberg column i of every active solve (one thread each)
-__global__ void k_givens(int S, int i, int M, double *__restrict__ Hc, double *cs, double *sn, double *g, const double *normb,
-                         const double *nrm2, double *hnorm, double tol, const int *scap, int *active, int *iters, int *capped,
-                         int *n_active) {
+__global__ void k_givens(int S, const int *__restrict__ iter, int M, double *const *__restrict__ Hp, double *cs, double *sn,
+                         double *g, const double *normb, const double *nrm2, double *hnorm, double tol, const int *scap, int *active,
+                         int *iters, int *capped, int *n_active_all) {
+    const int i = *iter;
+    int *n_active = n_active_all + i;
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (sidx >= S || !active[sidx]) return;
-    double *hc = Hc + (int64_t)sidx * (i + 2);
+    double *hc = Hp[i] + (int64_t)sidx * (i + 2);
     double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2), *gg = g + (int64_t)sidx * (M + 2);
     double hn = sqrt(nrm2[sidx]);
     hnorm[sidx] = hn;
@@ -1230,17 +1243,62 @@ __global__ void k_givens(int S, int i, int M, double *__restrict__ Hc, double *c
     }
 }
 
-// out[r][j] = v[r][j] / hn[solve of (j, r)] for active solves
-__global__ void k_scale(int64_t Np, int ks, const double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
-                        const int32_t *__restrict__ leaf_geom, double *__restrict__ out) {
+// out[r][j] = v[r][j] / hn[solve of (j, r)] for active solves, out = out_fixed
+// or basis vector *iter + 1; v is rewritten with the same values (it is the
+// input of the next product)
+__global__ void k_scale(int64_t Np, int ks, double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
+                        const int32_t *__restrict__ leaf_geom, double *__restrict__ out_fixed, double *const *__restrict__ Vp,
+                        const int *__restrict__ iter) {
+    double *out = out_fixed ? out_fixed : Vp[*iter + 1];
     int64_t n = (int64_t)ks * Np;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int r = (int)(t / Np);
         int64_t j = t - (int64_t)r * Np;
         int sidx = leaf_geom[j] * ks + r;
         if (active && !active[sidx]) continue;
-        out[t] = v[t] / hn[sidx];
+        double x = v[t] / hn[sidx];
+        out[t] = x;
+        v[t] = x;
     }
+}
+
+// Hessenberg column *iter of every active solve: out = Hp[i] + sidx*(i+2) + j,
+// j < i+1, summed over the solve's geometry chunks (one warp per output)
+__global__ void k_reduce_h(int ks, int G, int nch, const int *__restrict__ iter, const double *__restrict__ partial,
+                           const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
+                           const int *__restrict__ active, double *const *__restrict__ Hp) {
+    const int i = *iter, nvec = i + 1;
+    int lane = threadIdx.x & 31;
+    double *out = Hp[i];
+    for (int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; wid < (int64_t)nvec * ks * G;
+         wid += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        int j = (int)(wid % nvec);
+        int64_t rg = wid / nvec;
+        int r = (int)(rg % ks), g = (int)(rg / ks);
+        int sidx = g * ks + r;
+        if (!active[sidx]) continue;
+        double sum = 0.0;
+        int c0 = g_ch_first[g], cn = g_ch_count[g];
+        const double *pp = partial + ((int64_t)r * nvec + j) * nch + c0;
+        for (int c = lane; c < cn; c += 32) sum += pp[c];
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) out[(int64_t)sidx * (i + 2) + j] = sum;
+    }
+}
+
+// end of an Arnoldi step (one thread): advance the step index; go on while
+// a solve is active, the basis has room and no cancellation was asked for.
+// Inside the graph's while loop it sets the loop condition.
+__global__ void k_iter_advance(int *iter, const int *__restrict__ n_active, int cap, const volatile int *cancel, int *state,
+                               cudaGraphConditionalHandle cond, int use_cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int i = *iter;
+    int na = n_active[i];
+    int go = na > 0 && i + 1 < cap && !(cancel && *cancel);
+    *iter = i + 1;
+    state[0] = go;
+    state[1] = na;
+    if (use_cond) cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
 // back substitution R z = g for every solve (one thread each)
@@ -1591,6 +1649,10 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     ctx.refs.fetch_add(1);
     p->precision = precision;
     p->pin = pin_acquire(ctx);
+    if (p->pin && cudaHostGetDevicePointer((void **)&p->pin_dev, p->pin, 0) != cudaSuccess) {
+        cudaGetLastError();
+        p->pin_dev = NULL;
+    }
     p->Nn = a.n_nodes;
     p->Np = a.n_panels;
     p->L = a.n_links;
@@ -1804,7 +1866,10 @@ void problem_destroy(DeviceProblem *p) {
 int64_t problem_device_bytes(const DeviceProblem *p) { return p ? p->bytes : 0; }
 
 void problem_cancel(DeviceProblem *p) {
-    if (p) p->cancel.store(1);
+    if (!p) return;
+    p->cancel.store(1);
+    // the flag a running graph reads between Arnoldi steps
+    if (p->pin) ((volatile int *)p->pin)[4] = 1;
 }
 
 int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs, int iterations) {
@@ -1814,7 +1879,10 @@ int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs
     int kp = 1;
     while (kp < k) kp <<= 1;
     int64_t nch = (Np + kDotChunk - 1) / kDotChunk + 1;
-    int64_t vecs = ((iterations + 1 + 15) / 16) * 16;
+    // the basis is allocated 16 vectors at a time and, for the graph-run
+    // Arnoldi loop, for at least 32 steps (33 vectors) up front
+    int64_t steps = std::max(iterations, 32);
+    int64_t vecs = ((steps + 1 + 15) / 16) * 16;
     int64_t b = 0;
     b += Nn * (int64_t)(sizeof(NodeGeo) + 8 + 4 * 3 + 4 + 4 * 4);  // geometry, row pointers, tree, arrivals, sweep plan
     b += L * (4 + c);                                                  // links
@@ -1822,7 +1890,7 @@ int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs
     b += L * 8 + Nn * (int64_t)sizeof(fcg_tri64);                      // near-field list (bound: every link near) and tables
     b += (int64_t)kp * Nn * (8 * 3 + 4 + 8);                           // matvec node work
     b += (int64_t)k * Np * 8 * (5 + vecs);                             // Krylov vectors and basis
-    b += (int64_t)k * (iterations + 1) * nch * 8;                      // partial sums
+    b += (int64_t)k * (steps + 1) * nch * 8;                           // partial sums
     return b + b / 10;
 }
 
@@ -2261,7 +2329,17 @@ int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond)
     return FCG_NORMAL_END;
 }
 
+static void free_graph(DeviceProblem *p) {
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->gexec = NULL;
+    p->graph = NULL;
+    p->gkey.clear();
+}
+
 static void free_solve_ws(DeviceProblem *p) {
+    free_graph(p);
+    dfree(p->d_it); dfree(p->ptmp);
     dfree(p->cs); dfree(p->sn); dfree(p->g); dfree(p->z);
     dfree(p->normb); dfree(p->hnorm); dfree(p->nrm2);
     dfree(p->active); dfree(p->iters); dfree(p->capped); dfree(p->scap); dfree(p->n_active);
@@ -2294,6 +2372,7 @@ static int ensure_solve_ws(DeviceProblem *p, int k, int S, int M) {
             (r = dalloc(&p->x, n, B)))
             return r;
         if ((r = dalloc(&p->Vptr, (size_t)M + 2, B)) || (r = dalloc(&p->Hptr, (size_t)M + 2, B))) return r;
+        if ((r = dalloc(&p->d_it, 4, B))) return r;
         p->Vptr_cap = M + 2;
         p->gk = k;
         p->gS = S;
@@ -2507,6 +2586,115 @@ static int precond_apply(DeviceProblem *p, int kind, const double *in, double *o
     return FCG_NORMAL_END;
 }
 
+// ---- one Arnoldi step, enqueued on the problem's stream; the step index is
+// read on the device (d_it[0]), so the same launches serve every step and can
+// be captured once into a graph.
+struct StepArgs {
+    int k, S, G, M, nch, cap, pk;
+    SegChunks ch;
+    const double *diag;
+    double tol;
+    int use_cond;
+    cudaGraphConditionalHandle cond;
+};
+
+static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
+    cudaStream_t s = p->stream;
+    int64_t Np = p->Np;
+    int sms = p->ctx->sm_count, r;
+    const int g1 = grid_for((int64_t)a.k * Np, 256, sms), gs = (a.S + 127) / 128;
+    const int gh = (int)std::min<int64_t>(((int64_t)a.cap * a.k * a.G * 32 + 255) / 256, (int64_t)sms * 32);
+    const int g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
+    // w = A P q_i, q_i in vv
+    if (a.pk == FCG_PRECOND_TWO_LEVEL) {
+        if ((r = precond_apply(p, a.pk, p->vv, p->ptmp, a.k)) || (r = matvec(p, p->ptmp, p->w, a.k, NULL))) return r;
+    } else if ((r = matvec(p, p->vv, p->w, a.k, a.diag))) {
+        return r;
+    }
+    // classical Gram-Schmidt against q_0..q_i, per solve
+    k_dots<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial);
+    k_reduce_h<<<gh, 256, 0, s>>>(a.k, a.G, a.nch, p->d_it, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->Hptr);
+    k_update<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial);
+    k_reduce_seg<<<g1v, 256, 0, s>>>(1, a.k, a.G, a.nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1, 0);
+    k_givens<<<gs, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, a.tol, p->scap,
+                                p->active, p->iters, p->capped, p->n_active);
+    k_scale<<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it);
+    k_iter_advance<<<1, 32, 0, s>>>(p->d_it, p->n_active, a.cap, p->pin_dev ? p->pin_dev + 4 : NULL, p->d_it + 1, a.cond,
+                                    a.use_cond);
+    p->timings.launches += 7;
+    FCG_CK(cudaGetLastError());
+    return FCG_NORMAL_END;
+}
+
+// Build (or reuse) the graph "while (go) { one Arnoldi step }". Everything a
+// step reads is in a key; the graph is rebuilt only when the key changes.
+static int ensure_step_graph(DeviceProblem *p, StepArgs a) {
+    std::vector<unsigned char> key;
+    auto put = [&](const void *x, size_t n) { key.insert(key.end(), (const unsigned char *)x, (const unsigned char *)x + n); };
+    put(&a.k, sizeof(int) * 7);
+    put(&a.ch, sizeof(a.ch));
+    put(&a.diag, sizeof(a.diag));
+    put(&a.tol, sizeof(a.tol));
+    const void *ptrs[] = {p->w, p->vv, p->ptmp, p->partial, p->Vptr, p->Hptr, p->n_active, p->cs, p->sn, p->g, p->normb, p->nrm2,
+                          p->hnorm, p->scap, p->active, p->iters, p->capped, p->leaf_geom, p->g_ch_first, p->g_ch_count, p->Qd,
+                          p->Qf, p->Pd, p->Pf2, p->Ad, p->sup_T, p->sup_pot, p->sup_chg, p->d_it, p->pin_dev};
+    put(ptrs, sizeof(ptrs));
+    int ints[] = {p->kcap, p->sup_m, p->sup_kcap, p->spmv_lanes, p->profiling ? 1 : 0};
+    put(ints, sizeof(ints));
+    if (p->gexec && key == p->gkey) return FCG_NORMAL_END;
+    free_graph(p);
+    cudaGraph_t g = NULL, body = NULL;
+    cudaGraphExec_t ge = NULL;
+    cudaGraphConditionalHandle h;
+    cudaGraphNode_t node;
+    cudaGraphNodeParams cp = {};
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, NULL, NULL, 0, &cp);
+    }
+    if (e == cudaSuccess) {
+        body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(p->stream, body, NULL, NULL, 0, cudaStreamCaptureModeThreadLocal);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        set_error(std::string("cannot build the Arnoldi graph: ") + cudaGetErrorString(e));
+        return FCG_DEVICE_ERROR;
+    }
+    // launches made while capturing are not runs: keep the counters as they were
+    SolveTimings saved = p->timings;
+    a.use_cond = 1;
+    a.cond = h;
+    int r = enqueue_step(p, a);
+    SolveTimings after = p->timings;
+    p->timings = saved;
+    cudaGraph_t got = NULL;
+    e = cudaStreamEndCapture(p->stream, &got);
+    if (r == FCG_NORMAL_END && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (r != FCG_NORMAL_END || e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(g);
+        if (r == FCG_NORMAL_END) {
+            set_error(std::string("cannot build the Arnoldi graph: ") + cudaGetErrorString(e));
+            r = FCG_DEVICE_ERROR;
+        }
+        return r;
+    }
+    p->graph = g;
+    p->gexec = ge;
+    p->gkey = key;
+    p->g_launches = (int)(after.launches - saved.launches);
+    p->g_link_launches = (int)(after.link_launches - saved.link_launches);
+    p->g_link_bytes = after.link_bytes - saved.link_bytes;
+    return FCG_NORMAL_END;
+}
+
 int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations) {
     AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
@@ -2550,6 +2738,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     }
     const double *diag = (pk == FCG_PRECOND_JACOBI) ? p->self : NULL;
     const bool pre = pk != FCG_PRECOND_NONE;
+    if (p->pin) ((volatile int *)p->pin)[4] = p->cancel.load() ? 1 : 0;
     cudaStream_t s = p->stream;
     int sms = p->ctx->sm_count;
     SegChunks chunks = {p->ch_start, p->ch_len, p->ch_geom, nch};
@@ -2636,7 +2825,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
         k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
                                         p->capped, p->n_active + M + 1);
-        k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0);
+        k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL);
         FCG_CK(cudaGetLastError());
         p->timings.launches += pre ? 7 : 7;
         // does any solve need an Arnoldi step?
@@ -2644,33 +2833,55 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         FCG_CK(cudaStreamSynchronize(s));
         bool any = pin[0] > 0;
-        for (int i = 0; any && i < M; i++) {
-            if ((r = ensure_basis(p, i + 1)) || (r = ensure_partial(p, (size_t)k * (i + 1) * nch))) { status = r; break; }
-            double *Vi = basis_addr(p, i), *Vn = basis_addr(p, i + 1);
-            double *hcol = p->Hc[i];
-            // w = A P q_i
-            if (pk == FCG_PRECOND_TWO_LEVEL) {
-                if ((r = precond_apply(p, pk, Vi, p->vv, k)) || (r = matvec(p, p->vv, p->w, k, NULL))) { status = r; break; }
-            } else if ((r = matvec(p, Vi, p->w, k, diag))) {
-                status = r;
-                break;
+        FCG_CK(cudaMemsetAsync(p->d_it, 0, 4 * sizeof(int), s));
+        if (pk == FCG_PRECOND_TWO_LEVEL && !p->ptmp && (r = dalloc(&p->ptmp, (size_t)k * Np, p->bytes))) {
+            free_batch();
+            status = r;
+            break;
+        }
+        StepArgs sa = {k, S, G, M, nch, M, pk, chunks, diag, opt.tol, 0, 0};
+        // the workspace a step touches exists before any capture
+        if ((r = ensure_matvec_ws(p, kpad(k))) ||
+            (pk == FCG_PRECOND_TWO_LEVEL && (r = precond_apply(p, pk, p->vv, p->ptmp, k)))) {
+            free_batch();
+            status = r;
+            break;
+        }
+        const bool use_graph = !p->profiling && getenv("FCG_NO_GRAPH") == NULL;
+        int steps = 0;  // Arnoldi steps taken
+        while (any && status == FCG_NORMAL_END) {
+            if (use_graph) {
+                // the whole loop in one graph launch, up to the basis capacity
+                int capv = std::min(M, std::max(32, 2 * steps));
+                sa.cap = capv;
+                if ((r = ensure_basis(p, capv)) || (r = ensure_partial(p, (size_t)k * capv * nch)) || (r = ensure_step_graph(p, sa))) {
+                    status = r;
+                    break;
+                }
+                FCG_CK(cudaGraphLaunch(p->gexec, s));
+                FCG_CK(cudaMemcpyAsync(pin, p->d_it, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+                FCG_CK(cudaStreamSynchronize(s));
+                int ran = pin[0] - steps;
+                p->timings.launches += (int64_t)ran * p->g_launches;
+                p->timings.link_launches += (int64_t)ran * p->g_link_launches;
+                p->timings.link_bytes += (int64_t)ran * p->g_link_bytes;
+                p->timings.matvecs += ran;
+                steps = pin[0];
+                // stopped with solves still active: the basis is full (grow it) or a cancel
+                any = pin[2] > 0 && steps < M;
+            } else {
+                sa.cap = M;
+                if ((r = ensure_basis(p, steps + 1)) || (r = ensure_partial(p, (size_t)k * (steps + 1) * nch)) ||
+                    (r = enqueue_step(p, sa))) {
+                    status = r;
+                    break;
+                }
+                FCG_CK(cudaMemcpyAsync(pin, p->d_it, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+                FCG_CK(cudaStreamSynchronize(s));
+                prof_collect(p);
+                steps = pin[0];
+                any = pin[1] != 0;
             }
-            // classical Gram-Schmidt against q_0..q_i, per solve
-            k_dots<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, chunks, k, p->active, p->partial);
-            k_reduce_seg<<<seg_grid(i + 1), 256, 0, s>>>(i + 1, k, G, nch, p->partial, p->g_ch_first, p->g_ch_count, p->active,
-                                                          hcol, i + 2, 1);
-            k_update<<<dim3(nch, k), 256, 0, s>>>(Np, i + 1, p->Vptr, p->w, hcol, chunks, k, p->active, p->vv, p->partial);
-            k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1,
-                                                      0);
-            k_givens<<<gs, 128, 0, s>>>(S, i, M, hcol, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, opt.tol, p->scap, p->active,
-                                        p->iters, p->capped, p->n_active + i);
-            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, p->active, p->leaf_geom, Vn);
-            FCG_CK(cudaGetLastError());
-            p->timings.launches += 6;
-            FCG_CK(cudaMemcpyAsync(pin, p->n_active + i, sizeof(int), cudaMemcpyDeviceToHost, s));
-            FCG_CK(cudaStreamSynchronize(s));
-            prof_collect(p);
-            any = pin[0] > 0;
             if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
         }
         if (status != FCG_NORMAL_END) { free_batch(); break; }
