@@ -164,6 +164,7 @@ def lib() -> C.CDLL:
     L.fcg_run_command_line.argtypes = [C.c_char_p]
     L.fcg_model_concat.argtypes = [C.POINTER(vp), i32, C.POINTER(vp), vp]
     L.fcg_problem_cancel.argtypes = [vp]
+    L.fcg_model_arrays_check.argtypes = [C.POINTER(ModelArrays)]
     L.fcg_problem_estimate_bytes.argtypes = [C.POINTER(ModelArrays), C.c_int, C.c_int, C.c_int]
     L.fcg_problem_estimate_bytes.restype = i64
     L.fcg_server_create.argtypes = [vp, C.POINTER(ServerConfig), C.POINTER(vp)]
@@ -335,6 +336,11 @@ class Model:
             setattr(a, name, arr.ctypes.data)
         self._keep = keep
         return a
+
+    def check(self):
+        """Structural checks of the arrays (no device needed); raises FCError."""
+        arr = self.c_arrays()
+        _check(lib().fcg_model_arrays_check(C.byref(arr)), "model check")
 
     def close(self):
         if self._h is not None:

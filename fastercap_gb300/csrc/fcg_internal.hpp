@@ -40,6 +40,9 @@ void context_unref(DeviceContext *ctx);
 
 int context_init(DeviceContext &ctx, int device);
 
+// structural checks of a model's arrays ("" when valid); no device work
+std::string model_check(const fcg_model_arrays &a);
+
 // problem lifetime
 int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out);
 void problem_destroy(DeviceProblem *p);

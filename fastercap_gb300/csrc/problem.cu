@@ -1636,6 +1636,8 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
     return FCG_NORMAL_END;
 }
 
+std::string model_check(const fcg_model_arrays &a) { return validate(a); }
+
 int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out) {
     *out = NULL;
     HostTrace tr;

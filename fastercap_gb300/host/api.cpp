@@ -270,6 +270,14 @@ int fcg_problem_get_charges(fcg_problem *p, double *charges) {
     return (p && charges) ? fcg::problem_get_charges(p->p, charges) : FCG_GENERIC_ERROR;
 }
 
+int fcg_model_arrays_check(const fcg_model_arrays *a) {
+    if (!a) return FCG_GENERIC_ERROR;
+    std::string bad = fcg::model_check(*a);
+    if (bad.empty()) return FCG_NORMAL_END;
+    fcg::set_error("invalid model: " + bad);
+    return FCG_GENERIC_ERROR;
+}
+
 int fcg_problem_cancel(fcg_problem *p) {
     if (!p) return FCG_GENERIC_ERROR;
     fcg::problem_cancel(p->p);
@@ -404,7 +412,7 @@ bool parse_cmd(const char *cmd, CmdOptions &o, std::string &err) {
 
 }  // namespace
 
-extern "C" int fcg_run_command_line(const char *command_line) {
+static int run_command_line_impl(const char *command_line) {
     CmdOptions o;
     std::string err;
     if (!command_line || parse_cmd(command_line, o, err)) {
@@ -507,5 +515,11 @@ extern "C" int fcg_run_command_line(const char *command_line) {
     fcg_problem_destroy(p);
     fcg_context_destroy(ctx);
     fcg_model_free(m);
+    return r;
+}
+
+extern "C" int fcg_run_command_line(const char *command_line) {
+    int r = run_command_line_impl(command_line);
+    fflush(stdout);  // the report is complete when the call returns
     return r;
 }

@@ -106,6 +106,13 @@ int fcg_model_arrays_get(const fcg_model *m, fcg_model_arrays *arrays);
 const char *fcg_model_conductor_name(const fcg_model *m, int32_t index);
 void fcg_model_free(fcg_model *m);
 
+/* Structural checks of caller-built arrays (tree in post-order with
+ * contiguous leaf ranges, link offsets, conductor ranges tiling the leaves,
+ * permittivity indices), the same checks fcg_problem_create makes before any
+ * device work; link sources are range-checked on the device at creation.
+ * FCG_GENERIC_ERROR with the reason in fcg_last_error(). No device needed. */
+int fcg_model_arrays_check(const fcg_model_arrays *arrays);
+
 /* Concatenate independent models (geometries) into one model: a forest with
  * no link between geometries, conductors and leaves in model order.
  * geometry_of_conductor (may be NULL) receives, per conductor of the result,
