@@ -68,7 +68,7 @@ MULTI = {
 # DRAM bytes per link-product launch (dram__bytes_read.sum +
 # dram__bytes_write.sum) from one ncu capture of the same kernel and workload
 LINK_TRAFFIC = {
-    "sphere_327680": 531.318272e6 + 4.354048e6,    # k_spmv32<1, 32> (16 lanes move the same bytes)
+    "sphere_327680": 534.116864e6 + 4.707072e6,    # k_spmv32<1, 16>
     "crossing8x8_slab": 679.950848e6 + 7.460608e6,  # k_spmv32_multi<16>
 }
 
