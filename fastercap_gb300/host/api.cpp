@@ -412,17 +412,134 @@ bool parse_cmd(const char *cmd, CmdOptions &o, std::string &err) {
 
 }  // namespace
 
+// One build + fill + solve at a given refinement, printing the reference's
+// report blocks; the C matrix and the model counts are returned.
+struct SolveRun {
+    std::vector<double> cap;
+    std::vector<int> iters;
+    fcg_model_info info;
+    int nc = 0;
+    double build_s = 0, fill_s = 0, solve_s = 0;
+    int64_t device_bytes = 0;
+};
+
+static int build_model_at(const CmdOptions &o, double mesh_eps, fcg_model **m, fcg_model_info &info) {
+    fcg_build_options bo = {mesh_eps, o.eps_ratio, o.mesh_curv, o.verbose ? 1 : 0};
+    char ebuf[512];
+    int r = fcg_model_build(o.file.c_str(), &bo, m, ebuf, sizeof ebuf);
+    if (r != FCG_NORMAL_END) { printf("Error: %s\n", ebuf); return r; }
+    fcg_model_info_get(*m, &info);
+    return FCG_NORMAL_END;
+}
+
+// CSolveCap::AutoSetPrecondType (Solver/SolveCapacitance.cpp:580-608)
+static void auto_precond(int64_t links, int cond_num, int &kind, unsigned &dim) {
+    long lx = (long)(links / 1000) * cond_num;
+    if (lx <= 500) { kind = FCG_PRECOND_JACOBI; return; }
+    kind = FCG_PRECOND_TWO_LEVEL;
+    dim = lx <= 5000 ? 128 : (lx <= 10000 ? 512 : 1024);
+}
+
+static int solve_model(fcg_context *ctx, fcg_model *m, const CmdOptions &o, double gmres_tol, int kind, unsigned dim, SolveRun &out) {
+    fcg_model_info &info = out.info;
+    fcg_model_info_get(m, &info);
+    if (kind == FCG_PRECOND_TWO_LEVEL) printf("Precond Type(s) (-p): Two-levels, dimension %u\n", dim);
+    else printf("Precond Type(s) (-p): %s\n", kind == FCG_PRECOND_JACOBI ? "Jacobi" : "None");
+    printf("Number of input panels to solver engine: %lld\n", (long long)info.input_panels);
+    printf("Number of panels after refinement: %lld\n", (long long)info.n_panels);
+    printf("Number of links to be computed: %lld\n", (long long)info.n_links);
+    fcg_problem *p = NULL;
+    fcg_model_arrays arr;
+    fcg_model_arrays_get(m, &arr);
+    int r = fcg_problem_create(ctx, &arr, o.precision, &p);
+    if (r == FCG_NORMAL_END) r = fcg_problem_fill(p);
+    out.nc = info.n_conductors - info.n_dielectrics;
+    if (r == FCG_NORMAL_END) {
+        out.cap.assign((size_t)out.nc * out.nc, 0.0);
+        out.iters.assign(out.nc, 0);
+        fcg_solve_options so = {gmres_tol, kind, 0, 0, (int)dim};
+        r = fcg_problem_solve(p, &so, out.cap.data(), out.iters.data());
+    }
+    if (r != FCG_NORMAL_END && r != FCG_NOT_CONVERGED) {
+        printf("Error: %s\n", fcg_last_error());
+        fcg_problem_destroy(p);
+        return r;
+    }
+    if (r == FCG_NOT_CONVERGED) printf("Error: GMRES not converging within the iteration cap\n");
+    printf("GMRES iterations per conductor:");
+    for (int i = 0; i < out.nc; i++) printf(" %d", out.iters[i]);
+    printf("\nCapacitance matrix is:\nDimension %d x %d\n", out.nc, out.nc);
+    int row = 0;
+    for (int32_t c = 0; c < info.n_conductors; c++) {
+        if (arr.cond_is_diel[c]) continue;
+        printf("%s  ", fcg_model_conductor_name(m, c));
+        for (int j = 0; j < out.nc; j++) printf("%g ", out.cap[(size_t)row * out.nc + j]);
+        printf("\n");
+        row++;
+    }
+    for (int i = 0; i < out.nc; i++)
+        for (int j = 0; j < out.nc; j++)
+            if (i != j && out.cap[(size_t)i * out.nc + j] >= 0.0)
+                printf("Warning: capacitance matrix has a non-negative off-diagonal element at row %d col %d\n", i + 1, j + 1);
+    fcg_problem_stats st;
+    fcg_problem_get_stats(p, &st);
+    out.fill_s = st.fill_ms / 1000.0;
+    out.solve_s = st.solve_ms / 1000.0;
+    out.device_bytes = fcg_problem_device_bytes(p);
+    fcg_problem_destroy(p);
+    return FCG_NORMAL_END;
+}
+
+static void print_stats(const CmdOptions &o, const SolveRun &run) {
+    printf("\nSolve statistics:\n");
+    printf("Number of panels after refinement: %lld\n", (long long)run.info.n_panels);
+    printf("Number of links: %lld\n", (long long)(run.info.n_links + run.info.n_panels));
+    printf("Max recursion level: %d\n", run.info.max_level);
+    printf("Max Mesh relative refinement value: %g\n", run.info.max_mesh_eps);
+    if (o.dump_time) {
+        printf("Time for building the model (host): %fs\n", run.build_s);
+        printf("Time for building potential matrix (GPU): %fs\n", run.fill_s);
+        printf("Time for gmres solving (GPU): %fs\n", run.solve_s);
+        printf("Device memory for the problem: %lld bytes\n", (long long)run.device_bytes);
+    }
+}
+
+// CSolveCap::OutputCapMtxToFile (Solver/SolveCapacitance.cpp:835-911): the
+// matrix as <input without extension>.csv
+static void write_csv(const CmdOptions &o, const SolveRun &run) {
+    std::string name = o.file;
+    size_t dot = name.rfind('.');
+    if (dot != std::string::npos) name.resize(dot);
+    name += ".csv";
+    FILE *f = fopen(name.c_str(), "w");
+    if (!f) { printf("Warning: cannot open \"%s\" for writing, skipping\n", name.c_str()); return; }
+    printf("Generating capacitance matrix file \"%s\"\n", name.c_str());
+    for (int i = 0; i < run.nc; i++) {
+        for (int j = 0; j < run.nc; j++) {
+            fprintf(f, "%g", run.cap[(size_t)i * run.nc + j]);
+            if (j < run.nc - 1) fprintf(f, ", ");
+        }
+        fprintf(f, "\n");
+    }
+    fclose(f);
+}
+
+static double fnorm(const std::vector<double> &a) {
+    double s = 0.0;
+    for (double v : a) s += v * v;
+    return sqrt(s);
+}
+
 static int run_command_line_impl(const char *command_line) {
     CmdOptions o;
     std::string err;
     if (!command_line || parse_cmd(command_line, o, err)) {
         printf("%s\n", err.c_str());
-        printf("Usage: fastercap_gb300 <input file> [-m<mesh>] [-mc<mesh curvature>] [-t<tolerance>] [-d<interaction coeff>]\n");
-        printf("                       [-pj|-pn|-ps<dim>] [-i] [-v] [-x64|-xm]\n");
+        printf("Usage: fastercap_gb300 <input file> [-a<max err>] [-ap] [-m<mesh>] [-mc<mesh curvature>] [-t<tolerance>]\n");
+        printf("                       [-d<interaction coeff>] [-pj|-pn|-ps<dim>] [-e] [-i] [-v] [-x64|-xm]\n");
         return FCG_COMMAND_LINE_ERROR;
     }
     if (o.galerkin) { printf("Error: the Galerkin scheme (-g) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
-    if (o.automatic) { printf("Error: automatic mode (-a) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
     if (o.precond & (2 | 8)) {
         printf("Error: the block (-pb) and hierarchical (-ph) preconditioners are not supported by the GPU solver\n");
         return FCG_COMMAND_LINE_ERROR;
@@ -441,80 +558,82 @@ static int run_command_line_impl(const char *command_line) {
             printf("Warning: minimum two-levels preconditioner dimension is 16, using 16\n");
         }
     }
-    const int precond_kind = (o.precond & 4) ? FCG_PRECOND_TWO_LEVEL : (o.precond & FCG_PRECOND_JACOBI) ? FCG_PRECOND_JACOBI
-                                                                                                       : FCG_PRECOND_NONE;
+    int kind = (o.precond & 4) ? FCG_PRECOND_TWO_LEVEL : (o.precond & FCG_PRECOND_JACOBI) ? FCG_PRECOND_JACOBI : FCG_PRECOND_NONE;
+    unsigned dim = o.super_dim;
     printf("Running fastercap_gb300 (GB300 solve path for FasterCap input files)\n");
     printf("Input file: %s\n", o.file.c_str());
     auto t0 = std::chrono::steady_clock::now();
-    fcg_build_options bo = {o.mesh_eps, o.eps_ratio, o.mesh_curv, o.verbose ? 1 : 0};
-    fcg_model *m = NULL;
-    char ebuf[512];
-    int r = fcg_model_build(o.file.c_str(), &bo, &m, ebuf, sizeof ebuf);
-    if (r != FCG_NORMAL_END) { printf("Error: %s\n", ebuf); return r; }
-    auto t1 = std::chrono::steady_clock::now();
-    fcg_model_info info;
-    fcg_model_info_get(m, &info);
-    printf("Mesh refinement (-m): %g\nGMRES tolerance (-t): %g\n", o.mesh_eps, o.gmres_tol);
-    if (precond_kind == FCG_PRECOND_TWO_LEVEL) printf("Precond Type(s) (-p): Two-levels, dimension %u\n", o.super_dim);
-    else printf("Precond Type(s) (-p): %s\n", precond_kind == FCG_PRECOND_JACOBI ? "Jacobi" : "None");
-    printf("Number of input panels to solver engine: %lld\n", (long long)info.input_panels);
-    printf("Number of panels after refinement: %lld\n", (long long)info.n_panels);
-    printf("Number of links to be computed: %lld\n", (long long)info.n_links);
     fcg_context *ctx = NULL;
-    fcg_problem *p = NULL;
-    fcg_model_arrays arr;
-    fcg_model_arrays_get(m, &arr);
-    r = fcg_context_create(0, &ctx);
-    if (r == FCG_NORMAL_END) r = fcg_problem_create(ctx, &arr, o.precision, &p);
-    if (r == FCG_NORMAL_END) r = fcg_problem_fill(p);
-    int nc = 0;
-    std::vector<double> cap;
-    std::vector<int> iters;
-    if (r == FCG_NORMAL_END) {
-        nc = info.n_conductors - info.n_dielectrics;
-        cap.resize((size_t)nc * nc);
-        iters.resize(nc);
-        fcg_solve_options so = {o.gmres_tol, precond_kind, 0, 0, (int)o.super_dim};
-        r = fcg_problem_solve(p, &so, cap.data(), iters.data());
+    fcg_model *m = NULL;
+    SolveRun run;
+    int r;
+    if (!o.automatic) {
+        // manual settings (CSolveCap::Run, Solver/SolveCapacitance.cpp:479-531)
+        auto tb = std::chrono::steady_clock::now();
+        r = build_model_at(o, o.mesh_eps, &m, run.info);
+        if (r != FCG_NORMAL_END) return r;
+        run.build_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - tb).count();
+        printf("Mesh refinement (-m): %g\nGMRES tolerance (-t): %g\n", o.mesh_eps, o.gmres_tol);
+        r = fcg_context_create(0, &ctx);
+        if (r != FCG_NORMAL_END) printf("Error: %s\n", fcg_last_error());
+        else r = solve_model(ctx, m, o, o.gmres_tol, kind, dim, run);
+    } else {
+        // automatic refinement (CSolveCap::Run auto branch,
+        // Solver/SolveCapacitance.cpp:294-477): start unrefined, then divide
+        // the mesh parameter by sqrt(2) (from the achieved refinement) until
+        // panels and links grow by 10 %, solve, and stop when the relative
+        // Frobenius norm of the change of C is within the error
+        const double tol = o.auto_err / 2.0;
+        printf("Auto calculation with max error: %g\n", o.auto_err);
+        printf("GMRES tolerance (-t): %g\n", tol);
+        r = fcg_context_create(0, &ctx);
+        if (r != FCG_NORMAL_END) { printf("Error: %s\n", fcg_last_error()); return r; }
+        printf("\nIteration number #0 ***************************\n\n");
+        r = build_model_at(o, 1e32, &m, run.info);
+        if (r == FCG_NORMAL_END) {
+            printf("Mesh refinement (-m): %g\n", 1e32);
+            if (o.auto_precond) auto_precond(run.info.n_links, (int)(run.info.n_conductors - run.info.n_dielectrics), kind, dim);
+            r = solve_model(ctx, m, o, tol, kind, dim, run);
+        }
+        int64_t old_panels = run.info.n_panels, old_links = run.info.n_links;
+        for (int it = 1; r == FCG_NORMAL_END && it < 128; it++) {
+            printf("\nIteration number #%d ***************************\n\n", it);
+            bool enough = false;
+            double meps = 0.0;
+            for (int j = 0; !enough && j < 128; j++) {
+                meps = run.info.max_mesh_eps / sqrt(2.0);
+                fcg_model_free(m);
+                m = NULL;
+                r = build_model_at(o, meps, &m, run.info);
+                if (r != FCG_NORMAL_END) break;
+                enough = run.info.n_links > old_links * 1.1 && run.info.n_panels > old_panels * 1.1;
+                if (!enough)
+                    printf("Delta in refined panel and link count w.r.t. previous iteration less than 10%%\n(Panels # %lld, Links # %lld)\n",
+                           (long long)run.info.n_panels, (long long)run.info.n_links);
+            }
+            if (r != FCG_NORMAL_END) break;
+            printf("Mesh refinement (-m): %g\n", meps);
+            if (o.auto_precond) auto_precond(run.info.n_links, (int)(run.info.n_conductors - run.info.n_dielectrics), kind, dim);
+            std::vector<double> prev = run.cap;
+            r = solve_model(ctx, m, o, tol, kind, dim, run);
+            if (r != FCG_NORMAL_END) break;
+            std::vector<double> d(run.cap.size());
+            for (size_t q = 0; q < d.size(); q++) d[q] = run.cap[q] - (q < prev.size() ? prev[q] : 0.0);
+            double diff = fnorm(d) / fnorm(run.cap);
+            printf("Weighted Frobenius norm of the difference between capacitance (auto option): %g\n", diff);
+            if (diff <= o.auto_err) break;
+            old_panels = run.info.n_panels;
+            old_links = run.info.n_links;
+        }
     }
     auto t2 = std::chrono::steady_clock::now();
-    if (r != FCG_NORMAL_END && r != FCG_NOT_CONVERGED) {
-        printf("Error: %s\n", fcg_last_error());
-    } else {
-        if (r == FCG_NOT_CONVERGED) printf("Error: GMRES not converging within the iteration cap\n");
-        printf("GMRES iterations per conductor:");
-        for (int i = 0; i < nc; i++) printf(" %d", iters[i]);
-        printf("\nCapacitance matrix is:\nDimension %d x %d\n", nc, nc);
-        int row = 0;
-        for (int32_t c = 0; c < info.n_conductors; c++) {
-            if (arr.cond_is_diel[c]) continue;
-            printf("%s  ", fcg_model_conductor_name(m, c));
-            for (int j = 0; j < nc; j++) printf("%g ", cap[(size_t)row * nc + j]);
-            printf("\n");
-            row++;
-        }
-        for (int i = 0; i < nc; i++)
-            for (int j = 0; j < nc; j++)
-                if (i != j && cap[(size_t)i * nc + j] >= 0.0)
-                    printf("Warning: capacitance matrix has a non-negative off-diagonal element at row %d col %d\n", i + 1, j + 1);
-        printf("\nSolve statistics:\n");
-        printf("Number of panels after refinement: %lld\n", (long long)info.n_panels);
-        printf("Number of links: %lld\n", (long long)(info.n_links + info.n_panels));
-        printf("Max recursion level: %d\n", info.max_level);
-        printf("Max Mesh relative refinement value: %g\n", info.max_mesh_eps);
-        if (o.dump_time) {
-            fcg::SolveTimings t = fcg::problem_timings(p->p);
-            printf("Time for building the model (host): %fs\n", std::chrono::duration<double>(t1 - t0).count());
-            printf("Time for building potential matrix (GPU): %fs\n", t.fill_ms / 1000.0);
-            printf("Time for gmres solving (GPU): %fs\n", t.solve_ms / 1000.0);
-            printf("Device memory for the problem: %lld bytes\n", (long long)fcg_problem_device_bytes(p));
-        }
+    if (r == FCG_NORMAL_END) {
+        print_stats(o, run);
+        if (o.out_cap) write_csv(o, run);
         printf("Total time: %fs\n", std::chrono::duration<double>(t2 - t0).count());
-        if (r == FCG_NOT_CONVERGED) r = FCG_NORMAL_END;
     }
-    fcg_problem_destroy(p);
-    fcg_context_destroy(ctx);
-    fcg_model_free(m);
+    if (ctx) fcg_context_destroy(ctx);
+    if (m) fcg_model_free(m);
     return r;
 }
 

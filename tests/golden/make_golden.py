@@ -129,6 +129,51 @@ def convert(dump: str) -> dict:
     return out
 
 
+# automatic refinement runs of the reference console (-a<err>): per-iteration
+# panel and link counts and the final capacitance matrix, parsed from its report
+AUTO_CASES = {
+    "auto_crossing2x2": (lambda: geo.crossing_2x2().text(), ["-a0.01", "-f0"]),
+    "auto_crossing2x2_slab": (lambda: geo.Crossing(k=2, length=10.0, pitch=3.0, gap=1.0, eps_r=3.9,
+                                                   slab=(3.5, 1.0, 3.9, 15.0), name="c2slab").text(), ["-a0.02", "-f0"]),
+}
+
+
+def parse_report(text: str) -> dict:
+    """Per-iteration panels/links and the last capacitance matrix of a console report."""
+    panels, links, caps, cur = [], [], [], None
+    lines = text.splitlines()
+    for i, ln in enumerate(lines):
+        if ln.startswith("Number of panels after refinement:") and (i + 1 < len(lines)) and \
+                lines[i + 1].startswith("Number of links to be computed:"):
+            panels.append(int(ln.split(":")[1]))
+            links.append(int(lines[i + 1].split(":")[1]))
+        if ln.startswith("Dimension "):
+            n = int(ln.split()[1])
+            cur = [[float(x) for x in lines[i + 1 + r].split()[1:1 + n]] for r in range(n)]
+            caps.append(cur)
+    return {"ref_auto_panels": np.array(panels, np.int64), "ref_auto_links": np.array(links, np.int64),
+            "ref_cap": np.array(caps[-1]), "ref_auto_iterations": np.array(len(caps))}
+
+
+def main_auto(ref_dir: str, only=()):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + ref_dir], check=True)
+    console = os.path.join(ROOT, "oracle", "_ref", "fcref")
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (text_fn, switches) in AUTO_CASES.items():
+            if only and name not in only:
+                continue
+            text = text_fn()
+            inp = os.path.join(tmp, name + ".txt")
+            with open(inp, "w") as f:
+                f.write(text)
+            rep = subprocess.run([console, inp] + switches, check=True, capture_output=True, text=True).stdout
+            out = parse_report(rep)
+            out["input_text"] = np.frombuffer(text.encode(), np.uint8)
+            out["switches"] = np.array(switches)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+            print("%-22s iterations %d, panels %s" % (name, int(out["ref_auto_iterations"]), list(out["ref_auto_panels"])))
+
+
 def main(ref_dir: str = "/root/reference", *only):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + ref_dir], check=True)
     dump_bin = os.path.join(ROOT, "oracle", "_ref", "fcref_dump")
@@ -151,4 +196,8 @@ def main(ref_dir: str = "/root/reference", *only):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    args = sys.argv[1:]
+    if args[1:] and all(a.startswith("auto_") for a in args[1:]):
+        main_auto(args[0], args[1:])
+    else:
+        main(*args)

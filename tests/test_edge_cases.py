@@ -162,3 +162,28 @@ def test_cli_two_level_runs(tmp_path, capfd):
     out = capfd.readouterr().out
     assert code == fc.NORMAL_END, out
     assert "Two-levels" in out and "Capacitance matrix is:" in out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["auto_crossing2x2", "auto_crossing2x2_slab"])
+def test_cli_auto_mode_matches_reference(name, tmp_path, capfd):
+    """-a<err>: the same refinement sequence (panels and links per iteration,
+    bit-exact builder) and final matrix as the reference console's own run."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden import parse_report
+    g = load_golden(name)
+    inp = tmp_path / "input.txt"
+    inp.write_bytes(bytes(g["input_text"]))
+    sw = " ".join(str(x) for x in g["switches"])
+    code = fc.run_command_line("fastercap_gb300 %s %s -x64 -e" % (inp, sw))
+    out = capfd.readouterr().out
+    assert code == fc.NORMAL_END, out
+    rep = parse_report(out)
+    np.testing.assert_array_equal(rep["ref_auto_panels"], g["ref_auto_panels"])
+    np.testing.assert_array_equal(rep["ref_auto_links"], g["ref_auto_links"])
+    np.testing.assert_allclose(rep["ref_cap"], g["ref_cap"], rtol=2e-5)
+    # -e: the matrix as <input>.csv
+    csv = np.loadtxt(tmp_path / "input.csv", delimiter=",")
+    np.testing.assert_allclose(csv, rep["ref_cap"], rtol=1e-5)
