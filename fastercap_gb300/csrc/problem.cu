@@ -467,8 +467,9 @@ __global__ void k_up(const SweepPlan plan, const int32_t *__restrict__ leaf_node
                      const int32_t *__restrict__ right_of, const int32_t *__restrict__ parent, int *arrive) {
     int b = blockIdx.x;
     int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b];
+    // right-hand side fastest: a node's kp values are written together
     for (int t = threadIdx.x; t < nl * k; t += blockDim.x) {
-        int i = t % nl, r = t / nl;
+        int i = t / k, r = t - i * k;
         int j = lf + i;
         double xv = in[(int64_t)r * ld + j];
         if (diag) xv = xv / diag[j];
@@ -481,7 +482,8 @@ __global__ void k_up(const SweepPlan plan, const int32_t *__restrict__ leaf_node
     for (int h = 0; h < nlv; h++) {
         int a0 = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a0;
         for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int n = plan.lvl_nodes[a0 + t % cnt], r = t / cnt;
+            int q = t / k, r = t - q * k;
+            int n = plan.lvl_nodes[a0 + q];
             double sum = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
             Qd[(int64_t)n * kp + r] = sum;
             if (MIXED) Qf[(int64_t)n * kp + r] = (float)sum;
@@ -553,7 +555,8 @@ __global__ void k_down(const SweepPlan plan, const int32_t *__restrict__ leaf_no
     for (int h = nlv - 1; h >= 0; h--) {
         int a0 = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a0;
         for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int n = plan.lvl_nodes[a0 + t % cnt], r = t / cnt;
+            int q = t / k, r = t - q * k;
+            int n = plan.lvl_nodes[a0 + q];
             double acc = pval(P, (int64_t)n * kp + r);
             if (n == root) {
                 if (hasp) acc = acc + s_anc[r];
@@ -1140,11 +1143,33 @@ __global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *
                 }
             }
         }
+        // reduce the eight sums over the warp by halving: each step keeps
+        // half of the values and adds the partner lane's copy of them
+        // (4 + 2 + 1 exchanges), then the last value over lane pairs: lane l
+        // ends with vector 4*bit4 + 2*bit3 + bit2 of its index
 #pragma unroll
-        for (int t = 0; t < T; t++)
-            for (int o = 16; o > 0; o >>= 1) acc[t] += __shfl_xor_sync(0xffffffffu, acc[t], o);
-        if (lane == 0)
-            for (int t = 0; t < T; t++) sh[warp][t] = acc[t];
+        for (int q = 0; q < 4; q++) {
+            bool hi = lane & 16;
+            double send = hi ? acc[q] : acc[q + 4];
+            double keep = hi ? acc[q + 4] : acc[q];
+            acc[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            bool hi = lane & 8;
+            double send = hi ? acc[q] : acc[q + 2];
+            double keep = hi ? acc[q + 2] : acc[q];
+            acc[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+        {
+            bool hi = lane & 4;
+            double send = hi ? acc[0] : acc[1];
+            double keep = hi ? acc[1] : acc[0];
+            acc[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+        }
+        acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 2);
+        acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 1);
+        if ((lane & 3) == 0) sh[warp][((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = acc[0];
         __syncthreads();
         if (threadIdx.x < T && j0 + threadIdx.x < nvec) {
             double sum = 0.0;
@@ -1188,15 +1213,27 @@ __global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const
     const double *h = Hp[nvec - 1] + (int64_t)sidx * (nvec + 1);
     int64_t base = ch.start[c];
     int len = ch.len[c];
+    // four elements per thread, each its own subtraction chain (in basis
+    // order), so the loads of one vector for all four are in flight together
+    const int U = kDotChunk / 256;
+    double x[U];
+    int64_t t0 = (int64_t)r * Np + base + threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < U; u++) x[u] = (threadIdx.x + u * 256 < len) ? w[t0 + u * 256] : 0.0;
+    for (int jv = 0; jv < nvec; jv++) {
+        const double hj = h[jv];
+        const double *vj = Vp[jv] + t0;
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (threadIdx.x + u * 256 < len) x[u] = x[u] - hj * vj[u * 256];
+    }
     double s2 = 0.0;
-    for (int u = 0; u < kDotChunk / 256; u++) {
-        int o = threadIdx.x + u * 256;
-        if (o >= len) break;
-        int64_t t = (int64_t)r * Np + base + o;
-        double x = w[t];
-        for (int jv = 0; jv < nvec; jv++) x = x - h[jv] * Vp[jv][t];
-        v[t] = x;
-        s2 += x * x;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        if (threadIdx.x + u * 256 < len) {
+            v[t0 + u * 256] = x[u];
+            s2 += x[u] * x[u];
+        }
     }
     s2 = block_sum(s2, sh);
     if (threadIdx.x == 0) partial[(int64_t)r * ch.n + c] = s2;
