@@ -27,6 +27,7 @@
 #include <mutex>
 #include <string>
 #include <vector>
+#include <thread>
 
 #include "fc_potential.h"
 #include "fcg_internal.hpp"
@@ -1538,6 +1539,22 @@ void context_release(DeviceContext &ctx) {
     }
 }
 
+// Run fn(begin, end) over [0, n) on up to 16 host threads (chunks of at
+// least 32k items; small ranges stay on the calling thread).
+template <class F> static void parallel_for(int64_t n, F fn) {
+    int nt = (int)std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()), 16);
+    nt = (int)std::min<int64_t>(nt, (n + 32767) / 32768);
+    if (nt <= 1) { fn((int64_t)0, n); return; }
+    std::vector<std::thread> th;
+    int64_t step = (n + nt - 1) / nt;
+    for (int t = 1; t < nt; t++) {
+        int64_t b = t * step, e = std::min(n, b + step);
+        if (b < e) th.emplace_back(fn, b, e);
+    }
+    fn((int64_t)0, std::min(n, step));
+    for (auto &x : th) x.join();
+}
+
 static std::string validate(const fcg_model_arrays &a) {
     if (a.n_nodes <= 0 || a.n_panels <= 0 || a.n_links < 0 || a.n_conductors <= 0) return "empty model";
     if (a.n_nodes > (int64_t)kSrcMask || a.n_links > 0x7fffffffLL) return "model too large (nodes must fit 29 bits, links 31 bits)";
@@ -1547,22 +1564,41 @@ static std::string validate(const fcg_model_arrays &a) {
         !a.cond_surf_ptr || !a.cond_surf_outperm)
         return "null model array";
     if (a.link_ptr[0] != 0 || a.link_ptr[a.n_nodes] != a.n_links) return "link_ptr does not span the links";
-    int64_t leaves = 0;
-    for (int64_t i = 0; i < a.n_nodes; i++) {
-        if (a.link_ptr[i + 1] < a.link_ptr[i]) return "link_ptr not monotone";
-        bool leaf = a.node_type[i] & FCG_IS_LEAF;
-        if (leaf) {
-            if (a.node_left[i] != -1 || a.node_right[i] != -1 || a.node_leaf_count[i] != 1) return "bad leaf node";
-            leaves++;
-        } else {
-            int32_t l = a.node_left[i], r = a.node_right[i];
-            if (l < 0 || r < 0 || l >= i || r >= i) return "children must precede their parent (post-order)";
-            if (a.node_leaf_count[i] != a.node_leaf_count[l] + a.node_leaf_count[r]) return "inconsistent leaf counts";
-            if (a.node_leaf_first[i] != a.node_leaf_first[l] || a.node_leaf_first[r] != a.node_leaf_first[l] + a.node_leaf_count[l])
-                return "leaf ranges are not contiguous";
+    // per-node checks on all host threads; the first failing node (lowest
+    // index) decides the message
+    std::atomic<int64_t> bad_at{INT64_MAX};
+    std::atomic<int64_t> leaves_all{0};
+    std::mutex mu;
+    const char *why = "";
+    parallel_for(a.n_nodes, [&](int64_t b, int64_t e) {
+        int64_t leaves = 0;
+        for (int64_t i = b; i < e; i++) {
+            const char *w = NULL;
+            if (a.link_ptr[i + 1] < a.link_ptr[i]) w = "link_ptr not monotone";
+            bool leaf = a.node_type[i] & FCG_IS_LEAF;
+            if (!w && leaf) {
+                if (a.node_left[i] != -1 || a.node_right[i] != -1 || a.node_leaf_count[i] != 1) w = "bad leaf node";
+                leaves++;
+            } else if (!w) {
+                int32_t l = a.node_left[i], r = a.node_right[i];
+                if (l < 0 || r < 0 || l >= i || r >= i) w = "children must precede their parent (post-order)";
+                else if (a.node_leaf_count[i] != a.node_leaf_count[l] + a.node_leaf_count[r]) w = "inconsistent leaf counts";
+                else if (a.node_leaf_first[i] != a.node_leaf_first[l] ||
+                         a.node_leaf_first[r] != a.node_leaf_first[l] + a.node_leaf_count[l])
+                    w = "leaf ranges are not contiguous";
+            }
+            if (!w && (a.node_leaf_first[i] < 0 || a.node_leaf_first[i] + a.node_leaf_count[i] > a.n_panels))
+                w = "leaf range out of bounds";
+            if (w) {
+                std::lock_guard<std::mutex> lk(mu);
+                if (i < bad_at.load()) { bad_at.store(i); why = w; }
+                return;
+            }
         }
-        if (a.node_leaf_first[i] < 0 || a.node_leaf_first[i] + a.node_leaf_count[i] > a.n_panels) return "leaf range out of bounds";
-    }
+        leaves_all += leaves;
+    });
+    if (bad_at.load() != INT64_MAX) return why;
+    int64_t leaves = leaves_all.load();
     if (leaves != a.n_panels) return "leaf count does not match n_panels";
     // link sources are range-checked on the device while they are relabelled
     int64_t next = 0;
@@ -1603,9 +1639,10 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
                       const std::vector<int32_t> &height, const std::vector<int32_t> &lab, cudaStream_t s) {
     int64_t Nn = a.n_nodes;
     std::vector<int32_t> blk_leaf_first, blk_nleaves, blk_lvl_first, blk_nlvls, blk_root, lvl_ptr, lvl_nodes;
-    std::vector<int32_t> top_cnt, hcount;
     std::vector<std::vector<int32_t>> top_by_h;
     int max_lv = 0;
+    // subtree roots (at most kBlockLeaves leaves, parent above that) and the
+    // top nodes by height, in post-order
     for (int64_t i = 0; i < Nn; i++) {
         int64_t lc = a.node_leaf_count[i];
         int32_t par = parent[i];
@@ -1614,28 +1651,46 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
             top_by_h[height[i]].push_back((int32_t)i);
             continue;
         }
-        if (par >= 0 && a.node_leaf_count[par] <= kBlockLeaves) continue;  // not a subtree root
-        // subtree root: nodes [i - (2*lc - 1) + 1, i] in post-order
-        int64_t first = i - (2 * lc - 1) + 1;
+        if (par >= 0 && a.node_leaf_count[par] <= kBlockLeaves) continue;
         int H = height[i];
         blk_leaf_first.push_back((int32_t)a.node_leaf_first[i]);
         blk_nleaves.push_back((int32_t)lc);
-        blk_lvl_first.push_back((int32_t)lvl_ptr.size());
+        blk_lvl_first.push_back(0);
         blk_nlvls.push_back(H);
         blk_root.push_back((int32_t)i);
-        // internal nodes of the subtree grouped by height (counting sort)
-        hcount.assign(H + 2, 0);
-        for (int64_t n = first; n <= i; n++)
-            if (!(a.node_type[n] & FCG_IS_LEAF)) hcount[height[n] + 1]++;
-        for (int h = 1; h <= H; h++) hcount[h + 1] += hcount[h];
-        size_t base = lvl_nodes.size();
-        lvl_nodes.resize(base + hcount[H + 1]);
-        for (int h = 1; h <= H; h++) lvl_ptr.push_back((int32_t)(base + hcount[h]));
-        lvl_ptr.push_back((int32_t)(base + hcount[H + 1]));
-        for (int64_t n = first; n <= i; n++)
-            if (!(a.node_type[n] & FCG_IS_LEAF)) lvl_nodes[base + hcount[height[n]]++] = (int32_t)n;
         max_lv = std::max(max_lv, H);
     }
+    // every block's level offsets (H+1 entries) and internal nodes (lc-1) get
+    // their own slots, so the blocks are filled on all host threads
+    int64_t nb = (int64_t)blk_root.size();
+    std::vector<int64_t> node_off(nb + 1, 0);
+    int64_t lvl_total = 0;
+    for (int64_t b = 0; b < nb; b++) {
+        blk_lvl_first[b] = (int32_t)lvl_total;
+        lvl_total += blk_nlvls[b] + 1;
+        node_off[b + 1] = node_off[b] + (blk_nleaves[b] - 1);
+    }
+    lvl_ptr.assign(lvl_total, 0);
+    lvl_nodes.assign(node_off[nb], 0);
+    parallel_for(nb, [&](int64_t b0, int64_t b1) {
+        std::vector<int32_t> hcount;
+        for (int64_t b = b0; b < b1; b++) {
+            int64_t i = blk_root[b], lc = blk_nleaves[b];
+            int64_t first = i - (2 * lc - 1) + 1;  // the subtree's nodes in post-order
+            int H = blk_nlvls[b];
+            int64_t base = node_off[b];
+            // internal nodes of the subtree grouped by height (counting sort)
+            hcount.assign(H + 2, 0);
+            for (int64_t n = first; n <= i; n++)
+                if (!(a.node_type[n] & FCG_IS_LEAF)) hcount[height[n] + 1]++;
+            for (int h = 1; h <= H; h++) hcount[h + 1] += hcount[h];
+            int32_t *lp = lvl_ptr.data() + blk_lvl_first[b];
+            for (int h = 1; h <= H; h++) lp[h - 1] = (int32_t)(base + hcount[h]);
+            lp[H] = (int32_t)(base + hcount[H + 1]);
+            for (int64_t n = first; n <= i; n++)
+                if (!(a.node_type[n] & FCG_IS_LEAF)) lvl_nodes[base + hcount[height[n]]++] = (int32_t)n;
+        }
+    });
     // the down-sweep sums a subtree root's ancestors from a bounded chain
     for (size_t b = 0; b < blk_root.size(); b++) {
         int depth = 0;
@@ -1739,8 +1794,10 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     }
     tr.mark("labels");
     std::vector<int32_t> parent(Nn, -1);
-    for (int64_t i = 0; i < Nn; i++)
-        if (!(a.node_type[i] & FCG_IS_LEAF)) { parent[a.node_left[i]] = (int32_t)i; parent[a.node_right[i]] = (int32_t)i; }
+    parallel_for(Nn, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; i++)
+            if (!(a.node_type[i] & FCG_IS_LEAF)) { parent[a.node_left[i]] = (int32_t)i; parent[a.node_right[i]] = (int32_t)i; }
+    });
     p->h_ptr_model.assign(a.link_ptr, a.link_ptr + Nn + 1);
     p->h_ptr_dev.assign(Nn + 1, 0);
     p->h_inv = inv;

@@ -114,3 +114,21 @@ def test_estimate_covers_solve(ctx, models):
         p.fill()
         _, it = p.solve(tol=1e-4)
         assert p.device_bytes <= fc.estimate_bytes(m, fc.PREC_MIXED, iterations=int(it.max()))
+
+
+def test_failed_job_does_not_stop_the_server(ctx, models):
+    """A job whose model is refused fails alone with its status and message;
+    the jobs around it complete."""
+    from conftest import load_golden, model_arrays
+    bad = {k: np.array(v, copy=True) for k, v in model_arrays(load_golden("crossing2x2_m05")).items()}
+    bad["link_src"][3] = len(bad["node_type"]) + 7
+    with ctx.server(slots=2) as srv:
+        jobs = [srv.submit(models[0], fc.PREC_MIXED, tol=1e-4), srv.submit(fc.Model.from_arrays(bad), fc.PREC_MIXED, tol=1e-4),
+                srv.submit(models[1], fc.PREC_MIXED, tol=1e-4)]
+        jobs[0].result()
+        with pytest.raises(fc.FCError) as e:
+            jobs[1].result()
+        assert "out of range" in str(e.value)
+        assert jobs[1].info["state"] == fc.JOB_DONE and jobs[1].info["status"] == fc.GENERIC_ERROR
+        jobs[2].result()
+        assert srv.stats()["completed"] == 3
