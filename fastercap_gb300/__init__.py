@@ -79,12 +79,13 @@ class ModelInfo(C.Structure):
 
 class ProblemStats(C.Structure):
     _fields_ = [("kernel_launches", C.c_int64), ("link_launches", C.c_int64), ("link_ms", C.c_double),
-                ("link_bytes", C.c_int64), ("fill_ms", C.c_double), ("solve_ms", C.c_double)]
+                ("link_bytes", C.c_int64), ("fill_ms", C.c_double), ("solve_ms", C.c_double),
+                ("refine_checks", C.c_int64), ("refine_cycles", C.c_int64)]
 
 
 class SolveOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("precond", C.c_int), ("max_iter", C.c_int), ("rhs_width", C.c_int),
-                ("precond_dim", C.c_int)]
+                ("precond_dim", C.c_int), ("refine", C.c_int)]
 
 
 class ServerConfig(C.Structure):
@@ -421,12 +422,13 @@ class Problem:
         return int(lib().fcg_problem_matvec_device_noalloc(self._h, C.c_void_p(q_ptr), C.c_void_p(v_ptr), k))
 
     def solve(self, tol: float = 0.01, precond: int = PRECOND_JACOBI, max_iter: int = 0, allow_not_converged=False,
-              rhs_width: int = 0, precond_dim: int = 0):
-        """(C, iterations); with geometries set, lists of per-geometry C and iterations."""
+              rhs_width: int = 0, precond_dim: int = 0, refine: int = 0):
+        """(C, iterations); with geometries set, lists of per-geometry C and iterations.
+        refine: true-residual restarts (0 default: up to 2 in mixed precision, -1 none)."""
         sizes = self.geometries or [self.n_cond]
         cap = np.empty(sum(n * n for n in sizes), np.float64)
         it = np.empty(sum(sizes), np.int32)
-        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
         self._last_width = min(rhs_width, 32) if rhs_width > 0 else 32
         code = lib().fcg_problem_solve(self._h, C.byref(opt), _ptr(cap), _ptr(it))
         if not (code == NORMAL_END or (allow_not_converged and code == NOT_CONVERGED)):
@@ -546,10 +548,10 @@ class Server:
         self._h = h
 
     def submit(self, model: Model, precision: int = PREC_MIXED, tol: float = 0.01, precond: int = PRECOND_JACOBI,
-               max_iter: int = 0, rhs_width: int = 0, precond_dim: int = 0) -> Job:
+               max_iter: int = 0, rhs_width: int = 0, precond_dim: int = 0, refine: int = 0) -> Job:
         arr = model.c_arrays()
         keep = model._keep
-        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
         jid = C.c_int64()
         _check(lib().fcg_server_submit(self._h, C.byref(arr), precision, C.byref(opt), C.byref(jid)), "submit")
         job = Job(self, jid.value, model, (arr, keep))

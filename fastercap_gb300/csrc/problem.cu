@@ -1339,6 +1339,14 @@ __global__ void k_iter_advance(int *iter, const int *__restrict__ n_active, int 
     if (use_cond) cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
+// solves whose true residual |b - A x| / |b| is at or above tol
+__global__ void k_refine_count(int S, const double *__restrict__ nr2, const double *__restrict__ nb2, double tol, int *count) {
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= S) return;
+    double nb = sqrt(nb2[sidx]);
+    if (nb > 0.0 && sqrt(nr2[sidx]) / nb >= tol) atomicAdd(count, 1);
+}
+
 // back substitution R z = g for every solve (one thread each)
 __global__ void k_backsub(int S, int M, double *const *__restrict__ Hc, const double *g, const int *iters, double *z) {
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2017,6 +2025,7 @@ void problem_reset_stats(DeviceProblem *p) {
     p->timings.launches = p->timings.link_launches = p->timings.link_bytes = 0;
     p->timings.link_ms = 0;
     p->timings.matvecs = 0;
+    p->timings.refine_checks = p->timings.refine_cycles = 0;
 }
 
 // event pair around one link-product launch (profiling mode)
@@ -2903,114 +2912,147 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         cudaEventRecord(p->ev0, s);
         k_set_rhs<<<g1, 256, 0, s>>>(Np, k, p->leaf_geom, d_sf, d_sc, p->b);
         double *V0 = basis_addr(p, 0);
-        double *pr = p->partial, *pb = p->partial + (size_t)k * nch;
+        // GMRES from x0 = P b (or 0), then, for the mixed path, up to `cycles`
+        // restarts from the current x while the true residual b - A x (not
+        // the recurrence's estimate) is at or above the tolerance
+        const int cycles = opt.refine < 0 ? 0 : (opt.refine > 0 ? opt.refine : (p->precision == FCG_PREC_MIXED ? 2 : 0));
         if (pre) {
             if ((r = precond_apply(p, pk, p->b, p->x0, k)) || (r = matvec(p, p->x0, p->w, k, NULL))) {
                 free_batch();
                 status = r;
                 break;
             }
-            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, chunks, p->vv, pr, pb);
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, chunks, p->vv, p->partial, p->partial + (size_t)k * nch);
         } else {
             FCG_CK(cudaMemsetAsync(p->x0, 0, n * sizeof(double), s));
-            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, NULL, chunks, p->vv, pr, pb);
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, NULL, chunks, p->vv, p->partial, p->partial + (size_t)k * nch);
         }
-        k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pr, p->g_ch_first, p->g_ch_count, NULL, p->nrm2, 1, 0);
-        k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pb, p->g_ch_first, p->g_ch_count, NULL, p->nrm2 + S, 1, 0);
-        FCG_CK(cudaMemsetAsync(p->g, 0, (size_t)S * (M + 2) * sizeof(double), s));
-        FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
-        k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
-                                        p->capped, p->n_active + M + 1);
-        k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL);
-        FCG_CK(cudaGetLastError());
-        p->timings.launches += pre ? 7 : 7;
-        // does any solve need an Arnoldi step?
+        std::vector<int> it_total(S, 0);
+        bool notconv = false;
         int *pin = p->pin ? p->pin : p->pin_local;
-        FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-        FCG_CK(cudaStreamSynchronize(s));
-        bool any = pin[0] > 0;
-        FCG_CK(cudaMemsetAsync(p->d_it, 0, 4 * sizeof(int), s));
-        if (pk == FCG_PRECOND_TWO_LEVEL && !p->ptmp && (r = dalloc(&p->ptmp, (size_t)k * Np, p->bytes))) {
-            free_batch();
-            status = r;
-            break;
-        }
-        StepArgs sa = {k, S, G, M, nch, M, pk, chunks, diag, opt.tol, 0, 0};
-        // the workspace a step touches exists before any capture
-        if ((r = ensure_matvec_ws(p, kpad(k))) ||
-            (pk == FCG_PRECOND_TWO_LEVEL && (r = precond_apply(p, pk, p->vv, p->ptmp, k)))) {
-            free_batch();
-            status = r;
-            break;
-        }
-        const bool use_graph = !p->profiling && getenv("FCG_NO_GRAPH") == NULL;
-        int steps = 0;  // Arnoldi steps taken
-        while (any && status == FCG_NORMAL_END) {
-            if (use_graph) {
-                // the whole loop in one graph launch, up to the basis capacity
-                int capv = std::min(M, std::max(32, 2 * steps));
-                sa.cap = capv;
-                if ((r = ensure_basis(p, capv)) || (r = ensure_partial(p, (size_t)k * capv * nch)) || (r = ensure_step_graph(p, sa))) {
-                    status = r;
-                    break;
-                }
-                FCG_CK(cudaGraphLaunch(p->gexec, s));
-                FCG_CK(cudaMemcpyAsync(pin, p->d_it, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
-                FCG_CK(cudaStreamSynchronize(s));
-                int ran = pin[0] - steps;
-                p->timings.launches += (int64_t)ran * p->g_launches;
-                p->timings.link_launches += (int64_t)ran * p->g_link_launches;
-                p->timings.link_bytes += (int64_t)ran * p->g_link_bytes;
-                p->timings.matvecs += ran;
-                steps = pin[0];
-                // stopped with solves still active: the basis is full (grow it) or a cancel
-                any = pin[2] > 0 && steps < M;
-            } else {
-                sa.cap = M;
-                if ((r = ensure_basis(p, steps + 1)) || (r = ensure_partial(p, (size_t)k * (steps + 1) * nch)) ||
-                    (r = enqueue_step(p, sa))) {
-                    status = r;
-                    break;
-                }
-                FCG_CK(cudaMemcpyAsync(pin, p->d_it, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
-                FCG_CK(cudaStreamSynchronize(s));
-                prof_collect(p);
-                steps = pin[0];
-                any = pin[1] != 0;
+        for (int cycle = 0; status == FCG_NORMAL_END; cycle++) {
+            double *pr = p->partial, *pb = p->partial + (size_t)k * nch;
+            k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pr, p->g_ch_first, p->g_ch_count, NULL, p->nrm2, 1, 0);
+            k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pb, p->g_ch_first, p->g_ch_count, NULL, p->nrm2 + S, 1, 0);
+            FCG_CK(cudaMemsetAsync(p->g, 0, (size_t)S * (M + 2) * sizeof(double), s));
+            FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
+            k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
+                                            p->capped, p->n_active + M + 1);
+            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL);
+            FCG_CK(cudaGetLastError());
+            p->timings.launches += 7;
+            // does any solve need an Arnoldi step?
+            FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FCG_CK(cudaStreamSynchronize(s));
+            bool any = pin[0] > 0;
+            FCG_CK(cudaMemsetAsync(p->d_it, 0, 4 * sizeof(int), s));
+            if (pk == FCG_PRECOND_TWO_LEVEL && !p->ptmp && (r = dalloc(&p->ptmp, (size_t)k * Np, p->bytes))) {
+                status = r;
+                break;
             }
-            if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
+            StepArgs sa = {k, S, G, M, nch, M, pk, chunks, diag, opt.tol, 0, 0};
+            // the workspace a step touches exists before any capture
+            if ((r = ensure_matvec_ws(p, kpad(k))) ||
+                (pk == FCG_PRECOND_TWO_LEVEL && (r = precond_apply(p, pk, p->vv, p->ptmp, k)))) {
+                status = r;
+                break;
+            }
+            const bool use_graph = !p->profiling && getenv("FCG_NO_GRAPH") == NULL;
+            int steps = 0;  // Arnoldi steps taken
+            while (any && status == FCG_NORMAL_END) {
+                if (use_graph) {
+                    // the whole loop in one graph launch, up to the basis capacity
+                    int capv = std::min(M, std::max(32, 2 * steps));
+                    sa.cap = capv;
+                    if ((r = ensure_basis(p, capv)) || (r = ensure_partial(p, (size_t)k * capv * nch)) || (r = ensure_step_graph(p, sa))) {
+                        status = r;
+                        break;
+                    }
+                    FCG_CK(cudaGraphLaunch(p->gexec, s));
+                    FCG_CK(cudaMemcpyAsync(pin, p->d_it, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+                    FCG_CK(cudaStreamSynchronize(s));
+                    int ran = pin[0] - steps;
+                    p->timings.launches += (int64_t)ran * p->g_launches;
+                    p->timings.link_launches += (int64_t)ran * p->g_link_launches;
+                    p->timings.link_bytes += (int64_t)ran * p->g_link_bytes;
+                    p->timings.matvecs += ran;
+                    steps = pin[0];
+                    // stopped with solves still active: the basis is full (grow it) or a cancel
+                    any = pin[2] > 0 && steps < M;
+                } else {
+                    sa.cap = M;
+                    if ((r = ensure_basis(p, steps + 1)) || (r = ensure_partial(p, (size_t)k * (steps + 1) * nch)) ||
+                        (r = enqueue_step(p, sa))) {
+                        status = r;
+                        break;
+                    }
+                    FCG_CK(cudaMemcpyAsync(pin, p->d_it, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+                    FCG_CK(cudaStreamSynchronize(s));
+                    prof_collect(p);
+                    steps = pin[0];
+                    any = pin[1] != 0;
+                }
+                if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
+            }
+            if (status != FCG_NORMAL_END) break;
+            k_backsub<<<gs, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
+            k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
+            if (pk == FCG_PRECOND_TWO_LEVEL) {
+                if ((r = precond_apply(p, pk, p->w, p->vv, k))) { status = r; break; }
+                k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->vv, NULL, p->iters, p->leaf_geom, p->x);
+            } else {
+                k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->leaf_geom, p->x);
+            }
+            p->timings.launches += 3;
+            {
+                std::vector<int> hb(2 * (size_t)S);
+                FCG_CK(cudaMemcpyAsync(hb.data(), p->iters, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+                FCG_CK(cudaMemcpyAsync(hb.data() + S, p->capped, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+                FCG_CK(cudaStreamSynchronize(s));
+                // a later cycle that converges clears an earlier cap
+                notconv = false;
+                for (int q = 0; q < S; q++) {
+                    it_total[q] += hb[q] + 1;
+                    notconv |= hb[S + q] != 0;
+                }
+            }
+            if (cycle >= cycles) break;
+            // true residual of x: r = b - A x, in vv and the chunk partials
+            if ((r = matvec(p, p->x, p->w, k, NULL))) { status = r; break; }
+            pr = p->partial;
+            pb = p->partial + (size_t)k * nch;
+            k_residual<<<dim3(nch, k), 256, 0, s>>>(Np, p->b, p->w, chunks, p->vv, pr, pb);
+            k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pr, p->g_ch_first, p->g_ch_count, NULL, p->nrm2, 1, 0);
+            k_reduce_seg<<<seg_grid(1), 256, 0, s>>>(1, k, G, nch, pb, p->g_ch_first, p->g_ch_count, NULL, p->nrm2 + S, 1, 0);
+            FCG_CK(cudaMemsetAsync(p->n_active + M + 1, 0, sizeof(int), s));
+            k_refine_count<<<gs, 128, 0, s>>>(S, p->nrm2, p->nrm2 + S, opt.tol, p->n_active + M + 1);
+            p->timings.launches += 4;
+            FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FCG_CK(cudaStreamSynchronize(s));
+            p->timings.refine_checks++;
+            if (pin[0] == 0) break;
+            // restart from x: x0 = x, the residual is already in vv
+            p->timings.refine_cycles++;
+            FCG_CK(cudaMemcpyAsync(p->x0, p->x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         }
         if (status != FCG_NORMAL_END) { free_batch(); break; }
-        k_backsub<<<gs, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
-        k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
-        if (pk == FCG_PRECOND_TWO_LEVEL) {
-            if ((r = precond_apply(p, pk, p->w, p->vv, k))) { free_batch(); status = r; break; }
-            k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->vv, NULL, p->iters, p->leaf_geom, p->x);
-        } else {
-            k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->w, diag, p->iters, p->leaf_geom, p->x);
-        }
         cudaEventRecord(p->ev1, s);
         if (nentry > 0) {
             k_assemble_part<<<dim3(nentry, nslice), 256, 0, s>>>(Np, d_es, d_ef, d_ec, p->leaf_weight, p->x, d_part);
             k_assemble_sum<<<(nentry + 127) / 128, 128, 0, s>>>(nentry, nslice, d_part, d_eo, d_cap);
         }
         FCG_CK(cudaGetLastError());
-        p->timings.launches += nentry > 0 ? 5 : 3;
-        std::vector<int> hb(2 * (size_t)S);
-        FCG_CK(cudaMemcpyAsync(hb.data(), p->iters, S * sizeof(int), cudaMemcpyDeviceToHost, s));
-        FCG_CK(cudaMemcpyAsync(hb.data() + S, p->capped, S * sizeof(int), cudaMemcpyDeviceToHost, s));
+        p->timings.launches += nentry > 0 ? 2 : 0;
         FCG_CK(cudaStreamSynchronize(s));
         prof_collect(p);
         float ms = 0;
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         solve_ms_total += ms;
-        bool notconv = false;
         for (int g = 0; g < G; g++)
             for (int rr = 0; rr < k && r0 + rr < ncol[g]; rr++) {
-                int sidx = g * k + rr, it = hb[sidx] + 1;
+                int sidx = g * k + rr, it = it_total[sidx];
                 h_iters[it_off[g] + r0 + rr] = it;
                 p->timings.iterations_max = std::max(p->timings.iterations_max, it);
-                notconv |= hb[S + sidx] != 0;
             }
         free_batch();
         any_capped |= notconv;

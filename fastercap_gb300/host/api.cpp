@@ -263,6 +263,7 @@ int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap,
     o.max_iter = 0;
     o.rhs_width = 0;
     o.precond_dim = 0;
+    o.refine = 0;
     if (opt) o = *opt;
     return fcg::problem_solve(p->p, o, cap, iterations);
 }
@@ -305,6 +306,8 @@ int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *st) {
     st->link_bytes = t.link_bytes;
     st->fill_ms = t.fill_ms;
     st->solve_ms = t.solve_ms;
+    st->refine_checks = t.refine_checks;
+    st->refine_cycles = t.refine_cycles;
     return FCG_NORMAL_END;
 }
 
@@ -457,7 +460,7 @@ static int solve_model(fcg_context *ctx, fcg_model *m, const CmdOptions &o, doub
     if (r == FCG_NORMAL_END) {
         out.cap.assign((size_t)out.nc * out.nc, 0.0);
         out.iters.assign(out.nc, 0);
-        fcg_solve_options so = {gmres_tol, kind, 0, 0, (int)dim};
+        fcg_solve_options so = {gmres_tol, kind, 0, 0, (int)dim, 0};
         r = fcg_problem_solve(p, &so, out.cap.data(), out.iters.data());
     }
     if (r != FCG_NORMAL_END && r != FCG_NOT_CONVERGED) {

@@ -218,6 +218,7 @@ int fcg_server_submit(fcg_server *s, const fcg_model_arrays *a, int precision, c
     j->opt.max_iter = 0;
     j->opt.rhs_width = 0;
     j->opt.precond_dim = 0;
+    j->opt.refine = 0;
     if (opt) j->opt = *opt;
     for (int32_t c = 0; c < a->n_conductors; c++) j->n_cond += (a->cond_is_diel && a->cond_is_diel[c]) ? 0 : 1;
     j->footprint = fcg::problem_estimate_bytes(*a, precision, j->n_cond, s->iterations_hint);

@@ -179,6 +179,9 @@ typedef struct {
     int max_iter;     /* 0: the reference's cap min(1000, n_panels) */
     int rhs_width;    /* right-hand sides per batched solve: 0 = up to 32, 1 = one at a time */
     int precond_dim;  /* two-level dimension (the number of -ps<dim>), clamped to [16, 4096]; 0 = 128 */
+    int refine;       /* restarts from the current solution while the true residual |b - A x| / |b| is
+                         at or above tol: 0 = default (up to 2 for FCG_PREC_MIXED, none for FP64),
+                         -1 = none, n > 0 = up to n */
 } fcg_solve_options;
 
 /* Declare that the problem holds several independent geometries: conductor c
@@ -228,6 +231,8 @@ typedef struct {
     int64_t link_bytes;       /* algorithmic bytes of those launches */
     double fill_ms;           /* device time of the last coefficient fill */
     double solve_ms;          /* device time of the last solve */
+    int64_t refine_checks;    /* true-residual checks after GMRES (mixed precision) */
+    int64_t refine_cycles;    /* GMRES restarts those checks caused */
 } fcg_problem_stats;
 int fcg_problem_set_profiling(fcg_problem *p, int enable);
 int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *stats);
