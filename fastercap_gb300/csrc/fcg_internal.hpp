@@ -5,6 +5,7 @@
 
 #include <stdint.h>
 #include <atomic>
+#include <map>
 #include <mutex>
 #include <vector>
 #include <string>
@@ -34,6 +35,9 @@ struct DeviceContext {
     int *pin = nullptr;
     std::mutex pin_mu;
     std::vector<int> pin_free;
+    // link-product launch shapes chosen by measurement, per problem shape
+    std::mutex tune_mu;
+    std::map<uint64_t, int> tune;
 };
 void context_release(DeviceContext &ctx);
 void context_unref(DeviceContext *ctx);

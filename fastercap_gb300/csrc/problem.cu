@@ -164,6 +164,7 @@ struct DeviceProblem {
     int spmv_lanes = 32;  // lanes per destination node in the link product (8, 16 or 32)
     int32_t *row_split = NULL;  // multi-right-hand-side link product: CTA b owns rows [row_split[b], row_split[b+1])
     int n_row_split = 0;
+    uint64_t tuned = 0;  // bit kp: the launch shape for kp right-hand sides is settled
 
     // two-level preconditioner (built for one dimension, kept until another is asked for)
     int sup_dim = -1;  // dimension it was built for (-1: never built)
@@ -1736,6 +1737,31 @@ static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::ve
     return FCG_NORMAL_END;
 }
 
+// Contiguous row ranges of about equal work (links + 8 per row) for the
+// multi-right-hand-side link product: ctas ranges (capped so that each has at
+// least 64 rows).
+static int set_row_split(DeviceProblem *p, int64_t ctas) {
+    int64_t Nn = p->Nn, L = p->L;
+    int64_t nb = std::max<int64_t>(1, std::min<int64_t>(ctas, (Nn + 63) / 64));
+    if (p->row_split && nb == p->n_row_split) return FCG_NORMAL_END;
+    std::vector<int32_t> split(nb + 1, 0);
+    double total = (double)L + 8.0 * (double)Nn;
+    int64_t row = 0;
+    for (int64_t b = 1; b < nb; b++) {
+        double target = total * (double)b / (double)nb;
+        while (row < Nn && (double)p->h_ptr_dev[row] + 8.0 * (double)row < target) row++;
+        split[b] = (int32_t)row;
+    }
+    split[nb] = (int32_t)Nn;
+    dfree(p->row_split);
+    p->n_row_split = 0;
+    int r = upload(&p->row_split, split.data(), split.size(), p->bytes, p->stream);
+    if (r != FCG_NORMAL_END) return r;
+    FCG_CK(cudaStreamSynchronize(p->stream));  // the host vector goes out of scope
+    p->n_row_split = (int)nb;
+    return FCG_NORMAL_END;
+}
+
 std::string model_check(const fcg_model_arrays &a) { return validate(a); }
 
 int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out) {
@@ -1897,22 +1923,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     FCG_TRY(build_plan(p, a, parent, height, lab, s));
     tr.mark("sweep plan");
     FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
-    {
-        // contiguous row ranges of about equal work (links + 8 per row) for
-        // the multi-right-hand-side link product, at least 64 rows each
-        int64_t nb = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx.sm_count * 32, (Nn + 63) / 64));
-        std::vector<int32_t> split(nb + 1, 0);
-        double total = (double)L + 8.0 * (double)Nn;
-        int64_t row = 0;
-        for (int64_t b = 1; b < nb; b++) {
-            double target = total * (double)b / (double)nb;
-            while (row < Nn && (double)p->h_ptr_dev[row] + 8.0 * (double)row < target) row++;
-            split[b] = (int32_t)row;
-        }
-        split[nb] = (int32_t)Nn;
-        p->n_row_split = (int)nb;
-        FCG_TRY(upload(&p->row_split, split.data(), split.size(), p->bytes, s));
-    }
+    FCG_TRY(set_row_split(p, (int64_t)ctx.sm_count * 32));
     // lanes per node in the link product: about four links per lane per pass
     {
         double avg = (double)a.n_links / (double)Nn;
@@ -2204,28 +2215,12 @@ struct NodeWork {
     double *Ad;
 };
 
-// The three launches of one product v = P * (in / diag): up-sweep, link
-// product, down-sweep. Arrays in/out are [k][Np] on the device.
-static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag) {
+// One link-product launch (the kernel follows kp, precision and the
+// problem's launch shape: lanes per row, CTA row ranges).
+static void launch_link(DeviceProblem *p, const NodeWork &w, int kp, bool mixed) {
     cudaStream_t s = p->stream;
-    bool mixed = p->precision == FCG_PREC_MIXED;
-    const SweepPlan &pl = p->plan;
-    int64_t Np = p->Np;
-    size_t n = (size_t)p->Nn * kp;
-    if (mixed) k_up<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
-    else k_up<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
-    FCG_CK(cudaGetLastError());
     int64_t rows_per_cta = 8 * (32 / p->spmv_lanes);
     int grid = (int)std::min<int64_t>((p->Nn + rows_per_cta - 1) / rows_per_cta, (int64_t)p->ctx->sm_count * 32);
-    int64_t launches = 2;
-    if (p->L > 0) {
-        // coefficient + source word per link, row offsets, one charge read and
-        // one potential write per node and right-hand side
-        int64_t cb = mixed ? 4 : 8;
-        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + (cb + 8) * (int64_t)k * p->Nn;
-        p->timings.link_launches++;
-        launches++;
-        prof_begin(p);
         int sw = p->spmv_lanes;
 #define FCG_SPMV(KK)                                                                                                  \
     do {                                                                                                              \
@@ -2274,6 +2269,29 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
 #undef FCG_MULTI32
 #undef FCG_MULTI64
 #undef FCG_SPMV
+}
+
+// The three launches of one product v = P * (in / diag): up-sweep, link
+// product, down-sweep. Arrays in/out are [k][Np] on the device.
+static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag) {
+    cudaStream_t s = p->stream;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    const SweepPlan &pl = p->plan;
+    int64_t Np = p->Np;
+    size_t n = (size_t)p->Nn * kp;
+    if (mixed) k_up<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
+    else k_up<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
+    FCG_CK(cudaGetLastError());
+    int64_t launches = 2;
+    if (p->L > 0) {
+        // coefficient + source word per link, row offsets, one charge read and
+        // one potential write per node and right-hand side
+        int64_t cb = mixed ? 4 : 8;
+        p->timings.link_bytes += p->L * (cb + 4) + 8 * (p->Nn + 1) + (cb + 8) * (int64_t)k * p->Nn;
+        p->timings.link_launches++;
+        launches++;
+        prof_begin(p);
+        launch_link(p, w, kp, mixed);
         prof_end(p);
         FCG_CK(cudaGetLastError());
     } else {
@@ -2288,11 +2306,78 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     return FCG_NORMAL_END;
 }
 
+// Autotuner of the mixed link product's launch shape, per problem shape
+// (kp, links per node, node count): lanes per row for one right-hand side
+// (8, 16, 32), CTA row ranges for several (SMs x 8..64). Each candidate is
+// timed over three launches with CUDA events on the problem's stream; the
+// winner is kept in the context, so later problems of the same shape reuse
+// it without measuring. Problems under 4M links keep the built-in choice.
+// FCG_SPMV_LANES pins the lanes.
+static int autotune(DeviceProblem *p, int kp) {
+    if (kp >= 64 || (p->tuned >> kp) & 1u) return FCG_NORMAL_END;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return FCG_NORMAL_END;
+    p->tuned |= 1ull << kp;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    bool single = kp <= 2;
+    if (!mixed || p->L < (int64_t)4 << 20 || (single && getenv("FCG_SPMV_LANES"))) return FCG_NORMAL_END;
+    DeviceContext &ctx = *p->ctx;
+    double avg = (double)p->L / (double)p->Nn;
+    uint64_t key = (uint64_t)kp | ((uint64_t)(int)(4.0 * log2(avg + 1.0)) << 8) | ((uint64_t)(int)log2((double)p->Nn) << 16);
+    int sms = ctx.sm_count;
+    auto apply = [&](int v) -> int {
+        if (single) { p->spmv_lanes = v; return FCG_NORMAL_END; }
+        return set_row_split(p, (int64_t)sms * v);
+    };
+    {
+        std::lock_guard<std::mutex> lk(ctx.tune_mu);
+        auto it = ctx.tune.find(key);
+        if (it != ctx.tune.end()) return apply(it->second);
+    }
+    std::vector<int> cand = single ? std::vector<int>{8, 16, 32} : std::vector<int>{8, 16, 32, 64};
+    NodeWork w = {p->Qd, p->Qf, p->Pd, p->Pf2, p->Ad};
+    float best_ms = 1e30f;
+    int best = single ? p->spmv_lanes : 32;
+    cudaEvent_t e0, e1;
+    FCG_CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        set_error("cannot create timing events");
+        return FCG_DEVICE_ERROR;
+    }
+    cudaError_t err = cudaSuccess;
+    for (int v : cand) {
+        int r = apply(v);
+        if (r != FCG_NORMAL_END) { cudaEventDestroy(e0); cudaEventDestroy(e1); return r; }
+        launch_link(p, w, kp, true);  // warm
+        cudaEventRecord(e0, p->stream);
+        for (int q = 0; q < 3; q++) launch_link(p, w, kp, true);
+        cudaEventRecord(e1, p->stream);
+        if ((err = cudaGetLastError()) != cudaSuccess || (err = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        p->timings.launches += 4;
+        if (ms < best_ms) { best_ms = ms; best = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) {
+        set_error(std::string("link-product tuning failed: ") + cudaGetErrorString(err));
+        return FCG_DEVICE_ERROR;
+    }
+    {
+        std::lock_guard<std::mutex> lk(ctx.tune_mu);
+        ctx.tune[key] = best;
+    }
+    return apply(best);
+}
+
 // v = P * (in / diag) for k right-hand sides ([k][Np] device arrays)
 static int matvec(DeviceProblem *p, const double *in, double *out, int k, const double *diag) {
     if (k < 1 || k > kMaxK) { set_error("right-hand sides per matvec must be in [1, 32]"); return FCG_GENERIC_ERROR; }
     int kp = kpad(k);
     int r = ensure_matvec_ws(p, kp);
+    if (r == FCG_NORMAL_END) r = autotune(p, kp);
     if (r != FCG_NORMAL_END) return r;
     NodeWork w = {p->Qd, p->Qf, p->Pd, p->Pf2, p->Ad};
     return launch_matvec(p, w, in, out, k, kp, diag);
@@ -2742,9 +2827,10 @@ static int ensure_step_graph(DeviceProblem *p, StepArgs a) {
     put(&a.tol, sizeof(a.tol));
     const void *ptrs[] = {p->w, p->vv, p->ptmp, p->partial, p->Vptr, p->Hptr, p->n_active, p->cs, p->sn, p->g, p->normb, p->nrm2,
                           p->hnorm, p->scap, p->active, p->iters, p->capped, p->leaf_geom, p->g_ch_first, p->g_ch_count, p->Qd,
+                          p->row_split,
                           p->Qf, p->Pd, p->Pf2, p->Ad, p->sup_T, p->sup_pot, p->sup_chg, p->d_it, p->pin_dev};
     put(ptrs, sizeof(ptrs));
-    int ints[] = {p->kcap, p->sup_m, p->sup_kcap, p->spmv_lanes, p->profiling ? 1 : 0};
+    int ints[] = {p->kcap, p->sup_m, p->sup_kcap, p->spmv_lanes, p->n_row_split, p->profiling ? 1 : 0};
     put(ints, sizeof(ints));
     if (p->gexec && key == p->gkey) return FCG_NORMAL_END;
     free_graph(p);
@@ -2952,7 +3038,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             }
             StepArgs sa = {k, S, G, M, nch, M, pk, chunks, diag, opt.tol, 0, 0};
             // the workspace a step touches exists before any capture
-            if ((r = ensure_matvec_ws(p, kpad(k))) ||
+            if ((r = ensure_matvec_ws(p, kpad(k))) || (r = autotune(p, kpad(k))) ||
                 (pk == FCG_PRECOND_TWO_LEVEL && (r = precond_apply(p, pk, p->vv, p->ptmp, k)))) {
                 status = r;
                 break;
