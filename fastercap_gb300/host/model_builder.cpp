@@ -34,6 +34,7 @@
 #include <string.h>
 #include <math.h>
 #include <unistd.h>
+#include <chrono>
 
 #include "../csrc/fc_potential.h"
 
@@ -917,11 +918,22 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
         B.files.clear();
     }
     B.base_dir = dir;
+    // FCG_TRACE=1 prints the builder's phases to stderr
+    const bool trace = getenv("FCG_TRACE") != NULL;
+    auto t_last = std::chrono::steady_clock::now();
+    auto mark = [&](const char *what) {
+        if (!trace) return;
+        auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "[fcg build] %-22s %9.3f ms\n", what, std::chrono::duration<double, std::milli>(now - t_last).count());
+        t_last = now;
+    };
     int ret = B.parse_file(base, NULL, false, d3(0, 0, 0), 1.0, "", 0.0, d3(0, 0, 0));
+    mark("parse");
     if (ret != FC_NORMAL_END) { err = B.err; return ret; }
     if (B.order.empty()) { err = "no panels found in the input file"; return FC_FILE_ERROR; }
 
     if ((ret = B.build_super()) != FC_NORMAL_END) { err = B.err; return ret; }
+    mark("super hierarchy");
 
     // adaptive mesh: mutual refinement of all conductor pairs, then self
     B.level = 0;
@@ -939,12 +951,15 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
         ret = B.discretize_self(B.conds[B.order[i]].top, panels, nodes);
         if (ret != FC_NORMAL_END) { err = B.err; return ret; }
     }
+    mark("mesh refinement");
     // links: mutual interactions of all conductor pairs, then self, conductor by conductor
     for (size_t i = 0; i < nc; i++) {
         for (size_t j = i + 1; j < nc; j++) B.refine_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top);
         B.refine_self(B.conds[B.order[i]].top);
     }
+    mark("link traversal");
     if ((ret = B.flatten(M)) != FC_NORMAL_END) { err = B.err; return ret; }
+    mark("flatten");
     M.input_panels = B.input_panels;
     M.raw_cond_panels = B.raw_cond;
     M.raw_diel_panels = B.raw_diel;
