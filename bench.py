@@ -139,8 +139,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def build_multi(workload: str):
-    """(concatenated model, geometry_of_conductor, [per-geometry models], build s, tol, link eps)"""
+def build_multi(workload: str, ctx=None):
+    """(concatenated model, geometry_of_conductor, [per-geometry models], build s, tol, link eps);
+    with a context the link construction of every geometry runs on its GPU"""
     import fastercap_gb300 as fc
     make, meps, dratio, tol = MULTI[workload]
     models = []
@@ -149,21 +150,33 @@ def build_multi(workload: str):
         for g, cr in enumerate(make()):
             path = os.path.join(tmp, "g%d.txt" % g)
             cr.write(path)
-            models.append(fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio))
+            models.append(fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio, ctx=ctx))
     model, geom = fc.Model.concat(models)
     return model, geom, models, time.perf_counter() - t0, tol, meps * dratio
 
 
-def build_model(workload: str):
+def build_model(workload: str, ctx=None, compare=False):
+    """(model, build s, tol, analytic C, link eps). With a context the link
+    construction runs on its GPU; `compare` also builds on the host alone and
+    returns its time as a sixth value after checking that the models agree."""
     import fastercap_gb300 as fc
     writer, meps, dratio, tol, analytic = WORKLOADS[workload]
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, workload + ".txt")
         writer(path)
         t0 = time.perf_counter()
-        model = fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio)
+        model = fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio, ctx=ctx)
         build_s = time.perf_counter() - t0
-    return model, build_s, tol, analytic, meps * dratio
+        if not compare:
+            return model, build_s, tol, analytic, meps * dratio
+        t0 = time.perf_counter()
+        host = fc.Model.build(path, mesh_eps=meps, eps_ratio=dratio)
+        host_s = time.perf_counter() - t0
+    for k in ("link_ptr", "link_src", "node_left", "node_vertices"):
+        if not np.array_equal(model.arrays[k], host.arrays[k]):
+            raise RuntimeError("device-built model differs from the host build in " + k)
+    del host
+    return model, build_s, tol, analytic, meps * dratio, host_s
 
 
 def model_bytes(model) -> int:
@@ -290,9 +303,9 @@ def run_gb300_multi(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    model, geom, models, build_s, tol, eps = build_multi(args.workload)
-    G = len(models)
     ctx = fc.Context(local_rank)
+    model, geom, models, build_s, tol, eps = build_multi(args.workload, ctx)
+    G = len(models)
     stream = ctx.stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -644,8 +657,11 @@ def run_gb300(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    model, build_s, tol, analytic, eps = build_model(args.workload)
     ctx = fc.Context(local_rank)
+    compare = rank == 0 and world == 1
+    built = build_model(args.workload, ctx, compare=compare)
+    model, build_s, tol, analytic, eps = built[:5]
+    host_build_s = built[5] if compare else None
     stream = ctx.stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -715,7 +731,9 @@ def run_gb300(args, rank, world, local_rank):
         "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99)),
         "config": {"workload": args.workload, "panels": model.n_panels, "links": model.n_links, "link_eps": eps,
                    "gmres_tol": tol, "precond": "jacobi", "rhs": len(model.conductor_names),
-                   "l2": "flushed between steps (256 MiB write)", "host_build_s": round(build_s, 3),
+                   "l2": "flushed between steps (256 MiB write)",
+                   "model_build_s": {"gpu_links": round(build_s, 3),
+                                     "host": round(host_build_s, 3) if host_build_s is not None else None},
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"value": world * args.steps / (sum(times64) / 1000.0), "unit": "solves/s",
                  "p50_ms": float(np.percentile(times64, 50)), "p99_ms": float(np.percentile(times64, 99)),

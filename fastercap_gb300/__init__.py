@@ -134,6 +134,7 @@ def lib() -> C.CDLL:
     L = C.CDLL(LIB_PATH)
     vp, i32, i64, dp, ip = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int)
     L.fcg_model_build.argtypes = [C.c_char_p, C.POINTER(BuildOptions), C.POINTER(vp), C.c_char_p, C.c_size_t]
+    L.fcg_model_build_on.argtypes = [vp, C.c_char_p, C.POINTER(BuildOptions), C.POINTER(vp), C.c_char_p, C.c_size_t]
     L.fcg_model_info_get.argtypes = [vp, C.POINTER(ModelInfo)]
     L.fcg_model_arrays_get.argtypes = [vp, C.POINTER(ModelArrays)]
     L.fcg_model_conductor_name.argtypes = [vp, i32]
@@ -210,12 +211,18 @@ class Model:
 
     @classmethod
     def build(cls, path: str, mesh_eps: float = 0.1, eps_ratio: float = 1.0, mesh_curv: float = 3.0,
-              verbose: bool = False) -> "Model":
+              verbose: bool = False, ctx: "Context" = None) -> "Model":
+        """Build the refined hierarchy and the links of a FastCap-format file.
+        With a Context the link construction runs on its GPU; the model is
+        the same, link order included."""
         L = lib()
         h = C.c_void_p()
         err = C.create_string_buffer(512)
         opt = BuildOptions(mesh_eps, eps_ratio, mesh_curv, 1 if verbose else 0)
-        code = L.fcg_model_build(os.fsencode(path), C.byref(opt), C.byref(h), err, 512)
+        if ctx is not None:
+            code = L.fcg_model_build_on(ctx._h, os.fsencode(path), C.byref(opt), C.byref(h), err, 512)
+        else:
+            code = L.fcg_model_build(os.fsencode(path), C.byref(opt), C.byref(h), err, 512)
         if code != NORMAL_END:
             raise FCError(code, "model build failed: " + err.value.decode(errors="replace"))
         return cls._from_handle(h)

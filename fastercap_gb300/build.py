@@ -27,6 +27,9 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 REFERENCE = os.environ.get("FCG_REFERENCE_DIR", "/root/reference")
+# per-file device flags: the link construction rounds every operation like the
+# host builder (no fused multiply-add), so both take the same decisions
+CU_FLAGS = {"link_build.cu": ["-fmad=false"]}
 
 LIB = os.path.join(HERE, "libfastercap_gb300.so")
 CLI = os.path.join(HERE, "fastercap_gb300")
@@ -68,8 +71,8 @@ def build(verbose: bool = False, reference: bool = True) -> None:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         if _newer(obj, [src] + headers):
-            cmds.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                                         "-c", src, "-o", obj])
+            cmds.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
+                        + CU_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj])
     for src in cpp:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)

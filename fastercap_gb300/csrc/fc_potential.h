@@ -564,4 +564,74 @@ FCG_HD double fcg_self_potential(unsigned type, const float *c, const float *v, 
     return fcg_potential_opt(fcg_widen(c), v) / FCG_FOUR_PI_TIMES_E0;
 }
 
+// ---------------------------------------------------------------- refinement
+// The element-pair tests of the adaptive mesh and of the link construction,
+// shared by the host model builder and the device link construction. `E` is
+// any element record with float v[9], c[3], n[3], an integer `type`, double
+// `area` and `maxside` and int32 `left` / `right` children. Both sides are
+// compiled without contraction (host -ffp-contract=off, device -fmad=false);
+// the operations are +, -, *, / and sqrt only, so host and device take
+// bit-identical decisions.
+
+// Centroid distance vector (float difference, widened), its modulus and the
+// larger of the two elements' longest sides (the preamble of
+// CAutoRefine::RefineMutual, Solver/Autorefine.cpp:3112-3121).
+template <class E>
+FCG_HD void fcg_pair_span(const E &A, const E &B, fcg_d3 *dist, double *rdist, double *rmax) {
+    *dist = fcg_fsub(A.c, B.c);
+    *rdist = fcg_mod(*dist);
+    double r1 = A.maxside, r2 = B.maxside;
+    *rmax = r1 > r2 ? r1 : r2;
+}
+
+// CAutoRefine::RefineCriteria (Solver/Autorefine.cpp:2928-3003): the one-way
+// potential estimate of each element at the other's centroid (normal field
+// for a dielectric evaluation element; rule-2 quadrature when the centroids
+// are closer than twice the larger side, the point formula beyond), weighted
+// by the source's area (and longest side, for a dielectric) relative to the
+// model's largest. True when either weight exceeds `e`.
+template <class E>
+FCG_HD bool fcg_refine_criteria(const E &A, const E &B, fcg_d3 dist, double rdist, double rmax, double e, double ccoeff,
+                                double max_side, double max_area, double *c1, double *c2) {
+    bool force = false;
+    fcg_d3 n1 = fcg_diel_normal(A.type, A.n), n2 = fcg_diel_normal(B.type, B.n);
+    double pe1, pe2;
+    bool d1 = (A.type & FCG_IS_DIEL) != 0, d2 = (B.type & FCG_IS_DIEL) != 0;
+    if (rdist / rmax < 2.0) {
+        fcg_d3 ca = fcg_widen(A.c), cb = fcg_widen(B.c);
+        pe1 = d1 ? fcg_enfield_numerical(ca, B.v, n1, 2) : fcg_potential_numerical(ca, B.v, 2);
+        pe2 = d2 ? fcg_enfield_numerical(cb, A.v, n2, 2) : fcg_potential_numerical(cb, A.v, 2);
+    } else {
+        if (d1) pe1 = (dist.x * n1.x + dist.y * n1.y + dist.z * n1.z) / (rdist * rdist * rdist);
+        else pe1 = 1.0 / rdist;
+        if (d2) pe2 = (-dist.x * n2.x + -dist.y * n2.y + -dist.z * n2.z) / (rdist * rdist * rdist);
+        else pe2 = 1.0 / rdist;
+    }
+    if (d1) *c1 = fabs(pe1 * B.area * B.maxside / (max_side * max_area * ccoeff));
+    else *c1 = fabs(pe1 * B.area / (max_area * ccoeff));
+    if (*c1 > e) force = true;
+    if (d2) *c2 = fabs(pe2 * A.area * A.maxside / (max_side * max_area * ccoeff));
+    else *c2 = fabs(pe2 * A.area / (max_area * ccoeff));
+    if (*c2 > e) force = true;
+    return force;
+}
+
+// One step of CAutoRefine::RefineMutual (Solver/Autorefine.cpp:3096-3235):
+// 0 = the pair interacts through one link; 1 = recurse into A's children;
+// 2 = recurse into B's children. Two leaves always link; otherwise the pair
+// is split when the criteria at link tolerance `eps` fail, on the non-leaf
+// side, or on the larger-area side when both have children.
+template <class E>
+FCG_HD int fcg_link_decision(const E &A, const E &B, double eps, double max_side, double max_area) {
+    bool leaf1 = (A.type & FCG_IS_LEAF) != 0, leaf2 = (B.type & FCG_IS_LEAF) != 0;
+    if (leaf1 && leaf2) return 0;
+    fcg_d3 dist;
+    double rdist, rmax, c1, c2;
+    fcg_pair_span(A, B, &dist, &rdist, &rmax);
+    if (!fcg_refine_criteria(A, B, dist, rdist, rmax, eps, 1.0, max_side, max_area, &c1, &c2)) return 0;
+    if (!leaf1 && leaf2) return 1;
+    if (leaf1 && !leaf2) return 2;
+    return A.area > B.area ? 1 : 2;
+}
+
 #endif

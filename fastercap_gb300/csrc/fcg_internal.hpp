@@ -66,6 +66,18 @@ void problem_cancel(DeviceProblem *p);
 // right-hand sides in at most `iterations` Arnoldi steps
 int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs, int iterations);
 
+// Link construction on the device (csrc/link_build.cu): the traversal of
+// the element hierarchy `el` from the root pairs (root_a[i], root_b[i]),
+// visited at recursion level root_level[i], in the host builder's order;
+// node_of maps element ids to node ids. Fills link_ptr (n_nodes + 1) and
+// link_src exactly as the host traversal and its stable bucketing do, and
+// max_level with the deepest recursion level of the traversal.
+struct Element;
+int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const int32_t *root_a, const int32_t *root_b,
+                      const uint16_t *root_level, int64_t n_roots, const int32_t *node_of, int64_t n_nodes, double eps,
+                      double max_side, double max_area, std::vector<int64_t> &link_ptr, std::vector<int32_t> &link_src,
+                      int &max_level, std::string &err);
+
 // CUDA streams for host code compiled without the CUDA headers
 void *stream_create(int device);
 void stream_destroy(int device, void *stream);

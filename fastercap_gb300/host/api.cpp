@@ -51,6 +51,11 @@ static void finish_model(fcg_model *fm) {
 extern "C" {
 
 int fcg_model_build(const char *path, const fcg_build_options *opt, fcg_model **out, char *err, size_t err_len) {
+    return fcg_model_build_on(NULL, path, opt, out, err, err_len);
+}
+
+int fcg_model_build_on(fcg_context *ctx, const char *path, const fcg_build_options *opt, fcg_model **out, char *err,
+                       size_t err_len) {
     if (!path || !out) return FCG_GENERIC_ERROR;
     *out = NULL;
     fcg::BuildOptions o;
@@ -65,7 +70,7 @@ int fcg_model_build(const char *path, const fcg_build_options *opt, fcg_model **
     std::string e;
     int r;
     try {
-        r = fcg::build_model(path, o, fm->m, e);
+        r = fcg::build_model(path, o, fm->m, e, ctx ? ctx->dev : nullptr);
     } catch (std::bad_alloc &) {
         r = FCG_OUT_OF_MEMORY;
         e = "out of host memory while building the model";
@@ -426,10 +431,11 @@ struct SolveRun {
     int64_t device_bytes = 0;
 };
 
-static int build_model_at(const CmdOptions &o, double mesh_eps, fcg_model **m, fcg_model_info &info) {
+// the link construction runs on the console's GPU
+static int build_model_at(fcg_context *ctx, const CmdOptions &o, double mesh_eps, fcg_model **m, fcg_model_info &info) {
     fcg_build_options bo = {mesh_eps, o.eps_ratio, o.mesh_curv, o.verbose ? 1 : 0};
     char ebuf[512];
-    int r = fcg_model_build(o.file.c_str(), &bo, m, ebuf, sizeof ebuf);
+    int r = fcg_model_build_on(ctx, o.file.c_str(), &bo, m, ebuf, sizeof ebuf);
     if (r != FCG_NORMAL_END) { printf("Error: %s\n", ebuf); return r; }
     fcg_model_info_get(*m, &info);
     return FCG_NORMAL_END;
@@ -570,16 +576,23 @@ static int run_command_line_impl(const char *command_line) {
     fcg_model *m = NULL;
     SolveRun run;
     int r;
+    // an unreadable input is reported before the device is touched
+    if (FILE *f = fopen(o.file.c_str(), "rb")) {
+        fclose(f);
+    } else {
+        printf("Error: cannot open file '%s'\n", o.file.c_str());
+        return FCG_CANNOT_OPEN_FILE;
+    }
     if (!o.automatic) {
         // manual settings (CSolveCap::Run, Solver/SolveCapacitance.cpp:479-531)
+        r = fcg_context_create(0, &ctx);
+        if (r != FCG_NORMAL_END) { printf("Error: %s\n", fcg_last_error()); return r; }
         auto tb = std::chrono::steady_clock::now();
-        r = build_model_at(o, o.mesh_eps, &m, run.info);
-        if (r != FCG_NORMAL_END) return r;
+        r = build_model_at(ctx, o, o.mesh_eps, &m, run.info);
+        if (r != FCG_NORMAL_END) { fcg_context_destroy(ctx); return r; }
         run.build_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - tb).count();
         printf("Mesh refinement (-m): %g\nGMRES tolerance (-t): %g\n", o.mesh_eps, o.gmres_tol);
-        r = fcg_context_create(0, &ctx);
-        if (r != FCG_NORMAL_END) printf("Error: %s\n", fcg_last_error());
-        else r = solve_model(ctx, m, o, o.gmres_tol, kind, dim, run);
+        r = solve_model(ctx, m, o, o.gmres_tol, kind, dim, run);
     } else {
         // automatic refinement (CSolveCap::Run auto branch,
         // Solver/SolveCapacitance.cpp:294-477): start unrefined, then divide
@@ -592,7 +605,7 @@ static int run_command_line_impl(const char *command_line) {
         r = fcg_context_create(0, &ctx);
         if (r != FCG_NORMAL_END) { printf("Error: %s\n", fcg_last_error()); return r; }
         printf("\nIteration number #0 ***************************\n\n");
-        r = build_model_at(o, 1e32, &m, run.info);
+        r = build_model_at(ctx, o, 1e32, &m, run.info);
         if (r == FCG_NORMAL_END) {
             printf("Mesh refinement (-m): %g\n", 1e32);
             if (o.auto_precond) auto_precond(run.info.n_links, (int)(run.info.n_conductors - run.info.n_dielectrics), kind, dim);
@@ -607,7 +620,7 @@ static int run_command_line_impl(const char *command_line) {
                 meps = run.info.max_mesh_eps / sqrt(2.0);
                 fcg_model_free(m);
                 m = NULL;
-                r = build_model_at(o, meps, &m, run.info);
+                r = build_model_at(ctx, o, meps, &m, run.info);
                 if (r != FCG_NORMAL_END) break;
                 enough = run.info.n_links > old_links * 1.1 && run.info.n_panels > old_panels * 1.1;
                 if (!enough)

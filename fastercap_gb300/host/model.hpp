@@ -82,9 +82,12 @@ enum Status {
     FC_USER_BREAK = 125,
 };
 
+struct DeviceContext;
+
 // Parse, build the super hierarchy, refine the mesh, construct the links and
-// flatten. Returns an FC_* status; on error `err` holds a message.
-int build_model(const std::string &path, const BuildOptions &opt, Model &out, std::string &err);
+// flatten. Returns an FC_* status; on error `err` holds a message. With a
+// device context the link construction runs on that GPU (same arrays).
+int build_model(const std::string &path, const BuildOptions &opt, Model &out, std::string &err, DeviceContext *dev = nullptr);
 
 }  // namespace fcg
 

@@ -37,6 +37,7 @@
 #include <chrono>
 
 #include "../csrc/fc_potential.h"
+#include "../csrc/fcg_internal.hpp"
 
 namespace fcg {
 namespace {
@@ -692,28 +693,7 @@ struct Builder {
     }
 
     bool refine_criteria(double *c1, double *c2, int p1, int p2, D3 dist, double rdist, double rmax, double e, double ccoeff) {
-        const Element &A = el[p1], &B = el[p2];
-        bool force = false;
-        fcg_d3 n1 = fcg_diel_normal(A.type, A.n), n2 = fcg_diel_normal(B.type, B.n);
-        double pe1, pe2;
-        bool d1 = (A.type & FCG_IS_DIEL), d2 = (B.type & FCG_IS_DIEL);
-        if (rdist / rmax < 2.0) {
-            fcg_d3 ca = fcg_widen(A.c), cb = fcg_widen(B.c);
-            pe1 = d1 ? fcg_enfield_numerical(ca, B.v, n1, 2) : fcg_potential_numerical(ca, B.v, 2);
-            pe2 = d2 ? fcg_enfield_numerical(cb, A.v, n2, 2) : fcg_potential_numerical(cb, A.v, 2);
-        } else {
-            if (d1) pe1 = (dist.x * n1.x + dist.y * n1.y + dist.z * n1.z) / (rdist * rdist * rdist);
-            else pe1 = 1.0f / rdist;
-            if (d2) pe2 = (-dist.x * n2.x + -dist.y * n2.y + -dist.z * n2.z) / (rdist * rdist * rdist);
-            else pe2 = 1.0f / rdist;
-        }
-        if (d1) *c1 = fabs(pe1 * B.area * B.maxside / (max_side * max_area * ccoeff));
-        else *c1 = fabs(pe1 * B.area / (max_area * ccoeff));
-        if (*c1 > e) force = true;
-        if (d2) *c2 = fabs(pe2 * A.area * A.maxside / (max_side * max_area * ccoeff));
-        else *c2 = fabs(pe2 * A.area / (max_area * ccoeff));
-        if (*c2 > e) force = true;
-        return force;
+        return fcg_refine_criteria(el[p1], el[p2], fcg_mk(dist.x, dist.y, dist.z), rdist, rmax, e, ccoeff, max_side, max_area, c1, c2);
     }
 
     int discretize_mutual(int p1, int p2, bool selfc) {
@@ -768,26 +748,10 @@ struct Builder {
     void refine_mutual(int p1, int p2) {
         level++;
         if (level > max_level) max_level = level;
-        D3 dist = fsub(el[p1].c, el[p2].c);
-        double rdist = mod(dist);
-        double r1 = el[p1].maxside, r2 = el[p2].maxside;
-        double rmax = r1 > r2 ? r1 : r2;
-        bool leaf1 = el[p1].type & FCG_IS_LEAF, leaf2 = el[p2].type & FCG_IS_LEAF;
-        bool force = false;
-        if (!leaf1 || !leaf2) {
-            double c1, c2;
-            force = refine_criteria(&c1, &c2, p1, p2, dist, rdist, rmax, eps, 1.0f);
-        }
-        if (force) {
-            int which;
-            if (!leaf1 && leaf2) which = 1;
-            else if (leaf1 && !leaf2) which = 2;
-            else which = (el[p1].area > el[p2].area) ? 1 : 2;
-            if (which == 1) { refine_mutual(el[p1].left, p2); refine_mutual(el[p1].right, p2); }
-            else { refine_mutual(p1, el[p2].left); refine_mutual(p1, el[p2].right); }
-        } else {
-            pairs.push_back(std::make_pair(p1, p2));
-        }
+        int which = fcg_link_decision(el[p1], el[p2], eps, max_side, max_area);
+        if (which == 1) { refine_mutual(el[p1].left, p2); refine_mutual(el[p1].right, p2); }
+        else if (which == 2) { refine_mutual(p1, el[p2].left); refine_mutual(p1, el[p2].right); }
+        else pairs.push_back(std::make_pair(p1, p2));
         level--;
     }
 
@@ -802,8 +766,51 @@ struct Builder {
         level--;
     }
 
+    // ---------------------------------------------------------------- device links
+    // The root pairs of the link traversal in the host order (per conductor:
+    // its mutual pairs with the later conductors, then the self pairs of its
+    // internal elements in pre-order), each with the recursion level at which
+    // refine_mutual visits it; the traversal itself runs on the device
+    // (link_build_device) and yields the same rows as the host traversal.
+    int device_links(Model &M, const std::vector<int32_t> &node_of, DeviceContext &dev) {
+        std::vector<int32_t> ra, rb;
+        std::vector<uint16_t> rl;
+        int self_level = 0;
+        std::vector<std::pair<int32_t, int>> st;
+        for (size_t i = 0; i < order.size(); i++) {
+            int32_t ti = conds[order[i]].top;
+            for (size_t j = i + 1; j < order.size(); j++) {
+                ra.push_back(ti);
+                rb.push_back(conds[order[j]].top);
+                rl.push_back(1);
+            }
+            st.push_back(std::make_pair(ti, 0));
+            while (!st.empty()) {
+                int32_t id = st.back().first;
+                int s = st.back().second;
+                st.pop_back();
+                if (s + 1 > self_level) self_level = s + 1;  // refine_self's own level
+                if (el[id].type & FCG_IS_LEAF) continue;
+                if (s + 2 > 0xffff) { err = "element hierarchy too deep for the device link construction"; return FC_GENERIC_ERROR; }
+                ra.push_back(el[id].left);
+                rb.push_back(el[id].right);
+                rl.push_back((uint16_t)(s + 2));
+                st.push_back(std::make_pair(el[id].right, s + 1));
+                st.push_back(std::make_pair(el[id].left, s + 1));
+            }
+        }
+        int lvl = 0;
+        int r = link_build_device(dev, el.data(), (int64_t)el.size(), ra.data(), rb.data(), rl.data(), (int64_t)ra.size(),
+                                  node_of.data(), M.n_nodes, eps, max_side, max_area, M.link_ptr, M.link_src, lvl, err);
+        if (r != FC_NORMAL_END) return r;
+        M.n_links = (int64_t)M.link_src.size();
+        if (self_level > max_level) max_level = self_level;
+        if (lvl > max_level) max_level = lvl;
+        return FC_NORMAL_END;
+    }
+
     // ---------------------------------------------------------------- flatten
-    int flatten(Model &M) {
+    int flatten(Model &M, DeviceContext *dev) {
         size_t ne = el.size();
         std::vector<int32_t> node_of(ne, -1);
         std::vector<int32_t> post;
@@ -875,6 +882,7 @@ struct Builder {
                 M.leaf_diel[M.leaf_first[i]] = (e.type & FCG_IS_DIEL) ? 0 : e.diel;
             }
         }
+        if (dev) return device_links(M, node_of, *dev);
         // links: stable counting sort of the emitted pairs by destination node
         std::vector<int64_t> cnt(Nn + 1, 0);
         for (size_t k = 0; k < pairs.size(); k++) { cnt[node_of[pairs[k].first]]++; cnt[node_of[pairs[k].second]]++; }
@@ -893,7 +901,7 @@ struct Builder {
 
 }  // namespace
 
-int build_model(const std::string &path, const BuildOptions &opt, Model &M, std::string &err) {
+int build_model(const std::string &path, const BuildOptions &opt, Model &M, std::string &err, DeviceContext *dev) {
     Builder B;
     B.opt = opt;
     for (int i = 0; i < kMaxParseLevel + 2; i++) B.group_num[i] = 1;
@@ -952,13 +960,16 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
         if (ret != FC_NORMAL_END) { err = B.err; return ret; }
     }
     mark("mesh refinement");
-    // links: mutual interactions of all conductor pairs, then self, conductor by conductor
-    for (size_t i = 0; i < nc; i++) {
-        for (size_t j = i + 1; j < nc; j++) B.refine_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top);
-        B.refine_self(B.conds[B.order[i]].top);
+    // links: mutual interactions of all conductor pairs, then self, conductor
+    // by conductor (on the device, inside flatten, when a context is given)
+    if (!dev) {
+        for (size_t i = 0; i < nc; i++) {
+            for (size_t j = i + 1; j < nc; j++) B.refine_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top);
+            B.refine_self(B.conds[B.order[i]].top);
+        }
+        mark("link traversal");
     }
-    mark("link traversal");
-    if ((ret = B.flatten(M)) != FC_NORMAL_END) { err = B.err; return ret; }
+    if ((ret = B.flatten(M, dev)) != FC_NORMAL_END) { err = B.err; return ret; }
     mark("flatten");
     M.input_panels = B.input_panels;
     M.raw_cond_panels = B.raw_cond;

@@ -99,6 +99,14 @@ typedef struct {
  * (Solver/Autorefine.cpp:293) and the link-store pass and indexing of
  * CAutoRefine::AutoRefineLinks (Solver/Autorefine.cpp:481-728). */
 int fcg_model_build(const char *path, const fcg_build_options *opt, fcg_model **out, char *err, size_t err_len);
+/* fcg_model_build with the link construction (the hierarchical traversal of
+ * CAutoRefine::RefineMutual / RefineSelf, Solver/Autorefine.cpp:3096-3235,
+ * 2115-2229, and the per-node link lists of CAutoRefine::RecurseIndex,
+ * Solver/Autorefine.cpp:1173-1220) on the context's GPU. The model is
+ * identical to fcg_model_build's, link order included. A NULL context
+ * builds on the host. */
+int fcg_model_build_on(fcg_context *ctx, const char *path, const fcg_build_options *opt, fcg_model **out, char *err,
+                       size_t err_len);
 int fcg_model_info_get(const fcg_model *m, fcg_model_info *info);
 /* views into the model's arrays (valid until fcg_model_free) */
 int fcg_model_arrays_get(const fcg_model *m, fcg_model_arrays *arrays);
