@@ -25,6 +25,9 @@
 // device takes exactly the host's decisions and produces the same arrays.
 #include <cuda_runtime.h>
 
+#include <stdio.h>
+#include <stdlib.h>
+
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -141,27 +144,201 @@ __global__ void __launch_bounds__(kThreads) k_scan_apply(int64_t n, const TI *in
 }
 
 // ------------------------------------------------------------------ traversal
-// decide every frontier pair: 0 link, 1 split the first element, 2 the second
-__global__ void __launch_bounds__(kThreads) k_decide(int64_t n, const int2 *__restrict__ pairs, const uint16_t *__restrict__ root_level,
-                                                     int depth, const Element *__restrict__ el, double eps, double max_side,
-                                                     double max_area, uint8_t *flag, long long *tile_sums, int *max_level) {
+// FP32 pre-test. Most pairs are far from every decision boundary of the FP64
+// test (the rho = 2 switch between quadrature and point formula, the
+// threshold e itself), so an FP32 evaluation with a bound on its distance to
+// the FP64 value decides them; the rest (typically a few per cent) take the
+// FP64 test. Bounds are deliberately loose (a factor 4 and more over a
+// first-order rounding analysis): a loose bound only sends more pairs to
+// FP64, it never changes a decision.
+constexpr float kU = 5.9604645e-8f;  // 2^-24, unit roundoff of float
+
+// unit normal of a dielectric evaluation element (fcg_diel_normal in FP32);
+// false when a super node's normal is within rounding of the 1e-12 cut-off
+__device__ __forceinline__ bool diel_normal32(unsigned type, const float *n, float &x, float &y, float &z) {
+    x = n[0];
+    y = n[1];
+    z = n[2];
+    if (type & FCG_IS_SUPER_NODE) {
+        float m = sqrtf(x * x + y * y + z * z);
+        const float cut = (float)FCG_PANEL_EPS;
+        if (!(fabsf(m - cut) > 1e-5f * cut)) return false;
+        if (m < cut) {
+            x = y = z = 0.0f;
+        } else {
+            x /= m;
+            y /= m;
+            z /= m;
+        }
+    }
+    if ((type & FCG_OUTPERM_NORMAL_DIR) != FCG_OUTPERM_NORMAL_DIR) {
+        x = -x;
+        y = -y;
+        z = -z;
+    }
+    return true;
+}
+
+// rule-2 average over source triangle v (centroid c) of 1/|r - p| or, for a
+// field, (r - p).n / |r - p|^3, at r = c + d; `err` bounds the distance to
+// fcg_potential_numerical / fcg_enfield_numerical (rule 2)
+__device__ __forceinline__ bool quad2_32(float dx, float dy, float dz, const float *v, const float *c, bool efield, float nx,
+                                         float ny, float nz, float &val, float &err) {
+    float s1x = v[3] - v[0], s1y = v[4] - v[1], s1z = v[5] - v[2];
+    float s2x = v[6] - v[3], s2y = v[7] - v[4], s2z = v[8] - v[5];
+    float s3x = v[0] - v[6], s3y = v[1] - v[7], s3z = v[2] - v[8];
+    float nX = s1y * s2z - s1z * s2y, nY = -s1x * s2z + s1z * s2x, nZ = s1x * s2y - s1y * s2x;
+    float mn = sqrtf(nX * nX + nY * nY + nZ * nZ);
+    float m1 = sqrtf(s1x * s1x + s1y * s1y + s1z * s1z);
+    float m2 = sqrtf(s2x * s2x + s2y * s2y + s2z * s2z);
+    float m3 = sqrtf(s3x * s3x + s3y * s3y + s3z * s3z);
+    if (!(mn > 0.0f) || !(m1 > 0.0f)) return false;
+    float skew = (m1 * m2) / mn;  // 1 / sin of the angle between sides 1 and 2
+    float zx = nX / mn, zy = nY / mn, zz = nZ / mn;
+    float xx = s1x / m1, xy = s1y / m1, xz = s1z / m1;
+    float yx = xy * zz - xz * zy, yy = xz * zx - xx * zz, yz = xx * zy - xy * zx;
+    float v01 = m1, v02 = -(s3x * xx + s3y * xy + s3z * xz), v12 = -(s3x * yx + s3y * yy + s3z * yz);
+    float ratio = ((v02 - v01) * v12 - v12 * v02) / mn;  // jacobian / (2 area): +-1 up to rounding
+    float ox = v[0] - c[0], oy = v[1] - c[1], oz = v[2] - c[2];
+    float side = fmaxf(m1, fmaxf(m2, m3));
+    float dd = sqrtf(dx * dx + dy * dy + dz * dz);
+    // position error of a quadrature point relative to r, against the FP64 path
+    float ep = 64.0f * kU * (dd + 3.0f * side * skew);
+    const float a = 1.0f / 6.0f, b = 4.0f / 6.0f, w = 1.0f / 3.0f;
+    float sum = 0.0f, bnd = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        float px = i == 0 ? b : a, py = i == 1 ? b : a;
+        float p0 = (v01 - v02) * px + v02 * (1.0f - py);
+        float p1 = v12 * (1.0f - px - py);
+        float ex = dx - (ox + xx * p0 + yx * p1);
+        float ey = dy - (oy + xy * p0 + yy * p1);
+        float ez = dz - (oz + xz * p0 + yz * p1);
+        float r2 = ex * ex + ey * ey + ez * ez;
+        float r = sqrtf(r2);
+        if (!(r > 2.0f * ep)) return false;  // a point within rounding of r: FP64 decides
+        float ir = 1.0f / r;
+        if (efield) {
+            float t = (ex * nx + ey * ny + ez * nz) * ir * ir * ir;
+            sum += w * t;
+            bnd += w * (8.0f * ep * ir * ir * ir + 16.0f * kU * ir * ir);
+        } else {
+            sum += w * ir;
+            bnd += w * (4.0f * ep * ir * ir + 16.0f * kU * ir);
+        }
+    }
+    val = sum * ratio;
+    err = 4.0f * (bnd * fabsf(ratio) + (64.0f * kU * skew + 1e-6f) * fabsf(val));
+    return isfinite(val) && isfinite(err);
+}
+
+// one direction of CAutoRefine::RefineCriteria in FP32: the weight of source
+// S seen from evaluation element E (d = E.c - S.c), with its error bound
+__device__ __forceinline__ bool weight32(const Element &E, const Element &S, float dx, float dy, float dz, float r, bool quad,
+                                         float inv_max_area, float inv_max_side, float &cw, float &err) {
+    bool diel = (E.type & FCG_IS_DIEL) != 0;
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (diel && !diel_normal32(E.type, E.n, nx, ny, nz)) return false;
+    float pe, pe_err;
+    if (quad) {
+        if (!quad2_32(dx, dy, dz, S.v, S.c, diel, nx, ny, nz, pe, pe_err)) return false;
+    } else {
+        float ir = 1.0f / r;
+        if (diel) {
+            pe = (dx * nx + dy * ny + dz * nz) * ir * ir * ir;
+            pe_err = 4.0f * (16.0f * kU * ir * ir + 16.0f * kU * fabsf(pe));
+        } else {
+            pe = ir;
+            pe_err = 16.0f * kU * ir;
+        }
+    }
+    float W = (float)S.area * inv_max_area;
+    if (diel) W *= (float)S.maxside * inv_max_side;
+    cw = fabsf(pe * W);
+    err = pe_err * W + 32.0f * kU * cw + 1e-6f * cw;
+    return isfinite(cw) && isfinite(err);
+}
+
+// 1 above e, 0 at or below e (the FP64 test splits on c > e), -1 undecided
+__device__ __forceinline__ int side_test(float c, float err, float e) {
+    if (c - err > e * (1.0f + 4.0f * kU)) return 1;
+    if (c + err < e * (1.0f - 4.0f * kU)) return 0;
+    return -1;
+}
+
+// fcg_link_decision in FP32, or -1 when only the FP64 test can tell
+__device__ int decide32(const Element &A, const Element &B, float e, float inv_max_area, float inv_max_side) {
+    bool leaf1 = (A.type & FCG_IS_LEAF) != 0, leaf2 = (B.type & FCG_IS_LEAF) != 0;
+    if (leaf1 && leaf2) return 0;
+    float dx = A.c[0] - B.c[0], dy = A.c[1] - B.c[1], dz = A.c[2] - B.c[2];  // fcg_fsub's float values
+    float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    double rm = A.maxside > B.maxside ? A.maxside : B.maxside;
+    float rho = r / (float)rm;
+    if (!(r > 1e-10f) || !(fabsf(rho - 2.0f) > 1e-5f)) return -1;
+    bool quad = rho < 2.0f;
+    float c1, e1, c2, e2;
+    if (!weight32(A, B, dx, dy, dz, r, quad, inv_max_area, inv_max_side, c1, e1)) return -1;
+    if (!weight32(B, A, -dx, -dy, -dz, r, quad, inv_max_area, inv_max_side, c2, e2)) return -1;
+    int t1 = side_test(c1, e1, e), t2 = side_test(c2, e2, e);
+    if (t1 != 1 && t2 != 1) {
+        if (t1 == 0 && t2 == 0) return 0;
+        return -1;
+    }
+    if (!leaf1 && leaf2) return 1;
+    if (leaf1 && !leaf2) return 2;
+    return A.area > B.area ? 1 : 2;
+}
+
+// decide every frontier pair in FP32 where that is certain: 0 link, 1 split
+// the first element, 2 the second; undecided pairs go to a list for FP64
+__global__ void __launch_bounds__(kThreads) k_decide32(int64_t n, const int2 *__restrict__ pairs, const uint16_t *__restrict__ root_level,
+                                                       int depth, const Element *__restrict__ el, float e, float inv_max_area,
+                                                       float inv_max_side, uint8_t *flag, int32_t *undecided,
+                                                       unsigned long long *n_undecided, int *max_level) {
+    int lvl = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i - (threadIdx.x) < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int f = 0;
+        bool ok = i < n;
+        if (ok) {
+            int2 pr = pairs[i];
+            f = decide32(el[pr.x], el[pr.y], e, inv_max_area, inv_max_side);
+            flag[i] = (uint8_t)(f < 0 ? 0 : f);
+            lvl = max(lvl, (int)root_level[i] + depth);
+        }
+        // warp-aggregated append of the undecided pairs
+        unsigned m = __ballot_sync(0xffffffffu, ok && f < 0);
+        if (m) {
+            int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(n_undecided, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (ok && f < 0) undecided[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) lvl = max(lvl, __shfl_xor_sync(0xffffffffu, lvl, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(max_level, lvl);
+}
+
+// the FP64 test (the host builder's own code) for the undecided pairs
+__global__ void __launch_bounds__(128) k_decide64(const unsigned long long *__restrict__ n_undecided, const int32_t *__restrict__ undecided,
+                                                  const int2 *__restrict__ pairs, const Element *__restrict__ el, double eps,
+                                                  double max_side, double max_area, uint8_t *flag) {
+    int64_t m = (int64_t)*n_undecided;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        int32_t i = undecided[j];
+        int2 pr = pairs[i];
+        flag[i] = (uint8_t)fcg_link_decision(el[pr.x], el[pr.y], eps, max_side, max_area);
+    }
+}
+
+// per-tile count of split pairs
+__global__ void __launch_bounds__(kThreads) k_split_tiles(int64_t n, const uint8_t *__restrict__ flag, long long *tile_sums) {
     __shared__ long long wt[32];
     int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
     long long splits = 0;
-    int lvl = 0;
-    for (int j = 0; j < kItems; j++) {
-        int64_t i = base + j;
-        if (i >= n) break;
-        int2 pr = pairs[i];
-        int f = fcg_link_decision(el[pr.x], el[pr.y], eps, max_side, max_area);
-        flag[i] = (uint8_t)f;
-        splits += f != 0;
-        lvl = max(lvl, (int)root_level[i] + depth);
-    }
+    for (int j = 0; j < kItems; j++)
+        if (base + j < n) splits += flag[base + j] != 0;
     splits = block_sum(splits, wt);
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = splits;
-    for (int o = 16; o > 0; o >>= 1) lvl = max(lvl, __shfl_xor_sync(0xffffffffu, lvl, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(max_level, lvl);
 }
 
 // children of every split pair into the next level, at 2 * (exclusive rank)
@@ -380,6 +557,11 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
     long long *d_scalars;  // [0] scan total, [1] spare
     int *d_max_level;
     unsigned *d_bad;
+    unsigned long long *d_undecided;
+    const float inv_max_area = (float)(1.0 / max_area), inv_max_side = (float)(1.0 / max_side);
+    const bool trace = getenv("FCG_TRACE") != nullptr;
+    long long n_tests = 0, n_fp64 = 0;
+    LB_CK(B.alloc(&d_undecided, 1));
     LB_CK(B.alloc(&d_el, (size_t)ne));
     LB_CK(B.alloc(&d_node_of, (size_t)ne));
     LB_CK(B.alloc(&d_scalars, 2));
@@ -410,15 +592,26 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
         unsigned tiles = grid_tiles(n);
         uint8_t *flag;
         long long *sums;
+        int32_t *undecided;
         LB_CK(B.alloc(&flag, (size_t)n));
         LB_CK(B.alloc(&sums, tiles));
+        LB_CK(B.alloc(&undecided, (size_t)n));
         LB_CK(B.alloc(&L.rank, (size_t)n));
-        k_decide<<<tiles, kThreads, 0, s>>>(n, L.pairs, L.root_level, depth, d_el, eps, max_side, max_area, flag, sums, d_max_level);
+        LB_CK(cudaMemsetAsync(d_undecided, 0, sizeof(unsigned long long), s));
+        k_decide32<<<grid_stride(n, sms), 256, 0, s>>>(n, L.pairs, L.root_level, depth, d_el, (float)eps, inv_max_area,
+                                                        inv_max_side, flag, undecided, d_undecided, d_max_level);
+        k_decide64<<<grid_stride(n, sms), 128, 0, s>>>(d_undecided, undecided, L.pairs, d_el, eps, max_side, max_area, flag);
+        k_split_tiles<<<tiles, kThreads, 0, s>>>(n, flag, sums);
         k_scan_sums<<<1, 1024, 0, s>>>(tiles, sums, d_scalars);
         LB_CK(cudaGetLastError());
-        long long splits = 0;
-        LB_CK(cudaMemcpyAsync(&splits, d_scalars, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        long long level_counts[2] = {0, 0};  // splits, FP64 tests
+        LB_CK(cudaMemcpyAsync(&level_counts[0], d_scalars, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        LB_CK(cudaMemcpyAsync(&level_counts[1], d_undecided, sizeof(long long), cudaMemcpyDeviceToHost, s));
         LB_CK(cudaStreamSynchronize(s));
+        B.release(undecided);
+        long long splits = level_counts[0];
+        n_tests += n;
+        n_fp64 += level_counts[1];
         if (splits > (1ll << 29)) {
             err = "model too large for 32-bit link indices";
             return FCG_OUT_OF_MEMORY;
@@ -445,6 +638,9 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
         err = "device link construction: a split element without two children (" + std::to_string(bad) + " pairs)";
         return FCG_GENERIC_ERROR;
     }
+    if (trace)
+        fprintf(stderr, "[fcg links] %zu levels, %lld pair tests, %lld (%.2f %%) by the FP64 test\n", lv.size(), n_tests, n_fp64,
+                n_tests ? 100.0 * (double)n_fp64 / (double)n_tests : 0.0);
 
     // links under every item, deepest level first
     for (size_t d = lv.size(); d-- > 0;) {
