@@ -27,9 +27,10 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 REFERENCE = os.environ.get("FCG_REFERENCE_DIR", "/root/reference")
-# per-file device flags: the link construction rounds every operation like the
-# host builder (no fused multiply-add), so both take the same decisions
-CU_FLAGS = {"link_build.cu": ["-fmad=false"]}
+# per-file device flags: the link construction and the mesh refinement round
+# every operation like the host builder (no fused multiply-add), so both take
+# the same decisions
+CU_FLAGS = {"link_build.cu": ["-fmad=false"], "mesh_build.cu": ["-fmad=false"]}
 
 LIB = os.path.join(HERE, "libfastercap_gb300.so")
 CLI = os.path.join(HERE, "fastercap_gb300")

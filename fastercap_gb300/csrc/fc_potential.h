@@ -634,4 +634,125 @@ FCG_HD int fcg_link_decision(const E &A, const E &B, double eps, double max_side
     return A.area > B.area ? 1 : 2;
 }
 
+// ---------------------------------------------------------------- mesh
+// Newell normal of a triangle accumulated in float, normalised (in double,
+// rounded to float) when its modulus exceeds the panel epsilon; returns the
+// modulus (the normal of CAutoPanel::CalcPanelGeomPar, Solver/AutoPanel.cpp:51-104).
+FCG_HD double fcg_newell_normal(const float *v, float *n) {
+    n[0] = n[1] = n[2] = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        int j = i + 1 > 2 ? 0 : i + 1;
+        const float *a = v + 3 * i, *b = v + 3 * j;
+        n[0] += (a[1] - b[1]) * (a[2] + b[2]);
+        n[1] += (a[2] - b[2]) * (a[0] + b[0]);
+        n[2] += (a[0] - b[0]) * (a[1] + b[1]);
+    }
+    double m = fcg_mod(fcg_widen(n));
+    if (m > FCG_PANEL_EPS) {
+        n[0] = (float)(n[0] / m);
+        n[1] = (float)(n[1] / m);
+        n[2] = (float)(n[2] / m);
+    }
+    return m;
+}
+
+// geometric normal: a panel's own, a super node's from its synthetic triangle
+template <class E>
+FCG_HD fcg_d3 fcg_geo_normal(const E &e) {
+    if (e.type & FCG_IS_SUPER_NODE) {
+        float n[3];
+        fcg_newell_normal(e.v, n);
+        return fcg_widen(n);
+    }
+    return fcg_widen(e.n);
+}
+
+template <class E>
+FCG_HD void fcg_centroid3(E &e) {
+    float sx = e.v[0] + e.v[3], sy = e.v[1] + e.v[4], sz = e.v[2] + e.v[5];
+    sx = sx + e.v[6];
+    sy = sy + e.v[7];
+    sz = sz + e.v[8];
+    e.c[0] = (float)(sx / 3.0);
+    e.c[1] = (float)(sy / 3.0);
+    e.c[2] = (float)(sz / 3.0);
+}
+
+template <class E>
+FCG_HD int fcg_max_side3(E &e, double l0, double l1, double l2) {
+    if (l0 >= l1 && l0 >= l2) { e.maxside_idx = 0; e.maxside = l0; }
+    else if (l1 >= l0 && l1 >= l2) { e.maxside_idx = 1; e.maxside = l1; }
+    else { e.maxside_idx = 2; e.maxside = l2; }
+    return e.maxside_idx;
+}
+
+// CAutoPanel::Subdivide (Solver/AutoPanel.cpp:382-523): bisect a leaf
+// triangle across its longest side (midpoint = float sum halved in double,
+// rounded to float); the children keep the parent's type, dielectric index
+// and normal, halve its area and get their own centroid and longest side.
+template <class E>
+FCG_HD void fcg_subdivide(const E &P, E &Lc, E &Rc) {
+    int ms = P.maxside_idx;
+    const float *v0 = P.v, *v1 = P.v + 3, *v2 = P.v + 6;
+    const float *a, *b, *o;  // side endpoints a-b, opposite vertex o
+    if (ms == 0) { a = v1; b = v0; o = v2; }
+    else if (ms == 1) { a = v2; b = v1; o = v0; }
+    else { a = v0; b = v2; o = v1; }
+    float sx = a[0] + b[0], sy = a[1] + b[1], sz = a[2] + b[2];
+    fcg_d3 mid = fcg_mk(sx / 2.0, sy / 2.0, sz / 2.0);
+    double newside = fcg_mod(fcg_mk((double)o[0] - mid.x, (double)o[1] - mid.y, (double)o[2] - mid.z));
+    double half = P.maxside / 2.0;
+    float m[3] = {(float)mid.x, (float)mid.y, (float)mid.z};
+    const float *l0, *l1, *l2, *r0, *r1, *r2;
+    double lsl[3], rsl[3];
+    if (ms == 0) {
+        l0 = v0; l1 = m; l2 = v2;
+        lsl[0] = half; lsl[1] = newside; lsl[2] = fcg_mod(fcg_fsub(v0, v2));
+        r0 = m; r1 = v1; r2 = v2;
+        rsl[0] = half; rsl[1] = fcg_mod(fcg_fsub(v2, v1)); rsl[2] = newside;
+    } else if (ms == 1) {
+        l0 = v1; l1 = m; l2 = v0;
+        lsl[0] = half; lsl[1] = newside; lsl[2] = fcg_mod(fcg_fsub(v1, v0));
+        r0 = m; r1 = v2; r2 = v0;
+        rsl[0] = half; rsl[1] = fcg_mod(fcg_fsub(v0, v2)); rsl[2] = newside;
+    } else {
+        l0 = v2; l1 = m; l2 = v1;
+        lsl[0] = half; lsl[1] = newside; lsl[2] = fcg_mod(fcg_fsub(v2, v1));
+        r0 = m; r1 = v0; r2 = v1;
+        rsl[0] = half; rsl[1] = fcg_mod(fcg_fsub(v1, v0)); rsl[2] = newside;
+    }
+    for (int k = 0; k < 3; k++) {
+        Lc.v[k] = l0[k]; Lc.v[3 + k] = l1[k]; Lc.v[6 + k] = l2[k];
+        Rc.v[k] = r0[k]; Rc.v[3 + k] = r1[k]; Rc.v[6 + k] = r2[k];
+        Lc.n[k] = P.n[k];
+        Rc.n[k] = P.n[k];
+    }
+    Lc.type = Rc.type = P.type;
+    Lc.diel = Rc.diel = P.diel;
+    Lc.area = Rc.area = P.area / 2.0;
+    Lc.left = Lc.right = Rc.left = Rc.right = -1;
+    fcg_centroid3(Lc);
+    fcg_centroid3(Rc);
+    fcg_max_side3(Lc, lsl[0], lsl[1], lsl[2]);
+    fcg_max_side3(Rc, rsl[0], rsl[1], rsl[2]);
+}
+
+// One step of CAutoRefine::DiscretizeMutual (Solver/Autorefine.cpp:2638-2730):
+// 0 = the pair is fine enough (c1, c2 hold its weights); 1 / 2 = refine by
+// splitting the larger-area element (B on ties). For sibling pairs
+// of the self pass (`selfc`) the tolerance is relaxed by the curvature
+// coefficient (mesh_curv - 1) (n1.n2 + 1) + 1 of the two geometric normals.
+template <class E>
+FCG_HD int fcg_mesh_decision(const E &A, const E &B, bool selfc, double e, double mesh_curv, double max_side, double max_area,
+                             double *c1, double *c2) {
+    fcg_d3 dist;
+    double rdist, rmax;
+    fcg_pair_span(A, B, &dist, &rdist, &rmax);
+    double ccoeff;
+    if (selfc) ccoeff = (mesh_curv - 1.0) * (fcg_dot(fcg_geo_normal(A), fcg_geo_normal(B)) + 1.0) + 1.0;
+    else ccoeff = 1.0;
+    if (!fcg_refine_criteria(A, B, dist, rdist, rmax, e, ccoeff, max_side, max_area, c1, c2)) return 0;
+    return A.area > B.area ? 1 : 2;
+}
+
 #endif

@@ -78,6 +78,18 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
                       double max_side, double max_area, std::vector<int64_t> &link_ptr, std::vector<int32_t> &link_src,
                       int &max_level, std::string &err);
 
+// Mesh refinement on the device (csrc/mesh_build.cu): the closure of the
+// refinement of the root pairs (root_a[i], root_b[i]) with root_meta[i] =
+// recursion level | kMeshSelfPair for pairs of the self pass. `el` (with
+// `depth`, every element's depth in its conductor's tree) is replaced by the
+// refined hierarchy; max_mesh_eps and max_level receive the largest weight of
+// an unrefined pair and the deepest pair level.
+constexpr uint16_t kMeshSelfPair = 0x8000;
+int mesh_refine_device(DeviceContext &ctx, std::vector<Element> &el, const std::vector<int32_t> &depth,
+                       const std::vector<int32_t> &root_a, const std::vector<int32_t> &root_b,
+                       const std::vector<uint16_t> &root_meta, double mesh_eps, double mesh_curv, double max_side,
+                       double max_area, double &max_mesh_eps, int &max_level, std::string &err);
+
 // CUDA streams for host code compiled without the CUDA headers
 void *stream_create(int device);
 void stream_destroy(int device, void *stream);

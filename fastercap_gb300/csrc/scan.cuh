@@ -1,0 +1,161 @@
+// Building blocks shared by the device model-construction passes (link
+// construction, mesh refinement): CTA scans, a three-phase exclusive scan
+// over device arrays and a stream-ordered scratch allocator that frees
+// everything it still holds when it goes out of scope.
+#ifndef FCG_SCAN_CUH
+#define FCG_SCAN_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+namespace fcg {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kThreads * kItems;  // items per CTA in the tiled kernels
+constexpr int kWarps = kThreads / 32;
+
+// exclusive scan of one value per thread over the CTA; *total gets the sum
+template <class T>
+__device__ T block_exclusive_scan(T v, T *warp_tot, T *total) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        T y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        T t = lane < kWarps ? warp_tot[lane] : T(0);
+        for (int o = 1; o < 32; o <<= 1) {
+            T y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < kWarps) warp_tot[lane] = t;
+    }
+    __syncthreads();
+    T before = w > 0 ? warp_tot[w - 1] : T(0);
+    *total = warp_tot[kWarps - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+template <class T>
+__device__ T block_sum(T v, T *warp_tot) {
+    T total;
+    block_exclusive_scan(v, warp_tot, &total);
+    return total;
+}
+
+// ------------------------------------------------------------------ scans
+// Three-phase exclusive scan: per-tile sums, one CTA scanning the tile sums,
+// then every tile scanned again with its offset. In place is allowed.
+template <class TI>
+__global__ void __launch_bounds__(kThreads) k_scan_tiles(int64_t n, const TI *__restrict__ in, long long *sums) {
+    __shared__ long long wt[32];
+    int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
+    long long s = 0;
+    for (int j = 0; j < kItems; j++)
+        if (base + j < n) s += (long long)in[base + j];
+    s = block_sum(s, wt);
+    if (threadIdx.x == 0) sums[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(int64_t m, long long *sums, long long *total) {
+    __shared__ long long wt[32];
+    long long carry = 0;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t b = 0; b < m; b += blockDim.x) {
+        int64_t i = b + threadIdx.x;
+        long long v = i < m ? sums[i] : 0;
+        long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wt[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            long long t = lane < nw ? wt[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            if (lane < nw) wt[lane] = t;
+        }
+        __syncthreads();
+        long long before = w > 0 ? wt[w - 1] : 0;
+        if (i < m) sums[i] = carry + before + x - v;
+        carry += wt[nw - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+template <class TI, class TO>
+__global__ void __launch_bounds__(kThreads) k_scan_apply(int64_t n, const TI *in, TO *out, const long long *__restrict__ sums) {
+    __shared__ long long wt[32];
+    int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
+    long long v[kItems], s = 0;
+    for (int j = 0; j < kItems; j++) {
+        v[j] = base + j < n ? (long long)in[base + j] : 0;
+        s += v[j];
+    }
+    long long tot;
+    long long run = block_exclusive_scan(s, wt, &tot) + sums[blockIdx.x];
+    for (int j = 0; j < kItems; j++) {
+        if (base + j < n) out[base + j] = (TO)run;
+        run += v[j];
+    }
+}
+
+inline unsigned grid_tiles(int64_t n) { return (unsigned)std::max<int64_t>((n + kTile - 1) / kTile, 1); }
+inline unsigned grid_stride(int64_t n, int sms, int threads = 256) {
+    return (unsigned)std::max<int64_t>(std::min<int64_t>((n + threads - 1) / threads, (int64_t)sms * 16), 1);
+}
+
+// exclusive scan of in[0..n) into out (in place allowed); the total goes to
+// the device word *total. `sums` holds grid_tiles(n) words.
+template <class TI, class TO>
+inline void exclusive_scan(cudaStream_t s, int64_t n, const TI *in, TO *out, long long *sums, long long *total) {
+    unsigned tiles = grid_tiles(n);
+    k_scan_tiles<<<tiles, kThreads, 0, s>>>(n, in, sums);
+    k_scan_sums<<<1, 1024, 0, s>>>(tiles, sums, total);
+    k_scan_apply<<<tiles, kThreads, 0, s>>>(n, in, out, sums);
+}
+
+struct Bufs {
+    cudaStream_t s = nullptr;
+    std::vector<void *> live;
+    ~Bufs() {
+        if (!s) return;
+        for (void *p : live) cudaFreeAsync(p, s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    template <class T>
+    cudaError_t alloc(T **p, size_t n) {
+        *p = nullptr;
+        cudaError_t e = cudaMallocAsync((void **)p, std::max<size_t>(n, 1) * sizeof(T), s);
+        if (e == cudaSuccess) live.push_back(*p);
+        return e;
+    }
+    template <class T>
+    void release(T *&p) {
+        if (!p) return;
+        auto it = std::find(live.begin(), live.end(), (void *)p);
+        if (it != live.end()) live.erase(it);
+        cudaFreeAsync(p, s);
+        p = nullptr;
+    }
+};
+
+}  // namespace
+}  // namespace fcg
+
+#endif

@@ -179,35 +179,11 @@ struct Builder {
     }
 
     // -------------------------------------------------------------- panels
-    static uint8_t max_side3(Element &e, double l0, double l1, double l2) {
-        if (l0 >= l1 && l0 >= l2) { e.maxside_idx = 0; e.maxside = l0; }
-        else if (l1 >= l0 && l1 >= l2) { e.maxside_idx = 1; e.maxside = l1; }
-        else { e.maxside_idx = 2; e.maxside = l2; }
-        return e.maxside_idx;
-    }
+    static uint8_t max_side3(Element &e, double l0, double l1, double l2) { return (uint8_t)fcg_max_side3(e, l0, l1, l2); }
 
-    // Newell normal of the triangle accumulated in float; returns its modulus
-    static double newell_normal(const float *v, float *n) {
-        n[0] = n[1] = n[2] = 0.0f;
-        for (int i = 0; i < 3; i++) {
-            int j = i + 1 > 2 ? 0 : i + 1;
-            const float *a = v + 3 * i, *b = v + 3 * j;
-            n[0] += (a[1] - b[1]) * (a[2] + b[2]);
-            n[1] += (a[2] - b[2]) * (a[0] + b[0]);
-            n[2] += (a[0] - b[0]) * (a[1] + b[1]);
-        }
-        double m = mod(widen(n));
-        if (m > FCG_PANEL_EPS) {
-            n[0] = (float)(n[0] / m); n[1] = (float)(n[1] / m); n[2] = (float)(n[2] / m);
-        }
-        return m;
-    }
+    static double newell_normal(const float *v, float *n) { return fcg_newell_normal(v, n); }
 
-    static void centroid3(Element &e) {
-        float sx = e.v[0] + e.v[3], sy = e.v[1] + e.v[4], sz = e.v[2] + e.v[5];
-        sx = sx + e.v[6]; sy = sy + e.v[7]; sz = sz + e.v[8];
-        e.c[0] = (float)(sx / 3.0); e.c[1] = (float)(sy / 3.0); e.c[2] = (float)(sz / 3.0);
-    }
+    static void centroid3(Element &e) { fcg_centroid3(e); }
 
     // returns the cosine of the smallest angle
     static double geom_par(Element &e) {
@@ -504,16 +480,9 @@ struct Builder {
     }
 
     // ------------------------------------------------------ super hierarchy
-    double geo_normal_calc(const Element &e, D3 &out) {
-        float n[3];
-        double m = newell_normal(e.v, n);
-        out = widen(n);
-        return m;
-    }
     D3 geo_normal(int id) {
-        const Element &e = el[id];
-        if (e.type & FCG_IS_SUPER_NODE) { D3 n; geo_normal_calc(e, n); return n; }
-        return widen(e.n);
+        fcg_d3 n = fcg_geo_normal(el[id]);
+        return d3(n.x, n.y, n.z);
     }
 
     int make_super(int lid, int rid) {
@@ -639,50 +608,8 @@ struct Builder {
     // ------------------------------------------------------------ refinement
     int subdivide(int id) {
         if (!(el[id].type & FCG_IS_LEAF)) return FC_NORMAL_END;
-        Element P = el[id];
         Element Lc, Rc;
-        int ms = P.maxside_idx;
-        const float *v0 = P.v, *v1 = P.v + 3, *v2 = P.v + 6;
-        // midpoint of the longest side (float sum, exact halving)
-        const float *a, *b, *o;  // side endpoints a-b, opposite vertex o
-        if (ms == 0) { a = v1; b = v0; o = v2; }
-        else if (ms == 1) { a = v2; b = v1; o = v0; }
-        else { a = v0; b = v2; o = v1; }
-        float sx = a[0] + b[0], sy = a[1] + b[1], sz = a[2] + b[2];
-        D3 mid = d3(sx / 2.0, sy / 2.0, sz / 2.0);
-        double newside = mod(d3((double)o[0] - mid.x, (double)o[1] - mid.y, (double)o[2] - mid.z));
-        double half = P.maxside / 2.0;
-        float m[3];
-        store(m, mid);
-        double lsl[3], rsl[3];
-        auto setv = [](Element &e, const float *p0, const float *p1, const float *p2) {
-            memcpy(e.v, p0, 12); memcpy(e.v + 3, p1, 12); memcpy(e.v + 6, p2, 12);
-        };
-        if (ms == 0) {
-            setv(Lc, v0, m, v2);
-            lsl[0] = half; lsl[1] = newside; lsl[2] = mod(fsub(v0, v2));
-            setv(Rc, m, v1, v2);
-            rsl[0] = half; rsl[1] = mod(fsub(v2, v1)); rsl[2] = newside;
-        } else if (ms == 1) {
-            setv(Lc, v1, m, v0);
-            lsl[0] = half; lsl[1] = newside; lsl[2] = mod(fsub(v1, v0));
-            setv(Rc, m, v2, v0);
-            rsl[0] = half; rsl[1] = mod(fsub(v0, v2)); rsl[2] = newside;
-        } else {
-            setv(Lc, v2, m, v1);
-            lsl[0] = half; lsl[1] = newside; lsl[2] = mod(fsub(v2, v1));
-            setv(Rc, m, v0, v1);
-            rsl[0] = half; rsl[1] = mod(fsub(v1, v0)); rsl[2] = newside;
-        }
-        Lc.type = Rc.type = P.type;
-        Lc.diel = Rc.diel = P.diel;
-        Lc.area = Rc.area = P.area / 2.0;
-        memcpy(Lc.n, P.n, 12);
-        memcpy(Rc.n, P.n, 12);
-        centroid3(Lc);
-        centroid3(Rc);
-        max_side3(Lc, lsl[0], lsl[1], lsl[2]);
-        max_side3(Rc, rsl[0], rsl[1], rsl[2]);
+        fcg_subdivide(el[id], Lc, Rc);
         el.push_back(Lc);
         el.push_back(Rc);
         int l = (int)el.size() - 2, r = (int)el.size() - 1;
@@ -700,25 +627,15 @@ struct Builder {
         level++;
         if (level > max_level) max_level = level;
         if (level > kMaxDepth) { err = "mesh refinement recursion too deep (touching or overlapping panels?)"; return FC_GENERIC_ERROR; }
-        D3 dist = fsub(el[p1].c, el[p2].c);
-        double rdist = mod(dist);
-        double r1 = el[p1].maxside, r2 = el[p2].maxside;
-        double rmax = r1 > r2 ? r1 : r2;
-        double ccoeff;
-        if (selfc) ccoeff = (mesh_curv - 1.0) * (dot(geo_normal(p1), geo_normal(p2)) + 1.0) + 1.0;
-        else ccoeff = 1.0f;
         double c1, c2;
         int ret = FC_NORMAL_END;
-        if (refine_criteria(&c1, &c2, p1, p2, dist, rdist, rmax, mesh_eps, ccoeff)) {
-            if (el[p1].area > el[p2].area) {
-                subdivide(p1);
-                if ((ret = discretize_mutual(el[p1].left, p2, selfc)) == FC_NORMAL_END)
-                    ret = discretize_mutual(el[p1].right, p2, selfc);
-            } else {
-                subdivide(p2);
-                if ((ret = discretize_mutual(p1, el[p2].left, selfc)) == FC_NORMAL_END)
-                    ret = discretize_mutual(p1, el[p2].right, selfc);
-            }
+        int which = fcg_mesh_decision(el[p1], el[p2], selfc, mesh_eps, mesh_curv, max_side, max_area, &c1, &c2);
+        if (which == 1) {
+            subdivide(p1);
+            if ((ret = discretize_mutual(el[p1].left, p2, selfc)) == FC_NORMAL_END) ret = discretize_mutual(el[p1].right, p2, selfc);
+        } else if (which == 2) {
+            subdivide(p2);
+            if ((ret = discretize_mutual(p1, el[p2].left, selfc)) == FC_NORMAL_END) ret = discretize_mutual(p1, el[p2].right, selfc);
         } else {
             if (!(el[p1].type & FCG_IS_SUPER_NODE) && c1 > max_mesh_eps) max_mesh_eps = c1;
             if (!(el[p2].type & FCG_IS_SUPER_NODE) && c2 > max_mesh_eps) max_mesh_eps = c2;
@@ -764,6 +681,50 @@ struct Builder {
             refine_self(el[id].right);
         }
         level--;
+    }
+
+    // ---------------------------------------------------------------- device mesh
+    // The refinement closure runs on the device (mesh_refine_device) from the
+    // host order's root pairs: every conductor pair at level 1, then the
+    // children pair of every internal element at its depth + 2, flagged as
+    // self pairs. A conductor that is a single panel is bisected first, as the
+    // host self pass does at its top level.
+    int device_mesh(DeviceContext &dev) {
+        for (size_t i = 0; i < order.size(); i++) {
+            int32_t t = conds[order[i]].top;
+            if (el[t].type & FCG_IS_LEAF) subdivide(t);
+        }
+        std::vector<int32_t> depth(el.size(), 0), ra, rb;
+        std::vector<uint16_t> rm;
+        for (size_t i = 0; i < order.size(); i++)
+            for (size_t j = i + 1; j < order.size(); j++) {
+                ra.push_back(conds[order[i]].top);
+                rb.push_back(conds[order[j]].top);
+                rm.push_back(1);
+            }
+        std::vector<std::pair<int32_t, int>> st;
+        for (size_t i = 0; i < order.size(); i++) {
+            st.push_back(std::make_pair(conds[order[i]].top, 0));
+            while (!st.empty()) {
+                int32_t id = st.back().first;
+                int s = st.back().second;
+                st.pop_back();
+                depth[id] = s;
+                if (el[id].type & FCG_IS_LEAF) continue;
+                ra.push_back(el[id].left);
+                rb.push_back(el[id].right);
+                rm.push_back((uint16_t)(kMeshSelfPair | std::min(s + 2, 0x7fff)));
+                st.push_back(std::make_pair(el[id].right, s + 1));
+                st.push_back(std::make_pair(el[id].left, s + 1));
+            }
+        }
+        double meps = 0.0;
+        int lvl = 0;
+        int r = mesh_refine_device(dev, el, depth, ra, rb, rm, mesh_eps, mesh_curv, max_side, max_area, meps, lvl, err);
+        if (r != FC_NORMAL_END) return r;
+        if (meps > max_mesh_eps) max_mesh_eps = meps;
+        if (lvl > max_level) max_level = lvl;
+        return FC_NORMAL_END;
     }
 
     // ---------------------------------------------------------------- device links
@@ -948,16 +909,20 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
     B.max_level = 0;
     B.max_mesh_eps = 0.0;
     size_t nc = B.order.size();
-    for (size_t i = 0; i < nc; i++)
-        for (size_t j = i + 1; j < nc; j++) {
-            ret = B.discretize_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top, false);
+    if (dev) {
+        if ((ret = B.device_mesh(*dev)) != FC_NORMAL_END) { err = B.err; return ret; }
+    } else {
+        for (size_t i = 0; i < nc; i++)
+            for (size_t j = i + 1; j < nc; j++) {
+                ret = B.discretize_mutual(B.conds[B.order[i]].top, B.conds[B.order[j]].top, false);
+                if (ret != FC_NORMAL_END) { err = B.err; return ret; }
+            }
+        int64_t panels = 0, nodes = 0;
+        for (size_t i = 0; i < nc; i++) {
+            B.level = 0;
+            ret = B.discretize_self(B.conds[B.order[i]].top, panels, nodes);
             if (ret != FC_NORMAL_END) { err = B.err; return ret; }
         }
-    int64_t panels = 0, nodes = 0;
-    for (size_t i = 0; i < nc; i++) {
-        B.level = 0;
-        ret = B.discretize_self(B.conds[B.order[i]].top, panels, nodes);
-        if (ret != FC_NORMAL_END) { err = B.err; return ret; }
     }
     mark("mesh refinement");
     // links: mutual interactions of all conductor pairs, then self, conductor

@@ -95,3 +95,33 @@ def test_solve_on_device_built_model(ctx, tmp_path):
         pr.fill()
         caps.append(pr.solve(tol=1e-6)[0])
     np.testing.assert_array_equal(caps[0], caps[1])
+
+
+def test_touching_conductors(ctx, tmp_path):
+    """Two conductors sharing an edge: the refinement recurses towards the
+    contact; the device closure reaches the host's mesh (or its error)."""
+    p = tmp_path / "touch.txt"
+    p.write_text("0 touching\nT a 0 0 0  1 0 0  0 1 0\nT b 1 0 0  0 1 0  1 1 0.5\n")
+    results = []
+    for c in (ctx, None):
+        try:
+            m = fc.Model.build(str(p), mesh_eps=0.05, ctx=c)
+            results.append(("ok", m))
+        except fc.FCError as e:
+            results.append(("err", e.code))
+    assert results[0][0] == results[1][0]
+    if results[0][0] == "ok":
+        assert_same_model(results[0][1], results[1][1])
+    else:
+        assert results[0][1] == results[1][1]
+
+
+@pytest.mark.parametrize("meps", [0.2, 0.05, 0.01])
+def test_mesh_refinement_levels(ctx, tmp_path, meps):
+    """Refinement from coarse to fine on a crossing: the mesh (panel count,
+    node tree, max achieved refinement value) matches at every setting."""
+    p = str(tmp_path / "x.txt")
+    geo.random_crossing(11, kmin=3, kmax=3).write(p)
+    dev, host = build_pair(ctx, p, mesh_eps=meps)
+    assert dev.info["max_mesh_eps"] == host.info["max_mesh_eps"]
+    assert_same_model(dev, host)
