@@ -413,7 +413,8 @@ def run_gb300_multi(args, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "p50_ms": float(np.percentile(e2e_times, 50))},
         "gpu_launches": int(st_timed["kernel_launches"]),
-        "phases": {"fill_ms_last": st_timed["fill_ms"], "solve_ms_last": st_timed["solve_ms"]},
+        "phases": {"fill_ms_last": st_timed["fill_ms"], "solve_ms_last": st_timed["solve_ms"],
+                   "fill_fp64_coefficients": st_timed["fill_fp64"]},
         "roofline": {"kernel": "link product (k_spmv32_multi)", "bound": "hbm",
                      "timing": "CUDA events around every link-product launch, steps re-run after the timed region",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -680,7 +681,8 @@ def run_gb300(args, rank, world, local_rank):
         times, cap_m, it_m = time_steps(prob, stream, args.steps, tol, flush, torch)
     barrier()
     st_timed = prob.stats()
-    phase = {"fill_ms_last": st_timed["fill_ms"], "solve_ms_last": st_timed["solve_ms"]}
+    phase = {"fill_ms_last": st_timed["fill_ms"], "solve_ms_last": st_timed["solve_ms"],
+             "fill_fp64_coefficients": st_timed["fill_fp64"]}
     # link-product roofline: the same steps again with CUDA events around
     # every link-product launch (the timed steps run each Arnoldi loop as one
     # CUDA graph, which cannot bracket single kernels)

@@ -80,7 +80,7 @@ class ModelInfo(C.Structure):
 class ProblemStats(C.Structure):
     _fields_ = [("kernel_launches", C.c_int64), ("link_launches", C.c_int64), ("link_ms", C.c_double),
                 ("link_bytes", C.c_int64), ("fill_ms", C.c_double), ("solve_ms", C.c_double),
-                ("refine_checks", C.c_int64), ("refine_cycles", C.c_int64)]
+                ("refine_checks", C.c_int64), ("refine_cycles", C.c_int64), ("fill_fp64", C.c_int64)]
 
 
 class SolveOptions(C.Structure):

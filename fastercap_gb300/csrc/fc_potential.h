@@ -437,6 +437,146 @@ FCG_HD double fcg_potential_opt_fast(fcg_d3 r, const float *v, const fcg_tri64 &
     return (result * 2.0) / t.nmod;
 }
 
+// ---- single-precision analytic potential (mixed-precision near field)
+// The potential_opt formula in FP32, in a frame centred on the source
+// triangle's centroid and scaled by its largest vertex distance `s` (every
+// quantity O(1)); the potential of the scaled problem is s times the
+// original. Two rewrites keep FP32 accurate: R + l for l < 0 is formed as
+// (P0^2 + d^2) / (R - l) (no cancellation), and the reference's guards
+// (P0, R + lplus, R + lminus against 1e-6 lmax) are tested with an error
+// bound. When an R + l guard is too close to call in FP32 the evaluation
+// reports it and the caller computes that coefficient with the FP64
+// formula; an undecidable P0 guard is accepted when the edge's term (which
+// is proportional to P0) is below 2e-6 of the scaled potential, since
+// keeping or dropping it then changes the result by less than FP32 noise.
+struct fcg_tri32 {
+    float n[3];      // unit normal
+    float inv_s;     // 1 / s
+    float w[9];      // vertices - centroid, scaled
+    float rp[9];     // the same projected on the plane through the centroid
+    float l[9];      // unit edge vectors
+    float u[9];      // in-plane edge normals l x n
+    float inv_area;  // 1 / area of the scaled triangle
+    float pad[3];
+};
+
+FCG_HD void fcg_tri32_make(const float *v, const float *c, fcg_tri32 &t) {
+    fcg_tri64 T;
+    fcg_tri64_make(v, T);
+    fcg_d3 cc = fcg_widen(c), n = fcg_mk(T.n[0], T.n[1], T.n[2]);
+    fcg_d3 w[3];
+    double smax = 0.0;
+    for (int i = 0; i < 3; i++) {
+        fcg_d3 vi = fcg_widen(v + 3 * i);
+        w[i] = fcg_mk(vi.x - cc.x, vi.y - cc.y, vi.z - cc.z);
+        double m = fcg_mod(w[i]);
+        smax = m > smax ? m : smax;
+    }
+    double is = smax > 0.0 ? 1.0 / smax : 1.0;
+    for (int k = 0; k < 3; k++) t.n[k] = (float)T.n[k];
+    t.inv_s = (float)is;
+    for (int i = 0; i < 3; i++) {
+        fcg_d3 a = fcg_mk(w[i].x * is, w[i].y * is, w[i].z * is);
+        double an = fcg_dot(n, a);
+        t.w[3 * i] = (float)a.x; t.w[3 * i + 1] = (float)a.y; t.w[3 * i + 2] = (float)a.z;
+        t.rp[3 * i] = (float)(a.x - n.x * an);
+        t.rp[3 * i + 1] = (float)(a.y - n.y * an);
+        t.rp[3 * i + 2] = (float)(a.z - n.z * an);
+        for (int k = 0; k < 3; k++) {
+            t.l[3 * i + k] = (float)T.l[3 * i + k];
+            t.u[3 * i + k] = (float)T.u[3 * i + k];
+        }
+    }
+    t.inv_area = (float)(2.0 / (T.nmod * is * is));
+    t.pad[0] = t.pad[1] = t.pad[2] = 0.0f;
+}
+
+// potential_opt at r = centroid + (px, py, pz) (unscaled float offsets);
+// false when the FP32 evaluation cannot decide a guard the way FP64 would
+FCG_HD bool fcg_potential32(float px, float py, float pz, const fcg_tri32 &t, float *out) {
+    const float U = 5.9604645e-8f;
+    px *= t.inv_s;
+    py *= t.inv_s;
+    pz *= t.inv_s;
+    float nr = t.n[0] * px + t.n[1] * py + t.n[2] * pz;
+    float rx = px - t.n[0] * nr, ry = py - t.n[1] * nr, rz = pz - t.n[2] * nr;
+    float pm = sqrtf(px * px + py * py + pz * pz);
+    float eP = 32.0f * U * (pm + 1.0f);  // absolute error of P0, d, lplus, lminus
+    float Pm[9], R[3];
+    for (int i = 0; i < 3; i++) {
+        Pm[3 * i] = t.rp[3 * i] - rx;
+        Pm[3 * i + 1] = t.rp[3 * i + 1] - ry;
+        Pm[3 * i + 2] = t.rp[3 * i + 2] - rz;
+        float ax = t.w[3 * i] - px, ay = t.w[3 * i + 1] - py, az = t.w[3 * i + 2] - pz;
+        R[i] = sqrtf(ax * ax + ay * ay + az * az);
+    }
+    float d = -(t.n[0] * (t.w[0] - px) + t.n[1] * (t.w[1] - py) + t.n[2] * (t.w[2] - pz));
+    float dn = fabsf(d);
+    float res = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        int j = (i == 2) ? 0 : i + 1;
+        const float *l = t.l + 3 * i, *u = t.u + 3 * i, *Pj = Pm + 3 * j, *Pi = Pm + 3 * i;
+        float P0s = Pj[0] * u[0] + Pj[1] * u[1] + Pj[2] * u[2];
+        float P0 = fabsf(P0s);
+        float lp = Pj[0] * l[0] + Pj[1] * l[1] + Pj[2] * l[2];
+        float lm = Pi[0] * l[0] + Pi[1] * l[1] + Pi[2] * l[2];
+        float lmax = (lp > lm) ? fabsf(lp) : fabsf(lm);
+        float tol = (float)FCG_POTENTIAL_GEO_EPS * lmax;
+        float etol = (float)FCG_POTENTIAL_GEO_EPS * eP + 4.0f * U * tol;
+        float R0sq = P0 * P0 + d * d;
+        float eR0 = 2.0f * (P0 + dn) * eP + 2.0f * eP * eP + 4.0f * U * R0sq;
+        float ap, eap, am, eam;
+        if (lp >= 0.0f) { ap = R[j] + lp; eap = 16.0f * U * ap + 2.0f * eP; }
+        else { float q = R[j] - lp; ap = R0sq / q; eap = (eR0 + 2.0f * eP * ap) / q + 8.0f * U * ap; }
+        if (lm >= 0.0f) { am = R[i] + lm; eam = 16.0f * U * am + 2.0f * eP; }
+        else { float q = R[i] - lm; am = R0sq / q; eam = (eR0 + 2.0f * eP * am) / q + 8.0f * U * am; }
+        // the R + l guards keep or drop a term whose logarithm diverges: FP32
+        // must decide them with certainty
+        if (!(fabsf(ap - tol) > 2.0f * (eap + etol)) || !(fabsf(am - tol) > 2.0f * (eam + etol))) return false;
+        // the P0 guard keeps or drops a term proportional to P0 (a field point
+        // on the edge's line, common between perpendicular faces): when FP32
+        // cannot decide it, either choice is fine while the term is negligible
+        bool p0_close = !(fabsf(P0 - tol) > 2.0f * (eP + etol));
+        bool keep = P0 > tol && ap > tol && am > tol;
+        if (keep || (p0_close && ap > tol && am > tol)) {
+            float dt = 0.0f;
+            if (dn > 0.0f) {
+                float N1 = P0 * lp, D1 = R0sq + dn * R[j];
+                float N2 = P0 * lm, D2 = R0sq + dn * R[i];
+                dt = atan2f(N1 * D2 - N2 * D1, D1 * D2 + N1 * N2);
+            }
+            float ln = logf(ap / am);
+            float sg = (float)((P0s > 0.0f) - (P0s < 0.0f));
+            float term = sg * (P0 * ln - dn * dt);
+            if (p0_close && !(fabsf(term) < 2e-6f)) return false;
+            if (keep) res += term;
+        }
+    }
+    *out = res * t.inv_area * t.inv_s;
+    return true;
+}
+
+// Near-field coefficient in FP32 (the mixed-precision fill): the analytic
+// potential, or for a dielectric evaluation element its central difference
+// across the panel; false where an FP64 evaluation must decide a guard.
+FCG_HD bool fcg_pot_near32(unsigned type1, const float *c1, const float *n1, const float *c2, const fcg_tri32 &t, float *out) {
+    const float k = (float)(1.0 / FCG_FOUR_PI_TIMES_E0);
+    float dx = c1[0] - c2[0], dy = c1[1] - c2[1], dz = c1[2] - c2[2];
+    float v;
+    if ((type1 & FCG_IS_DIEL) != FCG_IS_DIEL) {
+        if (!fcg_potential32(dx, dy, dz, t, &v)) return false;
+        *out = k * v;
+        return true;
+    }
+    fcg_d3 nrm = fcg_diel_normal(type1, n1);
+    float h = sqrtf(dx * dx + dy * dy + dz * dz) / 20.0f;
+    float hx = (float)nrm.x * h, hy = (float)nrm.y * h, hz = (float)nrm.z * h;
+    float pp, pn;
+    if (!fcg_potential32(dx + hx, dy + hy, dz + hz, t, &pp) || !fcg_potential32(dx - hx, dy - hy, dz - hz, t, &pn)) return false;
+    *out = k * ((pn - pp) / (2.0f * h));
+    return true;
+}
+
 // Near-field coefficient with the source triangle's precomputed table.
 FCG_HD double fcg_pot_near_tri(unsigned type1, const float *c1, const float *n1, const float *c2, const float *v2,
                                const fcg_tri64 &t) {

@@ -99,6 +99,7 @@ struct SolveTimings {
     float fill_ms = 0, solve_ms = 0, assemble_ms = 0;
     int iterations_max = 0;
     int64_t refine_checks = 0, refine_cycles = 0;  // true-residual checks, restarts they caused
+    int64_t fill_fp64 = 0;  // mixed fill: near-field / self coefficients the FP64 formula decided
     int64_t matvecs = 0;
     int64_t launches = 0, link_launches = 0, link_bytes = 0;
     double link_ms = 0;

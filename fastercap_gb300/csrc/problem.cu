@@ -132,7 +132,9 @@ struct DeviceProblem {
     // near-field (band 0) link list, built on the first fill
     int64_t n_near = -1;
     int32_t *near_link = NULL, *near_row = NULL;
-    fcg_tri64 *tri = NULL;  // source-triangle tables for the near field
+    fcg_tri64 *tri = NULL;    // source-triangle tables for the FP64 near field
+    fcg_tri32 *tri32 = NULL;  // scaled FP32 tables for the mixed near field and self terms
+    unsigned long long *fill_fp64 = NULL;  // mixed fill: coefficients the FP64 formula decided
     // host copies mapping device rows (height-major labels) back to the model's links
     std::vector<int64_t> h_ptr_model, h_ptr_dev;
     std::vector<int32_t> h_inv;
@@ -434,6 +436,67 @@ __global__ void k_fill_near(int64_t n, const int32_t *__restrict__ near_link, co
         if (!isfinite(val)) atomicOr(status, 1u);
         if (c64) c64[l] = val;
         else c32[l] = (float)val;
+    }
+}
+
+__global__ void k_make_tri32(int64_t Nn, const NodeGeo *__restrict__ geo, fcg_tri32 *__restrict__ tri) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x)
+        fcg_tri32_make(geo[i].v, geo[i].c, tri[i]);
+}
+
+// FP64 formulas for the mixed fill's few coefficients that FP32 cannot
+// decide (kept out of line: they would otherwise set the kernels' registers)
+__device__ __noinline__ float near_fp64(unsigned type1, const float *c1, const float *n1, const float *c2, const float *v2) {
+    return (float)fcg_pot_near(type1, c1, n1, c2, v2);
+}
+__device__ __noinline__ double self_fp64(const float *c, const float *v) {
+    return fcg_potential_opt(fcg_widen(c), v) / FCG_FOUR_PI_TIMES_E0;
+}
+
+// Mixed-precision near-field links: the analytic potential in FP32 in the
+// source triangle's scaled frame (fcg_pot_near32), one thread per listed
+// link; a link whose guard FP32 cannot decide takes the FP64 formula.
+__global__ void k_fill_near32(int64_t n, const int32_t *__restrict__ near_link, const int32_t *__restrict__ near_row,
+                              const uint32_t *__restrict__ src, const NodeGeo *__restrict__ geo, const fcg_tri32 *__restrict__ tri,
+                              float *__restrict__ c32, unsigned *status, unsigned long long *fb) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t l = near_link[t];
+        const NodeGeo &g1 = geo[near_row[t]];
+        uint32_t j = src[l] & kSrcMask;
+        const NodeGeo &g2 = geo[j];
+        float val;
+        if (!fcg_pot_near32(g1.type, g1.c, g1.n, g2.c, tri[j], &val)) {
+            val = near_fp64(g1.type, g1.c, g1.n, g2.c, g2.v);
+            atomicAdd(fb, 1ull);
+        }
+        if (!isfinite(val)) atomicOr(status, 1u);
+        c32[l] = val;
+    }
+}
+
+// Mixed-precision self terms: conductor leaves by the FP32 analytic potential
+// at the own centroid (FP64 where FP32 cannot decide a guard), dielectric
+// leaves by their closed form.
+__global__ void k_fill_self32(int64_t Np, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
+                              const fcg_tri32 *__restrict__ tri, const double *__restrict__ eb, const double *__restrict__ ea,
+                              double *__restrict__ self, unsigned *status, unsigned long long *fb) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
+        int32_t node = leaf_node[j];
+        const NodeGeo &g = geo[node];
+        double val;
+        if (g.type & FCG_IS_DIEL) {
+            val = fcg_self_potential(g.type, g.c, g.v, g.area, eb[j], ea[j]);
+        } else {
+            float v;
+            if (fcg_potential32(0.0f, 0.0f, 0.0f, tri[node], &v)) {
+                val = (double)(v * (float)(1.0 / FCG_FOUR_PI_TIMES_E0));
+            } else {
+                val = self_fp64(g.c, g.v);
+                atomicAdd(fb, 1ull);
+            }
+        }
+        if (!isfinite(val) || val == 0.0) atomicOr(status, 2u);
+        self[j] = val;
     }
 }
 
@@ -1920,6 +1983,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
+    FCG_TRY(dalloc(&p->fill_fp64, 1, p->bytes));
     FCG_TRY(build_plan(p, a, parent, height, lab, s));
     tr.mark("sweep plan");
     FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
@@ -1959,7 +2023,7 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
     dfree(p->left); dfree(p->right); dfree(p->node_lfirst); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
     dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
-    dfree(p->near_link); dfree(p->near_row); dfree(p->tri);
+    dfree(p->near_link); dfree(p->near_row); dfree(p->tri); dfree(p->tri32); dfree(p->fill_fp64);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
     dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
@@ -2002,7 +2066,7 @@ int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs
     b += Nn * (int64_t)(sizeof(NodeGeo) + 8 + 4 * 3 + 4 + 4 * 4);  // geometry, row pointers, tree, arrivals, sweep plan
     b += L * (4 + c);                                                  // links
     b += Np * (4 + 8 * 4 + 4);                                         // leaf maps, permittivities, self terms, geometry map
-    b += L * 8 + Nn * (int64_t)sizeof(fcg_tri64);                      // near-field list (bound: every link near) and tables
+    b += L * 8 + Nn * (int64_t)(precision == FCG_PREC_FP64 ? sizeof(fcg_tri64) : sizeof(fcg_tri32));  // near list (bound) and tables
     b += (int64_t)kp * Nn * (8 * 3 + 4 + 8);                           // matvec node work
     b += (int64_t)k * Np * 8 * (5 + vecs);                             // Krylov vectors and basis
     b += (int64_t)k * (steps + 1) * nch * 8;                           // partial sums
@@ -2104,8 +2168,15 @@ static int build_near_list(DeviceProblem *p) {
     if (n > 0) {
         k_near_list<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, ctr + 1, n, p->near_link, p->near_row);
         p->timings.launches++;
-        if ((r = dalloc(&p->tri, p->Nn, p->bytes))) { dfree(ctr); return r; }
-        k_make_tri<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri);
+        if (p->precision == FCG_PREC_FP64) {
+            if ((r = dalloc(&p->tri, p->Nn, p->bytes))) { dfree(ctr); return r; }
+            k_make_tri<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri);
+            p->timings.launches++;
+        }
+    }
+    if (p->precision == FCG_PREC_MIXED) {  // the self terms read the tables too
+        if ((r = dalloc(&p->tri32, p->Nn, p->bytes))) { dfree(ctr); return r; }
+        k_make_tri32<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri32);
         p->timings.launches++;
     }
     cudaError_t e = cudaGetLastError();
@@ -2124,6 +2195,7 @@ int problem_fill(DeviceProblem *p) {
         if (r != FCG_NORMAL_END) return r;
     }
     FCG_CK(cudaMemsetAsync(p->status, 0, sizeof(unsigned), s));
+    FCG_CK(cudaMemsetAsync(p->fill_fp64, 0, sizeof(unsigned long long), s));
     FCG_CK(cudaEventRecord(p->ev0, s));
     int sms = p->ctx->sm_count;
     bool mixed = p->precision == FCG_PREC_MIXED;
@@ -2134,17 +2206,29 @@ int problem_fill(DeviceProblem *p) {
         FCG_CK(cudaGetLastError());
         p->timings.launches++;
         if (p->n_near > 0) {
-            k_fill_near<<<grid_for(p->n_near, 128, sms), 128, 0, s>>>(p->n_near, p->near_link, p->near_row, p->link_src, p->geo,
-                                                                     p->tri, p->coef64, p->coef32, p->status);
+            if (mixed)
+                k_fill_near32<<<grid_for(p->n_near, 128, sms), 128, 0, s>>>(p->n_near, p->near_link, p->near_row, p->link_src,
+                                                                           p->geo, p->tri32, p->coef32, p->status, p->fill_fp64);
+            else
+                k_fill_near<<<grid_for(p->n_near, 128, sms), 128, 0, s>>>(p->n_near, p->near_link, p->near_row, p->link_src,
+                                                                         p->geo, p->tri, p->coef64, p->coef32, p->status);
             FCG_CK(cudaGetLastError());
             p->timings.launches++;
         }
     }
-    k_fill_self<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->leaf_eb, p->leaf_ea, p->self, p->status);
+    if (mixed)
+        k_fill_self32<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->tri32, p->leaf_eb, p->leaf_ea,
+                                                               p->self, p->status, p->fill_fp64);
+    else
+        k_fill_self<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->leaf_eb, p->leaf_ea, p->self,
+                                                             p->status);
     FCG_CK(cudaGetLastError());
     p->timings.launches++;
     FCG_CK(cudaEventRecord(p->ev1, s));
+    unsigned long long fb = 0;
+    FCG_CK(cudaMemcpyAsync(&fb, p->fill_fp64, sizeof fb, cudaMemcpyDeviceToHost, s));
     int r = check_status(p, "coefficient fill");
+    p->timings.fill_fp64 = (int64_t)fb;
     cudaEventElapsedTime(&p->timings.fill_ms, p->ev0, p->ev1);
     if (r != FCG_NORMAL_END) return r;
     p->filled = true;

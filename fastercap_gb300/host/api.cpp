@@ -313,6 +313,7 @@ int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *st) {
     st->solve_ms = t.solve_ms;
     st->refine_checks = t.refine_checks;
     st->refine_cycles = t.refine_cycles;
+    st->fill_fp64 = t.fill_fp64;
     return FCG_NORMAL_END;
 }
 

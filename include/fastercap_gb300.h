@@ -241,6 +241,8 @@ typedef struct {
     double solve_ms;          /* device time of the last solve */
     int64_t refine_checks;    /* true-residual checks after GMRES (mixed precision) */
     int64_t refine_cycles;    /* GMRES restarts those checks caused */
+    int64_t fill_fp64;        /* last mixed fill: near-field and self coefficients computed by the FP64
+                               * formula because FP32 could not decide one of its guards */
 } fcg_problem_stats;
 int fcg_problem_set_profiling(fcg_problem *p, int enable);
 int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *stats);

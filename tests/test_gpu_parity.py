@@ -7,9 +7,12 @@ central differences of the analytic potential, where the device's fused
 multiply-adds move the cancellation noise; coplanar dielectric links are zero
 up to that noise),
 matvec 1e-13 relative norm, capacitance 1e-6 relative per entry with the reference's GMRES
-iteration counts; mixed path - coefficients 1e-6 relative (FP32 quadrature
-and far field, FP64 near field rounded to FP32), matvec 2e-6 relative norm, every capacitance
-entry within 1e-3 (0.1 %) of the reference FP64 result."""
+iteration counts; mixed path - coefficients within 1e-5 relative plus 2e-6
+of the largest coefficient (FP32 quadrature and point formulas in the far
+field, the FP32 analytic potential in the near field and for the self terms;
+the near-field dielectric links are central differences, where FP32 noise is
+amplified about tenfold), matvec 2e-6 relative norm, every capacitance entry
+within 1e-3 (0.1 %) of the reference FP64 result."""
 
 import numpy as np
 import pytest
@@ -48,12 +51,13 @@ def test_fill_fp64(ctx, golden):
     np.testing.assert_allclose(sc, g["ref_self_coef"], rtol=1e-12, atol=0)
 
 
-def test_fill_mixed_rounds_fp64(ctx, golden):
+def test_fill_mixed(ctx, golden):
     name, g = golden
     p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_MIXED)
     p.fill()
-    lc, _ = p.coefficients()
-    check_coef(lc, g, 1e-6, 1e-13)
+    lc, sc = p.coefficients()
+    check_coef(lc, g, 1e-5, 2e-6)
+    np.testing.assert_allclose(sc, g["ref_self_coef"], rtol=1e-6, atol=0)
 
 
 @pytest.mark.parametrize("precision,tol", [(fc.PREC_FP64, 1e-13), (fc.PREC_MIXED, 2e-6)])
@@ -122,7 +126,7 @@ def test_oracle_fill_vs_gpu_larger(ctx, tmp_path):
     pm = ctx.problem(m, fc.PREC_MIXED)
     pm.fill()
     lm, _ = pm.coefficients()
-    np.testing.assert_allclose(lm, oc, rtol=1e-6, atol=1e-13 * np.abs(oc).max())
+    np.testing.assert_allclose(lm, oc, rtol=1e-5, atol=2e-6 * np.abs(oc).max())
     capm, _ = pm.solve(tol=1e-4)
     assert np.max(np.abs(capm - ocap) / np.abs(ocap)) < 1e-3
 

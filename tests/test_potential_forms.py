@@ -7,6 +7,13 @@ about a triangle size (the near band): random points, points in the plane
 (coplanar neighbours), just above it, near edges and vertices, and on the
 band edge. (Far away both forms lose accuracy to cancellation alike; the
 fill uses quadrature there.)
+
+The mixed-precision fill evaluates the same potential in FP32 in the source
+triangle's scaled frame (fcg_potential32). Where it decides the reference's
+guards itself it must agree with the FP64 formula to 5e-5 of the same scale;
+it must decide every generic, in-plane, just-above-plane and band-edge point,
+and it hands points where an R + l guard is too close to call in FP32 (near
+a vertex, close to an edge itself) to the FP64 formula.
 """
 
 import ctypes as C
@@ -27,6 +34,8 @@ def lib(tmp_path_factory):
     L = C.CDLL(out)
     L.pot_pair.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.pot_pair.restype = None
+    L.pot32_pair.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.pot32_pair.restype = None
     return L
 
 
@@ -39,7 +48,7 @@ def run(lib, tri, pts):
     return ref, fast
 
 
-def cases(seed, n=20000):
+def cases(seed, n=20000, with_kind=False):
     rng = np.random.default_rng(seed)
     tri = rng.uniform(-1, 1, (n, 3, 3)) * rng.uniform(1e-6, 1e2, (n, 1, 1))
     cen = tri.mean(axis=1)
@@ -58,6 +67,8 @@ def cases(seed, n=20000):
     pts = np.where((kind == 4)[:, None], tri[:, 2] + size * 1e-5 * off, pts)                    # near a vertex
     unit = off / np.linalg.norm(off, axis=1)[:, None]
     pts = np.where((kind == 5)[:, None], cen + size * unit, pts)                                # at the band edge
+    if with_kind:
+        return tri.astype(np.float32), pts, kind
     return tri.astype(np.float32), pts
 
 
@@ -70,3 +81,21 @@ def test_fast_form_matches_reference_order(lib, seed):
     scale = np.maximum(np.abs(ref), 1.0 / size)
     err = np.abs(fast - ref) / scale
     assert err.max() < 1e-12, (err.max(), np.argmax(err))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_fp32_form(lib, seed):
+    tri, pts, kind = cases(seed, with_kind=True)
+    tri = np.ascontiguousarray(tri, np.float32)
+    pts = np.ascontiguousarray(pts, np.float32)
+    n = len(tri)
+    ref, f32, ok = np.empty(n), np.empty(n), np.empty(n, np.int32)
+    lib.pot32_pair(n, tri.ctypes.data, pts.ctypes.data, ref.ctypes.data, f32.ctypes.data, ok.ctypes.data)
+    size = np.linalg.norm(tri[:, 1].astype(np.float64) - tri[:, 0], axis=1)
+    scale = np.maximum(np.abs(ref), 1.0 / size)
+    decided = ok == 1
+    err = np.abs(f32 - ref) / scale
+    assert np.all(np.isfinite(f32[decided]))
+    assert err[decided].max() < 5e-5, (err[decided].max(), np.argmax(np.where(decided, err, 0)))
+    generic = np.isin(kind, [0, 1, 2, 5])
+    assert decided[generic].all()
