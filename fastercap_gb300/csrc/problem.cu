@@ -372,12 +372,10 @@ __global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const u
     }
 }
 
-// Links of bands 1..4 (quadrature and point formulas): one warp per row;
-// FP32 in the mixed path, the reference's FP64 formulas otherwise.
-template <bool MIXED>
+// Links of bands 1..4 (quadrature and point formulas), FP64 path: the
+// reference's formulas, one warp per row.
 __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                           const NodeGeo *__restrict__ geo, double *__restrict__ c64, float *__restrict__ c32,
-                           unsigned *status) {
+                           const NodeGeo *__restrict__ geo, double *__restrict__ c64, unsigned *status) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -386,7 +384,6 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const ui
         bool diel = g1.type & FCG_IS_DIEL;
         fcg_d3 n64 = fcg_mk(0, 0, 0);
         if (diel) n64 = fcg_diel_normal(g1.type, g1.n);
-        float nx = (float)n64.x, ny = (float)n64.y, nz = (float)n64.z;
         fcg_d3 r1 = fcg_widen(g1.c);
         int64_t s = ptr[row], e = ptr[row + 1];
         for (int64_t l = s + lane; l < e; l += 32) {
@@ -394,25 +391,95 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const ui
             int band = (int)(w >> kBandShift);
             if (band == 0) continue;
             const NodeGeo &g2 = geo[w & kSrcMask];
-            if (MIXED) {
-                float dx = g1.c[0] - g2.c[0], dy = g1.c[1] - g2.c[1], dz = g1.c[2] - g2.c[2];
-                float val = fcg_pot_mid32(band, diel, dx, dy, dz, nx, ny, nz, g2.c, g2.v);
-                if (!isfinite(val)) atomicOr(status, 1u);
-                c32[l] = val;
+            double val;
+            if (band == 4) {
+                fcg_d3 dist = fcg_fsub(g1.c, g2.c);
+                double rd = fcg_mod(dist);
+                val = diel ? fcg_dot(dist, n64) / (FCG_FOUR_PI_TIMES_E0 * rd * rd * rd) : 1 / (FCG_FOUR_PI_TIMES_E0 * rd);
             } else {
-                double val;
-                if (band == 4) {
-                    fcg_d3 dist = fcg_fsub(g1.c, g2.c);
-                    double rd = fcg_mod(dist);
-                    val = diel ? fcg_dot(dist, n64) / (FCG_FOUR_PI_TIMES_E0 * rd * rd * rd) : 1 / (FCG_FOUR_PI_TIMES_E0 * rd);
-                } else {
-                    int rule = band == 1 ? 5 : (band == 2 ? 3 : 2);
-                    val = (diel ? fcg_enfield_numerical(r1, g2.v, n64, rule) : fcg_potential_numerical(r1, g2.v, rule)) /
-                          FCG_FOUR_PI_TIMES_E0;
-                }
-                if (!isfinite(val)) atomicOr(status, 1u);
-                c64[l] = val;
+                int rule = band == 1 ? 5 : (band == 2 ? 3 : 2);
+                val = (diel ? fcg_enfield_numerical(r1, g2.v, n64, rule) : fcg_potential_numerical(r1, g2.v, rule)) /
+                      FCG_FOUR_PI_TIMES_E0;
             }
+            if (!isfinite(val)) atomicOr(status, 1u);
+            c64[l] = val;
+        }
+    }
+}
+
+// Mixed-precision far field (bands 1-4): the collocation quadratures of
+// CPotential::PotentialNumerical / EnFieldNumerical (Solver/Potential.cpp:2077-2254)
+// in FP32 without a per-link frame. A rule point (x, y) of the reference's
+// frame (origin v0, x along v1 - v0) is the barycentric point (y, x, 1-x-y)
+// of (v0, v1, v2), and the frame's jacobian / (2 area) is exactly 1, so the
+// triangle average is the weighted sum over barycentric points: rule 2 the
+// three permutations of (2/3, 1/6, 1/6), rule 3 the edge midpoints, rule 5
+// the six permutations of its three coordinates. Every link evaluates six
+// slots of a per-band table (unused slots: the centroid with weight 0; the
+// point formula: the centroid offset itself with weight 1), so the lanes of
+// a warp run the same code whatever their links' bands.
+__global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
+                                                    const NodeGeo *__restrict__ geo, float *__restrict__ c32, unsigned *status) {
+    __shared__ float4 tab[5][6];  // [band][slot] = (weight of v0, of v1, of v2, quadrature weight)
+    if (threadIdx.x < 30) {
+        int band = threadIdx.x / 6, sl = threadIdx.x % 6;
+        const float t3 = 1.0f / 3.0f;
+        float4 e = make_float4(t3, t3, t3, 0.0f);
+        if (band == 4 && sl == 0) e = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        if (band == 3 && sl < 3) {  // rule 2
+            const float a = 1.0f / 6.0f, c = 4.0f / 6.0f;
+            e = sl == 0 ? make_float4(a, c, a, t3) : (sl == 1 ? make_float4(c, a, a, t3) : make_float4(a, a, c, t3));
+        }
+        if (band == 2 && sl < 3)  // rule 3
+            e = sl == 0 ? make_float4(0.5f, 0.0f, 0.5f, t3) : (sl == 1 ? make_float4(0.0f, 0.5f, 0.5f, t3) : make_float4(0.5f, 0.5f, 0.0f, t3));
+        if (band == 1) {  // rule 5
+            const float a = 0.659027622374092f, b = 0.231933368553031f, c = 0.109039009072877f, w = 1.0f / 6.0f;
+            const float4 r5[6] = {make_float4(b, a, c, w), make_float4(c, a, b, w), make_float4(a, b, c, w),
+                                  make_float4(c, b, a, w), make_float4(a, c, b, w), make_float4(b, c, a, w)};
+            e = r5[sl];
+        }
+        tab[band][sl] = e;
+    }
+    __syncthreads();
+    const float k = (float)(1.0 / FCG_FOUR_PI_TIMES_E0);
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < Nn; row += nwarps) {
+        const NodeGeo &g1 = geo[row];
+        bool diel = g1.type & FCG_IS_DIEL;
+        float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+        if (diel) {
+            fcg_d3 n64 = fcg_diel_normal(g1.type, g1.n);
+            nx = (float)n64.x; ny = (float)n64.y; nz = (float)n64.z;
+        }
+        const float c1x = g1.c[0], c1y = g1.c[1], c1z = g1.c[2];
+        int64_t s0 = ptr[row], e0 = ptr[row + 1];
+        for (int64_t l = s0 + lane; l < e0; l += 32) {
+            uint32_t w = src[l];
+            int band = (int)(w >> kBandShift);
+            if (band == 0) continue;
+            const float4 *G = reinterpret_cast<const float4 *>(geo + (w & kSrcMask));
+            float4 A = G[0], B = G[1], Cq = G[2];  // v0 v1 v2 (9 floats) and the centroid
+            float cx = Cq.y, cy = Cq.z, cz = Cq.w;
+            float dx = c1x - cx, dy = c1y - cy, dz = c1z - cz;
+            float w0x = A.x - cx, w0y = A.y - cy, w0z = A.z - cz;
+            float w1x = A.w - cx, w1y = B.x - cy, w1z = B.y - cz;
+            float w2x = B.z - cx, w2y = B.w - cy, w2z = Cq.x - cz;
+            float acc = 0.0f;
+#pragma unroll
+            for (int sl = 0; sl < 6; sl++) {
+                float4 t = tab[band][sl];
+                float ex = dx - (t.x * w0x + t.y * w1x + t.z * w2x);
+                float ey = dy - (t.x * w0y + t.y * w1y + t.z * w2y);
+                float ez = dz - (t.x * w0z + t.y * w1z + t.z * w2z);
+                float ir = rsqrtf(ex * ex + ey * ey + ez * ez);
+                float f = diel ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
+                acc += t.w * f;
+            }
+            float val = k * acc;
+            if (!isfinite(val)) atomicOr(status, 1u);
+            c32[l] = val;
         }
     }
 }
@@ -2201,8 +2268,8 @@ int problem_fill(DeviceProblem *p) {
     bool mixed = p->precision == FCG_PREC_MIXED;
     if (p->L > 0) {
         int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)sms * 32);
-        if (mixed) k_fill_far<true><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->coef32, p->status);
-        else k_fill_far<false><<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->coef32, p->status);
+        if (mixed) k_fill_far32<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef32, p->status);
+        else k_fill_far<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->status);
         FCG_CK(cudaGetLastError());
         p->timings.launches++;
         if (p->n_near > 0) {
