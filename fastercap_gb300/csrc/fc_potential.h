@@ -1,5 +1,6 @@
-// Panel-pair potential integrals shared by the host model builder (refinement
-// criteria) and the device coefficient-fill kernels.
+// Panel-pair potential integrals and element-pair tests shared by the host
+// model builder, the device model construction (mesh refinement, link
+// construction) and the device coefficient-fill kernels.
 //
 // Restated from the reference's collocation formulas:
 //   potential_opt        CPotential::PotentialOpt        Solver/Potential.cpp:1561-1711
@@ -10,6 +11,12 @@
 //                                                        Solver/Autorefine.cpp:3474-3733
 //   self_potential       CAutoRefine::SelfPotential      Solver/Autorefine.cpp:2358-2427
 //   diel_normal          CAutoPanel::GetDielNormal       Solver/AutoPanel.h:114-139
+//   refine_criteria      CAutoRefine::RefineCriteria     Solver/Autorefine.cpp:2928-3003
+//   link_decision        one step of CAutoRefine::RefineMutual  Solver/Autorefine.cpp:3096-3235
+//   mesh_decision        one step of CAutoRefine::DiscretizeMutual  Solver/Autorefine.cpp:2638-2730
+//   subdivide            CAutoPanel::Subdivide           Solver/AutoPanel.cpp:382-523
+//   newell_normal        normal of CAutoPanel::CalcPanelGeomPar  Solver/AutoPanel.cpp:51-104
+// plus FP32 forms for the mixed-precision fill (potential32, pot_near32).
 //
 // Panel vertices, centroids and normals are single precision (as the
 // reference stores them); every formula works in double. A difference of two
@@ -609,18 +616,7 @@ FCG_HD double fcg_pot_near(unsigned type1, const float *c1, const float *n1, con
     return (pn - pp) / (2 * h * FCG_FOUR_PI_TIMES_E0);
 }
 
-// ---- single-precision mid/far field (mixed-precision fill)
-
-FCG_HD float fcg_rsqrtf(float x) {
-#if defined(__CUDA_ARCH__)
-    return rsqrtf(x);
-#else
-    return 1.0f / sqrtf(x);
-#endif
-}
-//
-// Distance bands from squared float distances (no square root): the same
-// thresholds rho = |c1 - c2| / rmax < 1, 2, 4, 10.
+// ---- single-precision band classification (mixed-precision fill)
 // fcg_band of the float offset (dx, dy, dz) and rmax, decided in single
 // precision where that is certain: the FP32 ratio carries a relative error
 // below 1e-6, so outside a 1e-5 relative margin around each threshold its
@@ -636,64 +632,6 @@ FCG_HD int fcg_band_exact(float dx, float dy, float dz, double rmax) {
     if (sure) return rho < 1.0f ? 0 : rho < 2.0f ? 1 : rho < 4.0f ? 2 : rho < 10.0f ? 3 : 4;
     double rd = sqrt((double)dx * (double)dx + (double)dy * (double)dy + (double)dz * (double)dz);
     return fcg_band(rd, rmax);
-}
-
-FCG_HD int fcg_band32(float dx, float dy, float dz, float rmax) {
-    float d2 = dx * dx + dy * dy + dz * dz, r2 = rmax * rmax;
-    if (d2 < r2) return 0;
-    if (d2 < 4.0f * r2) return 1;
-    if (d2 < 16.0f * r2) return 2;
-    if (d2 < 100.0f * r2) return 3;
-    return 4;
-}
-
-// Quadrature of the source triangle v (centroid c2) seen from the evaluation
-// point at offset (dx,dy,dz) = c1 - c2. Quadrature points are formed relative
-// to c2, so the single-precision differences carry no cancellation from the
-// absolute coordinates. efield selects (r - p).n / |r - p|^3 over 1/|r - p|.
-// Result divided by the area, not by 4 pi eps0.
-FCG_HD float fcg_quad32(float dx, float dy, float dz, const float *v, const float *c2, int rule, bool efield, float nx,
-                        float ny, float nz) {
-    float s1x = v[3] - v[0], s1y = v[4] - v[1], s1z = v[5] - v[2];
-    float s2x = v[6] - v[3], s2y = v[7] - v[4], s2z = v[8] - v[5];
-    float s3x = v[0] - v[6], s3y = v[1] - v[7], s3z = v[2] - v[8];
-    float nX = s1y * s2z - s1z * s2y, nY = -s1x * s2z + s1z * s2x, nZ = s1x * s2y - s1y * s2x;
-    float mn = sqrtf(nX * nX + nY * nY + nZ * nZ);
-    float zx = nX / mn, zy = nY / mn, zz = nZ / mn;
-    float m1 = sqrtf(s1x * s1x + s1y * s1y + s1z * s1z);
-    float xx = s1x / m1, xy = s1y / m1, xz = s1z / m1;
-    float yx = xy * zz - xz * zy, yy = xz * zx - xx * zz, yz = xx * zy - xy * zx;
-    float v01 = m1, v02 = -(s3x * xx + s3y * xy + s3z * xz), v12 = -(s3x * yx + s3y * yy + s3z * yz);
-    float jac = (v02 - v01) * v12 - v12 * v02;
-    float ox = v[0] - c2[0], oy = v[1] - c2[1], oz = v[2] - c2[2];
-    float res = 0.0f;
-    int np = fcg_rule_npts(rule);
-    for (int i = 0; i < np; i++) {
-        double pxd, pyd, wd;
-        fcg_rule_point(rule, i, &pxd, &pyd, &wd);
-        float px = (float)pxd, py = (float)pyd, w = (float)wd;
-        float p0 = (v01 - v02) * px + v02 * (1.0f - py);
-        float p1 = v12 * (1.0f - px - py);
-        float ex = dx - (ox + xx * p0 + yx * p1);
-        float ey = dy - (oy + xy * p0 + yy * p1);
-        float ez = dz - (oz + xz * p0 + yz * p1);
-        float ir = fcg_rsqrtf(ex * ex + ey * ey + ez * ez);
-        float val = efield ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
-        res += w * val;
-    }
-    return res * (jac / mn);
-}
-
-// Mixed-precision coefficient for bands 1..4 (band 0 goes to fcg_pot_near).
-FCG_HD float fcg_pot_mid32(int band, bool diel, float dx, float dy, float dz, float nx, float ny, float nz, const float *c2,
-                           const float *v2) {
-    const float k = (float)(1.0 / FCG_FOUR_PI_TIMES_E0);
-    if (band == 4) {
-        float ir = fcg_rsqrtf(dx * dx + dy * dy + dz * dz);
-        return diel ? k * (dx * nx + dy * ny + dz * nz) * ir * ir * ir : k * ir;
-    }
-    int rule = band == 1 ? 5 : (band == 2 ? 3 : 2);
-    return k * fcg_quad32(dx, dy, dz, v2, c2, rule, diel, nx, ny, nz);
 }
 
 // Self coefficient of a leaf panel: collocated analytic potential for a
