@@ -455,31 +455,45 @@ __global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *_
         }
         const float c1x = g1.c[0], c1y = g1.c[1], c1z = g1.c[2];
         int64_t s0 = ptr[row], e0 = ptr[row + 1];
-        for (int64_t l = s0 + lane; l < e0; l += 32) {
-            uint32_t w = src[l];
-            int band = (int)(w >> kBandShift);
-            if (band == 0) continue;
-            const float4 *G = reinterpret_cast<const float4 *>(geo + (w & kSrcMask));
-            float4 A = G[0], B = G[1], Cq = G[2];  // v0 v1 v2 (9 floats) and the centroid
-            float cx = Cq.y, cy = Cq.z, cz = Cq.w;
-            float dx = c1x - cx, dy = c1y - cy, dz = c1z - cz;
-            float w0x = A.x - cx, w0y = A.y - cy, w0z = A.z - cz;
-            float w1x = A.w - cx, w1y = B.x - cy, w1z = B.y - cz;
-            float w2x = B.z - cx, w2y = B.w - cy, w2z = Cq.x - cz;
-            float acc = 0.0f;
+        // two links per lane in flight: both source words and both geometry
+        // gathers are issued before either is evaluated
+        for (int64_t l = s0 + lane; l < e0; l += 64) {
+            bool has2 = l + 32 < e0;
+            uint32_t wv[2];
+            wv[0] = src[l];
+            wv[1] = has2 ? src[l + 32] : 0u;  // a band-0 word: skipped below
+            float4 A[2], B[2], Cq[2];
 #pragma unroll
-            for (int sl = 0; sl < 6; sl++) {
-                float4 t = tab[band][sl];
-                float ex = dx - (t.x * w0x + t.y * w1x + t.z * w2x);
-                float ey = dy - (t.x * w0y + t.y * w1y + t.z * w2y);
-                float ez = dz - (t.x * w0z + t.y * w1z + t.z * w2z);
-                float ir = rsqrtf(ex * ex + ey * ey + ez * ez);
-                float f = diel ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
-                acc += t.w * f;
+            for (int u = 0; u < 2; u++) {
+                const float4 *G = reinterpret_cast<const float4 *>(geo + (wv[u] & kSrcMask));
+                A[u] = G[0];  // v0 v1 v2 (9 floats) and the centroid
+                B[u] = G[1];
+                Cq[u] = G[2];
             }
-            float val = k * acc;
-            if (!isfinite(val)) atomicOr(status, 1u);
-            c32[l] = val;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                int band = (int)(wv[u] >> kBandShift);
+                if (band == 0) continue;
+                float cx = Cq[u].y, cy = Cq[u].z, cz = Cq[u].w;
+                float dx = c1x - cx, dy = c1y - cy, dz = c1z - cz;
+                float w0x = A[u].x - cx, w0y = A[u].y - cy, w0z = A[u].z - cz;
+                float w1x = A[u].w - cx, w1y = B[u].x - cy, w1z = B[u].y - cz;
+                float w2x = B[u].z - cx, w2y = B[u].w - cy, w2z = Cq[u].x - cz;
+                float acc = 0.0f;
+#pragma unroll
+                for (int sl = 0; sl < 6; sl++) {
+                    float4 t = tab[band][sl];
+                    float ex = dx - (t.x * w0x + t.y * w1x + t.z * w2x);
+                    float ey = dy - (t.x * w0y + t.y * w1y + t.z * w2y);
+                    float ez = dz - (t.x * w0z + t.y * w1z + t.z * w2z);
+                    float ir = rsqrtf(ex * ex + ey * ey + ez * ez);
+                    float f = diel ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
+                    acc += t.w * f;
+                }
+                float val = k * acc;
+                if (!isfinite(val)) atomicOr(status, 1u);
+                c32[l + 32 * u] = val;
+            }
         }
     }
 }
