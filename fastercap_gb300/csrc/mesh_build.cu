@@ -41,6 +41,8 @@
 
 namespace fcg {
 
+using namespace devscan;
+
 namespace {
 
 constexpr int kMaxMeshLevel = 4096;           // the host recursion's limit

@@ -30,6 +30,7 @@
 #include <thread>
 
 #include "fc_potential.h"
+#include "scan.cuh"
 #include "fcg_internal.hpp"
 
 namespace fcg {
@@ -111,10 +112,9 @@ template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes
 }
 
 struct SweepPlan {
-    int n_blocks = 0, n_top_levels = 0, max_block_levels = 0;
+    int n_blocks = 0;
     int32_t *blk_leaf_first = NULL, *blk_nleaves = NULL, *blk_lvl_first = NULL, *blk_nlvls = NULL, *blk_root = NULL;
     int32_t *lvl_ptr = NULL, *lvl_nodes = NULL;
-    int32_t *top_lvl_ptr = NULL, *top_nodes = NULL;
 };
 
 struct DeviceProblem {
@@ -136,8 +136,10 @@ struct DeviceProblem {
     fcg_tri32 *tri32 = NULL;  // scaled FP32 tables for the mixed near field and self terms
     unsigned long long *fill_fp64 = NULL;  // mixed fill: coefficients the FP64 formula decided
     // host copies mapping device rows (height-major labels) back to the model's links
+    // (filled on the first coefficient readback)
     std::vector<int64_t> h_ptr_model, h_ptr_dev;
     std::vector<int32_t> h_inv;
+    int32_t *inv = NULL;  // device: the model node of every device label
     SolveTimings timings;
     // profiling of the link product: event pairs awaiting readout
     bool profiling = false;
@@ -1771,9 +1773,6 @@ static std::string validate(const fcg_model_arrays &a) {
     return "";
 }
 
-// Cut the node forest into subtrees of at most kBlockLeaves leaves (one CTA
-// each in the sweep kernels) and the top nodes above them, each listed by
-// height so that children are processed before parents.
 // FCG_TRACE=1 prints the host phases of problem creation to stderr
 struct HostTrace {
     bool on;
@@ -1788,97 +1787,169 @@ struct HostTrace {
     }
 };
 
-static int build_plan(DeviceProblem *p, const fcg_model_arrays &a, const std::vector<int32_t> &parent,
-                      const std::vector<int32_t> &height, const std::vector<int32_t> &lab, cudaStream_t s) {
-    int64_t Nn = a.n_nodes;
-    std::vector<int32_t> blk_leaf_first, blk_nleaves, blk_lvl_first, blk_nlvls, blk_root, lvl_ptr, lvl_nodes;
-    std::vector<std::vector<int32_t>> top_by_h;
-    int max_lv = 0;
-    // subtree roots (at most kBlockLeaves leaves, parent above that) and the
-    // top nodes by height, in post-order
-    for (int64_t i = 0; i < Nn; i++) {
-        int64_t lc = a.node_leaf_count[i];
-        int32_t par = parent[i];
-        if (lc > kBlockLeaves) {
-            if ((int)top_by_h.size() <= height[i]) top_by_h.resize(height[i] + 1);
-            top_by_h[height[i]].push_back((int32_t)i);
+// ---- device layout of a problem, from the caller's post-order arrays
+// Device node labels are height-major (leaves in leaf order, then every
+// height in post-order), rows are offset in that order, and the sweep plan
+// cuts the forest into subtrees of at most kBlockLeaves leaves (one CTA
+// each in the sweep kernels) whose internal nodes are listed by height. All
+// of it is computed here on the device; the host reads back three numbers.
+
+__global__ void k_model_parents(int64_t Nn, const uint8_t *__restrict__ type, const int32_t *__restrict__ left,
+                                const int32_t *__restrict__ right, int32_t *__restrict__ par) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x)
+        if (!(type[i] & FCG_IS_LEAF)) {
+            par[left[i]] = (int32_t)i;
+            par[right[i]] = (int32_t)i;
+        }
+}
+
+// Heights and leaf counts bottom-up: every leaf climbs while it is the
+// second of its parent's two children to arrive (the first one stops), so
+// each node is computed once, after both children. Nothing waits.
+__global__ void k_heights(int64_t Nn, const uint8_t *__restrict__ type, const int32_t *__restrict__ left,
+                          const int32_t *__restrict__ right, const int32_t *__restrict__ par, int32_t *height, int32_t *cnt,
+                          int *arrive, int *hmax) {
+    int hm = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!(type[i] & FCG_IS_LEAF)) continue;
+        int32_t n = (int32_t)i;
+        int h = 0;
+        height[n] = 0;
+        cnt[n] = 1;
+        for (;;) {
+            int32_t q = par[n];
+            if (q < 0) break;
+            __threadfence();  // this node's values are visible before the arrival is counted
+            if (atomicAdd(&arrive[q], 1) == 0) break;
+            __threadfence();
+            int32_t l = left[q], r = right[q];
+            h = 1 + max(__ldcg(&height[l]), __ldcg(&height[r]));
+            height[q] = h;
+            cnt[q] = __ldcg(&cnt[l]) + __ldcg(&cnt[r]);
+            n = q;
+        }
+        hm = max(hm, h);
+    }
+    for (int o = 16; o > 0; o >>= 1) hm = max(hm, __shfl_xor_sync(0xffffffffu, hm, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(hmax, hm);
+}
+
+// entries (height << 32 | node) for the stable sort by height
+__global__ void k_height_entries(int64_t Nn, const int32_t *__restrict__ height, unsigned long long *e) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x)
+        e[i] = ((unsigned long long)(uint32_t)height[i] << 32) | (unsigned long long)i;
+}
+
+__global__ void k_labels(int64_t Nn, const int32_t *__restrict__ inv, int32_t *__restrict__ lab) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < Nn; q += (int64_t)gridDim.x * blockDim.x)
+        lab[inv[q]] = (int32_t)q;
+}
+
+// the label range [seg_lo[h], seg_hi[h]) of every height h < nseg
+__global__ void k_seg_bounds(int64_t Nn, const int32_t *__restrict__ inv, const int32_t *__restrict__ height, int nseg,
+                             int32_t *seg_lo, int32_t *seg_hi) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < Nn; q += (int64_t)gridDim.x * blockDim.x) {
+        int h = height[inv[q]];
+        if (h >= nseg) continue;
+        if (q == 0 || height[inv[q - 1]] != h) seg_lo[h] = (int32_t)q;
+        if (q == Nn - 1 || height[inv[q + 1]] != h) seg_hi[h] = (int32_t)(q + 1);
+    }
+}
+
+// link count of every row, in label order
+__global__ void k_row_lengths(int64_t Nn, const int32_t *__restrict__ inv, const int64_t *__restrict__ ptr_model,
+                              int64_t *__restrict__ len) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < Nn; q += (int64_t)gridDim.x * blockDim.x) {
+        int32_t i = inv[q];
+        len[q] = ptr_model[i + 1] - ptr_model[i];
+    }
+}
+
+// subtree roots: at most kBlockLeaves leaves, the parent above that; marked
+// at their first leaf (block ranges tile the leaves, so a scan numbers the
+// blocks in leaf order)
+__global__ void k_block_flags(int64_t Nn, const int32_t *__restrict__ cnt, const int32_t *__restrict__ par,
+                              const int64_t *__restrict__ lf, int32_t *__restrict__ bflag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t q = par[i];
+        if (cnt[i] <= kBlockLeaves && (q < 0 || cnt[q] > kBlockLeaves)) bflag[lf[i]] = 1;
+    }
+}
+
+__global__ void k_blocks(int64_t Nn, const int32_t *__restrict__ cnt, const int32_t *__restrict__ par,
+                         const int32_t *__restrict__ height, const int64_t *__restrict__ lf, const int32_t *__restrict__ lab,
+                         const int32_t *__restrict__ bid, SweepPlan pl, int32_t *broot, int32_t *lvl_cnt, int32_t *node_cnt,
+                         int *max_depth) {
+    int md = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t q = par[i];
+        if (!(cnt[i] <= kBlockLeaves && (q < 0 || cnt[q] > kBlockLeaves))) continue;
+        int32_t b = bid[lf[i]];
+        pl.blk_leaf_first[b] = (int32_t)lf[i];
+        pl.blk_nleaves[b] = cnt[i];
+        pl.blk_nlvls[b] = height[i];
+        pl.blk_root[b] = lab[i];
+        broot[b] = (int32_t)i;
+        lvl_cnt[b] = height[i] + 1;
+        node_cnt[b] = cnt[i] - 1;
+        int depth = 0;  // ancestors above the subtree (the down-sweep's chain)
+        for (int32_t a = q; a >= 0; a = par[a]) depth++;
+        md = max(md, depth);
+    }
+    for (int o = 16; o > 0; o >>= 1) md = max(md, __shfl_xor_sync(0xffffffffu, md, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(max_depth, md);
+}
+
+// the internal nodes of every block by height: in height-major labels the
+// block's nodes of one height are one run of the height's label range (both
+// are in post-order), found by binary search for the block's post-order range
+__global__ void k_block_levels(int nb, const int32_t *__restrict__ broot, const int32_t *__restrict__ cnt,
+                               const int32_t *__restrict__ height, const int32_t *__restrict__ inv, const int32_t *__restrict__ seg_lo,
+                               const int32_t *__restrict__ seg_hi, const int32_t *__restrict__ node_off, SweepPlan pl) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        int32_t i = broot[b];
+        int32_t first = i - (2 * cnt[i] - 1) + 1;
+        int H = height[i];
+        int32_t off = node_off[b];
+        int32_t *lp = pl.lvl_ptr + pl.blk_lvl_first[b];
+        for (int h = 1; h <= H; h++) {
+            int32_t lo = seg_lo[h], hi = seg_hi[h];
+            while (lo < hi) {  // first label of height h with post-order index >= first
+                int32_t m = lo + ((hi - lo) >> 1);
+                if (inv[m] < first) lo = m + 1;
+                else hi = m;
+            }
+            int32_t a0 = lo;
+            hi = seg_hi[h];
+            while (lo < hi) {  // first label of height h with post-order index > i
+                int32_t m = lo + ((hi - lo) >> 1);
+                if (inv[m] <= i) lo = m + 1;
+                else hi = m;
+            }
+            lp[h - 1] = off;
+            for (int32_t q = a0; q < lo; q++) pl.lvl_nodes[off++] = q;
+        }
+        lp[H] = off;
+    }
+}
+
+// Contiguous row ranges of about equal work (links + 8 per row): the first
+// row whose work offset reaches b/nb of the total (a binary search per range)
+__global__ void k_row_split(int64_t Nn, const int64_t *__restrict__ ptr, int64_t nb, double total, int32_t *split) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b <= nb; b += (int64_t)gridDim.x * blockDim.x) {
+        if (b == 0 || b == nb) {
+            split[b] = b == 0 ? 0 : (int32_t)Nn;
             continue;
         }
-        if (par >= 0 && a.node_leaf_count[par] <= kBlockLeaves) continue;
-        int H = height[i];
-        blk_leaf_first.push_back((int32_t)a.node_leaf_first[i]);
-        blk_nleaves.push_back((int32_t)lc);
-        blk_lvl_first.push_back(0);
-        blk_nlvls.push_back(H);
-        blk_root.push_back((int32_t)i);
-        max_lv = std::max(max_lv, H);
-    }
-    // every block's level offsets (H+1 entries) and internal nodes (lc-1) get
-    // their own slots, so the blocks are filled on all host threads
-    int64_t nb = (int64_t)blk_root.size();
-    std::vector<int64_t> node_off(nb + 1, 0);
-    int64_t lvl_total = 0;
-    for (int64_t b = 0; b < nb; b++) {
-        blk_lvl_first[b] = (int32_t)lvl_total;
-        lvl_total += blk_nlvls[b] + 1;
-        node_off[b + 1] = node_off[b] + (blk_nleaves[b] - 1);
-    }
-    lvl_ptr.assign(lvl_total, 0);
-    lvl_nodes.assign(node_off[nb], 0);
-    parallel_for(nb, [&](int64_t b0, int64_t b1) {
-        std::vector<int32_t> hcount;
-        for (int64_t b = b0; b < b1; b++) {
-            int64_t i = blk_root[b], lc = blk_nleaves[b];
-            int64_t first = i - (2 * lc - 1) + 1;  // the subtree's nodes in post-order
-            int H = blk_nlvls[b];
-            int64_t base = node_off[b];
-            // internal nodes of the subtree grouped by height (counting sort)
-            hcount.assign(H + 2, 0);
-            for (int64_t n = first; n <= i; n++)
-                if (!(a.node_type[n] & FCG_IS_LEAF)) hcount[height[n] + 1]++;
-            for (int h = 1; h <= H; h++) hcount[h + 1] += hcount[h];
-            int32_t *lp = lvl_ptr.data() + blk_lvl_first[b];
-            for (int h = 1; h <= H; h++) lp[h - 1] = (int32_t)(base + hcount[h]);
-            lp[H] = (int32_t)(base + hcount[H + 1]);
-            for (int64_t n = first; n <= i; n++)
-                if (!(a.node_type[n] & FCG_IS_LEAF)) lvl_nodes[base + hcount[height[n]]++] = (int32_t)n;
+        double target = total * (double)b / (double)nb;
+        int64_t lo = 0, hi = Nn;
+        while (lo < hi) {
+            int64_t m = lo + ((hi - lo) >> 1);
+            if ((double)ptr[m] + 8.0 * (double)m < target) lo = m + 1;
+            else hi = m;
         }
-    });
-    // the down-sweep sums a subtree root's ancestors from a bounded chain
-    for (size_t b = 0; b < blk_root.size(); b++) {
-        int depth = 0;
-        for (int32_t q = parent[blk_root[b]]; q >= 0; q = parent[q]) depth++;
-        if (depth > 96) {
-            set_error("node tree too deep above its 256-leaf subtrees (" + std::to_string(depth) + " levels, at most 96)");
-            return FCG_GENERIC_ERROR;
-        }
+        split[b] = (int32_t)lo;
     }
-    // lvl_ptr holds, per block, H+1 offsets; blk_lvl_first indexes into it
-    std::vector<int32_t> top_lvl_ptr(1, 0), top_nodes;
-    for (size_t h = 0; h < top_by_h.size(); h++) {
-        if (top_by_h[h].empty()) continue;
-        top_nodes.insert(top_nodes.end(), top_by_h[h].begin(), top_by_h[h].end());
-        top_lvl_ptr.push_back((int32_t)top_nodes.size());
-    }
-    // node ids on the device are the height-major labels
-    for (size_t i = 0; i < blk_root.size(); i++) blk_root[i] = lab[blk_root[i]];
-    for (size_t i = 0; i < lvl_nodes.size(); i++) lvl_nodes[i] = lab[lvl_nodes[i]];
-    for (size_t i = 0; i < top_nodes.size(); i++) top_nodes[i] = lab[top_nodes[i]];
-    SweepPlan &pl = p->plan;
-    pl.n_blocks = (int)blk_leaf_first.size();
-    pl.n_top_levels = (int)top_lvl_ptr.size() - 1;
-    pl.max_block_levels = max_lv;
-    int r;
-    if ((r = upload(&pl.blk_leaf_first, blk_leaf_first.data(), blk_leaf_first.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.blk_nleaves, blk_nleaves.data(), blk_nleaves.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.blk_lvl_first, blk_lvl_first.data(), blk_lvl_first.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.blk_nlvls, blk_nlvls.data(), blk_nlvls.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.blk_root, blk_root.data(), blk_root.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.lvl_ptr, lvl_ptr.data(), lvl_ptr.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.lvl_nodes, lvl_nodes.data(), lvl_nodes.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.top_lvl_ptr, top_lvl_ptr.data(), top_lvl_ptr.size(), p->bytes, s))) return r;
-    if ((r = upload(&pl.top_nodes, top_nodes.data(), top_nodes.size(), p->bytes, s))) return r;
-    return FCG_NORMAL_END;
 }
 
 // Contiguous row ranges of about equal work (links + 8 per row) for the
@@ -1888,20 +1959,14 @@ static int set_row_split(DeviceProblem *p, int64_t ctas) {
     int64_t Nn = p->Nn, L = p->L;
     int64_t nb = std::max<int64_t>(1, std::min<int64_t>(ctas, (Nn + 63) / 64));
     if (p->row_split && nb == p->n_row_split) return FCG_NORMAL_END;
-    std::vector<int32_t> split(nb + 1, 0);
-    double total = (double)L + 8.0 * (double)Nn;
-    int64_t row = 0;
-    for (int64_t b = 1; b < nb; b++) {
-        double target = total * (double)b / (double)nb;
-        while (row < Nn && (double)p->h_ptr_dev[row] + 8.0 * (double)row < target) row++;
-        split[b] = (int32_t)row;
-    }
-    split[nb] = (int32_t)Nn;
     dfree(p->row_split);
     p->n_row_split = 0;
-    int r = upload(&p->row_split, split.data(), split.size(), p->bytes, p->stream);
+    int r = dalloc(&p->row_split, nb + 1, p->bytes);
     if (r != FCG_NORMAL_END) return r;
-    FCG_CK(cudaStreamSynchronize(p->stream));  // the host vector goes out of scope
+    k_row_split<<<grid_for(nb + 1, 128, p->ctx->sm_count), 128, 0, p->stream>>>(Nn, p->link_ptr, nb, (double)L + 8.0 * (double)Nn,
+                                                                               p->row_split);
+    FCG_CK(cudaGetLastError());
+    p->timings.launches++;
     p->n_row_split = (int)nb;
     return FCG_NORMAL_END;
 }
@@ -1950,40 +2015,13 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     cudaStream_t s = p->stream;
     int64_t Nn = a.n_nodes, Np = a.n_panels, L = a.n_links;
     AllocScope alloc_scope(s);
-    // Device node labels: height-major (all leaves in leaf order, then every
-    // height in tree order). Interaction partners have similar heights and are
-    // spatially close, so the link product's charge gathers cluster (2.3x
-    // fewer distinct sectors than the post-order numbering on a 327k-panel
-    // sphere). Rows move as whole units: each row keeps its links in order.
-    std::vector<int32_t> height(Nn, 0), lab(Nn), inv(Nn);
-    for (int64_t i = 0; i < Nn; i++)
-        if (!(a.node_type[i] & FCG_IS_LEAF)) height[i] = 1 + std::max(height[a.node_left[i]], height[a.node_right[i]]);
-    {
-        int hmax = 0;
-        for (int64_t i = 0; i < Nn; i++) hmax = std::max(hmax, height[i]);
-        std::vector<int64_t> start(hmax + 2, 0);
-        for (int64_t i = 0; i < Nn; i++) start[height[i] + 1]++;
-        for (int h = 0; h <= hmax; h++) start[h + 1] += start[h];
-        for (int64_t i = 0; i < Nn; i++) {
-            int32_t q = (int32_t)start[height[i]]++;
-            lab[i] = q;
-            inv[q] = (int32_t)i;
-        }
-    }
-    tr.mark("labels");
-    std::vector<int32_t> parent(Nn, -1);
-    parallel_for(Nn, [&](int64_t b, int64_t e) {
-        for (int64_t i = b; i < e; i++)
-            if (!(a.node_type[i] & FCG_IS_LEAF)) { parent[a.node_left[i]] = (int32_t)i; parent[a.node_right[i]] = (int32_t)i; }
-    });
-    p->h_ptr_model.assign(a.link_ptr, a.link_ptr + Nn + 1);
-    p->h_ptr_dev.assign(Nn + 1, 0);
-    p->h_inv = inv;
-    for (int64_t q = 0; q < Nn; q++) {
-        int64_t i = inv[q];
-        p->h_ptr_dev[q + 1] = p->h_ptr_dev[q] + (a.link_ptr[i + 1] - a.link_ptr[i]);
-    }
-    tr.mark("parents, row offsets");
+    // Device node labels are height-major (all leaves in leaf order, then
+    // every height in post-order): interaction partners have similar heights
+    // and are spatially close, so the link product's charge gathers cluster
+    // (2.3x fewer distinct sectors than the post-order numbering on a
+    // 327k-panel sphere). Rows move as whole units: each row keeps its links
+    // in order. Labels, row offsets and the sweep plan are computed on the
+    // device from the uploaded arrays (one synchronisation at the end).
     FCG_TRY(dalloc(&p->geo, Nn, p->bytes));
     FCG_TRY(dalloc(&p->parent, Nn, p->bytes));
     FCG_TRY(dalloc(&p->left, Nn, p->bytes));
@@ -1993,22 +2031,49 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     FCG_TRY(dalloc(&p->leaf_eb, Np, p->bytes));
     FCG_TRY(dalloc(&p->leaf_ea, Np, p->bytes));
     FCG_TRY(dalloc(&p->leaf_weight, Np, p->bytes));
-    FCG_TRY(upload(&p->link_ptr, p->h_ptr_dev.data(), Nn + 1, p->bytes, s));
+    FCG_TRY(dalloc(&p->link_ptr, Nn + 1, p->bytes));
+    FCG_TRY(dalloc(&p->inv, Nn, p->bytes));
+    FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
+    {
+        // sweep plan arrays at their bounds (blocks <= leaves; a block's
+        // heights <= its leaves - 1, its internal nodes = its leaves - 1)
+        SweepPlan &pl = p->plan;
+        FCG_TRY(dalloc(&pl.blk_leaf_first, Np, p->bytes));
+        FCG_TRY(dalloc(&pl.blk_nleaves, Np, p->bytes));
+        FCG_TRY(dalloc(&pl.blk_lvl_first, Np + 1, p->bytes));
+        FCG_TRY(dalloc(&pl.blk_nlvls, Np, p->bytes));
+        FCG_TRY(dalloc(&pl.blk_root, Np, p->bytes));
+        FCG_TRY(dalloc(&pl.lvl_ptr, Np + 1, p->bytes));
+        FCG_TRY(dalloc(&pl.lvl_nodes, Np + 1, p->bytes));
+    }
+    tr.mark("allocate");
     {
         // the caller's node, leaf and link arrays go to the device as they
-        // are; kernels scatter them into the device layout
+        // are; kernels build the device layout from them
+        const int kMaxHeights = 1 << 16;  // heights sorted in two 8-bit passes
         int64_t tb = 0;
-        int32_t *d_lab = NULL, *d_left = NULL, *d_right = NULL, *d_sptr = NULL;
+        int32_t *d_left = NULL, *d_right = NULL, *d_sptr = NULL;
         uint8_t *d_type = NULL, *d_cdiel = NULL, *d_ldiel = NULL;
         float *d_vert = NULL, *d_cent = NULL, *d_norm = NULL;
         double *d_area = NULL, *d_maxs = NULL, *d_out = NULL, *d_in = NULL, *d_surf = NULL;
         int64_t *d_lf = NULL, *d_cf = NULL, *ptr_model = NULL;
         uint32_t *src_model = NULL;
-        unsigned *dbad = NULL, hbad = 0;
+        // layout scratch
+        int32_t *d_lab = NULL, *d_par = NULL, *d_height = NULL, *d_cnt = NULL, *seg_lo = NULL, *seg_hi = NULL, *hist = NULL;
+        int32_t *bflag = NULL, *bid = NULL, *broot = NULL, *lvl_cnt = NULL, *node_cnt = NULL, *node_off = NULL;
+        unsigned long long *ent = NULL, *ent2 = NULL;
+        int64_t *rowlen = NULL;
+        long long *sums = NULL, *scal = NULL;  // scal: [0] blocks, [1] plan levels, [2] nodes, [3] links, [4] spare
+        int *iscal = NULL;                     // [0] max height, [1] max depth above a block
+        unsigned *dbad = NULL;
+        unsigned hbad = 0;
+        int hscal[2] = {0, 0};
+        long long hblocks[1] = {0};
         int nsurf = a.cond_surf_ptr[a.n_conductors];
         int rr = FCG_NORMAL_END;
+        const int64_t ntile_max = devscan::grid_tiles(std::max<int64_t>(Nn, 1) * 1) * devscan::kDigits + 1;
 #define FCG_UP(ptr, host, n) if (rr == FCG_NORMAL_END) rr = upload(&ptr, host, n, tb, s)
-        FCG_UP(d_lab, lab.data(), Nn);
+#define FCG_AL(ptr, n) if (rr == FCG_NORMAL_END) rr = dalloc(&ptr, (size_t)(n), tb)
         FCG_UP(d_type, a.node_type, Nn);
         FCG_UP(d_vert, a.node_vertices, 9 * Nn);
         FCG_UP(d_cent, a.node_centroid, 3 * Nn);
@@ -2027,47 +2092,127 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_UP(d_ldiel, a.leaf_diel, Np);
         FCG_UP(src_model, (const uint32_t *)a.link_src, L);
         FCG_UP(ptr_model, a.link_ptr, Nn + 1);
+        FCG_AL(d_lab, Nn);
+        FCG_AL(d_par, Nn);
+        FCG_AL(d_height, Nn);
+        FCG_AL(d_cnt, Nn);
+        FCG_AL(seg_lo, kMaxHeights);
+        FCG_AL(seg_hi, kMaxHeights);
+        FCG_AL(hist, ntile_max);
+        FCG_AL(ent, Nn);
+        FCG_AL(ent2, Nn);
+        FCG_AL(rowlen, Nn);
+        FCG_AL(sums, devscan::grid_tiles(std::max<int64_t>(Nn, ntile_max)) + 1);
+        FCG_AL(scal, 5);
+        FCG_AL(iscal, 2);
+        FCG_AL(bflag, Np + 1);
+        FCG_AL(bid, Np + 1);
+        FCG_AL(broot, Np);
+        FCG_AL(lvl_cnt, Np + 1);
+        FCG_AL(node_cnt, Np + 1);
+        FCG_AL(node_off, Np + 1);
+        FCG_AL(dbad, 1);
 #undef FCG_UP
-        if (rr == FCG_NORMAL_END) rr = dalloc(&dbad, 1, tb);
+#undef FCG_AL
         if (rr == FCG_NORMAL_END) rr = dalloc(&p->link_src, L, p->bytes);
         if (rr == FCG_NORMAL_END) {
+            using namespace devscan;
             int sms = ctx.sm_count;
-            cudaMemsetAsync(p->parent, 0xff, Nn * sizeof(int32_t), s);  // roots: -1
+            int gN = grid_for(Nn, 256, sms);
+            cudaMemsetAsync(d_par, 0xff, Nn * sizeof(int32_t), s);     // roots: -1
+            cudaMemsetAsync(p->parent, 0xff, Nn * sizeof(int32_t), s);
+            cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s);
+            cudaMemsetAsync(iscal, 0, 2 * sizeof(int), s);
             cudaMemsetAsync(dbad, 0, sizeof(unsigned), s);
-            k_build_nodes<<<grid_for(Nn, 256, sms), 256, 0, s>>>(Nn, d_lab, d_type, d_vert, d_cent, d_norm, d_area, d_maxs, d_left,
-                                                                  d_right, d_lf, p->geo, p->left, p->right, p->parent, p->leaf_node,
-                                                                  p->node_lfirst);
+            cudaMemsetAsync(bflag, 0, (Np + 1) * sizeof(int32_t), s);
+            k_model_parents<<<gN, 256, 0, s>>>(Nn, d_type, d_left, d_right, d_par);
+            k_heights<<<gN, 256, 0, s>>>(Nn, d_type, d_left, d_right, d_par, d_height, d_cnt, p->arrive, iscal);
+            cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s);  // zero again for the up-sweep
+            // labels: stable sort of the nodes by height (two 8-bit passes)
+            k_height_entries<<<gN, 256, 0, s>>>(Nn, d_height, ent);
+            {
+                unsigned tiles = grid_tiles(Nn);
+                int64_t nh = (int64_t)tiles * kDigits;
+                unsigned long long *src = ent, *dst = ent2;
+                for (int pass = 0; pass < 2; pass++) {
+                    int shift = 32 + 8 * pass;
+                    k_radix_hist<<<tiles, kThreads, 0, s>>>(Nn, src, shift, hist);
+                    exclusive_scan(s, nh, hist, hist, sums, scal + 4);
+                    k_radix_scatter<<<tiles, kThreads, 0, s>>>(Nn, src, shift, hist, pass == 1 ? nullptr : dst,
+                                                               pass == 1 ? p->inv : nullptr);
+                    std::swap(src, dst);
+                }
+            }
+            k_labels<<<gN, 256, 0, s>>>(Nn, p->inv, d_lab);
+            k_seg_bounds<<<gN, 256, 0, s>>>(Nn, p->inv, d_height, kMaxHeights, seg_lo, seg_hi);
+            // row offsets in label order
+            k_row_lengths<<<gN, 256, 0, s>>>(Nn, p->inv, ptr_model, rowlen);
+            exclusive_scan(s, Nn, rowlen, p->link_ptr, sums, (long long *)(p->link_ptr + Nn));
+            // the device model
+            k_build_nodes<<<gN, 256, 0, s>>>(Nn, d_lab, d_type, d_vert, d_cent, d_norm, d_area, d_maxs, d_left, d_right, d_lf, p->geo,
+                                             p->left, p->right, p->parent, p->leaf_node, p->node_lfirst);
             k_build_leaves<<<grid_for(Np, 256, sms), 256, 0, s>>>(Np, a.n_conductors, d_cf, d_cdiel, d_out, d_in, d_sptr, d_surf,
                                                                    d_ldiel, p->leaf_eb, p->leaf_ea, p->leaf_weight);
             if (L > 0) {
                 int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
                 k_relabel_links<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, d_lab, p->link_ptr, p->link_src, dbad);
             }
-            p->timings.launches += L > 0 ? 3 : 2;
+            // sweep plan: blocks numbered in leaf order, their levels
+            k_block_flags<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_lf, bflag);
+            exclusive_scan(s, Np, bflag, bid, sums, scal + 0);
+            k_blocks<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_height, d_lf, d_lab, bid, p->plan, broot, lvl_cnt, node_cnt,
+                                        iscal + 1);
+            p->timings.launches += 12 + (L > 0 ? 1 : 0);
             if (cudaGetLastError() != cudaSuccess ||
-                cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaMemcpyAsync(hblocks, scal, sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                 cudaStreamSynchronize(s) != cudaSuccess) {
                 set_error("building the device model failed");
                 rr = FCG_DEVICE_ERROR;
-            } else if (hbad) {
-                set_error("invalid model: " + std::to_string(hbad) + " link sources out of range");
-                rr = FCG_GENERIC_ERROR;
+            }
+            int nb = (int)hblocks[0];
+            if (rr == FCG_NORMAL_END && nb > 0) {
+                exclusive_scan(s, nb, lvl_cnt, p->plan.blk_lvl_first, sums, scal + 1);
+                exclusive_scan(s, nb, node_cnt, node_off, sums, scal + 2);
+                k_block_levels<<<grid_for(nb, 128, sms), 128, 0, s>>>(nb, broot, d_cnt, d_height, p->inv, seg_lo, seg_hi, node_off,
+                                                                      p->plan);
+                p->timings.launches += 7;
+            }
+            if (rr == FCG_NORMAL_END &&
+                (cudaGetLastError() != cudaSuccess ||
+                 cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                 cudaMemcpyAsync(hscal, iscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                 cudaStreamSynchronize(s) != cudaSuccess)) {
+                set_error("building the device model failed");
+                rr = FCG_DEVICE_ERROR;
+            }
+            if (rr == FCG_NORMAL_END) {
+                p->plan.n_blocks = nb;
+                if (hbad) {
+                    set_error("invalid model: " + std::to_string(hbad) + " link sources out of range");
+                    rr = FCG_GENERIC_ERROR;
+                } else if (hscal[0] >= kMaxHeights) {
+                    set_error("node tree too high (" + std::to_string(hscal[0]) + " levels)");
+                    rr = FCG_GENERIC_ERROR;
+                } else if (hscal[1] > 96) {
+                    set_error("node tree too deep above its 256-leaf subtrees (" + std::to_string(hscal[1]) + " levels, at most 96)");
+                    rr = FCG_GENERIC_ERROR;
+                }
             }
         }
-        dfree(d_lab); dfree(d_type); dfree(d_vert); dfree(d_cent); dfree(d_norm); dfree(d_area); dfree(d_maxs);
+        dfree(d_type); dfree(d_vert); dfree(d_cent); dfree(d_norm); dfree(d_area); dfree(d_maxs);
         dfree(d_left); dfree(d_right); dfree(d_lf); dfree(d_cf); dfree(d_cdiel); dfree(d_out); dfree(d_in);
         dfree(d_sptr); dfree(d_surf); dfree(d_ldiel); dfree(src_model); dfree(ptr_model); dfree(dbad);
+        dfree(d_lab); dfree(d_par); dfree(d_height); dfree(d_cnt); dfree(seg_lo); dfree(seg_hi); dfree(hist);
+        dfree(ent); dfree(ent2); dfree(rowlen); dfree(sums); dfree(scal); dfree(iscal);
+        dfree(bflag); dfree(bid); dfree(broot); dfree(lvl_cnt); dfree(node_cnt); dfree(node_off);
         if (rr != FCG_NORMAL_END) { problem_destroy(p); return rr; }
     }
-    tr.mark("device model");
+    tr.mark("device model and layout");
     FCG_TRY(dalloc(&p->self, Np, p->bytes));
     if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
     FCG_TRY(dalloc(&p->fill_fp64, 1, p->bytes));
-    FCG_TRY(build_plan(p, a, parent, height, lab, s));
-    tr.mark("sweep plan");
-    FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
     FCG_TRY(set_row_split(p, (int64_t)ctx.sm_count * 32));
     // lanes per node in the link product: about four links per lane per pass
     {
@@ -2107,7 +2252,7 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->near_link); dfree(p->near_row); dfree(p->tri); dfree(p->tri32); dfree(p->fill_fp64);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
-    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.top_lvl_ptr); dfree(pl.top_nodes);
+    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(p->inv);
     dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->arrive); dfree(p->row_split);
     free_solve_ws(p);
     dfree(p->partial);
@@ -2332,6 +2477,18 @@ int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_c
             for (int64_t l = 0; l < p->L; l++) dev[l] = tmp[l];
         }
         // device rows are in height-major order; return the model's link order
+        if (p->h_inv.empty()) {  // the maps between the orders, made on first use
+            int64_t Nn = p->Nn;
+            p->h_inv.resize(Nn);
+            p->h_ptr_dev.resize(Nn + 1);
+            FCG_CK(cudaMemcpyAsync(p->h_inv.data(), p->inv, Nn * sizeof(int32_t), cudaMemcpyDeviceToHost, p->stream));
+            FCG_CK(cudaMemcpyAsync(p->h_ptr_dev.data(), p->link_ptr, (Nn + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, p->stream));
+            FCG_CK(cudaStreamSynchronize(p->stream));
+            std::vector<int64_t> len(Nn);
+            for (int64_t q = 0; q < Nn; q++) len[p->h_inv[q]] = p->h_ptr_dev[q + 1] - p->h_ptr_dev[q];
+            p->h_ptr_model.assign(Nn + 1, 0);
+            for (int64_t i = 0; i < Nn; i++) p->h_ptr_model[i + 1] = p->h_ptr_model[i] + len[i];
+        }
         for (int64_t q = 0; q < p->Nn; q++) {
             int64_t i = p->h_inv[q], cnt = p->h_ptr_dev[q + 1] - p->h_ptr_dev[q];
             memcpy(link_coef + p->h_ptr_model[i], dev.data() + p->h_ptr_dev[q], cnt * sizeof(double));

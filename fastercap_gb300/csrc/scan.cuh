@@ -1,7 +1,9 @@
 // Building blocks shared by the device model-construction passes (link
-// construction, mesh refinement): CTA scans, a three-phase exclusive scan
-// over device arrays and a stream-ordered scratch allocator that frees
-// everything it still holds when it goes out of scope.
+// construction, mesh refinement) and the problem layout: CTA scans, a
+// three-phase exclusive scan over device arrays, a stable LSD radix pass on
+// the high 32 bits of 64-bit entries and a stream-ordered scratch allocator
+// that frees everything it still holds when it goes out of scope. Every
+// translation unit gets its own copy (internal linkage).
 #ifndef FCG_SCAN_CUH
 #define FCG_SCAN_CUH
 
@@ -12,9 +14,11 @@
 #include <vector>
 
 namespace fcg {
+namespace devscan {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kDigits = 256;
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;  // items per CTA in the tiled kernels
 constexpr int kWarps = kThreads / 32;
@@ -155,7 +159,70 @@ struct Bufs {
     }
 };
 
+// digit histogram of one tile, digit-major: hist[digit * ntiles + tile]
+__global__ void __launch_bounds__(kThreads) k_radix_hist(int64_t n, const unsigned long long *__restrict__ in, int shift, int *hist) {
+    __shared__ int h[kDigits];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t t0 = (int64_t)blockIdx.x * kTile;
+    for (int j = threadIdx.x; j < kTile; j += kThreads) {
+        int64_t i = t0 + j;
+        if (i < n) atomicAdd(&h[(int)((in[i] >> shift) & 255)], 1);
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// stable scatter of one tile by digit. Warp w owns tile items
+// [w*256, w*256+256) in eight rounds of 32 consecutive items, so (warp,
+// round, lane) is the items' order; inside a round the lanes of one digit
+// rank themselves with a warp match, across rounds a per-warp running count
+// carries the order, across warps an exclusive prefix per digit.
+__global__ void __launch_bounds__(kThreads) k_radix_scatter(int64_t n, const unsigned long long *__restrict__ in, int shift,
+                                                            const int *__restrict__ hist_off, unsigned long long *out,
+                                                            int32_t *out_src) {
+    __shared__ int wcnt[kWarps][kDigits];
+    for (int j = threadIdx.x; j < kWarps * kDigits; j += kThreads) (&wcnt[0][0])[j] = 0;
+    __syncthreads();
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t t0 = (int64_t)blockIdx.x * kTile + w * (32 * kItems);
+    unsigned long long v[kItems];
+    int pos[kItems], dg[kItems];
+    for (int r = 0; r < kItems; r++) {
+        int64_t i = t0 + r * 32 + lane;
+        bool ok = i < n;
+        v[r] = ok ? in[i] : 0ull;
+        int d = ok ? (int)((v[r] >> shift) & 255) : kDigits + lane;  // lanes past the end match nobody
+        unsigned m = __match_any_sync(0xffffffffu, d);
+        int rk = __popc(m & ((1u << lane) - 1u));
+        pos[r] = ok ? wcnt[w][d] + rk : 0;
+        dg[r] = d;
+        __syncwarp();
+        if (ok && rk == 0) wcnt[w][d] += __popc(m);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        int run = 0;
+        for (int ww = 0; ww < kWarps; ww++) {
+            int c = wcnt[ww][threadIdx.x];
+            wcnt[ww][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int r = 0; r < kItems; r++) {
+        int64_t i = t0 + r * 32 + lane;
+        if (i >= n) break;
+        int d = dg[r];
+        int64_t dst = (int64_t)hist_off[(int64_t)d * gridDim.x + blockIdx.x] + wcnt[w][d] + pos[r];
+        if (out_src) out_src[dst] = (int32_t)(uint32_t)(v[r] & 0xffffffffull);
+        else out[dst] = v[r];
+    }
+}
+
 }  // namespace
+}  // namespace devscan
 }  // namespace fcg
 
 #endif
