@@ -25,6 +25,7 @@ struct DeviceProblem;
 struct DeviceContext {
     int device = 0;
     int sm_count = 0;
+    size_t smem_optin = 0;  // shared memory a CTA may opt into (bytes)
     size_t free_bytes = 0, total_bytes = 0;
     void *stream = nullptr;  // cudaStream_t owned by the context
     // the handle and every problem created on the context hold a reference;

@@ -45,6 +45,8 @@ namespace fcg {
     } while (0)
 
 static const int kBlockLeaves = 256;  // leaves per sweep subtree
+static const int kMaxChain = 96;      // ancestors above a sweep subtree
+static const int kSweepCols = 4;      // right-hand sides per shared-memory pass of the sweeps
 static const int kMaxK = 32;          // right-hand sides per matvec batch
 static const int kDotChunk = 1024;    // vector elements per CTA in the Krylov kernels
 static const int kPinSlots = 1024;    // pinned readback slots per context
@@ -111,10 +113,21 @@ template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes
     return FCG_NORMAL_END;
 }
 
+// The sweeps' plan. Blocks are the maximal subtrees of at most kBlockLeaves
+// leaves (one CTA each); inside a block a node has a local index: leaves
+// 0..nl-1 in leaf order, internal nodes nl + their position in the block's
+// by-height list. Top nodes (more than kBlockLeaves leaves) form a forest
+// over the blocks, listed by height; their children are named by top-local
+// indices (block b -> b, top entry t -> n_blocks + t).
 struct SweepPlan {
     int n_blocks = 0;
+    int n_top = 0, n_top_levels = 0;  // top nodes; heights 0..n_top_levels-1 (top_hptr has n_top_levels + 1 entries)
     int32_t *blk_leaf_first = NULL, *blk_nleaves = NULL, *blk_lvl_first = NULL, *blk_nlvls = NULL, *blk_root = NULL;
     int32_t *lvl_ptr = NULL, *lvl_nodes = NULL;
+    uint32_t *lvl_kids = NULL;                      // per internal block node: left | right << 16 (local indices)
+    int32_t *blk_chain = NULL, *chain = NULL;       // ancestors of every block root, parent first (device labels)
+    int32_t *top_nodes = NULL, *top_hptr = NULL;    // top nodes by height (device labels), offsets per height
+    int2 *top_kids = NULL;                          // children of every top node (top-local indices)
 };
 
 struct DeviceProblem {
@@ -164,7 +177,6 @@ struct DeviceProblem {
     double *Qd = NULL, *Pd = NULL, *Ad = NULL;
     float *Qf = NULL;
     float2 *Pf2 = NULL;
-    int *arrive = NULL;  // per-node arrival counters of the up-sweep (zero between products)
     int spmv_lanes = 32;  // lanes per destination node in the link product (8, 16 or 32)
     int32_t *row_split = NULL;  // multi-right-hand-side link product: CTA b owns rows [row_split[b], row_split[b+1])
     int n_row_split = 0;
@@ -602,62 +614,119 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
     }
 }
 
-// Up-sweep (CMultHier::ComputePanelCharges_fast, Solver/MultiplyHierarchical.cpp:72-127):
-// each CTA takes one subtree of at most kBlockLeaves leaves - leaves read the
-// (optionally Jacobi-scaled) input, internal nodes add their children level by
-// level - and then climbs the top of the tree: a CTA that completes a top
-// node's child increments that node's arrival counter, and the CTA that
-// arrives second (both children done) computes the node and goes on to its
-// parent. Nothing ever waits; the second arriver resets the counter.
+// Up-sweep (CMultHier::ComputePanelCharges_fast, Solver/MultiplyHierarchical.cpp:72-127),
+// in two launches. k_up_blk: one CTA per block; the block's node list, its
+// children (local indices) and its level offsets are staged in shared
+// memory, the leaves read the (optionally Jacobi-scaled) input, and every
+// internal node sums its two children level by level in shared memory
+// (left + right, in FP64), so a level costs a barrier, not a round trip to
+// memory. Node charges go to Qf (mixed) or Qd (FP64); the mixed path also
+// keeps the block root's FP64 charge for the top pass. Leaf j has device
+// label j. Right-hand sides are processed kc at a time.
 template <bool MIXED>
-__global__ void k_up(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const double *__restrict__ in, int64_t ld,
-                     int k, int kp, const double *__restrict__ diag, double *Qd, float *Qf, const int32_t *__restrict__ left_of,
-                     const int32_t *__restrict__ right_of, const int32_t *__restrict__ parent, int *arrive) {
-    int b = blockIdx.x;
-    int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b];
-    // right-hand side fastest: a node's kp values are written together
-    for (int t = threadIdx.x; t < nl * k; t += blockDim.x) {
-        int i = t / k, r = t - i * k;
-        int j = lf + i;
-        double xv = in[(int64_t)r * ld + j];
-        if (diag) xv = xv / diag[j];
-        int64_t node = leaf_node[j];
-        Qd[node * kp + r] = xv;
-        if (MIXED) Qf[node * kp + r] = (float)xv;
+__global__ void __launch_bounds__(kBlockLeaves) k_up_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld, int k,
+                                                         int kp, int kc, const double *__restrict__ diag, double *__restrict__ Qd,
+                                                         float *__restrict__ Qf) {
+    extern __shared__ double sh[];
+    double *val = sh;                                                 // (2 kBlockLeaves - 1) x kc
+    uint32_t *kids = (uint32_t *)(sh + (2 * kBlockLeaves - 1) * kc);  // kBlockLeaves
+    int32_t *lbl = (int32_t *)(kids + kBlockLeaves);                  // kBlockLeaves
+    int32_t *lp = lbl + kBlockLeaves;                                 // kBlockLeaves + 1
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b], lv0 = plan.blk_lvl_first[b], H = plan.blk_nlvls[b];
+    const int base = plan.lvl_ptr[lv0], ni = nl - 1;
+    for (int t = tid; t < ni; t += blockDim.x) {
+        kids[t] = plan.lvl_kids[base + t];
+        lbl[t] = plan.lvl_nodes[base + t];
     }
-    __syncthreads();
-    int lv0 = plan.blk_lvl_first[b], nlv = plan.blk_nlvls[b];
-    for (int h = 0; h < nlv; h++) {
-        int a0 = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a0;
-        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int q = t / k, r = t - q * k;
-            int n = plan.lvl_nodes[a0 + q];
-            double sum = Qd[(int64_t)left_of[n] * kp + r] + Qd[(int64_t)right_of[n] * kp + r];
-            Qd[(int64_t)n * kp + r] = sum;
-            if (MIXED) Qf[(int64_t)n * kp + r] = (float)sum;
+    for (int t = tid; t <= H; t += blockDim.x) lp[t] = plan.lvl_ptr[lv0 + t] - base;
+    for (int c0 = 0; c0 < k; c0 += kc) {
+        const int kk = min(kc, k - c0);
+        for (int t = tid; t < nl * kk; t += blockDim.x) {
+            int r = t / nl, i = t - r * nl;
+            double x = in[(int64_t)(c0 + r) * ld + lf + i];
+            if (diag) x = x / diag[lf + i];
+            val[i * kc + r] = x;
+            int64_t o = (int64_t)(lf + i) * kp + c0 + r;
+            if (!MIXED || ni == 0) Qd[o] = x;
+            if (MIXED) Qf[o] = (float)x;
         }
         __syncthreads();
-    }
-    // every thread publishes its node values GPU-wide before the root is signalled
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x >= 32) return;
-    int lane = threadIdx.x;
-    int p = parent[plan.blk_root[b]];
-    while (p >= 0) {
-        __threadfence();  // this CTA's node values are visible GPU-wide before it signals
-        int old = 0;
-        if (lane == 0) old = atomicAdd(&arrive[p], 1);
-        old = __shfl_sync(0xffffffffu, old, 0);
-        if (old == 0) break;  // the sibling's CTA finishes this node
-        if (lane == 0) arrive[p] = 0;
-        int l = left_of[p], r = right_of[p];
-        for (int rr = lane; rr < k; rr += 32) {
-            double sum = __ldcg(&Qd[(int64_t)l * kp + rr]) + __ldcg(&Qd[(int64_t)r * kp + rr]);
-            Qd[(int64_t)p * kp + rr] = sum;
-            if (MIXED) Qf[(int64_t)p * kp + rr] = (float)sum;
+        for (int h = 0; h < H; h++) {
+            const int a = lp[h], cnt = lp[h + 1] - a;
+            for (int t = tid; t < cnt * kk; t += blockDim.x) {
+                int q = a + t / kk, r = t - (t / kk) * kk;
+                uint32_t kd = kids[q];
+                double sum = val[(kd & 0xffffu) * kc + r] + val[(kd >> 16) * kc + r];
+                val[(nl + q) * kc + r] = sum;
+                int64_t o = (int64_t)lbl[q] * kp + c0 + r;
+                if (!MIXED || q == ni - 1) Qd[o] = sum;  // the root is the block's last (highest) node
+                if (MIXED) Qf[o] = (float)sum;
+            }
+            __syncthreads();
         }
-        p = parent[p];
+    }
+}
+
+// k_up_top: one CTA computes every top node from the block roots' FP64
+// charges, height by height in shared memory (the host sizes kc so that
+// (blocks + top nodes) x kc values fit). k_up_top_global is the same pass
+// through device memory for forests too large for shared memory.
+template <bool MIXED>
+__global__ void __launch_bounds__(1024) k_up_top(const SweepPlan plan, int k, int kp, int kc, double *__restrict__ Qd,
+                                                 float *__restrict__ Qf) {
+    extern __shared__ double sh[];
+    const int nb = plan.n_blocks, T = plan.n_top, nh = plan.n_top_levels, tid = threadIdx.x;
+    double *val = sh;                                        // (nb + T) x kc
+    int2 *kids = (int2 *)(sh + (int64_t)(nb + T) * kc);      // T
+    int32_t *lbl = (int32_t *)(kids + T);                    // T
+    int32_t *hp = lbl + T;                                   // nh + 1
+    for (int t = tid; t < T; t += blockDim.x) {
+        kids[t] = plan.top_kids[t];
+        lbl[t] = plan.top_nodes[t];
+    }
+    for (int t = tid; t <= nh; t += blockDim.x) hp[t] = plan.top_hptr[t];
+    for (int c0 = 0; c0 < k; c0 += kc) {
+        const int kk = min(kc, k - c0);
+        for (int t = tid; t < nb * kk; t += blockDim.x) {
+            int r = t / nb, bb = t - r * nb;
+            val[bb * kc + r] = Qd[(int64_t)plan.blk_root[bb] * kp + c0 + r];
+        }
+        __syncthreads();
+        for (int h = 0; h < nh; h++) {
+            const int a = hp[h], cnt = hp[h + 1] - a;
+            if (cnt == 0) continue;  // uniform: every thread reads the same offsets
+            for (int t = tid; t < cnt * kk; t += blockDim.x) {
+                int q = a + t / kk, r = t - (t / kk) * kk;
+                int2 kd = kids[q];
+                double sum = val[(int64_t)kd.x * kc + r] + val[(int64_t)kd.y * kc + r];
+                val[(int64_t)(nb + q) * kc + r] = sum;
+                int64_t o = (int64_t)lbl[q] * kp + c0 + r;
+                if (!MIXED) Qd[o] = sum;
+                if (MIXED) Qf[o] = (float)sum;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(1024) k_up_top_global(const SweepPlan plan, int k, int kp, double *Qd, float *Qf) {
+    const int nb = plan.n_blocks, nh = plan.n_top_levels;
+    for (int h = 0; h < nh; h++) {
+        const int a = plan.top_hptr[h], cnt = plan.top_hptr[h + 1] - a;
+        if (cnt == 0) continue;
+        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
+            int q = a + t / k, r = t - (t / k) * k;
+            int2 kd = plan.top_kids[q];
+            int32_t l = kd.x < nb ? plan.blk_root[kd.x] : plan.top_nodes[kd.x - nb];
+            int32_t rt = kd.y < nb ? plan.blk_root[kd.y] : plan.top_nodes[kd.y - nb];
+            double sum = Qd[(int64_t)l * kp + r] + Qd[(int64_t)rt * kp + r];
+            int64_t o = (int64_t)plan.top_nodes[q] * kp + r;
+            Qd[o] = sum;
+            if (MIXED) Qf[o] = (float)sum;
+        }
+        __syncthreads();  // this level's charges are visible to the CTA's next level
     }
 }
 
@@ -668,67 +737,81 @@ __device__ __forceinline__ double pval(const float2 *P, int64_t i) {
 }
 
 // Down-sweep (CMultHier::ComputeLeafPotentials_fast, Solver/MultiplyHierarchical.cpp:231-283):
-// A(n) = P(n) + A(parent(n)) from the top; each CTA first sums the link
-// potentials of its subtree root's ancestors (top down, the reference's
-// order), then descends its subtree level by level and writes
-// v = (self * x + P(leaf)) + A(parent(leaf)).
+// A(n) = P(n) + A(parent(n)) from the top. One CTA per block: the link
+// potentials of the block's nodes and of its root's ancestors are staged in
+// shared memory, the ancestors are summed top down (the reference's order),
+// then every internal node, level by level from the root, adds its A to its
+// internal children's P (which makes their A) or hands it to its leaf
+// children, and every leaf writes v = (self * x + P(leaf)) + A(parent(leaf)).
 template <class TP>
-__global__ void k_down(const SweepPlan plan, const int32_t *__restrict__ leaf_node, const double *__restrict__ in, int64_t ld,
-                       int k, int kp, const double *__restrict__ diag, const double *__restrict__ self, const TP *__restrict__ P,
-                       double *A, const int32_t *__restrict__ parent, double *__restrict__ out, unsigned *status) {
-    __shared__ double s_anc[32];
-    __shared__ int s_hasp;
-    const int kMaxChain = 96;
-    int b = blockIdx.x;
-    int root = plan.blk_root[b];
-    if (threadIdx.x < 32) {
-        int chain[kMaxChain];
-        int n = 0;
-        int pp = parent[root];
-        while (pp >= 0 && n < kMaxChain) { chain[n++] = pp; pp = parent[pp]; }
-        if (pp >= 0 && threadIdx.x == 0) atomicOr(status, 4u);  // deeper than supported: flagged, result invalid
-        for (int rr = threadIdx.x; rr < k; rr += 32) {
-            double acc = 0.0;
-            if (n > 0) {
-                acc = pval(P, (int64_t)chain[n - 1] * kp + rr);
-                for (int i = n - 2; i >= 0; i--) acc = pval(P, (int64_t)chain[i] * kp + rr) + acc;
-            }
-            s_anc[rr] = acc;
-        }
-        if (threadIdx.x == 0) s_hasp = n > 0;
+__global__ void __launch_bounds__(kBlockLeaves) k_down_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld, int k,
+                                                           int kp, int kc, const double *__restrict__ diag,
+                                                           const double *__restrict__ self, const TP *__restrict__ P,
+                                                           double *__restrict__ out) {
+    extern __shared__ double sh[];
+    double *pv = sh;                                           // (2 kBlockLeaves - 1) x kc: P, then A of internal nodes
+    double *al = pv + (2 * kBlockLeaves - 1) * kc;             // kBlockLeaves x kc: A of each leaf's parent
+    double *cp = al + kBlockLeaves * kc;                       // kMaxChain x kc: P of the root's ancestors
+    uint32_t *kids = (uint32_t *)(cp + kMaxChain * kc);        // kBlockLeaves
+    int32_t *lbl = (int32_t *)(kids + kBlockLeaves);           // kBlockLeaves
+    int32_t *lp = lbl + kBlockLeaves;                          // kBlockLeaves + 1
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b], lv0 = plan.blk_lvl_first[b], H = plan.blk_nlvls[b];
+    const int base = plan.lvl_ptr[lv0], ni = nl - 1;
+    const int ch0 = plan.blk_chain[b], nc = plan.blk_chain[b + 1] - ch0;
+    for (int t = tid; t < ni; t += blockDim.x) {
+        kids[t] = plan.lvl_kids[base + t];
+        lbl[t] = plan.lvl_nodes[base + t];
     }
+    for (int t = tid; t <= H; t += blockDim.x) lp[t] = plan.lvl_ptr[lv0 + t] - base;
     __syncthreads();
-    bool hasp = s_hasp != 0;
-    int lv0 = plan.blk_lvl_first[b], nlv = plan.blk_nlvls[b];
-    for (int h = nlv - 1; h >= 0; h--) {
-        int a0 = plan.lvl_ptr[lv0 + h], e = plan.lvl_ptr[lv0 + h + 1], cnt = e - a0;
-        for (int t = threadIdx.x; t < cnt * k; t += blockDim.x) {
-            int q = t / k, r = t - q * k;
-            int n = plan.lvl_nodes[a0 + q];
-            double acc = pval(P, (int64_t)n * kp + r);
-            if (n == root) {
-                if (hasp) acc = acc + s_anc[r];
-            } else {
-                acc = acc + A[(int64_t)parent[n] * kp + r];
-            }
-            A[(int64_t)n * kp + r] = acc;
+    const bool hasA = ni > 0 || nc > 0;
+    for (int c0 = 0; c0 < k; c0 += kc) {
+        const int kk = min(kc, k - c0);
+        for (int t = tid; t < nl * kk; t += blockDim.x) {
+            int r = t / nl, i = t - r * nl;
+            pv[i * kc + r] = pval(P, (int64_t)(lf + i) * kp + c0 + r);
+        }
+        for (int t = tid; t < ni * kk; t += blockDim.x) {
+            int r = t / ni, q = t - r * ni;
+            pv[(nl + q) * kc + r] = pval(P, (int64_t)lbl[q] * kp + c0 + r);
+        }
+        for (int t = tid; t < nc * kk; t += blockDim.x) {
+            int r = t / nc, j = t - r * nc;
+            cp[j * kc + r] = pval(P, (int64_t)plan.chain[ch0 + j] * kp + c0 + r);
         }
         __syncthreads();
-    }
-    int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b];
-    for (int t = threadIdx.x; t < nl * k; t += blockDim.x) {
-        int i = t % nl, r = t / nl;
-        int j = lf + i;
-        double xv = in[(int64_t)r * ld + j];
-        if (diag) xv = xv / diag[j];
-        int node = leaf_node[j];
-        double v = self[j] * xv + pval(P, (int64_t)node * kp + r);
-        if (node == root) {
-            if (hasp) v = v + s_anc[r];
-        } else {
-            v = v + A[(int64_t)parent[node] * kp + r];
+        if (tid < kk && nc > 0) {
+            double acc = cp[(nc - 1) * kc + tid];
+            for (int j = nc - 2; j >= 0; j--) acc = cp[j * kc + tid] + acc;
+            if (ni > 0) pv[(nl + ni - 1) * kc + tid] = pv[(nl + ni - 1) * kc + tid] + acc;  // A of the block root
+            else al[tid] = acc;                                                             // a leaf root's parent sum
         }
-        out[(int64_t)r * ld + j] = v;
+        __syncthreads();
+        for (int h = H - 1; h >= 0; h--) {
+            const int a = lp[h], cnt = lp[h + 1] - a;
+            for (int t = tid; t < cnt * kk; t += blockDim.x) {
+                int q = a + t / kk, r = t - (t / kk) * kk;
+                double A = pv[(nl + q) * kc + r];
+                uint32_t kd = kids[q];
+                int c1 = kd & 0xffffu, c2 = kd >> 16;
+                if (c1 < nl) al[c1 * kc + r] = A;
+                else pv[c1 * kc + r] = pv[c1 * kc + r] + A;
+                if (c2 < nl) al[c2 * kc + r] = A;
+                else pv[c2 * kc + r] = pv[c2 * kc + r] + A;
+            }
+            __syncthreads();
+        }
+        for (int t = tid; t < nl * kk; t += blockDim.x) {
+            int r = t / nl, i = t - r * nl;
+            int j = lf + i;
+            double xv = in[(int64_t)(c0 + r) * ld + j];
+            if (diag) xv = xv / diag[j];
+            double v = self[j] * xv + pv[i * kc + r];
+            if (hasA) v = v + al[i * kc + r];
+            out[(int64_t)(c0 + r) * ld + j] = v;
+        }
+        __syncthreads();  // the next pass reuses the shared arrays
     }
 }
 
@@ -1634,6 +1717,10 @@ int context_init(DeviceContext &ctx, int device) {
     FCG_CK(cudaGetDeviceProperties(&prop, device));
     ctx.device = device;
     ctx.sm_count = prop.multiProcessorCount;
+    ctx.smem_optin = prop.sharedMemPerBlockOptin;
+    // the up-sweep's top pass holds the whole top forest in shared memory
+    FCG_CK(cudaFuncSetAttribute(k_up_top<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
+    FCG_CK(cudaFuncSetAttribute(k_up_top<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
     FCG_CK(cudaMemGetInfo(&ctx.free_bytes, &ctx.total_bytes));
     cudaStream_t st;
     FCG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -1879,7 +1966,7 @@ __global__ void k_block_flags(int64_t Nn, const int32_t *__restrict__ cnt, const
 __global__ void k_blocks(int64_t Nn, const int32_t *__restrict__ cnt, const int32_t *__restrict__ par,
                          const int32_t *__restrict__ height, const int64_t *__restrict__ lf, const int32_t *__restrict__ lab,
                          const int32_t *__restrict__ bid, SweepPlan pl, int32_t *broot, int32_t *lvl_cnt, int32_t *node_cnt,
-                         int *max_depth) {
+                         int32_t *bdepth, int *max_depth) {
     int md = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
         int32_t q = par[i];
@@ -1893,7 +1980,8 @@ __global__ void k_blocks(int64_t Nn, const int32_t *__restrict__ cnt, const int3
         lvl_cnt[b] = height[i] + 1;
         node_cnt[b] = cnt[i] - 1;
         int depth = 0;  // ancestors above the subtree (the down-sweep's chain)
-        for (int32_t a = q; a >= 0; a = par[a]) depth++;
+        for (int32_t a = q; a >= 0 && depth <= kMaxChain; a = par[a]) depth++;
+        bdepth[b] = min(depth, kMaxChain + 1);
         md = max(md, depth);
     }
     for (int o = 16; o > 0; o >>= 1) md = max(md, __shfl_xor_sync(0xffffffffu, md, o));
@@ -1905,7 +1993,8 @@ __global__ void k_blocks(int64_t Nn, const int32_t *__restrict__ cnt, const int3
 // are in post-order), found by binary search for the block's post-order range
 __global__ void k_block_levels(int nb, const int32_t *__restrict__ broot, const int32_t *__restrict__ cnt,
                                const int32_t *__restrict__ height, const int32_t *__restrict__ inv, const int32_t *__restrict__ seg_lo,
-                               const int32_t *__restrict__ seg_hi, const int32_t *__restrict__ node_off, SweepPlan pl) {
+                               const int32_t *__restrict__ seg_hi, const int32_t *__restrict__ node_off, SweepPlan pl,
+                               int32_t *__restrict__ ent_blk, int32_t *__restrict__ pos_of) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         int32_t i = broot[b];
         int32_t first = i - (2 * cnt[i] - 1) + 1;
@@ -1927,9 +2016,80 @@ __global__ void k_block_levels(int nb, const int32_t *__restrict__ broot, const 
                 else hi = m;
             }
             lp[h - 1] = off;
-            for (int32_t q = a0; q < lo; q++) pl.lvl_nodes[off++] = q;
+            for (int32_t q = a0; q < lo; q++) {
+                pl.lvl_nodes[off] = q;
+                ent_blk[off] = b;
+                pos_of[q] = off;
+                off++;
+            }
         }
         lp[H] = off;
+    }
+}
+
+// children of every internal block node as local indices (leaves by leaf
+// offset, internal nodes by list position), packed left | right << 16
+__global__ void k_block_kids(const long long *__restrict__ n_ent, SweepPlan pl, const int32_t *__restrict__ ent_blk,
+                             const int32_t *__restrict__ pos_of, const int32_t *__restrict__ inv, const int32_t *__restrict__ lab,
+                             const uint8_t *__restrict__ type, const int32_t *__restrict__ left, const int32_t *__restrict__ right,
+                             const int64_t *__restrict__ lf) {
+    const int64_t ne = *n_ent;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        int b = ent_blk[e];
+        int32_t i = inv[pl.lvl_nodes[e]];
+        int lfb = pl.blk_leaf_first[b], nlb = pl.blk_nleaves[b], base = pl.lvl_ptr[pl.blk_lvl_first[b]];
+        int32_t c[2] = {left[i], right[i]};
+        uint32_t loc[2];
+        for (int u = 0; u < 2; u++)
+            loc[u] = (type[c[u]] & FCG_IS_LEAF) ? (uint32_t)(lf[c[u]] - lfb) : (uint32_t)(nlb + pos_of[lab[c[u]]] - base);
+        pl.lvl_kids[e] = loc[0] | (loc[1] << 16);
+    }
+}
+
+// top nodes (more than kBlockLeaves leaves) in label order, which is by
+// height; every leaf must carry its own leaf index as label
+__global__ void k_top_flags(int64_t Nn, int64_t Np, const int32_t *__restrict__ inv, const int32_t *__restrict__ cnt,
+                            const int32_t *__restrict__ leaf_node, int32_t *__restrict__ flag, unsigned *bad) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < Nn; q += (int64_t)gridDim.x * blockDim.x) {
+        flag[q] = cnt[inv[q]] > kBlockLeaves ? 1 : 0;
+        if (q < Np && leaf_node[q] != (int32_t)q) atomicAdd(bad, 1u);
+    }
+}
+
+__global__ void k_top_list(int64_t Nn, const int32_t *__restrict__ inv, const int32_t *__restrict__ lab, const int32_t *__restrict__ cnt,
+                           const int32_t *__restrict__ left, const int32_t *__restrict__ right, const int64_t *__restrict__ lf,
+                           const int32_t *__restrict__ bid, const int32_t *__restrict__ tpos, const long long *__restrict__ n_blocks,
+                           SweepPlan pl) {
+    const int nb = (int)*n_blocks;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < Nn; q += (int64_t)gridDim.x * blockDim.x) {
+        int32_t i = inv[q];
+        if (cnt[i] <= kBlockLeaves) continue;
+        int t = tpos[q];
+        pl.top_nodes[t] = (int32_t)q;
+        int32_t c[2] = {left[i], right[i]};
+        int loc[2];
+        for (int u = 0; u < 2; u++) loc[u] = cnt[c[u]] > kBlockLeaves ? nb + tpos[lab[c[u]]] : bid[lf[c[u]]];
+        pl.top_kids[t] = make_int2(loc[0], loc[1]);
+    }
+}
+
+// offsets of every height in the top list: the top nodes before the
+// height's first label
+__global__ void k_top_hptr(const int *__restrict__ hmax, int hcap, const int32_t *__restrict__ seg_lo, const int32_t *__restrict__ tpos,
+                           const long long *__restrict__ n_top, int32_t *hptr) {
+    const int H = *hmax;
+    if (H > hcap) return;  // too high: the model is rejected
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h <= H + 1; h += gridDim.x * blockDim.x)
+        hptr[h] = h <= H ? tpos[seg_lo[h]] : (int32_t)*n_top;
+}
+
+// the ancestors of every block root, parent first
+__global__ void k_chains(int nb, const int32_t *__restrict__ broot, const int32_t *__restrict__ par, const int32_t *__restrict__ lab,
+                         SweepPlan pl) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        int32_t c = pl.blk_chain[b];
+        for (int32_t a = par[broot[b]]; a >= 0; a = par[a]) pl.chain[c++] = lab[a];
+        if (b == nb - 1) pl.blk_chain[nb] = c;
     }
 }
 
@@ -2033,7 +2193,6 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     FCG_TRY(dalloc(&p->leaf_weight, Np, p->bytes));
     FCG_TRY(dalloc(&p->link_ptr, Nn + 1, p->bytes));
     FCG_TRY(dalloc(&p->inv, Nn, p->bytes));
-    FCG_TRY(dalloc(&p->arrive, Nn, p->bytes));
     {
         // sweep plan arrays at their bounds (blocks <= leaves; a block's
         // heights <= its leaves - 1, its internal nodes = its leaves - 1)
@@ -2045,6 +2204,12 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_TRY(dalloc(&pl.blk_root, Np, p->bytes));
         FCG_TRY(dalloc(&pl.lvl_ptr, Np + 1, p->bytes));
         FCG_TRY(dalloc(&pl.lvl_nodes, Np + 1, p->bytes));
+        FCG_TRY(dalloc(&pl.lvl_kids, Np + 1, p->bytes));
+        FCG_TRY(dalloc(&pl.blk_chain, Np + 1, p->bytes));
+        FCG_TRY(dalloc(&pl.top_nodes, Np, p->bytes));
+        FCG_TRY(dalloc(&pl.top_kids, Np, p->bytes));
+        // heights of an accepted tree are below 2^16 and below Np
+        FCG_TRY(dalloc(&pl.top_hptr, std::min<int64_t>(Np, 1 << 16) + 2, p->bytes));
     }
     tr.mark("allocate");
     {
@@ -2061,13 +2226,17 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         // layout scratch
         int32_t *d_lab = NULL, *d_par = NULL, *d_height = NULL, *d_cnt = NULL, *seg_lo = NULL, *seg_hi = NULL, *hist = NULL;
         int32_t *bflag = NULL, *bid = NULL, *broot = NULL, *lvl_cnt = NULL, *node_cnt = NULL, *node_off = NULL;
+        int32_t *bdep = NULL, *ent_blk = NULL, *pos_of = NULL, *tflag = NULL, *tpos = NULL;
+        int *d_arrive = NULL;
         unsigned long long *ent = NULL, *ent2 = NULL;
         int64_t *rowlen = NULL;
-        long long *sums = NULL, *scal = NULL;  // scal: [0] blocks, [1] plan levels, [2] nodes, [3] links, [4] spare
-        int *iscal = NULL;                     // [0] max height, [1] max depth above a block
-        unsigned *dbad = NULL;
-        unsigned hbad = 0;
+        // scal: [0] blocks, [1] plan levels, [2] block nodes, [3] top nodes, [4] spare, [5] chain entries
+        long long *sums = NULL, *scal = NULL;
+        int *iscal = NULL;  // [0] max height, [1] max depth above a block
+        unsigned *dbad = NULL;  // [0] link sources out of range, [1] leaves not labelled by their leaf index
+        unsigned hbad[2] = {0, 0};
         int hscal[2] = {0, 0};
+        long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         long long hblocks[1] = {0};
         int nsurf = a.cond_surf_ptr[a.n_conductors];
         int rr = FCG_NORMAL_END;
@@ -2103,7 +2272,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_AL(ent2, Nn);
         FCG_AL(rowlen, Nn);
         FCG_AL(sums, devscan::grid_tiles(std::max<int64_t>(Nn, ntile_max)) + 1);
-        FCG_AL(scal, 5);
+        FCG_AL(scal, 8);
         FCG_AL(iscal, 2);
         FCG_AL(bflag, Np + 1);
         FCG_AL(bid, Np + 1);
@@ -2111,7 +2280,13 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_AL(lvl_cnt, Np + 1);
         FCG_AL(node_cnt, Np + 1);
         FCG_AL(node_off, Np + 1);
-        FCG_AL(dbad, 1);
+        FCG_AL(dbad, 2);
+        FCG_AL(bdep, Np + 1);
+        FCG_AL(ent_blk, Np + 1);
+        FCG_AL(pos_of, Nn);
+        FCG_AL(tflag, Nn);
+        FCG_AL(tpos, Nn);
+        FCG_AL(d_arrive, Nn);
 #undef FCG_UP
 #undef FCG_AL
         if (rr == FCG_NORMAL_END) rr = dalloc(&p->link_src, L, p->bytes);
@@ -2121,13 +2296,13 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             int gN = grid_for(Nn, 256, sms);
             cudaMemsetAsync(d_par, 0xff, Nn * sizeof(int32_t), s);     // roots: -1
             cudaMemsetAsync(p->parent, 0xff, Nn * sizeof(int32_t), s);
-            cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s);
+            cudaMemsetAsync(d_arrive, 0, Nn * sizeof(int), s);
             cudaMemsetAsync(iscal, 0, 2 * sizeof(int), s);
-            cudaMemsetAsync(dbad, 0, sizeof(unsigned), s);
+            cudaMemsetAsync(scal, 0, 8 * sizeof(long long), s);
+            cudaMemsetAsync(dbad, 0, 2 * sizeof(unsigned), s);
             cudaMemsetAsync(bflag, 0, (Np + 1) * sizeof(int32_t), s);
             k_model_parents<<<gN, 256, 0, s>>>(Nn, d_type, d_left, d_right, d_par);
-            k_heights<<<gN, 256, 0, s>>>(Nn, d_type, d_left, d_right, d_par, d_height, d_cnt, p->arrive, iscal);
-            cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s);  // zero again for the up-sweep
+            k_heights<<<gN, 256, 0, s>>>(Nn, d_type, d_left, d_right, d_par, d_height, d_cnt, d_arrive, iscal);
             // labels: stable sort of the nodes by height (two 8-bit passes)
             k_height_entries<<<gN, 256, 0, s>>>(Nn, d_height, ent);
             {
@@ -2160,7 +2335,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             // sweep plan: blocks numbered in leaf order, their levels
             k_block_flags<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_lf, bflag);
             exclusive_scan(s, Np, bflag, bid, sums, scal + 0);
-            k_blocks<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_height, d_lf, d_lab, bid, p->plan, broot, lvl_cnt, node_cnt,
+            k_blocks<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_height, d_lf, d_lab, bid, p->plan, broot, lvl_cnt, node_cnt, bdep,
                                         iscal + 1);
             p->timings.launches += 12 + (L > 0 ? 1 : 0);
             if (cudaGetLastError() != cudaSuccess ||
@@ -2174,28 +2349,55 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                 exclusive_scan(s, nb, lvl_cnt, p->plan.blk_lvl_first, sums, scal + 1);
                 exclusive_scan(s, nb, node_cnt, node_off, sums, scal + 2);
                 k_block_levels<<<grid_for(nb, 128, sms), 128, 0, s>>>(nb, broot, d_cnt, d_height, p->inv, seg_lo, seg_hi, node_off,
-                                                                      p->plan);
-                p->timings.launches += 7;
+                                                                      p->plan, ent_blk, pos_of);
+                k_block_kids<<<grid_for(Np, 256, sms), 256, 0, s>>>(scal + 2, p->plan, ent_blk, pos_of, p->inv, d_lab, d_type, d_left,
+                                                                    d_right, d_lf);
+                exclusive_scan(s, nb, bdep, p->plan.blk_chain, sums, scal + 5);
+                // top nodes by height, their children as top-local indices
+                k_top_flags<<<gN, 256, 0, s>>>(Nn, Np, p->inv, d_cnt, p->leaf_node, tflag, dbad + 1);
+                exclusive_scan(s, Nn, tflag, tpos, sums, scal + 3);
+                k_top_list<<<gN, 256, 0, s>>>(Nn, p->inv, d_lab, d_cnt, d_left, d_right, d_lf, bid, tpos, scal + 0, p->plan);
+                k_top_hptr<<<grid_for(std::min<int64_t>(Np, kMaxHeights) + 2, 256, sms), 256, 0, s>>>(
+                    iscal + 0, (int)std::min<int64_t>(Np, kMaxHeights) - 1, seg_lo, tpos, scal + 3, p->plan.top_hptr);
+                p->timings.launches += 18;
             }
             if (rr == FCG_NORMAL_END &&
                 (cudaGetLastError() != cudaSuccess ||
-                 cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                 cudaMemcpyAsync(hbad, dbad, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hscal, iscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                 cudaMemcpyAsync(hs, scal, 8 * sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaStreamSynchronize(s) != cudaSuccess)) {
                 set_error("building the device model failed");
                 rr = FCG_DEVICE_ERROR;
             }
             if (rr == FCG_NORMAL_END) {
                 p->plan.n_blocks = nb;
-                if (hbad) {
-                    set_error("invalid model: " + std::to_string(hbad) + " link sources out of range");
+                if (hbad[0]) {
+                    set_error("invalid model: " + std::to_string(hbad[0]) + " link sources out of range");
                     rr = FCG_GENERIC_ERROR;
-                } else if (hscal[0] >= kMaxHeights) {
+                } else if (hscal[0] >= kMaxHeights || hscal[0] >= Np) {
                     set_error("node tree too high (" + std::to_string(hscal[0]) + " levels)");
                     rr = FCG_GENERIC_ERROR;
-                } else if (hscal[1] > 96) {
-                    set_error("node tree too deep above its 256-leaf subtrees (" + std::to_string(hscal[1]) + " levels, at most 96)");
+                } else if (hscal[1] > kMaxChain) {
+                    set_error("node tree too deep above its 256-leaf subtrees (more than " + std::to_string(kMaxChain) + " levels)");
                     rr = FCG_GENERIC_ERROR;
+                } else if (hbad[1]) {
+                    set_error("invalid model: leaves are not in post-order leaf order");
+                    rr = FCG_GENERIC_ERROR;
+                }
+            }
+            if (rr == FCG_NORMAL_END && nb > 0) {
+                // the ancestor chains, now that their total is known
+                p->plan.n_top = (int)hs[3];
+                p->plan.n_top_levels = hscal[0] + 1;
+                rr = dalloc(&p->plan.chain, (size_t)std::max<long long>(hs[5], 1), p->bytes);
+                if (rr == FCG_NORMAL_END) {
+                    k_chains<<<grid_for(nb, 128, sms), 128, 0, s>>>(nb, broot, d_par, d_lab, p->plan);
+                    p->timings.launches++;
+                    if (cudaGetLastError() != cudaSuccess) {
+                        set_error("building the sweep plan failed");
+                        rr = FCG_DEVICE_ERROR;
+                    }
                 }
             }
         }
@@ -2205,6 +2407,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         dfree(d_lab); dfree(d_par); dfree(d_height); dfree(d_cnt); dfree(seg_lo); dfree(seg_hi); dfree(hist);
         dfree(ent); dfree(ent2); dfree(rowlen); dfree(sums); dfree(scal); dfree(iscal);
         dfree(bflag); dfree(bid); dfree(broot); dfree(lvl_cnt); dfree(node_cnt); dfree(node_off);
+        dfree(bdep); dfree(ent_blk); dfree(pos_of); dfree(tflag); dfree(tpos); dfree(d_arrive);
         if (rr != FCG_NORMAL_END) { problem_destroy(p); return rr; }
     }
     tr.mark("device model and layout");
@@ -2220,11 +2423,6 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         p->spmv_lanes = avg < 40.0 ? 8 : (avg < 160.0 ? 16 : 32);
         const char *env = getenv("FCG_SPMV_LANES");
         if (env && (atoi(env) == 8 || atoi(env) == 16 || atoi(env) == 32)) p->spmv_lanes = atoi(env);
-    }
-    if (cudaMemsetAsync(p->arrive, 0, Nn * sizeof(int), s) != cudaSuccess) {
-        set_error("cannot clear the arrival counters");
-        problem_destroy(p);
-        return FCG_DEVICE_ERROR;
     }
     // the uploads read host vectors that go out of scope: finish them here
     if (cudaStreamSynchronize(s) != cudaSuccess) {
@@ -2252,8 +2450,9 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->near_link); dfree(p->near_row); dfree(p->tri); dfree(p->tri32); dfree(p->fill_fp64);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
-    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(p->inv);
-    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->arrive); dfree(p->row_split);
+    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.lvl_kids); dfree(pl.blk_chain); dfree(pl.chain);
+    dfree(pl.top_nodes); dfree(pl.top_kids); dfree(pl.top_hptr); dfree(p->inv);
+    dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->row_split);
     free_solve_ws(p);
     dfree(p->partial);
     dfree(p->leaf_geom); dfree(p->ch_start); dfree(p->ch_len); dfree(p->ch_geom); dfree(p->g_ch_first); dfree(p->g_ch_count);
@@ -2289,7 +2488,8 @@ int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs
     int64_t steps = std::max(iterations, 32);
     int64_t vecs = ((steps + 1 + 15) / 16) * 16;
     int64_t b = 0;
-    b += Nn * (int64_t)(sizeof(NodeGeo) + 8 + 4 * 3 + 4 + 4 * 4);  // geometry, row pointers, tree, arrivals, sweep plan
+    b += Nn * (int64_t)(sizeof(NodeGeo) + 8 + 4 * 3 + 4);  // geometry, row pointers, tree, labels
+    b += Np * (int64_t)(4 * 7 + 4 + 12 + 4 + 8);          // sweep plan: blocks, levels, children, top forest, chains (typical)
     b += L * (4 + c);                                                  // links
     b += Np * (4 + 8 * 4 + 4);                                         // leaf maps, permittivities, self terms, geometry map
     b += L * 8 + Nn * (int64_t)(precision == FCG_PREC_FP64 ? sizeof(fcg_tri64) : sizeof(fcg_tri32));  // near list (bound) and tables
@@ -2593,18 +2793,39 @@ static void launch_link(DeviceProblem *p, const NodeWork &w, int kp, bool mixed)
 #undef FCG_SPMV
 }
 
-// The three launches of one product v = P * (in / diag): up-sweep, link
-// product, down-sweep. Arrays in/out are [k][Np] on the device.
+// The launches of one product v = P * (in / diag): up-sweep (blocks, then
+// the top forest when there is one), link product, down-sweep. Arrays in/out
+// are [k][Np] on the device.
 static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag) {
     cudaStream_t s = p->stream;
     bool mixed = p->precision == FCG_PREC_MIXED;
     const SweepPlan &pl = p->plan;
     int64_t Np = p->Np;
     size_t n = (size_t)p->Nn * kp;
-    if (mixed) k_up<true><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
-    else k_up<false><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, w.Qd, w.Qf, p->left, p->right, p->parent, p->arrive);
+    const int kc = std::min(k, kSweepCols);
+    const size_t up_smem = (size_t)(2 * kBlockLeaves - 1) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
+    const size_t down_smem = (size_t)(3 * kBlockLeaves - 1 + kMaxChain) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
+    if (mixed) k_up_blk<true><<<pl.n_blocks, kBlockLeaves, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
+    else k_up_blk<false><<<pl.n_blocks, kBlockLeaves, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
     FCG_CK(cudaGetLastError());
     int64_t launches = 2;
+    if (pl.n_top > 0) {
+        // the top forest in shared memory, as many right-hand sides per pass as fit
+        size_t fixed = (size_t)pl.n_top * (sizeof(int2) + sizeof(int32_t)) + (size_t)(pl.n_top_levels + 1) * sizeof(int32_t);
+        size_t per_col = (size_t)(pl.n_blocks + pl.n_top) * sizeof(double);
+        size_t room = p->ctx->smem_optin > fixed ? p->ctx->smem_optin - fixed : 0;
+        int tkc = (int)std::min<size_t>((size_t)k, room / per_col);
+        if (tkc >= 1) {
+            size_t top_smem = fixed + per_col * tkc;
+            if (mixed) k_up_top<true><<<1, 1024, top_smem, s>>>(pl, k, kp, tkc, w.Qd, w.Qf);
+            else k_up_top<false><<<1, 1024, top_smem, s>>>(pl, k, kp, tkc, w.Qd, w.Qf);
+        } else {
+            if (mixed) k_up_top_global<true><<<1, 1024, 0, s>>>(pl, k, kp, w.Qd, w.Qf);
+            else k_up_top_global<false><<<1, 1024, 0, s>>>(pl, k, kp, w.Qd, w.Qf);
+        }
+        FCG_CK(cudaGetLastError());
+        launches++;
+    }
     if (p->L > 0) {
         // coefficient + source word per link, row offsets, one charge read and
         // one potential write per node and right-hand side
@@ -2620,8 +2841,8 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
         if (mixed) FCG_CK(cudaMemsetAsync(w.Pf2, 0, n * sizeof(float2), s));
         else FCG_CK(cudaMemsetAsync(w.Pd, 0, n * sizeof(double), s));
     }
-    if (mixed) k_down<float2><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, w.Pf2, w.Ad, p->parent, out, p->status);
-    else k_down<double><<<pl.n_blocks, 256, 0, s>>>(pl, p->leaf_node, in, Np, k, kp, diag, p->self, w.Pd, w.Ad, p->parent, out, p->status);
+    if (mixed) k_down_blk<float2><<<pl.n_blocks, kBlockLeaves, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pf2, out);
+    else k_down_blk<double><<<pl.n_blocks, kBlockLeaves, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pd, out);
     FCG_CK(cudaGetLastError());
     p->timings.matvecs++;
     p->timings.launches += launches;
