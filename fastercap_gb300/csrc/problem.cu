@@ -47,6 +47,7 @@ namespace fcg {
 static const int kBlockLeaves = 256;  // leaves per sweep subtree
 static const int kMaxChain = 96;      // ancestors above a sweep subtree
 static const int kSweepCols = 4;      // right-hand sides per shared-memory pass of the sweeps
+static const int kSweepThreads = 128;  // threads per sweep CTA
 static const int kMaxK = 32;          // right-hand sides per matvec batch
 static const int kDotChunk = 1024;    // vector elements per CTA in the Krylov kernels
 static const int kPinSlots = 1024;    // pinned readback slots per context
@@ -123,6 +124,7 @@ struct SweepPlan {
     int n_blocks = 0;
     int n_top = 0, n_top_levels = 0;  // top nodes; heights 0..n_top_levels-1 (top_hptr has n_top_levels + 1 entries)
     int32_t *blk_leaf_first = NULL, *blk_nleaves = NULL, *blk_lvl_first = NULL, *blk_nlvls = NULL, *blk_root = NULL;
+    int32_t *blk_node_first = NULL;                 // first entry of the block's internal nodes in lvl_nodes
     int32_t *lvl_ptr = NULL, *lvl_nodes = NULL;
     uint32_t *lvl_kids = NULL;                      // per internal block node: left | right << 16 (local indices)
     int32_t *blk_chain = NULL, *chain = NULL;       // ancestors of every block root, parent first (device labels)
@@ -615,18 +617,19 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
 }
 
 // Up-sweep (CMultHier::ComputePanelCharges_fast, Solver/MultiplyHierarchical.cpp:72-127),
-// in two launches. k_up_blk: one CTA per block; the block's node list, its
-// children (local indices) and its level offsets are staged in shared
-// memory, the leaves read the (optionally Jacobi-scaled) input, and every
+// in two launches. k_up_blk: one CTA per block; the block's children lists
+// (local indices), node labels and level offsets are staged in shared memory
+// together with the (optionally Jacobi-scaled) leaf inputs, then every
 // internal node sums its two children level by level in shared memory
 // (left + right, in FP64), so a level costs a barrier, not a round trip to
 // memory. Node charges go to Qf (mixed) or Qd (FP64); the mixed path also
 // keeps the block root's FP64 charge for the top pass. Leaf j has device
-// label j. Right-hand sides are processed kc at a time.
+// label j. Right-hand sides are processed kc at a time; kSweepThreads
+// threads per CTA keep every block of a large model resident at once.
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlockLeaves) k_up_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld, int k,
-                                                         int kp, int kc, const double *__restrict__ diag, double *__restrict__ Qd,
-                                                         float *__restrict__ Qf) {
+__global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld,
+                                                              int k, int kp, int kc, const double *__restrict__ diag,
+                                                              double *__restrict__ Qd, float *__restrict__ Qf) {
     extern __shared__ double sh[];
     double *val = sh;                                                 // (2 kBlockLeaves - 1) x kc
     uint32_t *kids = (uint32_t *)(sh + (2 * kBlockLeaves - 1) * kc);  // kBlockLeaves
@@ -634,7 +637,7 @@ __global__ void __launch_bounds__(kBlockLeaves) k_up_blk(const SweepPlan plan, c
     int32_t *lp = lbl + kBlockLeaves;                                 // kBlockLeaves + 1
     const int b = blockIdx.x, tid = threadIdx.x;
     const int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b], lv0 = plan.blk_lvl_first[b], H = plan.blk_nlvls[b];
-    const int base = plan.lvl_ptr[lv0], ni = nl - 1;
+    const int base = plan.blk_node_first[b], ni = nl - 1;
     for (int t = tid; t < ni; t += blockDim.x) {
         kids[t] = plan.lvl_kids[base + t];
         lbl[t] = plan.lvl_nodes[base + t];
@@ -738,47 +741,52 @@ __device__ __forceinline__ double pval(const float2 *P, int64_t i) {
 
 // Down-sweep (CMultHier::ComputeLeafPotentials_fast, Solver/MultiplyHierarchical.cpp:231-283):
 // A(n) = P(n) + A(parent(n)) from the top. One CTA per block: the link
-// potentials of the block's nodes and of its root's ancestors are staged in
-// shared memory, the ancestors are summed top down (the reference's order),
-// then every internal node, level by level from the root, adds its A to its
-// internal children's P (which makes their A) or hands it to its leaf
-// children, and every leaf writes v = (self * x + P(leaf)) + A(parent(leaf)).
+// potentials of the block's nodes and of its root's ancestors, the leaves'
+// scaled inputs and self terms are staged in shared memory (each thread
+// fetches a node's label and then its potential, so the staging is two
+// dependent rounds of loads), the ancestors are summed top down (the
+// reference's order), then every internal node, level by level from the
+// root, adds its A to its internal children's P (which makes their A) or
+// hands it to its leaf children, and every leaf writes
+// v = (self * x + P(leaf)) + A(parent(leaf)).
 template <class TP>
-__global__ void __launch_bounds__(kBlockLeaves) k_down_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld, int k,
-                                                           int kp, int kc, const double *__restrict__ diag,
-                                                           const double *__restrict__ self, const TP *__restrict__ P,
-                                                           double *__restrict__ out) {
+__global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld,
+                                                                int k, int kp, int kc, const double *__restrict__ diag,
+                                                                const double *__restrict__ self, const TP *__restrict__ P,
+                                                                double *__restrict__ out) {
     extern __shared__ double sh[];
-    double *pv = sh;                                           // (2 kBlockLeaves - 1) x kc: P, then A of internal nodes
-    double *al = pv + (2 * kBlockLeaves - 1) * kc;             // kBlockLeaves x kc: A of each leaf's parent
-    double *cp = al + kBlockLeaves * kc;                       // kMaxChain x kc: P of the root's ancestors
-    uint32_t *kids = (uint32_t *)(cp + kMaxChain * kc);        // kBlockLeaves
-    int32_t *lbl = (int32_t *)(kids + kBlockLeaves);           // kBlockLeaves
-    int32_t *lp = lbl + kBlockLeaves;                          // kBlockLeaves + 1
+    double *pv = sh;                                     // (2 kBlockLeaves - 1) x kc: P, then A of internal nodes
+    double *al = pv + (2 * kBlockLeaves - 1) * kc;       // kBlockLeaves x kc: A of each leaf's parent
+    double *cp = al + kBlockLeaves * kc;                 // kMaxChain x kc: P of the root's ancestors
+    double *xs = cp + kMaxChain * kc;                    // kBlockLeaves x kc: scaled leaf inputs
+    double *ss = xs + kBlockLeaves * kc;                 // kBlockLeaves: leaf self terms
+    uint32_t *kids = (uint32_t *)(ss + kBlockLeaves);    // kBlockLeaves
+    int32_t *lp = (int32_t *)(kids + kBlockLeaves);      // kBlockLeaves + 1
     const int b = blockIdx.x, tid = threadIdx.x;
     const int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b], lv0 = plan.blk_lvl_first[b], H = plan.blk_nlvls[b];
-    const int base = plan.lvl_ptr[lv0], ni = nl - 1;
+    const int base = plan.blk_node_first[b], ni = nl - 1;
     const int ch0 = plan.blk_chain[b], nc = plan.blk_chain[b + 1] - ch0;
-    for (int t = tid; t < ni; t += blockDim.x) {
-        kids[t] = plan.lvl_kids[base + t];
-        lbl[t] = plan.lvl_nodes[base + t];
-    }
     for (int t = tid; t <= H; t += blockDim.x) lp[t] = plan.lvl_ptr[lv0 + t] - base;
-    __syncthreads();
+    for (int t = tid; t < nl; t += blockDim.x) ss[t] = self[lf + t];
     const bool hasA = ni > 0 || nc > 0;
     for (int c0 = 0; c0 < k; c0 += kc) {
         const int kk = min(kc, k - c0);
+        for (int t = tid; t < ni; t += blockDim.x) {
+            if (c0 == 0) kids[t] = plan.lvl_kids[base + t];
+            int64_t o = (int64_t)plan.lvl_nodes[base + t] * kp + c0;
+            for (int r = 0; r < kk; r++) pv[(nl + t) * kc + r] = pval(P, o + r);
+        }
+        for (int t = tid; t < nc; t += blockDim.x) {
+            int64_t o = (int64_t)plan.chain[ch0 + t] * kp + c0;
+            for (int r = 0; r < kk; r++) cp[t * kc + r] = pval(P, o + r);
+        }
         for (int t = tid; t < nl * kk; t += blockDim.x) {
             int r = t / nl, i = t - r * nl;
-            pv[i * kc + r] = pval(P, (int64_t)(lf + i) * kp + c0 + r);
-        }
-        for (int t = tid; t < ni * kk; t += blockDim.x) {
-            int r = t / ni, q = t - r * ni;
-            pv[(nl + q) * kc + r] = pval(P, (int64_t)lbl[q] * kp + c0 + r);
-        }
-        for (int t = tid; t < nc * kk; t += blockDim.x) {
-            int r = t / nc, j = t - r * nc;
-            cp[j * kc + r] = pval(P, (int64_t)plan.chain[ch0 + j] * kp + c0 + r);
+            int j = lf + i;
+            pv[i * kc + r] = pval(P, (int64_t)j * kp + c0 + r);
+            double xv = in[(int64_t)(c0 + r) * ld + j];
+            if (diag) xv = xv / diag[j];
+            xs[i * kc + r] = xv;
         }
         __syncthreads();
         if (tid < kk && nc > 0) {
@@ -804,12 +812,9 @@ __global__ void __launch_bounds__(kBlockLeaves) k_down_blk(const SweepPlan plan,
         }
         for (int t = tid; t < nl * kk; t += blockDim.x) {
             int r = t / nl, i = t - r * nl;
-            int j = lf + i;
-            double xv = in[(int64_t)(c0 + r) * ld + j];
-            if (diag) xv = xv / diag[j];
-            double v = self[j] * xv + pv[i * kc + r];
+            double v = ss[i] * xs[i * kc + r] + pv[i * kc + r];
             if (hasA) v = v + al[i * kc + r];
-            out[(int64_t)(c0 + r) * ld + j] = v;
+            out[(int64_t)(c0 + r) * ld + lf + i] = v;
         }
         __syncthreads();  // the next pass reuses the shared arrays
     }
@@ -2000,6 +2005,7 @@ __global__ void k_block_levels(int nb, const int32_t *__restrict__ broot, const 
         int32_t first = i - (2 * cnt[i] - 1) + 1;
         int H = height[i];
         int32_t off = node_off[b];
+        pl.blk_node_first[b] = off;
         int32_t *lp = pl.lvl_ptr + pl.blk_lvl_first[b];
         for (int h = 1; h <= H; h++) {
             int32_t lo = seg_lo[h], hi = seg_hi[h];
@@ -2205,6 +2211,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_TRY(dalloc(&pl.lvl_ptr, Np + 1, p->bytes));
         FCG_TRY(dalloc(&pl.lvl_nodes, Np + 1, p->bytes));
         FCG_TRY(dalloc(&pl.lvl_kids, Np + 1, p->bytes));
+        FCG_TRY(dalloc(&pl.blk_node_first, Np, p->bytes));
         FCG_TRY(dalloc(&pl.blk_chain, Np + 1, p->bytes));
         FCG_TRY(dalloc(&pl.top_nodes, Np, p->bytes));
         FCG_TRY(dalloc(&pl.top_kids, Np, p->bytes));
@@ -2450,7 +2457,7 @@ void problem_destroy(DeviceProblem *p) {
     dfree(p->near_link); dfree(p->near_row); dfree(p->tri); dfree(p->tri32); dfree(p->fill_fp64);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
-    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.lvl_kids); dfree(pl.blk_chain); dfree(pl.chain);
+    dfree(pl.lvl_ptr); dfree(pl.lvl_nodes); dfree(pl.lvl_kids); dfree(pl.blk_node_first); dfree(pl.blk_chain); dfree(pl.chain);
     dfree(pl.top_nodes); dfree(pl.top_kids); dfree(pl.top_hptr); dfree(p->inv);
     dfree(p->Qd); dfree(p->Pd); dfree(p->Ad); dfree(p->Qf); dfree(p->Pf2); dfree(p->row_split);
     free_solve_ws(p);
@@ -2804,9 +2811,10 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     size_t n = (size_t)p->Nn * kp;
     const int kc = std::min(k, kSweepCols);
     const size_t up_smem = (size_t)(2 * kBlockLeaves - 1) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
-    const size_t down_smem = (size_t)(3 * kBlockLeaves - 1 + kMaxChain) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
-    if (mixed) k_up_blk<true><<<pl.n_blocks, kBlockLeaves, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
-    else k_up_blk<false><<<pl.n_blocks, kBlockLeaves, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
+    const size_t down_smem = ((size_t)(4 * kBlockLeaves - 1 + kMaxChain) * kc + kBlockLeaves) * sizeof(double) +
+                             (2 * kBlockLeaves + 1) * sizeof(int32_t);
+    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
+    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
     FCG_CK(cudaGetLastError());
     int64_t launches = 2;
     if (pl.n_top > 0) {
@@ -2841,8 +2849,8 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
         if (mixed) FCG_CK(cudaMemsetAsync(w.Pf2, 0, n * sizeof(float2), s));
         else FCG_CK(cudaMemsetAsync(w.Pd, 0, n * sizeof(double), s));
     }
-    if (mixed) k_down_blk<float2><<<pl.n_blocks, kBlockLeaves, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pf2, out);
-    else k_down_blk<double><<<pl.n_blocks, kBlockLeaves, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pd, out);
+    if (mixed) k_down_blk<float2><<<pl.n_blocks, kSweepThreads, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pf2, out);
+    else k_down_blk<double><<<pl.n_blocks, kSweepThreads, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pd, out);
     FCG_CK(cudaGetLastError());
     p->timings.matvecs++;
     p->timings.launches += launches;
