@@ -231,36 +231,6 @@ struct DeviceProblem {
 
 // --------------------------------------------------------------- kernels
 
-// Distance band of every link, in FP64 exactly as the reference decides it
-// (CAutoRefine::PotEstimateOpt, Solver/Autorefine.cpp:3495-3505, 3561-3598),
-// stored in the top bits of the link's source word. Runs once per problem.
-// band of every link, packed into the source word; counts the near-field
-// (band 0) links into *n_near
-__global__ void k_classify(int64_t Nn, const int64_t *__restrict__ ptr, uint32_t *__restrict__ src,
-                           const NodeGeo *__restrict__ geo, unsigned long long *n_near) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned cnt = 0;
-    for (int64_t row = warp; row < Nn; row += nwarps) {
-        const float c1[3] = {geo[row].c[0], geo[row].c[1], geo[row].c[2]};
-        double ms1 = geo[row].maxside;
-        int64_t s = ptr[row], e = ptr[row + 1];
-        for (int64_t l = s + lane; l < e; l += 32) {
-            uint32_t j = src[l] & kSrcMask;
-            const NodeGeo &g2 = geo[j];
-            double ms2 = g2.maxside;
-            int band = fcg_band_exact(c1[0] - g2.c[0], c1[1] - g2.c[1], c1[2] - g2.c[2], ms1 > ms2 ? ms1 : ms2);
-            src[l] = j | ((uint32_t)band << kBandShift);
-            cnt += band == 0;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0 && cnt) atomicAdd(n_near, (unsigned long long)cnt);
-}
-
-// Move every model row to its device position (height-major label) and
-// relabel its sources; rows keep their links in order.
 // Device node arrays in height-major labels from the caller's post-order
 // arrays: geometry, children, parent, leaf map, first leaf of every node.
 __global__ void k_build_nodes(int64_t Nn, const int32_t *__restrict__ lab, const uint8_t *__restrict__ type,
@@ -321,24 +291,100 @@ __global__ void k_node_geom(int64_t Nn, const int64_t *__restrict__ node_lfirst,
         node_geom[v] = leaf_geom[node_lfirst[v]];
 }
 
-// also validates the caller's sources: an index outside [0, Nn) is counted
-// in *bad and stored as node 0
-__global__ void k_relabel_links(int64_t Nn, const int64_t *__restrict__ ptr_model, const uint32_t *__restrict__ src_model,
-                                const int32_t *__restrict__ lab, const int64_t *__restrict__ ptr_dev, uint32_t *__restrict__ src_dev,
-                                unsigned *bad) {
+// Move every model row to its device position (height-major label), relabel
+// its sources and classify each link's distance band once per problem
+// (fcg_band_exact: the FP64 decision of CAutoRefine::PotEstimateOpt,
+// Solver/Autorefine.cpp:3495-3505, 3561-3598, from an FP32 ratio where that is
+// certain), stored in the source word's top bits. Band-0 (near-field) links
+// are appended to the near list while it has room; *n_near counts them all.
+// The caller's sources are validated here: an index outside [0, Nn) is
+// counted in *bad and stored as node 0. One warp per model row; rows keep
+// their links in order.
+__global__ void k_relabel_classify(int64_t Nn, const int64_t *__restrict__ ptr_model, const uint32_t *__restrict__ src_model,
+                                   const int32_t *__restrict__ lab, const int64_t *__restrict__ ptr_dev,
+                                   const NodeGeo *__restrict__ geo, uint32_t *__restrict__ src_dev, unsigned *bad,
+                                   unsigned long long *n_near, int64_t cap, int32_t *__restrict__ near_link,
+                                   int32_t *__restrict__ near_row) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned nbad = 0;
     for (int64_t i = warp; i < Nn; i += nwarps) {
-        int64_t b0 = ptr_model[i], e0 = ptr_model[i + 1], o = ptr_dev[lab[i]] - b0;
-        for (int64_t l = b0 + lane; l < e0; l += 32) {
-            uint32_t j = src_model[l];  // a negative int32 reads as >= Nn
-            if (j >= (uint64_t)Nn) { nbad++; j = 0; }
-            src_dev[o + l] = (uint32_t)lab[j];
+        int32_t q = lab[i];
+        int64_t b0 = ptr_model[i], e0 = ptr_model[i + 1], o = ptr_dev[q] - b0;
+        const float c1[3] = {geo[q].c[0], geo[q].c[1], geo[q].c[2]};
+        double ms1 = geo[q].maxside;
+        for (int64_t base = b0; base < e0; base += 32) {
+            int64_t l = base + lane;
+            int band = -1;
+            if (l < e0) {
+                uint32_t j = src_model[l];  // a negative int32 reads as >= Nn
+                if (j >= (uint64_t)Nn) { nbad++; j = 0; }
+                uint32_t jq = (uint32_t)lab[j];
+                const NodeGeo &g2 = geo[jq];
+                double ms2 = g2.maxside;
+                band = fcg_band_exact(c1[0] - g2.c[0], c1[1] - g2.c[1], c1[2] - g2.c[2], ms1 > ms2 ? ms1 : ms2);
+                src_dev[o + l] = jq | ((uint32_t)band << kBandShift);
+            }
+            unsigned m = __ballot_sync(0xffffffffu, band == 0);
+            if (!m) continue;
+            unsigned long long at0 = 0;
+            if (lane == 0) at0 = atomicAdd(n_near, (unsigned long long)__popc(m));
+            at0 = __shfl_sync(0xffffffffu, at0, 0);
+            if (band == 0) {
+                int64_t at = (int64_t)at0 + __popc(m & ((1u << lane) - 1u));
+                if (at < cap) {
+                    near_link[at] = (int32_t)(o + l);
+                    near_row[at] = q;
+                }
+            }
         }
     }
     if (nbad) atomicAdd(bad, nbad);
+}
+
+// Structural checks of the caller's tree, run before any kernel indexes with
+// it (the per-node part of the host's model check, same rules): the lowest
+// failing node and its reason go to first[0] (node << 8 | code), the leaves
+// are counted in first[1].
+__global__ void k_check_model(int64_t Nn, int64_t Np, const uint8_t *__restrict__ type, const int32_t *__restrict__ left,
+                              const int32_t *__restrict__ right, const int64_t *__restrict__ lf, const int64_t *__restrict__ lc,
+                              const int64_t *__restrict__ ptr, unsigned long long *first) {
+    unsigned long long nleaf = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        int code = 0;
+        if (ptr[i + 1] < ptr[i]) {
+            code = 1;
+        } else if (type[i] & FCG_IS_LEAF) {
+            if (left[i] != -1 || right[i] != -1 || lc[i] != 1) code = 2;
+            nleaf++;
+        } else {
+            int32_t l = left[i], r = right[i];
+            if (l < 0 || r < 0 || l >= i || r >= i) code = 3;
+            else if (lc[i] != lc[l] + lc[r]) code = 4;
+            else if (lf[i] != lf[l] || lf[r] != lf[l] + lc[l]) code = 5;
+        }
+        if (!code && (lf[i] < 0 || lf[i] + lc[i] > Np)) code = 6;
+        if (code) atomicMin(&first[0], ((unsigned long long)i << 8) | (unsigned long long)code);
+    }
+    for (int o = 16; o > 0; o >>= 1) nleaf += __shfl_xor_sync(0xffffffffu, nleaf, o);
+    if ((threadIdx.x & 31) == 0 && nleaf) atomicAdd(&first[1], nleaf);
+}
+
+// every conductor leaf's permittivity index within its conductor's list (the
+// conductors tile the leaves, checked on the host); the lowest failing leaf
+// goes to *first
+__global__ void k_check_leaves(int64_t Np, int n_cond, const int64_t *__restrict__ cfirst, const uint8_t *__restrict__ is_diel,
+                               const int32_t *__restrict__ sptr, const uint8_t *__restrict__ leaf_diel, unsigned long long *first) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_cond - 1;  // last conductor whose first leaf is <= j
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (cfirst[mid] <= j) lo = mid;
+            else hi = mid - 1;
+        }
+        if (!is_diel[lo] && (int)leaf_diel[j] >= sptr[lo + 1] - sptr[lo]) atomicMin(first, (unsigned long long)j);
+    }
 }
 
 // counts tree edges and links whose two nodes lie in different geometries
@@ -1802,7 +1848,12 @@ template <class F> static void parallel_for(int64_t n, F fn) {
     for (auto &x : th) x.join();
 }
 
-static std::string validate(const fcg_model_arrays &a) {
+// The model checks without a pass over the nodes or leaves: sizes,
+// pointers, the ends of link_ptr, the conductors tiling the leaves and their
+// permittivities. problem_create runs the per-node and per-leaf checks on
+// the device (k_check_model, k_check_leaves) before any kernel indexes with
+// the caller's arrays.
+static std::string validate_host(const fcg_model_arrays &a) {
     if (a.n_nodes <= 0 || a.n_panels <= 0 || a.n_links < 0 || a.n_conductors <= 0) return "empty model";
     if (a.n_nodes > (int64_t)kSrcMask || a.n_links > 0x7fffffffLL) return "model too large (nodes must fit 29 bits, links 31 bits)";
     if (!a.node_type || !a.node_left || !a.node_right || !a.node_leaf_first || !a.node_leaf_count || !a.node_vertices ||
@@ -1811,59 +1862,75 @@ static std::string validate(const fcg_model_arrays &a) {
         !a.cond_surf_ptr || !a.cond_surf_outperm)
         return "null model array";
     if (a.link_ptr[0] != 0 || a.link_ptr[a.n_nodes] != a.n_links) return "link_ptr does not span the links";
-    // per-node checks on all host threads; the first failing node (lowest
-    // index) decides the message
-    std::atomic<int64_t> bad_at{INT64_MAX};
-    std::atomic<int64_t> leaves_all{0};
-    std::mutex mu;
-    const char *why = "";
-    parallel_for(a.n_nodes, [&](int64_t b, int64_t e) {
-        int64_t leaves = 0;
-        for (int64_t i = b; i < e; i++) {
-            const char *w = NULL;
-            if (a.link_ptr[i + 1] < a.link_ptr[i]) w = "link_ptr not monotone";
-            bool leaf = a.node_type[i] & FCG_IS_LEAF;
-            if (!w && leaf) {
-                if (a.node_left[i] != -1 || a.node_right[i] != -1 || a.node_leaf_count[i] != 1) w = "bad leaf node";
-                leaves++;
-            } else if (!w) {
-                int32_t l = a.node_left[i], r = a.node_right[i];
-                if (l < 0 || r < 0 || l >= i || r >= i) w = "children must precede their parent (post-order)";
-                else if (a.node_leaf_count[i] != a.node_leaf_count[l] + a.node_leaf_count[r]) w = "inconsistent leaf counts";
-                else if (a.node_leaf_first[i] != a.node_leaf_first[l] ||
-                         a.node_leaf_first[r] != a.node_leaf_first[l] + a.node_leaf_count[l])
-                    w = "leaf ranges are not contiguous";
-            }
-            if (!w && (a.node_leaf_first[i] < 0 || a.node_leaf_first[i] + a.node_leaf_count[i] > a.n_panels))
-                w = "leaf range out of bounds";
-            if (w) {
-                std::lock_guard<std::mutex> lk(mu);
-                if (i < bad_at.load()) { bad_at.store(i); why = w; }
-                return;
-            }
-        }
-        leaves_all += leaves;
-    });
-    if (bad_at.load() != INT64_MAX) return why;
-    int64_t leaves = leaves_all.load();
-    if (leaves != a.n_panels) return "leaf count does not match n_panels";
-    // link sources are range-checked on the device while they are relabelled
     int64_t next = 0;
     for (int32_t c = 0; c < a.n_conductors; c++) {
         if (a.cond_leaf_first[c] != next || a.cond_leaf_count[c] <= 0) return "conductor leaf ranges must tile the leaves";
         next += a.cond_leaf_count[c];
         if (a.cond_surf_ptr[c + 1] < a.cond_surf_ptr[c]) return "cond_surf_ptr not monotone";
-        if (!a.cond_is_diel[c]) {
-            int32_t ns = a.cond_surf_ptr[c + 1] - a.cond_surf_ptr[c];
-            for (int64_t j = a.cond_leaf_first[c]; j < a.cond_leaf_first[c] + a.cond_leaf_count[c]; j++)
-                if (a.leaf_diel[j] >= ns) return "leaf permittivity index out of range";
-        } else if (a.cond_outperm[c] == a.cond_inperm[c]) {
-            return "dielectric interface with equal permittivities";
-        }
+        if (a.cond_is_diel[c] && a.cond_outperm[c] == a.cond_inperm[c]) return "dielectric interface with equal permittivities";
     }
     if (next != a.n_panels) return "conductor leaf ranges must tile the leaves";
     return "";
 }
+
+static const char *node_check_message(int code) {
+    switch (code) {
+    case 1: return "link_ptr not monotone";
+    case 2: return "bad leaf node";
+    case 3: return "children must precede their parent (post-order)";
+    case 4: return "inconsistent leaf counts";
+    case 5: return "leaf ranges are not contiguous";
+    default: return "leaf range out of bounds";
+    }
+}
+
+// the full check on the host (no device work): validate_host, then every
+// node (on all host threads; the lowest failing node decides the message)
+// and every conductor leaf's permittivity index
+static std::string validate(const fcg_model_arrays &a) {
+    std::string hs = validate_host(a);
+    if (!hs.empty()) return hs;
+    std::atomic<int64_t> bad_at{INT64_MAX};
+    std::atomic<int64_t> leaves_all{0};
+    std::mutex mu;
+    int why = 0;
+    parallel_for(a.n_nodes, [&](int64_t b, int64_t e) {
+        int64_t leaves = 0;
+        for (int64_t i = b; i < e; i++) {
+            int code = 0;
+            if (a.link_ptr[i + 1] < a.link_ptr[i]) {
+                code = 1;
+            } else if (a.node_type[i] & FCG_IS_LEAF) {
+                if (a.node_left[i] != -1 || a.node_right[i] != -1 || a.node_leaf_count[i] != 1) code = 2;
+                leaves++;
+            } else {
+                int32_t l = a.node_left[i], r = a.node_right[i];
+                if (l < 0 || r < 0 || l >= i || r >= i) code = 3;
+                else if (a.node_leaf_count[i] != a.node_leaf_count[l] + a.node_leaf_count[r]) code = 4;
+                else if (a.node_leaf_first[i] != a.node_leaf_first[l] ||
+                         a.node_leaf_first[r] != a.node_leaf_first[l] + a.node_leaf_count[l])
+                    code = 5;
+            }
+            if (!code && (a.node_leaf_first[i] < 0 || a.node_leaf_first[i] + a.node_leaf_count[i] > a.n_panels)) code = 6;
+            if (code) {
+                std::lock_guard<std::mutex> lk(mu);
+                if (i < bad_at.load()) { bad_at.store(i); why = code; }
+                return;
+            }
+        }
+        leaves_all += leaves;
+    });
+    if (bad_at.load() != INT64_MAX) return node_check_message(why);
+    if (leaves_all.load() != a.n_panels) return "leaf count does not match n_panels";
+    for (int32_t c = 0; c < a.n_conductors; c++) {
+        if (a.cond_is_diel[c]) continue;
+        int32_t ns = a.cond_surf_ptr[c + 1] - a.cond_surf_ptr[c];
+        for (int64_t j = a.cond_leaf_first[c]; j < a.cond_leaf_first[c] + a.cond_leaf_count[c]; j++)
+            if (a.leaf_diel[j] >= ns) return "leaf permittivity index out of range";
+    }
+    return "";
+}
+
 
 // FCG_TRACE=1 prints the host phases of problem creation to stderr
 struct HostTrace {
@@ -2142,7 +2209,7 @@ std::string model_check(const fcg_model_arrays &a) { return validate(a); }
 int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision, void *stream, DeviceProblem **out) {
     *out = NULL;
     HostTrace tr;
-    std::string bad = validate(a);
+    std::string bad = validate_host(a);
     tr.mark("validate");
     if (!bad.empty()) { set_error("invalid model: " + bad); return FCG_GENERIC_ERROR; }
     if (precision != FCG_PREC_FP64 && precision != FCG_PREC_MIXED) { set_error("unknown precision"); return FCG_GENERIC_ERROR; }
@@ -2220,22 +2287,27 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     }
     tr.mark("allocate");
     {
-        // the caller's node, leaf and link arrays go to the device as they
-        // are; kernels build the device layout from them
+        // The caller's node, leaf and link arrays go to the device as they
+        // are; kernels check them and build the device layout. The arrays the
+        // structural checks read go first, then the checks (their result to a
+        // pinned word), then the geometry on the problem's stream and the
+        // link sources on a side stream, so the link upload overlaps the
+        // layout kernels; the host waits only for the checks before it
+        // launches anything that indexes with the caller's arrays.
         const int kMaxHeights = 1 << 16;  // heights sorted in two 8-bit passes
         int64_t tb = 0;
         int32_t *d_left = NULL, *d_right = NULL, *d_sptr = NULL;
         uint8_t *d_type = NULL, *d_cdiel = NULL, *d_ldiel = NULL;
         float *d_vert = NULL, *d_cent = NULL, *d_norm = NULL;
         double *d_area = NULL, *d_maxs = NULL, *d_out = NULL, *d_in = NULL, *d_surf = NULL;
-        int64_t *d_lf = NULL, *d_cf = NULL, *ptr_model = NULL;
+        int64_t *d_lf = NULL, *d_lc = NULL, *d_cf = NULL, *ptr_model = NULL;
         uint32_t *src_model = NULL;
         // layout scratch
         int32_t *d_lab = NULL, *d_par = NULL, *d_height = NULL, *d_cnt = NULL, *seg_lo = NULL, *seg_hi = NULL, *hist = NULL;
         int32_t *bflag = NULL, *bid = NULL, *broot = NULL, *lvl_cnt = NULL, *node_cnt = NULL, *node_off = NULL;
         int32_t *bdep = NULL, *ent_blk = NULL, *pos_of = NULL, *tflag = NULL, *tpos = NULL;
         int *d_arrive = NULL;
-        unsigned long long *ent = NULL, *ent2 = NULL;
+        unsigned long long *ent = NULL, *ent2 = NULL, *chk = NULL, *d_near = NULL;
         int64_t *rowlen = NULL;
         // scal: [0] blocks, [1] plan levels, [2] block nodes, [3] top nodes, [4] spare, [5] chain entries
         long long *sums = NULL, *scal = NULL;
@@ -2245,29 +2317,68 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         int hscal[2] = {0, 0};
         long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         long long hblocks[1] = {0};
+        unsigned long long hchk_local[4] = {0, 0, 0, 0}, hnear = 0;
+        // check results: [0] first bad node << 8 | code, [1] leaves, [2] first bad leaf
+        unsigned long long *hchk = p->pin ? (unsigned long long *)p->pin : hchk_local;
+        cudaStream_t s2 = NULL;
+        cudaEvent_t ev_alloc = NULL, ev_src = NULL;
         int nsurf = a.cond_surf_ptr[a.n_conductors];
         int rr = FCG_NORMAL_END;
         const int64_t ntile_max = devscan::grid_tiles(std::max<int64_t>(Nn, 1) * 1) * devscan::kDigits + 1;
+        const int64_t near_cap = L / 16 + 4096;  // near list room; a larger count takes a second pass
+        const int sms = ctx.sm_count;
+        const int gN = grid_for(Nn, 256, sms);
+        if (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_alloc, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_src, cudaEventDisableTiming) != cudaSuccess) {
+            set_error("cannot create the upload stream");
+            rr = FCG_DEVICE_ERROR;
+        }
 #define FCG_UP(ptr, host, n) if (rr == FCG_NORMAL_END) rr = upload(&ptr, host, n, tb, s)
 #define FCG_AL(ptr, n) if (rr == FCG_NORMAL_END) rr = dalloc(&ptr, (size_t)(n), tb)
+        // 1. what the checks read, and the checks
         FCG_UP(d_type, a.node_type, Nn);
+        FCG_UP(d_left, a.node_left, Nn);
+        FCG_UP(d_right, a.node_right, Nn);
+        FCG_UP(d_lf, a.node_leaf_first, Nn);
+        FCG_UP(d_lc, a.node_leaf_count, Nn);
+        FCG_UP(ptr_model, a.link_ptr, Nn + 1);
+        FCG_UP(d_cf, a.cond_leaf_first, a.n_conductors);
+        FCG_UP(d_cdiel, a.cond_is_diel, a.n_conductors);
+        FCG_UP(d_sptr, a.cond_surf_ptr, a.n_conductors + 1);
+        FCG_UP(d_ldiel, a.leaf_diel, Np);
+        FCG_AL(chk, 3);
+        if (rr == FCG_NORMAL_END) {
+            cudaMemsetAsync(chk, 0xff, 3 * sizeof(unsigned long long), s);
+            cudaMemsetAsync(chk + 1, 0, sizeof(unsigned long long), s);
+            k_check_model<<<gN, 256, 0, s>>>(Nn, Np, d_type, d_left, d_right, d_lf, d_lc, ptr_model, chk);
+            k_check_leaves<<<grid_for(Np, 256, sms), 256, 0, s>>>(Np, a.n_conductors, d_cf, d_cdiel, d_sptr, d_ldiel, chk + 2);
+            p->timings.launches += 2;
+            if (cudaGetLastError() != cudaSuccess ||
+                cudaMemcpyAsync(hchk, chk, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaEventRecord(p->ev1, s) != cudaSuccess) {
+                set_error("checking the model failed");
+                rr = FCG_DEVICE_ERROR;
+            }
+        }
+        // 2. the rest of the model: geometry on s, link sources on s2
         FCG_UP(d_vert, a.node_vertices, 9 * Nn);
         FCG_UP(d_cent, a.node_centroid, 3 * Nn);
         FCG_UP(d_norm, a.node_normal, 3 * Nn);
         FCG_UP(d_area, a.node_area, Nn);
         FCG_UP(d_maxs, a.node_maxside, Nn);
-        FCG_UP(d_left, a.node_left, Nn);
-        FCG_UP(d_right, a.node_right, Nn);
-        FCG_UP(d_lf, a.node_leaf_first, Nn);
-        FCG_UP(d_cf, a.cond_leaf_first, a.n_conductors);
-        FCG_UP(d_cdiel, a.cond_is_diel, a.n_conductors);
         FCG_UP(d_out, a.cond_outperm, a.n_conductors);
         FCG_UP(d_in, a.cond_inperm, a.n_conductors);
-        FCG_UP(d_sptr, a.cond_surf_ptr, a.n_conductors + 1);
         FCG_UP(d_surf, a.cond_surf_outperm, std::max(nsurf, 1));
-        FCG_UP(d_ldiel, a.leaf_diel, Np);
-        FCG_UP(src_model, (const uint32_t *)a.link_src, L);
-        FCG_UP(ptr_model, a.link_ptr, Nn + 1);
+        FCG_AL(src_model, L);
+        if (rr == FCG_NORMAL_END && L > 0) {
+            if (cudaEventRecord(ev_alloc, s) != cudaSuccess || cudaStreamWaitEvent(s2, ev_alloc, 0) != cudaSuccess ||
+                cudaMemcpyAsync(src_model, a.link_src, L * sizeof(uint32_t), cudaMemcpyHostToDevice, s2) != cudaSuccess ||
+                cudaEventRecord(ev_src, s2) != cudaSuccess) {
+                set_error("uploading the links failed");
+                rr = FCG_DEVICE_ERROR;
+            }
+        }
         FCG_AL(d_lab, Nn);
         FCG_AL(d_par, Nn);
         FCG_AL(d_height, Nn);
@@ -2294,13 +2405,32 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_AL(tflag, Nn);
         FCG_AL(tpos, Nn);
         FCG_AL(d_arrive, Nn);
+        FCG_AL(d_near, 1);
 #undef FCG_UP
 #undef FCG_AL
         if (rr == FCG_NORMAL_END) rr = dalloc(&p->link_src, L, p->bytes);
+        if (rr == FCG_NORMAL_END) rr = dalloc(&p->near_link, (size_t)near_cap, p->bytes);
+        if (rr == FCG_NORMAL_END) rr = dalloc(&p->near_row, (size_t)near_cap, p->bytes);
+        // 3. the checks' verdict before anything indexes with the arrays
+        if (rr == FCG_NORMAL_END) {
+            if (cudaEventSynchronize(p->ev1) != cudaSuccess) {
+                set_error("checking the model failed");
+                rr = FCG_DEVICE_ERROR;
+            } else if (hchk[0] != ~0ull) {
+                set_error(std::string("invalid model: ") + node_check_message((int)(hchk[0] & 255)));
+                rr = FCG_GENERIC_ERROR;
+            } else if ((int64_t)hchk[1] != Np) {
+                set_error("invalid model: leaf count does not match n_panels");
+                rr = FCG_GENERIC_ERROR;
+            } else if (hchk[2] != ~0ull) {
+                set_error("invalid model: leaf permittivity index out of range");
+                rr = FCG_GENERIC_ERROR;
+            }
+        }
+        tr.mark("uploads and checks");
         if (rr == FCG_NORMAL_END) {
             using namespace devscan;
-            int sms = ctx.sm_count;
-            int gN = grid_for(Nn, 256, sms);
+            cudaMemsetAsync(d_near, 0, sizeof(unsigned long long), s);
             cudaMemsetAsync(d_par, 0xff, Nn * sizeof(int32_t), s);     // roots: -1
             cudaMemsetAsync(p->parent, 0xff, Nn * sizeof(int32_t), s);
             cudaMemsetAsync(d_arrive, 0, Nn * sizeof(int), s);
@@ -2335,16 +2465,12 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                                              p->left, p->right, p->parent, p->leaf_node, p->node_lfirst);
             k_build_leaves<<<grid_for(Np, 256, sms), 256, 0, s>>>(Np, a.n_conductors, d_cf, d_cdiel, d_out, d_in, d_sptr, d_surf,
                                                                    d_ldiel, p->leaf_eb, p->leaf_ea, p->leaf_weight);
-            if (L > 0) {
-                int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
-                k_relabel_links<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, d_lab, p->link_ptr, p->link_src, dbad);
-            }
             // sweep plan: blocks numbered in leaf order, their levels
             k_block_flags<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_lf, bflag);
             exclusive_scan(s, Np, bflag, bid, sums, scal + 0);
             k_blocks<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_height, d_lf, d_lab, bid, p->plan, broot, lvl_cnt, node_cnt, bdep,
                                         iscal + 1);
-            p->timings.launches += 12 + (L > 0 ? 1 : 0);
+            p->timings.launches += 12;
             if (cudaGetLastError() != cudaSuccess ||
                 cudaMemcpyAsync(hblocks, scal, sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                 cudaStreamSynchronize(s) != cudaSuccess) {
@@ -2368,8 +2494,17 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                     iscal + 0, (int)std::min<int64_t>(Np, kMaxHeights) - 1, seg_lo, tpos, scal + 3, p->plan.top_hptr);
                 p->timings.launches += 18;
             }
+            // the links, once their upload is done (it overlapped everything above)
+            if (rr == FCG_NORMAL_END && L > 0) {
+                int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
+                cudaStreamWaitEvent(s, ev_src, 0);
+                k_relabel_classify<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, d_lab, p->link_ptr, p->geo, p->link_src, dbad, d_near,
+                                                        near_cap, p->near_link, p->near_row);
+                p->timings.launches++;
+            }
             if (rr == FCG_NORMAL_END &&
                 (cudaGetLastError() != cudaSuccess ||
+                 cudaMemcpyAsync(&hnear, d_near, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hbad, dbad, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hscal, iscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hs, scal, 8 * sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -2407,7 +2542,40 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                     }
                 }
             }
+            if (rr == FCG_NORMAL_END) {
+                // the near-field list: complete unless it overflowed its room
+                p->n_near = (int64_t)hnear;
+                if (p->n_near > near_cap) {
+                    dfree(p->near_link);
+                    dfree(p->near_row);
+                    rr = dalloc(&p->near_link, (size_t)p->n_near, p->bytes);
+                    if (rr == FCG_NORMAL_END) rr = dalloc(&p->near_row, (size_t)p->n_near, p->bytes);
+                    if (rr == FCG_NORMAL_END) {
+                        int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
+                        cudaMemsetAsync(d_near, 0, sizeof(unsigned long long), s);
+                        k_near_list<<<grid, 256, 0, s>>>(Nn, p->link_ptr, p->link_src, d_near, p->n_near, p->near_link, p->near_row);
+                        p->timings.launches++;
+                    }
+                }
+                // per-source triangle tables: the FP64 near field; the mixed
+                // near field and self terms
+                if (rr == FCG_NORMAL_END && precision == FCG_PREC_FP64 && p->n_near > 0) {
+                    rr = dalloc(&p->tri, Nn, p->bytes);
+                    if (rr == FCG_NORMAL_END) k_make_tri<<<grid_for(Nn, 128, sms), 128, 0, s>>>(Nn, p->geo, p->tri);
+                    p->timings.launches++;
+                }
+                if (rr == FCG_NORMAL_END && precision == FCG_PREC_MIXED) {
+                    rr = dalloc(&p->tri32, Nn, p->bytes);
+                    if (rr == FCG_NORMAL_END) k_make_tri32<<<grid_for(Nn, 128, sms), 128, 0, s>>>(Nn, p->geo, p->tri32);
+                    p->timings.launches++;
+                }
+                if (rr == FCG_NORMAL_END && cudaGetLastError() != cudaSuccess) {
+                    set_error("building the near-field list failed");
+                    rr = FCG_DEVICE_ERROR;
+                }
+            }
         }
+        if (s2) cudaStreamSynchronize(s2);  // the link upload reads the caller's array and writes src_model
         dfree(d_type); dfree(d_vert); dfree(d_cent); dfree(d_norm); dfree(d_area); dfree(d_maxs);
         dfree(d_left); dfree(d_right); dfree(d_lf); dfree(d_cf); dfree(d_cdiel); dfree(d_out); dfree(d_in);
         dfree(d_sptr); dfree(d_surf); dfree(d_ldiel); dfree(src_model); dfree(ptr_model); dfree(dbad);
@@ -2415,6 +2583,10 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         dfree(ent); dfree(ent2); dfree(rowlen); dfree(sums); dfree(scal); dfree(iscal);
         dfree(bflag); dfree(bid); dfree(broot); dfree(lvl_cnt); dfree(node_cnt); dfree(node_off);
         dfree(bdep); dfree(ent_blk); dfree(pos_of); dfree(tflag); dfree(tpos); dfree(d_arrive);
+        dfree(d_lc); dfree(chk); dfree(d_near);
+        if (ev_alloc) cudaEventDestroy(ev_alloc);
+        if (ev_src) cudaEventDestroy(ev_src);
+        if (s2) cudaStreamDestroy(s2);
         if (rr != FCG_NORMAL_END) { problem_destroy(p); return rr; }
     }
     tr.mark("device model and layout");
@@ -2573,60 +2745,10 @@ static int check_status(DeviceProblem *p, const char *what) {
     return FCG_NORMAL_END;
 }
 
-// Classify every link's distance band (stored with the source index) and
-// build the near-field link list once per problem: per-row counts, an
-// exclusive scan on the host, then an ordered per-row compaction.
-static int build_near_list(DeviceProblem *p) {
-    cudaStream_t s = p->stream;
-    int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
-    unsigned long long *ctr = NULL, hn[2] = {0, 0};
-    int64_t tmp = 0;
-    int r;
-    if ((r = dalloc(&ctr, 2, tmp))) return r;
-    cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), s);
-    k_classify<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, ctr);
-    p->timings.launches++;
-    if (cudaMemcpyAsync(hn, ctr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        set_error(std::string("link classification failed: ") + cudaGetErrorString(cudaGetLastError()));
-        dfree(ctr);
-        return FCG_DEVICE_ERROR;
-    }
-    int64_t n = (int64_t)hn[0];
-    if ((r = dalloc(&p->near_link, (size_t)std::max<int64_t>(n, 1), p->bytes)) ||
-        (r = dalloc(&p->near_row, (size_t)std::max<int64_t>(n, 1), p->bytes))) {
-        dfree(ctr);
-        return r;
-    }
-    if (n > 0) {
-        k_near_list<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, ctr + 1, n, p->near_link, p->near_row);
-        p->timings.launches++;
-        if (p->precision == FCG_PREC_FP64) {
-            if ((r = dalloc(&p->tri, p->Nn, p->bytes))) { dfree(ctr); return r; }
-            k_make_tri<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri);
-            p->timings.launches++;
-        }
-    }
-    if (p->precision == FCG_PREC_MIXED) {  // the self terms read the tables too
-        if ((r = dalloc(&p->tri32, p->Nn, p->bytes))) { dfree(ctr); return r; }
-        k_make_tri32<<<grid_for(p->Nn, 128, p->ctx->sm_count), 128, 0, s>>>(p->Nn, p->geo, p->tri32);
-        p->timings.launches++;
-    }
-    cudaError_t e = cudaGetLastError();
-    dfree(ctr);
-    if (e != cudaSuccess) { set_error(std::string("near-field list failed: ") + cudaGetErrorString(e)); return FCG_DEVICE_ERROR; }
-    p->n_near = n;
-    return FCG_NORMAL_END;
-}
-
 int problem_fill(DeviceProblem *p) {
     AllocScope alloc_scope(p->stream);
     FCG_CK(cudaSetDevice(p->ctx->device));
     cudaStream_t s = p->stream;
-    if (p->n_near < 0) {
-        int r = build_near_list(p);
-        if (r != FCG_NORMAL_END) return r;
-    }
     FCG_CK(cudaMemsetAsync(p->status, 0, sizeof(unsigned), s));
     FCG_CK(cudaMemsetAsync(p->fill_fp64, 0, sizeof(unsigned long long), s));
     FCG_CK(cudaEventRecord(p->ev0, s));
@@ -3023,16 +3145,18 @@ int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond)
         gch_count[g] = (int32_t)ch_start.size() - gch_first[g];
     }
     // every node and link must stay inside one geometry: a product that
-    // couples geometries would make the separate solves wrong
+    // couples geometries would make the separate solves wrong (nothing to
+    // check for a single geometry)
     cudaStream_t s = p->stream;
     int64_t tb = 0;
     int32_t *d_ng = NULL, *d_lg = NULL;
     unsigned *d_bad = NULL;
-    int r = upload(&d_lg, leaf_geom.data(), Np, tb, s);
-    if (r == FCG_NORMAL_END) r = dalloc(&d_ng, Nn, tb);
-    if (r == FCG_NORMAL_END) r = dalloc(&d_bad, 1, tb);
+    int r = FCG_NORMAL_END;
+    if (n > 1) r = upload(&d_lg, leaf_geom.data(), Np, tb, s);
+    if (n > 1 && r == FCG_NORMAL_END) r = dalloc(&d_ng, Nn, tb);
+    if (n > 1 && r == FCG_NORMAL_END) r = dalloc(&d_bad, 1, tb);
     unsigned bad = 0;
-    if (r == FCG_NORMAL_END) {
+    if (n > 1 && r == FCG_NORMAL_END) {
         cudaMemsetAsync(d_bad, 0, sizeof(unsigned), s);
         k_node_geom<<<grid_for(Nn, 256, p->ctx->sm_count), 256, 0, s>>>(Nn, p->node_lfirst, d_lg, d_ng);
         int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)p->ctx->sm_count * 32);
