@@ -291,56 +291,168 @@ __global__ void k_node_geom(int64_t Nn, const int64_t *__restrict__ node_lfirst,
         node_geom[v] = leaf_geom[node_lfirst[v]];
 }
 
-// Move every model row to its device position (height-major label), relabel
-// its sources and classify each link's distance band once per problem
+// Device label, centroid and largest side of a node (model order): all the
+// link relabelling and band classification read of a source, one 32-byte
+// sector per gather.
+struct __align__(32) CentMax {
+    float c[3];
+    int32_t lab;
+    double ms;
+    double pad;
+};
+
+__global__ void k_cent_max(int64_t Nn, const float *__restrict__ cent, const double *__restrict__ maxside,
+                           const int32_t *__restrict__ lab, CentMax *__restrict__ cm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        CentMax r;
+        r.c[0] = cent[3 * i];
+        r.c[1] = cent[3 * i + 1];
+        r.c[2] = cent[3 * i + 2];
+        r.lab = lab[i];
+        r.ms = maxside[i];
+        r.pad = 0.0;
+        cm[i] = r;
+    }
+}
+
+// Links are relabelled in tiles of kRelTile consecutive links (model
+// order); tile_row[t] is the row holding the tile's first link.
+constexpr int kRelTile = 1024;
+constexpr int kRelRows = 256;  // rows a tile keeps in shared memory
+
+__global__ void k_tile_rows(int64_t Nn, const int64_t *__restrict__ ptr_model, int32_t *__restrict__ tile_row) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t a = ptr_model[i], b = ptr_model[i + 1];
+        for (int64_t t = (a + kRelTile - 1) / kRelTile; t * kRelTile < b; t++) tile_row[t] = (int32_t)i;
+    }
+}
+
+// Move every link to its row's device position (height-major label),
+// relabel its source and classify its distance band once per problem
 // (fcg_band_exact: the FP64 decision of CAutoRefine::PotEstimateOpt,
 // Solver/Autorefine.cpp:3495-3505, 3561-3598, from an FP32 ratio where that is
-// certain), stored in the source word's top bits. Band-0 (near-field) links
-// are appended to the near list while it has room; *n_near counts them all.
-// The caller's sources are validated here: an index outside [0, Nn) is
-// counted in *bad and stored as node 0. One warp per model row; rows keep
-// their links in order.
-__global__ void k_relabel_classify(int64_t Nn, const int64_t *__restrict__ ptr_model, const uint32_t *__restrict__ src_model,
-                                   const int32_t *__restrict__ lab, const int64_t *__restrict__ ptr_dev,
-                                   const NodeGeo *__restrict__ geo, uint32_t *__restrict__ src_dev, unsigned *bad,
-                                   unsigned long long *n_near, int64_t cap, int32_t *__restrict__ near_link,
-                                   int32_t *__restrict__ near_row) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+// certain), stored in the source word's top bits; every row's band-0
+// (near-field) links are added to ncount (model order, zeroed by the
+// caller). The caller's sources are validated here: an index outside
+// [0, Nn) is counted in *bad and stored as node 0. A CTA takes tiles
+// [t0, t1) of kRelTile links: the rows a tile touches (their offsets,
+// device positions and geometry) are staged in shared memory, each thread
+// takes four links (coalesced) and finds its row there; a source's label and
+// geometry are one 32-byte gather by its model index.
+__global__ void __launch_bounds__(256, 5) k_relabel_classify(int64_t Nn, int64_t L, int64_t t0, int64_t t1,
+                                                          const int32_t *__restrict__ tile_row, const int64_t *__restrict__ ptr_model,
+                                                          const uint32_t *__restrict__ src_model, const int64_t *__restrict__ ptr_dev,
+                                                          const CentMax *__restrict__ cm, uint32_t *__restrict__ src_dev,
+                                                          unsigned *bad, int32_t *__restrict__ ncount) {
+    __shared__ int64_t s_ptr[kRelRows + 1];
+    __shared__ int64_t s_o[kRelRows];
+    __shared__ CentMax s_cm[kRelRows];
+    __shared__ int s_cnt[kRelRows];
+    const int tid = threadIdx.x;
+    const int64_t ntiles = (L + kRelTile - 1) / kRelTile;
     unsigned nbad = 0;
-    for (int64_t i = warp; i < Nn; i += nwarps) {
-        int32_t q = lab[i];
-        int64_t b0 = ptr_model[i], e0 = ptr_model[i + 1], o = ptr_dev[q] - b0;
-        const float c1[3] = {geo[q].c[0], geo[q].c[1], geo[q].c[2]};
-        double ms1 = geo[q].maxside;
-        for (int64_t base = b0; base < e0; base += 32) {
-            int64_t l = base + lane;
-            int band = -1;
-            if (l < e0) {
-                uint32_t j = src_model[l];  // a negative int32 reads as >= Nn
-                if (j >= (uint64_t)Nn) { nbad++; j = 0; }
-                uint32_t jq = (uint32_t)lab[j];
-                const NodeGeo &g2 = geo[jq];
-                double ms2 = g2.maxside;
-                band = fcg_band_exact(c1[0] - g2.c[0], c1[1] - g2.c[1], c1[2] - g2.c[2], ms1 > ms2 ? ms1 : ms2);
-                src_dev[o + l] = jq | ((uint32_t)band << kBandShift);
-            }
-            unsigned m = __ballot_sync(0xffffffffu, band == 0);
-            if (!m) continue;
-            unsigned long long at0 = 0;
-            if (lane == 0) at0 = atomicAdd(n_near, (unsigned long long)__popc(m));
-            at0 = __shfl_sync(0xffffffffu, at0, 0);
-            if (band == 0) {
-                int64_t at = (int64_t)at0 + __popc(m & ((1u << lane) - 1u));
-                if (at < cap) {
-                    near_link[at] = (int32_t)(o + l);
-                    near_row[at] = q;
+    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
+        const int64_t lo = t * kRelTile, hi = min(lo + kRelTile, L);
+        const int64_t rlo = tile_row[t], rhi = t + 1 < ntiles ? tile_row[t + 1] : Nn - 1;
+        const int nr = (int)(rhi - rlo + 1);
+        const bool small = nr <= kRelRows;
+        uint32_t j[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            int64_t l = lo + u * 256 + tid;
+            j[u] = l < hi ? src_model[l] : 0u;  // a negative int32 reads as >= Nn
+            if (l < hi && j[u] >= (uint64_t)Nn) { nbad++; j[u] = 0; }
+        }
+        if (small) {
+            for (int k = tid; k <= nr; k += blockDim.x) {
+                int64_t pk = ptr_model[rlo + k];
+                s_ptr[k] = pk;
+                if (k < nr) {
+                    CentMax d = cm[rlo + k];
+                    s_cm[k] = d;
+                    s_o[k] = ptr_dev[d.lab] - pk;
+                    s_cnt[k] = 0;
                 }
             }
         }
+        float4 g[4];  // centroid and label bits
+        double gms[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            g[u] = *reinterpret_cast<const float4 *>(&cm[j[u]]);
+            gms[u] = cm[j[u]].ms;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            int64_t l = lo + u * 256 + tid;
+            if (l >= hi) continue;
+            // the row holding link l: the last row whose first link is <= l
+            int64_t row, o;
+            CentMax d;
+            if (small) {
+                int a = 0, b = nr - 1;
+                while (a < b) {
+                    int m = (a + b + 1) >> 1;
+                    if (s_ptr[m] <= l) a = m;
+                    else b = m - 1;
+                }
+                row = a;
+                o = s_o[a];
+                d = s_cm[a];
+            } else {
+                int64_t a = rlo, b = rhi;
+                while (a < b) {
+                    int64_t m = (a + b + 1) >> 1;
+                    if (ptr_model[m] <= l) a = m;
+                    else b = m - 1;
+                }
+                row = a;
+                d = cm[a];
+                o = ptr_dev[d.lab] - ptr_model[a];
+            }
+            int band = fcg_band_exact(d.c[0] - g[u].x, d.c[1] - g[u].y, d.c[2] - g[u].z, d.ms > gms[u] ? d.ms : gms[u]);
+            src_dev[o + l] = __float_as_uint(g[u].w) | ((uint32_t)band << kBandShift);
+            if (band == 0) {
+                if (small) atomicAdd(&s_cnt[row], 1);
+                else atomicAdd(&ncount[row], 1);
+            }
+        }
+        __syncthreads();
+        if (small)
+            for (int k = tid; k < nr; k += blockDim.x)
+                if (s_cnt[k]) atomicAdd(&ncount[rlo + k], s_cnt[k]);
+        __syncthreads();  // the next tile reuses the shared arrays
     }
     if (nbad) atomicAdd(bad, nbad);
+}
+
+// The near-field list in row order: model row i's band-0 links go to
+// [noff[i], noff[i] + ncount[i]) (entries at or beyond cap are dropped; the
+// caller then makes room and runs it again). One warp per row.
+__global__ void k_near_fill(int64_t Nn, const int64_t *__restrict__ ptr_model, const int32_t *__restrict__ lab,
+                            const int64_t *__restrict__ ptr_dev, const uint32_t *__restrict__ src_dev,
+                            const int32_t *__restrict__ ncount, const long long *__restrict__ noff, int64_t cap,
+                            int32_t *__restrict__ near_link, int32_t *__restrict__ near_row) {
+    int lane = threadIdx.x & 31;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < Nn; i += nwarps) {
+        if (ncount[i] == 0) continue;
+        int32_t q = lab[i];
+        int64_t o = ptr_dev[q], len = ptr_model[i + 1] - ptr_model[i], at = noff[i];
+        for (int64_t t = 0; t < len; t += 32) {
+            int64_t l = t + lane;
+            bool nr = l < len && (src_dev[o + l] >> kBandShift) == 0;
+            unsigned m = __ballot_sync(0xffffffffu, nr);
+            int64_t pos = at + __popc(m & ((1u << lane) - 1u));
+            if (nr && pos < cap) {
+                near_link[pos] = (int32_t)(o + l);
+                near_row[pos] = q;
+            }
+            at += __popc(m);
+        }
+    }
 }
 
 // Structural checks of the caller's tree, run before any kernel indexes with
@@ -403,36 +515,6 @@ __global__ void k_check_geometries(int64_t Nn, const int64_t *__restrict__ link_
 }
 
 // count the near-field (band 0) links of every row
-
-// list the near-field links of every row at its offset, in link order
-// (link, row) of every near-field link; slots are reserved with a cursor, so
-// the list order varies between runs (each entry is computed on its own)
-__global__ void k_near_list(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                            unsigned long long *cursor, int64_t cap, int32_t *__restrict__ near_link,
-                            int32_t *__restrict__ near_row) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t row = warp; row < Nn; row += nwarps) {
-        int64_t s = ptr[row], e = ptr[row + 1];
-        for (int64_t base = s; base < e; base += 32) {
-            int64_t l = base + lane;
-            bool nr = l < e && (src[l] >> kBandShift) == 0;
-            unsigned m = __ballot_sync(0xffffffffu, nr);
-            if (!m) continue;
-            unsigned long long at0 = 0;
-            if (lane == 0) at0 = atomicAdd(cursor, (unsigned long long)__popc(m));
-            at0 = __shfl_sync(0xffffffffu, at0, 0);
-            if (nr) {
-                int64_t at = (int64_t)at0 + __popc(m & ((1u << lane) - 1u));
-                if (at < cap) {
-                    near_link[at] = (int32_t)l;
-                    near_row[at] = (int32_t)row;
-                }
-            }
-        }
-    }
-}
 
 // Links of bands 1..4 (quadrature and point formulas), FP64 path: the
 // reference's formulas, one warp per row.
@@ -1944,6 +2026,31 @@ struct HostTrace {
                 std::chrono::duration<double, std::milli>(n - t0).count());
         t = n;
     }
+    // device-side marks: an event recorded on a stream, reported (relative
+    // to the first mark) once the work has finished
+    std::vector<std::pair<const char *, cudaEvent_t>> ev;
+    void dmark(const char *what, cudaStream_t st) {
+        if (!on) return;
+        cudaEvent_t e = NULL;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, st);
+        ev.push_back({what, e});
+    }
+    void dreport() {
+        if (!on || ev.empty()) return;
+        cudaEventSynchronize(ev.back().second);
+        for (auto &m : ev) {
+            float ms = 0.f;
+            cudaEventSynchronize(m.second);
+            cudaEventElapsedTime(&ms, ev[0].second, m.second);
+            fprintf(stderr, "[fcg]   device %-24s at %8.3f ms\n", m.first, ms);
+        }
+        for (auto &m : ev) cudaEventDestroy(m.second);
+        ev.clear();
+    }
+    ~HostTrace() {
+        for (auto &m : ev) cudaEventDestroy(m.second);
+    }
 };
 
 // ---- device layout of a problem, from the caller's post-order arrays
@@ -2307,7 +2414,9 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         int32_t *bflag = NULL, *bid = NULL, *broot = NULL, *lvl_cnt = NULL, *node_cnt = NULL, *node_off = NULL;
         int32_t *bdep = NULL, *ent_blk = NULL, *pos_of = NULL, *tflag = NULL, *tpos = NULL;
         int *d_arrive = NULL;
-        unsigned long long *ent = NULL, *ent2 = NULL, *chk = NULL, *d_near = NULL;
+        unsigned long long *ent = NULL, *ent2 = NULL, *chk = NULL;
+        int32_t *ncount = NULL;                               // near links per model row
+        long long *noff = NULL, *sums3 = NULL, *d_near = NULL;  // their offsets, scan scratch of s3, total
         int64_t *rowlen = NULL;
         // scal: [0] blocks, [1] plan levels, [2] block nodes, [3] top nodes, [4] spare, [5] chain entries
         long long *sums = NULL, *scal = NULL;
@@ -2317,11 +2426,25 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         int hscal[2] = {0, 0};
         long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         long long hblocks[1] = {0};
-        unsigned long long hchk_local[4] = {0, 0, 0, 0}, hnear = 0;
+        unsigned long long hchk_local[4] = {0, 0, 0, 0};
+        long long hnear = 0;
         // check results: [0] first bad node << 8 | code, [1] leaves, [2] first bad leaf
         unsigned long long *hchk = p->pin ? (unsigned long long *)p->pin : hchk_local;
-        cudaStream_t s2 = NULL;
-        cudaEvent_t ev_alloc = NULL, ev_src = NULL;
+        CentMax *d_cm = NULL;
+        // link upload; link relabelling (at the device's highest priority: it
+        // is the critical path, the layout kernels on s fill in around it)
+        cudaStream_t s2 = NULL, s3 = NULL;
+        int prio_hi = 0;
+        cudaEvent_t ev_alloc = NULL, ev_lab = NULL, ev_rel = NULL;
+        // the link sources go up in chunks of whole relabelling tiles; each
+        // chunk's relabelling starts when its upload is done
+        const int kLinkChunks = 8;
+        const int64_t ntiles = (L + kRelTile - 1) / kRelTile;
+        int nchunk = L > 0 ? kLinkChunks : 0;
+        std::vector<int64_t> tbound(nchunk + 1, 0);
+        std::vector<cudaEvent_t> ev_src(nchunk, (cudaEvent_t)NULL);
+        for (int c = 1; c <= nchunk; c++) tbound[c] = ntiles * c / nchunk;
+        int32_t *tile_row = NULL;
         int nsurf = a.cond_surf_ptr[a.n_conductors];
         int rr = FCG_NORMAL_END;
         const int64_t ntile_max = devscan::grid_tiles(std::max<int64_t>(Nn, 1) * 1) * devscan::kDigits + 1;
@@ -2329,14 +2452,23 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         const int sms = ctx.sm_count;
         const int gN = grid_for(Nn, 256, sms);
         if (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaDeviceGetStreamPriorityRange(NULL, &prio_hi) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&s3, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_alloc, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&ev_src, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreateWithFlags(&ev_lab, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_rel, cudaEventDisableTiming) != cudaSuccess) {
             set_error("cannot create the upload stream");
             rr = FCG_DEVICE_ERROR;
         }
+        for (int c = 0; c < nchunk && rr == FCG_NORMAL_END; c++)
+            if (cudaEventCreateWithFlags(&ev_src[c], cudaEventDisableTiming) != cudaSuccess) {
+                set_error("cannot create the upload events");
+                rr = FCG_DEVICE_ERROR;
+            }
 #define FCG_UP(ptr, host, n) if (rr == FCG_NORMAL_END) rr = upload(&ptr, host, n, tb, s)
 #define FCG_AL(ptr, n) if (rr == FCG_NORMAL_END) rr = dalloc(&ptr, (size_t)(n), tb)
         // 1. what the checks read, and the checks
+        tr.dmark("start", s);
         FCG_UP(d_type, a.node_type, Nn);
         FCG_UP(d_left, a.node_left, Nn);
         FCG_UP(d_right, a.node_right, Nn);
@@ -2372,9 +2504,17 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_UP(d_surf, a.cond_surf_outperm, std::max(nsurf, 1));
         FCG_AL(src_model, L);
         if (rr == FCG_NORMAL_END && L > 0) {
-            if (cudaEventRecord(ev_alloc, s) != cudaSuccess || cudaStreamWaitEvent(s2, ev_alloc, 0) != cudaSuccess ||
-                cudaMemcpyAsync(src_model, a.link_src, L * sizeof(uint32_t), cudaMemcpyHostToDevice, s2) != cudaSuccess ||
-                cudaEventRecord(ev_src, s2) != cudaSuccess) {
+            bool ok = cudaEventRecord(ev_alloc, s) == cudaSuccess && cudaStreamWaitEvent(s2, ev_alloc, 0) == cudaSuccess;
+            for (int c = 0; c < nchunk && ok; c++) {
+                int64_t lo = tbound[c] * kRelTile, hi = std::min(tbound[c + 1] * kRelTile, L);
+                if (hi > lo)
+                    ok = cudaMemcpyAsync(src_model + lo, a.link_src + lo, (hi - lo) * sizeof(uint32_t), cudaMemcpyHostToDevice, s2) ==
+                         cudaSuccess;
+                ok = ok && cudaEventRecord(ev_src[c], s2) == cudaSuccess;
+                if (c == 0) tr.dmark("link chunk 0 uploaded", s2);
+            }
+            tr.dmark("links uploaded", s2);
+            if (!ok) {
                 set_error("uploading the links failed");
                 rr = FCG_DEVICE_ERROR;
             }
@@ -2406,6 +2546,11 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         FCG_AL(tpos, Nn);
         FCG_AL(d_arrive, Nn);
         FCG_AL(d_near, 1);
+        FCG_AL(d_cm, Nn);
+        FCG_AL(ncount, Nn);
+        FCG_AL(noff, Nn);
+        FCG_AL(sums3, devscan::grid_tiles(Nn) + 1);
+        FCG_AL(tile_row, std::max<int64_t>(ntiles, 1));
 #undef FCG_UP
 #undef FCG_AL
         if (rr == FCG_NORMAL_END) rr = dalloc(&p->link_src, L, p->bytes);
@@ -2428,9 +2573,10 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             }
         }
         tr.mark("uploads and checks");
+        tr.dmark("checks done (host sees)", s);
         if (rr == FCG_NORMAL_END) {
             using namespace devscan;
-            cudaMemsetAsync(d_near, 0, sizeof(unsigned long long), s);
+            cudaMemsetAsync(d_near, 0, sizeof(long long), s);
             cudaMemsetAsync(d_par, 0xff, Nn * sizeof(int32_t), s);     // roots: -1
             cudaMemsetAsync(p->parent, 0xff, Nn * sizeof(int32_t), s);
             cudaMemsetAsync(d_arrive, 0, Nn * sizeof(int), s);
@@ -2460,16 +2606,55 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             // row offsets in label order
             k_row_lengths<<<gN, 256, 0, s>>>(Nn, p->inv, ptr_model, rowlen);
             exclusive_scan(s, Nn, rowlen, p->link_ptr, sums, (long long *)(p->link_ptr + Nn));
+            // the links: relabelled and classified on s3, chunk by chunk as
+            // their upload completes, next to the rest of the layout on s
+            k_cent_max<<<gN, 256, 0, s>>>(Nn, d_cent, d_maxs, d_lab, d_cm);
+            p->timings.launches++;
+            cudaEventRecord(ev_lab, s);
+            cudaStreamWaitEvent(s3, ev_lab, 0);
+            if (L > 0) {
+                cudaMemsetAsync(ncount, 0, Nn * sizeof(int32_t), s3);
+                k_tile_rows<<<gN, 256, 0, s3>>>(Nn, ptr_model, tile_row);
+                p->timings.launches++;
+            }
+            for (int c = 0; c < nchunk; c++) {
+                int64_t nt = tbound[c + 1] - tbound[c];
+                cudaStreamWaitEvent(s3, ev_src[c], 0);
+                if (nt <= 0) continue;
+                int grid = (int)std::min<int64_t>(nt, (int64_t)sms * 5);
+                k_relabel_classify<<<grid, 256, 0, s3>>>(Nn, L, tbound[c], tbound[c + 1], tile_row, ptr_model, src_model, p->link_ptr,
+                                                         d_cm, p->link_src, dbad, ncount);
+                p->timings.launches++;
+                if (c == 0) tr.dmark("relabel chunk 0", s3);
+            }
+            if (L > 0) {
+                // the near-field list in row order
+                int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
+                exclusive_scan(s3, Nn, ncount, noff, sums3, d_near);
+                k_near_fill<<<grid, 256, 0, s3>>>(Nn, ptr_model, d_lab, p->link_ptr, p->link_src, ncount, noff, near_cap, p->near_link,
+                                                  p->near_row);
+                p->timings.launches += 4;
+            }
+            cudaEventRecord(ev_rel, s3);
+            tr.dmark("relabel done", s3);
             // the device model
             k_build_nodes<<<gN, 256, 0, s>>>(Nn, d_lab, d_type, d_vert, d_cent, d_norm, d_area, d_maxs, d_left, d_right, d_lf, p->geo,
                                              p->left, p->right, p->parent, p->leaf_node, p->node_lfirst);
             k_build_leaves<<<grid_for(Np, 256, sms), 256, 0, s>>>(Np, a.n_conductors, d_cf, d_cdiel, d_out, d_in, d_sptr, d_surf,
                                                                    d_ldiel, p->leaf_eb, p->leaf_ea, p->leaf_weight);
+            // scaled FP32 triangle tables of the mixed near field and self
+            // terms (while the links are still uploading)
+            if (precision == FCG_PREC_MIXED) {
+                rr = dalloc(&p->tri32, Nn, p->bytes);
+                if (rr == FCG_NORMAL_END) k_make_tri32<<<grid_for(Nn, 128, sms), 128, 0, s>>>(Nn, p->geo, p->tri32);
+                p->timings.launches++;
+            }
             // sweep plan: blocks numbered in leaf order, their levels
             k_block_flags<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_lf, bflag);
             exclusive_scan(s, Np, bflag, bid, sums, scal + 0);
             k_blocks<<<gN, 256, 0, s>>>(Nn, d_cnt, d_par, d_height, d_lf, d_lab, bid, p->plan, broot, lvl_cnt, node_cnt, bdep,
                                         iscal + 1);
+            tr.dmark("layout kernels", s);
             p->timings.launches += 12;
             if (cudaGetLastError() != cudaSuccess ||
                 cudaMemcpyAsync(hblocks, scal, sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -2494,17 +2679,11 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                     iscal + 0, (int)std::min<int64_t>(Np, kMaxHeights) - 1, seg_lo, tpos, scal + 3, p->plan.top_hptr);
                 p->timings.launches += 18;
             }
-            // the links, once their upload is done (it overlapped everything above)
-            if (rr == FCG_NORMAL_END && L > 0) {
-                int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
-                cudaStreamWaitEvent(s, ev_src, 0);
-                k_relabel_classify<<<grid, 256, 0, s>>>(Nn, ptr_model, src_model, d_lab, p->link_ptr, p->geo, p->link_src, dbad, d_near,
-                                                        near_cap, p->near_link, p->near_row);
-                p->timings.launches++;
-            }
+            tr.dmark("plan kernels", s);
+            cudaStreamWaitEvent(s, ev_rel, 0);  // the relabelled links
             if (rr == FCG_NORMAL_END &&
                 (cudaGetLastError() != cudaSuccess ||
-                 cudaMemcpyAsync(&hnear, d_near, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                 cudaMemcpyAsync(&hnear, d_near, sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hbad, dbad, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hscal, iscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                  cudaMemcpyAsync(hs, scal, 8 * sizeof(long long), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -2552,21 +2731,15 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                     if (rr == FCG_NORMAL_END) rr = dalloc(&p->near_row, (size_t)p->n_near, p->bytes);
                     if (rr == FCG_NORMAL_END) {
                         int grid = (int)std::min<int64_t>((Nn * 32 + 255) / 256, (int64_t)sms * 32);
-                        cudaMemsetAsync(d_near, 0, sizeof(unsigned long long), s);
-                        k_near_list<<<grid, 256, 0, s>>>(Nn, p->link_ptr, p->link_src, d_near, p->n_near, p->near_link, p->near_row);
+                        k_near_fill<<<grid, 256, 0, s>>>(Nn, ptr_model, d_lab, p->link_ptr, p->link_src, ncount, noff, p->n_near,
+                                                         p->near_link, p->near_row);
                         p->timings.launches++;
                     }
                 }
-                // per-source triangle tables: the FP64 near field; the mixed
-                // near field and self terms
+                // per-source FP64 triangle tables of the FP64 near field
                 if (rr == FCG_NORMAL_END && precision == FCG_PREC_FP64 && p->n_near > 0) {
                     rr = dalloc(&p->tri, Nn, p->bytes);
                     if (rr == FCG_NORMAL_END) k_make_tri<<<grid_for(Nn, 128, sms), 128, 0, s>>>(Nn, p->geo, p->tri);
-                    p->timings.launches++;
-                }
-                if (rr == FCG_NORMAL_END && precision == FCG_PREC_MIXED) {
-                    rr = dalloc(&p->tri32, Nn, p->bytes);
-                    if (rr == FCG_NORMAL_END) k_make_tri32<<<grid_for(Nn, 128, sms), 128, 0, s>>>(Nn, p->geo, p->tri32);
                     p->timings.launches++;
                 }
                 if (rr == FCG_NORMAL_END && cudaGetLastError() != cudaSuccess) {
@@ -2576,6 +2749,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             }
         }
         if (s2) cudaStreamSynchronize(s2);  // the link upload reads the caller's array and writes src_model
+        if (s3) cudaStreamSynchronize(s3);  // the relabelling reads the scratch freed below
         dfree(d_type); dfree(d_vert); dfree(d_cent); dfree(d_norm); dfree(d_area); dfree(d_maxs);
         dfree(d_left); dfree(d_right); dfree(d_lf); dfree(d_cf); dfree(d_cdiel); dfree(d_out); dfree(d_in);
         dfree(d_sptr); dfree(d_surf); dfree(d_ldiel); dfree(src_model); dfree(ptr_model); dfree(dbad);
@@ -2583,13 +2757,19 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         dfree(ent); dfree(ent2); dfree(rowlen); dfree(sums); dfree(scal); dfree(iscal);
         dfree(bflag); dfree(bid); dfree(broot); dfree(lvl_cnt); dfree(node_cnt); dfree(node_off);
         dfree(bdep); dfree(ent_blk); dfree(pos_of); dfree(tflag); dfree(tpos); dfree(d_arrive);
-        dfree(d_lc); dfree(chk); dfree(d_near);
+        dfree(d_lc); dfree(chk); dfree(d_near); dfree(ncount); dfree(noff); dfree(sums3); dfree(tile_row);
         if (ev_alloc) cudaEventDestroy(ev_alloc);
-        if (ev_src) cudaEventDestroy(ev_src);
+        if (ev_lab) cudaEventDestroy(ev_lab);
+        if (ev_rel) cudaEventDestroy(ev_rel);
+        if (s3) cudaStreamDestroy(s3);
+        dfree(d_cm);
+        for (cudaEvent_t e : ev_src)
+            if (e) cudaEventDestroy(e);
         if (s2) cudaStreamDestroy(s2);
         if (rr != FCG_NORMAL_END) { problem_destroy(p); return rr; }
     }
     tr.mark("device model and layout");
+    tr.dreport();
     FCG_TRY(dalloc(&p->self, Np, p->bytes));
     if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
@@ -3096,6 +3276,21 @@ int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k) {
 
 // ------------------------------------------------------------------ GMRES
 
+// the chunk lists of a single geometry: chunk c covers leaves
+// [c * kDotChunk, min((c + 1) * kDotChunk, Np))
+__global__ void k_single_geometry_chunks(int64_t Np, int64_t nch, int64_t *start, int32_t *len, int32_t *geom, int32_t *g_first,
+                                         int32_t *g_count) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nch; c += (int64_t)gridDim.x * blockDim.x) {
+        start[c] = c * kDotChunk;
+        len[c] = (int32_t)min((int64_t)kDotChunk, Np - c * kDotChunk);
+        geom[c] = 0;
+        if (c == 0) {
+            g_first[0] = 0;
+            g_count[0] = (int32_t)nch;
+        }
+    }
+}
+
 int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond) {
     AllocScope alloc_scope(p->stream);
     if (n < 1 || !geom_of_cond) { set_error("need at least one geometry"); return FCG_GENERIC_ERROR; }
@@ -3120,12 +3315,13 @@ int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond)
     FCG_CK(cudaSetDevice(p->ctx->device));
     int64_t Np = p->Np, Nn = p->Nn;
     std::vector<int64_t> gfirst(n, -1), gcount(n, 0);
-    std::vector<int32_t> leaf_geom(Np);
+    std::vector<int32_t> leaf_geom(n > 1 ? Np : 0);  // one geometry: all zero, set on the device
     for (int c = 0; c < nc; c++) {
         int g = geom_of_cond[c];
         if (gfirst[g] < 0) gfirst[g] = p->cond_first[c];
         gcount[g] += p->cond_count[c];
-        for (int64_t j = p->cond_first[c]; j < p->cond_first[c] + p->cond_count[c]; j++) leaf_geom[j] = g;
+        if (n > 1)
+            for (int64_t j = p->cond_first[c]; j < p->cond_first[c] + p->cond_count[c]; j++) leaf_geom[j] = g;
     }
     for (int g = 0; g < n; g++)
         if (gcount[g] == 0) { set_error("geometry " + std::to_string(g) + " has no panels"); return FCG_GENERIC_ERROR; }
@@ -3178,14 +3374,28 @@ int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond)
     }
     dfree(p->leaf_geom); dfree(p->ch_start); dfree(p->ch_len); dfree(p->ch_geom); dfree(p->g_ch_first); dfree(p->g_ch_count);
     p->n_geom = 0;
-    if ((r = upload(&p->leaf_geom, leaf_geom.data(), Np, p->bytes, s)) ||
-        (r = upload(&p->ch_start, ch_start.data(), ch_start.size(), p->bytes, s)) ||
-        (r = upload(&p->ch_len, ch_len.data(), ch_len.size(), p->bytes, s)) ||
-        (r = upload(&p->ch_geom, ch_geom.data(), ch_geom.size(), p->bytes, s)) ||
-        (r = upload(&p->g_ch_first, gch_first.data(), n, p->bytes, s)) ||
-        (r = upload(&p->g_ch_count, gch_count.data(), n, p->bytes, s)))
-        return r;
-    FCG_CK(cudaStreamSynchronize(s));
+    if (n == 1) {
+        // one geometry: the leaf map and the chunk lists are made on the
+        // device, so nothing here waits for the stream's earlier work
+        int64_t nc1 = (int64_t)ch_start.size();
+        if ((r = dalloc(&p->leaf_geom, Np, p->bytes)) || (r = dalloc(&p->ch_start, nc1, p->bytes)) ||
+            (r = dalloc(&p->ch_len, nc1, p->bytes)) || (r = dalloc(&p->ch_geom, nc1, p->bytes)) ||
+            (r = dalloc(&p->g_ch_first, 1, p->bytes)) || (r = dalloc(&p->g_ch_count, 1, p->bytes)))
+            return r;
+        FCG_CK(cudaMemsetAsync(p->leaf_geom, 0, Np * sizeof(int32_t), s));
+        k_single_geometry_chunks<<<grid_for(nc1, 256, p->ctx->sm_count), 256, 0, s>>>(Np, nc1, p->ch_start, p->ch_len, p->ch_geom,
+                                                                                    p->g_ch_first, p->g_ch_count);
+        FCG_CK(cudaGetLastError());
+    } else {
+        if ((r = upload(&p->leaf_geom, leaf_geom.data(), Np, p->bytes, s)) ||
+            (r = upload(&p->ch_start, ch_start.data(), ch_start.size(), p->bytes, s)) ||
+            (r = upload(&p->ch_len, ch_len.data(), ch_len.size(), p->bytes, s)) ||
+            (r = upload(&p->ch_geom, ch_geom.data(), ch_geom.size(), p->bytes, s)) ||
+            (r = upload(&p->g_ch_first, gch_first.data(), n, p->bytes, s)) ||
+            (r = upload(&p->g_ch_count, gch_count.data(), n, p->bytes, s)))
+            return r;
+        FCG_CK(cudaStreamSynchronize(s));
+    }
     p->n_geom = n;
     p->nch = (int)ch_start.size();
     p->geom_cols_ptr = cols_ptr;
@@ -3702,10 +3912,9 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL);
             FCG_CK(cudaGetLastError());
             p->timings.launches += 7;
-            // does any solve need an Arnoldi step?
+            // does any solve need an Arnoldi step? (read below, after the
+            // host has prepared the steps while the device works)
             FCG_CK(cudaMemcpyAsync(pin, p->n_active + M + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-            FCG_CK(cudaStreamSynchronize(s));
-            bool any = pin[0] > 0;
             FCG_CK(cudaMemsetAsync(p->d_it, 0, 4 * sizeof(int), s));
             if (pk == FCG_PRECOND_TWO_LEVEL && !p->ptmp && (r = dalloc(&p->ptmp, (size_t)k * Np, p->bytes))) {
                 status = r;
@@ -3719,6 +3928,17 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
                 break;
             }
             const bool use_graph = !p->profiling && getenv("FCG_NO_GRAPH") == NULL;
+            if (use_graph) {
+                // the first graph launch's basis and graph (a new problem
+                // captures and instantiates it here, overlapping the device)
+                sa.cap = std::min(M, 32);
+                if ((r = ensure_basis(p, sa.cap)) || (r = ensure_partial(p, (size_t)k * sa.cap * nch)) || (r = ensure_step_graph(p, sa))) {
+                    status = r;
+                    break;
+                }
+            }
+            FCG_CK(cudaStreamSynchronize(s));
+            bool any = pin[0] > 0;
             int steps = 0;  // Arnoldi steps taken
             while (any && status == FCG_NORMAL_END) {
                 if (use_graph) {
