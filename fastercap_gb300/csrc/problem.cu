@@ -754,10 +754,22 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
 // keeps the block root's FP64 charge for the top pass. Leaf j has device
 // label j. Right-hand sides are processed kc at a time; kSweepThreads
 // threads per CTA keep every block of a large model resident at once.
+// The Arnoldi step's pending normalisation, done by the up-sweep as it reads
+// the step's vector (k_scale's work): q = v / |v| for every active solve,
+// written back to v and to basis vector *iter; nothing at step 0, whose
+// vector is normalised before the loop.
+struct StepScale {
+    const double *hn;  // NULL: no normalisation
+    const int *active;
+    const int32_t *leaf_geom;
+    double *const *Vp;
+    const int *iter;
+};
+
 template <bool MIXED>
-__global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld,
-                                                              int k, int kp, int kc, const double *__restrict__ diag,
-                                                              double *__restrict__ Qd, float *__restrict__ Qf) {
+__global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan plan, const double *in, int64_t ld, int k, int kp,
+                                                              int kc, const double *__restrict__ diag, double *__restrict__ Qd,
+                                                              float *__restrict__ Qf, const StepScale sc) {
     extern __shared__ double sh[];
     double *val = sh;                                                 // (2 kBlockLeaves - 1) x kc
     uint32_t *kids = (uint32_t *)(sh + (2 * kBlockLeaves - 1) * kc);  // kBlockLeaves
@@ -771,11 +783,22 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
         lbl[t] = plan.lvl_nodes[base + t];
     }
     for (int t = tid; t <= H; t += blockDim.x) lp[t] = plan.lvl_ptr[lv0 + t] - base;
+    const int step = sc.hn ? *sc.iter : 0;
+    double *Vi = step > 0 ? sc.Vp[step] : NULL;
     for (int c0 = 0; c0 < k; c0 += kc) {
         const int kk = min(kc, k - c0);
         for (int t = tid; t < nl * kk; t += blockDim.x) {
             int r = t / nl, i = t - r * nl;
-            double x = in[(int64_t)(c0 + r) * ld + lf + i];
+            int64_t at = (int64_t)(c0 + r) * ld + lf + i;
+            double x = in[at];
+            if (Vi) {
+                int sidx = sc.leaf_geom[lf + i] * k + c0 + r;
+                if (sc.active[sidx]) {
+                    x = x / sc.hn[sidx];
+                    const_cast<double *>(in)[at] = x;
+                    Vi[at] = x;
+                }
+            }
             if (diag) x = x / diag[lf + i];
             val[i * kc + r] = x;
             int64_t o = (int64_t)(lf + i) * kp + c0 + r;
@@ -1477,13 +1500,22 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // partial[(r*nvec + j)*nch + c] = <Vj[r], w[r]> over chunk c; the chunk of w
 // stays in registers, basis vectors are taken eight at a time with one block
 // reduction per group of eight.
+__device__ __forceinline__ void reduce_h_warp(int64_t wid, int lane, int i, int ks, int nch, const double *partial,
+                                              const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
+                                              const int *__restrict__ active, double *const *__restrict__ Hp);
+
+// With fuse_h set, the last CTA to finish (a ticket on *done) also sums the
+// Hessenberg column (k_reduce_h's work) and resets *done.
 __global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
-                       SegChunks ch, int ks, const int *__restrict__ active, double *__restrict__ partial) {
+                       SegChunks ch, int ks, const int *__restrict__ active, double *__restrict__ partial, int fuse_h, int G,
+                       const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
+                       double *const *__restrict__ Hp, int *done) {
     __shared__ double sh[8][8];
+    __shared__ int s_last;
     const int T = 8;
     const int nvec = *iter + 1;
     int r = blockIdx.y, c = blockIdx.x;
-    if (!active[ch.geom[c] * ks + r]) return;
+    if (active[ch.geom[c] * ks + r]) {
     int64_t base = ch.start[c];
     int len = ch.len[c];
     double wv[kDotChunk / 256];
@@ -1542,6 +1574,19 @@ __global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *
         }
         __syncthreads();
     }
+    }
+    if (!fuse_h) return;
+    if (threadIdx.x == 0) {
+        __threadfence();  // this CTA's partial sums are visible before its ticket
+        s_last = atomicAdd(done, 1) == (int)(gridDim.x * gridDim.y) - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31;
+    for (int64_t wid = threadIdx.x >> 5; wid < (int64_t)nvec * ks * G; wid += blockDim.x >> 5)
+        reduce_h_warp(wid, lane, nvec - 1, ks, ch.n, partial, g_ch_first, g_ch_count, active, Hp);
+    if (threadIdx.x == 0) *done = 0;
 }
 
 // out[sidx*ostride_s + j*ostride_j] = sum of partial[(r*nvec + j)*nch + c]
@@ -1565,52 +1610,11 @@ __global__ void k_reduce_seg(int nvec, int ks, int G, int nch, const double *__r
     if (lane == 0) out[sidx * ostride_s + j * ostride_j] = sum;
 }
 
-// v[r] = w[r] - sum_j h_j V_j[r] with the solve's own h; partial |v|^2 per chunk
-__global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
-                         double *const *__restrict__ Hp, SegChunks ch, int ks, const int *__restrict__ active,
-                         double *__restrict__ v, double *__restrict__ partial) {
-    __shared__ double sh[32];
-    const int nvec = *iter + 1;
-    int r = blockIdx.y, c = blockIdx.x;
-    int sidx = ch.geom[c] * ks + r;
-    if (!active[sidx]) return;
-    const double *h = Hp[nvec - 1] + (int64_t)sidx * (nvec + 1);
-    int64_t base = ch.start[c];
-    int len = ch.len[c];
-    // four elements per thread, each its own subtraction chain (in basis
-    // order), so the loads of one vector for all four are in flight together
-    const int U = kDotChunk / 256;
-    double x[U];
-    int64_t t0 = (int64_t)r * Np + base + threadIdx.x;
-#pragma unroll
-    for (int u = 0; u < U; u++) x[u] = (threadIdx.x + u * 256 < len) ? w[t0 + u * 256] : 0.0;
-    for (int jv = 0; jv < nvec; jv++) {
-        const double hj = h[jv];
-        const double *vj = Vp[jv] + t0;
-#pragma unroll
-        for (int u = 0; u < U; u++)
-            if (threadIdx.x + u * 256 < len) x[u] = x[u] - hj * vj[u * 256];
-    }
-    double s2 = 0.0;
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-        if (threadIdx.x + u * 256 < len) {
-            v[t0 + u * 256] = x[u];
-            s2 += x[u] * x[u];
-        }
-    }
-    s2 = block_sum(s2, sh);
-    if (threadIdx.x == 0) partial[(int64_t)r * ch.n + c] = s2;
-}
-
-// Givens update of Hessenberg column i of every active solve (one thread each)
-__global__ void k_givens(int S, const int *__restrict__ iter, int M, double *const *__restrict__ Hp, double *cs, double *sn,
-                         double *g, const double *normb, const double *nrm2, double *hnorm, double tol, const int *scap, int *active,
-                         int *iters, int *capped, int *n_active_all) {
-    const int i = *iter;
-    int *n_active = n_active_all + i;
-    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sidx >= S || !active[sidx]) return;
+// Givens update of Hessenberg column i of active solve sidx; true while the
+// solve goes on
+__device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ Hp, double *cs, double *sn, double *g,
+                           const double *normb, const double *nrm2, double *hnorm, double tol, const int *scap, int *active,
+                           int *iters, int *capped) {
     double *hc = Hp[i] + (int64_t)sidx * (i + 2);
     double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2), *gg = g + (int64_t)sidx * (M + 2);
     double hn = sqrt(nrm2[sidx]);
@@ -1640,17 +1644,28 @@ __global__ void k_givens(int S, const int *__restrict__ iter, int M, double *con
         iters[sidx] = i;
         capped[sidx] = 1;
     } else {
-        atomicAdd(n_active, 1);
+        return true;
     }
+    return false;
+}
+
+// Givens update of Hessenberg column i of every active solve (one thread each)
+__global__ void k_givens(int S, const int *__restrict__ iter, int M, double *const *__restrict__ Hp, double *cs, double *sn,
+                         double *g, const double *normb, const double *nrm2, double *hnorm, double tol, const int *scap, int *active,
+                         int *iters, int *capped, int *n_active_all) {
+    const int i = *iter;
+    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sidx >= S || !active[sidx]) return;
+    if (givens_one(sidx, i, M, Hp, cs, sn, g, normb, nrm2, hnorm, tol, scap, active, iters, capped)) atomicAdd(n_active_all + i, 1);
 }
 
 // out[r][j] = v[r][j] / hn[solve of (j, r)] for active solves, out = out_fixed
-// or basis vector *iter + 1; v is rewritten with the same values (it is the
-// input of the next product)
+// or basis vector *iter + vofs; v is rewritten with the same values (it is
+// the input of the next product)
 __global__ void k_scale(int64_t Np, int ks, double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
                         const int32_t *__restrict__ leaf_geom, double *__restrict__ out_fixed, double *const *__restrict__ Vp,
-                        const int *__restrict__ iter) {
-    double *out = out_fixed ? out_fixed : Vp[*iter + 1];
+                        const int *__restrict__ iter, int vofs) {
+    double *out = out_fixed ? out_fixed : Vp[*iter + vofs];
     int64_t n = (int64_t)ks * Np;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int r = (int)(t / Np);
@@ -1665,26 +1680,43 @@ __global__ void k_scale(int64_t Np, int ks, double *__restrict__ v, const double
 
 // Hessenberg column *iter of every active solve: out = Hp[i] + sidx*(i+2) + j,
 // j < i+1, summed over the solve's geometry chunks (one warp per output)
+__device__ __forceinline__ void reduce_h_warp(int64_t wid, int lane, int i, int ks, int nch, const double *partial,
+                                              const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
+                                              const int *__restrict__ active, double *const *__restrict__ Hp) {
+    const int nvec = i + 1;
+    int j = (int)(wid % nvec);
+    int64_t rg = wid / nvec;
+    int r = (int)(rg % ks), g = (int)(rg / ks);
+    int sidx = g * ks + r;
+    if (!active[sidx]) return;
+    double sum = 0.0;
+    int c0 = g_ch_first[g], cn = g_ch_count[g];
+    const double *pp = partial + ((int64_t)r * nvec + j) * nch + c0;
+    for (int c = lane; c < cn; c += 32) sum += __ldcg(&pp[c]);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) Hp[i][(int64_t)sidx * (i + 2) + j] = sum;
+}
+
 __global__ void k_reduce_h(int ks, int G, int nch, const int *__restrict__ iter, const double *__restrict__ partial,
                            const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
                            const int *__restrict__ active, double *const *__restrict__ Hp) {
     const int i = *iter, nvec = i + 1;
     int lane = threadIdx.x & 31;
-    double *out = Hp[i];
     for (int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; wid < (int64_t)nvec * ks * G;
-         wid += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-        int j = (int)(wid % nvec);
-        int64_t rg = wid / nvec;
-        int r = (int)(rg % ks), g = (int)(rg / ks);
-        int sidx = g * ks + r;
-        if (!active[sidx]) continue;
-        double sum = 0.0;
-        int c0 = g_ch_first[g], cn = g_ch_count[g];
-        const double *pp = partial + ((int64_t)r * nvec + j) * nch + c0;
-        for (int c = lane; c < cn; c += 32) sum += pp[c];
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        if (lane == 0) out[(int64_t)sidx * (i + 2) + j] = sum;
-    }
+         wid += ((int64_t)gridDim.x * blockDim.x) >> 5)
+        reduce_h_warp(wid, lane, i, ks, nch, partial, g_ch_first, g_ch_count, active, Hp);
+}
+
+// end of an Arnoldi step (one thread): advance the step index; go on while
+// a solve is active, the basis has room and no cancellation was asked for.
+// Inside the graph's while loop it sets the loop condition.
+__device__ void iter_advance_one(int *iter, int i, int na, int cap, const volatile int *cancel, int *state,
+                                 cudaGraphConditionalHandle cond, int use_cond) {
+    int go = na > 0 && i + 1 < cap && !(cancel && *cancel);
+    *iter = i + 1;
+    state[0] = go;
+    state[1] = na;
+    if (use_cond) cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
 // end of an Arnoldi step (one thread): advance the step index; go on while
@@ -1694,13 +1726,107 @@ __global__ void k_iter_advance(int *iter, const int *__restrict__ n_active, int 
                                cudaGraphConditionalHandle cond, int use_cond) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int i = *iter;
-    int na = n_active[i];
-    int go = na > 0 && i + 1 < cap && !(cancel && *cancel);
-    *iter = i + 1;
-    state[0] = go;
-    state[1] = na;
-    if (use_cond) cudaGraphSetConditional(cond, go ? 1u : 0u);
+    iter_advance_one(iter, i, n_active[i], cap, cancel, state, cond, use_cond);
 }
+
+// What ends an Arnoldi step (k_reduce_seg of the norms, k_givens,
+// k_iter_advance) when the last CTA of k_update runs it.
+struct StepEnd {
+    int S, ks, G, M, cap, use_cond;
+    const int32_t *g_ch_first, *g_ch_count;
+    double *const *Hp;
+    double *cs, *sn, *g, *nrm2, *hnorm;
+    const double *normb;
+    double tol;
+    const int *scap;
+    int *active, *iters, *capped, *n_active_all, *iter, *state;
+    const volatile int *cancel;
+    cudaGraphConditionalHandle cond;
+};
+
+// one CTA: the norm of every active solve (summed over its geometry's
+// chunks in the same order as k_reduce_seg), the Givens update, then the
+// step index and the loop condition
+__device__ void step_end(const StepEnd &e, int i, double *partial, int nch) {
+    __shared__ int s_na;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) s_na = 0;
+    for (int sidx = threadIdx.x >> 5; sidx < e.S; sidx += blockDim.x >> 5) {
+        if (!e.active[sidx]) continue;
+        int r = sidx % e.ks, gg = sidx / e.ks;
+        double sum = 0.0;
+        int c0 = e.g_ch_first[gg], cn = e.g_ch_count[gg];
+        const double *pp = partial + (int64_t)r * nch + c0;
+        for (int c = lane; c < cn; c += 32) sum += __ldcg(&pp[c]);
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) e.nrm2[sidx] = sum;
+    }
+    __syncthreads();
+    int na = 0;
+    for (int sidx = threadIdx.x; sidx < e.S; sidx += blockDim.x)
+        if (e.active[sidx] &&
+            givens_one(sidx, i, e.M, e.Hp, e.cs, e.sn, e.g, e.normb, e.nrm2, e.hnorm, e.tol, e.scap, e.active, e.iters, e.capped))
+            na++;
+    if (na) atomicAdd(&s_na, na);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        e.n_active_all[i] = s_na;
+        iter_advance_one(e.iter, i, s_na, e.cap, e.cancel, e.state, e.cond, e.use_cond);
+    }
+}
+
+// v[r] = w[r] - sum_j h_j V_j[r] with the solve's own h; partial |v|^2 per
+// chunk. With fuse_end set, the last CTA to finish (a ticket on *done) also
+// ends the Arnoldi step (step_end: norms, Givens, step index) and resets *done.
+__global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
+                         double *const *__restrict__ Hp, SegChunks ch, int ks, const int *__restrict__ active,
+                         double *__restrict__ v, double *__restrict__ partial, int fuse_end, StepEnd fe, int *done) {
+    __shared__ double sh[32];
+    __shared__ int s_last;
+    const int nvec = *iter + 1;
+    int r = blockIdx.y, c = blockIdx.x;
+    int sidx = ch.geom[c] * ks + r;
+    if (active[sidx]) {
+    const double *h = Hp[nvec - 1] + (int64_t)sidx * (nvec + 1);
+    int64_t base = ch.start[c];
+    int len = ch.len[c];
+    // four elements per thread, each its own subtraction chain (in basis
+    // order), so the loads of one vector for all four are in flight together
+    const int U = kDotChunk / 256;
+    double x[U];
+    int64_t t0 = (int64_t)r * Np + base + threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < U; u++) x[u] = (threadIdx.x + u * 256 < len) ? w[t0 + u * 256] : 0.0;
+    for (int jv = 0; jv < nvec; jv++) {
+        const double hj = h[jv];
+        const double *vj = Vp[jv] + t0;
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (threadIdx.x + u * 256 < len) x[u] = x[u] - hj * vj[u * 256];
+    }
+    double s2 = 0.0;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        if (threadIdx.x + u * 256 < len) {
+            v[t0 + u * 256] = x[u];
+            s2 += x[u] * x[u];
+        }
+    }
+    s2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) partial[(int64_t)r * ch.n + c] = s2;
+    }
+    if (!fuse_end) return;
+    if (threadIdx.x == 0) {
+        __threadfence();  // this CTA's partial norm is visible before its ticket
+        s_last = atomicAdd(done, 1) == (int)(gridDim.x * gridDim.y) - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    step_end(fe, nvec - 1, partial, ch.n);
+    if (threadIdx.x == 0) *done = 0;
+}
+
 
 // solves whose true residual |b - A x| / |b| is at or above tol
 __global__ void k_refine_count(int S, const double *__restrict__ nr2, const double *__restrict__ nb2, double tol, int *count) {
@@ -3105,7 +3231,9 @@ static void launch_link(DeviceProblem *p, const NodeWork &w, int kp, bool mixed)
 // The launches of one product v = P * (in / diag): up-sweep (blocks, then
 // the top forest when there is one), link product, down-sweep. Arrays in/out
 // are [k][Np] on the device.
-static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag) {
+static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag,
+                         const StepScale *scale = NULL) {
+    const StepScale sc = scale ? *scale : StepScale{NULL, NULL, NULL, NULL, NULL};
     cudaStream_t s = p->stream;
     bool mixed = p->precision == FCG_PREC_MIXED;
     const SweepPlan &pl = p->plan;
@@ -3115,8 +3243,8 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     const size_t up_smem = (size_t)(2 * kBlockLeaves - 1) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
     const size_t down_smem = ((size_t)(4 * kBlockLeaves - 1 + kMaxChain) * kc + kBlockLeaves) * sizeof(double) +
                              (2 * kBlockLeaves + 1) * sizeof(int32_t);
-    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
-    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf);
+    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf, sc);
+    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf, sc);
     FCG_CK(cudaGetLastError());
     int64_t launches = 2;
     if (pl.n_top > 0) {
@@ -3226,14 +3354,14 @@ static int autotune(DeviceProblem *p, int kp) {
 }
 
 // v = P * (in / diag) for k right-hand sides ([k][Np] device arrays)
-static int matvec(DeviceProblem *p, const double *in, double *out, int k, const double *diag) {
+static int matvec(DeviceProblem *p, const double *in, double *out, int k, const double *diag, const StepScale *scale = NULL) {
     if (k < 1 || k > kMaxK) { set_error("right-hand sides per matvec must be in [1, 32]"); return FCG_GENERIC_ERROR; }
     int kp = kpad(k);
     int r = ensure_matvec_ws(p, kp);
     if (r == FCG_NORMAL_END) r = autotune(p, kp);
     if (r != FCG_NORMAL_END) return r;
     NodeWork w = {p->Qd, p->Qf, p->Pd, p->Pf2, p->Ad};
-    return launch_matvec(p, w, in, out, k, kp, diag);
+    return launch_matvec(p, w, in, out, k, kp, diag, scale);
 }
 
 int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k) {
@@ -3677,26 +3805,49 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     cudaStream_t s = p->stream;
     int64_t Np = p->Np;
     int sms = p->ctx->sm_count, r;
-    const int g1 = grid_for((int64_t)a.k * Np, 256, sms), gs = (a.S + 127) / 128;
+    const int g1 = grid_for((int64_t)a.k * Np, 256, sms);
     const int gh = (int)std::min<int64_t>(((int64_t)a.cap * a.k * a.G * 32 + 255) / 256, (int64_t)sms * 32);
-    const int g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
-    // w = A P q_i, q_i in vv
+    // q_i = v / |v| (the previous step's normalisation, done by the
+    // up-sweep for the Jacobi and no-preconditioner paths), w = A P q_i
+    const bool fused_scale = a.pk != FCG_PRECOND_TWO_LEVEL;
     if (a.pk == FCG_PRECOND_TWO_LEVEL) {
         if ((r = precond_apply(p, a.pk, p->vv, p->ptmp, a.k)) || (r = matvec(p, p->ptmp, p->w, a.k, NULL))) return r;
-    } else if ((r = matvec(p, p->vv, p->w, a.k, a.diag))) {
-        return r;
+    } else {
+        StepScale sc = {p->hnorm, p->active, p->leaf_geom, p->Vptr, p->d_it};
+        if ((r = matvec(p, p->vv, p->w, a.k, a.diag, &sc))) return r;
     }
-    // classical Gram-Schmidt against q_0..q_i, per solve
-    k_dots<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial);
-    k_reduce_h<<<gh, 256, 0, s>>>(a.k, a.G, a.nch, p->d_it, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->Hptr);
-    k_update<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial);
-    k_reduce_seg<<<g1v, 256, 0, s>>>(1, a.k, a.G, a.nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1, 0);
-    k_givens<<<gs, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, a.tol, p->scap,
-                                p->active, p->iters, p->capped, p->n_active);
-    k_scale<<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it);
-    k_iter_advance<<<1, 32, 0, s>>>(p->d_it, p->n_active, a.cap, p->pin_dev ? p->pin_dev + 4 : NULL, p->d_it + 1, a.cond,
-                                    a.use_cond);
-    p->timings.launches += 7;
+    // classical Gram-Schmidt against q_0..q_i, per solve; for a few solves
+    // the Hessenberg column is summed by the last CTA of k_dots
+    const bool fuse_h = a.S <= 4;
+    k_dots<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial, fuse_h ? 1 : 0, a.G,
+                                            p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
+    if (!fuse_h)
+        k_reduce_h<<<gh, 256, 0, s>>>(a.k, a.G, a.nch, p->d_it, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->Hptr);
+    // v = w - sum h_j q_j; for a few solves its last CTA ends the step
+    // (norms, Givens, index), for many the three kernels do
+    const bool fuse_end = a.S <= 4;
+    const volatile int *cancel = p->pin_dev ? p->pin_dev + 4 : NULL;
+    StepEnd fe = {a.S, a.k, a.G, a.M, a.cap, a.use_cond, p->g_ch_first, p->g_ch_count, p->Hptr, p->cs, p->sn, p->g, p->nrm2,
+                  p->hnorm, p->normb, a.tol, p->scap, p->active, p->iters, p->capped, p->n_active, p->d_it, p->d_it + 1,
+                  cancel, a.cond};
+    k_update<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial,
+                                              fuse_end ? 1 : 0, fe, p->d_it + 3);
+    int launches = 3 + (fuse_h ? 0 : 1);
+    if (!fuse_end) {
+        const int gs = (a.S + 127) / 128, g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
+        k_reduce_seg<<<g1v, 256, 0, s>>>(1, a.k, a.G, a.nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1, 0);
+        k_givens<<<gs, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, a.tol, p->scap,
+                                    p->active, p->iters, p->capped, p->n_active);
+        k_iter_advance<<<1, 32, 0, s>>>(p->d_it, p->n_active, a.cap, cancel, p->d_it + 1, a.cond, a.use_cond);
+        launches += 3;
+    }
+    if (!fused_scale) {
+        // the two-level path normalises here (its preconditioner reads v first);
+        // k_update's step end has already advanced the index, hence Vp[*iter]
+        k_scale<<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
+        launches++;
+    }
+    p->timings.launches += launches;
     FCG_CK(cudaGetLastError());
     return FCG_NORMAL_END;
 }
@@ -3909,7 +4060,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
             k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
                                             p->capped, p->n_active + M + 1);
-            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL);
+            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
             FCG_CK(cudaGetLastError());
             p->timings.launches += 7;
             // does any solve need an Arnoldi step? (read below, after the
