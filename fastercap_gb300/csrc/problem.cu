@@ -171,6 +171,7 @@ struct DeviceProblem {
     double *coef64 = NULL;
     float *coef32 = NULL;
     double *self = NULL;
+    double *rself = NULL;  // mixed path: 1 / self, the Jacobi scaling of the sweeps as a multiply
     unsigned *status = NULL;
     SweepPlan plan;
 
@@ -617,6 +618,11 @@ __global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *_
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 int band = (int)(wv[u] >> kBandShift);
+                // slots with weight (rule 5: 6, rules 2 and 3: 3, point
+                // formula: 1), the most any lane running here needs: the
+                // others have weight 0 and add exactly nothing
+                int ns = band == 0 ? 0 : (band == 1 ? 6 : (band == 4 ? 1 : 3));
+                ns = __reduce_max_sync(__activemask(), ns);
                 if (band == 0) continue;
                 float cx = Cq[u].y, cy = Cq[u].z, cz = Cq[u].w;
                 float dx = c1x - cx, dy = c1y - cy, dz = c1z - cz;
@@ -626,6 +632,7 @@ __global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *_
                 float acc = 0.0f;
 #pragma unroll
                 for (int sl = 0; sl < 6; sl++) {
+                    if (sl >= ns) break;
                     float4 t = tab[band][sl];
                     float ex = dx - (t.x * w0x + t.y * w1x + t.z * w2x);
                     float ey = dy - (t.x * w0y + t.y * w1y + t.z * w2y);
@@ -704,7 +711,7 @@ __global__ void k_fill_near32(int64_t n, const int32_t *__restrict__ near_link, 
 // leaves by their closed form.
 __global__ void k_fill_self32(int64_t Np, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
                               const fcg_tri32 *__restrict__ tri, const double *__restrict__ eb, const double *__restrict__ ea,
-                              double *__restrict__ self, unsigned *status, unsigned long long *fb) {
+                              double *__restrict__ self, double *__restrict__ rself, unsigned *status, unsigned long long *fb) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
         int32_t node = leaf_node[j];
         const NodeGeo &g = geo[node];
@@ -722,6 +729,7 @@ __global__ void k_fill_self32(int64_t Np, const int32_t *__restrict__ leaf_node,
         }
         if (!isfinite(val) || val == 0.0) atomicOr(status, 2u);
         self[j] = val;
+        rself[j] = 1.0 / val;
     }
 }
 
@@ -768,8 +776,8 @@ struct StepScale {
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan plan, const double *in, int64_t ld, int k, int kp,
-                                                              int kc, const double *__restrict__ diag, double *__restrict__ Qd,
-                                                              float *__restrict__ Qf, const StepScale sc) {
+                                                              int kc, const double *__restrict__ diag, int recip,
+                                                              double *__restrict__ Qd, float *__restrict__ Qf, const StepScale sc) {
     extern __shared__ double sh[];
     double *val = sh;                                                 // (2 kBlockLeaves - 1) x kc
     uint32_t *kids = (uint32_t *)(sh + (2 * kBlockLeaves - 1) * kc);  // kBlockLeaves
@@ -799,7 +807,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
                     Vi[at] = x;
                 }
             }
-            if (diag) x = x / diag[lf + i];
+            if (diag) x = recip ? x * diag[lf + i] : x / diag[lf + i];
             val[i * kc + r] = x;
             int64_t o = (int64_t)(lf + i) * kp + c0 + r;
             if (!MIXED || ni == 0) Qd[o] = x;
@@ -903,8 +911,8 @@ __device__ __forceinline__ double pval(const float2 *P, int64_t i) {
 template <class TP>
 __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan plan, const double *__restrict__ in, int64_t ld,
                                                                 int k, int kp, int kc, const double *__restrict__ diag,
-                                                                const double *__restrict__ self, const TP *__restrict__ P,
-                                                                double *__restrict__ out) {
+                                                                int recip, const double *__restrict__ self,
+                                                                const TP *__restrict__ P, double *__restrict__ out) {
     extern __shared__ double sh[];
     double *pv = sh;                                     // (2 kBlockLeaves - 1) x kc: P, then A of internal nodes
     double *al = pv + (2 * kBlockLeaves - 1) * kc;       // kBlockLeaves x kc: A of each leaf's parent
@@ -936,7 +944,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
             int j = lf + i;
             pv[i * kc + r] = pval(P, (int64_t)j * kp + c0 + r);
             double xv = in[(int64_t)(c0 + r) * ld + j];
-            if (diag) xv = xv / diag[j];
+            if (diag) xv = recip ? xv * diag[j] : xv / diag[j];
             xs[i * kc + r] = xv;
         }
         __syncthreads();
@@ -2897,6 +2905,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     tr.mark("device model and layout");
     tr.dreport();
     FCG_TRY(dalloc(&p->self, Np, p->bytes));
+    if (precision == FCG_PREC_MIXED) FCG_TRY(dalloc(&p->rself, Np, p->bytes));
     if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
@@ -2931,7 +2940,7 @@ void problem_destroy(DeviceProblem *p) {
     AllocScope alloc_scope(p->stream);
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
     dfree(p->left); dfree(p->right); dfree(p->node_lfirst); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
-    dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->status);
+    dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->rself); dfree(p->status);
     dfree(p->near_link); dfree(p->near_row); dfree(p->tri); dfree(p->tri32); dfree(p->fill_fp64);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
@@ -3079,7 +3088,7 @@ int problem_fill(DeviceProblem *p) {
     }
     if (mixed)
         k_fill_self32<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->tri32, p->leaf_eb, p->leaf_ea,
-                                                               p->self, p->status, p->fill_fp64);
+                                                               p->self, p->rself, p->status, p->fill_fp64);
     else
         k_fill_self<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->leaf_eb, p->leaf_ea, p->self,
                                                              p->status);
@@ -3243,8 +3252,12 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     const size_t up_smem = (size_t)(2 * kBlockLeaves - 1) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
     const size_t down_smem = ((size_t)(4 * kBlockLeaves - 1 + kMaxChain) * kc + kBlockLeaves) * sizeof(double) +
                              (2 * kBlockLeaves + 1) * sizeof(int32_t);
-    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf, sc);
-    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, diag, w.Qd, w.Qf, sc);
+    // the mixed path's Jacobi scaling multiplies by the reciprocals (the
+    // FP64 path divides, as the reference does)
+    const int recip = mixed && diag == p->self && p->rself ? 1 : 0;
+    const double *dg = recip ? p->rself : diag;
+    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, sc);
+    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, sc);
     FCG_CK(cudaGetLastError());
     int64_t launches = 2;
     if (pl.n_top > 0) {
@@ -3279,8 +3292,8 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
         if (mixed) FCG_CK(cudaMemsetAsync(w.Pf2, 0, n * sizeof(float2), s));
         else FCG_CK(cudaMemsetAsync(w.Pd, 0, n * sizeof(double), s));
     }
-    if (mixed) k_down_blk<float2><<<pl.n_blocks, kSweepThreads, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pf2, out);
-    else k_down_blk<double><<<pl.n_blocks, kSweepThreads, down_smem, s>>>(pl, in, Np, k, kp, kc, diag, p->self, w.Pd, out);
+    if (mixed) k_down_blk<float2><<<pl.n_blocks, kSweepThreads, down_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, p->self, w.Pf2, out);
+    else k_down_blk<double><<<pl.n_blocks, kSweepThreads, down_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, p->self, w.Pd, out);
     FCG_CK(cudaGetLastError());
     p->timings.matvecs++;
     p->timings.launches += launches;
