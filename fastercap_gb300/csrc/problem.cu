@@ -767,7 +767,8 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
 // written back to v and to basis vector *iter; nothing at step 0, whose
 // vector is normalised before the loop.
 struct StepScale {
-    const double *hn;  // NULL: no normalisation
+    const double *hn;  // NULL: no normalisation; reciprocals of the norms when recip is set
+    int recip;
     const int *active;
     const int32_t *leaf_geom;
     double *const *Vp;
@@ -802,7 +803,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
             if (Vi) {
                 int sidx = sc.leaf_geom[lf + i] * k + c0 + r;
                 if (sc.active[sidx]) {
-                    x = x / sc.hn[sidx];
+                    x = sc.recip ? x * sc.hn[sidx] : x / sc.hn[sidx];
                     const_cast<double *>(in)[at] = x;
                     Vi[at] = x;
                 }
@@ -1621,12 +1622,13 @@ __global__ void k_reduce_seg(int nvec, int ks, int G, int nch, const double *__r
 // Givens update of Hessenberg column i of active solve sidx; true while the
 // solve goes on
 __device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ Hp, double *cs, double *sn, double *g,
-                           const double *normb, const double *nrm2, double *hnorm, double tol, const int *scap, int *active,
-                           int *iters, int *capped) {
+                           const double *normb, const double *nrm2, double *hnorm, double *rhnorm, double tol, const int *scap,
+                           int *active, int *iters, int *capped) {
     double *hc = Hp[i] + (int64_t)sidx * (i + 2);
     double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2), *gg = g + (int64_t)sidx * (M + 2);
     double hn = sqrt(nrm2[sidx]);
     hnorm[sidx] = hn;
+    if (rhnorm) rhnorm[sidx] = 1.0 / hn;
     hc[i + 1] = hn;
     for (int j = 0; j < i; j++) {
         double t1 = hc[j], t2 = hc[j + 1];
@@ -1659,12 +1661,13 @@ __device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ H
 
 // Givens update of Hessenberg column i of every active solve (one thread each)
 __global__ void k_givens(int S, const int *__restrict__ iter, int M, double *const *__restrict__ Hp, double *cs, double *sn,
-                         double *g, const double *normb, const double *nrm2, double *hnorm, double tol, const int *scap, int *active,
-                         int *iters, int *capped, int *n_active_all) {
+                         double *g, const double *normb, const double *nrm2, double *hnorm, double *rhnorm, double tol,
+                         const int *scap, int *active, int *iters, int *capped, int *n_active_all) {
     const int i = *iter;
     int sidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (sidx >= S || !active[sidx]) return;
-    if (givens_one(sidx, i, M, Hp, cs, sn, g, normb, nrm2, hnorm, tol, scap, active, iters, capped)) atomicAdd(n_active_all + i, 1);
+    if (givens_one(sidx, i, M, Hp, cs, sn, g, normb, nrm2, hnorm, rhnorm, tol, scap, active, iters, capped))
+        atomicAdd(n_active_all + i, 1);
 }
 
 // out[r][j] = v[r][j] / hn[solve of (j, r)] for active solves, out = out_fixed
@@ -1743,7 +1746,7 @@ struct StepEnd {
     int S, ks, G, M, cap, use_cond;
     const int32_t *g_ch_first, *g_ch_count;
     double *const *Hp;
-    double *cs, *sn, *g, *nrm2, *hnorm;
+    double *cs, *sn, *g, *nrm2, *hnorm, *rhnorm;
     const double *normb;
     double tol;
     const int *scap;
@@ -1773,7 +1776,8 @@ __device__ void step_end(const StepEnd &e, int i, double *partial, int nch) {
     int na = 0;
     for (int sidx = threadIdx.x; sidx < e.S; sidx += blockDim.x)
         if (e.active[sidx] &&
-            givens_one(sidx, i, e.M, e.Hp, e.cs, e.sn, e.g, e.normb, e.nrm2, e.hnorm, e.tol, e.scap, e.active, e.iters, e.capped))
+            givens_one(sidx, i, e.M, e.Hp, e.cs, e.sn, e.g, e.normb, e.nrm2, e.hnorm, e.rhnorm, e.tol, e.scap, e.active, e.iters,
+                       e.capped))
             na++;
     if (na) atomicAdd(&s_na, na);
     __syncthreads();
@@ -3242,7 +3246,7 @@ static void launch_link(DeviceProblem *p, const NodeWork &w, int kp, bool mixed)
 // are [k][Np] on the device.
 static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag,
                          const StepScale *scale = NULL) {
-    const StepScale sc = scale ? *scale : StepScale{NULL, NULL, NULL, NULL, NULL};
+    const StepScale sc = scale ? *scale : StepScale{NULL, 0, NULL, NULL, NULL, NULL};
     cudaStream_t s = p->stream;
     bool mixed = p->precision == FCG_PREC_MIXED;
     const SweepPlan &pl = p->plan;
@@ -3579,7 +3583,9 @@ static int ensure_solve_ws(DeviceProblem *p, int k, int S, int M) {
         size_t sm = (size_t)S * (M + 2);
         if ((r = dalloc(&p->cs, sm, B)) || (r = dalloc(&p->sn, sm, B)) || (r = dalloc(&p->g, sm, B)) || (r = dalloc(&p->z, sm, B)))
             return r;
-        if ((r = dalloc(&p->normb, S, B)) || (r = dalloc(&p->hnorm, S, B)) || (r = dalloc(&p->nrm2, 2 * (size_t)S, B))) return r;
+        // hnorm: the step's norms, then (mixed path) their reciprocals
+        if ((r = dalloc(&p->normb, S, B)) || (r = dalloc(&p->hnorm, 2 * (size_t)S, B)) || (r = dalloc(&p->nrm2, 2 * (size_t)S, B)))
+            return r;
         if ((r = dalloc(&p->active, S, B)) || (r = dalloc(&p->iters, S, B)) || (r = dalloc(&p->capped, S, B)) ||
             (r = dalloc(&p->scap, S, B)) || (r = dalloc(&p->n_active, (size_t)M + 2, B)))
             return r;
@@ -3826,7 +3832,9 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     if (a.pk == FCG_PRECOND_TWO_LEVEL) {
         if ((r = precond_apply(p, a.pk, p->vv, p->ptmp, a.k)) || (r = matvec(p, p->ptmp, p->w, a.k, NULL))) return r;
     } else {
-        StepScale sc = {p->hnorm, p->active, p->leaf_geom, p->Vptr, p->d_it};
+        // the mixed path multiplies by the reciprocal norms (the FP64 path divides, as the reference does)
+        const bool mixed = p->precision == FCG_PREC_MIXED;
+        StepScale sc = {mixed ? p->hnorm + a.S : p->hnorm, mixed ? 1 : 0, p->active, p->leaf_geom, p->Vptr, p->d_it};
         if ((r = matvec(p, p->vv, p->w, a.k, a.diag, &sc))) return r;
     }
     // classical Gram-Schmidt against q_0..q_i, per solve; for a few solves
@@ -3840,8 +3848,9 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     // (norms, Givens, index), for many the three kernels do
     const bool fuse_end = a.S <= 4;
     const volatile int *cancel = p->pin_dev ? p->pin_dev + 4 : NULL;
+    double *rhn = p->precision == FCG_PREC_MIXED ? p->hnorm + a.S : NULL;
     StepEnd fe = {a.S, a.k, a.G, a.M, a.cap, a.use_cond, p->g_ch_first, p->g_ch_count, p->Hptr, p->cs, p->sn, p->g, p->nrm2,
-                  p->hnorm, p->normb, a.tol, p->scap, p->active, p->iters, p->capped, p->n_active, p->d_it, p->d_it + 1,
+                  p->hnorm, rhn, p->normb, a.tol, p->scap, p->active, p->iters, p->capped, p->n_active, p->d_it, p->d_it + 1,
                   cancel, a.cond};
     k_update<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial,
                                               fuse_end ? 1 : 0, fe, p->d_it + 3);
@@ -3849,8 +3858,8 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     if (!fuse_end) {
         const int gs = (a.S + 127) / 128, g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
         k_reduce_seg<<<g1v, 256, 0, s>>>(1, a.k, a.G, a.nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1, 0);
-        k_givens<<<gs, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, a.tol, p->scap,
-                                    p->active, p->iters, p->capped, p->n_active);
+        k_givens<<<gs, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, rhn, a.tol,
+                                    p->scap, p->active, p->iters, p->capped, p->n_active);
         k_iter_advance<<<1, 32, 0, s>>>(p->d_it, p->n_active, a.cap, cancel, p->d_it + 1, a.cond, a.use_cond);
         launches += 3;
     }
