@@ -2575,10 +2575,18 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         int prio_hi = 0;
         cudaEvent_t ev_alloc = NULL, ev_lab = NULL, ev_rel = NULL;
         // the link sources go up in chunks of whole relabelling tiles; each
-        // chunk's relabelling starts when its upload is done
+        // chunk's relabelling starts when its upload is done. From pageable
+        // host memory a copy is staged synchronously, so chunks would only
+        // serialise: one copy then.
         const int kLinkChunks = 8;
         const int64_t ntiles = (L + kRelTile - 1) / kRelTile;
-        int nchunk = L > 0 ? kLinkChunks : 0;
+        bool src_pinned = false;
+        if (L > 0) {
+            cudaPointerAttributes pa;
+            src_pinned = cudaPointerGetAttributes(&pa, a.link_src) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+            cudaGetLastError();
+        }
+        int nchunk = L > 0 ? (src_pinned ? kLinkChunks : 1) : 0;
         std::vector<int64_t> tbound(nchunk + 1, 0);
         std::vector<cudaEvent_t> ev_src(nchunk, (cudaEvent_t)NULL);
         for (int c = 1; c <= nchunk; c++) tbound[c] = ntiles * c / nchunk;
