@@ -559,10 +559,10 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const ui
 // of (v0, v1, v2), and the frame's jacobian / (2 area) is exactly 1, so the
 // triangle average is the weighted sum over barycentric points: rule 2 the
 // three permutations of (2/3, 1/6, 1/6), rule 3 the edge midpoints, rule 5
-// the six permutations of its three coordinates. Every link evaluates six
-// slots of a per-band table (unused slots: the centroid with weight 0; the
-// point formula: the centroid offset itself with weight 1), so the lanes of
-// a warp run the same code whatever their links' bands.
+// the six permutations of its three coordinates. A link evaluates the
+// slots of a per-band table (unused slots: the centroid with weight 0) that
+// some lane of its warp needs, so the lanes run the same code whatever
+// their links' bands; the point formula (band 4) uses the centroid offset.
 __global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                                                     const NodeGeo *__restrict__ geo, float *__restrict__ c32, unsigned *status) {
     __shared__ float4 tab[5][6];  // [band][slot] = (weight of v0, of v1, of v2, quadrature weight)
@@ -618,28 +618,37 @@ __global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *_
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 int band = (int)(wv[u] >> kBandShift);
-                // slots with weight (rule 5: 6, rules 2 and 3: 3, point
-                // formula: 1), the most any lane running here needs: the
-                // others have weight 0 and add exactly nothing
-                int ns = band == 0 ? 0 : (band == 1 ? 6 : (band == 4 ? 1 : 3));
+                // quadrature slots with weight (rule 5: 6, rules 2 and 3: 3),
+                // the most any lane running here needs: the others have
+                // weight 0 and add exactly nothing
+                int ns = band == 1 ? 6 : ((band == 2 || band == 3) ? 3 : 0);
                 ns = __reduce_max_sync(__activemask(), ns);
                 if (band == 0) continue;
-                float cx = Cq[u].y, cy = Cq[u].z, cz = Cq[u].w;
-                float dx = c1x - cx, dy = c1y - cy, dz = c1z - cz;
-                float w0x = A[u].x - cx, w0y = A[u].y - cy, w0z = A[u].z - cz;
-                float w1x = A[u].w - cx, w1y = B[u].x - cy, w1z = B[u].y - cz;
-                float w2x = B[u].z - cx, w2y = B[u].w - cy, w2z = Cq[u].x - cz;
-                float acc = 0.0f;
+                float acc;
+                if (band == 4) {
+                    // point formula at the source centroid
+                    float dx = c1x - Cq[u].y, dy = c1y - Cq[u].z, dz = c1z - Cq[u].w;
+                    float ir = rsqrtf(dx * dx + dy * dy + dz * dz);
+                    acc = diel ? (dx * nx + dy * ny + dz * nz) * ir * ir * ir : ir;
+                } else {
+                    // a rule point is the barycentric combination sum t_k v_k
+                    // (sum t_k = 1), so the vector from it to the field point is
+                    // sum t_k (c1 - v_k)
+                    float f0x = c1x - A[u].x, f0y = c1y - A[u].y, f0z = c1z - A[u].z;
+                    float f1x = c1x - A[u].w, f1y = c1y - B[u].x, f1z = c1z - B[u].y;
+                    float f2x = c1x - B[u].z, f2y = c1y - B[u].w, f2z = c1z - Cq[u].x;
+                    acc = 0.0f;
 #pragma unroll
-                for (int sl = 0; sl < 6; sl++) {
-                    if (sl >= ns) break;
-                    float4 t = tab[band][sl];
-                    float ex = dx - (t.x * w0x + t.y * w1x + t.z * w2x);
-                    float ey = dy - (t.x * w0y + t.y * w1y + t.z * w2y);
-                    float ez = dz - (t.x * w0z + t.y * w1z + t.z * w2z);
-                    float ir = rsqrtf(ex * ex + ey * ey + ez * ez);
-                    float f = diel ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
-                    acc += t.w * f;
+                    for (int sl = 0; sl < 6; sl++) {
+                        if (sl >= ns) break;
+                        float4 t = tab[band][sl];
+                        float ex = t.x * f0x + t.y * f1x + t.z * f2x;
+                        float ey = t.x * f0y + t.y * f1y + t.z * f2y;
+                        float ez = t.x * f0z + t.y * f1z + t.z * f2z;
+                        float ir = rsqrtf(ex * ex + ey * ey + ez * ez);
+                        float f = diel ? (ex * nx + ey * ny + ez * nz) * ir * ir * ir : ir;
+                        acc += t.w * f;
+                    }
                 }
                 float val = k * acc;
                 if (!isfinite(val)) atomicOr(status, 1u);
