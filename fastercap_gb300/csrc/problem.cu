@@ -787,7 +787,8 @@ struct StepScale {
 template <bool MIXED>
 __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan plan, const double *in, int64_t ld, int k, int kp,
                                                               int kc, const double *__restrict__ diag, int recip,
-                                                              double *__restrict__ Qd, float *__restrict__ Qf, const StepScale sc) {
+                                                              double *__restrict__ Qd, float *__restrict__ Qf,
+                                                              double *__restrict__ rootq, const StepScale sc) {
     extern __shared__ double sh[];
     double *val = sh;                                                 // (2 kBlockLeaves - 1) x kc
     uint32_t *kids = (uint32_t *)(sh + (2 * kBlockLeaves - 1) * kc);  // kBlockLeaves
@@ -822,6 +823,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
             int64_t o = (int64_t)(lf + i) * kp + c0 + r;
             if (!MIXED || ni == 0) Qd[o] = x;
             if (MIXED) Qf[o] = (float)x;
+            if (ni == 0) rootq[(int64_t)b * kp + c0 + r] = x;
         }
         __syncthreads();
         for (int h = 0; h < H; h++) {
@@ -834,6 +836,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
                 int64_t o = (int64_t)lbl[q] * kp + c0 + r;
                 if (!MIXED || q == ni - 1) Qd[o] = sum;  // the root is the block's last (highest) node
                 if (MIXED) Qf[o] = (float)sum;
+                if (q == ni - 1) rootq[(int64_t)b * kp + c0 + r] = sum;
             }
             __syncthreads();
         }
@@ -845,8 +848,8 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
 // (blocks + top nodes) x kc values fit). k_up_top_global is the same pass
 // through device memory for forests too large for shared memory.
 template <bool MIXED>
-__global__ void __launch_bounds__(1024) k_up_top(const SweepPlan plan, int k, int kp, int kc, double *__restrict__ Qd,
-                                                 float *__restrict__ Qf) {
+__global__ void __launch_bounds__(1024) k_up_top(const SweepPlan plan, int k, int kp, int kc, const double *__restrict__ rootq,
+                                                 double *__restrict__ Qd, float *__restrict__ Qf) {
     extern __shared__ double sh[];
     const int nb = plan.n_blocks, T = plan.n_top, nh = plan.n_top_levels, tid = threadIdx.x;
     double *val = sh;                                        // (nb + T) x kc
@@ -862,7 +865,7 @@ __global__ void __launch_bounds__(1024) k_up_top(const SweepPlan plan, int k, in
         const int kk = min(kc, k - c0);
         for (int t = tid; t < nb * kk; t += blockDim.x) {
             int r = t / nb, bb = t - r * nb;
-            val[bb * kc + r] = Qd[(int64_t)plan.blk_root[bb] * kp + c0 + r];
+            val[bb * kc + r] = rootq[(int64_t)bb * kp + c0 + r];
         }
         __syncthreads();
         for (int h = 0; h < nh; h++) {
@@ -3199,7 +3202,7 @@ struct NodeWork {
     float *Qf;
     double *Pd;
     float2 *Pf2;
-    double *Ad;
+    double *Ad;  // the block roots' charges in block order (n_blocks x kp of it)
 };
 
 // One link-product launch (the kernel follows kp, precision and the
@@ -3277,8 +3280,9 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     // FP64 path divides, as the reference does)
     const int recip = mixed && diag == p->self && p->rself ? 1 : 0;
     const double *dg = recip ? p->rself : diag;
-    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, sc);
-    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, sc);
+    // w.Ad (n_nodes x kp) holds the block roots' charges in block order
+    if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, w.Ad, sc);
+    else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, w.Ad, sc);
     FCG_CK(cudaGetLastError());
     int64_t launches = 2;
     if (pl.n_top > 0) {
@@ -3289,8 +3293,8 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
         int tkc = (int)std::min<size_t>((size_t)k, room / per_col);
         if (tkc >= 1) {
             size_t top_smem = fixed + per_col * tkc;
-            if (mixed) k_up_top<true><<<1, 1024, top_smem, s>>>(pl, k, kp, tkc, w.Qd, w.Qf);
-            else k_up_top<false><<<1, 1024, top_smem, s>>>(pl, k, kp, tkc, w.Qd, w.Qf);
+            if (mixed) k_up_top<true><<<1, 1024, top_smem, s>>>(pl, k, kp, tkc, w.Ad, w.Qd, w.Qf);
+            else k_up_top<false><<<1, 1024, top_smem, s>>>(pl, k, kp, tkc, w.Ad, w.Qd, w.Qf);
         } else {
             if (mixed) k_up_top_global<true><<<1, 1024, 0, s>>>(pl, k, kp, w.Qd, w.Qf);
             else k_up_top_global<false><<<1, 1024, 0, s>>>(pl, k, kp, w.Qd, w.Qf);
