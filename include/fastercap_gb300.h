@@ -116,9 +116,11 @@ void fcg_model_free(fcg_model *m);
 
 /* Structural checks of caller-built arrays (tree in post-order with
  * contiguous leaf ranges, link offsets, conductor ranges tiling the leaves,
- * permittivity indices), the same checks fcg_problem_create makes before any
- * device work; link sources are range-checked on the device at creation.
- * FCG_GENERIC_ERROR with the reason in fcg_last_error(). No device needed. */
+ * permittivity indices) on the host, with the messages fcg_problem_create
+ * gives: creation runs the per-node and per-leaf checks on the device
+ * before any kernel indexes with the arrays, and range-checks the link
+ * sources there. FCG_GENERIC_ERROR with the reason in fcg_last_error().
+ * No device needed. */
 int fcg_model_arrays_check(const fcg_model_arrays *arrays);
 
 /* Concatenate independent models (geometries) into one model: a forest with
@@ -142,7 +144,9 @@ void *fcg_context_stream(fcg_context *ctx);
 
 /* Upload a model once (copies the arrays to HBM). Replaces the reference's
  * in-memory link chunks m_dPotCoeffLinks / m_pdPanelPtrLinks
- * (Solver/Autorefine.h:271-272) and node array m_pNodes (Solver/Autorefine.h:283). */
+ * (Solver/Autorefine.h:271-272) and node array m_pNodes (Solver/Autorefine.h:283).
+ * Arrays in pinned (page-locked) host memory upload fastest: the link
+ * sources then go up in chunks that overlap the device-side layout work. */
 int fcg_problem_create(fcg_context *ctx, const fcg_model_arrays *arrays, int precision, fcg_problem **out);
 /* same, with all of the problem's work on a caller-owned CUDA stream (a
  * cudaStream_t; NULL gives the problem a stream of its own) */
