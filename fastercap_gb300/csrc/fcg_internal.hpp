@@ -39,6 +39,11 @@ struct DeviceContext {
     // link-product launch shapes chosen by measurement, per problem shape
     std::mutex tune_mu;
     std::map<uint64_t, int> tune;
+    // pinned staging buffers for uploads from pageable host memory (taken
+    // two at a time by a problem creation, allocated on first need)
+    std::mutex stage_mu;
+    std::vector<void *> stage_free;
+    int stage_count = 0;
 };
 void context_release(DeviceContext &ctx);
 void context_unref(DeviceContext *ctx);

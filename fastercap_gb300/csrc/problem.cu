@@ -114,6 +114,85 @@ template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes
     return FCG_NORMAL_END;
 }
 
+// Host-to-device copies during problem creation. From pageable host memory
+// the driver stages a copy synchronously through its own buffers, and
+// concurrent creations (the serving slots) queue on that path; a Stager
+// instead copies through two pinned buffers of the context, the host filling
+// one while the DMA of the other runs, so every creating thread streams at
+// its own memcpy speed. Pinned sources go straight to the copy engine.
+static const size_t kStageBytes = (size_t)8 << 20;
+static const int kStageMax = 32;  // pinned staging buffers per context
+
+struct Stager {
+    DeviceContext *ctx = NULL;
+    void *buf[2] = {NULL, NULL};
+    cudaEvent_t ev[2] = {NULL, NULL};
+    int next = 0;
+    bool tried = false;
+    explicit Stager(DeviceContext &c) : ctx(&c) {}
+    // the two buffers, taken from the context (allocated there on first
+    // need) when the first pageable copy comes
+    void acquire() {
+        tried = true;
+        std::lock_guard<std::mutex> lk(ctx->stage_mu);
+        for (int i = 0; i < 2; i++) {
+            if (!ctx->stage_free.empty()) {
+                buf[i] = ctx->stage_free.back();
+                ctx->stage_free.pop_back();
+            } else if (ctx->stage_count < kStageMax && cudaHostAlloc(&buf[i], kStageBytes, cudaHostAllocDefault) == cudaSuccess) {
+                ctx->stage_count++;
+            } else {
+                cudaGetLastError();
+                buf[i] = NULL;
+            }
+            if (buf[i] && cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess) ev[i] = NULL;
+        }
+    }
+    bool usable() {
+        if (!tried) acquire();
+        return buf[0] && buf[1] && ev[0] && ev[1];
+    }
+    static bool pinned(const void *h) {
+        cudaPointerAttributes pa;
+        bool r = cudaPointerGetAttributes(&pa, h) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        return r;
+    }
+    cudaError_t copy(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+        if (!bytes) return cudaSuccess;
+        if (pinned(src) || !usable()) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+        for (size_t off = 0; off < bytes; off += kStageBytes) {
+            size_t n = std::min(kStageBytes, bytes - off);
+            int b = next;
+            next ^= 1;
+            cudaError_t e = cudaEventSynchronize(ev[b]);  // the buffer's previous DMA is done
+            if (e != cudaSuccess) return e;
+            memcpy(buf[b], (const char *)src + off, n);
+            if ((e = cudaMemcpyAsync((char *)dst + off, buf[b], n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(ev[b], s)) != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    ~Stager() {
+        for (int i = 0; i < 2; i++) {
+            if (ev[i]) {
+                cudaEventSynchronize(ev[i]);
+                cudaEventDestroy(ev[i]);
+            }
+        }
+        std::lock_guard<std::mutex> lk(ctx->stage_mu);
+        for (int i = 0; i < 2; i++)
+            if (buf[i]) ctx->stage_free.push_back(buf[i]);
+    }
+};
+
+template <class T> static int upload_staged(Stager &st, T **p, const T *h, size_t n, int64_t &bytes, cudaStream_t s) {
+    int r = dalloc(p, n, bytes);
+    if (r != FCG_NORMAL_END) return r;
+    if (n) FCG_CK(st.copy(*p, h, n * sizeof(T), s));
+    return FCG_NORMAL_END;
+}
+
 // The sweeps' plan. Blocks are the maximal subtrees of at most kBlockLeaves
 // leaves (one CTA each); inside a block a node has a local index: leaves
 // 0..nl-1 in leaf order, internal nodes nl + their position in the block's
@@ -2056,6 +2135,12 @@ void context_release(DeviceContext &ctx) {
         cudaFreeHost(ctx.pin);
         ctx.pin = nullptr;
     }
+    {
+        std::lock_guard<std::mutex> lk(ctx.stage_mu);
+        for (void *b : ctx.stage_free) cudaFreeHost(b);
+        ctx.stage_free.clear();
+        ctx.stage_count = 0;
+    }
     // hand the pool's unused blocks back
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, ctx.device) == cudaSuccess) {
@@ -2623,7 +2708,8 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
                 set_error("cannot create the upload events");
                 rr = FCG_DEVICE_ERROR;
             }
-#define FCG_UP(ptr, host, n) if (rr == FCG_NORMAL_END) rr = upload(&ptr, host, n, tb, s)
+        Stager st(ctx);
+#define FCG_UP(ptr, host, n) if (rr == FCG_NORMAL_END) rr = upload_staged(st, &ptr, host, n, tb, s)
 #define FCG_AL(ptr, n) if (rr == FCG_NORMAL_END) rr = dalloc(&ptr, (size_t)(n), tb)
         // 1. what the checks read, and the checks
         tr.dmark("start", s);
@@ -2665,9 +2751,7 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
             bool ok = cudaEventRecord(ev_alloc, s) == cudaSuccess && cudaStreamWaitEvent(s2, ev_alloc, 0) == cudaSuccess;
             for (int c = 0; c < nchunk && ok; c++) {
                 int64_t lo = tbound[c] * kRelTile, hi = std::min(tbound[c + 1] * kRelTile, L);
-                if (hi > lo)
-                    ok = cudaMemcpyAsync(src_model + lo, a.link_src + lo, (hi - lo) * sizeof(uint32_t), cudaMemcpyHostToDevice, s2) ==
-                         cudaSuccess;
+                if (hi > lo) ok = st.copy(src_model + lo, a.link_src + lo, (hi - lo) * sizeof(uint32_t), s2) == cudaSuccess;
                 ok = ok && cudaEventRecord(ev_src[c], s2) == cudaSuccess;
                 if (c == 0) tr.dmark("link chunk 0 uploaded", s2);
             }
