@@ -1159,6 +1159,15 @@ __device__ __forceinline__ void kmul_add(KSum &a, float c, float q) {
     a.c = y - (t - a.s);
     a.s = t;
 }
+// Kahan's update with a short plain FP32 sum of products (a group of links):
+// the group sum's rounding is of the order of the FP32 coefficients' own, the
+// compensation then carries across groups. Four instructions per group.
+__device__ __forceinline__ void kgroup_add(KSum &a, float x) {
+    float y = x + a.c;
+    float t = a.s + y;
+    a.c = y - (t - a.s);
+    a.s = t;
+}
 
 template <int K> __device__ __forceinline__ void load_q(const float *__restrict__ Q, uint32_t j, float *q) {
     if (K % 4 == 0) {
@@ -1192,18 +1201,23 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
         for (int r = 0; r < K; r++) { acc[r].s = 0.f; acc[r].c = 0.f; }
         int s = valid ? (int)ptr[row] : 0, e = valid ? (int)ptr[row + 1] : 0;
         int l = s + gl;
+        // four links per lane and pass, their products summed plainly and
+        // then added to the compensated sums (kgroup_add)
         for (; l + 3 * SW < e; l += 4 * SW) {
             float c[4];
             uint32_t j[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) { c[u] = __ldcs(&coef[l + SW * u]); j[u] = __ldcs(&src[l + SW * u]) & kSrcMask; }
+            float t[K];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 float q[K];
                 load_q<K>(Q, j[u], q);
 #pragma unroll
-                for (int r = 0; r < K; r++) kmul_add(acc[r], c[u], q[r]);
+                for (int r = 0; r < K; r++) t[r] = u == 0 ? c[0] * q[r] : fmaf(c[u], q[r], t[r]);
             }
+#pragma unroll
+            for (int r = 0; r < K; r++) kgroup_add(acc[r], t[r]);
         }
         if (l < e) {
             // the rest of the row (fewer than 4 links per lane): every load
@@ -1216,15 +1230,20 @@ __global__ void k_spmv32(int64_t Nn, const int64_t *__restrict__ ptr, const uint
                 c[u] = ok ? __ldcs(&coef[l + SW * u]) : 0.f;
                 j[u] = ok ? (__ldcs(&src[l + SW * u]) & kSrcMask) : 0u;
             }
+            float t[K];
+#pragma unroll
+            for (int r = 0; r < K; r++) t[r] = 0.f;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 if (l + SW * u < e) {
                     float q[K];
                     load_q<K>(Q, j[u], q);
 #pragma unroll
-                    for (int r = 0; r < K; r++) kmul_add(acc[r], c[u], q[r]);
+                    for (int r = 0; r < K; r++) t[r] = fmaf(c[u], q[r], t[r]);
                 }
             }
+#pragma unroll
+            for (int r = 0; r < K; r++) kgroup_add(acc[r], t[r]);
         }
 #pragma unroll
         for (int r = 0; r < K; r++) {
@@ -1293,12 +1312,22 @@ __global__ void __launch_bounds__(256) k_spmv32_multi(const int32_t *__restrict_
         int s = (int)ptr[row], e = (int)ptr[row + 1];
         int l = s + li;
         if (slot_ok) {
+            // two links per slot and pass; from 16 columns on (issue bound)
+            // their products are summed plainly, then added to the
+            // compensated sums (kgroup_add), below that each is (kmul_add)
             for (; l + LPW < e; l += 2 * LPW) {
                 float c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
                 uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
                 float4 q0 = Q4[(int64_t)j0 * LPL + ri], q1 = Q4[(int64_t)j1 * LPL + ri];
-                kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
-                kmul_add(acc[0], c1, q1.x); kmul_add(acc[1], c1, q1.y); kmul_add(acc[2], c1, q1.z); kmul_add(acc[3], c1, q1.w);
+                if constexpr (K >= 16) {
+                    kgroup_add(acc[0], fmaf(c1, q1.x, c0 * q0.x));
+                    kgroup_add(acc[1], fmaf(c1, q1.y, c0 * q0.y));
+                    kgroup_add(acc[2], fmaf(c1, q1.z, c0 * q0.z));
+                    kgroup_add(acc[3], fmaf(c1, q1.w, c0 * q0.w));
+                } else {
+                    kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
+                    kmul_add(acc[0], c1, q1.x); kmul_add(acc[1], c1, q1.y); kmul_add(acc[2], c1, q1.z); kmul_add(acc[3], c1, q1.w);
+                }
             }
             if (l < e) {
                 float c0 = __ldcs(&coef[l]);
