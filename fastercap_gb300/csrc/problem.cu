@@ -775,8 +775,10 @@ __device__ __noinline__ double self_fp64(const float *c, const float *v) {
 
 // Mixed-precision near-field links: the analytic potential in FP32 in the
 // source triangle's scaled frame (fcg_pot_near32), one thread per listed
-// link; a link whose guard FP32 cannot decide takes the FP64 formula.
-__global__ void k_fill_near32(int64_t n, const int32_t *__restrict__ near_link, const int32_t *__restrict__ near_row,
+// link; a link whose guard FP32 cannot decide takes the FP64 formula. Held
+// to 64 registers (eight 128-thread CTAs per SM): the few spills cost less
+// than the occupancy they buy (sphere fill 0.86 -> 0.77 ms).
+__global__ void __launch_bounds__(128, 8) k_fill_near32(int64_t n, const int32_t *__restrict__ near_link, const int32_t *__restrict__ near_row,
                               const uint32_t *__restrict__ src, const NodeGeo *__restrict__ geo, const fcg_tri32 *__restrict__ tri,
                               float *__restrict__ c32, unsigned *status, unsigned long long *fb) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
