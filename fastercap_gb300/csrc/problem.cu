@@ -759,7 +759,7 @@ __global__ void k_fill_near(int64_t n, const int32_t *__restrict__ near_link, co
     }
 }
 
-__global__ void k_make_tri32(int64_t Nn, const NodeGeo *__restrict__ geo, fcg_tri32 *__restrict__ tri) {
+__global__ void __launch_bounds__(128, 8) k_make_tri32(int64_t Nn, const NodeGeo *__restrict__ geo, fcg_tri32 *__restrict__ tri) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nn; i += (int64_t)gridDim.x * blockDim.x)
         fcg_tri32_make(geo[i].v, geo[i].c, tri[i]);
 }
@@ -799,7 +799,7 @@ __global__ void __launch_bounds__(128, 8) k_fill_near32(int64_t n, const int32_t
 // Mixed-precision self terms: conductor leaves by the FP32 analytic potential
 // at the own centroid (FP64 where FP32 cannot decide a guard), dielectric
 // leaves by their closed form.
-__global__ void k_fill_self32(int64_t Np, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
+__global__ void __launch_bounds__(256, 4) k_fill_self32(int64_t Np, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
                               const fcg_tri32 *__restrict__ tri, const double *__restrict__ eb, const double *__restrict__ ea,
                               double *__restrict__ self, double *__restrict__ rself, unsigned *status, unsigned long long *fb) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
