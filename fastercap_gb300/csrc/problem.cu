@@ -642,7 +642,7 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const ui
 // slots of a per-band table (unused slots: the centroid with weight 0) that
 // some lane of its warp needs, so the lanes run the same code whatever
 // their links' bands; the point formula (band 4) uses the centroid offset.
-__global__ void __launch_bounds__(256) k_fill_far32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
+__global__ void __launch_bounds__(256, 5) k_fill_far32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
                                                     const NodeGeo *__restrict__ geo, float *__restrict__ c32, unsigned *status) {
     __shared__ float4 tab[5][6];  // [band][slot] = (weight of v0, of v1, of v2, quadrature weight)
     if (threadIdx.x < 30) {
@@ -1925,18 +1925,29 @@ __global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const
     int64_t base = ch.start[c];
     int len = ch.len[c];
     // four elements per thread, each its own subtraction chain (in basis
-    // order), so the loads of one vector for all four are in flight together
+    // order); the elements of four basis vectors are loaded before any of
+    // them is used, so one pass waits for memory once per four vectors
     const int U = kDotChunk / 256;
     double x[U];
     int64_t t0 = (int64_t)r * Np + base + threadIdx.x;
 #pragma unroll
     for (int u = 0; u < U; u++) x[u] = (threadIdx.x + u * 256 < len) ? w[t0 + u * 256] : 0.0;
-    for (int jv = 0; jv < nvec; jv++) {
-        const double hj = h[jv];
-        const double *vj = Vp[jv] + t0;
+    for (int j0 = 0; j0 < nvec; j0 += 4) {
+        double hv[4], vv[4][U];
 #pragma unroll
-        for (int u = 0; u < U; u++)
-            if (threadIdx.x + u * 256 < len) x[u] = x[u] - hj * vj[u * 256];
+        for (int q = 0; q < 4; q++) {
+            const bool okq = j0 + q < nvec;
+            hv[q] = okq ? h[j0 + q] : 0.0;
+            const double *vj = okq ? Vp[j0 + q] + t0 : NULL;
+#pragma unroll
+            for (int u = 0; u < U; u++) vv[q][u] = (okq && threadIdx.x + u * 256 < len) ? vj[u * 256] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (j0 + q < nvec)
+#pragma unroll
+                for (int u = 0; u < U; u++)
+                    if (threadIdx.x + u * 256 < len) x[u] = x[u] - hv[q] * vv[q][u];
     }
     double s2 = 0.0;
 #pragma unroll
