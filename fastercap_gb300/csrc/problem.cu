@@ -1752,12 +1752,17 @@ __device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ H
     hnorm[sidx] = hn;
     if (rhnorm) rhnorm[sidx] = 1.0 / hn;
     hc[i + 1] = hn;
+    // the previous rotations, in order; the running entry stays in a register
+    // so the loads of the next column entries and rotations do not wait on it
+    double carry = hc[0];
+#pragma unroll 8
     for (int j = 0; j < i; j++) {
-        double t1 = hc[j], t2 = hc[j + 1];
+        double t1 = carry, t2 = hc[j + 1];
         hc[j] = c[j] * t1 - sv[j] * t2;
-        hc[j + 1] = c[j] * t2 + sv[j] * t1;
+        carry = c[j] * t2 + sv[j] * t1;
     }
-    double t1 = hc[i], t2 = hc[i + 1];
+    hc[i] = carry;
+    double t1 = carry, t2 = hn;
     double len = sqrt(t1 * t1 + t2 * t2);
     c[i] = t1 / len;
     sv[i] = -t2 / len;
