@@ -35,6 +35,7 @@
 #include <math.h>
 #include <unistd.h>
 #include <chrono>
+#include <thread>
 
 #include "../csrc/fc_potential.h"
 #include "../csrc/fcg_internal.hpp"
@@ -76,6 +77,42 @@ inline D3 cross(D3 a, D3 b) { return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x *
 inline void store(float *dst, D3 a) { dst[0] = (float)a.x; dst[1] = (float)a.y; dst[2] = (float)a.z; }
 inline void normalize(D3 &a) { double m = mod(a); a.x /= m; a.y /= m; a.z /= m; }
 
+// The fields of a 'T' or 'Q' panel line as the reference's sscanf sequence
+// reads them (Parse3DInputFile, Solver/Autorefine.cpp:5030-5110): the
+// conductor name, the raw vertex coordinates and the optional reference
+// point. A pure function of the line's text, so large files are read on all
+// host threads before the (sequential) parse.
+struct PanelLine {
+    bool ok = false;
+    std::string name;
+    float v[12];
+    float ref[3];
+    bool uselocal = false;
+};
+
+static void parse_panel_fields(const char *line, PanelLine &o) {
+    const int nv = line[0] == 'T' ? 3 : 4;
+    char tmpname[kMaxLineLen];
+    tmpname[0] = 0;
+    int skip = 0;
+    const char *point = line + 1;
+    sscanf(point, "%s%n", tmpname, &skip);
+    point += skip;
+    for (int i = 0; i < nv; i++) {
+        float x = 0, y = 0, z = 0;
+        sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+        o.v[3 * i] = x;
+        o.v[3 * i + 1] = y;
+        o.v[3 * i + 2] = z;
+        point += skip;
+    }
+    float x, y, z;
+    o.uselocal = sscanf(point, "%f%f%f%n", &x, &y, &z, &skip) == 3;
+    if (o.uselocal) { o.ref[0] = x; o.ref[1] = y; o.ref[2] = z; }
+    o.name = tmpname;
+    o.ok = true;
+}
+
 // One physical input file, split the way fgets() with a 512-byte buffer splits
 // it; `eof` marks a final chunk without a newline (the reference's read loop
 // stops before processing such a chunk).
@@ -83,6 +120,7 @@ struct InFile {
     std::vector<std::string> lines;
     std::vector<bool> eof;
     std::map<std::string, size_t> sub;  // "File <name>" sections -> first line index
+    std::vector<PanelLine> panels;      // pre-read panel lines (large files), by line index
 };
 
 struct Builder {
@@ -128,6 +166,27 @@ struct Builder {
             F.eof.push_back(!nl && feof(f));
         }
         fclose(f);
+        // a large file's panel lines are read on all host threads
+        // (FCG_PARSE_THREADS caps the threads; 1 reads them during the parse)
+        const size_t kParallelLines = 20000;
+        int nt = (int)std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16);
+        if (const char *pt = getenv("FCG_PARSE_THREADS")) nt = std::max(1, std::min(nt, atoi(pt)));
+        if (F.lines.size() >= kParallelLines && nt > 1) {
+            F.panels.resize(F.lines.size());
+            std::vector<std::thread> th;
+            size_t per = (F.lines.size() + nt - 1) / nt;
+            for (int t = 0; t < nt; t++) {
+                size_t b = t * per, e = std::min(F.lines.size(), b + per);
+                if (b >= e) break;
+                th.emplace_back([&F, b, e]() {
+                    for (size_t i = b; i < e; i++) {
+                        char c = F.lines[i][0];
+                        if ((c == 'T' || c == 'Q') && !F.eof[i]) parse_panel_fields(F.lines[i].c_str(), F.panels[i]);
+                    }
+                });
+            }
+            for (auto &x : th) x.join();
+        }
         for (size_t i = 0; i < F.lines.size(); i++) {
             if (F.lines[i][0] == 'F') {
                 char t1[kMaxLineLen], t2[kMaxLineLen];
@@ -402,14 +461,16 @@ struct Builder {
                 }
             } else if (c0 == 'T' || c0 == 'Q') {
                 int nv = (c0 == 'T') ? 3 : 4;
-                const char *point = line + 1;
-                sscanf(point, "%s%n", tmpname, &skip);
-                point += skip;
+                PanelLine own;
+                const PanelLine *pl = (li < F->panels.size() && F->panels[li].ok) ? &F->panels[li] : NULL;
+                if (!pl) {
+                    parse_panel_fields(line, own);
+                    pl = &own;
+                }
                 float fv[12];
                 D3 qv[4];
                 for (int i = 0; i < nv; i++) {
-                    float x = 0, y = 0, z = 0;
-                    sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+                    float x = pl->v[3 * i], y = pl->v[3 * i + 1], z = pl->v[3 * i + 2];
                     if (nv == 3) {
                         fv[3 * i] = (float)((double)x + offset.x);
                         fv[3 * i + 1] = (float)((double)y + offset.y);
@@ -417,17 +478,14 @@ struct Builder {
                     } else {
                         qv[i] = add(d3(x, y, z), offset);
                     }
-                    point += skip;
                 }
-                float x, y, z;
                 double lref[3] = {0, 0, 0};
-                bool uselocal = false;
-                if (sscanf(point, "%f%f%f%n", &x, &y, &z, &skip) == 3) {
-                    lref[0] = (double)x + offset.x; lref[1] = (double)y + offset.y; lref[2] = (double)z + offset.z;
-                    uselocal = true;
+                bool uselocal = pl->uselocal;
+                if (uselocal) {
+                    lref[0] = (double)pl->ref[0] + offset.x; lref[1] = (double)pl->ref[1] + offset.y; lref[2] = (double)pl->ref[2] + offset.z;
                 }
                 std::string cname = groupname;
-                if (!isdiel) cname += tmpname;
+                if (!isdiel) cname += pl->name;
                 double refp[3] = {dielref.x, dielref.y, dielref.z};
                 if (nv == 4) {
                     // degenerate (collinear) quadrilaterals are skipped before any conductor is created

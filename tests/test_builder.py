@@ -57,3 +57,18 @@ def test_external_subfile(tmp_path):
     m = fc.Model.build(str(tmp_path / "main.txt"), mesh_eps=0.05)
     assert m.names == ["g1_s", "g2_s"]
     assert m.n_panels > 4
+
+
+def test_parallel_panel_read_matches_sequential(tmp_path, monkeypatch):
+    """A file of at least 20,000 lines has its panel lines read on all host
+    threads before the parse; the model is the same as with the sequential
+    read, array for array."""
+    from fastercap_gb300 import geometry as geo
+    path = tmp_path / "s5.txt"
+    geo.write_sphere(str(path), 5)  # 20,480 'T' lines
+    par = fc.Model.build(str(path), mesh_eps=1e30, eps_ratio=1e-33)
+    monkeypatch.setenv("FCG_PARSE_THREADS", "1")
+    seq = fc.Model.build(str(path), mesh_eps=1e30, eps_ratio=1e-33)
+    assert par.n_panels == seq.n_panels == 20480
+    for k in par.arrays:
+        np.testing.assert_array_equal(np.asarray(par.arrays[k]), np.asarray(seq.arrays[k]), err_msg=k)
