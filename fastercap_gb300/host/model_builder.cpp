@@ -88,6 +88,10 @@ struct PanelLine {
     float v[12];
     float ref[3];
     bool uselocal = false;
+    // a triangle's element geometry for a zero file offset (pre-read only)
+    bool geo = false;
+    Element e;
+    double cosmin = 0;
 };
 
 static void parse_panel_fields(const char *line, PanelLine &o) {
@@ -181,7 +185,16 @@ struct Builder {
                 th.emplace_back([&F, b, e]() {
                     for (size_t i = b; i < e; i++) {
                         char c = F.lines[i][0];
-                        if ((c == 'T' || c == 'Q') && !F.eof[i]) parse_panel_fields(F.lines[i].c_str(), F.panels[i]);
+                        if ((c == 'T' || c == 'Q') && !F.eof[i]) {
+                            PanelLine &pl = F.panels[i];
+                            parse_panel_fields(F.lines[i].c_str(), pl);
+                            if (c == 'T') {
+                                // the vertices exactly as a zero offset leaves them
+                                for (int k = 0; k < 9; k++) pl.e.v[k] = (float)((double)pl.v[k] + 0.0);
+                                pl.cosmin = geom_par(pl.e);
+                                pl.geo = true;
+                            }
+                        }
                     }
                 });
             }
@@ -267,10 +280,18 @@ struct Builder {
         return (sl[a] * sl[a] + sl[c] * sl[c] - sl[b] * sl[b]) / (2.0 * sl[a] * sl[c]);
     }
 
-    int create_panel(const float *vtx, int cond, uint8_t diel_index, bool uselocal, const double *localref, bool triangulated) {
+    // pre: the element's geometry computed ahead from the same vertices
+    int create_panel(const float *vtx, int cond, uint8_t diel_index, bool uselocal, const double *localref, bool triangulated,
+                     const Element *pre = NULL, double pre_cosmin = 0.0) {
         Element e;
-        memcpy(e.v, vtx, sizeof(e.v));
-        double cosmin = geom_par(e);
+        double cosmin;
+        if (pre) {
+            e = *pre;
+            cosmin = pre_cosmin;
+        } else {
+            memcpy(e.v, vtx, sizeof(e.v));
+            cosmin = geom_par(e);
+        }
         Conductor &C = conds[cond];
         if (C.is_diel) {
             const double *ref = uselocal ? localref : C.ref;
@@ -504,7 +525,8 @@ struct Builder {
                 }
                 uint8_t di = 0;
                 int cond = get_conductor(cname, isdiel, outperm, inperm, refp, &di);
-                if (nv == 3) ret = create_panel(fv, cond, di, uselocal, lref, false);
+                const bool zero_off = offset.x == 0.0 && offset.y == 0.0 && offset.z == 0.0;
+                if (nv == 3) ret = create_panel(fv, cond, di, uselocal, lref, false, (pl->geo && zero_off) ? &pl->e : NULL, pl->cosmin);
                 else ret = quad_panel(qv, cond, di, uselocal, lref);
                 if (ret != FC_NORMAL_END) break;
                 if (isdiel) raw_diel++; else raw_cond++;
