@@ -194,3 +194,31 @@ def test_true_residual_refinement(ctx):
     st = p.stats()
     assert st["refine_checks"] >= 1 and st["refine_cycles"] == 0
     assert np.max(np.abs(c - ref) / np.abs(ref)) < 1e-3
+
+
+def test_pinned_model_arrays_same_result(ctx):
+    """Problem creation from arrays in pinned host memory (link sources
+    uploaded in chunks, each relabelled as it arrives) gives the same
+    capacitance matrix and iteration counts as from ordinary memory (one
+    staged upload)."""
+    torch = pytest.importorskip("torch")
+    g = load_golden("crossing2x2_m05")
+    arrays = model_arrays(g)
+    pinned, keep = {}, []
+    for k, v in arrays.items():
+        a = np.ascontiguousarray(v)
+        t = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        view = t.numpy()[:a.nbytes].view(a.dtype).reshape(a.shape)
+        view[...] = a
+        pinned[k] = view
+        keep.append(t)
+    for prec in (fc.PREC_MIXED, fc.PREC_FP64):
+        p1 = ctx.problem(fc.Model.from_arrays(arrays), prec)
+        p1.fill()
+        c1, it1 = p1.solve(tol=1e-4)
+        p2 = ctx.problem(fc.Model.from_arrays(pinned), prec)
+        p2.fill()
+        c2, it2 = p2.solve(tol=1e-4)
+        np.testing.assert_array_equal(c1, c2)
+        np.testing.assert_array_equal(it1, it2)
+        np.testing.assert_array_equal(p1.coefficients()[0], p2.coefficients()[0])
