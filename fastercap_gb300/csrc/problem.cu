@@ -115,7 +115,7 @@ template <class T> static int upload(T **p, const T *h, size_t n, int64_t &bytes
 }
 
 // Host-to-device copies during problem creation. From pageable host memory
-// the driver stages a copy synchronously through its own buffers, and
+// the CUDA driver stages a copy synchronously through its own buffers, and
 // concurrent creations (the serving slots) queue on that path; a Stager
 // instead copies through two pinned buffers of the context, the host filling
 // one while the DMA of the other runs, so every creating thread streams at
