@@ -89,30 +89,40 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
+    PERIOD_S = 0.05
+
     def __init__(self, device: int):
         self.device = device
-        self.samples = []
+        self.samples = []  # (host time, fields)
         self.proc = None
+        self.t_start = self.t_end = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(int(self.PERIOD_S * 1000))],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the timed region starts once the sampler is live (at most 3 s)
+            t0 = time.perf_counter()
+            while not self.samples and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.005)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.t_start = time.perf_counter()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
-                self.samples.append(parts)
+                self.samples.append((time.perf_counter(), parts))
 
     def __exit__(self, *a):
+        self.t_end = time.perf_counter()
         if self.proc:
+            time.sleep(self.PERIOD_S * 1.5)  # the sample in flight at the end of the region
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -120,14 +130,19 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        """Samples taken inside the timed region and the first one after its
+        end (a region shorter than the sampling period still gets one)."""
+        inside = [p for t, p in self.samples if self.t_start <= t <= self.t_end]
+        after = [p for t, p in self.samples if self.t_end is not None and t > self.t_end]
+        use = inside + after[:1]
+        if not use:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in use if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in use if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for s in use for i in range(4) if s[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(use), "period_ms": int(self.PERIOD_S * 1000)}
 
 
 def peaks():
