@@ -26,7 +26,9 @@ BUILD = os.path.join(HERE, "_build")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
-REFERENCE = os.environ.get("FCG_REFERENCE_DIR", "/root/reference")
+# reference source tree for the oracle build: FCG_REFERENCE_DIR, else the
+# default location named by oracle/Makefile (the recipe that reads it)
+REFERENCE = os.environ.get("FCG_REFERENCE_DIR")
 # per-file device flags: the link construction and the mesh refinement round
 # every operation like the host builder (no fused multiply-add), so both take
 # the same decisions
@@ -91,8 +93,13 @@ def build(verbose: bool = False, reference: bool = True) -> None:
     if _newer(CLI, [cli_src, LIB]):
         _run_all([["g++", "-O2", "-std=c++17", cli_src, "-o", CLI, "-L" + HERE, "-lfastercap_gb300",
                    "-Wl,-rpath,$ORIGIN"]])
-    if reference and os.path.isdir(os.path.join(REFERENCE, "Solver")) and shutil.which("make"):
-        _run_all([["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + REFERENCE]])
+    if reference and shutil.which("make"):
+        oracle_dir = os.path.join(ROOT, "oracle")
+        ref = ["REF=" + REFERENCE] if REFERENCE else []
+        have = subprocess.run(["make", "-s", "-C", oracle_dir, "have-ref"] + ref,
+                              stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode == 0
+        if have:
+            _run_all([["make", "-s", "-C", oracle_dir, "-j8"] + ref])
 
 
 if __name__ == "__main__":

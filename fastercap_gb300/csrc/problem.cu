@@ -4391,10 +4391,11 @@ int problem_get_charges(DeviceProblem *p, double *charges) {
 // ------------------------------------------------------ no-allocation matvec
 //
 // Some callers cannot allocate device memory at the point where they need a
-// product: code recording a CUDA graph (an allocation would break the
-// capture), hosts that reserve all device memory at start-up and forbid
-// allocation afterwards, or hosts whose device memory belongs to another
-// allocator. For them, problem_matvec_noalloc runs the same kernels as
+// product: hosts that reserve all device memory at start-up and forbid
+// allocation afterwards (a simulator that has sized its memory pool to the
+// whole GPU), or hosts whose device memory belongs to another allocator that
+// would not see, and could not account for, a cudaMalloc made behind its
+// back. For them, problem_matvec_noalloc runs the same kernels as
 // problem_matvec_device with the node work arrays (charges, potentials,
 // ancestor sums) placed in this fixed, file-scope device array instead of the
 // problem's lazily allocated workspace. Every GPU that loads the library holds
@@ -4460,9 +4461,20 @@ int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int
     w.Ad = (double *)(base + 2 * align256(n * sizeof(double)));
     w.Qf = (float *)(base + 3 * align256(n * sizeof(double)));
     cudaStream_t s = p->stream;
+    // The link product reads the padding columns k..kp-1 of the charges,
+    // which the up-sweep never writes, and the array still holds whatever the
+    // last call (any problem, any precision) left there: bits that may not
+    // even be a finite number. Columns never mix, so they could not reach the
+    // result, but they are cleared anyway so that every value the kernels
+    // read is a finite charge (a memset allocates nothing).
+    if (kp > k) {
+        FCG_CK(cudaMemsetAsync(w.Qd, 0, n * sizeof(double), s));
+        if (p->precision == FCG_PREC_MIXED) FCG_CK(cudaMemsetAsync(w.Qf, 0, n * sizeof(float), s));
+    }
     r = launch_matvec(p, w, d_q, d_v, k, kp, NULL);
     if (r != FCG_NORMAL_END) return r;
     FCG_CK(cudaStreamSynchronize(s));
+    prof_collect(p);  // with profiling on, read back (and release) the link-product events
     return FCG_NORMAL_END;
 }
 

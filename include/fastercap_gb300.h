@@ -171,16 +171,19 @@ int fcg_problem_matvec(fcg_problem *p, const double *q, double *v, int k);
 int fcg_problem_matvec_device(fcg_problem *p, const double *d_q, double *d_v, int k);
 
 /* Same product as fcg_problem_matvec_device for callers that must not
- * allocate device memory when they call it: code recording a CUDA graph,
- * hosts that reserve all device memory up front, hosts whose device memory is
- * owned by another allocator. It calls no cudaMalloc, cudaFree or allocating
- * library routine; the node work arrays live in one fixed 32 MiB device array
- * per GPU (held until the process exits) instead of the problem's workspace.
+ * allocate device memory when they call it: hosts that reserve all device
+ * memory at start-up and forbid allocation afterwards, and hosts whose device
+ * memory is owned by another allocator that a cudaMalloc behind its back
+ * would break. It calls no cudaMalloc, cudaFree or allocating library
+ * routine; the node work arrays live in one fixed 32 MiB device array per GPU
+ * (held until the process exits) instead of the problem's workspace.
  * Limit: 8*3 + 4 (mixed) or 8*3 (FP64) bytes per node and padded right-hand
  * side must fit 32 MiB, else FCG_OUT_OF_MEMORY with a message. The first call
  * on a device resolves the array's address and should come before any stream
- * capture. All calls share the array: calls that overlap on the GPU race and
- * must be serialised by the caller. Returns after the product completes.
+ * capture. All calls share the array and it keeps the last call's contents
+ * (the padding columns the product reads are cleared on every call): calls
+ * that overlap on the GPU race and must be serialised by the caller. Runs on
+ * the problem's stream and returns after the product completes.
  * No counterpart in the reference (FasterCap never runs without allocation). */
 int fcg_problem_matvec_device_noalloc(fcg_problem *p, const double *d_q, double *d_v, int k);
 

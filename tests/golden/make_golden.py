@@ -18,7 +18,12 @@ oracle/_ref/fcref_dump on it and packs the dump into <case>.npz:
   ref_sup_*             (two-level cases) the reference's super elements,
                         leaf map, leaf areas and inverse super matrix
 
+Cases named pin_* are kept compact (hashes of the model arrays, a sample of
+the link coefficients; see PIN_CASES); auto_* cases come from the reference
+console's report.
+
 Usage: python tests/golden/make_golden.py [reference dir [case ...]]
+  (an empty reference dir "" takes FCG_REFERENCE_DIR or oracle/Makefile's default)
 """
 
 from __future__ import annotations
@@ -129,6 +134,69 @@ def convert(dump: str) -> dict:
     return out
 
 
+# cases at the sizes the benchmark configurations name, too large to commit in
+# full: the fixture keeps the counts, a SHA-256 of every model array in the C-ABI
+# layout, the self coefficients, every PIN_STRIDE-th link coefficient, one
+# seeded product, the GMRES iteration counts and the capacitance matrix
+PIN_CASES = {
+    # 2x2 crossing of 1x1x10 um bars at 3 um pitch, layers 1 um apart, vacuum;
+    # -m0.0018 gives 5,088 panels (the "about 5k panels" configuration)
+    "pin_crossing2x2_5k": (lambda: geo.crossing_2x2().text(), ["-m0.0018", "-t1e-4", "-pj", "-f0"]),
+    # sphere R = 1 m, icosahedron subdivided 5 times (20,480 triangles), mesh
+    # refinement off, link tolerance 1e-3
+    "pin_sphere_20480": (lambda: geo.sphere_text(5), ["-m1e30", "-d1e-33", "-t1e-4", "-pj", "-f0"]),
+}
+PIN_STRIDE = 97
+MODEL_KEYS = ("node_type", "node_left", "node_right", "node_leaf_first", "node_leaf_count", "node_vertices",
+              "node_centroid", "node_normal", "node_area", "node_maxside", "link_ptr", "link_src", "leaf_diel",
+              "cond_is_diel", "cond_leaf_first", "cond_leaf_count", "cond_outperm", "cond_inperm", "cond_surf_ptr",
+              "cond_surf_outperm")
+
+
+def array_sha256(a) -> str:
+    """SHA-256 of an array's dtype, shape and little-endian bytes (C order)."""
+    import hashlib
+    a = np.ascontiguousarray(a)
+    h = hashlib.sha256()
+    h.update(("%s|%s|" % (a.dtype.newbyteorder("<").str, ",".join(str(x) for x in a.shape))).encode())
+    h.update(a.astype(a.dtype.newbyteorder("<"), copy=False).tobytes())
+    return h.hexdigest()
+
+
+def compact(full: dict) -> dict:
+    out = {"model_sha256": np.array(["%s:%s" % (k, array_sha256(full[k])) for k in MODEL_KEYS])}
+    for k in ("cond_names", "ref_self_coef", "ref_mv_q", "ref_mv_v", "ref_cap", "ref_iterations", "ref_counts",
+              "ref_max_mesh_eps", "ref_max_level", "cond_is_diel"):
+        out[k] = full[k]
+    idx = np.arange(0, len(full["ref_link_coef"]), PIN_STRIDE, dtype=np.int64)
+    out["ref_link_coef_index"] = idx
+    out["ref_link_coef_sample"] = full["ref_link_coef"][idx]
+    return out
+
+
+def main_pin(ref_dir: str = "", only=()):
+    make_reference(ref_dir)
+    dump_bin = os.path.join(ROOT, "oracle", "_ref", "fcref_dump")
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (text_fn, switches) in PIN_CASES.items():
+            if only and name not in only:
+                continue
+            text = text_fn()
+            inp = os.path.join(tmp, name + ".txt")
+            with open(inp, "w") as f:
+                f.write(text)
+            dump = os.path.join(tmp, name + "_dump")
+            subprocess.run([dump_bin, dump, inp] + switches + ["--mv", "1"], check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            out = compact(convert(dump))
+            out["switches"] = np.array(switches)
+            import hashlib
+            out["input_sha256"] = np.array(hashlib.sha256(text.encode()).hexdigest())
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+            print("%-22s panels %6d nodes %6d links %8d iterations %s" % (
+                (name,) + tuple(out["ref_counts"]) + (list(out["ref_iterations"]),)))
+
+
 # automatic refinement runs of the reference console (-a<err>): per-iteration
 # panel and link counts and the final capacitance matrix, parsed from its report
 AUTO_CASES = {
@@ -155,8 +223,16 @@ def parse_report(text: str) -> dict:
             "ref_cap": np.array(caps[-1]), "ref_auto_iterations": np.array(len(caps))}
 
 
+def make_reference(ref_dir: str = ""):
+    """Build oracle/_ref from the reference tree: ref_dir, else FCG_REFERENCE_DIR,
+    else the default location oracle/Makefile names."""
+    ref = ref_dir or os.environ.get("FCG_REFERENCE_DIR", "")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8"] + (["REF=" + ref] if ref else []),
+                   check=True)
+
+
 def main_auto(ref_dir: str, only=()):
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + ref_dir], check=True)
+    make_reference(ref_dir)
     console = os.path.join(ROOT, "oracle", "_ref", "fcref")
     with tempfile.TemporaryDirectory() as tmp:
         for name, (text_fn, switches) in AUTO_CASES.items():
@@ -174,8 +250,8 @@ def main_auto(ref_dir: str, only=()):
             print("%-22s iterations %d, panels %s" % (name, int(out["ref_auto_iterations"]), list(out["ref_auto_panels"])))
 
 
-def main(ref_dir: str = "/root/reference", *only):
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "REF=" + ref_dir], check=True)
+def main(ref_dir: str = "", *only):
+    make_reference(ref_dir)
     dump_bin = os.path.join(ROOT, "oracle", "_ref", "fcref_dump")
     with tempfile.TemporaryDirectory() as tmp:
         for name, (text_fn, switches) in CASES.items():
@@ -197,7 +273,9 @@ def main(ref_dir: str = "/root/reference", *only):
 
 if __name__ == "__main__":
     args = sys.argv[1:]
-    if args[1:] and all(a.startswith("auto_") for a in args[1:]):
+    if args[1:] and all(a.startswith("pin_") for a in args[1:]):
+        main_pin(args[0], args[1:])
+    elif args[1:] and all(a.startswith("auto_") for a in args[1:]):
         main_auto(args[0], args[1:])
     else:
         main(*args)

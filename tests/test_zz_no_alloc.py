@@ -1,8 +1,8 @@
 """The no-allocation matrix-vector product (fcg_problem_matvec_device_noalloc).
 
-Callers that cannot allocate device memory when they multiply - code being
-recorded into a CUDA graph, hosts that reserve all device memory at start-up,
-hosts whose device memory belongs to another allocator - use this entry point.
+Callers that cannot allocate device memory when they multiply - hosts that
+reserve all device memory at start-up, hosts whose device memory belongs to
+another allocator - use this entry point.
 It must give the same result as fcg_problem_matvec_device (same kernels, so
 the FP64 tolerance 1e-13 relative norm and the mixed 2e-6 both hold with
 room), call after call, and refuse models too large for its fixed 32 MiB
@@ -58,8 +58,13 @@ def test_noalloc_rejects_models_beyond_its_scratch(tmp_path):
     torch = pytest.importorskip("torch")
     from fastercap_gb300 import geometry as geo
     path = tmp_path / "sphere.txt"
-    geo.write_sphere(str(path), 6)  # 163,839 nodes: 8 right-hand sides need ~31 MB of doubles + floats
+    geo.write_sphere(str(path), 6)  # 163,839 nodes
     m = fc.Model.build(str(path), mesh_eps=1e30, eps_ratio=1e-32)
+    # 8 right-hand sides, mixed: 3 double + 1 float arrays of nodes x 8 values
+    # = 163,839 x 8 x 28 bytes = 36.7 MB, above the 32 MiB scratch
+    need = m.n_nodes * 8 * (3 * 8 + 4)
+    assert need > (32 << 20), "the case no longer exceeds the scratch; pick a larger model"
+
     with fc.Context(0) as ctx:
         p = ctx.problem(m, fc.PREC_MIXED)
         p.fill()
