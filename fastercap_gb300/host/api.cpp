@@ -550,6 +550,13 @@ static int run_command_line_impl(const char *command_line) {
         return FCG_COMMAND_LINE_ERROR;
     }
     if (o.galerkin) { printf("Error: the Galerkin scheme (-g) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
+    // the refined-geometry and charge-density list files of
+    // CAutoRefine::OutputFastCapFile (Solver/Autorefine.cpp:1230-1565) are not
+    // written by this solver: refuse the switches rather than drop the files
+    if (o.out_geo || o.dump_input || o.out_charge || o.keep_charge) {
+        printf("Error: the geometry and charge list files (-o, -oi, -c, -kc) are not written by the GPU solver\n");
+        return FCG_COMMAND_LINE_ERROR;
+    }
     if (o.precond & (2 | 8)) {
         printf("Error: the block (-pb) and hierarchical (-ph) preconditioners are not supported by the GPU solver\n");
         return FCG_COMMAND_LINE_ERROR;

@@ -154,6 +154,15 @@ def test_cli_two_level_switch_parsed(tmp_path):
     assert fc.run_command_line("fastercap_gb300 %s -ps" % inp) == fc.COMMAND_LINE_ERROR
 
 
+@pytest.mark.parametrize("switch", ["-o", "-oi", "-c", "-kc"])
+def test_cli_refuses_list_file_outputs(tmp_path, switch, capfd):
+    """The refined-geometry and charge list files are not written by this
+    solver: their switches are a command-line error, not silently dropped."""
+    inp = write(tmp_path, "one.txt", ONE_TRIANGLE)
+    assert fc.run_command_line("fastercap_gb300 %s %s" % (inp, switch)) == fc.COMMAND_LINE_ERROR
+    assert "not written by the GPU solver" in capfd.readouterr().out
+
+
 @pytest.mark.gpu
 def test_cli_two_level_runs(tmp_path, capfd):
     g = load_golden("crossing2x2_m02_ps64")
