@@ -532,8 +532,8 @@ done:
     return iteration;
 }
 
-int orc_solve_ex(const orc_model *m, const double *coef, const double *self, double tol, int pc, unsigned super_dim,
-                 double *cap, int *iterations, double *charges, int threads) {
+int orc_solve_rows(const orc_model *m, const double *coef, const double *self, double tol, int pc, unsigned super_dim,
+                   int row_first, int row_count, double *cap, int *iterations, double *charges, int threads) {
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
 #else
@@ -548,29 +548,38 @@ int orc_solve_ex(const orc_model *m, const double *coef, const double *self, dou
     if (pc == 2 && orc_super_build(m, super_dim, &sp) == 0) pc = 0;  /* too many roots: no preconditioner */
     int32_t c, c2;
     for (c = 0; c < m->n_conductors; c++) ncol += m->cond_is_diel[c] ? 0 : 1;
+    if (row_count < 0) row_count = ncol;
+    int out = 0;  /* rows written so far */
     for (c = 0; c < m->n_conductors; c++) {
         int64_t j;
         int capped, col = 0;
         if (m->cond_is_diel[c]) continue;
+        if (row < row_first || row >= row_first + row_count) { row++; continue; }
         for (j = m->cond_leaf_first[c]; j < m->cond_leaf_first[c] + m->cond_leaf_count[c]; j++) b[j] = 1.0;
         int it = gmres(m, coef, self, &sp, b, x, tol, pc, &capped, chg, pot);
         any_capped |= capped;
-        if (iterations) iterations[row] = it + 1;
-        if (charges) memcpy(charges + (size_t)row * n, x, sizeof(double) * (size_t)n);
+        if (iterations) iterations[out] = it + 1;
+        if (charges) memcpy(charges + (size_t)out * n, x, sizeof(double) * (size_t)n);
         for (c2 = 0; c2 < m->n_conductors; c2++) {
             double acc = 0.0;
             if (m->cond_is_diel[c2]) continue;
             for (j = m->cond_leaf_first[c2]; j < m->cond_leaf_first[c2] + m->cond_leaf_count[c2]; j++)
                 acc += m->cond_surf_outperm[m->cond_surf_ptr[c2] + m->leaf_diel[j]] * x[j];
-            cap[(size_t)row * ncol + col] = acc;
+            cap[(size_t)out * ncol + col] = acc;
             col++;
         }
         for (j = m->cond_leaf_first[c]; j < m->cond_leaf_first[c] + m->cond_leaf_count[c]; j++) b[j] = 0.0;
         row++;
+        out++;
     }
     free(b); free(x); free(chg); free(pot);
     orc_super_free(&sp);
     return any_capped;
+}
+
+int orc_solve_ex(const orc_model *m, const double *coef, const double *self, double tol, int pc, unsigned super_dim,
+                 double *cap, int *iterations, double *charges, int threads) {
+    return orc_solve_rows(m, coef, self, tol, pc, super_dim, 0, -1, cap, iterations, charges, threads);
 }
 
 int orc_solve(const orc_model *m, const double *coef, const double *self, double tol, int pc, double *cap, int *iterations,

@@ -67,6 +67,16 @@ void orc_super_free(orc_super *s);
 int orc_solve_ex(const orc_model *m, const double *link_coef, const double *self_coef, double tol, int precond,
                  unsigned super_dim, double *cap, int *iterations, double *charges, int threads);
 
+/* orc_solve_ex for the rows row_first .. row_first + row_count - 1 of the
+ * matrix only (the right-hand sides of those conductors, in solver order;
+ * row_count < 0: all): cap receives row_count rows of the full width,
+ * iterations and charges one entry per solved row. The reference solves its
+ * conductors one after another (Solver/SolveCapacitance.cpp:1138-1425), so
+ * the time of a few rows is a fixed share of a whole solve. */
+int orc_solve_rows(const orc_model *m, const double *link_coef, const double *self_coef, double tol, int precond,
+                   unsigned super_dim, int row_first, int row_count, double *cap, int *iterations, double *charges,
+                   int threads);
+
 #ifdef __cplusplus
 }
 #endif

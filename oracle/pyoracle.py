@@ -60,6 +60,8 @@ def lib():
         L.orc_matvec.restype = None
         L.orc_solve.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_double, C.c_int, vp, vp, vp, C.c_int]
         L.orc_solve_ex.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_double, C.c_int, C.c_uint, vp, vp, vp, C.c_int]
+        L.orc_solve_rows.argtypes = [C.POINTER(OrcModel), vp, vp, C.c_double, C.c_int, C.c_uint, C.c_int, C.c_int, vp, vp,
+                                     vp, C.c_int]
         L.orc_super_build.argtypes = [C.POINTER(OrcModel), C.c_uint, C.POINTER(OrcSuper)]
         L.orc_super_free.argtypes = [C.POINTER(OrcSuper)]
         L.orc_super_free.restype = None
@@ -125,3 +127,16 @@ class Oracle:
         capped = lib().orc_solve_ex(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, tol, precond, super_dim,
                                     cap.ctypes.data, it.ctypes.data, ch.ctypes.data, self.threads)
         return cap, it, ch, bool(capped)
+
+    def solve_rows(self, row_first, row_count, tol=0.01, precond=1, coef=None, self_coef=None, super_dim=0):
+        """Rows row_first .. row_first + row_count - 1 of the capacitance
+        matrix (those conductors' solves only): (rows, iterations)."""
+        coef = self.coef if coef is None else np.ascontiguousarray(coef, np.float64)
+        sc = self.self_coef if self_coef is None else np.ascontiguousarray(self_coef, np.float64)
+        nc = int((self.a["cond_is_diel"] == 0).sum())
+        row_count = max(0, min(row_count, nc - row_first))
+        cap = np.empty((row_count, nc), np.float64)
+        it = np.empty(max(1, row_count), np.int32)
+        lib().orc_solve_rows(C.byref(self.s), coef.ctypes.data, sc.ctypes.data, tol, precond, super_dim, row_first,
+                             row_count, cap.ctypes.data, it.ctypes.data, None, self.threads)
+        return cap, it[:row_count]

@@ -74,3 +74,16 @@ def test_two_level_disabled_with_many_conductors(tmp_path):
     c0, i0, _, _ = o.solve(1e-3, 0)
     np.testing.assert_array_equal(c2, c0)
     np.testing.assert_array_equal(i2, i0)
+
+
+def test_solve_rows_equal_full_solve():
+    """A few rows of the matrix (those conductors' solves alone) equal the
+    same rows of the full solve."""
+    g = load_golden("random3")
+    o = Oracle(model_arrays(g))
+    o.fill()
+    tol, precond = solve_params(g)
+    cap, it, _, _ = o.solve(tol, precond)
+    rows, rit = o.solve_rows(1, 2, tol, precond)
+    np.testing.assert_array_equal(rows, cap[1:3])
+    np.testing.assert_array_equal(rit, it[1:3])
