@@ -80,7 +80,8 @@ class ModelInfo(C.Structure):
 class ProblemStats(C.Structure):
     _fields_ = [("kernel_launches", C.c_int64), ("link_launches", C.c_int64), ("link_ms", C.c_double),
                 ("link_bytes", C.c_int64), ("fill_ms", C.c_double), ("solve_ms", C.c_double),
-                ("refine_checks", C.c_int64), ("refine_cycles", C.c_int64), ("fill_fp64", C.c_int64)]
+                ("refine_checks", C.c_int64), ("refine_cycles", C.c_int64), ("fill_fp64", C.c_int64),
+                ("rhs_width", C.c_int64)]
 
 
 class SolveOptions(C.Structure):
@@ -96,7 +97,8 @@ class JobInfo(C.Structure):
     _fields_ = [("state", C.c_int), ("status", C.c_int), ("n_cond", C.c_int), ("iterations_max", C.c_int),
                 ("slot", C.c_int), ("footprint_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("queue_ms", C.c_double), ("run_ms", C.c_double), ("fill_ms", C.c_double), ("solve_ms", C.c_double),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("build_ms", C.c_double), ("n_panels", C.c_int64),
+                ("n_links", C.c_int64)]
 
 
 class ServerStats(C.Structure):
@@ -173,6 +175,9 @@ def lib() -> C.CDLL:
     L.fcg_server_destroy.argtypes = [vp]
     L.fcg_server_destroy.restype = None
     L.fcg_server_submit.argtypes = [vp, C.POINTER(ModelArrays), C.c_int, C.POINTER(SolveOptions), C.POINTER(i64)]
+    L.fcg_server_submit_file.argtypes = [vp, C.c_char_p, C.POINTER(BuildOptions), C.c_int, C.POINTER(SolveOptions),
+                                         C.POINTER(i64)]
+    L.fcg_server_wait.argtypes = [vp, i64, C.POINTER(JobInfo)]
     L.fcg_server_poll.argtypes = [vp, i64, C.POINTER(JobInfo)]
     L.fcg_server_result.argtypes = [vp, i64, vp, vp, C.POINTER(JobInfo)]
     L.fcg_server_cancel.argtypes = [vp, i64]
@@ -515,12 +520,19 @@ def estimate_bytes(model: Model, precision: int = PREC_MIXED, rhs: int = 0, iter
 class Job:
     """A submitted extraction; result() waits for it."""
 
-    def __init__(self, server: "Server", jid: int, model: Model, arrays: ModelArrays):
+    def __init__(self, server: "Server", jid: int, model, arrays):
         self.server, self.id, self.model = server, jid, model
         self._arrays = arrays  # the C view must outlive the job
-        self.n_cond = len(model.conductor_names)
+        # a file job's matrix size is known once it is done
+        self.n_cond = len(model.conductor_names) if model is not None else None
         self.info = None
         self.status = None
+
+    def wait(self) -> dict:
+        """Block until the job is done or cancelled; its description."""
+        info = JobInfo()
+        _check(lib().fcg_server_wait(self.server._h, self.id, C.byref(info)), "wait")
+        return {f: getattr(info, f) for f, _ in JobInfo._fields_}
 
     def poll(self) -> dict:
         info = JobInfo()
@@ -532,6 +544,8 @@ class Job:
 
     def result(self, allow_not_converged=False):
         """(C, iterations); raises FCError if the job failed or was cancelled."""
+        if self.n_cond is None:
+            self.n_cond = int(self.wait()["n_cond"])
         cap = np.empty((self.n_cond, self.n_cond), np.float64)
         it = np.empty(self.n_cond, np.int32)
         info = JobInfo()
@@ -563,6 +577,18 @@ class Server:
         _check(lib().fcg_server_submit(self._h, C.byref(arr), precision, C.byref(opt), C.byref(jid)), "submit")
         job = Job(self, jid.value, model, (arr, keep))
         return job
+
+    def submit_file(self, path: str, precision: int = PREC_MIXED, tol: float = 0.01, mesh_eps: float = 0.1,
+                    eps_ratio: float = 1.0, mesh_curv: float = 3.0, precond: int = PRECOND_JACOBI, max_iter: int = 0,
+                    rhs_width: int = 0, precond_dim: int = 0, refine: int = 0) -> Job:
+        """An extraction request from an input file: the slot builds its
+        model on the GPU (switches -m, -d, -mc), then solves it."""
+        bo = BuildOptions(mesh_eps, eps_ratio, mesh_curv, 0)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
+        jid = C.c_int64()
+        _check(lib().fcg_server_submit_file(self._h, os.fsencode(path), C.byref(bo), precision, C.byref(opt),
+                                            C.byref(jid)), "submit_file")
+        return Job(self, jid.value, None, None)
 
     def stats(self) -> dict:
         st = ServerStats()

@@ -57,6 +57,10 @@ __global__ void __launch_bounds__(128) k_mesh_decide(int64_t n, const int2 *__re
                                                      double max_side, double max_area, uint8_t *flag, uint8_t *split,
                                                      unsigned long long *max_eps_bits, int *max_level, unsigned *too_deep) {
     int lvl_max = 0;
+    // largest weight of the pairs this thread kept, as the bits of a
+    // non-negative double (their order is the values' order); one atomic per
+    // warp at the end instead of one per pair on a single word
+    unsigned long long eps_max = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int2 pr = pairs[i];
         uint16_t m = meta[i];
@@ -76,12 +80,18 @@ __global__ void __launch_bounds__(128) k_mesh_decide(int64_t n, const int2 *__re
             if (el[x].type & FCG_IS_LEAF) split[x] = 1;  // many pairs may mark the same leaf
         } else {
             // the largest weight of a pair that needed no refinement (weights are >= 0)
-            if (!(A.type & FCG_IS_SUPER_NODE) && c1 == c1) atomicMax(max_eps_bits, (unsigned long long)__double_as_longlong(c1));
-            if (!(B.type & FCG_IS_SUPER_NODE) && c2 == c2) atomicMax(max_eps_bits, (unsigned long long)__double_as_longlong(c2));
+            if (!(A.type & FCG_IS_SUPER_NODE) && c1 == c1) eps_max = max(eps_max, (unsigned long long)__double_as_longlong(c1));
+            if (!(B.type & FCG_IS_SUPER_NODE) && c2 == c2) eps_max = max(eps_max, (unsigned long long)__double_as_longlong(c2));
         }
     }
-    for (int o = 16; o > 0; o >>= 1) lvl_max = max(lvl_max, __shfl_xor_sync(0xffffffffu, lvl_max, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(max_level, lvl_max);
+    for (int o = 16; o > 0; o >>= 1) {
+        lvl_max = max(lvl_max, __shfl_xor_sync(0xffffffffu, lvl_max, o));
+        eps_max = max(eps_max, __shfl_xor_sync(0xffffffffu, eps_max, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(max_level, lvl_max);
+        if (eps_max) atomicMax(max_eps_bits, eps_max);
+    }
 }
 
 // bisect the marked leaves into ids ne + 2 rank, ne + 2 rank + 1; the pair of

@@ -31,6 +31,13 @@ double now_ms() {
 
 struct Job {
     int64_t id = 0;
+    // file jobs: the slot builds the model from the input file first
+    bool from_file = false;
+    std::string path;
+    fcg_build_options bopt;
+    fcg_model *model = nullptr;  // built by the slot, freed with the job's problem
+    double build_ms = 0;
+    bool admitted = false;  // footprint counted in the server's in_use
     fcg_model_arrays a;
     int precision = FCG_PREC_MIXED;
     fcg_solve_options opt;
@@ -58,6 +65,7 @@ struct fcg_server {
     int64_t budget = 0, in_use = 0, peak_in_use = 0;
     int iterations_hint = 64;
     int running = 0, max_running = 0;
+    int solving = 0;  // running jobs whose footprint is counted in in_use
     int64_t next_id = 1, submitted = 0, completed = 0;
     bool stop = false;
     std::mutex mu;
@@ -68,15 +76,57 @@ struct fcg_server {
     std::vector<void *> streams;
 };
 
+// The head job takes a free slot once its footprint fits next to the
+// footprints already admitted (or nothing holds memory). A file job's
+// footprint is known only after its model is built: it takes the slot at
+// once, builds, and then waits in run_job for the same memory rule.
 static bool can_admit(const fcg_server *s) {
     if (s->queue.empty()) return false;
     const Job *j = s->queue.front();
-    return s->running == 0 || s->in_use + j->footprint <= s->budget;
+    return j->from_file || s->solving == 0 || s->in_use + j->footprint <= s->budget;
+}
+
+static int count_conductors(const fcg_model_arrays &a) {
+    int n = 0;
+    for (int32_t c = 0; c < a.n_conductors; c++) n += (a.cond_is_diel && a.cond_is_diel[c]) ? 0 : 1;
+    return n;
+}
+
+// build a file job's model on the server's GPU (mesh refinement and link
+// construction on the device), then wait until its footprint may be admitted
+static int build_file_job(fcg_server *s, Job *j) {
+    double t0 = now_ms();
+    fcg_context handle;
+    handle.dev = s->ctx;
+    char ebuf[512] = {0};
+    int r = fcg_model_build_on(&handle, j->path.c_str(), &j->bopt, &j->model, ebuf, sizeof ebuf);
+    j->build_ms = now_ms() - t0;
+    if (r != FCG_NORMAL_END) {
+        j->error = ebuf[0] ? std::string(ebuf) : fcg::get_error();
+        return r;
+    }
+    fcg_model_arrays_get(j->model, &j->a);
+    j->n_cond = count_conductors(j->a);
+    j->footprint = fcg::problem_estimate_bytes(j->a, j->precision, j->n_cond, s->iterations_hint);
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_admit.wait(lk, [&] { return j->cancel || s->solving == 0 || s->in_use + j->footprint <= s->budget; });
+    if (j->cancel) {
+        j->footprint = 0;
+        j->error = "job cancelled before its solve";
+        return FCG_USER_BREAK;
+    }
+    s->in_use += j->footprint;
+    s->peak_in_use = std::max(s->peak_in_use, s->in_use);
+    s->solving++;
+    j->admitted = true;
+    return FCG_NORMAL_END;
 }
 
 static void run_job(fcg_server *s, Job *j, void *stream) {
     fcg::DeviceProblem *p = nullptr;
-    int r = fcg::problem_create(*s->ctx, j->a, j->precision, stream, &p);
+    int r = FCG_NORMAL_END;
+    if (j->from_file) r = build_file_job(s, j);
+    if (r == FCG_NORMAL_END) r = fcg::problem_create(*s->ctx, j->a, j->precision, stream, &p);
     if (r == FCG_NORMAL_END) {
         std::lock_guard<std::mutex> lk(s->mu);
         j->prob = p;
@@ -101,8 +151,12 @@ static void run_job(fcg_server *s, Job *j, void *stream) {
         }
         fcg::problem_destroy(p);
     }
+    if (j->model) {
+        fcg_model_free(j->model);
+        j->model = nullptr;
+    }
     j->status = r;
-    if (r != FCG_NORMAL_END) j->error = fcg::get_error();
+    if (r != FCG_NORMAL_END && j->error.empty()) j->error = fcg::get_error();
 }
 
 static void worker(fcg_server *s, int slot) {
@@ -114,8 +168,12 @@ static void worker(fcg_server *s, int slot) {
             if (s->stop) return;
             j = s->queue.front();
             s->queue.pop_front();
-            s->in_use += j->footprint;
-            s->peak_in_use = std::max(s->peak_in_use, s->in_use);
+            if (!j->from_file) {
+                s->in_use += j->footprint;
+                s->peak_in_use = std::max(s->peak_in_use, s->in_use);
+                s->solving++;
+                j->admitted = true;
+            }
             s->running++;
             s->max_running = std::max(s->max_running, s->running);
             j->state = FCG_JOB_RUNNING;
@@ -125,7 +183,11 @@ static void worker(fcg_server *s, int slot) {
         run_job(s, j, s->streams[slot]);
         {
             std::lock_guard<std::mutex> lk(s->mu);
-            s->in_use -= j->footprint;
+            // a file job that failed or was cancelled while building holds no memory
+            if (j->admitted) {
+                s->in_use -= j->footprint;
+                s->solving--;
+            }
             s->running--;
             s->completed++;
             j->t_end = now_ms();
@@ -153,6 +215,9 @@ static void fill_info(const Job *j, fcg_job_info *info) {
     info->fill_ms = j->fill_ms;
     info->solve_ms = j->solve_ms;
     info->kernel_launches = j->launches;
+    info->build_ms = j->build_ms;
+    info->n_panels = j->a.n_panels;
+    info->n_links = j->a.n_links;
 }
 
 extern "C" {
@@ -204,14 +269,13 @@ void fcg_server_destroy(fcg_server *s) {
     delete s;
 }
 
-int fcg_server_submit(fcg_server *s, const fcg_model_arrays *a, int precision, const fcg_solve_options *opt, int64_t *job) {
-    if (!s || !a || !job) return FCG_GENERIC_ERROR;
+static Job *new_job(int precision, const fcg_solve_options *opt) {
     if (precision != FCG_PREC_FP64 && precision != FCG_PREC_MIXED) {
         fcg::set_error("unknown precision");
-        return FCG_GENERIC_ERROR;
+        return nullptr;
     }
     Job *j = new Job();
-    j->a = *a;
+    memset(&j->a, 0, sizeof j->a);
     j->precision = precision;
     j->opt.tol = 0.01;
     j->opt.precond = FCG_PRECOND_JACOBI;
@@ -220,8 +284,10 @@ int fcg_server_submit(fcg_server *s, const fcg_model_arrays *a, int precision, c
     j->opt.precond_dim = 0;
     j->opt.refine = 0;
     if (opt) j->opt = *opt;
-    for (int32_t c = 0; c < a->n_conductors; c++) j->n_cond += (a->cond_is_diel && a->cond_is_diel[c]) ? 0 : 1;
-    j->footprint = fcg::problem_estimate_bytes(*a, precision, j->n_cond, s->iterations_hint);
+    return j;
+}
+
+static int enqueue(fcg_server *s, Job *j, int64_t *job) {
     j->t_submit = now_ms();
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -237,6 +303,45 @@ int fcg_server_submit(fcg_server *s, const fcg_model_arrays *a, int precision, c
         *job = j->id;
     }
     s->cv_admit.notify_one();
+    return FCG_NORMAL_END;
+}
+
+int fcg_server_submit(fcg_server *s, const fcg_model_arrays *a, int precision, const fcg_solve_options *opt, int64_t *job) {
+    if (!s || !a || !job) return FCG_GENERIC_ERROR;
+    Job *j = new_job(precision, opt);
+    if (!j) return FCG_GENERIC_ERROR;
+    j->a = *a;
+    j->n_cond = count_conductors(*a);
+    j->footprint = fcg::problem_estimate_bytes(*a, precision, j->n_cond, s->iterations_hint);
+    return enqueue(s, j, job);
+}
+
+int fcg_server_submit_file(fcg_server *s, const char *path, const fcg_build_options *bopt, int precision,
+                           const fcg_solve_options *opt, int64_t *job) {
+    if (!s || !path || !job) return FCG_GENERIC_ERROR;
+    Job *j = new_job(precision, opt);
+    if (!j) return FCG_GENERIC_ERROR;
+    j->from_file = true;
+    j->path = path;
+    j->bopt.mesh_eps = 0.1;
+    j->bopt.eps_ratio = 1.0;
+    j->bopt.mesh_curv = 3.0;
+    j->bopt.verbose = 0;
+    if (bopt) j->bopt = *bopt;
+    return enqueue(s, j, job);
+}
+
+int fcg_server_wait(fcg_server *s, int64_t job, fcg_job_info *info) {
+    if (!s) return FCG_GENERIC_ERROR;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job);
+    if (it == s->jobs.end()) {
+        fcg::set_error("unknown job");
+        return FCG_GENERIC_ERROR;
+    }
+    Job *j = it->second;
+    s->cv_done.wait(lk, [&] { return j->state == FCG_JOB_DONE || j->state == FCG_JOB_CANCELLED; });
+    fill_info(j, info);
     return FCG_NORMAL_END;
 }
 

@@ -192,7 +192,8 @@ typedef struct {
     double tol;       /* -t GMRES relative residual tolerance (default 0.01) */
     int precond;      /* FCG_PRECOND_NONE, FCG_PRECOND_JACOBI or FCG_PRECOND_TWO_LEVEL */
     int max_iter;     /* 0: the reference's cap min(1000, n_panels) */
-    int rhs_width;    /* right-hand sides per batched solve: 0 = up to 32, 1 = one at a time */
+    int rhs_width;    /* right-hand sides per batched solve: 0 = chosen by measurement (mixed problems of
+                         at least 4M links; else all conductors, at most 32), 1 = one at a time */
     int precond_dim;  /* two-level dimension (the number of -ps<dim>), clamped to [16, 4096]; 0 = 128 */
     int refine;       /* restarts from the current solution while the true residual |b - A x| / |b| is
                          at or above tol: 0 = default (up to 2 for FCG_PREC_MIXED, none for FP64),
@@ -250,6 +251,8 @@ typedef struct {
     int64_t refine_cycles;    /* GMRES restarts those checks caused */
     int64_t fill_fp64;        /* last mixed fill: near-field and self coefficients computed by the FP64
                                * formula because FP32 could not decide one of its guards */
+    int64_t rhs_width;        /* right-hand sides per batched solve in the last solve (chosen by
+                               * measurement when fcg_solve_options.rhs_width is 0) */
 } fcg_problem_stats;
 int fcg_problem_set_profiling(fcg_problem *p, int enable);
 int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *stats);
@@ -288,6 +291,8 @@ typedef struct {
     double run_ms;          /* admission -> result (host clock) */
     double fill_ms, solve_ms;  /* device time of fill and solve (CUDA events) */
     int64_t kernel_launches;   /* kernels the library launched for the job */
+    double build_ms;           /* file jobs: model construction (host clock), part of run_ms */
+    int64_t n_panels, n_links; /* size of the job's model */
 } fcg_job_info;
 
 typedef struct {
@@ -303,6 +308,19 @@ int fcg_server_create(fcg_context *ctx, const fcg_server_config *cfg, fcg_server
 void fcg_server_destroy(fcg_server *s);
 int fcg_server_submit(fcg_server *s, const fcg_model_arrays *arrays, int precision, const fcg_solve_options *opt,
                       int64_t *job);
+/* An extraction request as FasterCap receives one: an input file and the
+ * mesh/link switches (-m, -d, -mc). The slot that takes the job builds the
+ * model on the server's GPU (fcg_model_build_on: the same model as the
+ * reference's ReadFastCapFile + AutoRefinePanels + AutoRefineLinks,
+ * Solver/Autorefine.cpp:4568, 293, 481-728), then waits until the model's
+ * footprint fits the memory budget (or nothing else holds memory) and
+ * solves it like fcg_server_submit's jobs. The file is read when the job
+ * starts. The job's matrix size is known once it is done (fcg_server_wait). */
+int fcg_server_submit_file(fcg_server *s, const char *path, const fcg_build_options *build, int precision,
+                           const fcg_solve_options *opt, int64_t *job);
+/* wait until the job is done or cancelled and describe it, keeping its
+ * result for fcg_server_result */
+int fcg_server_wait(fcg_server *s, int64_t job, fcg_job_info *info);
 /* state and timings without waiting */
 int fcg_server_poll(fcg_server *s, int64_t job, fcg_job_info *info);
 /* wait until the job is done or cancelled, copy its matrix (n_cond^2 values)

@@ -132,3 +132,53 @@ def test_failed_job_does_not_stop_the_server(ctx, models):
         assert jobs[1].info["state"] == fc.JOB_DONE and jobs[1].info["status"] == fc.GENERIC_ERROR
         jobs[2].result()
         assert srv.stats()["completed"] == 3
+
+
+def test_file_jobs_equal_model_jobs(ctx, tmp_path):
+    """A request given as an input file (the slot builds its model on the GPU)
+    gives the matrix of the same model submitted built, bit for bit, alone
+    and in a mix with model jobs; a missing file fails alone with the
+    builder's status."""
+    paths, built = [], []
+    for r in range(4):
+        path = tmp_path / ("req%d.txt" % r)
+        geo.random_crossing(100 + r, kmin=2, kmax=5).write(str(path))
+        paths.append(str(path))
+        built.append(fc.Model.build(str(path), mesh_eps=0.02, eps_ratio=2.0))
+    with ctx.server(slots=3) as srv:
+        ref = [srv.submit(m, fc.PREC_MIXED, tol=1e-4).result() for m in built]
+        jobs = []
+        for p, m in zip(paths, built):
+            jobs.append(srv.submit_file(p, fc.PREC_MIXED, tol=1e-4, mesh_eps=0.02, eps_ratio=2.0))
+            jobs.append(srv.submit(m, fc.PREC_MIXED, tol=1e-4))
+        missing = srv.submit_file(str(tmp_path / "nope.txt"), fc.PREC_MIXED, tol=1e-4)
+        out = [j.result() for j in jobs]
+        with pytest.raises(fc.FCError) as e:
+            missing.result()
+        assert e.value.code == fc.CANNOT_OPEN_FILE
+        st = srv.stats()
+    assert st["in_use"] == 0 and st["running"] == 0
+    for i, (cap, it) in enumerate(out):
+        np.testing.assert_array_equal(cap, ref[i // 2][0])
+        np.testing.assert_array_equal(it, ref[i // 2][1])
+    for i in range(0, len(jobs), 2):
+        info = jobs[i].info
+        assert info["build_ms"] > 0 and info["n_panels"] == built[i // 2].n_panels
+        assert info["n_links"] == built[i // 2].n_links
+
+
+def test_file_jobs_respect_the_budget(ctx, tmp_path):
+    """File jobs build first and then wait for memory: with a budget below
+    every footprint only one solve holds memory at a time."""
+    paths = []
+    for r in range(3):
+        path = tmp_path / ("req%d.txt" % r)
+        geo.random_crossing(200 + r, kmin=2, kmax=4).write(str(path))
+        paths.append(str(path))
+    with ctx.server(slots=3, memory_budget=1) as srv:
+        jobs = [srv.submit_file(p, fc.PREC_FP64, tol=1e-4, mesh_eps=0.05) for p in paths]
+        for j in jobs:
+            j.result()
+        st = srv.stats()
+    assert st["completed"] == 3 and st["in_use"] == 0
+    assert st["peak_in_use"] <= max(j.info["footprint_bytes"] for j in jobs)
