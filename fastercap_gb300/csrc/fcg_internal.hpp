@@ -109,6 +109,7 @@ struct SolveTimings {
     int64_t matvecs = 0;
     int64_t launches = 0, link_launches = 0, link_bytes = 0;
     double link_ms = 0;
+    int rhs_width = 0;  // columns per batched solve of the last solve
 };
 SolveTimings problem_timings(const DeviceProblem *p);
 int problem_set_profiling(DeviceProblem *p, bool on);

@@ -263,6 +263,7 @@ struct DeviceProblem {
     int32_t *row_split = NULL;  // multi-right-hand-side link product: CTA b owns rows [row_split[b], row_split[b+1])
     int n_row_split = 0;
     uint64_t tuned = 0;  // bit kp: the launch shape for kp right-hand sides is settled
+    int tune_val[64] = {0};  // the settled shape per kp (lanes, or CTA row ranges per SM; 0 = built-in)
 
     // two-level preconditioner (built for one dimension, kept until another is asked for)
     int sup_dim = -1;  // dimension it was built for (-1: never built)
@@ -3464,21 +3465,25 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
 // it without measuring. Problems under 4M links keep the built-in choice.
 // FCG_SPMV_LANES pins the lanes.
 static int autotune(DeviceProblem *p, int kp) {
-    if (kp >= 64 || (p->tuned >> kp) & 1u) return FCG_NORMAL_END;
+    if (kp >= 64) return FCG_NORMAL_END;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return FCG_NORMAL_END;
-    p->tuned |= 1ull << kp;
-    bool mixed = p->precision == FCG_PREC_MIXED;
     bool single = kp <= 2;
-    if (!mixed || p->L < (int64_t)4 << 20 || (single && getenv("FCG_SPMV_LANES"))) return FCG_NORMAL_END;
     DeviceContext &ctx = *p->ctx;
-    double avg = (double)p->L / (double)p->Nn;
-    uint64_t key = (uint64_t)kp | ((uint64_t)(int)(4.0 * log2(avg + 1.0)) << 8) | ((uint64_t)(int)log2((double)p->Nn) << 16);
     int sms = ctx.sm_count;
     auto apply = [&](int v) -> int {
+        p->tune_val[kp] = v;
         if (single) { p->spmv_lanes = v; return FCG_NORMAL_END; }
         return set_row_split(p, (int64_t)sms * v);
     };
+    // settled before: put this width's shape back (another width may have
+    // set the problem's lanes or row ranges since)
+    if ((p->tuned >> kp) & 1u) return p->tune_val[kp] ? apply(p->tune_val[kp]) : FCG_NORMAL_END;
+    p->tuned |= 1ull << kp;
+    bool mixed = p->precision == FCG_PREC_MIXED;
+    if (!mixed || p->L < (int64_t)4 << 20 || (single && getenv("FCG_SPMV_LANES"))) return FCG_NORMAL_END;
+    double avg = (double)p->L / (double)p->Nn;
+    uint64_t key = (uint64_t)kp | ((uint64_t)(int)(4.0 * log2(avg + 1.0)) << 8) | ((uint64_t)(int)log2((double)p->Nn) << 16);
     {
         std::lock_guard<std::mutex> lk(ctx.tune_mu);
         auto it = ctx.tune.find(key);
@@ -3520,6 +3525,76 @@ static int autotune(DeviceProblem *p, int kp) {
         ctx.tune[key] = best;
     }
     return apply(best);
+}
+
+// Right-hand-side width of the batched solves (columns per batch) when the
+// caller leaves it open: with more columns per batch the coefficients and
+// source words are read once for more columns, but the charge gathers grow
+// with the width and stop hitting in L1. Candidates 4, 8, 16 and all of the
+// conductors (at most 32); each candidate's link product (in its tuned launch
+// shape) is timed over three launches and the width with the least product
+// time per solve, ceil(columns / width) x time(width), wins. Mixed problems
+// of at least 4M links and more than 4 columns only; the choice is kept in
+// the context per problem shape.
+static int choose_rhs_width(DeviceProblem *p, int cols, int *width) {
+    *width = std::min(cols, kMaxK);
+    if (p->precision != FCG_PREC_MIXED || p->L < ((int64_t)4 << 20) || cols <= 4) return FCG_NORMAL_END;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return FCG_NORMAL_END;
+    DeviceContext &ctx = *p->ctx;
+    const int full = std::min(cols, kMaxK);
+    double avg = (double)p->L / (double)p->Nn;
+    uint64_t key = (1ull << 40) | (uint64_t)full | ((uint64_t)(int)(4.0 * log2(avg + 1.0)) << 8) |
+                   ((uint64_t)(int)log2((double)p->Nn) << 16);
+    {
+        std::lock_guard<std::mutex> lk(ctx.tune_mu);
+        auto it = ctx.tune.find(key);
+        if (it != ctx.tune.end()) { *width = it->second; return FCG_NORMAL_END; }
+    }
+    std::vector<int> cand;
+    for (int w : {4, 8, 16, full})
+        if (w <= full && std::find(cand.begin(), cand.end(), w) == cand.end()) cand.push_back(w);
+    cudaEvent_t e0, e1;
+    FCG_CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        set_error("cannot create timing events");
+        return FCG_DEVICE_ERROR;
+    }
+    // the workspace for the widest candidate serves them all
+    int r = ensure_matvec_ws(p, kpad(full));
+    double best = 1e300;
+    int best_w = full;
+    for (size_t i = 0; i < cand.size() && r == FCG_NORMAL_END; i++) {
+        int w = cand[i], kp = kpad(w);
+        if ((r = autotune(p, kp)) != FCG_NORMAL_END) break;
+        NodeWork nw = {p->Qd, p->Qf, p->Pd, p->Pf2, p->Ad};
+        launch_link(p, nw, kp, true);  // warm
+        cudaEventRecord(e0, p->stream);
+        for (int q = 0; q < 3; q++) launch_link(p, nw, kp, true);
+        cudaEventRecord(e1, p->stream);
+        cudaError_t err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        if (err != cudaSuccess) {
+            set_error(std::string("right-hand-side width tuning failed: ") + cudaGetErrorString(err));
+            r = FCG_DEVICE_ERROR;
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        p->timings.launches += 4;
+        double cost = (double)((full + w - 1) / w) * ms;
+        if (cost < best) { best = cost; best_w = w; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r != FCG_NORMAL_END) return r;
+    {
+        std::lock_guard<std::mutex> lk(ctx.tune_mu);
+        ctx.tune[key] = best_w;
+    }
+    *width = best_w;
+    return FCG_NORMAL_END;
 }
 
 // v = P * (in / diag) for k right-hand sides ([k][Np] device arrays)
@@ -4153,7 +4228,9 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     float solve_ms_total = 0;
     // columns in batches of at most `width`: batch column r of geometry g is the
     // solve for the geometry's conductor r0 + r
-    const int width = opt.rhs_width > 0 ? std::min(opt.rhs_width, kMaxK) : kMaxK;
+    int width = opt.rhs_width > 0 ? std::min(opt.rhs_width, kMaxK) : kMaxK;
+    if (opt.rhs_width == 0 && (r = choose_rhs_width(p, ks, &width)) != FCG_NORMAL_END) return r;
+    p->timings.rhs_width = std::min(width, ks);
     for (int r0 = 0; r0 < ks && status == FCG_NORMAL_END; r0 += width) {
         if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
         const int k = std::min(width, ks - r0);

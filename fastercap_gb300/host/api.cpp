@@ -314,6 +314,7 @@ int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *st) {
     st->refine_checks = t.refine_checks;
     st->refine_cycles = t.refine_cycles;
     st->fill_fp64 = t.fill_fp64;
+    st->rhs_width = t.rhs_width;
     return FCG_NORMAL_END;
 }
 
