@@ -29,10 +29,12 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <chrono>
 #include <string>
 #include <vector>
 
 #include "fc_potential.h"
+#include "pair32.cuh"
 #include "fcg_internal.hpp"
 #include "scan.cuh"
 #include "../host/model.hpp"
@@ -40,6 +42,7 @@
 namespace fcg {
 
 using namespace devscan;
+using namespace pair32;
 
 namespace {
 
@@ -47,126 +50,7 @@ namespace {
 static_assert(sizeof(Element) == 96, "element record layout");
 
 // ------------------------------------------------------------------ traversal
-// FP32 pre-test. Most pairs are far from every decision boundary of the FP64
-// test (the rho = 2 switch between quadrature and point formula, the
-// threshold e itself), so an FP32 evaluation with a bound on its distance to
-// the FP64 value decides them; the rest (typically a few per cent) take the
-// FP64 test. Bounds are deliberately loose (a factor 4 and more over a
-// first-order rounding analysis): a loose bound only sends more pairs to
-// FP64, it never changes a decision.
-constexpr float kU = 5.9604645e-8f;  // 2^-24, unit roundoff of float
-
-// unit normal of a dielectric evaluation element (fcg_diel_normal in FP32);
-// false when a super node's normal is within rounding of the 1e-12 cut-off
-__device__ __forceinline__ bool diel_normal32(unsigned type, const float *n, float &x, float &y, float &z) {
-    x = n[0];
-    y = n[1];
-    z = n[2];
-    if (type & FCG_IS_SUPER_NODE) {
-        float m = sqrtf(x * x + y * y + z * z);
-        const float cut = (float)FCG_PANEL_EPS;
-        if (!(fabsf(m - cut) > 1e-5f * cut)) return false;
-        if (m < cut) {
-            x = y = z = 0.0f;
-        } else {
-            x /= m;
-            y /= m;
-            z /= m;
-        }
-    }
-    if ((type & FCG_OUTPERM_NORMAL_DIR) != FCG_OUTPERM_NORMAL_DIR) {
-        x = -x;
-        y = -y;
-        z = -z;
-    }
-    return true;
-}
-
-// rule-2 average over source triangle v (centroid c) of 1/|r - p| or, for a
-// field, (r - p).n / |r - p|^3, at r = c + d; `err` bounds the distance to
-// fcg_potential_numerical / fcg_enfield_numerical (rule 2)
-__device__ __forceinline__ bool quad2_32(float dx, float dy, float dz, const float *v, const float *c, bool efield, float nx,
-                                         float ny, float nz, float &val, float &err) {
-    float s1x = v[3] - v[0], s1y = v[4] - v[1], s1z = v[5] - v[2];
-    float s2x = v[6] - v[3], s2y = v[7] - v[4], s2z = v[8] - v[5];
-    float s3x = v[0] - v[6], s3y = v[1] - v[7], s3z = v[2] - v[8];
-    float nX = s1y * s2z - s1z * s2y, nY = -s1x * s2z + s1z * s2x, nZ = s1x * s2y - s1y * s2x;
-    float mn = sqrtf(nX * nX + nY * nY + nZ * nZ);
-    float m1 = sqrtf(s1x * s1x + s1y * s1y + s1z * s1z);
-    float m2 = sqrtf(s2x * s2x + s2y * s2y + s2z * s2z);
-    float m3 = sqrtf(s3x * s3x + s3y * s3y + s3z * s3z);
-    if (!(mn > 0.0f) || !(m1 > 0.0f)) return false;
-    float skew = (m1 * m2) / mn;  // 1 / sin of the angle between sides 1 and 2
-    float zx = nX / mn, zy = nY / mn, zz = nZ / mn;
-    float xx = s1x / m1, xy = s1y / m1, xz = s1z / m1;
-    float yx = xy * zz - xz * zy, yy = xz * zx - xx * zz, yz = xx * zy - xy * zx;
-    float v01 = m1, v02 = -(s3x * xx + s3y * xy + s3z * xz), v12 = -(s3x * yx + s3y * yy + s3z * yz);
-    float ratio = ((v02 - v01) * v12 - v12 * v02) / mn;  // jacobian / (2 area): +-1 up to rounding
-    float ox = v[0] - c[0], oy = v[1] - c[1], oz = v[2] - c[2];
-    float side = fmaxf(m1, fmaxf(m2, m3));
-    float dd = sqrtf(dx * dx + dy * dy + dz * dz);
-    // position error of a quadrature point relative to r, against the FP64 path
-    float ep = 64.0f * kU * (dd + 3.0f * side * skew);
-    const float a = 1.0f / 6.0f, b = 4.0f / 6.0f, w = 1.0f / 3.0f;
-    float sum = 0.0f, bnd = 0.0f;
-    for (int i = 0; i < 3; i++) {
-        float px = i == 0 ? b : a, py = i == 1 ? b : a;
-        float p0 = (v01 - v02) * px + v02 * (1.0f - py);
-        float p1 = v12 * (1.0f - px - py);
-        float ex = dx - (ox + xx * p0 + yx * p1);
-        float ey = dy - (oy + xy * p0 + yy * p1);
-        float ez = dz - (oz + xz * p0 + yz * p1);
-        float r2 = ex * ex + ey * ey + ez * ez;
-        float r = sqrtf(r2);
-        if (!(r > 2.0f * ep)) return false;  // a point within rounding of r: FP64 decides
-        float ir = 1.0f / r;
-        if (efield) {
-            float t = (ex * nx + ey * ny + ez * nz) * ir * ir * ir;
-            sum += w * t;
-            bnd += w * (8.0f * ep * ir * ir * ir + 16.0f * kU * ir * ir);
-        } else {
-            sum += w * ir;
-            bnd += w * (4.0f * ep * ir * ir + 16.0f * kU * ir);
-        }
-    }
-    val = sum * ratio;
-    err = 4.0f * (bnd * fabsf(ratio) + (64.0f * kU * skew + 1e-6f) * fabsf(val));
-    return isfinite(val) && isfinite(err);
-}
-
-// one direction of CAutoRefine::RefineCriteria in FP32: the weight of source
-// S seen from evaluation element E (d = E.c - S.c), with its error bound
-__device__ __forceinline__ bool weight32(const Element &E, const Element &S, float dx, float dy, float dz, float r, bool quad,
-                                         float inv_max_area, float inv_max_side, float &cw, float &err) {
-    bool diel = (E.type & FCG_IS_DIEL) != 0;
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-    if (diel && !diel_normal32(E.type, E.n, nx, ny, nz)) return false;
-    float pe, pe_err;
-    if (quad) {
-        if (!quad2_32(dx, dy, dz, S.v, S.c, diel, nx, ny, nz, pe, pe_err)) return false;
-    } else {
-        float ir = 1.0f / r;
-        if (diel) {
-            pe = (dx * nx + dy * ny + dz * nz) * ir * ir * ir;
-            pe_err = 4.0f * (16.0f * kU * ir * ir + 16.0f * kU * fabsf(pe));
-        } else {
-            pe = ir;
-            pe_err = 16.0f * kU * ir;
-        }
-    }
-    float W = (float)S.area * inv_max_area;
-    if (diel) W *= (float)S.maxside * inv_max_side;
-    cw = fabsf(pe * W);
-    err = pe_err * W + 32.0f * kU * cw + 1e-6f * cw;
-    return isfinite(cw) && isfinite(err);
-}
-
-// 1 above e, 0 at or below e (the FP64 test splits on c > e), -1 undecided
-__device__ __forceinline__ int side_test(float c, float err, float e) {
-    if (c - err > e * (1.0f + 4.0f * kU)) return 1;
-    if (c + err < e * (1.0f - 4.0f * kU)) return 0;
-    return -1;
-}
+// FP32 pre-test of every pair (pair32.cuh), FP64 for the undecided ones.
 
 // fcg_link_decision in FP32, or -1 when only the FP64 test can tell
 __device__ int decide32(const Element &A, const Element &B, float e, float inv_max_area, float inv_max_side) {
@@ -354,7 +238,7 @@ struct Level {
 int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const int32_t *root_a, const int32_t *root_b,
                       const uint16_t *root_level, int64_t n_roots, const int32_t *node_of, int64_t n_nodes, double eps,
                       double max_side, double max_area, std::vector<int64_t> &link_ptr, std::vector<int32_t> &link_src,
-                      int &max_level, std::string &err) {
+                      int &max_level, std::string &err, std::shared_ptr<int32_t> *device_src) {
     LB_CK(cudaSetDevice(ctx.device));
     Bufs B;
     LB_CK(cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking));
@@ -373,6 +257,7 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
     unsigned long long *d_undecided;
     const float inv_max_area = (float)(1.0 / max_area), inv_max_side = (float)(1.0 / max_side);
     const bool trace = getenv("FCG_TRACE") != nullptr;
+    const auto t_begin = std::chrono::steady_clock::now();
     long long n_tests = 0, n_fp64 = 0;
     LB_CK(B.alloc(&d_undecided, 1));
     LB_CK(B.alloc(&d_el, (size_t)ne));
@@ -455,6 +340,15 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
         fprintf(stderr, "[fcg links] %zu levels, %lld pair tests, %lld (%.2f %%) by the FP64 test\n", lv.size(), n_tests, n_fp64,
                 n_tests ? 100.0 * (double)n_fp64 / (double)n_tests : 0.0);
 
+    auto t_mark = std::chrono::steady_clock::now();
+    auto mark = [&](const char *what) {
+        if (!trace) return;
+        auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "[fcg links]   %-28s %9.3f ms\n", what, std::chrono::duration<double, std::milli>(now - t_mark).count());
+        t_mark = now;
+    };
+    if (trace) fprintf(stderr, "[fcg links]   traversal                    %9.3f ms\n",
+                       std::chrono::duration<double, std::milli>(t_mark - t_begin).count());
     // links under every item, deepest level first
     for (size_t d = lv.size(); d-- > 0;) {
         Level &L = lv[d];
@@ -546,10 +440,24 @@ int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const i
             std::swap(src, dst);
         }
     }
-    link_src.resize((size_t)nent);
+    if (trace) {
+        LB_CK(cudaStreamSynchronize(s));
+        mark("placement and row sort");
+    }
     LB_CK(cudaMemcpyAsync(link_ptr.data(), d_ptr, ((size_t)n_nodes + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    if (nent > 0) LB_CK(cudaMemcpyAsync(link_src.data(), d_src, (size_t)nent * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (device_src) {
+        // hand the sources over: off the builder's list, freed by the last owner
+        auto it = std::find(B.live.begin(), B.live.end(), (void *)d_src);
+        if (it != B.live.end()) B.live.erase(it);
+        device_src->reset(d_src, [](int32_t *q) { cudaFreeAsync(q, 0); });
+        link_src.clear();
+    } else {
+        link_src.resize((size_t)nent);
+        mark("host link array");
+        if (nent > 0) LB_CK(cudaMemcpyAsync(link_src.data(), d_src, (size_t)nent * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    }
     LB_CK(cudaStreamSynchronize(s));
+    mark("download");
     if (link_ptr[(size_t)n_nodes] != nent) {
         err = "device link construction: row offsets do not add up to the link count";
         return FCG_GENERIC_ERROR;

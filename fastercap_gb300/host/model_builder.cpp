@@ -842,9 +842,10 @@ struct Builder {
         }
         int lvl = 0;
         int r = link_build_device(dev, el.data(), (int64_t)el.size(), ra.data(), rb.data(), rl.data(), (int64_t)ra.size(),
-                                  node_of.data(), M.n_nodes, eps, max_side, max_area, M.link_ptr, M.link_src, lvl, err);
+                                  node_of.data(), M.n_nodes, eps, max_side, max_area, M.link_ptr, M.link_src, lvl, err,
+                                  opt.links_on_device ? &M.d_link_src : nullptr);
         if (r != FC_NORMAL_END) return r;
-        M.n_links = (int64_t)M.link_src.size();
+        M.n_links = M.link_ptr[(size_t)M.n_nodes];
         if (self_level > max_level) max_level = self_level;
         if (lvl > max_level) max_level = lvl;
         return FC_NORMAL_END;
@@ -852,6 +853,7 @@ struct Builder {
 
     // ---------------------------------------------------------------- flatten
     int flatten(Model &M, DeviceContext *dev) {
+        const auto t_flat = std::chrono::steady_clock::now();
         size_t ne = el.size();
         std::vector<int32_t> node_of(ne, -1);
         std::vector<int32_t> post;
@@ -923,7 +925,12 @@ struct Builder {
                 M.leaf_diel[M.leaf_first[i]] = (e.type & FCG_IS_DIEL) ? 0 : e.diel;
             }
         }
-        if (dev) return device_links(M, node_of, *dev);
+        if (dev) {
+            if (getenv("FCG_TRACE"))
+                fprintf(stderr, "[fcg build]   flatten on the host %9.3f ms\n",
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_flat).count());
+            return device_links(M, node_of, *dev);
+        }
         // links: stable counting sort of the emitted pairs by destination node
         std::vector<int64_t> cnt(Nn + 1, 0);
         for (size_t k = 0; k < pairs.size(); k++) { cnt[node_of[pairs[k].first]]++; cnt[node_of[pairs[k].second]]++; }
