@@ -152,6 +152,7 @@ def lib() -> C.CDLL:
     L.fcg_context_stream.argtypes = [vp]
     L.fcg_context_stream.restype = vp
     L.fcg_problem_set_profiling.argtypes = [vp, C.c_int]
+    L.fcg_problem_set_tuning.argtypes = [vp, C.c_int]
     L.fcg_problem_get_stats.argtypes = [vp, C.POINTER(ProblemStats)]
     L.fcg_problem_reset_stats.argtypes = [vp]
     L.fcg_problem_destroy.argtypes = [vp]
@@ -393,6 +394,10 @@ class Problem:
         diel = np.asarray(self.model.arrays["cond_is_diel"]) != 0
         self.geometries = [int(np.sum((geom == g) & ~diel)) for g in range(ng)]
 
+    def set_tuning(self, on: bool):
+        """Measure launch shapes and the right-hand-side width on first use (default on)."""
+        _check(lib().fcg_problem_set_tuning(self._h, 1 if on else 0), "set_tuning")
+
     def set_profiling(self, on: bool):
         _check(lib().fcg_problem_set_profiling(self._h, 1 if on else 0), "profiling")
 
@@ -441,8 +446,8 @@ class Problem:
         cap = np.empty(sum(n * n for n in sizes), np.float64)
         it = np.empty(sum(sizes), np.int32)
         opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
-        self._last_width = min(rhs_width, 32) if rhs_width > 0 else 32
         code = lib().fcg_problem_solve(self._h, C.byref(opt), _ptr(cap), _ptr(it))
+        self._last_width = int(self.stats()["rhs_width"]) or 32  # the width the solve used
         if not (code == NORMAL_END or (allow_not_converged and code == NOT_CONVERGED)):
             _check(code, "solve")
         caps, its, oc, oi = [], [], 0, 0

@@ -8,6 +8,7 @@
 #include <map>
 #include <mutex>
 #include <vector>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -77,12 +78,14 @@ int64_t problem_estimate_bytes(const fcg_model_arrays &a, int precision, int rhs
 // visited at recursion level root_level[i], in the host builder's order;
 // node_of maps element ids to node ids. Fills link_ptr (n_nodes + 1) and
 // link_src exactly as the host traversal and its stable bucketing do, and
-// max_level with the deepest recursion level of the traversal.
+// max_level with the deepest recursion level of the traversal. With
+// device_src the link sources stay in device memory (complete when the call
+// returns; freed with the last reference) and link_src is left empty.
 struct Element;
 int link_build_device(DeviceContext &ctx, const Element *el, int64_t ne, const int32_t *root_a, const int32_t *root_b,
                       const uint16_t *root_level, int64_t n_roots, const int32_t *node_of, int64_t n_nodes, double eps,
                       double max_side, double max_area, std::vector<int64_t> &link_ptr, std::vector<int32_t> &link_src,
-                      int &max_level, std::string &err);
+                      int &max_level, std::string &err, std::shared_ptr<int32_t> *device_src = nullptr);
 
 // Mesh refinement on the device (csrc/mesh_build.cu): the closure of the
 // refinement of the root pairs (root_a[i], root_b[i]) with root_meta[i] =
@@ -113,6 +116,7 @@ struct SolveTimings {
 };
 SolveTimings problem_timings(const DeviceProblem *p);
 int problem_set_profiling(DeviceProblem *p, bool on);
+int problem_set_tuning(DeviceProblem *p, bool on);
 void problem_reset_stats(DeviceProblem *p);
 
 }  // namespace fcg

@@ -152,15 +152,17 @@ struct Stager {
         if (!tried) acquire();
         return buf[0] && buf[1] && ev[0] && ev[1];
     }
-    static bool pinned(const void *h) {
+    // page-locked host memory or device memory: the copy engine reads it directly
+    static bool direct(const void *h) {
         cudaPointerAttributes pa;
-        bool r = cudaPointerGetAttributes(&pa, h) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        bool r = cudaPointerGetAttributes(&pa, h) == cudaSuccess &&
+                 (pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
         cudaGetLastError();
         return r;
     }
     cudaError_t copy(void *dst, const void *src, size_t bytes, cudaStream_t s) {
         if (!bytes) return cudaSuccess;
-        if (pinned(src) || !usable()) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+        if (direct(src) || !usable()) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s);
         for (size_t off = 0; off < bytes; off += kStageBytes) {
             size_t n = std::min(kStageBytes, bytes - off);
             int b = next;
@@ -237,6 +239,7 @@ struct DeviceProblem {
     SolveTimings timings;
     // profiling of the link product: event pairs awaiting readout
     bool profiling = false;
+    bool tuning = true;  // measure launch shapes and the right-hand-side width (else the built-in rules)
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
 
@@ -2725,12 +2728,8 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
         // serialise: one copy then.
         const int kLinkChunks = 8;
         const int64_t ntiles = (L + kRelTile - 1) / kRelTile;
-        bool src_pinned = false;
-        if (L > 0) {
-            cudaPointerAttributes pa;
-            src_pinned = cudaPointerGetAttributes(&pa, a.link_src) == cudaSuccess && pa.type == cudaMemoryTypeHost;
-            cudaGetLastError();
-        }
+        // (pinned host or device memory: the chunks go straight to the copy engine)
+        const bool src_pinned = L > 0 && Stager::direct(a.link_src);
         int nchunk = L > 0 ? (src_pinned ? kLinkChunks : 1) : 0;
         std::vector<int64_t> tbound(nchunk + 1, 0);
         std::vector<cudaEvent_t> ev_src(nchunk, (cudaEvent_t)NULL);
@@ -3172,6 +3171,11 @@ int problem_set_profiling(DeviceProblem *p, bool on) {
     return FCG_NORMAL_END;
 }
 
+int problem_set_tuning(DeviceProblem *p, bool on) {
+    p->tuning = on;
+    return FCG_NORMAL_END;
+}
+
 void problem_reset_stats(DeviceProblem *p) {
     p->timings.launches = p->timings.link_launches = p->timings.link_bytes = 0;
     p->timings.link_ms = 0;
@@ -3481,7 +3485,7 @@ static int autotune(DeviceProblem *p, int kp) {
     if ((p->tuned >> kp) & 1u) return p->tune_val[kp] ? apply(p->tune_val[kp]) : FCG_NORMAL_END;
     p->tuned |= 1ull << kp;
     bool mixed = p->precision == FCG_PREC_MIXED;
-    if (!mixed || p->L < (int64_t)4 << 20 || (single && getenv("FCG_SPMV_LANES"))) return FCG_NORMAL_END;
+    if (!mixed || !p->tuning || p->L < (int64_t)4 << 20 || (single && getenv("FCG_SPMV_LANES"))) return FCG_NORMAL_END;
     double avg = (double)p->L / (double)p->Nn;
     uint64_t key = (uint64_t)kp | ((uint64_t)(int)(4.0 * log2(avg + 1.0)) << 8) | ((uint64_t)(int)log2((double)p->Nn) << 16);
     {
@@ -3538,7 +3542,7 @@ static int autotune(DeviceProblem *p, int kp) {
 // the context per problem shape.
 static int choose_rhs_width(DeviceProblem *p, int cols, int *width) {
     *width = std::min(cols, kMaxK);
-    if (p->precision != FCG_PREC_MIXED || p->L < ((int64_t)4 << 20) || cols <= 4) return FCG_NORMAL_END;
+    if (p->precision != FCG_PREC_MIXED || !p->tuning || p->L < ((int64_t)4 << 20) || cols <= 4) return FCG_NORMAL_END;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return FCG_NORMAL_END;
     DeviceContext &ctx = *p->ctx;

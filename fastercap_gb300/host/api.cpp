@@ -54,8 +54,27 @@ int fcg_model_build(const char *path, const fcg_build_options *opt, fcg_model **
     return fcg_model_build_on(NULL, path, opt, out, err, err_len);
 }
 
-int fcg_model_build_on(fcg_context *ctx, const char *path, const fcg_build_options *opt, fcg_model **out, char *err,
-                       size_t err_len) {
+}  // extern "C"
+
+static int build_on(fcg::DeviceContext *dev, const char *path, const fcg_build_options *opt, bool links_on_device,
+                    fcg_model **out, char *err, size_t err_len);
+
+namespace fcg {
+// a server job's model: built on the server's GPU with the link sources left
+// in device memory (problem creation copies them device to device)
+int model_build_device_links(DeviceContext *dev, const char *path, const fcg_build_options *opt, fcg_model **out, char *err,
+                             size_t err_len) {
+    return build_on(dev, path, opt, true, out, err, err_len);
+}
+}  // namespace fcg
+
+extern "C" int fcg_model_build_on(fcg_context *ctx, const char *path, const fcg_build_options *opt, fcg_model **out,
+                                  char *err, size_t err_len) {
+    return build_on(ctx ? ctx->dev : nullptr, path, opt, false, out, err, err_len);
+}
+
+static int build_on(fcg::DeviceContext *dev, const char *path, const fcg_build_options *opt, bool links_on_device,
+                    fcg_model **out, char *err, size_t err_len) {
     if (!path || !out) return FCG_GENERIC_ERROR;
     *out = NULL;
     fcg::BuildOptions o;
@@ -65,12 +84,13 @@ int fcg_model_build_on(fcg_context *ctx, const char *path, const fcg_build_optio
         o.mesh_curv = opt->mesh_curv;
         o.verbose = opt->verbose != 0;
     }
+    o.links_on_device = links_on_device && dev;
     fcg_model *fm = new (std::nothrow) fcg_model();
     if (!fm) return FCG_OUT_OF_MEMORY;
     std::string e;
     int r;
     try {
-        r = fcg::build_model(path, o, fm->m, e, ctx ? ctx->dev : nullptr);
+        r = fcg::build_model(path, o, fm->m, e, dev);
     } catch (std::bad_alloc &) {
         r = FCG_OUT_OF_MEMORY;
         e = "out of host memory while building the model";
@@ -85,6 +105,8 @@ int fcg_model_build_on(fcg_context *ctx, const char *path, const fcg_build_optio
     *out = fm;
     return FCG_NORMAL_END;
 }
+
+extern "C" {
 
 int fcg_model_info_get(const fcg_model *fm, fcg_model_info *info) {
     if (!fm || !info) return FCG_GENERIC_ERROR;
@@ -122,7 +144,7 @@ int fcg_model_arrays_get(const fcg_model *fm, fcg_model_arrays *a) {
     a->node_area = m.area.data();
     a->node_maxside = m.maxside.data();
     a->link_ptr = m.link_ptr.data();
-    a->link_src = m.link_src.data();
+    a->link_src = m.d_link_src ? m.d_link_src.get() : m.link_src.data();
     a->leaf_diel = m.leaf_diel.data();
     a->cond_is_diel = fm->cond_is_diel.data();
     a->cond_leaf_first = fm->cond_first.data();
@@ -300,6 +322,10 @@ int fcg_problem_set_geometries(fcg_problem *p, int32_t n, const int32_t *geom) {
 
 int fcg_problem_set_profiling(fcg_problem *p, int enable) {
     return p ? fcg::problem_set_profiling(p->p, enable != 0) : FCG_GENERIC_ERROR;
+}
+
+int fcg_problem_set_tuning(fcg_problem *p, int enable) {
+    return p ? fcg::problem_set_tuning(p->p, enable != 0) : FCG_GENERIC_ERROR;
 }
 
 int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *st) {

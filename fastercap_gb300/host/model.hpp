@@ -5,6 +5,7 @@
 #define FCG_HOST_MODEL_HPP
 
 #include <stdint.h>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,9 @@ struct BuildOptions {
     double eps_ratio = 1.0;       // -d   (m_dEpsRatio); link eps = d * m
     double mesh_curv = 3.0;       // -mc  (m_dMeshCurvCoeff)
     bool verbose = false;
+    // device builds only: leave the link sources in device memory
+    // (Model::d_link_src) instead of copying them to link_src
+    bool links_on_device = false;
 };
 
 // One element of the hierarchy: an input panel, a refined sub-panel or a
@@ -57,6 +61,9 @@ struct Model {
     std::vector<uint8_t> maxside_idx;
     // links
     std::vector<int32_t> link_src;
+    // the link sources in device memory when the build left them there
+    // (BuildOptions::links_on_device); link_src is then empty
+    std::shared_ptr<int32_t> d_link_src;
     // leaves
     std::vector<int32_t> leaf_node;                // node of every leaf
     std::vector<uint8_t> leaf_diel;

@@ -96,10 +96,8 @@ static int count_conductors(const fcg_model_arrays &a) {
 // construction on the device), then wait until its footprint may be admitted
 static int build_file_job(fcg_server *s, Job *j) {
     double t0 = now_ms();
-    fcg_context handle;
-    handle.dev = s->ctx;
     char ebuf[512] = {0};
-    int r = fcg_model_build_on(&handle, j->path.c_str(), &j->bopt, &j->model, ebuf, sizeof ebuf);
+    int r = fcg::model_build_device_links(s->ctx, j->path.c_str(), &j->bopt, &j->model, ebuf, sizeof ebuf);
     j->build_ms = now_ms() - t0;
     if (r != FCG_NORMAL_END) {
         j->error = ebuf[0] ? std::string(ebuf) : fcg::get_error();
@@ -127,6 +125,8 @@ static void run_job(fcg_server *s, Job *j, void *stream) {
     int r = FCG_NORMAL_END;
     if (j->from_file) r = build_file_job(s, j);
     if (r == FCG_NORMAL_END) r = fcg::problem_create(*s->ctx, j->a, j->precision, stream, &p);
+    // a job solves once: measuring launch shapes would not pay
+    if (r == FCG_NORMAL_END) fcg::problem_set_tuning(p, false);
     if (r == FCG_NORMAL_END) {
         std::lock_guard<std::mutex> lk(s->mu);
         j->prob = p;

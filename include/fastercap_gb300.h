@@ -255,6 +255,13 @@ typedef struct {
                                * measurement when fcg_solve_options.rhs_width is 0) */
 } fcg_problem_stats;
 int fcg_problem_set_profiling(fcg_problem *p, int enable);
+/* Measure the link product's launch shape and the right-hand-side width on
+ * first use (default on; mixed problems of at least 4M links). The
+ * measurement takes a few tens of launches per shape, which pays when a
+ * problem (or problems of the same shape) solve many times; a problem solved
+ * once can switch it off and take the built-in rules. Server jobs run with
+ * it off. No counterpart in the reference. */
+int fcg_problem_set_tuning(fcg_problem *p, int enable);
 int fcg_problem_get_stats(fcg_problem *p, fcg_problem_stats *stats);
 int fcg_problem_reset_stats(fcg_problem *p);
 
