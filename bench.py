@@ -464,56 +464,164 @@ def run_gb300_multi(args, rank, world, local_rank):
         torch.distributed.destroy_process_group()
 
 
-# Serving: request r is random_crossing(r) with k in 2..12 (numpy
-# default_rng(r)); arrivals are Poisson at rate lam with inter-arrival times
-# from default_rng(10000 + lam). Host models are built before the clock
-# starts (the solve is measured from an uploaded host model).
-SERVING = {"mesh_eps": 1e-3, "tol": 1e-4, "kmin": 2, "kmax": 12}
+# Serving (the metric's configuration): request r is the input file of
+# random_crossing(r) (numpy default_rng(r): k in 2..12, bar length 10-60 um,
+# pitch 2-4 um, gap 1-3 um, vacuum); arrivals are Poisson at rate lam with
+# inter-arrival times from default_rng(10000 + lam). A request is a whole
+# extraction as FasterCap runs one: the server's slot builds the refined mesh
+# and the links on the GPU at -m2.5e-4 -d4 (mesh tolerance 2.5e-4, link
+# tolerance 1e-3: up to about 400k panels for the largest crossings), fills
+# the coefficients and solves every conductor at GMRES tolerance 1e-4 with
+# the Jacobi preconditioner. Mixed: FP32 links, all conductors in one batched
+# solve; FP64: the plain FP64 path, one right-hand side at a time.
+SERVING = {"mesh_eps": 4e-4, "eps_ratio": 2.5, "tol": 1e-4, "kmin": 2, "kmax": 12}
+SERVE_ARMS = (("mixed", 1, 0), ("fp64_single_rhs", 0, 1))  # (name, precision, rhs_width)
 
 
-def build_requests(n: int, rank: int = 0, world: int = 1):
-    import fastercap_gb300 as fc
+def serving_config(args):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": "serving", "requests": args.requests,
+            "rates_req_s": [float(x) for x in args.rates.split(",")],
+            "request": "input file of random_crossing(seed = request id): k x k crossing, k in 2..12, length 10-60 um, "
+                       "pitch 2-4 um, gap 1-3 um, vacuum; built, filled and solved per request",
+            "switches": "-m%g -d%g -t%g -pj" % (SERVING["mesh_eps"], SERVING["eps_ratio"], SERVING["tol"]),
+            "link_eps": SERVING["mesh_eps"] * SERVING["eps_ratio"], "gmres_tol": SERVING["tol"], "precond": "jacobi"}
+
+
+def write_requests(ids, directory):
     from fastercap_gb300 import geometry as geo
-    from concurrent.futures import ThreadPoolExecutor
-    tmp = tempfile.mkdtemp()
-
-    def one(r):
-        path = os.path.join(tmp, "req%d.txt" % r)
-        geo.random_crossing(r, SERVING["kmin"], SERVING["kmax"]).write(path)
-        m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"])
-        os.unlink(path)
-        return m
-
-    from fastercap_gb300 import replicas
-    ids = replicas.shard(n, rank, world)  # request r is served by GPU r mod world
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:  # the native builder releases the GIL
-        models = list(ex.map(one, ids))
-    os.rmdir(tmp)
-    return models, ids, time.perf_counter() - t0
+    paths = []
+    for r in ids:
+        path = os.path.join(directory, "req%d.txt" % r)
+        geo.random_crossing(int(r), SERVING["kmin"], SERVING["kmax"]).write(path)
+        paths.append(path)
+    return paths
 
 
-def serve_pass(srv, models, ids, n_total, precision, lam, tol, world=1):
+def arrivals(n_total, lam):
+    return np.cumsum(np.random.default_rng(10000 + int(lam)).exponential(1.0 / lam, n_total))
+
+
+def serve_pass(srv, paths, ids, n_total, precision, rhs_width, lam, world=1):
     """Submit every request of this GPU's shard at its arrival time (one
-    Poisson schedule over all n_total requests); returns per-request
-    (latency ms, completion s, C, iterations, info)."""
-    arr = np.cumsum(np.random.default_rng(10000 + int(lam)).exponential(1.0 / lam, n_total))
+    Poisson schedule over all n_total requests); per request (latency ms,
+    completion s, C, iterations, info)."""
+    arr = arrivals(n_total, lam)
     from fastercap_gb300 import replicas
     replicas.barrier(world)
     t0 = time.perf_counter()
     sub = []
-    for r, m in zip(ids, models):
+    for r, path in zip(ids, paths):
         dt = t0 + arr[r] - time.perf_counter()
         if dt > 0:
             time.sleep(dt)
         ts = time.perf_counter()
-        sub.append((ts, srv.submit(m, precision, tol=tol)))
+        sub.append((ts, srv.submit_file(path, precision, tol=SERVING["tol"], mesh_eps=SERVING["mesh_eps"],
+                                        eps_ratio=SERVING["eps_ratio"], rhs_width=rhs_width)))
     out = []
     for ts, j in sub:
         cap, it = j.result()
         lat = j.info["queue_ms"] + j.info["run_ms"]
         out.append((lat, ts - t0 + lat / 1000.0, cap, it, j.info))
     return out
+
+
+def summarize(out, parts, n):
+    lat = np.array([x for p_ in parts for x in p_[0]])
+    span = max(p_[1] for p_ in parts)
+    infos = [o[4] for o in out]
+    return {"solves_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "span_s": span, "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])),
+            "mean_build_ms": float(np.mean([i["build_ms"] for i in infos])),
+            "mean_fill_ms": float(np.mean([i["fill_ms"] for i in infos])),
+            "mean_solve_ms": float(np.mean([i["solve_ms"] for i in infos]))}
+
+
+def serving_roofline(ctx, path):
+    """Link-product roofline of one request solved resident (mixed, all
+    conductors batched): CUDA events around every link-product launch."""
+    import fastercap_gb300 as fc
+    m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"], ctx=ctx)
+    p = ctx.problem(m, fc.PREC_MIXED)
+    p.fill()
+    p.solve(tol=SERVING["tol"])
+    p.reset_stats()
+    p.set_profiling(True)
+    p.fill()
+    p.solve(tol=SERVING["tol"])
+    st = p.stats()
+    p.close()
+    peak, peak_kind = peaks()
+    ms = st["link_ms"] / max(1, st["link_launches"])
+    b = st["link_bytes"] / max(1, st["link_launches"])
+    ach = b / (ms / 1000.0) / 1e9 if ms > 0 else None
+    return {"kernel": "k_spmv32_multi (link product)", "bound": "hbm",
+            "timing": "CUDA events around every link-product launch of one resident solve of the request",
+            "request_panels": m.n_panels, "request_links": m.n_links, "rhs": len(m.conductor_names),
+            "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None, "peak_source": peak_kind,
+            "traffic": None, "launches": int(st["link_launches"]), "bytes_per_launch": b, "avg_launch_ms": ms}
+
+
+def converged_accuracy(ctx, paths, tol=1e-8):
+    """Mixed against FP64 with both solves converged far below the serving
+    tolerance: the difference that precision alone makes (at the serving
+    tolerance both share the same GMRES truncation error, which dominates
+    the small couplings). Per request the largest per-entry difference."""
+    import fastercap_gb300 as fc
+    errs = []
+    for path in paths:
+        m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"], ctx=ctx)
+        caps = []
+        for prec in (fc.PREC_MIXED, fc.PREC_FP64):
+            p = ctx.problem(m, prec)
+            p.fill()
+            caps.append(p.solve(tol=tol)[0])
+            p.close()
+        errs.append(float(np.max(np.abs(caps[0] - caps[1]) / np.abs(caps[1]))))
+    return {"gmres_tol": tol, "requests": len(paths), "max_rel_c_err": max(errs),
+            "per_request": [round(e, 9) for e in errs]}
+
+
+def cpu_serving_sample(paths, budget_s, cores, build_in_subprocess=False):
+    """The CPU port on a fixed, ordered sample of the requests: per request
+    the FP64 fill and the first conductor's GMRES solve, extrapolated to the
+    whole request (the reference solves conductors one after another; fill
+    + n_cond x the first solve); stops after budget_s. Returns (solves/s,
+    number of requests, per-request seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    est, t_start = [], time.perf_counter()
+    for path in paths:
+        arrays, n_cond = load_request_arrays(path, build_in_subprocess)
+        o = Oracle(arrays, threads=cores)
+        t0 = time.perf_counter()
+        o.fill()
+        t1 = time.perf_counter()
+        o.solve_rows(0, 1, SERVING["tol"], 1)
+        t2 = time.perf_counter()
+        est.append((t1 - t0) + n_cond * (t2 - t1))
+        if time.perf_counter() - t_start > budget_s:
+            break
+    return len(est) / sum(est), len(est), est
+
+
+def load_request_arrays(path, build_in_subprocess):
+    """Model arrays of a request file. In a subprocess, the CPU arm builds
+    the model there (it writes an .npz), so the arm's own process never loads
+    the GPU library."""
+    if not build_in_subprocess:
+        import fastercap_gb300 as fc
+        m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"])
+        return dict(m.arrays), int(sum(1 for k in m.arrays["cond_is_diel"] if not k))
+    out = path + ".npz"
+    code = ("import sys, numpy as np; sys.path.insert(0, %r); import fastercap_gb300 as fc; "
+            "m = fc.Model.build(%r, mesh_eps=%r, eps_ratio=%r); np.savez(%r, **m.arrays)"
+            % (ROOT, path, SERVING["mesh_eps"], SERVING["eps_ratio"], out))
+    subprocess.run([sys.executable, "-c", code], check=True)
+    d = np.load(out)
+    arrays = {k: d[k] for k in d.files}
+    os.unlink(out)
+    return arrays, int(np.sum(arrays["cond_is_diel"] == 0))
 
 
 def run_serving(args, rank, world, local_rank):
@@ -527,109 +635,120 @@ def run_serving(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     rates = [float(x) for x in args.rates.split(",")]
-    models, ids, build_s = build_requests(args.requests, rank, world)
+    tmp = tempfile.mkdtemp()
+    ids = replicas.shard(args.requests, rank, world)  # request r is served by GPU r mod world
+    paths = write_requests(ids, tmp)
+    warm = write_requests(range(10 ** 6, 10 ** 6 + 2 * args.slots), tmp)
     ctx = fc.Context(local_rank)
-    tol = SERVING["tol"]
-    res = {}
-    caps = {}
-    launches = 0
-    clk_summary = None
+    res, caps, its = {}, {}, {}
+    launches, clk_summary, sizes = 0, None, None
     with ctx.server(slots=args.slots) as srv:
-        # warm the pool and the kernels
-        for j in [srv.submit(m, fc.PREC_MIXED, tol=tol) for m in models[:4]]:
-            j.result()
-        for prec, name in ((fc.PREC_MIXED, "mixed"), (fc.PREC_FP64, "fp64")):
+        # warm the pools, the kernels and the tuned launch shapes
+        for name, prec, width in SERVE_ARMS:
+            for j in [srv.submit_file(p, prec, tol=SERVING["tol"], mesh_eps=SERVING["mesh_eps"],
+                                      eps_ratio=SERVING["eps_ratio"], rhs_width=width) for p in warm]:
+                j.result()
+        for name, prec, width in SERVE_ARMS:
             res[name] = {}
             for lam in rates:
-                if name == "mixed" and lam == rates[-1]:
+                headline = name == "mixed" and lam == rates[-1]
+                if headline:
                     with ClockSampler(local_rank) as clk:
-                        out = serve_pass(srv, models, ids, args.requests, prec, lam, tol, world)
+                        out = serve_pass(srv, paths, ids, args.requests, prec, width, lam, world)
                     clk_summary = clk.summary()
                 else:
-                    out = serve_pass(srv, models, ids, args.requests, prec, lam, tol, world)
+                    out = serve_pass(srv, paths, ids, args.requests, prec, width, lam, world)
                 # latencies of every GPU's shard; the job ends with the slowest GPU
                 parts = replicas.gather_to_all(([o[0] for o in out], max(o[1] for o in out)), world)
-                lat = np.array([x for p_ in parts for x in p_[0]])
-                span = max(p_[1] for p_ in parts)
-                res[name][str(int(lam))] = {"solves_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
-                                            "p99_ms": float(np.percentile(lat, 99)),
-                                            "mean_queue_ms": float(np.mean([o[4]["queue_ms"] for o in out]))}
+                res[name][str(int(lam))] = summarize(out, parts, args.requests)
                 caps[(name, lam)] = [o[2] for o in out]
-                if name == "mixed" and lam == rates[-1]:
+                its[(name, lam)] = [o[3] for o in out]
+                if headline:
                     launches = int(sum(o[4]["kernel_launches"] for o in out))
+                    sizes = [(o[4]["n_panels"], o[4]["n_links"]) for o in out]
+                log("serving %s at %g req/s: %.1f solves/s, p50 %.0f ms, p99 %.0f ms" % (
+                    name, lam, res[name][str(int(lam))]["solves_s"], res[name][str(int(lam))]["p50_ms"],
+                    res[name][str(int(lam))]["p99_ms"]))
         st = srv.stats()
     top = str(int(rates[-1]))
-    err = max(float(np.max(np.abs(a - b) / np.abs(b))) for a, b in zip(caps[("mixed", rates[-1])], caps[("fp64", rates[-1])]))
+    # per request: the largest per-entry difference of the mixed matrix from
+    # the plain FP64 one, and that entry's size relative to its diagonal
+    errs, ent = [], []
+    for a, b in zip(caps[("mixed", rates[-1])], caps[("fp64_single_rhs", rates[-1])]):
+        e = np.abs(a - b) / np.abs(b)
+        i = np.unravel_index(int(np.argmax(e)), e.shape)
+        errs.append(float(e[i]))
+        ent.append(float(abs(b[i]) / abs(b[i[0], i[0]])))
     # the same request gives the same matrix at every rate (alone or in any mix)
     same = all(np.array_equal(a, b) for lam in rates for a, b in zip(caps[("mixed", lam)], caps[("mixed", rates[0])]))
-    h2d = int(np.mean([model_bytes(m) for m in models]))
+    panels = np.array([x[0] for x in sizes])
+    links = np.array([x[1] for x in sizes])
     mixed_top = res["mixed"][top]
+    roof = serving_roofline(ctx, paths[0]) if rank == 0 else None
+    conv = converged_accuracy(ctx, paths[:args.accuracy_sample]) if rank == 0 and args.accuracy_sample > 0 else None
     result = {
         "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": world, "steps": args.requests,
-        "warmup": 4, "ms_per_step": 1000.0 / mixed_top["solves_s"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
+        "warmup": 2 * args.slots, "ms_per_step": 1000.0 / mixed_top["solves_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
         "p50_ms": mixed_top["p50_ms"], "p99_ms": mixed_top["p99_ms"],
-        "config": {"workload": "serving", "requests": args.requests, "rates_req_s": rates, "slots": args.slots,
-                   "parallelism": "request r on GPU r mod N" if world > 1 else "single GPU",
-                   "request": "random k x k crossing, k in 2..12, seed = request id", "link_eps": SERVING["mesh_eps"],
-                   "gmres_tol": tol, "precond": "jacobi",
-                   "panels_min_max_mean": [min(m.n_panels for m in models), max(m.n_panels for m in models),
-                                           int(np.mean([m.n_panels for m in models]))],
-                   "links_mean": int(np.mean([m.n_links for m in models])), "host_build_s": round(build_s, 2),
-                   "step": "one request (upload + fill + GMRES + C), value at the highest rate",
-                   "l2": "each request's links exceed L2 on average; no flush"},
+        "config": serving_config(args),
+        "run": {"slots": args.slots, "parallelism": "request r on GPU r mod N" if world > 1 else "single GPU",
+                "step": "one request: GPU model build + coefficient fill + GMRES over every conductor + C read back; "
+                        "value = mixed solves/s at the highest rate",
+                "l2": "no flush: every request builds and uploads its own model (tens to hundreds of MB)",
+                "panels_min_max_mean": [int(panels.min()), int(panels.max()), int(panels.mean())],
+                "links_min_max_mean": [int(links.min()), int(links.max()), int(links.mean())]},
         "serving": res,
-        "mixed_vs_fp64": {"speedup_at_top_rate": mixed_top["solves_s"] / res["fp64"][top]["solves_s"],
-                          "max_rel_c_err": err},
+        "mixed_vs_fp64": {"speedup_at_top_rate": mixed_top["solves_s"] / res["fp64_single_rhs"][top]["solves_s"],
+                          "max_rel_c_err": max(errs), "requests_compared": len(errs),
+                          "requests_above_1e-3": int(sum(e > 1e-3 for e in errs)),
+                          "p99_rel_c_err": float(np.percentile(errs, 99)),
+                          "worst_entry_over_its_diagonal": ent[int(np.argmax(errs))]},
+        "mixed_vs_fp64_converged": conv,
         "same_result_every_rate": bool(same),
         "server": {"max_running": st["max_running"], "peak_in_use_bytes": st["peak_in_use"], "budget_bytes": st["budget"]},
-        "e2e": {"value": mixed_top["solves_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": int(np.mean([c.nbytes for c in caps[("mixed", rates[-1])]]))},
+        "e2e": {"value": mixed_top["solves_s"], "unit": "solves/s",
+                "h2d_bytes_per_step": int(np.mean([os.path.getsize(p) for p in paths])) + int(
+                    np.mean(panels) * 2 * 101 + np.mean(links) * 4),
+                "d2h_bytes_per_step": int(np.mean([c.nbytes for c in caps[("mixed", rates[-1])]])),
+                "note": "requests arrive as input files on the host; a request's time includes its model build, "
+                        "upload and the matrix read back (H2D counts the model arrays problem creation uploads)"},
         "gpu_launches": launches,
+        "roofline": roof,
         "clocks": clk_summary,
     }
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        from pyoracle import Oracle
         cores = os.cpu_count() or 1
-        t0 = time.perf_counter()
-        n = 0
-        for m in models:
-            o = Oracle(m.arrays, threads=cores)
-            o.fill()
-            o.solve(tol, 1)
-            n += 1
-            if time.perf_counter() - t0 > 20.0:
-                break
-        dt = time.perf_counter() - t0
-        result["cpu_baseline"] = {"value": n / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-                                  "sample": "the first %d requests, solved one after another" % n}
+        v, n, est = cpu_serving_sample(paths, 20.0, cores)
+        result["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                                  "sample": "requests 0..%d in order: FP64 fill + the first conductor's GMRES, "
+                                            "extrapolated to every conductor (%.1f s of CPU work)" % (n - 1, sum(est))}
+    if args.sphere and rank == 0:
+        result["sphere_327680"] = run_gb300(argparse.Namespace(**{**vars(args), "workload": "sphere_327680"}), rank,
+                                            world, local_rank, ctx=ctx, emit=False)
     if rank == 0:
         print(json.dumps(result), flush=True)
     ctx.close()
+    import shutil
+    shutil.rmtree(tmp, ignore_errors=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
 def run_reference_serving(args, rank, world):
-    """CPU arm for serving: the oracle port on every host core solves the
-    requests one after another (the first steps + warmup requests)."""
+    """CPU arm for serving: the oracle port on every host core, on the
+    requests in order (warmup ones first); per step one request's FP64 fill
+    and first conductor's GMRES, extrapolated to all its conductors. Models
+    are built in a subprocess, so this process never loads the GPU library."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from pyoracle import Oracle
     from fastercap_gb300 import build as fbuild
     fbuild.build(reference=False)
-    models, _, build_s = build_requests(args.warmup + args.steps)
+    tmp = tempfile.mkdtemp()
+    paths = write_requests(range(args.warmup + args.steps), tmp)
     cores = os.cpu_count() or 1
-    times = []
-    for i, m in enumerate(models):
-        o = Oracle(m.arrays, threads=cores)
-        t0 = time.perf_counter()
-        o.fill()
-        o.solve(SERVING["tol"], 1)
-        if i >= args.warmup:
-            times.append(time.perf_counter() - t0)
+    _, _, est = cpu_serving_sample(paths, float("inf"), cores, build_in_subprocess=True)
+    times = est[args.warmup:]
     total = sum(times)
     value = len(times) / total
     line = {
@@ -637,13 +756,15 @@ def run_reference_serving(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "p50_ms": 1000 * float(np.percentile(times, 50)), "p99_ms": 1000 * float(np.percentile(times, 99)),
-        "config": {"workload": "serving", "requests": args.steps, "link_eps": SERVING["mesh_eps"],
-                   "gmres_tol": SERVING["tol"], "precond": "jacobi"},
+        "config": serving_config(args),
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": "requests %d..%d solved one after another (no arrival process)"
+                         "sample": "requests %d..%d in order, one per step: FP64 fill + the first conductor's GMRES "
+                                   "solve, extrapolated to every conductor (model build not timed)"
                                    % (args.warmup, args.warmup + args.steps - 1)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    import shutil
+    shutil.rmtree(tmp, ignore_errors=True)
     print(json.dumps(line), flush=True)
 
 
@@ -664,16 +785,20 @@ def time_steps(prob, stream, n, tol, flush_buf, torch):
     return times, cap, it
 
 
-def run_gb300(args, rank, world, local_rank):
+def run_gb300(args, rank, world, local_rank, ctx=None, emit=True):
+    """One resident workload; prints its line (emit) or returns it (inside
+    another workload's run, on that run's context)."""
     import torch
     import fastercap_gb300 as fc
     from fastercap_gb300 import build as fbuild
-    fbuild.build(reference=False)
-    torch.cuda.set_device(local_rank)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    ctx = fc.Context(local_rank)
+    own = ctx is None
+    if own:
+        fbuild.build(reference=False)
+        torch.cuda.set_device(local_rank)
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        ctx = fc.Context(local_rank)
     compare = rank == 0 and world == 1
     built = build_model(args.workload, ctx, compare=compare)
     model, build_s, tol, analytic, eps = built[:5]
@@ -785,9 +910,11 @@ def run_gb300(args, rank, world, local_rank):
         result["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
                                   "sample": "one full solve (fill + GMRES + C) of the same model"}
         result["accuracy"]["max_rel_c_err_vs_cpu_fp64"] = float(np.max(np.abs(cap_m - ocap) / np.abs(ocap)))
+    prob.close()
+    if not own:
+        return result
     if rank == 0:
         print(json.dumps(result), flush=True)
-    prob.close()
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -799,10 +926,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sphere_327680", choices=sorted(WORKLOADS) + sorted(MULTI) + ["serving"])
-    ap.add_argument("--requests", type=int, default=200, help="serving: number of requests")
-    ap.add_argument("--rates", default="50,200,500", help="serving: arrival rates (req/s), comma separated")
-    ap.add_argument("--slots", type=int, default=4, help="serving: concurrent jobs")
+    ap.add_argument("--workload", default="serving", choices=sorted(WORKLOADS) + sorted(MULTI) + ["serving"])
+    ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
+    ap.add_argument("--rates", default="500", help="serving: arrival rates (req/s), comma separated")
+    ap.add_argument("--slots", type=int, default=8, help="serving: concurrent jobs")
+    ap.add_argument("--accuracy-sample", type=int, default=8,
+                    help="serving: requests re-solved at GMRES tolerance 1e-8 in both precisions")
+    ap.add_argument("--no-sphere", dest="sphere", action="store_false",
+                    help="serving: skip the resident 327,680-triangle sphere measured after the requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
