@@ -1015,8 +1015,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
     double *pv = sh;                                     // (2 kBlockLeaves - 1) x kc: P, then A of internal nodes
     double *al = pv + (2 * kBlockLeaves - 1) * kc;       // kBlockLeaves x kc: A of each leaf's parent
     double *cp = al + kBlockLeaves * kc;                 // kMaxChain x kc: P of the root's ancestors
-    double *xs = cp + kMaxChain * kc;                    // kBlockLeaves x kc: scaled leaf inputs
-    double *ss = xs + kBlockLeaves * kc;                 // kBlockLeaves: leaf self terms
+    double *ss = cp + kMaxChain * kc;                    // kBlockLeaves: leaf self terms
     uint32_t *kids = (uint32_t *)(ss + kBlockLeaves);    // kBlockLeaves
     int32_t *lp = (int32_t *)(kids + kBlockLeaves);      // kBlockLeaves + 1
     const int b = blockIdx.x, tid = threadIdx.x;
@@ -1039,11 +1038,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
         }
         for (int t = tid; t < nl * kk; t += blockDim.x) {
             int r = t / nl, i = t - r * nl;
-            int j = lf + i;
-            pv[i * kc + r] = pval(P, (int64_t)j * kp + c0 + r);
-            double xv = in[(int64_t)(c0 + r) * ld + j];
-            if (diag) xv = recip ? xv * diag[j] : xv / diag[j];
-            xs[i * kc + r] = xv;
+            pv[i * kc + r] = pval(P, (int64_t)(lf + i) * kp + c0 + r);
         }
         __syncthreads();
         if (tid < kk && nc > 0) {
@@ -1069,9 +1064,13 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
         }
         for (int t = tid; t < nl * kk; t += blockDim.x) {
             int r = t / nl, i = t - r * nl;
-            double v = ss[i] * xs[i * kc + r] + pv[i * kc + r];
+            int j = lf + i;
+            // the leaf's (scaled) input, read here once instead of staged
+            double xv = in[(int64_t)(c0 + r) * ld + j];
+            if (diag) xv = recip ? xv * diag[j] : xv / diag[j];
+            double v = ss[i] * xv + pv[i * kc + r];
             if (hasA) v = v + al[i * kc + r];
-            out[(int64_t)(c0 + r) * ld + lf + i] = v;
+            out[(int64_t)(c0 + r) * ld + j] = v;
         }
         __syncthreads();  // the next pass reuses the shared arrays
     }
@@ -1318,6 +1317,24 @@ __global__ void __launch_bounds__(256) k_spmv32_multi(const int32_t *__restrict_
         int s = (int)ptr[row], e = (int)ptr[row + 1];
         int l = s + li;
         if (slot_ok) {
+            if constexpr (K >= 16) {
+                // four links per slot and pass (four charge gathers in flight
+                // per lane), their products summed plainly, then added to
+                // the compensated sums (served 22-column requests: 1.5 %
+                // faster than two per pass)
+                for (; l + 3 * LPW < e; l += 4 * LPW) {
+                    float c0 = __ldcs(&coef[l]), c1 = __ldcs(&coef[l + LPW]);
+                    float c2 = __ldcs(&coef[l + 2 * LPW]), c3 = __ldcs(&coef[l + 3 * LPW]);
+                    uint32_t j0 = __ldcs(&src[l]) & kSrcMask, j1 = __ldcs(&src[l + LPW]) & kSrcMask;
+                    uint32_t j2 = __ldcs(&src[l + 2 * LPW]) & kSrcMask, j3 = __ldcs(&src[l + 3 * LPW]) & kSrcMask;
+                    float4 q0 = Q4[(int64_t)j0 * LPL + ri], q1 = Q4[(int64_t)j1 * LPL + ri];
+                    float4 q2 = Q4[(int64_t)j2 * LPL + ri], q3 = Q4[(int64_t)j3 * LPL + ri];
+                    kgroup_add(acc[0], fmaf(c3, q3.x, fmaf(c2, q2.x, fmaf(c1, q1.x, c0 * q0.x))));
+                    kgroup_add(acc[1], fmaf(c3, q3.y, fmaf(c2, q2.y, fmaf(c1, q1.y, c0 * q0.y))));
+                    kgroup_add(acc[2], fmaf(c3, q3.z, fmaf(c2, q2.z, fmaf(c1, q1.z, c0 * q0.z))));
+                    kgroup_add(acc[3], fmaf(c3, q3.w, fmaf(c2, q2.w, fmaf(c1, q1.w, c0 * q0.w))));
+                }
+            }
             // two links per slot and pass; from 16 columns on (issue bound)
             // their products are summed plainly, then added to the
             // compensated sums (kgroup_add), below that each is (kmul_add)
@@ -3410,7 +3427,7 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     size_t n = (size_t)p->Nn * kp;
     const int kc = std::min(k, kSweepCols);
     const size_t up_smem = (size_t)(2 * kBlockLeaves - 1) * kc * sizeof(double) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
-    const size_t down_smem = ((size_t)(4 * kBlockLeaves - 1 + kMaxChain) * kc + kBlockLeaves) * sizeof(double) +
+    const size_t down_smem = ((size_t)(3 * kBlockLeaves - 1 + kMaxChain) * kc + kBlockLeaves) * sizeof(double) +
                              (2 * kBlockLeaves + 1) * sizeof(int32_t);
     // the mixed path's Jacobi scaling multiplies by the reciprocals (the
     // FP64 path divides, as the reference does)
