@@ -57,11 +57,12 @@ WORKLOADS = {
 # many independent geometries in one problem: name -> (crossing list,
 # mesh_eps, eps_ratio, gmres tol). crossings32: 32 random k x k crossings in
 # vacuum drawn in order from default_rng(0) (k in 2..10, length 10-60 um,
-# pitch 2-4 um, gap 1-3 um): 4,736 to 48,128 panels each, 765,504 panels,
-# 428 conductors and 255.2M links in all.
+# pitch 2-4 um, gap 1-3 um) at -m5e-4 -d2 (link tolerance 1e-3): 13,056 to
+# 165,888 panels each, 2,193,543 panels, 428 conductors and 318.8M links in
+# all (within 32-bit link indices, so one problem holds the whole batch).
 MULTI = {
     "crossings32": (lambda: __import__("fastercap_gb300.geometry", fromlist=["x"]).crossing_batch(0, 32, 2, 10),
-                    1e-3, 1.0, 1e-4),
+                    5e-4, 2.0, 1e-4),
 }
 
 
@@ -583,45 +584,51 @@ def converged_accuracy(ctx, paths, tol=1e-8):
 
 
 def cpu_serving_sample(paths, budget_s, cores, build_in_subprocess=False):
-    """The CPU port on a fixed, ordered sample of the requests: per request
-    the FP64 fill and the first conductor's GMRES solve, extrapolated to the
-    whole request (the reference solves conductors one after another; fill
-    + n_cond x the first solve); stops after budget_s. Returns (solves/s,
-    number of requests, per-request seconds)."""
+    """The CPU path on a fixed, ordered sample of the requests: per request
+    the model build (the host restatement of the reference's parse, mesh
+    refinement and link construction; one thread, the same model bit for
+    bit), the FP64 fill and the first conductor's GMRES solve, extrapolated
+    to the whole request (the reference solves conductors one after another:
+    build + fill + n_cond x the first solve); stops after budget_s. Returns
+    (solves/s, number of requests, per-request seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from pyoracle import Oracle
     est, t_start = [], time.perf_counter()
     for path in paths:
-        arrays, n_cond = load_request_arrays(path, build_in_subprocess)
+        arrays, n_cond, build_s = load_request_arrays(path, build_in_subprocess)
         o = Oracle(arrays, threads=cores)
         t0 = time.perf_counter()
         o.fill()
         t1 = time.perf_counter()
         o.solve_rows(0, 1, SERVING["tol"], 1)
         t2 = time.perf_counter()
-        est.append((t1 - t0) + n_cond * (t2 - t1))
+        est.append(build_s + (t1 - t0) + n_cond * (t2 - t1))
         if time.perf_counter() - t_start > budget_s:
             break
     return len(est) / sum(est), len(est), est
 
 
 def load_request_arrays(path, build_in_subprocess):
-    """Model arrays of a request file. In a subprocess, the CPU arm builds
-    the model there (it writes an .npz), so the arm's own process never loads
-    the GPU library."""
+    """(model arrays, conductors, host build seconds) of a request file. In a
+    subprocess, the CPU arm builds the model there (it writes an .npz with
+    the build time), so the arm's own process never loads the GPU library."""
     if not build_in_subprocess:
         import fastercap_gb300 as fc
+        t0 = time.perf_counter()
         m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"])
-        return dict(m.arrays), int(sum(1 for k in m.arrays["cond_is_diel"] if not k))
+        dt = time.perf_counter() - t0
+        return dict(m.arrays), int(sum(1 for k in m.arrays["cond_is_diel"] if not k)), dt
     out = path + ".npz"
-    code = ("import sys, numpy as np; sys.path.insert(0, %r); import fastercap_gb300 as fc; "
-            "m = fc.Model.build(%r, mesh_eps=%r, eps_ratio=%r); np.savez(%r, **m.arrays)"
+    code = ("import sys, time, numpy as np; sys.path.insert(0, %r); import fastercap_gb300 as fc; "
+            "t0 = time.perf_counter(); m = fc.Model.build(%r, mesh_eps=%r, eps_ratio=%r); "
+            "dt = time.perf_counter() - t0; np.savez(%r, _build_s=np.array(dt), **m.arrays)"
             % (ROOT, path, SERVING["mesh_eps"], SERVING["eps_ratio"], out))
     subprocess.run([sys.executable, "-c", code], check=True)
     d = np.load(out)
-    arrays = {k: d[k] for k in d.files}
+    arrays = {k: d[k] for k in d.files if k != "_build_s"}
+    build_s = float(d["_build_s"])
     os.unlink(out)
-    return arrays, int(np.sum(arrays["cond_is_diel"] == 0))
+    return arrays, int(np.sum(arrays["cond_is_diel"] == 0)), build_s
 
 
 def run_serving(args, rank, world, local_rank):
@@ -721,8 +728,9 @@ def run_serving(args, rank, world, local_rank):
         cores = os.cpu_count() or 1
         v, n, est = cpu_serving_sample(paths, 20.0, cores)
         result["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                                  "sample": "requests 0..%d in order: FP64 fill + the first conductor's GMRES, "
-                                            "extrapolated to every conductor (%.1f s of CPU work)" % (n - 1, sum(est))}
+                                  "sample": "requests 0..%d in order: host model build + FP64 fill + the first "
+                                            "conductor's GMRES, extrapolated to every conductor (%.1f s of CPU work)"
+                                            % (n - 1, sum(est))}
     if args.sphere and rank == 0:
         result["sphere_327680"] = run_gb300(argparse.Namespace(**{**vars(args), "workload": "sphere_327680"}), rank,
                                             world, local_rank, ctx=ctx, emit=False)
@@ -737,9 +745,10 @@ def run_serving(args, rank, world, local_rank):
 
 def run_reference_serving(args, rank, world):
     """CPU arm for serving: the oracle port on every host core, on the
-    requests in order (warmup ones first); per step one request's FP64 fill
-    and first conductor's GMRES, extrapolated to all its conductors. Models
-    are built in a subprocess, so this process never loads the GPU library."""
+    requests in order (warmup ones first); per step one request's host model
+    build, FP64 fill and first conductor's GMRES, extrapolated to all its
+    conductors. Models are built in a subprocess (timed there), so this
+    process never loads the GPU library."""
     if rank != 0:
         return
     from fastercap_gb300 import build as fbuild
@@ -758,8 +767,8 @@ def run_reference_serving(args, rank, world):
         "p50_ms": 1000 * float(np.percentile(times, 50)), "p99_ms": 1000 * float(np.percentile(times, 99)),
         "config": serving_config(args),
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": "requests %d..%d in order, one per step: FP64 fill + the first conductor's GMRES "
-                                   "solve, extrapolated to every conductor (model build not timed)"
+                         "sample": "requests %d..%d in order, one per step: host model build + FP64 fill + the first "
+                                   "conductor's GMRES solve, extrapolated to every conductor"
                                    % (args.warmup, args.warmup + args.steps - 1)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
