@@ -254,6 +254,8 @@ struct DeviceProblem {
     float *coef32 = NULL;
     double *self = NULL;
     double *rself = NULL;  // mixed path: 1 / self, the Jacobi scaling of the sweeps as a multiply
+    float *rself32 = NULL;  // mixed path: 1 / self rounded to FP32 (the up-sweep's leaf charge scale)
+    double *srself = NULL;  // mixed path: self * (1 / self) (the down-sweep's leaf term under Jacobi scaling)
     unsigned *status = NULL;
     SweepPlan plan;
 
@@ -805,7 +807,8 @@ __global__ void __launch_bounds__(128, 8) k_fill_near32(int64_t n, const int32_t
 // leaves by their closed form.
 __global__ void __launch_bounds__(256, 4) k_fill_self32(int64_t Np, const int32_t *__restrict__ leaf_node, const NodeGeo *__restrict__ geo,
                               const fcg_tri32 *__restrict__ tri, const double *__restrict__ eb, const double *__restrict__ ea,
-                              double *__restrict__ self, double *__restrict__ rself, unsigned *status, unsigned long long *fb) {
+                              double *__restrict__ self, double *__restrict__ rself, float *__restrict__ rself32,
+                              double *__restrict__ srself, unsigned *status, unsigned long long *fb) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Np; j += (int64_t)gridDim.x * blockDim.x) {
         int32_t node = leaf_node[j];
         const NodeGeo &g = geo[node];
@@ -823,7 +826,10 @@ __global__ void __launch_bounds__(256, 4) k_fill_self32(int64_t Np, const int32_
         }
         if (!isfinite(val) || val == 0.0) atomicOr(status, 2u);
         self[j] = val;
-        rself[j] = 1.0 / val;
+        const double r = 1.0 / val;
+        rself[j] = r;
+        rself32[j] = (float)r;
+        srself[j] = val * r;
     }
 }
 
@@ -1073,6 +1079,310 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
             out[(int64_t)(c0 + r) * ld + j] = v;
         }
         __syncthreads();  // the next pass reuses the shared arrays
+    }
+}
+
+// ---- mixed-path sweeps in FP32 pairs
+//
+// GB300 runs FP64 arithmetic and every FP64<->FP32 conversion on its FP64
+// pipe, at about 1.6 operations per SM and clock (measured; FP32 about 119):
+// the FP64 sweeps spent most of their time there (the down-sweep did six
+// FP64 operations or conversions per leaf and right-hand side, four per
+// internal node). The mixed path's sweeps therefore sum in unevaluated FP32
+// pairs (value = s + c, about 44 significant bits: Knuth's TwoSum for the
+// leading parts, then the trailing parts and a Fast2Sum renormalisation) and
+// convert with integer operations; FP64 arithmetic is left for the Krylov
+// vectors themselves (the step's normalisation, written back to v and to
+// the basis, and the leaf output v = x * self/diag + potential).
+
+// float -> double by integer operations (exact); zero included, subnormal,
+// infinite and NaN inputs through the conversion instruction
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (e == 0u || e == 255u) return (double)f;
+    const uint32_t m = u & 0x7fffffu;
+    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | (m >> 3)), (int)(m << 29));
+}
+
+// double -> float, round to nearest even, by integer operations for results
+// in the normal float range (and zero); the rest through the instruction
+__device__ __forceinline__ float d2f_bits(double d) {
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    if (e < 897u || e > 1150u) return (float)d;
+    const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
+    uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry rounds into the exponent
+    return __uint_as_float(f);
+}
+
+// (a.x + a.y) + (b.x + b.y) as a normalised pair
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
+    const float s = __fadd_rn(a.x, b.x);
+    const float bb = __fsub_rn(s, a.x);
+    float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+    e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+
+// KC consecutive values of a node (KC = 1, 2, 4): vector loads and stores
+// where the node's KC values form an aligned 8, 16 or 32-byte group (kp is
+// 1, 2 or a multiple of 4 and a pass starts at a multiple of KC)
+template <int KC> __device__ __forceinline__ void load_pairs(const float2 *__restrict__ p, float2 *v) {
+    if constexpr (KC == 4) {
+        const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+        v[0] = make_float2(a.x, a.y); v[1] = make_float2(a.z, a.w); v[2] = make_float2(b.x, b.y); v[3] = make_float2(b.z, b.w);
+    } else if constexpr (KC == 2) {
+        const float4 a = reinterpret_cast<const float4 *>(p)[0];
+        v[0] = make_float2(a.x, a.y); v[1] = make_float2(a.z, a.w);
+    } else {
+        v[0] = p[0];
+    }
+}
+template <int KC> __device__ __forceinline__ void store_pairs(float2 *p, const float2 *v) {
+    if constexpr (KC == 4) {
+        reinterpret_cast<float4 *>(p)[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+        reinterpret_cast<float4 *>(p)[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+    } else if constexpr (KC == 2) {
+        reinterpret_cast<float4 *>(p)[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+    } else {
+        p[0] = v[0];
+    }
+}
+template <int KC> __device__ __forceinline__ void store_leading(float *p, const float2 *v) {
+    if constexpr (KC == 4) reinterpret_cast<float4 *>(p)[0] = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
+    else if constexpr (KC == 2) reinterpret_cast<float2 *>(p)[0] = make_float2(v[0].x, v[1].x);
+    else p[0] = v[0].x;
+}
+
+// Up-sweep, mixed: k_up_blk with the block's sums in FP32 pairs, one thread
+// per node carrying KC right-hand sides; CTA (block, y) takes columns
+// y*KC .. y*KC+KC-1 of all kp (the padding columns k..kp-1 get zero
+// charges), so the column groups of a block run side by side. A leaf's charge is its input
+// (normalised in FP64 first when the step asks for it) rounded to FP32,
+// times the FP32 Jacobi reciprocal when rs is set; node charges go to Qf
+// (the pair's leading part), the block root's pair to rootq for the top
+// pass.
+template <int KC>
+__global__ void __launch_bounds__(kSweepThreads, 8) k_up_blk32(const SweepPlan plan, const double *in, int64_t ld, int k, int kp,
+                                                                const float *__restrict__ rs, float *__restrict__ Qf,
+                                                                float2 *__restrict__ rootq, const StepScale sc) {
+    extern __shared__ __align__(16) float2 shp[];
+    float2 *val = shp;                                                // (2 kBlockLeaves - 1) x KC
+    uint32_t *kids = (uint32_t *)(shp + (2 * kBlockLeaves - 1) * KC);  // kBlockLeaves
+    int32_t *lbl = (int32_t *)(kids + kBlockLeaves);                  // kBlockLeaves
+    int32_t *lp = lbl + kBlockLeaves;                                 // kBlockLeaves + 1
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b], lv0 = plan.blk_lvl_first[b], H = plan.blk_nlvls[b];
+    const int base = plan.blk_node_first[b], ni = nl - 1;
+    for (int t = tid; t < ni; t += blockDim.x) {
+        kids[t] = plan.lvl_kids[base + t];
+        lbl[t] = plan.lvl_nodes[base + t];
+    }
+    for (int t = tid; t <= H; t += blockDim.x) lp[t] = plan.lvl_ptr[lv0 + t] - base;
+    const int step = sc.hn ? *sc.iter : 0;
+    double *Vi = step > 0 ? sc.Vp[step] : NULL;
+    const int c0 = blockIdx.y * KC;
+    {
+        for (int i = tid; i < nl; i += blockDim.x) {
+            const int j = lf + i;
+            double x[KC];
+#pragma unroll
+            for (int r = 0; r < KC; r++) x[r] = c0 + r < k ? in[(int64_t)(c0 + r) * ld + j] : 0.0;
+            if (Vi) {
+                const int g = sc.leaf_geom[j] * k;
+#pragma unroll
+                for (int r = 0; r < KC; r++) {
+                    if (c0 + r < k && sc.active[g + c0 + r]) {
+                        x[r] = sc.recip ? x[r] * sc.hn[g + c0 + r] : x[r] / sc.hn[g + c0 + r];
+                        const int64_t at = (int64_t)(c0 + r) * ld + j;
+                        const_cast<double *>(in)[at] = x[r];
+                        Vi[at] = x[r];
+                    }
+                }
+            }
+            const float sj = rs ? rs[j] : 1.0f;
+            float2 q[KC];
+#pragma unroll
+            for (int r = 0; r < KC; r++) q[r] = make_float2(rs ? d2f_bits(x[r]) * sj : d2f_bits(x[r]), 0.0f);
+            store_pairs<KC>(val + i * KC, q);
+            store_leading<KC>(Qf + (int64_t)j * kp + c0, q);
+            if (ni == 0) store_pairs<KC>(rootq + (int64_t)b * kp + c0, q);
+        }
+        __syncthreads();
+        for (int h = 0; h < H; h++) {
+            const int a = lp[h], cnt = lp[h + 1] - a;
+            for (int t = tid; t < cnt; t += blockDim.x) {
+                const int q = a + t;
+                const uint32_t kd = kids[q];
+                float2 u[KC], w[KC];
+                load_pairs<KC>(val + (kd & 0xffffu) * KC, u);
+                load_pairs<KC>(val + (kd >> 16) * KC, w);
+#pragma unroll
+                for (int r = 0; r < KC; r++) u[r] = f2_add(u[r], w[r]);
+                store_pairs<KC>(val + (nl + q) * KC, u);
+                store_leading<KC>(Qf + (int64_t)lbl[q] * kp + c0, u);
+                if (q == ni - 1) store_pairs<KC>(rootq + (int64_t)b * kp + c0, u);  // the root is the block's last (highest) node
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Top pass, mixed: k_up_top with FP32 pairs in shared memory, one CTA per
+// group of KC right-hand sides, one thread per node.
+template <int KC>
+__global__ void __launch_bounds__(1024) k_up_top32(const SweepPlan plan, int kp, const float2 *__restrict__ rootq,
+                                                   float *__restrict__ Qf) {
+    extern __shared__ __align__(16) float2 shp[];
+    const int nb = plan.n_blocks, T = plan.n_top, nh = plan.n_top_levels, tid = threadIdx.x;
+    float2 *val = shp;                                       // (nb + T) x KC
+    int2 *kids = (int2 *)(shp + (int64_t)(nb + T) * KC);     // T
+    int32_t *lbl = (int32_t *)(kids + T);                    // T
+    int32_t *hp = lbl + T;                                   // nh + 1
+    for (int t = tid; t < T; t += blockDim.x) {
+        kids[t] = plan.top_kids[t];
+        lbl[t] = plan.top_nodes[t];
+    }
+    for (int t = tid; t <= nh; t += blockDim.x) hp[t] = plan.top_hptr[t];
+    const int c0 = blockIdx.x * KC;
+    {
+        for (int bb = tid; bb < nb; bb += blockDim.x) {
+            float2 v[KC];
+            load_pairs<KC>(rootq + (int64_t)bb * kp + c0, v);
+            store_pairs<KC>(val + bb * KC, v);
+        }
+        __syncthreads();
+        for (int h = 0; h < nh; h++) {
+            const int a = hp[h], cnt = hp[h + 1] - a;
+            if (cnt == 0) continue;  // uniform: every thread reads the same offsets
+            for (int t = tid; t < cnt; t += blockDim.x) {
+                const int q = a + t;
+                const int2 kd = kids[q];
+                float2 u[KC], w[KC];
+                load_pairs<KC>(val + (int64_t)kd.x * KC, u);
+                load_pairs<KC>(val + (int64_t)kd.y * KC, w);
+#pragma unroll
+                for (int r = 0; r < KC; r++) u[r] = f2_add(u[r], w[r]);
+                store_pairs<KC>(val + (int64_t)(nb + q) * KC, u);
+                store_leading<KC>(Qf + (int64_t)lbl[q] * kp + c0, u);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// The same pass through device memory (forests too large for shared
+// memory): the top nodes' pairs go to Qp (n_nodes x kp).
+__global__ void __launch_bounds__(1024) k_up_top32_global(const SweepPlan plan, int kp, const float2 *__restrict__ rootq,
+                                                          float2 *Qp, float *__restrict__ Qf) {
+    const int nb = plan.n_blocks, nh = plan.n_top_levels;
+    for (int h = 0; h < nh; h++) {
+        const int a = plan.top_hptr[h], cnt = plan.top_hptr[h + 1] - a;
+        if (cnt == 0) continue;
+        for (int t = threadIdx.x; t < cnt * kp; t += blockDim.x) {
+            int q = a + t / kp, r = t - (t / kp) * kp;
+            int2 kd = plan.top_kids[q];
+            float2 l = kd.x < nb ? rootq[(int64_t)kd.x * kp + r] : Qp[(int64_t)plan.top_nodes[kd.x - nb] * kp + r];
+            float2 rt = kd.y < nb ? rootq[(int64_t)kd.y * kp + r] : Qp[(int64_t)plan.top_nodes[kd.y - nb] * kp + r];
+            float2 sum = f2_add(l, rt);
+            int64_t o = (int64_t)plan.top_nodes[q] * kp + r;
+            Qp[o] = sum;
+            Qf[o] = sum.x;
+        }
+        __syncthreads();  // this level's charges are visible to the CTA's next level
+    }
+}
+
+// Down-sweep, mixed: k_down_blk with the link potentials (the link
+// product's compensated (sum, correction) pairs) propagated in FP32 pairs,
+// one thread per node carrying KC right-hand sides; CTA (block, y) takes
+// columns y*KC .. y*KC+KC-1. Every internal node, level by level from the
+// root, adds its A to both children's P (an internal child's sum is its A,
+// a leaf's is its potential P(leaf) + A(parent)); every leaf writes
+// v = x * sr + potential in FP64 for its columns below k, sr being the
+// leaf's self term times its Jacobi scale.
+template <int KC>
+__global__ void __launch_bounds__(kSweepThreads, 8) k_down_blk32(const SweepPlan plan, const double *__restrict__ in, int64_t ld,
+                                                                 int k, int kp, const double *__restrict__ sr,
+                                                                 const float2 *__restrict__ P, double *__restrict__ out) {
+    extern __shared__ __align__(16) float2 shp[];
+    float2 *pv = shp;                                    // (2 kBlockLeaves - 1) x KC: P, then A (potential at leaves)
+    float2 *cp = pv + (2 * kBlockLeaves - 1) * KC;       // kMaxChain x KC: P of the root's ancestors
+    double *ss = (double *)(cp + kMaxChain * KC);        // kBlockLeaves: leaf self x scale
+    uint32_t *kids = (uint32_t *)(ss + kBlockLeaves);    // kBlockLeaves
+    int32_t *lbl = (int32_t *)(kids + kBlockLeaves);     // kBlockLeaves: internal node labels
+    int32_t *chl = lbl + kBlockLeaves;                   // kMaxChain: ancestor labels
+    int32_t *lp = chl + kMaxChain;                       // kBlockLeaves + 1
+    const int b = blockIdx.x, tid = threadIdx.x, c0 = blockIdx.y * KC;
+    const int lf = plan.blk_leaf_first[b], nl = plan.blk_nleaves[b], lv0 = plan.blk_lvl_first[b], H = plan.blk_nlvls[b];
+    const int base = plan.blk_node_first[b], ni = nl - 1;
+    const int ch0 = plan.blk_chain[b], nc = plan.blk_chain[b + 1] - ch0;
+    for (int t = tid; t < kBlockLeaves; t += blockDim.x) {
+        if (t < ni) {
+            kids[t] = plan.lvl_kids[base + t];
+            lbl[t] = plan.lvl_nodes[base + t];
+        }
+        if (t < nl) ss[t] = sr[lf + t];
+        if (t < nc) chl[t] = plan.chain[ch0 + t];
+    }
+    for (int t = tid; t <= H; t += blockDim.x) lp[t] = plan.lvl_ptr[lv0 + t] - base;
+    // the leaves' link potentials need no label: load them with the labels
+    float2 v[KC];
+    for (int i = tid; i < nl; i += blockDim.x) {
+        load_pairs<KC>(P + (int64_t)(lf + i) * kp + c0, v);
+        store_pairs<KC>(pv + i * KC, v);
+    }
+    __syncthreads();
+    for (int t = tid; t < ni; t += blockDim.x) {
+        load_pairs<KC>(P + (int64_t)lbl[t] * kp + c0, v);
+        store_pairs<KC>(pv + (nl + t) * KC, v);
+    }
+    for (int t = tid; t < nc; t += blockDim.x) {
+        load_pairs<KC>(P + (int64_t)chl[t] * kp + c0, v);
+        store_pairs<KC>(cp + t * KC, v);
+    }
+    __syncthreads();
+    if (tid < KC && nc > 0) {
+        float2 acc = cp[(nc - 1) * KC + tid];
+        for (int j = nc - 2; j >= 0; j--) acc = f2_add(cp[j * KC + tid], acc);
+        // A of the block root (P(leaf) + A(parent) for a single-leaf block)
+        pv[(nl + ni - 1) * KC + tid] = f2_add(pv[(nl + ni - 1) * KC + tid], acc);
+    }
+    __syncthreads();
+    for (int h = H - 1; h >= 0; h--) {
+        const int a = lp[h], cnt = lp[h + 1] - a;
+        for (int t = tid; t < cnt; t += blockDim.x) {
+            const int q = a + t;
+            float2 A[KC], u[KC];
+            load_pairs<KC>(pv + (nl + q) * KC, A);
+            const uint32_t kd = kids[q];
+            const int c1 = kd & 0xffffu, c2 = kd >> 16;
+            load_pairs<KC>(pv + c1 * KC, u);
+#pragma unroll
+            for (int r = 0; r < KC; r++) u[r] = f2_add(u[r], A[r]);
+            store_pairs<KC>(pv + c1 * KC, u);
+            load_pairs<KC>(pv + c2 * KC, u);
+#pragma unroll
+            for (int r = 0; r < KC; r++) u[r] = f2_add(u[r], A[r]);
+            store_pairs<KC>(pv + c2 * KC, u);
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < nl; i += blockDim.x) {
+        const int j = lf + i;
+        double x[KC];
+#pragma unroll
+        for (int r = 0; r < KC; r++) x[r] = c0 + r < k ? in[(int64_t)(c0 + r) * ld + j] : 0.0;
+        float2 pt[KC];
+        load_pairs<KC>(pv + i * KC, pt);
+        const double sj = ss[i];
+#pragma unroll
+        for (int r = 0; r < KC; r++)
+            if (c0 + r < k) out[(int64_t)(c0 + r) * ld + j] = fma(x[r], sj, f2d_bits(pt[r].x)) + f2d_bits(pt[r].y);
     }
 }
 
@@ -2151,6 +2461,9 @@ int context_init(DeviceContext &ctx, int device) {
     // the up-sweep's top pass holds the whole top forest in shared memory
     FCG_CK(cudaFuncSetAttribute(k_up_top<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
     FCG_CK(cudaFuncSetAttribute(k_up_top<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
+    FCG_CK(cudaFuncSetAttribute(k_up_top32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
+    FCG_CK(cudaFuncSetAttribute(k_up_top32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
+    FCG_CK(cudaFuncSetAttribute(k_up_top32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.smem_optin));
     FCG_CK(cudaMemGetInfo(&ctx.free_bytes, &ctx.total_bytes));
     cudaStream_t st;
     FCG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -3077,7 +3390,11 @@ int problem_create(DeviceContext &ctx, const fcg_model_arrays &a, int precision,
     tr.mark("device model and layout");
     tr.dreport();
     FCG_TRY(dalloc(&p->self, Np, p->bytes));
-    if (precision == FCG_PREC_MIXED) FCG_TRY(dalloc(&p->rself, Np, p->bytes));
+    if (precision == FCG_PREC_MIXED) {
+        FCG_TRY(dalloc(&p->rself, Np, p->bytes));
+        FCG_TRY(dalloc(&p->rself32, Np, p->bytes));
+        FCG_TRY(dalloc(&p->srself, Np, p->bytes));
+    }
     if (precision == FCG_PREC_FP64) FCG_TRY(dalloc(&p->coef64, a.n_links, p->bytes));
     else FCG_TRY(dalloc(&p->coef32, a.n_links, p->bytes));
     FCG_TRY(dalloc(&p->status, 1, p->bytes));
@@ -3112,7 +3429,7 @@ void problem_destroy(DeviceProblem *p) {
     AllocScope alloc_scope(p->stream);
     dfree(p->geo); dfree(p->link_ptr); dfree(p->link_src); dfree(p->leaf_node); dfree(p->parent);
     dfree(p->left); dfree(p->right); dfree(p->node_lfirst); dfree(p->leaf_eb); dfree(p->leaf_ea); dfree(p->leaf_weight);
-    dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->rself); dfree(p->status);
+    dfree(p->coef64); dfree(p->coef32); dfree(p->self); dfree(p->rself); dfree(p->rself32); dfree(p->srself); dfree(p->status);
     dfree(p->near_link); dfree(p->near_row); dfree(p->tri); dfree(p->tri32); dfree(p->fill_fp64);
     SweepPlan &pl = p->plan;
     dfree(pl.blk_leaf_first); dfree(pl.blk_nleaves); dfree(pl.blk_lvl_first); dfree(pl.blk_nlvls); dfree(pl.blk_root);
@@ -3265,7 +3582,8 @@ int problem_fill(DeviceProblem *p) {
     }
     if (mixed)
         k_fill_self32<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->tri32, p->leaf_eb, p->leaf_ea,
-                                                               p->self, p->rself, p->status, p->fill_fp64);
+                                                               p->self, p->rself, p->rself32, p->srself, p->status,
+                                                               p->fill_fp64);
     else
         k_fill_self<<<grid_for(p->Np, 256, sms), 256, 0, s>>>(p->Np, p->leaf_node, p->geo, p->leaf_eb, p->leaf_ea, p->self,
                                                              p->status);
@@ -3433,6 +3751,55 @@ static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, 
     // FP64 path divides, as the reference does)
     const int recip = mixed && diag == p->self && p->rself ? 1 : 0;
     const double *dg = recip ? p->rself : diag;
+    // the mixed path's sweeps in FP32 pairs, for Jacobi scaling (the self
+    // terms' reciprocals) or none; any other scaling takes the FP64 sweeps
+    if (mixed && (diag == NULL || recip)) {
+        // KC right-hand sides per thread and pass (over all kp columns)
+        const int KC = kp >= 4 ? 4 : kp;
+        const size_t up32 = (size_t)(2 * kBlockLeaves - 1) * KC * sizeof(float2) + (3 * kBlockLeaves + 1) * sizeof(int32_t);
+        const size_t down32 = (size_t)(2 * kBlockLeaves - 1 + kMaxChain) * KC * sizeof(float2) + kBlockLeaves * sizeof(double) +
+                              (3 * kBlockLeaves + kMaxChain + 1) * sizeof(int32_t);
+        const dim3 bgrid(pl.n_blocks, kp / KC);
+        float2 *rootq = reinterpret_cast<float2 *>(w.Ad);
+        const float *rs = recip ? p->rself32 : NULL;
+        const double *sr = recip ? p->srself : p->self;
+        if (KC == 4) k_up_blk32<4><<<bgrid, kSweepThreads, up32, s>>>(pl, in, Np, k, kp, rs, w.Qf, rootq, sc);
+        else if (KC == 2) k_up_blk32<2><<<bgrid, kSweepThreads, up32, s>>>(pl, in, Np, k, kp, rs, w.Qf, rootq, sc);
+        else k_up_blk32<1><<<bgrid, kSweepThreads, up32, s>>>(pl, in, Np, k, kp, rs, w.Qf, rootq, sc);
+        FCG_CK(cudaGetLastError());
+        int64_t launches = 2;
+        if (pl.n_top > 0) {
+            size_t fixed = (size_t)pl.n_top * (sizeof(int2) + sizeof(int32_t)) + (size_t)(pl.n_top_levels + 1) * sizeof(int32_t);
+            size_t top32 = fixed + (size_t)(pl.n_blocks + pl.n_top) * KC * sizeof(float2);
+            if (top32 <= p->ctx->smem_optin) {
+                if (KC == 4) k_up_top32<4><<<kp / KC, 1024, top32, s>>>(pl, kp, rootq, w.Qf);
+                else if (KC == 2) k_up_top32<2><<<kp / KC, 1024, top32, s>>>(pl, kp, rootq, w.Qf);
+                else k_up_top32<1><<<kp / KC, 1024, top32, s>>>(pl, kp, rootq, w.Qf);
+            } else {
+                k_up_top32_global<<<1, 1024, 0, s>>>(pl, kp, rootq, reinterpret_cast<float2 *>(w.Qd), w.Qf);
+            }
+            FCG_CK(cudaGetLastError());
+            launches++;
+        }
+        if (p->L > 0) {
+            p->timings.link_bytes += p->L * 8 + 8 * (p->Nn + 1) + 12 * (int64_t)k * p->Nn;
+            p->timings.link_launches++;
+            launches++;
+            prof_begin(p);
+            launch_link(p, w, kp, true);
+            prof_end(p);
+            FCG_CK(cudaGetLastError());
+        } else {
+            FCG_CK(cudaMemsetAsync(w.Pf2, 0, n * sizeof(float2), s));
+        }
+        if (KC == 4) k_down_blk32<4><<<bgrid, kSweepThreads, down32, s>>>(pl, in, Np, k, kp, sr, w.Pf2, out);
+        else if (KC == 2) k_down_blk32<2><<<bgrid, kSweepThreads, down32, s>>>(pl, in, Np, k, kp, sr, w.Pf2, out);
+        else k_down_blk32<1><<<bgrid, kSweepThreads, down32, s>>>(pl, in, Np, k, kp, sr, w.Pf2, out);
+        FCG_CK(cudaGetLastError());
+        p->timings.matvecs++;
+        p->timings.launches += launches;
+        return FCG_NORMAL_END;
+    }
     // w.Ad (n_nodes x kp) holds the block roots' charges in block order
     if (mixed) k_up_blk<true><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, w.Ad, sc);
     else k_up_blk<false><<<pl.n_blocks, kSweepThreads, up_smem, s>>>(pl, in, Np, k, kp, kc, dg, recip, w.Qd, w.Qf, w.Ad, sc);
