@@ -531,7 +531,8 @@ def summarize(out, parts, n):
     lat = np.array([x for p_ in parts for x in p_[0]])
     span = max(p_[1] for p_ in parts)
     infos = [o[4] for o in out]
-    return {"solves_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+    return {"requests": int(len(lat)), "solves_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)),
             "span_s": span, "mean_queue_ms": float(np.mean([i["queue_ms"] for i in infos])),
             "mean_build_ms": float(np.mean([i["build_ms"] for i in infos])),
             "mean_fill_ms": float(np.mean([i["fill_ms"] for i in infos])),
@@ -608,6 +609,43 @@ def cpu_serving_sample(paths, budget_s, cores, build_in_subprocess=False):
     return len(est) / sum(est), len(est), est
 
 
+def cpu_sample_subprocess(budget_s):
+    """cpu_serving_sample in a fresh process (no CUDA context, no torch and
+    its OpenMP runtime next to the oracle's): its cpu_baseline object, or
+    the failure."""
+    cores = os.cpu_count() or 1
+    r = subprocess.run([sys.executable, "-X", "faulthandler", os.path.abspath(__file__), "--cpu-sample", str(budget_s)],
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    if r.returncode != 0 or not lines:
+        log(r.stderr[-2000:])
+        return {"value": None, "unit": "solves/s", "cores": cores, "kind": "port",
+                "sample": "failed: exit code %d" % r.returncode}
+    return json.loads(lines[-1])
+
+
+def run_cpu_sample(budget_s):
+    """--cpu-sample: the serving requests in order through the CPU path for
+    about budget_s seconds; prints the cpu_baseline object."""
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    tmp = tempfile.mkdtemp()
+    cores = os.cpu_count() or 1
+    est, n, t_start = [], 0, time.perf_counter()
+    while time.perf_counter() - t_start <= budget_s:
+        path = write_requests([n], tmp)[0]
+        v, _, e = cpu_serving_sample([path], float("inf"), cores)
+        est += e
+        os.unlink(path)
+        n += 1
+    import shutil
+    shutil.rmtree(tmp, ignore_errors=True)
+    print(json.dumps({"value": len(est) / sum(est), "unit": "solves/s", "cores": cores, "kind": "port",
+                      "sample": "requests 0..%d in order: host model build + FP64 fill + the first conductor's "
+                                "GMRES, extrapolated to every conductor (%.1f s of CPU work)" % (n - 1, sum(est))}),
+          flush=True)
+
+
 def load_request_arrays(path, build_in_subprocess):
     """(model arrays, conductors, host build seconds) of a request file. In a
     subprocess, the CPU arm builds the model there (it writes an .npz with
@@ -617,7 +655,9 @@ def load_request_arrays(path, build_in_subprocess):
         t0 = time.perf_counter()
         m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"])
         dt = time.perf_counter() - t0
-        return dict(m.arrays), int(sum(1 for k in m.arrays["cond_is_diel"] if not k)), dt
+        # the model's arrays are views of its native storage, freed with it: copy
+        arrays = {k: np.array(v, copy=True) for k, v in m.arrays.items()}
+        return arrays, int(np.sum(arrays["cond_is_diel"] == 0)), dt
     out = path + ".npz"
     code = ("import sys, time, numpy as np; sys.path.insert(0, %r); import fastercap_gb300 as fc; "
             "t0 = time.perf_counter(); m = fc.Model.build(%r, mesh_eps=%r, eps_ratio=%r); "
@@ -657,14 +697,18 @@ def run_serving(args, rank, world, local_rank):
                 j.result()
         for name, prec, width in SERVE_ARMS:
             res[name] = {}
+            # the FP64 arm serves the first --fp64-requests of the same arrival
+            # schedule (both arms run saturated at the top rate, so their
+            # solves/s are the GPU's service rates)
+            n_arm = len(ids) if name == "mixed" else sum(1 for r in ids if r < min(args.requests, args.fp64_requests))
             for lam in rates:
                 headline = name == "mixed" and lam == rates[-1]
                 if headline:
                     with ClockSampler(local_rank) as clk:
-                        out = serve_pass(srv, paths, ids, args.requests, prec, width, lam, world)
+                        out = serve_pass(srv, paths[:n_arm], ids[:n_arm], args.requests, prec, width, lam, world)
                     clk_summary = clk.summary()
                 else:
-                    out = serve_pass(srv, paths, ids, args.requests, prec, width, lam, world)
+                    out = serve_pass(srv, paths[:n_arm], ids[:n_arm], args.requests, prec, width, lam, world)
                 # latencies of every GPU's shard; the job ends with the slowest GPU
                 parts = replicas.gather_to_all(([o[0] for o in out], max(o[1] for o in out)), world)
                 res[name][str(int(lam))] = summarize(out, parts, args.requests)
@@ -691,7 +735,9 @@ def run_serving(args, rank, world, local_rank):
     panels = np.array([x[0] for x in sizes])
     links = np.array([x[1] for x in sizes])
     mixed_top = res["mixed"][top]
+    log("link-product roofline of request 0")
     roof = serving_roofline(ctx, paths[0]) if rank == 0 else None
+    log("converged accuracy sample")
     conv = converged_accuracy(ctx, paths[:args.accuracy_sample]) if rank == 0 and args.accuracy_sample > 0 else None
     result = {
         "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": world, "steps": args.requests,
@@ -725,12 +771,8 @@ def run_serving(args, rank, world, local_rank):
         "clocks": clk_summary,
     }
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        cores = os.cpu_count() or 1
-        v, n, est = cpu_serving_sample(paths, 20.0, cores)
-        result["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                                  "sample": "requests 0..%d in order: host model build + FP64 fill + the first "
-                                            "conductor's GMRES, extrapolated to every conductor (%.1f s of CPU work)"
-                                            % (n - 1, sum(est))}
+        log("CPU sample")
+        result["cpu_baseline"] = cpu_sample_subprocess(20.0)
     if args.sphere and rank == 0:
         result["sphere_327680"] = run_gb300(argparse.Namespace(**{**vars(args), "workload": "sphere_327680"}), rank,
                                             world, local_rank, ctx=ctx, emit=False)
@@ -939,12 +981,18 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
     ap.add_argument("--rates", default="500", help="serving: arrival rates (req/s), comma separated")
     ap.add_argument("--slots", type=int, default=8, help="serving: concurrent jobs")
+    ap.add_argument("--fp64-requests", type=int, default=400,
+                    help="serving: requests the plain FP64 arm serves (the first ones of the same schedule)")
     ap.add_argument("--accuracy-sample", type=int, default=8,
                     help="serving: requests re-solved at GMRES tolerance 1e-8 in both precisions")
     ap.add_argument("--no-sphere", dest="sphere", action="store_false",
                     help="serving: skip the resident 327,680-triangle sphere measured after the requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=float, default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.cpu_sample is not None:
+        run_cpu_sample(args.cpu_sample)
+        return
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3

@@ -201,15 +201,34 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
 
+class _NativeModel:
+    """Owner of a native model: freed when the last view of its arrays (and
+    the Model) is gone."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        try:
+            if self.h is not None:
+                lib().fcg_model_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
 class Model:
     """A refined panel hierarchy with its links (host memory).
 
     ``arrays`` holds numpy views (or owned copies for models made from
-    arrays) of the flattened layout described in ``include/fastercap_gb300.h``.
+    arrays) of the flattened layout described in ``include/fastercap_gb300.h``;
+    a view keeps the native model alive, so the arrays stay valid after the
+    Model itself is closed or dropped.
     """
 
-    def __init__(self, handle, arrays: dict, names: list, info: dict):
+    def __init__(self, handle, arrays: dict, names: list, info: dict, owner=None):
         self._h = handle
+        self._owner = owner
         self.arrays = arrays
         self.names = names
         self.info = info
@@ -271,6 +290,7 @@ class Model:
         _check(L.fcg_model_arrays_get(h, C.byref(a)), "model arrays")
         counts = {"n_nodes": a.n_nodes, "n_nodes+1": a.n_nodes + 1, "n_links": a.n_links, "n_panels": a.n_panels,
                   "n_conductors": a.n_conductors, "n_conductors+1": a.n_conductors + 1}
+        owner = _NativeModel(h)
         arrays = {}
         for name, dt, key, cols in ARRAY_FIELDS:
             n = counts[key] * cols
@@ -279,13 +299,15 @@ class Model:
                 arrays[name] = np.zeros((0,) if cols == 1 else (0, cols), dtype=dt)
                 continue
             buf = (C.c_char * (n * np.dtype(dt).itemsize)).from_address(addr)
+            buf._owner = owner  # the view's buffer keeps the native model alive
             arr = np.frombuffer(buf, dtype=dt, count=n)
             arrays[name] = arr.reshape(-1, cols) if cols > 1 else arr
         nsurf = int(arrays["cond_surf_ptr"][-1])
         buf = (C.c_char * (max(nsurf, 1) * 8)).from_address(a.cond_surf_outperm)
+        buf._owner = owner
         arrays["cond_surf_outperm"] = np.frombuffer(buf, dtype=np.float64, count=max(nsurf, 1))
         names = [L.fcg_model_conductor_name(h, i).decode() for i in range(a.n_conductors)]
-        return cls(h, arrays, names, info)
+        return cls(h, arrays, names, info, owner)
 
     @classmethod
     def _concat_arrays(cls, models) -> tuple:
@@ -357,15 +379,10 @@ class Model:
         _check(lib().fcg_model_arrays_check(C.byref(arr)), "model check")
 
     def close(self):
-        if self._h is not None:
-            lib().fcg_model_free(self._h)
-            self._h = None
-
-    def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass
+        """Drop this Model's hold on the native model (its memory goes with
+        the last view of its arrays)."""
+        self._h = None
+        self._owner = None
 
 
 class Problem:

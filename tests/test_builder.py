@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 import fastercap_gb300 as fc
+from fastercap_gb300 import geometry as geo
 from conftest import MODEL_KEYS, build_from_golden, load_golden
 
 
@@ -72,3 +73,22 @@ def test_parallel_panel_read_matches_sequential(tmp_path, monkeypatch):
     assert par.n_panels == seq.n_panels == 20480
     for k in par.arrays:
         np.testing.assert_array_equal(np.asarray(par.arrays[k]), np.asarray(seq.arrays[k]), err_msg=k)
+
+
+def test_array_views_outlive_model(tmp_path):
+    """A built model's arrays are views of its native storage; they keep it
+    alive after the Model is closed and dropped."""
+    import gc
+
+    path = str(tmp_path / "c.txt")
+    geo.crossing_2x2().write(path)
+    m = fc.Model.build(path, mesh_eps=0.05)
+    src, ptr = m.arrays["link_src"], m.arrays["link_ptr"]
+    expect = (src.copy(), ptr.copy())
+    m.close()
+    del m
+    gc.collect()
+    churn = [bytearray(1 << 20) for _ in range(64)]
+    np.testing.assert_array_equal(src, expect[0])
+    np.testing.assert_array_equal(ptr, expect[1])
+    del churn
