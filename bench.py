@@ -701,6 +701,8 @@ def run_serving(args, rank, world, local_rank):
             # schedule (both arms run saturated at the top rate, so their
             # solves/s are the GPU's service rates)
             n_arm = len(ids) if name == "mixed" else sum(1 for r in ids if r < min(args.requests, args.fp64_requests))
+            if n_arm == 0:
+                continue
             for lam in rates:
                 headline = name == "mixed" and lam == rates[-1]
                 if headline:
@@ -720,12 +722,27 @@ def run_serving(args, rank, world, local_rank):
                 log("serving %s at %g req/s: %.1f solves/s, p50 %.0f ms, p99 %.0f ms" % (
                     name, lam, res[name][str(int(lam))]["solves_s"], res[name][str(int(lam))]["p50_ms"],
                     res[name][str(int(lam))]["p99_ms"]))
+        # latency below saturation: a shorter stream at lower rates (the
+        # plain FP64 arm at the lowest one, under its service rate)
+        lat_rates = [float(x) for x in args.latency_rates.split(",")] if args.latency_rates else []
+        latency = {}
+        for name, prec, width in SERVE_ARMS:
+            for lam in lat_rates if name == "mixed" else lat_rates[:1]:
+                n_arm = sum(1 for r in ids if r < min(args.requests, args.latency_requests))
+                if n_arm == 0:
+                    continue
+                out = serve_pass(srv, paths[:n_arm], ids[:n_arm], args.latency_requests, prec, width, lam, world)
+                parts = replicas.gather_to_all(([o[0] for o in out], max(o[1] for o in out)), world)
+                latency.setdefault(name, {})[str(int(lam))] = summarize(out, parts, args.latency_requests)
+                log("latency %s at %g req/s: %.1f solves/s, p50 %.0f ms, p99 %.0f ms" % (
+                    name, lam, latency[name][str(int(lam))]["solves_s"], latency[name][str(int(lam))]["p50_ms"],
+                    latency[name][str(int(lam))]["p99_ms"]))
         st = srv.stats()
     top = str(int(rates[-1]))
     # per request: the largest per-entry difference of the mixed matrix from
     # the plain FP64 one, and that entry's size relative to its diagonal
     errs, ent = [], []
-    for a, b in zip(caps[("mixed", rates[-1])], caps[("fp64_single_rhs", rates[-1])]):
+    for a, b in zip(caps[("mixed", rates[-1])], caps.get(("fp64_single_rhs", rates[-1]), [])):
         e = np.abs(a - b) / np.abs(b)
         i = np.unravel_index(int(np.argmax(e)), e.shape)
         errs.append(float(e[i]))
@@ -752,11 +769,12 @@ def run_serving(args, rank, world, local_rank):
                 "panels_min_max_mean": [int(panels.min()), int(panels.max()), int(panels.mean())],
                 "links_min_max_mean": [int(links.min()), int(links.max()), int(links.mean())]},
         "serving": res,
+        "latency_below_saturation": latency,
         "mixed_vs_fp64": {"speedup_at_top_rate": mixed_top["solves_s"] / res["fp64_single_rhs"][top]["solves_s"],
                           "max_rel_c_err": max(errs), "requests_compared": len(errs),
                           "requests_above_1e-3": int(sum(e > 1e-3 for e in errs)),
                           "p99_rel_c_err": float(np.percentile(errs, 99)),
-                          "worst_entry_over_its_diagonal": ent[int(np.argmax(errs))]},
+                          "worst_entry_over_its_diagonal": ent[int(np.argmax(errs))]} if errs else None,
         "mixed_vs_fp64_converged": conv,
         "same_result_every_rate": bool(same),
         "server": {"max_running": st["max_running"], "peak_in_use_bytes": st["peak_in_use"], "budget_bytes": st["budget"]},
@@ -981,6 +999,9 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
     ap.add_argument("--rates", default="500", help="serving: arrival rates (req/s), comma separated")
     ap.add_argument("--slots", type=int, default=8, help="serving: concurrent jobs")
+    ap.add_argument("--latency-rates", default="5,20",
+                    help="serving: arrival rates (req/s) of the shorter latency passes (FP64 arm: the first only)")
+    ap.add_argument("--latency-requests", type=int, default=60, help="serving: requests per latency pass")
     ap.add_argument("--fp64-requests", type=int, default=400,
                     help="serving: requests the plain FP64 arm serves (the first ones of the same schedule)")
     ap.add_argument("--accuracy-sample", type=int, default=8,

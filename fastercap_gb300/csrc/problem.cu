@@ -50,6 +50,7 @@ static const int kSweepCols = 4;      // right-hand sides per shared-memory pass
 static const int kSweepThreads = 128;  // threads per sweep CTA
 static const int kMaxK = 32;          // right-hand sides per matvec batch
 static const int kDotChunk = 1024;    // vector elements per CTA in the Krylov kernels
+static const int kDotThreads = 128;   // threads per chunk in k_dots
 static const int kPinSlots = 1024;    // pinned readback slots per context
 static const int kPinSlotInts = 16;
 // link words: source node in the low 29 bits, distance band (0..4) in the top 3
@@ -1095,15 +1096,28 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
 // vectors themselves (the step's normalisation, written back to v and to
 // the basis, and the leaf output v = x * self/diag + potential).
 
-// float -> double by integer operations (exact); zero included, subnormal,
-// infinite and NaN inputs through the conversion instruction
+// float -> double by integer operations (exact for every input: zeros,
+// subnormals, infinities and NaNs included), so no conversion instruction
+// is issued on the FP64 pipe
 __device__ __forceinline__ double f2d_bits(float f) {
-    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu;
-    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (e == 0u || e == 255u) return (double)f;
-    const uint32_t m = u & 0x7fffffu;
-    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | (m >> 3)), (int)(m << 29));
+    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+    uint64_t bits;
+    if (e == 255u) {
+        bits = sign | 0x7ff0000000000000ull | ((uint64_t)m << 29);
+    } else if (e != 0u) {
+        bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    } else if (m == 0u) {
+        bits = sign;
+    } else {  // subnormal: m * 2^-149 with its top bit at position p
+        const int p = 31 - __clz(m);
+        bits = sign | ((uint64_t)(p + 874) << 52) | (((uint64_t)m << (52 - p)) & 0xfffffffffffffull);
+    }
+    return __longlong_as_double((long long)bits);
 }
+
+// the conversion instruction, out of line: only rare inputs take it
+__device__ __noinline__ float d2f_rare(double d) { return (float)d; }
 
 // double -> float, round to nearest even, by integer operations for results
 // in the normal float range (and zero); the rest through the instruction
@@ -1111,7 +1125,7 @@ __device__ __forceinline__ float d2f_bits(double d) {
     const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
     const uint32_t e = (hi >> 20) & 0x7ffu;
     if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-    if (e < 897u || e > 1150u) return (float)d;
+    if (e < 897u || e > 1150u) return d2f_rare(d);
     const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
     uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
     f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry rounds into the exponent
@@ -1967,12 +1981,19 @@ __device__ __forceinline__ void reduce_h_warp(int64_t wid, int lane, int i, int 
                                               const int *__restrict__ active, double *const *__restrict__ Hp);
 
 // With fuse_h set, the last CTA to finish (a ticket on *done) also sums the
-// Hessenberg column (k_reduce_h's work) and resets *done.
-__global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
-                       SegChunks ch, int ks, const int *__restrict__ active, double *__restrict__ partial, int fuse_h, int G,
-                       const int32_t *__restrict__ g_ch_first, const int32_t *__restrict__ g_ch_count,
-                       double *const *__restrict__ Hp, int *done) {
-    __shared__ double sh[8][8];
+// Hessenberg column (k_reduce_h's work) and resets *done. kDotThreads
+// threads per chunk, each holding kDotChunk / kDotThreads elements of w: on
+// GB300 the FP64 pipe bounds this kernel, and the FP64 additions of the
+// cross-lane reductions are paid per group of eight vectors, so fewer,
+// fuller threads spend a smaller share of the pipe on them.
+__global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp,
+                                                      const double *__restrict__ w, SegChunks ch, int ks,
+                                                      const int *__restrict__ active, double *__restrict__ partial, int fuse_h,
+                                                      int G, const int32_t *__restrict__ g_ch_first,
+                                                      const int32_t *__restrict__ g_ch_count, double *const *__restrict__ Hp,
+                                                      int *done) {
+    constexpr int NW = kDotThreads / 32, U = kDotChunk / kDotThreads;
+    __shared__ double sh[NW][8];
     __shared__ int s_last;
     const int T = 8;
     const int nvec = *iter + 1;
@@ -1980,10 +2001,10 @@ __global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *
     if (active[ch.geom[c] * ks + r]) {
     int64_t base = ch.start[c];
     int len = ch.len[c];
-    double wv[kDotChunk / 256];
+    double wv[U];
 #pragma unroll
-    for (int u = 0; u < kDotChunk / 256; u++) {
-        int o = threadIdx.x + u * 256;
+    for (int u = 0; u < U; u++) {
+        int o = threadIdx.x + u * kDotThreads;
         wv[u] = (o < len) ? w[(int64_t)r * Np + base + o] : 0.0;
     }
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1995,8 +2016,8 @@ __global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *
             if (j0 + t < nvec) {
                 const double *v = Vp[j0 + t] + (int64_t)r * Np + base;
 #pragma unroll
-                for (int u = 0; u < kDotChunk / 256; u++) {
-                    int o = threadIdx.x + u * 256;
+                for (int u = 0; u < U; u++) {
+                    int o = threadIdx.x + u * kDotThreads;
                     if (o < len) acc[t] += v[o] * wv[u];
                 }
             }
@@ -2031,7 +2052,7 @@ __global__ void k_dots(int64_t Np, const int *__restrict__ iter, double *const *
         __syncthreads();
         if (threadIdx.x < T && j0 + threadIdx.x < nvec) {
             double sum = 0.0;
-            for (int ww = 0; ww < 8; ww++) sum += sh[ww][threadIdx.x];
+            for (int ww = 0; ww < NW; ww++) sum += sh[ww][threadIdx.x];
             partial[((int64_t)r * nvec + j0 + threadIdx.x) * ch.n + c] = sum;
         }
         __syncthreads();
@@ -4455,7 +4476,7 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     // classical Gram-Schmidt against q_0..q_i, per solve; for a few solves
     // the Hessenberg column is summed by the last CTA of k_dots
     const bool fuse_h = a.S <= 4;
-    k_dots<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial, fuse_h ? 1 : 0, a.G,
+    k_dots<<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial, fuse_h ? 1 : 0, a.G,
                                             p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
     if (!fuse_h)
         k_reduce_h<<<gh, 256, 0, s>>>(a.k, a.G, a.nch, p->d_it, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->Hptr);
