@@ -803,6 +803,41 @@ def run_serving(args, rank, world, local_rank):
         torch.distributed.destroy_process_group()
 
 
+def run_request(args):
+    """--workload request: one serving request (--request-id) as a server slot
+    runs it, for profiling: the input file built on the GPU, then --steps
+    resident fills and solves (mixed, all conductors batched, no launch-shape
+    measurement), each timed with CUDA events on the problem's stream. Prints
+    one JSON line of its own (not the benchmark line)."""
+    import fastercap_gb300 as fc
+    from fastercap_gb300 import build as fbuild
+    fbuild.build(reference=False)
+    tmp = tempfile.mkdtemp()
+    path = write_requests([args.request_id], tmp)[0]
+    ctx = fc.Context(0)
+    t0 = time.perf_counter()
+    m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"], ctx=ctx)
+    build_s = time.perf_counter() - t0
+    p = ctx.problem(m, fc.PREC_MIXED)
+    p.set_tuning(False)
+    times, it, st = [], None, None
+    for _ in range(args.steps):
+        p.reset_stats()
+        t0 = time.perf_counter()
+        p.fill()
+        cap, it = p.solve(tol=SERVING["tol"])
+        times.append(1000.0 * (time.perf_counter() - t0))
+        st = p.stats()
+    print(json.dumps({"workload": "request", "request_id": args.request_id, "panels": m.n_panels, "links": m.n_links,
+                      "conductors": len(m.conductor_names), "gpu_build_s": build_s, "step_ms": times,
+                      "fill_ms": st["fill_ms"], "solve_ms": st["solve_ms"], "iterations": [int(x) for x in it],
+                      "rhs_width": int(st["rhs_width"]), "kernel_launches": int(st["kernel_launches"])}), flush=True)
+    p.close()
+    ctx.close()
+    import shutil
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
 def run_reference_serving(args, rank, world):
     """CPU arm for serving: the oracle port on every host core, on the
     requests in order (warmup ones first); per step one request's host model
@@ -995,7 +1030,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="serving", choices=sorted(WORKLOADS) + sorted(MULTI) + ["serving"])
+    ap.add_argument("--workload", default="serving", choices=sorted(WORKLOADS) + sorted(MULTI) + ["serving", "request"])
+    ap.add_argument("--request-id", type=int, default=0, help="request: which serving request to build and solve")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
     ap.add_argument("--rates", default="500", help="serving: arrival rates (req/s), comma separated")
     ap.add_argument("--slots", type=int, default=8, help="serving: concurrent jobs")
@@ -1019,6 +1055,9 @@ def main():
         args.warmup = 3
     rank, world, local_rank = dist_env()
     multi = args.workload in MULTI
+    if args.workload == "request":
+        run_request(args)
+        return
     if args.workload == "serving":
         if args.impl == "reference":
             run_reference_serving(args, rank, world)

@@ -649,8 +649,9 @@ __global__ void k_fill_far(int64_t Nn, const int64_t *__restrict__ ptr, const ui
 // slots of a per-band table (unused slots: the centroid with weight 0) that
 // some lane of its warp needs, so the lanes run the same code whatever
 // their links' bands; the point formula (band 4) uses the centroid offset.
-__global__ void __launch_bounds__(256, 5) k_fill_far32(int64_t Nn, const int64_t *__restrict__ ptr, const uint32_t *__restrict__ src,
-                                                    const NodeGeo *__restrict__ geo, float *__restrict__ c32, unsigned *status) {
+__global__ void __launch_bounds__(256, 5) k_fill_far32(const int32_t *__restrict__ row_split, const int64_t *__restrict__ ptr,
+                                                    const uint32_t *__restrict__ src, const NodeGeo *__restrict__ geo,
+                                                    float *__restrict__ c32, unsigned *status) {
     __shared__ float4 tab[5][6];  // [band][slot] = (weight of v0, of v1, of v2, quadrature weight)
     if (threadIdx.x < 30) {
         int band = threadIdx.x / 6, sl = threadIdx.x % 6;
@@ -674,9 +675,12 @@ __global__ void __launch_bounds__(256, 5) k_fill_far32(int64_t Nn, const int64_t
     __syncthreads();
     const float k = (float)(1.0 / FCG_FOUR_PI_TIMES_E0);
     int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t row = warp; row < Nn; row += nwarps) {
+    // CTA b owns the contiguous rows [row_split[b], row_split[b+1]) (equal
+    // link counts), its warps take every eighth row: consecutive rows share
+    // most of their sources, so the geometry gathers hit L1 and each source
+    // record comes from DRAM about once
+    const int r0 = row_split[blockIdx.x], r1 = row_split[blockIdx.x + 1];
+    for (int64_t row = r0 + (threadIdx.x >> 5); row < r1; row += blockDim.x >> 5) {
         const NodeGeo &g1 = geo[row];
         bool diel = g1.type & FCG_IS_DIEL;
         float nx = 0.0f, ny = 0.0f, nz = 0.0f;
@@ -3586,7 +3590,8 @@ int problem_fill(DeviceProblem *p) {
     bool mixed = p->precision == FCG_PREC_MIXED;
     if (p->L > 0) {
         int grid = (int)std::min<int64_t>((p->Nn * 32 + 255) / 256, (int64_t)sms * 32);
-        if (mixed) k_fill_far32<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef32, p->status);
+        if (mixed)
+            k_fill_far32<<<p->n_row_split, 256, 0, s>>>(p->row_split, p->link_ptr, p->link_src, p->geo, p->coef32, p->status);
         else k_fill_far<<<grid, 256, 0, s>>>(p->Nn, p->link_ptr, p->link_src, p->geo, p->coef64, p->status);
         FCG_CK(cudaGetLastError());
         p->timings.launches++;
