@@ -67,10 +67,12 @@ MULTI = {
 
 
 # DRAM bytes per link-product launch (dram__bytes_read.sum +
-# dram__bytes_write.sum) from one ncu capture of the same kernel and workload
+# dram__bytes_write.sum) from one ncu capture of the same kernel and
+# workload, with the summary that records the capture
 LINK_TRAFFIC = {
-    "sphere_327680": 534.116864e6 + 4.707072e6,    # k_spmv32<1, 16>
-    "crossing8x8_slab": 679.950848e6 + 7.460608e6,  # k_spmv32_multi<16>
+    "sphere_327680": (534.116864e6 + 4.707072e6, "profiles/sphere_327680_kernels_full.md"),  # k_spmv32<1, 16>
+    "crossing8x8_slab": (679.950848e6 + 7.460608e6, "profiles/crossing8x8_slab_spmv32_multi.md"),  # k_spmv32_multi<16>
+    "serving_request0": (282.506752e6 + 16.958976e6, "profiles/serving_request0_kernels.md"),  # k_spmv32_multi<24>
 }
 
 
@@ -561,7 +563,12 @@ def serving_roofline(ctx, path):
             "timing": "CUDA events around every link-product launch of one resident solve of the request",
             "request_panels": m.n_panels, "request_links": m.n_links, "rhs": len(m.conductor_names),
             "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None, "peak_source": peak_kind,
-            "traffic": None, "launches": int(st["link_launches"]), "bytes_per_launch": b, "avg_launch_ms": ms}
+            "traffic": LINK_TRAFFIC["serving_request0"][0], "traffic_source": LINK_TRAFFIC["serving_request0"][1],
+            "launches": int(st["link_launches"]), "bytes_per_launch": b, "avg_launch_ms": ms,
+            "gather_path": "bound by the L1 gather path, not HBM: L1 LSU wavefronts 63.5 % of peak, issue 60 %, "
+                           "DRAM 12 % (ncu, %s)" % LINK_TRAFFIC["serving_request0"][1],
+            "krylov": "k_dots and k_update (34 % of the request's device time) are bound by the FP64 pipe: "
+                      "89 % and 87 % active (ncu, %s)" % LINK_TRAFFIC["serving_request0"][1]}
 
 
 def converged_accuracy(ctx, paths, tol=1e-8):
@@ -998,7 +1005,8 @@ def run_gb300(args, rank, world, local_rank, ctx=None, emit=True):
                      "timing": "CUDA events around every link-product launch, same steps re-run after the timed region",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-                     "traffic": LINK_TRAFFIC.get(args.workload), "launches": int(st["link_launches"]),
+                     "traffic": LINK_TRAFFIC.get(args.workload, (None, None))[0],
+                     "traffic_source": LINK_TRAFFIC.get(args.workload, (None, None))[1], "launches": int(st["link_launches"]),
                      "bytes_per_launch": link_bytes, "avg_launch_ms": link_avg_ms},
         "clocks": clk.summary(),
     }
