@@ -2342,18 +2342,24 @@ __global__ void k_refine_count(int S, const double *__restrict__ nr2, const doub
     if (nb > 0.0 && sqrt(nr2[sidx]) / nb >= tol) atomicAdd(count, 1);
 }
 
-// back substitution R z = g for every solve (one thread each)
+// back substitution R z = g for every solve, one warp each: column by
+// column from the last, the lane that owns z_i divides it by R_ii, then the
+// lanes update z_j -= R_ji z_i for all j < i at once (every z_j sees the
+// same sequence of updates as in a serial column-oriented sweep)
 __global__ void k_backsub(int S, int M, double *const *__restrict__ Hc, const double *g, const int *iters, double *z) {
-    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sidx = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (sidx >= S) return;
-    int it = iters[sidx];
+    const int it = iters[sidx];
     double *zz = z + (int64_t)sidx * (M + 2);
     const double *gg = g + (int64_t)sidx * (M + 2);
-    for (int i = 0; i <= it; i++) zz[i] = gg[i];
+    for (int i = lane; i <= it; i += 32) zz[i] = gg[i];
+    __syncwarp();
     for (int i = it; i >= 0; i--) {
         const double *hc = Hc[i] + (int64_t)sidx * (i + 2);
-        zz[i] = zz[i] / hc[i];
-        for (int j = i - 1; j >= 0; j--) zz[j] = zz[j] - hc[j] * zz[i];
+        const double zi = zz[i] / hc[i];
+        for (int j = lane; j < i; j += 32) zz[j] = zz[j] - hc[j] * zi;
+        if (lane == 0) zz[i] = zi;
+        __syncwarp();
     }
 }
 
@@ -4792,7 +4798,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
                 if (p->cancel.load()) { set_error("solve cancelled"); status = FCG_USER_BREAK; break; }
             }
             if (status != FCG_NORMAL_END) break;
-            k_backsub<<<gs, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
+            k_backsub<<<(S * 32 + 127) / 128, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
             k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
             if (pk == FCG_PRECOND_TWO_LEVEL) {
                 if ((r = precond_apply(p, pk, p->w, p->vv, k))) { status = r; break; }
