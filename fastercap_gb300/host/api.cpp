@@ -459,11 +459,14 @@ struct SolveRun {
     int64_t device_bytes = 0;
 };
 
-// the link construction runs on the console's GPU
+// the mesh refinement and the link construction run on the console's GPU,
+// and the links stay in device memory for the problem built from them (the
+// automatic refinement builds a model per pass: none of them goes through
+// host memory and back)
 static int build_model_at(fcg_context *ctx, const CmdOptions &o, double mesh_eps, fcg_model **m, fcg_model_info &info) {
     fcg_build_options bo = {mesh_eps, o.eps_ratio, o.mesh_curv, o.verbose ? 1 : 0};
-    char ebuf[512];
-    int r = fcg_model_build_on(ctx, o.file.c_str(), &bo, m, ebuf, sizeof ebuf);
+    char ebuf[512] = {0};
+    int r = fcg::model_build_device_links(ctx->dev, o.file.c_str(), &bo, m, ebuf, sizeof ebuf);
     if (r != FCG_NORMAL_END) { printf("Error: %s\n", ebuf); return r; }
     fcg_model_info_get(*m, &info);
     return FCG_NORMAL_END;
