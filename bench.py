@@ -565,10 +565,10 @@ def serving_roofline(ctx, path):
             "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None, "peak_source": peak_kind,
             "traffic": LINK_TRAFFIC["serving_request0"][0], "traffic_source": LINK_TRAFFIC["serving_request0"][1],
             "launches": int(st["link_launches"]), "bytes_per_launch": b, "avg_launch_ms": ms,
-            "gather_path": "bound by the L1 gather path, not HBM: L1 LSU wavefronts 63.5 % of peak, issue 60 %, "
-                           "DRAM 12 % (ncu, %s)" % LINK_TRAFFIC["serving_request0"][1],
-            "krylov": "k_dots and k_update (34 % of the request's device time) are bound by the FP64 pipe: "
-                      "89 % and 87 % active (ncu, %s)" % LINK_TRAFFIC["serving_request0"][1]}
+            "gather_path": "bound by the L1 gather path, not HBM: L1 LSU wavefronts 63.5 pct of peak, issue 60 pct, "
+                           "DRAM 12 pct (ncu, " + LINK_TRAFFIC["serving_request0"][1] + ")",
+            "krylov": "k_dots and k_update (34 pct of the request's device time) are bound by the FP64 pipe: "
+                      "89 and 87 pct active (ncu, " + LINK_TRAFFIC["serving_request0"][1] + ")"}
 
 
 def converged_accuracy(ctx, paths, tol=1e-8):

@@ -35,6 +35,7 @@
 #include <math.h>
 #include <unistd.h>
 #include <chrono>
+#include <atomic>
 #include <thread>
 
 #include "../csrc/fc_potential.h"
@@ -120,6 +121,26 @@ static void parse_panel_fields(const char *line, PanelLine &o) {
 // One physical input file, split the way fgets() with a 512-byte buffer splits
 // it; `eof` marks a final chunk without a newline (the reference's read loop
 // stops before processing such a chunk).
+// fn(0..n-1) on up to 16 host threads (inline when par is false;
+// FCG_HOST_THREADS caps the threads, 1 runs everything inline)
+static const size_t kParallelNodes = 50000;
+template <class F> static void host_parallel(int64_t n, bool par, F fn) {
+    int nt = (int)std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16);
+    if (const char *ht = getenv("FCG_HOST_THREADS")) nt = std::max(1, std::min(nt, atoi(ht)));
+    if (!par || nt <= 1 || n <= 1) {
+        for (int64_t i = 0; i < n; i++) fn(i);
+        return;
+    }
+    nt = (int)std::min<int64_t>(nt, n);
+    std::atomic<int64_t> next(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+        th.emplace_back([&]() {
+            for (int64_t i; (i = next.fetch_add(1)) < n;) fn(i);
+        });
+    for (std::thread &t : th) t.join();
+}
+
 struct InFile {
     std::vector<std::string> lines;
     std::vector<bool> eof;
@@ -852,32 +873,27 @@ struct Builder {
     }
 
     // ---------------------------------------------------------------- flatten
+    // The conductors' trees are walked in post-order side by side (each
+    // conductor's nodes and leaves are one contiguous range, placed by prefix
+    // sums), then the node arrays are written in parallel: the same arrays as
+    // one sequential walk over the conductors in solver order.
     int flatten(Model &M, DeviceContext *dev) {
         const auto t_flat = std::chrono::steady_clock::now();
         size_t ne = el.size();
-        std::vector<int32_t> node_of(ne, -1);
-        std::vector<int32_t> post;
-        post.reserve(ne);
-        int64_t leaf_counter = 0;
-        M.conductors.clear();
-        M.cond_leaf_first.clear();
-        std::vector<int64_t> leaf_first_of(ne, 0), leaf_count_of(ne, 0);
-        std::vector<int32_t> cond_of;
-        for (size_t k = 0; k < order.size(); k++) {
-            Conductor &C = conds[order[k]];
-            int64_t start = leaf_counter;
+        const size_t nc = order.size();
+        std::vector<std::vector<int32_t>> cpost(nc);
+        std::vector<int64_t> cleaves(nc, 0);
+        host_parallel((int64_t)nc, ne >= kParallelNodes, [&](int64_t k) {
+            std::vector<int32_t> &out = cpost[(size_t)k];
             // iterative post-order traversal
             std::vector<std::pair<int32_t, int>> st;
-            st.push_back(std::make_pair(C.top, 0));
+            st.push_back(std::make_pair(conds[order[(size_t)k]].top, 0));
             while (!st.empty()) {
                 std::pair<int32_t, int> &t = st.back();
                 int32_t id = t.first;
                 if (el[id].type & FCG_IS_LEAF) {
-                    leaf_first_of[id] = leaf_counter;
-                    leaf_count_of[id] = 1;
-                    leaf_counter++;
-                    node_of[id] = (int32_t)post.size();
-                    post.push_back(id);
+                    cleaves[(size_t)k]++;
+                    out.push_back(id);
                     st.pop_back();
                 } else if (t.second == 0) {
                     t.second = 1;
@@ -886,45 +902,73 @@ struct Builder {
                     t.second = 2;
                     st.push_back(std::make_pair(el[id].right, 0));
                 } else {
-                    leaf_first_of[id] = leaf_first_of[el[id].left];
-                    leaf_count_of[id] = leaf_count_of[el[id].left] + leaf_count_of[el[id].right];
-                    node_of[id] = (int32_t)post.size();
-                    post.push_back(id);
+                    out.push_back(id);
                     st.pop_back();
                 }
             }
-            cond_of.resize(post.size(), (int32_t)k);
-            C.leaf_count = leaf_counter - start;
-            M.cond_leaf_first.push_back(start);
+        });
+        std::vector<int64_t> node_off(nc + 1, 0), leaf_off(nc + 1, 0);
+        for (size_t k = 0; k < nc; k++) {
+            node_off[k + 1] = node_off[k] + (int64_t)cpost[k].size();
+            leaf_off[k + 1] = leaf_off[k] + cleaves[k];
+        }
+        M.conductors.clear();
+        M.cond_leaf_first.clear();
+        for (size_t k = 0; k < nc; k++) {
+            Conductor &C = conds[order[k]];
+            C.leaf_count = cleaves[k];
+            M.cond_leaf_first.push_back(leaf_off[k]);
             M.conductors.push_back(C);
         }
-        int64_t Nn = (int64_t)post.size(), Np = leaf_counter, L = 2 * (int64_t)pairs.size();
+        int64_t Nn = node_off[nc], Np = leaf_off[nc], L = 2 * (int64_t)pairs.size();
         if (L > 0x7fffffffLL || Nn > 0x7fffffffLL) { err = "model too large for 32-bit link indices"; return FC_OUT_OF_MEMORY; }
+        std::vector<int32_t> node_of(ne, -1), post((size_t)Nn), cond_of((size_t)Nn);
+        std::vector<int64_t> leaf_first_of(ne, 0), leaf_count_of(ne, 0);
+        host_parallel((int64_t)nc, ne >= kParallelNodes, [&](int64_t k) {
+            int64_t n0 = node_off[(size_t)k], leaf = leaf_off[(size_t)k];
+            const std::vector<int32_t> &cp = cpost[(size_t)k];
+            for (size_t t = 0; t < cp.size(); t++) {
+                const int32_t id = cp[t];
+                post[(size_t)n0 + t] = id;
+                node_of[id] = (int32_t)(n0 + (int64_t)t);
+                cond_of[(size_t)n0 + t] = (int32_t)k;
+                if (el[id].type & FCG_IS_LEAF) {
+                    leaf_first_of[id] = leaf++;
+                    leaf_count_of[id] = 1;
+                } else {  // post-order: both children are done
+                    leaf_first_of[id] = leaf_first_of[el[id].left];
+                    leaf_count_of[id] = leaf_count_of[el[id].left] + leaf_count_of[el[id].right];
+                }
+            }
+        });
         M.n_nodes = Nn; M.n_panels = Np; M.n_links = L;
         M.type.resize(Nn); M.left.resize(Nn); M.right.resize(Nn); M.cond.resize(Nn);
         M.leaf_first.resize(Nn); M.leaf_count.resize(Nn); M.link_ptr.assign(Nn + 1, 0);
         M.vert.resize(Nn * 9); M.cent.resize(Nn * 3); M.norm.resize(Nn * 3);
         M.area.resize(Nn); M.maxside.resize(Nn); M.maxside_idx.resize(Nn);
         M.leaf_node.resize(Np); M.leaf_diel.resize(Np);
-        for (int64_t i = 0; i < Nn; i++) {
-            const Element &e = el[post[i]];
-            M.cond[i] = cond_of[i];
-            M.type[i] = e.type;
-            M.left[i] = e.left >= 0 ? node_of[e.left] : -1;
-            M.right[i] = e.right >= 0 ? node_of[e.right] : -1;
-            M.leaf_first[i] = leaf_first_of[post[i]];
-            M.leaf_count[i] = leaf_count_of[post[i]];
-            memcpy(&M.vert[i * 9], e.v, 36);
-            memcpy(&M.cent[i * 3], e.c, 12);
-            memcpy(&M.norm[i * 3], e.n, 12);
-            M.area[i] = e.area;
-            M.maxside[i] = e.maxside;
-            M.maxside_idx[i] = e.maxside_idx;
-            if (e.type & FCG_IS_LEAF) {
-                M.leaf_node[M.leaf_first[i]] = (int32_t)i;
-                M.leaf_diel[M.leaf_first[i]] = (e.type & FCG_IS_DIEL) ? 0 : e.diel;
+        const int64_t kChunk = 4096;
+        host_parallel((Nn + kChunk - 1) / kChunk, Nn >= (int64_t)kParallelNodes, [&](int64_t c) {
+            for (int64_t i = c * kChunk; i < std::min(Nn, (c + 1) * kChunk); i++) {
+                const Element &e = el[post[i]];
+                M.cond[i] = cond_of[i];
+                M.type[i] = e.type;
+                M.left[i] = e.left >= 0 ? node_of[e.left] : -1;
+                M.right[i] = e.right >= 0 ? node_of[e.right] : -1;
+                M.leaf_first[i] = leaf_first_of[post[i]];
+                M.leaf_count[i] = leaf_count_of[post[i]];
+                memcpy(&M.vert[i * 9], e.v, 36);
+                memcpy(&M.cent[i * 3], e.c, 12);
+                memcpy(&M.norm[i * 3], e.n, 12);
+                M.area[i] = e.area;
+                M.maxside[i] = e.maxside;
+                M.maxside_idx[i] = e.maxside_idx;
+                if (e.type & FCG_IS_LEAF) {
+                    M.leaf_node[M.leaf_first[i]] = (int32_t)i;
+                    M.leaf_diel[M.leaf_first[i]] = (e.type & FCG_IS_DIEL) ? 0 : e.diel;
+                }
             }
-        }
+        });
         if (dev) {
             if (getenv("FCG_TRACE"))
                 fprintf(stderr, "[fcg build]   flatten on the host %9.3f ms\n",

@@ -92,3 +92,18 @@ def test_array_views_outlive_model(tmp_path):
     np.testing.assert_array_equal(src, expect[0])
     np.testing.assert_array_equal(ptr, expect[1])
     del churn
+
+
+def test_parallel_flatten_same_model(tmp_path, monkeypatch):
+    """A model large enough for the multi-threaded flatten (70k nodes, 18
+    conductors) is the same, array for array, as the single-threaded one."""
+    path = str(tmp_path / "r.txt")
+    geo.random_crossing(4, 2, 12).write(path)
+    monkeypatch.setenv("FCG_HOST_THREADS", "1")
+    a = fc.Model.build(path, mesh_eps=1e-3)
+    monkeypatch.delenv("FCG_HOST_THREADS")
+    b = fc.Model.build(path, mesh_eps=1e-3)
+    assert a.n_nodes >= 50000
+    for k in MODEL_KEYS:
+        np.testing.assert_array_equal(np.asarray(a.arrays[k]), np.asarray(b.arrays[k]), err_msg=k)
+    assert list(a.names) == list(b.names)
