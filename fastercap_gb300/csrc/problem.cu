@@ -1634,7 +1634,15 @@ __global__ void __launch_bounds__(256) k_spmv32_multi(const int32_t *__restrict_
                                                       const uint32_t *__restrict__ src, const float *__restrict__ coef,
                                                       const float *__restrict__ Q, float2 *__restrict__ P) {
     constexpr int LPL = K / 4, LPW = 32 / LPL;
+    // from 20 columns on (at most six slots) a row's slot sums meet in shared
+    // memory: lane c < K adds the slots' (sum, correction) pairs of column c
+    // in slot order and writes it (fewer instructions than the shuffle tree;
+    // with eight or more slots the extra shared-memory wavefronts cost more
+    // than they save: 16-column slab product 0.538 -> 0.593 ms)
+    constexpr bool SMEM_RED = K >= 20;
+    __shared__ __align__(16) KSum red[SMEM_RED ? 8 : 1][SMEM_RED ? LPW * K : 1];
     int lane = threadIdx.x & 31, li = lane / LPL, ri = lane % LPL;
+    KSum *wred = red[SMEM_RED ? (threadIdx.x >> 5) : 0];
     bool slot_ok = li < LPW;
     const float4 *Q4 = reinterpret_cast<const float4 *>(Q);
     int r0 = row_split[blockIdx.x], r1 = row_split[blockIdx.x + 1];
@@ -1687,12 +1695,32 @@ __global__ void __launch_bounds__(256) k_spmv32_multi(const int32_t *__restrict_
                 kmul_add(acc[0], c0, q0.x); kmul_add(acc[1], c0, q0.y); kmul_add(acc[2], c0, q0.z); kmul_add(acc[3], c0, q0.w);
             }
         }
+        if constexpr (SMEM_RED) {
+            if (slot_ok) {
+                float4 *o = reinterpret_cast<float4 *>(wred + li * K + 4 * ri);
+                o[0] = make_float4(acc[0].s, acc[0].c, acc[1].s, acc[1].c);
+                o[1] = make_float4(acc[2].s, acc[2].c, acc[3].s, acc[3].c);
+            }
+            __syncwarp();
+            if (lane < K) {
+                KSum a = wred[lane];
 #pragma unroll
-        for (int r = 0; r < 4; r++) slot_reduce<LPL, LPW>(acc[r], lane, li);
-        if (li == 0) {
-            float4 *out = reinterpret_cast<float4 *>(P + (int64_t)row * K + 4 * ri);
-            out[0] = make_float4(acc[0].s, acc[0].c, acc[1].s, acc[1].c);
-            out[1] = make_float4(acc[2].s, acc[2].c, acc[3].s, acc[3].c);
+                for (int q = 1; q < LPW; q++) {
+                    const KSum b = wred[q * K + lane];
+                    a.c += b.c;
+                    kadd(a, b.s);
+                }
+                P[(int64_t)row * K + lane] = make_float2(a.s, a.c);
+            }
+            __syncwarp();  // the buffer is reused by the warp's next row
+        } else {
+#pragma unroll
+            for (int r = 0; r < 4; r++) slot_reduce<LPL, LPW>(acc[r], lane, li);
+            if (li == 0) {
+                float4 *out = reinterpret_cast<float4 *>(P + (int64_t)row * K + 4 * ri);
+                out[0] = make_float4(acc[0].s, acc[0].c, acc[1].s, acc[1].c);
+                out[1] = make_float4(acc[2].s, acc[2].c, acc[3].s, acc[3].c);
+            }
         }
     }
 }
