@@ -63,7 +63,9 @@ int problem_get_coefficients(DeviceProblem *p, double *link_coef, double *self_c
 int problem_matvec_host(DeviceProblem *p, const double *q, double *v, int k);
 int problem_matvec_device(DeviceProblem *p, const double *d_q, double *d_v, int k);
 int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int k);
-int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations);
+// all_charges (optional, host, one geometry): every conductor's charge
+// vector, [conductors][n_panels], copied as its batch ends
+int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations, double *all_charges = nullptr);
 int problem_get_charges(DeviceProblem *p, double *charges);
 int problem_set_geometries(DeviceProblem *p, int n, const int32_t *geom_of_cond);
 int problem_n_cond(const DeviceProblem *p);

@@ -4619,7 +4619,7 @@ static int ensure_step_graph(DeviceProblem *p, StepArgs a) {
     return FCG_NORMAL_END;
 }
 
-int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations) {
+int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, int *iterations, double *all_charges) {
     AllocScope alloc_scope(p->stream);
     if (!p->filled) { set_error("coefficients not filled"); return FCG_GENERIC_ERROR; }
     FCG_CK(cudaSetDevice(p->ctx->device));
@@ -4632,6 +4632,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     const int G = p->n_geom;
     const int64_t Np = p->Np;
     const int nch = p->nch;
+    if (all_charges && G != 1) { set_error("charge vectors are kept for one geometry only"); return FCG_GENERIC_ERROR; }
     // per geometry: columns, output offsets, iteration cap (the reference's
     // min(1000, panels) for the geometry alone)
     std::vector<int> ncol(G);
@@ -4879,6 +4880,10 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
         float ms = 0;
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         solve_ms_total += ms;
+        if (all_charges)
+            for (int rr = 0; rr < k && r0 + rr < ncol[0]; rr++)
+                FCG_CK(cudaMemcpy(all_charges + (size_t)(r0 + rr) * Np, p->x + (size_t)rr * Np, (size_t)Np * sizeof(double),
+                                  cudaMemcpyDeviceToHost));
         for (int g = 0; g < G; g++)
             for (int rr = 0; rr < k && r0 + rr < ncol[g]; rr++) {
                 int sidx = g * k + rr, it = it_total[sidx];

@@ -453,6 +453,7 @@ bool parse_cmd(const char *cmd, CmdOptions &o, std::string &err) {
 struct SolveRun {
     std::vector<double> cap;
     std::vector<int> iters;
+    std::vector<double> charges;  // -c: every conductor's panel charges, [conductor][panel]
     fcg_model_info info;
     int nc = 0;
     double build_s = 0, fill_s = 0, solve_s = 0;
@@ -498,7 +499,14 @@ static int solve_model(fcg_context *ctx, fcg_model *m, const CmdOptions &o, doub
         out.cap.assign((size_t)out.nc * out.nc, 0.0);
         out.iters.assign(out.nc, 0);
         fcg_solve_options so = {gmres_tol, kind, 0, 0, (int)dim, 0};
-        r = fcg_problem_solve(p, &so, out.cap.data(), out.iters.data());
+        if (o.out_charge) {
+            // the charge vectors of every conductor's solve (the reference's
+            // m_pCondCharges) for the charge-density files
+            out.charges.assign((size_t)out.nc * (size_t)info.n_panels, 0.0);
+            r = fcg::problem_solve(p->p, so, out.cap.data(), out.iters.data(), out.charges.data());
+        } else {
+            r = fcg_problem_solve(p, &so, out.cap.data(), out.iters.data());
+        }
     }
     if (r != FCG_NORMAL_END && r != FCG_NOT_CONVERGED) {
         printf("Error: %s\n", fcg_last_error());
@@ -564,6 +572,93 @@ static void write_csv(const CmdOptions &o, const SolveRun &run) {
     fclose(f);
 }
 
+// CAutoRefine::OutputFastCapFile / OutputPanelFile / OutputPanel
+// (Solver/Autorefine.cpp:1230-1565): a list file <input without
+// extension>_<suffix>.lst naming one panel file per conductor surface
+// (conductors: one per distinct outer permittivity, dielectric interfaces:
+// one), each holding the conductor's refined panels in leaf order; with
+// charges, every panel line ends with its charge density (charge / area).
+// Names, line formats and the path handling (only a backslash separates a
+// directory in the list file's names) follow the reference, so the files
+// read back as FastCap input.
+// node type bits (include/fastercap_gb300.h): outer permittivity on the
+// normal's side; the side given by the panel's own reference point
+static const uint8_t kOutpermNormalDir = 4, kOutpermElementLevel = 8;
+
+static void write_panel_file(const fcg::Model &M, size_t c, int diel_index, const std::string &name, const std::string &filein,
+                             const std::string &fileout, const double *charges) {
+    FILE *f = fopen(name.c_str(), "w");
+    if (!f) {
+        printf("  Warning: cannot open \"%s\" for writing, skipping\n", name.c_str());
+        return;
+    }
+    fprintf(f, "0 Refined FastCap file derived from %s, referenced in list file %s\n", filein.c_str(), fileout.c_str());
+    fprintf(f, "*\n");
+    const fcg::Conductor &C = M.conductors[c];
+    const int64_t first = M.cond_leaf_first[c];
+    for (int64_t j = first; j < first + C.leaf_count; j++) {
+        if (diel_index >= 0 && M.leaf_diel[(size_t)j] != diel_index) continue;
+        const size_t n = (size_t)M.leaf_node[(size_t)j];
+        const float *v = &M.vert[n * 9];
+        fprintf(f, "T %s  %g %g %g  %g %g %g  %g %g %g", C.name.c_str(), v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8]);
+        const uint8_t t = M.type[n];
+        if (t & kOutpermElementLevel) {
+            // the panel's local dielectric reference point: centroid + the
+            // unit normal toward the outer permittivity
+            double nx = M.norm[n * 3], ny = M.norm[n * 3 + 1], nz = M.norm[n * 3 + 2];
+            if (!(t & kOutpermNormalDir)) { nx = -nx; ny = -ny; nz = -nz; }
+            fprintf(f, "  %g %g %g", (double)M.cent[n * 3] + nx, (double)M.cent[n * 3 + 1] + ny, (double)M.cent[n * 3 + 2] + nz);
+        }
+        if (charges) fprintf(f, "  %e\n", charges[j] / M.area[n]);
+        else fprintf(f, "\n");
+    }
+    fclose(f);
+}
+
+static void write_fastcap_files(const fcg::Model &M, const std::string &path, const std::string &suffix, const double *charges) {
+    // the reference runs in the input's directory: the files go there and
+    // name the input by its bare file name
+    std::string dir, filein = path;
+    size_t sl = filein.rfind('/');
+    if (sl != std::string::npos) {
+        dir = filein.substr(0, sl + 1);
+        filein = filein.substr(sl + 1);
+    }
+    std::string base = filein;
+    size_t pos = base.rfind('.');
+    if (pos != std::string::npos) base.resize(pos);
+    const std::string fileout = base + "_" + suffix + ".lst";
+    FILE *f = fopen((dir + fileout).c_str(), "w");
+    if (!f) {
+        printf("  Warning: cannot open \"%s\" for writing, skipping\n", fileout.c_str());
+        return;
+    }
+    printf("  generating list file \"%s\"\n", fileout.c_str());
+    fprintf(f, "* Refined FastCap file derived from %s\n", filein.c_str());
+    fprintf(f, "*\n");
+    fprintf(f, "* Total number of panels %lu\n", (unsigned long)M.n_panels);
+    fprintf(f, "*\n");
+    for (size_t c = 0; c < M.conductors.size(); c++) {
+        const fcg::Conductor &C = M.conductors[c];
+        std::string cname = base + "_" + C.name + "_" + suffix, nopath = cname;
+        size_t bs = cname.rfind('\\');
+        if (bs != std::string::npos) nopath = cname.substr(bs + 1);
+        if (!C.is_diel) {
+            const size_t ns = C.surf_outperm.size();
+            for (size_t i = 0; i < ns; i++) {
+                const std::string ext = "_" + std::to_string(i) + ".txt";
+                fprintf(f, "C %s  %g  0.0 0.0 0.0%s\n", (nopath + ext).c_str(), C.surf_outperm[i], i + 1 == ns ? "" : " +");
+                write_panel_file(M, c, (int)i, dir + cname + ext, filein, fileout, charges);
+            }
+        } else {
+            fprintf(f, "D %s  %g %g  0.0 0.0 0.0  %g %g %g\n", (nopath + ".txt").c_str(), C.outperm, C.inperm, C.ref[0], C.ref[1],
+                    C.ref[2]);
+            write_panel_file(M, c, -1, dir + cname + ".txt", filein, fileout, charges);
+        }
+    }
+    fclose(f);
+}
+
 static double fnorm(const std::vector<double> &a) {
     double s = 0.0;
     for (double v : a) s += v * v;
@@ -580,11 +675,10 @@ static int run_command_line_impl(const char *command_line) {
         return FCG_COMMAND_LINE_ERROR;
     }
     if (o.galerkin) { printf("Error: the Galerkin scheme (-g) is not supported by the GPU solver\n"); return FCG_COMMAND_LINE_ERROR; }
-    // the refined-geometry and charge-density list files of
-    // CAutoRefine::OutputFastCapFile (Solver/Autorefine.cpp:1230-1565) are not
+    // the input-geometry dump and the kept global charges (-oi, -kc) are not
     // written by this solver: refuse the switches rather than drop the files
-    if (o.out_geo || o.dump_input || o.out_charge || o.keep_charge) {
-        printf("Error: the geometry and charge list files (-o, -oi, -c, -kc) are not written by the GPU solver\n");
+    if (o.dump_input || o.keep_charge) {
+        printf("Error: the input-geometry dump and kept-charge files (-oi, -kc) are not written by the GPU solver\n");
         return FCG_COMMAND_LINE_ERROR;
     }
     if (o.precond & (2 | 8)) {
@@ -684,6 +778,25 @@ static int run_command_line_impl(const char *command_line) {
     if (r == FCG_NORMAL_END) {
         print_stats(o, run);
         if (o.out_cap) write_csv(o, run);
+        // CSolveCap::Run (Solver/SolveCapacitance.cpp:538-568): charge
+        // densities per conductor solve, then the refined geometry
+        if (o.out_charge && m) {
+            printf("\n");
+            const fcg::Model &M = m->m;
+            int capnum = 0;
+            for (size_t c = 0; c < M.conductors.size() && capnum < run.nc; c++) {
+                if (M.conductors[c].is_diel) continue;
+                printf("Outputting charge densities for conductor %s..\n", M.conductors[c].name.c_str());
+                write_fastcap_files(M, o.file, M.conductors[c].name, run.charges.data() + (size_t)capnum * (size_t)M.n_panels);
+                printf("Done\n");
+                capnum++;
+            }
+        }
+        if (o.out_geo && m) {
+            printf("\nOutputting refined geometry in FastCap compatible format..\n");
+            write_fastcap_files(m->m, o.file, "ref", NULL);
+            printf("Done\n");
+        }
         printf("Total time: %fs\n", std::chrono::duration<double>(t2 - t0).count());
     }
     if (ctx) fcg_context_destroy(ctx);

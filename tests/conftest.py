@@ -25,9 +25,10 @@ def pytest_configure(config):
 
 def golden_names():
     """cases with the reference's full model dump (auto_* are console-report
-    fixtures, pin_* compact fixtures of the benchmark-size cases)"""
+    fixtures, out_* the console's -o/-c files, pin_* compact fixtures of the
+    benchmark-size cases)"""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("auto_", "pin_")))
+                  if not os.path.basename(p).startswith(("auto_", "out_", "pin_")))
 
 
 def load_golden(name):

@@ -250,6 +250,36 @@ def main_auto(ref_dir: str, only=()):
             print("%-22s iterations %d, panels %s" % (name, int(out["ref_auto_iterations"]), list(out["ref_auto_panels"])))
 
 
+# -o / -c runs of the reference console: every list and panel file it
+# writes (names relative to the input's directory), with the input saved as
+# <name>.txt, since the file names and contents derive from it
+OUTPUT_CASES = {
+    "out_c22": (lambda: geo.crossing_2x2().text(), ["-m0.05", "-f0"]),
+    "out_slab": (lambda: geo.Crossing(k=2, length=10.0, pitch=3.0, gap=1.0, eps_r=3.9,
+                                      slab=(3.5, 1.0, 3.9, 15.0), name="c2slab").text(), ["-m0.05", "-f0"]),
+}
+
+
+def main_output(ref_dir: str, only=()):
+    make_reference(ref_dir)
+    console = os.path.join(ROOT, "oracle", "_ref", "fcref")
+    for name, (text_fn, switches) in OUTPUT_CASES.items():
+        if only and name not in only:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            text = text_fn()
+            inp = os.path.join(tmp, name + ".txt")
+            with open(inp, "w") as f:
+                f.write(text)
+            subprocess.run([console, inp] + switches + ["-o", "-c"], check=True, capture_output=True, text=True)
+            files = sorted(f for f in os.listdir(tmp) if f != name + ".txt")
+            blob = {f: open(os.path.join(tmp, f)).read() for f in files}
+        out = {"input_text": np.frombuffer(text.encode(), np.uint8), "switches": np.array(switches),
+               "files_json": np.frombuffer(json.dumps(blob).encode(), np.uint8)}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("%-22s %d files" % (name, len(files)))
+
+
 def main(ref_dir: str = "", *only):
     make_reference(ref_dir)
     dump_bin = os.path.join(ROOT, "oracle", "_ref", "fcref_dump")
@@ -277,5 +307,7 @@ if __name__ == "__main__":
         main_pin(args[0], args[1:])
     elif args[1:] and all(a.startswith("auto_") for a in args[1:]):
         main_auto(args[0], args[1:])
+    elif args[1:] and all(a.startswith("out_") for a in args[1:]):
+        main_output(args[0], args[1:])
     else:
         main(*args)

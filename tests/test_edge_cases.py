@@ -154,10 +154,11 @@ def test_cli_two_level_switch_parsed(tmp_path):
     assert fc.run_command_line("fastercap_gb300 %s -ps" % inp) == fc.COMMAND_LINE_ERROR
 
 
-@pytest.mark.parametrize("switch", ["-o", "-oi", "-c", "-kc"])
+@pytest.mark.parametrize("switch", ["-oi", "-kc"])
 def test_cli_refuses_list_file_outputs(tmp_path, switch, capfd):
-    """The refined-geometry and charge list files are not written by this
-    solver: their switches are a command-line error, not silently dropped."""
+    """The input-geometry dump and the kept-charge files are not written by
+    this solver: their switches are a command-line error, not silently
+    dropped."""
     inp = write(tmp_path, "one.txt", ONE_TRIANGLE)
     assert fc.run_command_line("fastercap_gb300 %s %s" % (inp, switch)) == fc.COMMAND_LINE_ERROR
     assert "not written by the GPU solver" in capfd.readouterr().out
@@ -197,3 +198,45 @@ def test_cli_auto_mode_matches_reference(name, tmp_path, capfd):
     # -e: the matrix as <input>.csv
     csv = np.loadtxt(tmp_path / "input.csv", delimiter=",")
     np.testing.assert_allclose(csv, rep["ref_cap"], rtol=1e-5)
+
+
+def _compare_list_file(got: str, ref: str, rtol: float, what: str):
+    """Line by line, token by token: names and %g coordinates equal as text,
+    the trailing %e charge densities within rtol (plus 1e-6 of the file's
+    largest density, for densities that nearly cancel)."""
+    gl, rl = got.splitlines(), ref.splitlines()
+    assert len(gl) == len(rl), what
+    dens = [abs(float(ln.split()[-1])) for ln in rl if ln.startswith("T ") and "e" in ln.split()[-1]]
+    atol = 1e-6 * max(dens) if dens else 0.0
+    for a, b in zip(gl, rl):
+        ta, tb = a.split(), b.split()
+        assert len(ta) == len(tb), (what, a, b)
+        for x, y in zip(ta, tb):
+            if "e-" in y or "e+" in y:
+                assert abs(float(x) - float(y)) <= rtol * abs(float(y)) + atol, (what, a, b)
+            else:
+                assert x == y, (what, a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["out_c22", "out_slab"])
+@pytest.mark.parametrize("prec,rtol", [("-x64", 1e-5), ("-xm", 2e-3)])
+def test_cli_list_files_match_reference(name, prec, rtol, tmp_path, capfd):
+    """-o and -c: the same list and panel files as the reference console's
+    (CAutoRefine::OutputFastCapFile): names, panel lines in leaf order,
+    surfaces, dielectric lines; charge densities within the precision's
+    tolerance (FP64 path 1e-5, mixed 2e-3)."""
+    import json
+    import os
+    g = load_golden(name)
+    ref = json.loads(bytes(g["files_json"]).decode())
+    inp = tmp_path / (name + ".txt")
+    inp.write_bytes(bytes(g["input_text"]))
+    sw = " ".join(str(x) for x in g["switches"])
+    code = fc.run_command_line("fastercap_gb300 %s %s -o -c %s" % (inp, sw, prec))
+    out = capfd.readouterr().out
+    assert code == fc.NORMAL_END, out
+    got = sorted(f for f in os.listdir(tmp_path) if f != inp.name)
+    assert got == sorted(ref), out
+    for f in ref:
+        _compare_list_file((tmp_path / f).read_text(), ref[f], rtol, f)
