@@ -29,10 +29,10 @@ CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-un
 # reference source tree for the oracle build: FCG_REFERENCE_DIR, else the
 # default location named by oracle/Makefile (the recipe that reads it)
 REFERENCE = os.environ.get("FCG_REFERENCE_DIR")
-# per-file device flags: the link construction and the mesh refinement round
-# every operation like the host builder (no fused multiply-add), so both take
-# the same decisions
-CU_FLAGS = {"link_build.cu": ["-fmad=false"], "mesh_build.cu": ["-fmad=false"]}
+# per-file device flags: the link construction, the mesh refinement and the
+# super hierarchy round every operation like the host builder (no fused
+# multiply-add), so both take the same decisions and make the same elements
+CU_FLAGS = {"link_build.cu": ["-fmad=false"], "mesh_build.cu": ["-fmad=false"], "super_build.cu": ["-fmad=false"]}
 
 LIB = os.path.join(HERE, "libfastercap_gb300.so")
 CLI = os.path.join(HERE, "fastercap_gb300")

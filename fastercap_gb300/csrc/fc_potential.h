@@ -745,6 +745,86 @@ FCG_HD fcg_d3 fcg_geo_normal(const E &e) {
     return fcg_widen(e.n);
 }
 
+// CAutoPanel::MakeSuperPanel (Solver/AutoPanel.cpp:209-379): the super node
+// of two elements: area-weighted centroid and outer-permittivity normal, and
+// an equilateral synthetic triangle of the summed area in the plane of that
+// normal. Host and device builders share this code (FP64, no contraction),
+// so both make the same super nodes bit for bit; lid and rid are the
+// children's element ids.
+#define FCG_2_DIV_4TH_ROOT_27 0.87738267530166164054614593453133
+#define FCG_2_DIV_4TH_ROOT_3 1.5196713713031850946623755013091
+#define FCG_M05_PLUS_SQR2_DIV_4 -0.14644660940672623779957781894758
+#define FCG_05_PLUS_SQR2_DIV_4 0.85355339059327376220042218105242
+#define FCG_SQR2 1.4142135623730950488016887242097
+template <class E>
+FCG_HD void fcg_make_super(const E &L, const E &R, int lid, int rid, E &e) {
+    const bool ld = (L.type & FCG_IS_DIEL) != 0, rd = (R.type & FCG_IS_DIEL) != 0;
+    e.type = FCG_IS_LEAF;
+    if (ld && rd) e.type |= (FCG_IS_SUPER_NODE | FCG_IS_DIEL | FCG_OUTPERM_NORMAL_DIR);
+    else e.type |= FCG_IS_SUPER_NODE;
+    e.type &= ~FCG_IS_LEAF;
+    e.left = lid;
+    e.right = rid;
+    e.diel = 0;
+    e.area = L.area + R.area;
+    fcg_d3 cen = fcg_mk((L.c[0] * L.area + R.c[0] * R.area) / e.area, ((double)L.c[1] * L.area + (double)R.c[1] * R.area) / e.area,
+                        ((double)L.c[2] * L.area + (double)R.c[2] * R.area) / e.area);
+    e.c[0] = (float)cen.x;
+    e.c[1] = (float)cen.y;
+    e.c[2] = (float)cen.z;
+    fcg_d3 ln = fcg_widen(L.n), rn = fcg_widen(R.n);
+    if (!(L.type & FCG_OUTPERM_NORMAL_DIR)) ln = fcg_mk(-ln.x, -ln.y, -ln.z);
+    if (!(R.type & FCG_OUTPERM_NORMAL_DIR)) rn = fcg_mk(-rn.x, -rn.y, -rn.z);
+    e.n[0] = (float)((ln.x * L.area + rn.x * R.area) / e.area);
+    e.n[1] = (float)((ln.y * L.area + rn.y * R.area) / e.area);
+    e.n[2] = (float)((ln.z * L.area + rn.z * R.area) / e.area);
+    const double modnormal = fcg_mod(fcg_widen(e.n));
+    fcg_d3 normal;
+    if (modnormal < FCG_PANEL_EPS) {
+        if (fabs(ln.x) > FCG_PANEL_EPS) {
+            normal.x = (-ln.y - ln.z) / ln.x; normal.y = 1.0; normal.z = 1.0;
+        } else if (fabs(ln.y) > FCG_PANEL_EPS) {
+            normal.y = (-ln.x - ln.z) / ln.y; normal.x = 1.0; normal.z = 1.0;
+        } else if (fabs(ln.z) > FCG_PANEL_EPS) {
+            normal.z = (-ln.x - ln.y) / ln.z; normal.x = 1.0; normal.y = 1.0;
+        } else {
+            const fcg_d3 gl = fcg_geo_normal(L), gr = fcg_geo_normal(R);
+            normal = fcg_mk(gl.x * L.area + gr.x * R.area, gl.y * L.area + gr.y * R.area, gl.z * L.area + gr.z * R.area);
+            const double m = fcg_mod(normal);
+            normal = fcg_mk(normal.x / m, normal.y / m, normal.z / m);
+            if (fcg_mod(normal) < FCG_PANEL_EPS) normal = fcg_mk(0.0, 0.0, 1.0);
+        }
+    } else {
+        normal = fcg_mk((double)e.n[0] / modnormal, (double)e.n[1] / modnormal, (double)e.n[2] / modnormal);
+    }
+    fcg_d3 cm = L.area < R.area ? fcg_fsub(L.c, e.c) : fcg_fsub(R.c, e.c);
+    if (fcg_mod(fcg_cross(normal, cm)) < FCG_PANEL_EPS) {
+        cm.x = normal.x * 0.5 + normal.y * FCG_M05_PLUS_SQR2_DIV_4 + normal.z * FCG_05_PLUS_SQR2_DIV_4;
+        cm.y = normal.x * 0.5 + normal.y * FCG_05_PLUS_SQR2_DIV_4 + normal.z * FCG_M05_PLUS_SQR2_DIV_4;
+        cm.z = normal.x * (-FCG_SQR2) + normal.y * 0.5 + normal.z * 0.5;
+    }
+    fcg_d3 xv = fcg_cross(cm, normal);
+    double mx = fcg_mod(xv);
+    xv = fcg_mk(xv.x / mx, xv.y / mx, xv.z / mx);
+    fcg_d3 yv = fcg_cross(normal, xv);
+    double my = fcg_mod(yv);
+    yv = fcg_mk(yv.x / my, yv.y / my, yv.z / my);
+    const double Rr = FCG_2_DIV_4TH_ROOT_27 * sqrt(e.area);
+    const fcg_d3 c = fcg_widen(e.c);
+    e.v[0] = (float)(c.x + yv.x * Rr);
+    e.v[1] = (float)(c.y + yv.y * Rr);
+    e.v[2] = (float)(c.z + yv.z * Rr);
+    const double a = FCG_2_DIV_4TH_ROOT_3 * sqrt(e.area);
+    e.v[3] = (float)((c.x - yv.x * (Rr / 2.0)) - xv.x * (a / 2.0));
+    e.v[4] = (float)((c.y - yv.y * (Rr / 2.0)) - xv.y * (a / 2.0));
+    e.v[5] = (float)((c.z - yv.z * (Rr / 2.0)) - xv.z * (a / 2.0));
+    e.v[6] = (float)((c.x - yv.x * (Rr / 2.0)) + xv.x * (a / 2.0));
+    e.v[7] = (float)((c.y - yv.y * (Rr / 2.0)) + xv.y * (a / 2.0));
+    e.v[8] = (float)((c.z - yv.z * (Rr / 2.0)) + xv.z * (a / 2.0));
+    e.maxside_idx = 0;
+    e.maxside = a;
+}
+
 template <class E>
 FCG_HD void fcg_centroid3(E &e) {
     float sx = e.v[0] + e.v[3], sy = e.v[1] + e.v[4], sz = e.v[2] + e.v[5];

@@ -101,6 +101,15 @@ int mesh_refine_device(DeviceContext &ctx, std::vector<Element> &el, const std::
                        const std::vector<uint16_t> &root_meta, double mesh_eps, double mesh_curv, double max_side,
                        double max_area, double &max_mesh_eps, int &max_level, std::string &err);
 
+// Super hierarchy on the device (csrc/super_build.cu): every conductor's
+// panels (element ids in `el`, conductors in solver order) split by the host
+// recursion's mid-plane rule, the super nodes appended to `el` (made by
+// fcg_make_super, the same elements as the host's) and tops[k] set to
+// conductor k's root element. FC_FILE_ERROR (with err) for coincident
+// centroids or a tree deeper than max_depth.
+int super_build_device(DeviceContext &ctx, std::vector<Element> &el, const std::vector<std::vector<int32_t>> &panels,
+                       std::vector<int32_t> &tops, int max_depth, std::string &err);
+
 // CUDA streams for host code compiled without the CUDA headers
 void *stream_create(int device);
 void stream_destroy(int device, void *stream);

@@ -587,57 +587,10 @@ struct Builder {
     }
 
     int make_super(int lid, int rid) {
-        Element e;
-        const Element &L = el[lid], &R = el[rid];
-        bool ld = L.type & FCG_IS_DIEL, rd = R.type & FCG_IS_DIEL;
+        const bool ld = el[lid].type & FCG_IS_DIEL, rd = el[rid].type & FCG_IS_DIEL;
         if (ld != rd) warn("internal: dielectric sub-panels not coherent in type");
-        if (ld && rd) e.type |= (FCG_IS_SUPER_NODE | FCG_IS_DIEL | FCG_OUTPERM_NORMAL_DIR);
-        else e.type |= FCG_IS_SUPER_NODE;
-        e.type &= ~FCG_IS_LEAF;
-        e.left = lid;
-        e.right = rid;
-        e.area = L.area + R.area;
-        D3 cen = divs(add(scale(widen(L.c), L.area), scale(widen(R.c), R.area)), e.area);
-        store(e.c, cen);
-        D3 ln = widen(L.n), rn = widen(R.n);
-        if (!(L.type & FCG_OUTPERM_NORMAL_DIR)) ln = d3(-ln.x, -ln.y, -ln.z);
-        if (!(R.type & FCG_OUTPERM_NORMAL_DIR)) rn = d3(-rn.x, -rn.y, -rn.z);
-        D3 an = divs(add(scale(ln, L.area), scale(rn, R.area)), e.area);
-        store(e.n, an);
-        double modnormal = mod(widen(e.n));
-        D3 normal;
-        if (modnormal < FCG_PANEL_EPS) {
-            if (fabs(ln.x) > FCG_PANEL_EPS) { normal.x = (-ln.y - ln.z) / ln.x; normal.y = 1.0f; normal.z = 1.0f; }
-            else if (fabs(ln.y) > FCG_PANEL_EPS) { normal.y = (-ln.x - ln.z) / ln.y; normal.x = 1.0f; normal.z = 1.0f; }
-            else if (fabs(ln.z) > FCG_PANEL_EPS) { normal.z = (-ln.x - ln.y) / ln.z; normal.x = 1.0f; normal.y = 1.0f; }
-            else {
-                normal = add(scale(geo_normal(lid), el[lid].area), scale(geo_normal(rid), el[rid].area));
-                normalize(normal);
-                if (mod(normal) < FCG_PANEL_EPS) normal = d3(0, 0, 1);
-            }
-        } else {
-            normal = divs(widen(e.n), modnormal);
-        }
-        D3 cm;
-        if (L.area < R.area) cm = fsub(L.c, e.c);
-        else cm = fsub(R.c, e.c);
-        if (mod(cross(normal, cm)) < FCG_PANEL_EPS) {
-            cm.x = normal.x * 0.5 + normal.y * kMinus05PlusSqr2Div4 + normal.z * k05PlusSqr2Div4;
-            cm.y = normal.x * 0.5 + normal.y * k05PlusSqr2Div4 + normal.z * kMinus05PlusSqr2Div4;
-            cm.z = normal.x * (-kSqr2) + normal.y * 0.5 + normal.z * 0.5;
-        }
-        D3 xv = cross(cm, normal);
-        normalize(xv);
-        D3 yv = cross(normal, xv);
-        normalize(yv);
-        double Rr = k2DivFourthRoot27 * sqrt(e.area);
-        D3 c = widen(e.c);
-        store(e.v, add(c, scale(yv, Rr)));
-        double a = k2DivFourthRoot3 * sqrt(e.area);
-        store(e.v + 3, sub(sub(c, scale(yv, Rr / 2.0)), scale(xv, a / 2.0)));
-        store(e.v + 6, add(sub(c, scale(yv, Rr / 2.0)), scale(xv, a / 2.0)));
-        e.maxside_idx = 0;
-        e.maxside = a;
+        Element e;
+        fcg_make_super(el[lid], el[rid], lid, rid, e);
         el.push_back(e);
         return (int)el.size() - 1;
     }
@@ -687,8 +640,33 @@ struct Builder {
         return make_super(l, r);
     }
 
-    int build_super() {
+    // panel sets of at least this size build their super hierarchy on the
+    // device when there is one (the same tree and elements)
+    static const size_t kDeviceSuperPanels = 20000;
+
+    int build_super(DeviceContext *dev) {
         max_area = max_side = total_area = 0.0;
+        size_t total = 0;
+        for (size_t k = 0; k < order.size(); k++) total += conds[order[k]].panels.size();
+        if (dev && total >= kDeviceSuperPanels) {
+            std::vector<std::vector<int32_t>> sets(order.size());
+            for (size_t k = 0; k < order.size(); k++) {
+                Conductor &C = conds[order[k]];
+                if (C.panels.empty()) { err = "conductor " + C.name + " has no panels"; return FC_FILE_ERROR; }
+                sets[k] = C.panels;
+            }
+            std::vector<int32_t> tops;
+            int r = super_build_device(*dev, el, sets, tops, kMaxDepth, err);
+            if (r != FC_NORMAL_END) return r;
+            for (size_t k = 0; k < order.size(); k++) {
+                Conductor &C = conds[order[k]];
+                C.top = tops[k];
+                if (el[C.top].maxside > max_side) max_side = el[C.top].maxside;
+                if (el[C.top].area > max_area) max_area = el[C.top].area;
+                total_area += el[C.top].area;
+            }
+            return FC_NORMAL_END;
+        }
         for (size_t k = 0; k < order.size(); k++) {
             Conductor &C = conds[order[k]];
             if (C.panels.empty()) { err = "conductor " + C.name + " has no panels"; return FC_FILE_ERROR; }
@@ -1032,7 +1010,7 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
     if (ret != FC_NORMAL_END) { err = B.err; return ret; }
     if (B.order.empty()) { err = "no panels found in the input file"; return FC_FILE_ERROR; }
 
-    if ((ret = B.build_super()) != FC_NORMAL_END) { err = B.err; return ret; }
+    if ((ret = B.build_super(dev)) != FC_NORMAL_END) { err = B.err; return ret; }
     mark("super hierarchy");
 
     // adaptive mesh: mutual refinement of all conductor pairs, then self

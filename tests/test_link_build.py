@@ -125,3 +125,34 @@ def test_mesh_refinement_levels(ctx, tmp_path, meps):
     dev, host = build_pair(ctx, p, mesh_eps=meps)
     assert dev.info["max_mesh_eps"] == host.info["max_mesh_eps"]
     assert_same_model(dev, host)
+
+
+def test_super_hierarchy_sphere_81920(ctx, tmp_path):
+    """81,920 input panels: the super hierarchy is built on the device (every
+    set of at least 20,000 panels); the same tree and super nodes as the host
+    recursion, so the same model bit for bit."""
+    p = str(tmp_path / "s6.txt")
+    geo.write_sphere(p, 6)
+    dev, host = build_pair(ctx, p, mesh_eps=1e30, eps_ratio=1e-33)
+    assert dev.n_panels == 81920
+    assert_same_model(dev, host)
+
+
+def test_super_hierarchy_dielectric_shell(ctx, tmp_path):
+    """A conductor sphere inside a dielectric shell (40,960 input panels, the
+    shell's super nodes dielectric): device and host super hierarchies agree."""
+    V1, T1 = geo.icosphere(5, 1.0)
+    V2, T2 = geo.icosphere(5, 2.0)
+    lines = ["* conductor sphere in a dielectric shell", "C c.txt  3.9  0.0 0.0 0.0",
+             "D d.txt  1.0 3.9  0.0 0.0 0.0  0.0 0.0 3.0", "End", "File c.txt"]
+    for a, b, c in T1:
+        lines.append("T ball  %.9e %.9e %.9e  %.9e %.9e %.9e  %.9e %.9e %.9e" % (*V1[a], *V1[b], *V1[c]))
+    lines += ["End", "File d.txt"]
+    for a, b, c in T2:
+        lines.append("T shell  %.9e %.9e %.9e  %.9e %.9e %.9e  %.9e %.9e %.9e" % (*V2[a], *V2[b], *V2[c]))
+    lines.append("End")
+    p = tmp_path / "shell.txt"
+    p.write_text("\n".join(lines) + "\n")
+    dev, host = build_pair(ctx, str(p), mesh_eps=1e30, eps_ratio=1e-33)
+    assert dev.n_panels == 40960
+    assert_same_model(dev, host)
