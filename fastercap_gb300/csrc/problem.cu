@@ -30,6 +30,7 @@
 #include <thread>
 
 #include "fc_potential.h"
+#include "fp_bits.cuh"
 #include "scan.cuh"
 #include "fcg_internal.hpp"
 
@@ -1099,42 +1100,6 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
 // convert with integer operations; FP64 arithmetic is left for the Krylov
 // vectors themselves (the step's normalisation, written back to v and to
 // the basis, and the leaf output v = x * self/diag + potential).
-
-// float -> double by integer operations (exact for every input: zeros,
-// subnormals, infinities and NaNs included), so no conversion instruction
-// is issued on the FP64 pipe
-__device__ __forceinline__ double f2d_bits(float f) {
-    const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-    const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
-    uint64_t bits;
-    if (e == 255u) {
-        bits = sign | 0x7ff0000000000000ull | ((uint64_t)m << 29);
-    } else if (e != 0u) {
-        bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
-    } else if (m == 0u) {
-        bits = sign;
-    } else {  // subnormal: m * 2^-149 with its top bit at position p
-        const int p = 31 - __clz(m);
-        bits = sign | ((uint64_t)(p + 874) << 52) | (((uint64_t)m << (52 - p)) & 0xfffffffffffffull);
-    }
-    return __longlong_as_double((long long)bits);
-}
-
-// the conversion instruction, out of line: only rare inputs take it
-__device__ __noinline__ float d2f_rare(double d) { return (float)d; }
-
-// double -> float, round to nearest even, by integer operations for results
-// in the normal float range (and zero); the rest through the instruction
-__device__ __forceinline__ float d2f_bits(double d) {
-    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
-    const uint32_t e = (hi >> 20) & 0x7ffu;
-    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-    if (e < 897u || e > 1150u) return d2f_rare(d);
-    const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
-    uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
-    f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // a carry rounds into the exponent
-    return __uint_as_float(f);
-}
 
 // (a.x + a.y) + (b.x + b.y) as a normalised pair
 __device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
