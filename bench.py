@@ -71,7 +71,7 @@ MULTI = {
 # workload, with the summary that records the capture
 LINK_TRAFFIC = {
     "sphere_327680": (534.116864e6 + 4.707072e6, "profiles/sphere_327680_kernels_full.md"),  # k_spmv32<1, 16>
-    "crossing8x8_slab": (679.950848e6 + 7.460608e6, "profiles/crossing8x8_slab_spmv32_multi.md"),  # k_spmv32_multi<16>
+    "crossing8x8_slab": (677.425664e6 + 7.629056e6, "profiles/crossing8x8_slab_spmv32_multi.md"),  # k_spmv32_multi<16>
     "serving_request0": (282.506752e6 + 16.958976e6, "profiles/serving_request0_kernels.md"),  # k_spmv32_multi<24>
 }
 
