@@ -2092,30 +2092,28 @@ __global__ void k_reduce_seg(int nvec, int ks, int G, int nch, const double *__r
 
 // Givens update of Hessenberg column i of active solve sidx; true while the
 // solve goes on
-__device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ Hp, double *cs, double *sn, double *g,
-                           const double *normb, const double *nrm2, double *hnorm, double *rhnorm, double tol, const int *scap,
-                           int *active, int *iters, int *capped) {
-    double *hc = Hp[i] + (int64_t)sidx * (i + 2);
+// one previous rotation applied to (t1, t2), every product rounded before
+// the sum (no contraction: the per-solve and per-warp Givens kernels round
+// the same way)
+__device__ __forceinline__ double rot_lo(double c, double s, double t1, double t2) {
+    return __dsub_rn(__dmul_rn(c, t1), __dmul_rn(s, t2));
+}
+__device__ __forceinline__ double rot_hi(double c, double s, double t1, double t2) {
+    return __dadd_rn(__dmul_rn(c, t2), __dmul_rn(s, t1));
+}
+
+// the rest of a solve's Givens step once its column's previous rotations
+// are applied (hc[0..i-1] rotated, `carry` the running entry i): the new
+// rotation, the right-hand side, the convergence test
+__device__ bool givens_finish(int sidx, int i, int M, double *hc, double carry, double hn, double *cs, double *sn, double *g,
+                              const double *normb, double tol, const int *scap, int *active, int *iters, int *capped) {
     double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2), *gg = g + (int64_t)sidx * (M + 2);
-    double hn = sqrt(nrm2[sidx]);
-    hnorm[sidx] = hn;
-    if (rhnorm) rhnorm[sidx] = 1.0 / hn;
-    hc[i + 1] = hn;
-    // the previous rotations, in order; the running entry stays in a register
-    // so the loads of the next column entries and rotations do not wait on it
-    double carry = hc[0];
-#pragma unroll 8
-    for (int j = 0; j < i; j++) {
-        double t1 = carry, t2 = hc[j + 1];
-        hc[j] = c[j] * t1 - sv[j] * t2;
-        carry = c[j] * t2 + sv[j] * t1;
-    }
     hc[i] = carry;
     double t1 = carry, t2 = hn;
-    double len = sqrt(t1 * t1 + t2 * t2);
+    double len = __dsqrt_rn(__dadd_rn(__dmul_rn(t1, t1), __dmul_rn(t2, t2)));
     c[i] = t1 / len;
     sv[i] = -t2 / len;
-    hc[i] = c[i] * t1 - sv[i] * t2;
+    hc[i] = rot_lo(c[i], sv[i], t1, t2);
     hc[i + 1] = 0;
     t1 = gg[i];
     gg[i] = c[i] * t1;
@@ -2135,14 +2133,64 @@ __device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ H
     return false;
 }
 
-// Givens update of Hessenberg column i of every active solve (one thread each)
-__global__ void k_givens(int S, const int *__restrict__ iter, int M, double *const *__restrict__ Hp, double *cs, double *sn,
-                         double *g, const double *normb, const double *nrm2, double *hnorm, double *rhnorm, double tol,
-                         const int *scap, int *active, int *iters, int *capped, int *n_active_all) {
+__device__ bool givens_one(int sidx, int i, int M, double *const *__restrict__ Hp, double *cs, double *sn, double *g,
+                           const double *normb, const double *nrm2, double *hnorm, double *rhnorm, double tol, const int *scap,
+                           int *active, int *iters, int *capped) {
+    double *hc = Hp[i] + (int64_t)sidx * (i + 2);
+    const double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2);
+    double hn = sqrt(nrm2[sidx]);
+    hnorm[sidx] = hn;
+    if (rhnorm) rhnorm[sidx] = 1.0 / hn;
+    hc[i + 1] = hn;
+    // the previous rotations, in order; the running entry stays in a register
+    // so the loads of the next column entries and rotations do not wait on it
+    double carry = hc[0];
+#pragma unroll 8
+    for (int j = 0; j < i; j++) {
+        double t1 = carry, t2 = hc[j + 1];
+        hc[j] = rot_lo(c[j], sv[j], t1, t2);
+        carry = rot_hi(c[j], sv[j], t1, t2);
+    }
+    return givens_finish(sidx, i, M, hc, carry, hn, cs, sn, g, normb, tol, scap, active, iters, capped);
+}
+
+// Givens update of Hessenberg column i of every active solve, one warp per solve: the lanes load 32 entries of the
+// column and of the previous rotations at a time, and every lane runs the
+// chain of rotations on shuffled values (the same operations in the same
+// order as k_givens), so a step waits for memory once per 32 rotations.
+__global__ void __launch_bounds__(128) k_givens_warp(int S, const int *__restrict__ iter, int M, double *const *__restrict__ Hp,
+                                                     double *cs, double *sn, double *g, const double *normb, const double *nrm2,
+                                                     double *hnorm, double *rhnorm, double tol, const int *scap, int *active,
+                                                     int *iters, int *capped, int *n_active_all) {
     const int i = *iter;
-    int sidx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sidx >= S || !active[sidx]) return;
-    if (givens_one(sidx, i, M, Hp, cs, sn, g, normb, nrm2, hnorm, rhnorm, tol, scap, active, iters, capped))
+    const int sidx = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (sidx >= S || !active[sidx]) return;  // the whole warp
+    double *hc = Hp[i] + (int64_t)sidx * (i + 2);
+    const double *c = cs + (int64_t)sidx * (M + 2), *sv = sn + (int64_t)sidx * (M + 2);
+    const double hn = sqrt(nrm2[sidx]);
+    double carry = hc[0];
+    for (int j0 = 0; j0 < i; j0 += 32) {
+        const int j = j0 + lane, cnt = min(32, i - j0);
+        double cj = 0.0, sj = 0.0, hj = 0.0, out = 0.0;
+        if (j < i) {
+            cj = c[j];
+            sj = sv[j];
+            hj = hc[j + 1];
+        }
+        for (int q = 0; q < cnt; q++) {
+            const double cq = __shfl_sync(0xffffffffu, cj, q), sq = __shfl_sync(0xffffffffu, sj, q);
+            const double t1 = carry, t2 = __shfl_sync(0xffffffffu, hj, q);
+            const double h = rot_lo(cq, sq, t1, t2);
+            carry = rot_hi(cq, sq, t1, t2);
+            if (lane == q) out = h;
+        }
+        __syncwarp();  // every lane has read the entries it overwrites next
+        if (j < i) hc[j] = out;
+    }
+    if (lane != 0) return;
+    hnorm[sidx] = hn;
+    if (rhnorm) rhnorm[sidx] = 1.0 / hn;
+    if (givens_finish(sidx, i, M, hc, carry, hn, cs, sn, g, normb, tol, scap, active, iters, capped))
         atomicAdd(n_active_all + i, 1);
 }
 
@@ -4496,9 +4544,10 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
                                               fuse_end ? 1 : 0, fe, p->d_it + 3);
     int launches = 3 + (fuse_h ? 0 : 1);
     if (!fuse_end) {
-        const int gs = (a.S + 127) / 128, g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
+        const int g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
         k_reduce_seg<<<g1v, 256, 0, s>>>(1, a.k, a.G, a.nch, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->nrm2, 1, 0);
-        k_givens<<<gs, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2, p->hnorm, rhn, a.tol,
+        k_givens_warp<<<(a.S * 32 + 127) / 128, 128, 0, s>>>(a.S, p->d_it, a.M, p->Hptr, p->cs, p->sn, p->g, p->normb, p->nrm2,
+                                                              p->hnorm, rhn, a.tol,
                                     p->scap, p->active, p->iters, p->capped, p->n_active);
         k_iter_advance<<<1, 32, 0, s>>>(p->d_it, p->n_active, a.cap, cancel, p->d_it + 1, a.cond, a.use_cond);
         launches += 3;
