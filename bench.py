@@ -759,6 +759,7 @@ def run_serving(args, rank, world, local_rank):
     panels = np.array([x[0] for x in sizes])
     links = np.array([x[1] for x in sizes])
     mixed_top = res["mixed"][top]
+    lat_top = latency.get("mixed", {}).get(str(int(lat_rates[-1]))) if lat_rates else None
     log("link-product roofline of request 0")
     roof = serving_roofline(ctx, paths[0]) if rank == 0 else None
     log("converged accuracy sample")
@@ -767,7 +768,11 @@ def run_serving(args, rank, world, local_rank):
         "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": world, "steps": args.requests,
         "warmup": 2 * args.slots, "ms_per_step": 1000.0 / mixed_top["solves_s"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 links / f64 Krylov", "data": "synthetic",
-        "p50_ms": mixed_top["p50_ms"], "p99_ms": mixed_top["p99_ms"],
+        # latency under load below the service rate (the highest latency
+        # pass); at the top rate every request waits in the queue
+        "p50_ms": lat_top["p50_ms"] if lat_top else mixed_top["p50_ms"],
+        "p99_ms": lat_top["p99_ms"] if lat_top else mixed_top["p99_ms"],
+        "latency_at_req_s": float(lat_rates[-1]) if lat_top else float(rates[-1]),
         "config": serving_config(args),
         "run": {"slots": args.slots, "parallelism": "request r on GPU r mod N" if world > 1 else "single GPU",
                 "step": "one request: GPU model build + coefficient fill + GMRES over every conductor + C read back; "
