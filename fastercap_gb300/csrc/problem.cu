@@ -28,6 +28,7 @@
 #include <string>
 #include <vector>
 #include <thread>
+#include <type_traits>
 
 #include "fc_potential.h"
 #include "fp_bits.cuh"
@@ -870,8 +871,8 @@ __global__ void k_fill_self(int64_t Np, const int32_t *__restrict__ leaf_node, c
 // threads per CTA keep every block of a large model resident at once.
 // The Arnoldi step's pending normalisation, done by the up-sweep as it reads
 // the step's vector (k_scale's work): q = v / |v| for every active solve,
-// written back to v and to basis vector *iter; nothing at step 0, whose
-// vector is normalised before the loop.
+// written back to v and to basis vector *iter (FP64, or an FP32 pair on the
+// mixed path); nothing at step 0, whose vector is normalised before the loop.
 struct StepScale {
     const double *hn;  // NULL: no normalisation; reciprocals of the norms when recip is set
     int recip;
@@ -912,7 +913,8 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
                 if (sc.active[sidx]) {
                     x = sc.recip ? x * sc.hn[sidx] : x / sc.hn[sidx];
                     const_cast<double *>(in)[at] = x;
-                    Vi[at] = x;
+                    if (MIXED) reinterpret_cast<float2 *>(Vi)[at] = d2pair_bits(x);
+                    else Vi[at] = x;
                 }
             }
             if (diag) x = recip ? x * diag[lf + i] : x / diag[lf + i];
@@ -1098,8 +1100,9 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_down_blk(const SweepPlan 
 // pairs (value = s + c, about 44 significant bits: Knuth's TwoSum for the
 // leading parts, then the trailing parts and a Fast2Sum renormalisation) and
 // convert with integer operations; FP64 arithmetic is left for the Krylov
-// vectors themselves (the step's normalisation, written back to v and to
-// the basis, and the leaf output v = x * self/diag + potential).
+// vectors themselves (the step's normalisation, written back to v in FP64
+// and to the basis as a pair, and the leaf output v = x * self/diag +
+// potential).
 
 // (a.x + a.y) + (b.x + b.y) as a normalised pair
 __device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
@@ -1110,6 +1113,36 @@ __device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
     const float h = __fadd_rn(s, e);
     return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
 }
+
+// acc + a b for pairs a, b: the leading product exactly as p + e (one FMA),
+// the cross terms folded into e, p added to the leading sum by TwoSum and
+// the rounding errors gathered in the trailing part (Ogita, Rump and
+// Oishi's Dot2, 2005, with pair inputs); acc is left unnormalised
+__device__ __forceinline__ float2 f2_fma(float2 acc, float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float s = __fadd_rn(acc.x, p);
+    const float bb = __fsub_rn(s, acc.x);
+    const float err = __fadd_rn(__fsub_rn(acc.x, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    return make_float2(s, __fadd_rn(acc.y, __fadd_rn(err, e)));
+}
+
+// The Krylov kernels' element types: the FP64 path keeps the basis and its
+// sums in FP64; the mixed path stores basis vectors as FP32 pairs (same
+// 8 bytes per element, d2pair_bits) and sums in pairs on the FP32 pipe.
+__device__ __forceinline__ double kv_add(double a, double b) { return a + b; }
+__device__ __forceinline__ float2 kv_add(float2 a, float2 b) { return f2_add(a, b); }
+__device__ __forceinline__ double kv_shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float2 kv_shfl_xor(float2 v, int m) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ __forceinline__ double kv_double(double v) { return v; }
+__device__ __forceinline__ double kv_double(float2 v) { return pair2d(v); }
+template <typename E> __device__ __forceinline__ E kv_zero();
+template <> __device__ __forceinline__ double kv_zero<double>() { return 0.0; }
+template <> __device__ __forceinline__ float2 kv_zero<float2>() { return make_float2(0.0f, 0.0f); }
 
 // KC consecutive values of a node (KC = 1, 2, 4): vector loads and stores
 // where the node's KC values form an aligned 8, 16 or 32-byte group (kp is
@@ -1183,7 +1216,7 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_up_blk32(const SweepPlan p
                         x[r] = sc.recip ? x[r] * sc.hn[g + c0 + r] : x[r] / sc.hn[g + c0 + r];
                         const int64_t at = (int64_t)(c0 + r) * ld + j;
                         const_cast<double *>(in)[at] = x[r];
-                        Vi[at] = x[r];
+                        reinterpret_cast<float2 *>(Vi)[at] = d2pair_bits(x[r]);
                     }
                 }
             }
@@ -1980,17 +2013,22 @@ __device__ __forceinline__ void reduce_h_warp(int64_t wid, int lane, int i, int 
 // With fuse_h set, the last CTA to finish (a ticket on *done) also sums the
 // Hessenberg column (k_reduce_h's work) and resets *done. kDotThreads
 // threads per chunk, each holding kDotChunk / kDotThreads elements of w: on
-// GB300 the FP64 pipe bounds this kernel, and the FP64 additions of the
+// GB300 the FP64 pipe bounds the FP64 variant, and the FP64 additions of the
 // cross-lane reductions are paid per group of eight vectors, so fewer,
-// fuller threads spend a smaller share of the pipe on them.
+// fuller threads spend a smaller share of the pipe on them. PB (the mixed
+// path): basis vectors are FP32 pairs, w is split into pairs once and every
+// product and sum is pair arithmetic on the FP32 pipe (f2_fma, f2_add); the
+// chunk's sums are rounded to FP64 once.
+template <bool PB>
 __global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp,
                                                       const double *__restrict__ w, SegChunks ch, int ks,
                                                       const int *__restrict__ active, double *__restrict__ partial, int fuse_h,
                                                       int G, const int32_t *__restrict__ g_ch_first,
                                                       const int32_t *__restrict__ g_ch_count, double *const *__restrict__ Hp,
                                                       int *done) {
+    using E = typename std::conditional<PB, float2, double>::type;
     constexpr int NW = kDotThreads / 32, U = kDotChunk / kDotThreads;
-    __shared__ double sh[NW][8];
+    __shared__ E sh[NW][8];
     __shared__ int s_last;
     const int T = 8;
     const int nvec = *iter + 1;
@@ -1998,24 +2036,30 @@ __global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__r
     if (active[ch.geom[c] * ks + r]) {
     int64_t base = ch.start[c];
     int len = ch.len[c];
-    double wv[U];
+    E wv[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
         int o = threadIdx.x + u * kDotThreads;
-        wv[u] = (o < len) ? w[(int64_t)r * Np + base + o] : 0.0;
+        const double x = (o < len) ? w[(int64_t)r * Np + base + o] : 0.0;
+        if constexpr (PB) wv[u] = d2pair_bits(x);
+        else wv[u] = x;
     }
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int j0 = 0; j0 < nvec; j0 += T) {
-        double acc[T];
+        E acc[T];
 #pragma unroll
         for (int t = 0; t < T; t++) {
-            acc[t] = 0.0;
+            acc[t] = kv_zero<E>();
             if (j0 + t < nvec) {
-                const double *v = Vp[j0 + t] + (int64_t)r * Np + base;
+                const E *v = reinterpret_cast<const E *>(Vp[j0 + t]) + (int64_t)r * Np + base;
 #pragma unroll
                 for (int u = 0; u < U; u++) {
                     int o = threadIdx.x + u * kDotThreads;
-                    if (o < len) acc[t] += v[o] * wv[u];
+                    if constexpr (PB) {
+                        if (o < len) acc[t] = f2_fma(acc[t], v[o], wv[u]);
+                    } else {
+                        if (o < len) acc[t] += v[o] * wv[u];
+                    }
                 }
             }
         }
@@ -2026,31 +2070,31 @@ __global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__r
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             bool hi = lane & 16;
-            double send = hi ? acc[q] : acc[q + 4];
-            double keep = hi ? acc[q + 4] : acc[q];
-            acc[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+            E send = hi ? acc[q] : acc[q + 4];
+            E keep = hi ? acc[q + 4] : acc[q];
+            acc[q] = kv_add(keep, kv_shfl_xor(send, 16));
         }
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             bool hi = lane & 8;
-            double send = hi ? acc[q] : acc[q + 2];
-            double keep = hi ? acc[q + 2] : acc[q];
-            acc[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+            E send = hi ? acc[q] : acc[q + 2];
+            E keep = hi ? acc[q + 2] : acc[q];
+            acc[q] = kv_add(keep, kv_shfl_xor(send, 8));
         }
         {
             bool hi = lane & 4;
-            double send = hi ? acc[0] : acc[1];
-            double keep = hi ? acc[1] : acc[0];
-            acc[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+            E send = hi ? acc[0] : acc[1];
+            E keep = hi ? acc[1] : acc[0];
+            acc[0] = kv_add(keep, kv_shfl_xor(send, 4));
         }
-        acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 2);
-        acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 1);
+        acc[0] = kv_add(acc[0], kv_shfl_xor(acc[0], 2));
+        acc[0] = kv_add(acc[0], kv_shfl_xor(acc[0], 1));
         if ((lane & 3) == 0) sh[warp][((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = acc[0];
         __syncthreads();
         if (threadIdx.x < T && j0 + threadIdx.x < nvec) {
-            double sum = 0.0;
-            for (int ww = 0; ww < NW; ww++) sum += sh[ww][threadIdx.x];
-            partial[((int64_t)r * nvec + j0 + threadIdx.x) * ch.n + c] = sum;
+            E sum = kv_zero<E>();
+            for (int ww = 0; ww < NW; ww++) sum = kv_add(sum, sh[ww][threadIdx.x]);
+            partial[((int64_t)r * nvec + j0 + threadIdx.x) * ch.n + c] = kv_double(sum);
         }
         __syncthreads();
     }
@@ -2195,8 +2239,9 @@ __global__ void __launch_bounds__(128) k_givens_warp(int S, const int *__restric
 }
 
 // out[r][j] = v[r][j] / hn[solve of (j, r)] for active solves, out = out_fixed
-// or basis vector *iter + vofs; v is rewritten with the same values (it is
-// the input of the next product)
+// or basis vector *iter + vofs (as FP32 pairs when PB); v is rewritten with
+// the same values in FP64 (it is the input of the next product)
+template <bool PB>
 __global__ void k_scale(int64_t Np, int ks, double *__restrict__ v, const double *__restrict__ hn, const int *__restrict__ active,
                         const int32_t *__restrict__ leaf_geom, double *__restrict__ out_fixed, double *const *__restrict__ Vp,
                         const int *__restrict__ iter, int vofs) {
@@ -2208,7 +2253,8 @@ __global__ void k_scale(int64_t Np, int ks, double *__restrict__ v, const double
         int sidx = leaf_geom[j] * ks + r;
         if (active && !active[sidx]) continue;
         double x = v[t] / hn[sidx];
-        out[t] = x;
+        if constexpr (PB) reinterpret_cast<float2 *>(out)[t] = d2pair_bits(x);
+        else out[t] = x;
         v[t] = x;
     }
 }
@@ -2314,9 +2360,14 @@ __device__ void step_end(const StepEnd &e, int i, double *partial, int nch) {
 // v[r] = w[r] - sum_j h_j V_j[r] with the solve's own h; partial |v|^2 per
 // chunk. With fuse_end set, the last CTA to finish (a ticket on *done) also
 // ends the Arnoldi step (step_end: norms, Givens, step index) and resets *done.
-__global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
+// PB (the mixed path): basis vectors are FP32 pairs and each element's
+// subtraction chain runs in pair arithmetic (w and every h_j split into
+// pairs, f2_fma), rounded to FP64 once for v and its norm.
+template <bool PB>
+__global__ void __launch_bounds__(256, PB ? 4 : 1) k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
                          double *const *__restrict__ Hp, SegChunks ch, int ks, const int *__restrict__ active,
                          double *__restrict__ v, double *__restrict__ partial, int fuse_end, StepEnd fe, int *done) {
+    using E = typename std::conditional<PB, float2, double>::type;
     __shared__ double sh[32];
     __shared__ int s_last;
     const int nvec = *iter + 1;
@@ -2330,33 +2381,47 @@ __global__ void k_update(int64_t Np, const int *__restrict__ iter, double *const
     // order); the elements of four basis vectors are loaded before any of
     // them is used, so one pass waits for memory once per four vectors
     const int U = kDotChunk / 256;
-    double x[U];
+    E x[U];
     int64_t t0 = (int64_t)r * Np + base + threadIdx.x;
 #pragma unroll
-    for (int u = 0; u < U; u++) x[u] = (threadIdx.x + u * 256 < len) ? w[t0 + u * 256] : 0.0;
+    for (int u = 0; u < U; u++) {
+        const double wd = (threadIdx.x + u * 256 < len) ? w[t0 + u * 256] : 0.0;
+        if constexpr (PB) x[u] = d2pair_bits(wd);
+        else x[u] = wd;
+    }
     for (int j0 = 0; j0 < nvec; j0 += 4) {
-        double hv[4], vv[4][U];
+        E hv[4], vv[4][U];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const bool okq = j0 + q < nvec;
-            hv[q] = okq ? h[j0 + q] : 0.0;
-            const double *vj = okq ? Vp[j0 + q] + t0 : NULL;
+            const double hq = okq ? h[j0 + q] : 0.0;
+            if constexpr (PB) {
+                const float2 hp = d2pair_bits(hq);
+                hv[q] = make_float2(-hp.x, -hp.y);
+            } else {
+                hv[q] = hq;
+            }
+            const E *vj = okq ? reinterpret_cast<const E *>(Vp[j0 + q]) + t0 : NULL;
 #pragma unroll
-            for (int u = 0; u < U; u++) vv[q][u] = (okq && threadIdx.x + u * 256 < len) ? vj[u * 256] : 0.0;
+            for (int u = 0; u < U; u++) vv[q][u] = (okq && threadIdx.x + u * 256 < len) ? vj[u * 256] : kv_zero<E>();
         }
 #pragma unroll
         for (int q = 0; q < 4; q++)
             if (j0 + q < nvec)
 #pragma unroll
                 for (int u = 0; u < U; u++)
-                    if (threadIdx.x + u * 256 < len) x[u] = x[u] - hv[q] * vv[q][u];
+                    if (threadIdx.x + u * 256 < len) {
+                        if constexpr (PB) x[u] = f2_fma(x[u], hv[q], vv[q][u]);
+                        else x[u] = x[u] - hv[q] * vv[q][u];
+                    }
     }
     double s2 = 0.0;
 #pragma unroll
     for (int u = 0; u < U; u++) {
         if (threadIdx.x + u * 256 < len) {
-            v[t0 + u * 256] = x[u];
-            s2 += x[u] * x[u];
+            const double xd = kv_double(x[u]);
+            v[t0 + u * 256] = xd;
+            s2 += xd * xd;
         }
     }
     s2 = block_sum(s2, sh);
@@ -2404,7 +2469,9 @@ __global__ void k_backsub(int S, int M, double *const *__restrict__ Hc, const do
     }
 }
 
-// y[r][j] = sum_{jv <= iters(s)} z_s[jv] V_jv[r][j]
+// y[r][j] = sum_{jv <= iters(s)} z_s[jv] V_jv[r][j] (in pair arithmetic on
+// the FP32 pairs of the mixed path's basis when PB)
+template <bool PB>
 __global__ void k_combine(int64_t Np, int ks, int M, double *const *__restrict__ Vp, const double *__restrict__ z,
                           const int *__restrict__ iters, const int32_t *__restrict__ leaf_geom, double *__restrict__ y) {
     int64_t n = (int64_t)ks * Np;
@@ -2413,9 +2480,26 @@ __global__ void k_combine(int64_t Np, int ks, int M, double *const *__restrict__
         int64_t j = t - (int64_t)r * Np;
         int sidx = leaf_geom[j] * ks + r;
         int it = iters[sidx];
-        double sum = 0.0;
-        for (int jv = 0; jv <= it; jv++) sum += Vp[jv][t] * z[(int64_t)sidx * (M + 2) + jv];
-        y[t] = sum;
+        if constexpr (PB) {
+            // four basis elements loaded before any is used (one wait for
+            // memory per four vectors), summed in basis order
+            const double *zs = z + (int64_t)sidx * (M + 2);
+            float2 sum = make_float2(0.0f, 0.0f);
+            int jv = 0;
+            for (; jv + 3 <= it; jv += 4) {
+                float2 v4[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) v4[q] = reinterpret_cast<const float2 *>(Vp[jv + q])[t];
+#pragma unroll
+                for (int q = 0; q < 4; q++) sum = f2_fma(sum, v4[q], d2pair_bits(zs[jv + q]));
+            }
+            for (; jv <= it; jv++) sum = f2_fma(sum, reinterpret_cast<const float2 *>(Vp[jv])[t], d2pair_bits(zs[jv]));
+            y[t] = pair2d(sum);
+        } else {
+            double sum = 0.0;
+            for (int jv = 0; jv <= it; jv++) sum += Vp[jv][t] * z[(int64_t)sidx * (M + 2) + jv];
+            y[t] = sum;
+        }
     }
 }
 
@@ -4528,8 +4612,13 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     // classical Gram-Schmidt against q_0..q_i, per solve; for a few solves
     // the Hessenberg column is summed by the last CTA of k_dots
     const bool fuse_h = a.S <= 4;
-    k_dots<<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial, fuse_h ? 1 : 0, a.G,
-                                            p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
+    const bool pb = p->precision == FCG_PREC_MIXED;  // basis vectors as FP32 pairs
+    if (pb)
+        k_dots<true><<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial,
+                                                              fuse_h ? 1 : 0, a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
+    else
+        k_dots<false><<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial,
+                                                               fuse_h ? 1 : 0, a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
     if (!fuse_h)
         k_reduce_h<<<gh, 256, 0, s>>>(a.k, a.G, a.nch, p->d_it, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->Hptr);
     // v = w - sum h_j q_j; for a few solves its last CTA ends the step
@@ -4540,8 +4629,12 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     StepEnd fe = {a.S, a.k, a.G, a.M, a.cap, a.use_cond, p->g_ch_first, p->g_ch_count, p->Hptr, p->cs, p->sn, p->g, p->nrm2,
                   p->hnorm, rhn, p->normb, a.tol, p->scap, p->active, p->iters, p->capped, p->n_active, p->d_it, p->d_it + 1,
                   cancel, a.cond};
-    k_update<<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial,
-                                              fuse_end ? 1 : 0, fe, p->d_it + 3);
+    if (pb)
+        k_update<true><<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial,
+                                                        fuse_end ? 1 : 0, fe, p->d_it + 3);
+    else
+        k_update<false><<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv,
+                                                         p->partial, fuse_end ? 1 : 0, fe, p->d_it + 3);
     int launches = 3 + (fuse_h ? 0 : 1);
     if (!fuse_end) {
         const int g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
@@ -4555,7 +4648,8 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     if (!fused_scale) {
         // the two-level path normalises here (its preconditioner reads v first);
         // k_update's step end has already advanced the index, hence Vp[*iter]
-        k_scale<<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
+        if (pb) k_scale<true><<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
+        else k_scale<false><<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
         launches++;
     }
     p->timings.launches += launches;
@@ -4774,7 +4868,8 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
             k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
                                             p->capped, p->n_active + M + 1);
-            k_scale<<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
+            if (p->precision == FCG_PREC_MIXED) k_scale<true><<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
+            else k_scale<false><<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
             FCG_CK(cudaGetLastError());
             p->timings.launches += 7;
             // does any solve need an Arnoldi step? (read below, after the
@@ -4842,7 +4937,8 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             }
             if (status != FCG_NORMAL_END) break;
             k_backsub<<<(S * 32 + 127) / 128, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
-            k_combine<<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
+            if (p->precision == FCG_PREC_MIXED) k_combine<true><<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
+            else k_combine<false><<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
             if (pk == FCG_PRECOND_TWO_LEVEL) {
                 if ((r = precond_apply(p, pk, p->w, p->vv, k))) { status = r; break; }
                 k_finish<<<g1, 256, 0, s>>>(Np, k, p->x0, p->vv, NULL, p->iters, p->leaf_geom, p->x);
