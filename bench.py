@@ -593,6 +593,38 @@ def converged_accuracy(ctx, paths, tol=1e-8):
             "per_request": [round(e, 9) for e in errs]}
 
 
+def krylov_accuracy(ctx, paths):
+    """The mixed path's Krylov basis in FP32 pairs (the default) against the
+    same solve with an FP64 basis (fcg_solve_options.krylov), and both
+    against the FP64 solver, at the serving tolerance on the same requests;
+    launch-shape measurement off, so every solve is deterministic. Per
+    request the largest per-entry difference over the FP64 solver's entry."""
+    import fastercap_gb300 as fc
+    d_ab, e_pair, e_f64k, it_diff, n_solves = [], [], [], 0, 0
+    for path in paths:
+        m = fc.Model.build(path, mesh_eps=SERVING["mesh_eps"], eps_ratio=SERVING["eps_ratio"], ctx=ctx)
+        res = {}
+        for name, prec, kry in (("pair", fc.PREC_MIXED, fc.KRYLOV_PAIR), ("fp64_basis", fc.PREC_MIXED, fc.KRYLOV_FP64),
+                                ("fp64", fc.PREC_FP64, fc.KRYLOV_FP64)):
+            p = ctx.problem(m, prec)
+            p.set_tuning(False)
+            p.fill()
+            res[name] = p.solve(tol=SERVING["tol"], krylov=kry)
+            p.close()
+        ref = np.abs(res["fp64"][0])
+        d_ab.append(float(np.max(np.abs(res["pair"][0] - res["fp64_basis"][0]) / ref)))
+        e_pair.append(float(np.max(np.abs(res["pair"][0] - res["fp64"][0]) / ref)))
+        e_f64k.append(float(np.max(np.abs(res["fp64_basis"][0] - res["fp64"][0]) / ref)))
+        it_diff += int(np.sum(res["pair"][1] != res["fp64_basis"][1]))
+        n_solves += len(res["pair"][1])
+
+    def dist(e):
+        return {"median": float(np.median(e)), "p90": float(np.percentile(e, 90)), "max": float(np.max(e))}
+    return {"requests": len(paths), "gmres_tol": SERVING["tol"], "pair_vs_fp64_basis": dist(d_ab),
+            "vs_fp64_solver": {"pair_basis": dist(e_pair), "fp64_basis": dist(e_f64k)},
+            "iteration_counts_differing": it_diff, "solves": n_solves}
+
+
 def cpu_serving_sample(paths, budget_s, cores, build_in_subprocess=False):
     """The CPU path on a fixed, ordered sample of the requests: per request
     the model build (the host restatement of the reference's parse, mesh
@@ -766,6 +798,8 @@ def run_serving(args, rank, world, local_rank):
     roof = serving_roofline(ctx, paths[0]) if rank == 0 else None
     log("converged accuracy sample")
     conv = converged_accuracy(ctx, paths[:args.accuracy_sample]) if rank == 0 and args.accuracy_sample > 0 else None
+    log("Krylov basis arithmetic sample")
+    kry = krylov_accuracy(ctx, paths[:args.krylov_sample]) if rank == 0 and args.krylov_sample > 0 else None
     result = {
         "metric": METRIC, "value": mixed_top["solves_s"], "unit": "solves/s", "n_gpus": world, "steps": args.requests,
         "warmup": 2 * args.slots, "ms_per_step": 1000.0 / mixed_top["solves_s"], "higher_is_better": True,
@@ -790,6 +824,7 @@ def run_serving(args, rank, world, local_rank):
                           "p99_rel_c_err": float(np.percentile(errs, 99)),
                           "worst_entry_over_its_diagonal": ent[int(np.argmax(errs))]} if errs else None,
         "mixed_vs_fp64_converged": conv,
+        "mixed_krylov_pair_vs_fp64_basis": kry,
         "same_result_every_rate": bool(same),
         "server": {"max_running": st["max_running"], "peak_in_use_bytes": st["peak_in_use"], "budget_bytes": st["budget"]},
         "e2e": {"value": mixed_top["solves_s"], "unit": "solves/s",
@@ -1057,6 +1092,8 @@ def main():
                     help="serving: requests the plain FP64 arm serves (the first ones of the same schedule)")
     ap.add_argument("--accuracy-sample", type=int, default=8,
                     help="serving: requests re-solved at GMRES tolerance 1e-8 in both precisions")
+    ap.add_argument("--krylov-sample", type=int, default=40,
+                    help="serving: requests solved mixed with the FP32-pair and the FP64 Krylov basis and in FP64")
     ap.add_argument("--no-sphere", dest="sphere", action="store_false",
                     help="serving: skip the resident 327,680-triangle sphere measured after the requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")

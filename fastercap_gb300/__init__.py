@@ -40,6 +40,8 @@ PRECOND_JACOBI = 1
 PRECOND_TWO_LEVEL = 2
 PREC_FP64 = 0
 PREC_MIXED = 1
+# Krylov basis arithmetic of mixed-precision solves (FP64 problems: always FP64)
+KRYLOV_PAIR, KRYLOV_FP64 = 0, 1
 
 # element type bits
 IS_LEAF, IS_DIEL, OUTPERM_NORMAL_DIR, IS_SUPER_NODE = 1, 2, 4, 128
@@ -86,7 +88,7 @@ class ProblemStats(C.Structure):
 
 class SolveOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("precond", C.c_int), ("max_iter", C.c_int), ("rhs_width", C.c_int),
-                ("precond_dim", C.c_int), ("refine", C.c_int)]
+                ("precond_dim", C.c_int), ("refine", C.c_int), ("krylov", C.c_int)]
 
 
 class ServerConfig(C.Structure):
@@ -456,13 +458,14 @@ class Problem:
         return int(lib().fcg_problem_matvec_device_noalloc(self._h, C.c_void_p(q_ptr), C.c_void_p(v_ptr), k))
 
     def solve(self, tol: float = 0.01, precond: int = PRECOND_JACOBI, max_iter: int = 0, allow_not_converged=False,
-              rhs_width: int = 0, precond_dim: int = 0, refine: int = 0):
+              rhs_width: int = 0, precond_dim: int = 0, refine: int = 0, krylov: int = KRYLOV_PAIR):
         """(C, iterations); with geometries set, lists of per-geometry C and iterations.
-        refine: true-residual restarts (0 default: up to 2 in mixed precision, -1 none)."""
+        refine: true-residual restarts (0 default: up to 2 in mixed precision, -1 none).
+        krylov: mixed precision's basis arithmetic, KRYLOV_PAIR (FP32 pairs) or KRYLOV_FP64."""
         sizes = self.geometries or [self.n_cond]
         cap = np.empty(sum(n * n for n in sizes), np.float64)
         it = np.empty(sum(sizes), np.int32)
-        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine, krylov)
         code = lib().fcg_problem_solve(self._h, C.byref(opt), _ptr(cap), _ptr(it))
         self._last_width = int(self.stats()["rhs_width"]) or 32  # the width the solve used
         if not (code == NORMAL_END or (allow_not_converged and code == NOT_CONVERGED)):
@@ -591,10 +594,11 @@ class Server:
         self._h = h
 
     def submit(self, model: Model, precision: int = PREC_MIXED, tol: float = 0.01, precond: int = PRECOND_JACOBI,
-               max_iter: int = 0, rhs_width: int = 0, precond_dim: int = 0, refine: int = 0) -> Job:
+               max_iter: int = 0, rhs_width: int = 0, precond_dim: int = 0, refine: int = 0,
+               krylov: int = KRYLOV_PAIR) -> Job:
         arr = model.c_arrays()
         keep = model._keep
-        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine, krylov)
         jid = C.c_int64()
         _check(lib().fcg_server_submit(self._h, C.byref(arr), precision, C.byref(opt), C.byref(jid)), "submit")
         job = Job(self, jid.value, model, (arr, keep))
@@ -602,11 +606,11 @@ class Server:
 
     def submit_file(self, path: str, precision: int = PREC_MIXED, tol: float = 0.01, mesh_eps: float = 0.1,
                     eps_ratio: float = 1.0, mesh_curv: float = 3.0, precond: int = PRECOND_JACOBI, max_iter: int = 0,
-                    rhs_width: int = 0, precond_dim: int = 0, refine: int = 0) -> Job:
+                    rhs_width: int = 0, precond_dim: int = 0, refine: int = 0, krylov: int = KRYLOV_PAIR) -> Job:
         """An extraction request from an input file: the slot builds its
         model on the GPU (switches -m, -d, -mc), then solves it."""
         bo = BuildOptions(mesh_eps, eps_ratio, mesh_curv, 0)
-        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine)
+        opt = SolveOptions(tol, precond, max_iter, rhs_width, precond_dim, refine, krylov)
         jid = C.c_int64()
         _check(lib().fcg_server_submit_file(self._h, os.fsencode(path), C.byref(bo), precision, C.byref(opt),
                                             C.byref(jid)), "submit_file")

@@ -880,6 +880,7 @@ struct StepScale {
     const int32_t *leaf_geom;
     double *const *Vp;
     const int *iter;
+    int pair;  // basis vectors as FP32 pairs (the mixed path's FCG_KRYLOV_PAIR)
 };
 
 template <bool MIXED>
@@ -913,7 +914,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_up_blk(const SweepPlan pl
                 if (sc.active[sidx]) {
                     x = sc.recip ? x * sc.hn[sidx] : x / sc.hn[sidx];
                     const_cast<double *>(in)[at] = x;
-                    if (MIXED) reinterpret_cast<float2 *>(Vi)[at] = d2pair_bits(x);
+                    if (sc.pair) reinterpret_cast<float2 *>(Vi)[at] = d2pair_bits(x);
                     else Vi[at] = x;
                 }
             }
@@ -1216,7 +1217,8 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_up_blk32(const SweepPlan p
                         x[r] = sc.recip ? x[r] * sc.hn[g + c0 + r] : x[r] / sc.hn[g + c0 + r];
                         const int64_t at = (int64_t)(c0 + r) * ld + j;
                         const_cast<double *>(in)[at] = x[r];
-                        reinterpret_cast<float2 *>(Vi)[at] = d2pair_bits(x[r]);
+                        if (sc.pair) reinterpret_cast<float2 *>(Vi)[at] = d2pair_bits(x[r]);
+                        else Vi[at] = x[r];
                     }
                 }
             }
@@ -3894,7 +3896,7 @@ static void launch_link(DeviceProblem *p, const NodeWork &w, int kp, bool mixed)
 // are [k][Np] on the device.
 static int launch_matvec(DeviceProblem *p, const NodeWork &w, const double *in, double *out, int k, int kp, const double *diag,
                          const StepScale *scale = NULL) {
-    const StepScale sc = scale ? *scale : StepScale{NULL, 0, NULL, NULL, NULL, NULL};
+    const StepScale sc = scale ? *scale : StepScale{NULL, 0, NULL, NULL, NULL, NULL, 0};
     cudaStream_t s = p->stream;
     bool mixed = p->precision == FCG_PREC_MIXED;
     const SweepPlan &pl = p->plan;
@@ -4584,7 +4586,7 @@ static int precond_apply(DeviceProblem *p, int kind, const double *in, double *o
 // read on the device (d_it[0]), so the same launches serve every step and can
 // be captured once into a graph.
 struct StepArgs {
-    int k, S, G, M, nch, cap, pk;
+    int k, S, G, M, nch, cap, pk, pair;  // pair: basis vectors as FP32 pairs
     SegChunks ch;
     const double *diag;
     double tol;
@@ -4606,14 +4608,14 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     } else {
         // the mixed path multiplies by the reciprocal norms (the FP64 path divides, as the reference does)
         const bool mixed = p->precision == FCG_PREC_MIXED;
-        StepScale sc = {mixed ? p->hnorm + a.S : p->hnorm, mixed ? 1 : 0, p->active, p->leaf_geom, p->Vptr, p->d_it};
+        StepScale sc = {mixed ? p->hnorm + a.S : p->hnorm, mixed ? 1 : 0, p->active, p->leaf_geom, p->Vptr, p->d_it, a.pair};
         if ((r = matvec(p, p->vv, p->w, a.k, a.diag, &sc))) return r;
     }
     // classical Gram-Schmidt against q_0..q_i, per solve; for a few solves
     // the Hessenberg column is summed by the last CTA of k_dots
     const bool fuse_h = a.S <= 4;
-    const bool pb = p->precision == FCG_PREC_MIXED;  // basis vectors as FP32 pairs
-    if (pb)
+    const bool pair_basis = a.pair != 0;
+    if (pair_basis)
         k_dots<true><<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial,
                                                               fuse_h ? 1 : 0, a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
     else
@@ -4629,7 +4631,7 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     StepEnd fe = {a.S, a.k, a.G, a.M, a.cap, a.use_cond, p->g_ch_first, p->g_ch_count, p->Hptr, p->cs, p->sn, p->g, p->nrm2,
                   p->hnorm, rhn, p->normb, a.tol, p->scap, p->active, p->iters, p->capped, p->n_active, p->d_it, p->d_it + 1,
                   cancel, a.cond};
-    if (pb)
+    if (pair_basis)
         k_update<true><<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial,
                                                         fuse_end ? 1 : 0, fe, p->d_it + 3);
     else
@@ -4648,7 +4650,7 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     if (!fused_scale) {
         // the two-level path normalises here (its preconditioner reads v first);
         // k_update's step end has already advanced the index, hence Vp[*iter]
-        if (pb) k_scale<true><<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
+        if (pair_basis) k_scale<true><<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
         else k_scale<false><<<g1, 256, 0, s>>>(Np, a.k, p->vv, p->hnorm, p->active, p->leaf_geom, NULL, p->Vptr, p->d_it, 0);
         launches++;
     }
@@ -4662,7 +4664,7 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
 static int ensure_step_graph(DeviceProblem *p, StepArgs a) {
     std::vector<unsigned char> key;
     auto put = [&](const void *x, size_t n) { key.insert(key.end(), (const unsigned char *)x, (const unsigned char *)x + n); };
-    put(&a.k, sizeof(int) * 7);
+    put(&a.k, sizeof(int) * 8);
     put(&a.ch, sizeof(a.ch));
     put(&a.diag, sizeof(a.diag));
     put(&a.tol, sizeof(a.tol));
@@ -4741,6 +4743,13 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
     const int64_t Np = p->Np;
     const int nch = p->nch;
     if (all_charges && G != 1) { set_error("charge vectors are kept for one geometry only"); return FCG_GENERIC_ERROR; }
+    if (opt.krylov != FCG_KRYLOV_PAIR && opt.krylov != FCG_KRYLOV_FP64) {
+        set_error("unknown Krylov basis arithmetic " + std::to_string(opt.krylov));
+        return FCG_GENERIC_ERROR;
+    }
+    // the mixed path's Krylov basis as FP32 pairs (FCG_KRYLOV_PAIR): same
+    // 8 bytes per element, the Arnoldi kernels on the FP32 pipe
+    const bool pair_basis = p->precision == FCG_PREC_MIXED && opt.krylov == FCG_KRYLOV_PAIR;
     // per geometry: columns, output offsets, iteration cap (the reference's
     // min(1000, panels) for the geometry alone)
     std::vector<int> ncol(G);
@@ -4868,7 +4877,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             FCG_CK(cudaMemsetAsync(p->n_active, 0, (size_t)(M + 2) * sizeof(int), s));
             k_init_state<<<gs, 128, 0, s>>>(S, M, p->nrm2, p->nrm2 + S, p->normb, p->g, p->hnorm, opt.tol, p->active, p->iters,
                                             p->capped, p->n_active + M + 1);
-            if (p->precision == FCG_PREC_MIXED) k_scale<true><<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
+            if (pair_basis) k_scale<true><<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
             else k_scale<false><<<g1, 256, 0, s>>>(Np, k, p->vv, p->hnorm, NULL, p->leaf_geom, V0, NULL, NULL, 0);
             FCG_CK(cudaGetLastError());
             p->timings.launches += 7;
@@ -4880,7 +4889,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
                 status = r;
                 break;
             }
-            StepArgs sa = {k, S, G, M, nch, M, pk, chunks, diag, opt.tol, 0, 0};
+            StepArgs sa = {k, S, G, M, nch, M, pk, pair_basis ? 1 : 0, chunks, diag, opt.tol, 0, 0};
             // the workspace a step touches exists before any capture
             if ((r = ensure_matvec_ws(p, kpad(k))) || (r = autotune(p, kpad(k))) ||
                 (pk == FCG_PRECOND_TWO_LEVEL && (r = precond_apply(p, pk, p->vv, p->ptmp, k)))) {
@@ -4937,7 +4946,7 @@ int problem_solve(DeviceProblem *p, const fcg_solve_options &opt, double *cap, i
             }
             if (status != FCG_NORMAL_END) break;
             k_backsub<<<(S * 32 + 127) / 128, 128, 0, s>>>(S, M, p->Hptr, p->g, p->iters, p->z);
-            if (p->precision == FCG_PREC_MIXED) k_combine<true><<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
+            if (pair_basis) k_combine<true><<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
             else k_combine<false><<<g1, 256, 0, s>>>(Np, k, M, p->Vptr, p->z, p->iters, p->leaf_geom, p->w);
             if (pk == FCG_PRECOND_TWO_LEVEL) {
                 if ((r = precond_apply(p, pk, p->w, p->vv, k))) { status = r; break; }

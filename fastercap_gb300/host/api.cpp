@@ -291,6 +291,7 @@ int fcg_problem_solve(fcg_problem *p, const fcg_solve_options *opt, double *cap,
     o.rhs_width = 0;
     o.precond_dim = 0;
     o.refine = 0;
+    o.krylov = FCG_KRYLOV_PAIR;
     if (opt) o = *opt;
     return fcg::problem_solve(p->p, o, cap, iterations);
 }

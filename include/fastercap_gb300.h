@@ -44,7 +44,14 @@ extern "C" {
 
 /* arithmetic of the link coefficients and the link product */
 #define FCG_PREC_FP64 0  /* FP64 coefficients, FP64 sums */
-#define FCG_PREC_MIXED 1 /* FP32 coefficients and link sums (compensated), FP64 near field and Krylov */
+#define FCG_PREC_MIXED 1 /* FP32 coefficients and link sums (compensated), FP64 near field, Hessenberg and
+                            Givens; the Krylov basis as fcg_solve_options.krylov says */
+
+/* arithmetic of the Krylov basis in mixed precision (FP64 problems: always FP64) */
+#define FCG_KRYLOV_PAIR 0 /* basis vectors stored as unevaluated FP32 pairs (about 46 significant bits),
+                             Arnoldi dot products, updates and the solution's combination in FP32-pair
+                             arithmetic (FP32 pipe) */
+#define FCG_KRYLOV_FP64 1 /* basis, dot products, updates and combination in FP64 */
 
 typedef struct fcg_context fcg_context;
 typedef struct fcg_model fcg_model;
@@ -198,6 +205,7 @@ typedef struct {
     int refine;       /* restarts from the current solution while the true residual |b - A x| / |b| is
                          at or above tol: 0 = default (up to 2 for FCG_PREC_MIXED, none for FP64),
                          -1 = none, n > 0 = up to n */
+    int krylov;       /* FCG_PREC_MIXED problems: FCG_KRYLOV_PAIR (0, default) or FCG_KRYLOV_FP64 */
 } fcg_solve_options;
 
 /* Declare that the problem holds several independent geometries: conductor c

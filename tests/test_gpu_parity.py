@@ -94,6 +94,45 @@ def test_solve_mixed_within_tenth_percent(ctx, golden):
     assert err.max() < 1e-3, err.max()
 
 
+def test_krylov_basis_arithmetic(ctx, golden):
+    """Mixed path with either Krylov basis arithmetic, FP32 pairs (the
+    default) or FP64: every capacitance entry within 0.1 % of the reference,
+    iteration counts within one of each other."""
+    name, g = golden
+    tol, precond = solve_params(g)
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_MIXED)
+    p.fill()
+    kw = dict(tol=tol, precond=precond, precond_dim=super_dim(g))
+    cp, itp = p.solve(krylov=fc.KRYLOV_PAIR, **kw)
+    cf, itf = p.solve(krylov=fc.KRYLOV_FP64, **kw)
+    for c in (cp, cf):
+        err = np.abs(c - g["ref_cap"]) / np.abs(g["ref_cap"])
+        assert err.max() < 1e-3, err.max()
+    assert np.abs(itp.astype(int) - itf.astype(int)).max() <= 1, (itp, itf)
+
+
+def test_krylov_pair_converged(ctx):
+    """Solved far below the serving tolerance, the FP32-pair basis gives the
+    FP64 basis' matrix to 1e-5 of each row's diagonal (the FP32 link
+    coefficients, not the basis, set the mixed path's accuracy); FP64
+    problems ignore the option (bit-identical), and an unknown value is an
+    error."""
+    g = load_golden("random3")
+    p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_MIXED)
+    p.fill()
+    cp, _ = p.solve(tol=1e-8, krylov=fc.KRYLOV_PAIR)
+    cf, _ = p.solve(tol=1e-8, krylov=fc.KRYLOV_FP64)
+    d = np.abs(np.diag(cf))[:, None]
+    assert (np.abs(cp - cf) / d).max() < 1e-5, (np.abs(cp - cf) / d).max()
+    with pytest.raises(fc.FCError):
+        p.solve(tol=1e-4, krylov=7)
+    p64 = ctx.problem(fc.Model.from_arrays(model_arrays(g)), fc.PREC_FP64)
+    p64.fill()
+    a, ia = p64.solve(tol=1e-6, krylov=fc.KRYLOV_PAIR)
+    b, ib = p64.solve(tol=1e-6, krylov=fc.KRYLOV_FP64)
+    assert np.array_equal(a, b) and np.array_equal(ia, ib)
+
+
 def test_builder_to_gpu_end_to_end(ctx, golden, tmp_path):
     """Input file -> host builder -> GPU fill and solve, against the reference."""
     name, g = golden
