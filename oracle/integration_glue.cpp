@@ -125,7 +125,7 @@ static int SolveOnGpu(CSolveCap &solve, CLin_Matrix *cRe) {
         for (size_t c = 0; c < g.is_diel.size(); c++) nc += g.is_diel[c] ? 0 : 1;
         cRe->newsize(nc, nc);
         std::vector<double> cap((size_t)nc * nc);
-        fcg_solve_options so = {solve.m_clsGlobalVars.m_dGmresTol, FCG_PRECOND_JACOBI, 0, 0, 0, 0};
+        fcg_solve_options so = {solve.m_clsGlobalVars.m_dGmresTol, FCG_PRECOND_JACOBI, 0, 0, 0, 0, FCG_KRYLOV_PAIR};
         if (solve.m_clsGlobalVars.m_ucPrecondType & AUTOREFINE_PRECOND_SUPER) {
             so.precond = FCG_PRECOND_TWO_LEVEL;
             so.precond_dim = (int)solve.m_clsGlobalVars.m_uiSuperPreDim;
