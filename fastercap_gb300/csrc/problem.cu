@@ -5120,8 +5120,17 @@ int problem_matvec_noalloc(DeviceProblem *p, const double *d_q, double *d_v, int
         FCG_CK(cudaMemsetAsync(w.Qd, 0, n * sizeof(double), s));
         if (p->precision == FCG_PREC_MIXED) FCG_CK(cudaMemsetAsync(w.Qf, 0, n * sizeof(float), s));
     }
+    // while the caller records a graph on this stream the launches go into
+    // the graph: no wait (it would end the recording) and no profiling
+    // events (they would time nothing)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FCG_CK(cudaStreamIsCapturing(s, &cs));
+    const bool recording = cs != cudaStreamCaptureStatusNone;
+    const bool profiling = p->profiling;
+    if (recording) p->profiling = false;
     r = launch_matvec(p, w, d_q, d_v, k, kp, NULL);
-    if (r != FCG_NORMAL_END) return r;
+    p->profiling = profiling;
+    if (r != FCG_NORMAL_END || recording) return r;
     FCG_CK(cudaStreamSynchronize(s));
     prof_collect(p);  // with profiling on, read back (and release) the link-product events
     return FCG_NORMAL_END;

@@ -190,7 +190,10 @@ int fcg_problem_matvec_device(fcg_problem *p, const double *d_q, double *d_v, in
  * capture. All calls share the array and it keeps the last call's contents
  * (the padding columns the product reads are cleared on every call): calls
  * that overlap on the GPU race and must be serialised by the caller. Runs on
- * the problem's stream and returns after the product completes.
+ * the problem's stream and returns after the product completes; while that
+ * stream records a CUDA graph it returns once the product's work is queued
+ * into the graph (no wait, no profiling events), and each replay computes
+ * the product of whatever d_q then holds.
  * No counterpart in the reference (FasterCap never runs without allocation). */
 int fcg_problem_matvec_device_noalloc(fcg_problem *p, const double *d_q, double *d_v, int k);
 

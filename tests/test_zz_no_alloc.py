@@ -54,6 +54,41 @@ def test_noalloc_matches_allocating_matvec(case, precision, tol, k):
         p.close()
 
 
+@pytest.mark.parametrize("precision,tol", [(fc.PREC_FP64, 1e-13), (fc.PREC_MIXED, 2e-6)])
+def test_noalloc_records_into_a_cuda_graph(precision, tol):
+    """Called while the caller records a CUDA graph on the problem's own
+    (caller-owned) stream, the product goes into the graph; every replay
+    computes the product of what the input buffer then holds, equal to
+    fcg_problem_matvec_device's."""
+    torch = pytest.importorskip("torch")
+    g = load_golden("crossing2x2_m02")
+    k = 3
+    with fc.Context(0) as ctx:
+        s = torch.cuda.Stream()
+        p = ctx.problem(fc.Model.from_arrays(model_arrays(g)), precision, stream=s.cuda_stream)
+        p.fill()
+        n = p.n_panels
+        q = torch.tensor(np.random.default_rng(5).uniform(-1, 1, (k, n)), dtype=torch.float64, device="cuda")
+        v = torch.zeros_like(q)
+        torch.cuda.synchronize()
+        # one call before the first recording resolves the scratch address
+        assert p.matvec_device_noalloc(q.data_ptr(), v.data_ptr(), k) == fc.NORMAL_END, fc.last_error()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=s):
+            code = p.matvec_device_noalloc(q.data_ptr(), v.data_ptr(), k)
+        assert code == fc.NORMAL_END, fc.last_error()
+        ref = torch.empty_like(q)
+        for seed in (6, 7):
+            q.copy_(torch.from_numpy(np.random.default_rng(seed).uniform(-1, 1, (k, n))))
+            v.fill_(float("nan"))
+            torch.cuda.synchronize()
+            graph.replay()
+            torch.cuda.synchronize()
+            p.matvec_device(q.data_ptr(), ref.data_ptr(), k)
+            assert rel_norm(v.cpu().numpy(), ref.cpu().numpy()) < tol
+        p.close()
+
+
 def test_noalloc_rejects_models_beyond_its_scratch(tmp_path):
     torch = pytest.importorskip("torch")
     from fastercap_gb300 import geometry as geo
