@@ -2035,7 +2035,11 @@ __global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__r
     const int T = 8;
     const int nvec = *iter + 1;
     int r = blockIdx.y, c = blockIdx.x;
-    if (active[ch.geom[c] * ks + r]) {
+    // grid.z splits the basis vectors of a chunk over CTAs (groups of T
+    // taken z, z + Z, ...); every (vector, chunk) sum is the same either way.
+    // CTAs past the last group have nothing to do but take the ticket.
+    const int z = blockIdx.z, Z = gridDim.z;
+    if (z * T < nvec && active[ch.geom[c] * ks + r]) {
     int64_t base = ch.start[c];
     int len = ch.len[c];
     E wv[U];
@@ -2047,7 +2051,7 @@ __global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__r
         else wv[u] = x;
     }
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int j0 = 0; j0 < nvec; j0 += T) {
+    for (int j0 = z * T; j0 < nvec; j0 += Z * T) {
         E acc[T];
 #pragma unroll
         for (int t = 0; t < T; t++) {
@@ -2104,7 +2108,7 @@ __global__ void __launch_bounds__(kDotThreads) k_dots(int64_t Np, const int *__r
     if (!fuse_h) return;
     if (threadIdx.x == 0) {
         __threadfence();  // this CTA's partial sums are visible before its ticket
-        s_last = atomicAdd(done, 1) == (int)(gridDim.x * gridDim.y) - 1;
+        s_last = atomicAdd(done, 1) == (int)(gridDim.x * gridDim.y * gridDim.z) - 1;
     }
     __syncthreads();
     if (!s_last) return;
@@ -2364,9 +2368,11 @@ __device__ void step_end(const StepEnd &e, int i, double *partial, int nch) {
 // ends the Arnoldi step (step_end: norms, Givens, step index) and resets *done.
 // PB (the mixed path): basis vectors are FP32 pairs and each element's
 // subtraction chain runs in pair arithmetic (w and every h_j split into
-// pairs, f2_fma), rounded to FP64 once for v and its norm.
-template <bool PB>
-__global__ void __launch_bounds__(256, PB ? 4 : 1) k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
+// pairs, f2_fma), rounded to FP64 once for v and its norm. QV basis vectors
+// are loaded per pass: 8 for small models (few CTAs, so the passes' memory
+// waits are the time), else 4; the subtractions are the same either way.
+template <bool PB, int QV>
+__global__ void __launch_bounds__(256, QV == 8 ? 2 : (PB ? 4 : 1)) k_update(int64_t Np, const int *__restrict__ iter, double *const *__restrict__ Vp, const double *__restrict__ w,
                          double *const *__restrict__ Hp, SegChunks ch, int ks, const int *__restrict__ active,
                          double *__restrict__ v, double *__restrict__ partial, int fuse_end, StepEnd fe, int *done) {
     using E = typename std::conditional<PB, float2, double>::type;
@@ -2391,10 +2397,10 @@ __global__ void __launch_bounds__(256, PB ? 4 : 1) k_update(int64_t Np, const in
         if constexpr (PB) x[u] = d2pair_bits(wd);
         else x[u] = wd;
     }
-    for (int j0 = 0; j0 < nvec; j0 += 4) {
-        E hv[4], vv[4][U];
+    for (int j0 = 0; j0 < nvec; j0 += QV) {
+        E hv[QV], vv[QV][U];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < QV; q++) {
             const bool okq = j0 + q < nvec;
             const double hq = okq ? h[j0 + q] : 0.0;
             if constexpr (PB) {
@@ -2408,7 +2414,7 @@ __global__ void __launch_bounds__(256, PB ? 4 : 1) k_update(int64_t Np, const in
             for (int u = 0; u < U; u++) vv[q][u] = (okq && threadIdx.x + u * 256 < len) ? vj[u * 256] : kv_zero<E>();
         }
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+        for (int q = 0; q < QV; q++)
             if (j0 + q < nvec)
 #pragma unroll
                 for (int u = 0; u < U; u++)
@@ -4611,16 +4617,28 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
         StepScale sc = {mixed ? p->hnorm + a.S : p->hnorm, mixed ? 1 : 0, p->active, p->leaf_geom, p->Vptr, p->d_it, a.pair};
         if ((r = matvec(p, p->vv, p->w, a.k, a.diag, &sc))) return r;
     }
-    // classical Gram-Schmidt against q_0..q_i, per solve; for a few solves
-    // the Hessenberg column is summed by the last CTA of k_dots
-    const bool fuse_h = a.S <= 4;
+    // classical Gram-Schmidt against q_0..q_i, per solve. The last CTA of
+    // k_dots sums the Hessenberg column (four warps, one output after the
+    // other) only while that is short: at most 32 outputs (solves x the
+    // basis capacity); longer columns take k_reduce_h, one warp per output
+    // in parallel, the same sums.
+    const bool fuse_h = (int64_t)a.S * a.cap <= 32;
+    // basis vectors over grid.z while chunks x columns alone would leave
+    // the GPU short of CTAs (small models: fewer than two per SM), up to
+    // four CTAs per SM and at most one group of eight vectors per CTA and z
+    // (4 conductors, 18.8k panels: 4.9 -> 3.5 ms per fill + solve with the
+    // eight-vector passes of k_update below)
+    const int dot_ctas = a.nch * a.k;
+    const bool small = dot_ctas < 2 * sms;
+    const int dz = !small ? 1 : std::max(1, std::min((4 * sms + dot_ctas - 1) / dot_ctas, (a.cap + 7) / 8));
+    const dim3 dgrid(a.nch, a.k, dz);
     const bool pair_basis = a.pair != 0;
     if (pair_basis)
-        k_dots<true><<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial,
-                                                              fuse_h ? 1 : 0, a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
+        k_dots<true><<<dgrid, kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial, fuse_h ? 1 : 0,
+                                                   a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
     else
-        k_dots<false><<<dim3(a.nch, a.k), kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial,
-                                                               fuse_h ? 1 : 0, a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
+        k_dots<false><<<dgrid, kDotThreads, 0, s>>>(Np, p->d_it, p->Vptr, p->w, a.ch, a.k, p->active, p->partial, fuse_h ? 1 : 0,
+                                                    a.G, p->g_ch_first, p->g_ch_count, p->Hptr, p->d_it + 3);
     if (!fuse_h)
         k_reduce_h<<<gh, 256, 0, s>>>(a.k, a.G, a.nch, p->d_it, p->partial, p->g_ch_first, p->g_ch_count, p->active, p->Hptr);
     // v = w - sum h_j q_j; for a few solves its last CTA ends the step
@@ -4631,12 +4649,18 @@ static int enqueue_step(DeviceProblem *p, const StepArgs &a) {
     StepEnd fe = {a.S, a.k, a.G, a.M, a.cap, a.use_cond, p->g_ch_first, p->g_ch_count, p->Hptr, p->cs, p->sn, p->g, p->nrm2,
                   p->hnorm, rhn, p->normb, a.tol, p->scap, p->active, p->iters, p->capped, p->n_active, p->d_it, p->d_it + 1,
                   cancel, a.cond};
-    if (pair_basis)
-        k_update<true><<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial,
-                                                        fuse_end ? 1 : 0, fe, p->d_it + 3);
-    else
-        k_update<false><<<dim3(a.nch, a.k), 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv,
-                                                         p->partial, fuse_end ? 1 : 0, fe, p->d_it + 3);
+    const dim3 ugrid(a.nch, a.k);
+#define FCG_UPDATE(PBV, QV) \
+    k_update<PBV, QV><<<ugrid, 256, 0, s>>>(Np, p->d_it, p->Vptr, p->w, p->Hptr, a.ch, a.k, p->active, p->vv, p->partial, \
+                                            fuse_end ? 1 : 0, fe, p->d_it + 3)
+    if (pair_basis) {
+        if (small) FCG_UPDATE(true, 8);
+        else FCG_UPDATE(true, 4);
+    } else {
+        if (small) FCG_UPDATE(false, 8);
+        else FCG_UPDATE(false, 4);
+    }
+#undef FCG_UPDATE
     int launches = 3 + (fuse_h ? 0 : 1);
     if (!fuse_end) {
         const int g1v = (int)(((int64_t)a.k * a.G * 32 + 255) / 256);
