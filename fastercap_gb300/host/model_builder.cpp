@@ -985,15 +985,17 @@ int build_model(const std::string &path, const BuildOptions &opt, Model &M, std:
     size_t slash = path.rfind('/');
     if (slash != std::string::npos) { dir = path.substr(0, slash + 1); base = path.substr(slash + 1); }
     {
-        InFile *F = NULL;
-        int r = B.load_file(path, F);
-        if (r != FC_NORMAL_END) { err = B.err; return r; }
-        // the first line decides 2D versus 3D
-        if (!F->lines.empty() && (strstr(F->lines[0].c_str(), "2D") || strstr(F->lines[0].c_str(), "2d"))) {
+        // the first line (as the first fgets() chunk) decides 2D versus 3D;
+        // the parse below reads the file itself
+        FILE *f = fopen(path.c_str(), "rb");
+        if (!f) { err = "cannot open file '" + path + "'"; return FC_CANNOT_OPEN_FILE; }
+        char first[kMaxLineLen];
+        const bool have = fgets(first, kMaxLineLen, f) != NULL;
+        fclose(f);
+        if (have && (strstr(first, "2D") || strstr(first, "2d"))) {
             err = "2D input files are not supported by this solver";
             return FC_FILE_ERROR;
         }
-        B.files.clear();
     }
     B.base_dir = dir;
     // FCG_TRACE=1 prints the builder's phases to stderr
