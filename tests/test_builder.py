@@ -28,6 +28,22 @@ def test_missing_file_status(tmp_path):
     assert e.value.code == fc.CANNOT_OPEN_FILE
 
 
+@pytest.mark.parametrize("title", ["0 2D strip", "0 a 2d cross-section", "2D"])
+def test_2d_input_refused(tmp_path, title):
+    """The first line decides 2D against 3D, as in the reference's reader:
+    a 2D input is refused with FC_FILE_ERROR (no 2D solver here), the same
+    panels under a 3D title build."""
+    body = "T c 0 0 0 1 0 0 0 1 0\nT c 0 0 1 1 0 1 0 1 1\n"
+    path = tmp_path / "in.txt"
+    path.write_text(title + "\n" + body)
+    with pytest.raises(fc.FCError) as e:
+        fc.Model.build(str(path))
+    assert e.value.code == fc.FILE_ERROR and "2D" in str(e.value)
+    path.write_text("0 two plates\n" + body)
+    m = fc.Model.build(str(path))
+    assert m.n_panels >= 2
+
+
 def test_empty_file_status(tmp_path):
     p = tmp_path / "empty.txt"
     p.write_text("* nothing here\n")
