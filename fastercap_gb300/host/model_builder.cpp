@@ -28,6 +28,7 @@
 #include "model.hpp"
 
 #include <deque>
+#include <errno.h>
 #include <map>
 #include <stdio.h>
 #include <stdlib.h>
@@ -95,24 +96,92 @@ struct PanelLine {
     double cosmin = 0;
 };
 
+static inline bool c_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; }
+
+// One "%f" conversion as sscanf makes it, for a plain decimal token: C-locale
+// whitespace, [+-]digits[.digits][(e|E)[+-]digits] with at least one
+// mantissa digit, then whitespace or the end of the text. strtof rounds such
+// a token to the nearest float exactly as the %f conversion does (glibc's
+// %f hands the same characters to the same conversion). Anything else - hex,
+// inf, nan, an exponent without digits, a token glued to other text, a
+// value out of float range - returns false, and the caller runs sscanf
+// itself. `used` counts the characters consumed from p, as %n would.
+static bool scan_plain_float(const char *p, float &x, int &used) {
+    const char *s = p;
+    while (c_space(*s)) s++;
+    const char *t = s;
+    if (*t == '+' || *t == '-') t++;
+    int digits = 0;
+    while (*t >= '0' && *t <= '9') { t++; digits++; }
+    if (*t == '.') {
+        t++;
+        while (*t >= '0' && *t <= '9') { t++; digits++; }
+    }
+    if (digits == 0) return false;
+    if (*t == 'e' || *t == 'E') {
+        const char *u = t + 1;
+        if (*u == '+' || *u == '-') u++;
+        if (!(*u >= '0' && *u <= '9')) return false;
+        while (*u >= '0' && *u <= '9') u++;
+        t = u;
+    }
+    if (*t != 0 && !c_space(*t)) return false;
+    char *end = NULL;
+    errno = 0;
+    const float v = strtof(s, &end);
+    if (end != t || errno != 0) return false;
+    x = v;
+    used = (int)(t - p);
+    return true;
+}
+
+// sscanf(p, "%f%f%f%n", ...) for three plain tokens: true with the values and
+// the characters used; false leaves everything to sscanf
+static bool scan_plain_float3(const char *p, float &x, float &y, float &z, int &used) {
+    int a, b, c;
+    if (!scan_plain_float(p, x, a) || !scan_plain_float(p + a, y, b) || !scan_plain_float(p + a + b, z, c)) return false;
+    used = a + b + c;
+    return true;
+}
+
 static void parse_panel_fields(const char *line, PanelLine &o) {
     const int nv = line[0] == 'T' ? 3 : 4;
     char tmpname[kMaxLineLen];
     tmpname[0] = 0;
     int skip = 0;
     const char *point = line + 1;
-    sscanf(point, "%s%n", tmpname, &skip);
+    {
+        // "%s%n": the conductor name (sscanf for a line with none)
+        const char *s = point;
+        while (c_space(*s)) s++;
+        const char *t = s;
+        while (*t && !c_space(*t)) t++;
+        if (t > s) {
+            memcpy(tmpname, s, (size_t)(t - s));
+            tmpname[t - s] = 0;
+            skip = (int)(t - point);
+        } else {
+            sscanf(point, "%s%n", tmpname, &skip);
+        }
+    }
     point += skip;
     for (int i = 0; i < nv; i++) {
         float x = 0, y = 0, z = 0;
-        sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+        if (!scan_plain_float3(point, x, y, z, skip)) {
+            x = y = z = 0;
+            sscanf(point, "%f%f%f%n", &x, &y, &z, &skip);
+        }
         o.v[3 * i] = x;
         o.v[3 * i + 1] = y;
         o.v[3 * i + 2] = z;
         point += skip;
     }
     float x, y, z;
-    o.uselocal = sscanf(point, "%f%f%f%n", &x, &y, &z, &skip) == 3;
+    const char *rest = point;
+    while (c_space(*rest)) rest++;
+    if (*rest == 0) o.uselocal = false;  // sscanf would find no input (EOF)
+    else if (scan_plain_float3(point, x, y, z, skip)) o.uselocal = true;
+    else o.uselocal = sscanf(point, "%f%f%f%n", &x, &y, &z, &skip) == 3;
     if (o.uselocal) { o.ref[0] = x; o.ref[1] = y; o.ref[2] = z; }
     o.name = tmpname;
     o.ok = true;
