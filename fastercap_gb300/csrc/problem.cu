@@ -18,6 +18,11 @@
 //   down_top/down_block A(node) = P(node) + A(parent); v = self*q + P + A(parent)
 //                                                                     (:231-283)
 // Node-indexed work arrays hold the k values of one node contiguously.
+// GMRES (CSolveCap::gmresPrecondSFastAll, Solver/SolveCapacitance.cpp:2288-2574)
+// keeps its Krylov basis as [k][n_panels] vectors: FP64 on the FP64 path,
+// FP32 pairs (8 bytes per element too) on the mixed path unless the solve
+// asks for FP64 (fcg_solve_options.krylov); Hessenberg columns, Givens
+// rotations and norms are FP64 on both.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
