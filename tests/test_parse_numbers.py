@@ -38,11 +38,13 @@ def plain_forms(rng, value):
     return forms[int(rng.integers(len(forms)))]
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_panel_coordinates_match_strtof(tmp_path, seed):
+# 240 panels: the reader converts lines as it parses them; 20,500: files of
+# 20,000 lines and more are converted on all host threads before the parse
+@pytest.mark.parametrize("seed,n_panels", [(0, 240), (1, 240), (2, 20500)])
+def test_panel_coordinates_match_strtof(tmp_path, seed, n_panels):
     rng = np.random.default_rng(seed)
     rows, expect = [], []
-    for i in range(240):
+    for i in range(n_panels):
         x0, y0 = rng.uniform(-5, 5, 2)
         a, b = rng.uniform(0.5, 2.0, 2)
         z = 3.0 * i  # panels far apart, one plane each
@@ -55,16 +57,17 @@ def test_panel_coordinates_match_strtof(tmp_path, seed):
     # lands on the midpoint and rounds to even, the wrong side in both cases
     for k, (base, sign) in enumerate(((Decimal(1), 1), (Decimal(1) + Decimal(2) ** -23, -1))):
         t = str(base + Decimal(2) ** -24 + sign * Decimal(2) ** -60)
-        z = "%d" % (700 + 3 * k)
+        z = "%d" % (3 * n_panels + 700 + 3 * k)
         toks = (t, "0", z, "3", "0", z, "0", "1", z)
         assert np.float32(float(t)) != strtof(t)  # the case needs correct rounding
         rows.append("T c " + " ".join(toks))
         expect.append([strtof(x) for x in toks])
     # forms the builder leaves to sscanf: hexadecimal, a value below the float
     # range, an exponent glued to a sign, upper-case infix
-    odd = [("0x1p-1", "0", "600", "1", "0", "600", "0", "1", "600"),
-           ("1e-50", "0", "603", "1", "0", "603", "0", "1", "603"),
-           ("0", "0", "606", "0X1.8P1", "0", "606", "0", "1", "606")]
+    zs = ["%d" % (3 * n_panels + 600 + 3 * k) for k in range(3)]
+    odd = [("0x1p-1", "0", zs[0], "1", "0", zs[0], "0", "1", zs[0]),
+           ("1e-50", "0", zs[1], "1", "0", zs[1], "0", "1", zs[1]),
+           ("0", "0", zs[2], "0X1.8P1", "0", zs[2], "0", "1", zs[2])]
     for toks in odd:
         rows.append("T c " + " ".join(toks))
         expect.append([strtof(t) for t in toks])
