@@ -83,3 +83,26 @@ def test_panel_coordinates_match_strtof(tmp_path, seed, n_panels):
     def rows_sorted(x):
         return x[np.lexsort(x.T[::-1])]
     np.testing.assert_array_equal(rows_sorted(got).view(np.uint32), rows_sorted(want).view(np.uint32))
+
+
+def test_crlf_and_tabs_build_the_same_model(tmp_path):
+    """Windows line ends and tab separators are whitespace to the reader, as
+    to sscanf: the same panels with LF, CRLF and tab-separated lines build
+    the same model, array for array."""
+    rng = np.random.default_rng(7)
+    lines = ["0 line ends"]
+    for i in range(60):
+        x0, y0 = rng.uniform(-5, 5, 2)
+        v = [x0, y0, 3.0 * i, x0 + 1.5, y0, 3.0 * i, x0, y0 + 1.25, 3.0 * i]
+        lines.append("T c%d " % (i % 3) + " ".join("%.9g" % t for t in v))
+    models = []
+    for name, text in (("lf", "\n".join(lines) + "\n"), ("crlf", "\r\n".join(lines) + "\r\n"),
+                       ("tabs", "\n".join(l.replace(" ", "\t") for l in lines) + "\n")):
+        path = tmp_path / (name + ".txt")
+        path.write_bytes(text.encode())
+        models.append(fc.Model.build(str(path), mesh_eps=0.2))
+    ref = models[0]
+    for m in models[1:]:
+        assert list(m.names) == list(ref.names)
+        for k, a in ref.arrays.items():
+            np.testing.assert_array_equal(np.asarray(m.arrays[k]), np.asarray(a), err_msg=k)
